@@ -1,0 +1,385 @@
+"""hcc_gb300 — GB300-native explicit right-hand-side path of HyperCloudCore.jl, driven through its C ABI.
+
+Host mirror of the reference's interface for this path (names and argument meaning follow it):
+
+  * physics modules   ``LinearAdvection`` (test/PDEs/linear_advection.jl), ``Euler`` (new), ``KineticRelaxation``
+                      (test/kinetic_source.jl) — the ``HyperbolicPDE`` subtypes compiled into the kernels;
+  * schemes           ``MUSCL(order, div_order)`` (src/Interpolation/MUSCL.jl:116), ``MOOD(strategy, criterion)``
+                      with ``MOODu1`` / ``MOODPAD`` / ``OnlyMOOD`` / ``NoMOOD`` and ``EPD0/EPD1/EPD2``
+                      (src/TimeStepping/MOOD.jl);
+  * stepper           ``GB300RKTimeStepper`` — ``ts(t, dt)`` is ``(ts::GeneralRKTimeStepper)(eq, pg, t, dt)``
+                      (src/TimeStepping/TimeSteppers.jl:531) and ``ts.get_time_step()`` is
+                      ``get_time_step(pg, eq, interp)`` (src/Grid/ParticleGrids.jl:386);
+  * ``Context``       the raw C-ABI handle (include/hcc.h).
+
+All compute runs in libhcc_gb300.so (hand-written sm_103a kernels). There is no CPU fallback: without the
+library or a GPU every call raises ``HCCError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import (HccConfig, HccCounters, FP32, FP64, PDE_ADVECTION, PDE_BGK, PDE_EULER, MOOD_NONE, MOOD_ONLY,
+                   MOOD_PAD, MOOD_U1, EPD_NONE, EPD0, EPD1, EPD2, TABLEAUS, BC_KEEP, BC_DIRICHLET, BC_OUTFLOW)
+from .cloud import Cloud, rectangular_cloud, morton_permutation, splitmix64_uniform
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libhcc_gb300.so"
+
+
+class HCCError(RuntimeError):
+    """A failed C-ABI call (status code + the context's last error message)."""
+
+    def __init__(self, status: int, message: str, call: str = ""):
+        self.status = status
+        name = _abi.STATUS_NAMES[status] if 0 <= status < len(_abi.STATUS_NAMES) else str(status)
+        super().__init__(f"{call}: {name}: {message}" if call else f"{name}: {message}")
+
+
+_LIB: Optional[C.CDLL] = None
+
+
+def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
+    """Load libhcc_gb300.so (built in-tree by build.build()). Raises if it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise HCCError(_abi.HCC_ERR_STATE, f"{p} is missing: run build() first")
+    lib = _abi.bind(C.CDLL(str(p)))
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+# ------------------------------------------------------------------------------------------ descriptors
+@dataclass
+class LinearAdvection:
+    """Diagonal linear advection: F_d(U)_m = c[d][m] U_m. `velocities[d][m]` (one tuple per axis)."""
+    velocities: Sequence[Sequence[float]]
+    pde: int = PDE_ADVECTION
+
+    @property
+    def dim(self) -> int:
+        return len(self.velocities)
+
+    @property
+    def n_vars(self) -> int:
+        return len(self.velocities[0])
+
+
+@dataclass
+class Euler:
+    """Compressible Euler equations of an ideal gas, U = (rho, rho u_1..u_D, E)."""
+    dim: int
+    gamma: float = 1.4
+    pde: int = PDE_EULER
+
+    @property
+    def n_vars(self) -> int:
+        return self.dim + 2
+
+
+@dataclass
+class KineticRelaxation:
+    """Discrete-velocity BGK relaxation: kinetic speeds `speeds[k][d]`, relaxation time `epsilon`, one macro
+    moment u = Σ_k f_k advected with `macro_velocity`, Maxwellian M_k = coefficient (u + Σ_d F_d(u) D / v_k,d)."""
+    speeds: Sequence[Sequence[float]]
+    epsilon: float = 1e-4
+    macro_velocity: Sequence[float] = (1.0, 0.0)
+    coefficient: Optional[float] = None
+    interior_factor: Optional[float] = None
+    pde: int = PDE_BGK
+
+    @property
+    def dim(self) -> int:
+        return len(self.speeds[0])
+
+    @property
+    def n_vars(self) -> int:
+        return len(self.speeds)
+
+
+@dataclass
+class MUSCL:
+    order: int = 2
+    div_order: int = 0
+
+
+@dataclass
+class MOODu1:
+    delta: float
+
+
+class MOODPAD:
+    pass
+
+
+class OnlyMOOD:
+    pass
+
+
+class NoMOOD:
+    pass
+
+
+@dataclass
+class MOOD:
+    strategy: int = EPD1
+    criterion: object = field(default_factory=NoMOOD)
+
+
+def config_defaults() -> HccConfig:
+    """Python twin of hcc_config_defaults (include/hcc.h): the reference's defaults."""
+    cfg = HccConfig()
+    cfg.abi_version = _abi.HCC_ABI_VERSION
+    cfg.dim, cfg.n_vars, cfg.pde, cfg.precision = 2, 1, PDE_ADVECTION, FP64
+    cfg.muscl_order, cfg.div_order = 2, 0
+    cfg.mood_criterion, cfg.mood_strategy = MOOD_U1, EPD1
+    cfg.tableau, cfg.mood_substeps, cfg.max_mood_iterations = TABLEAUS["RK3_SSP"], 1, 64
+    cfg.weight_alpha, cfg.gamma = 1.0, 1.4
+    cfg.bgk_epsilon, cfg.bgk_coefficient, cfg.bgk_interior_factor = 1e-4, 1.0, 2.0
+    for d in range(_abi.HCC_MAX_DIM):
+        cfg.dx[d], cfg.canvas_max[d], cfg.domain_max[d] = 1.0, 1.0, 1.0
+    return cfg
+
+
+def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, tableau: str = "RK3_SSP",
+                precision: str = "fp64", bc_map: Optional[dict] = None, alpha: float = 1.0,
+                mood_substeps: bool = True, max_mood_iterations: int = 64) -> HccConfig:
+    """The hcc_config of a stepper (the arguments of GeneralRKTimeStepper / MUSCL / ParticleGrid)."""
+    scheme = scheme or MUSCL()
+    mood = mood or MOOD()
+    cfg = config_defaults()
+    D = cloud.dim
+    if pde.dim != D:
+        raise HCCError(_abi.HCC_ERR_INVALID, f"physics dimension {pde.dim} != cloud dimension {D}")
+    cfg.dim = D
+    cfg.n_vars = pde.n_vars
+    cfg.pde = pde.pde
+    cfg.precision = FP32 if str(precision).lower() in ("fp32", "f32", "float32") else FP64
+    cfg.muscl_order = scheme.order
+    cfg.div_order = scheme.div_order
+    cfg.tableau = TABLEAUS[tableau] if isinstance(tableau, str) else int(tableau)
+    cfg.mood_substeps = 1 if mood_substeps else 0
+    cfg.max_mood_iterations = max_mood_iterations
+    cfg.mood_strategy = mood.strategy
+    crit = mood.criterion
+    if isinstance(crit, MOODu1):
+        cfg.mood_criterion, cfg.mood_delta = MOOD_U1, float(crit.delta)
+    elif isinstance(crit, MOODPAD):
+        cfg.mood_criterion = MOOD_PAD
+    elif isinstance(crit, OnlyMOOD):
+        cfg.mood_criterion = MOOD_ONLY
+    else:
+        cfg.mood_criterion = MOOD_NONE
+    for d in range(D):
+        cfg.periodic[d] = int(cloud.periodic[d])
+        cfg.dx[d] = cloud.dx[d]
+        cfg.canvas_min[d], cfg.canvas_max[d] = cloud.canvas_min[d], cloud.canvas_max[d]
+        cfg.domain_min[d], cfg.domain_max[d] = cloud.domain_min[d], cloud.domain_max[d]
+    cfg.radius = cloud.radius
+    cfg.weight_alpha = alpha
+    for tag, kind in (bc_map or {}).items():
+        cfg.bc_by_tag[int(tag) - 1] = int(kind)
+    if isinstance(pde, LinearAdvection):
+        for d in range(D):
+            for m in range(pde.n_vars):
+                cfg.velocity[d][m] = float(pde.velocities[d][m])
+    elif isinstance(pde, Euler):
+        cfg.gamma = float(pde.gamma)
+    elif isinstance(pde, KineticRelaxation):
+        for k, v in enumerate(pde.speeds):
+            for d in range(D):
+                cfg.velocity[d][k] = float(v[d])
+        cfg.bgk_epsilon = float(pde.epsilon)
+        for d in range(D):
+            cfg.bgk_macro_velocity[d] = float(pde.macro_velocity[d])
+        cfg.bgk_coefficient = float(pde.coefficient if pde.coefficient is not None else 1.0 / pde.n_vars)
+        cfg.bgk_interior_factor = float(pde.interior_factor if pde.interior_factor is not None else D)
+    return cfg
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Context:
+    """Owner of one hcc_ctx (one CUDA stream, library-owned device memory)."""
+
+    def __init__(self, cfg: HccConfig, capacity: int = 0, lib: Optional[C.CDLL] = None):
+        self.lib = lib or load_library()
+        self.cfg = cfg
+        self.D, self.M = cfg.dim, cfg.n_vars
+        self.f32 = cfg.precision == FP32
+        self._h = C.c_void_p()
+        st = self.lib.hcc_create(C.byref(cfg), int(capacity), C.byref(self._h))
+        if st != 0:
+            msg = self.lib.hcc_last_error(self._h).decode()
+            self.lib.hcc_destroy(self._h)
+            self._h = None
+            raise HCCError(st, msg, "hcc_create")
+        self.n = 0
+
+    # -- plumbing
+    def _check(self, st: int, call: str):
+        if st != 0:
+            raise HCCError(st, self.lib.hcc_last_error(self._h).decode(), call)
+
+    def close(self):
+        if self._h:
+            self.lib.hcc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- cloud and geometry
+    def upload_cloud(self, cloud: Cloud):
+        pos = np.ascontiguousarray(cloud.pos, dtype=np.float64)
+        bnd = np.ascontiguousarray(cloud.is_boundary, dtype=np.uint8)
+        tags = np.ascontiguousarray(cloud.tags, dtype=np.int32)
+        vol = np.ascontiguousarray(cloud.volumes, dtype=np.float64)
+        self._check(self.lib.hcc_upload_cloud(self._h, pos.shape[0], _ptr(pos, C.c_double), _ptr(bnd, C.c_uint8),
+                                              _ptr(tags, C.c_int32), _ptr(vol, C.c_double)), "hcc_upload_cloud")
+        self.n = pos.shape[0]
+
+    def build_neighbours(self):
+        self._check(self.lib.hcc_build_neighbours(self._h), "hcc_build_neighbours")
+
+    def prepare_geometry(self):
+        self._check(self.lib.hcc_prepare_geometry(self._h), "hcc_prepare_geometry")
+
+    def neighbours(self):
+        """(counts, idx, w, dist) in the reference's row-major order."""
+        counts = np.zeros(self.n, dtype=np.int32)
+        self._check(self.lib.hcc_download_neighbours(self._h, _ptr(counts, C.c_int32), None, None, None),
+                    "hcc_download_neighbours")
+        tot = int(counts.sum())
+        idx = np.zeros(tot, dtype=np.int32)
+        w = np.zeros(tot, dtype=np.float64)
+        dist = np.zeros((tot, self.D), dtype=np.float64)
+        self._check(self.lib.hcc_download_neighbours(self._h, None, _ptr(idx, C.c_int32), _ptr(w, C.c_double),
+                                                     _ptr(dist, C.c_double)), "hcc_download_neighbours")
+        return counts, idx, w, dist
+
+    def geometry(self, total: int):
+        dw = np.zeros((total, self.D), dtype=np.float64)
+        okr = np.zeros(self.n, dtype=np.uint8)
+        okd = np.zeros(self.n, dtype=np.uint8)
+        self._check(self.lib.hcc_download_geometry(self._h, _ptr(dw, C.c_double), _ptr(okr, C.c_uint8),
+                                                   _ptr(okd, C.c_uint8)), "hcc_download_geometry")
+        return dw, okr, okd
+
+    # -- state
+    def upload_state(self, U: np.ndarray):
+        if U.dtype == np.float32:
+            a = np.ascontiguousarray(U, dtype=np.float32)
+            self._check(self.lib.hcc_upload_state_f32(self._h, _ptr(a, C.c_float)), "hcc_upload_state_f32")
+        else:
+            a = np.ascontiguousarray(U, dtype=np.float64)
+            self._check(self.lib.hcc_upload_state(self._h, _ptr(a, C.c_double)), "hcc_upload_state")
+
+    def download_state(self, dtype=np.float64) -> np.ndarray:
+        out = np.zeros((self.n, self.M), dtype=dtype)
+        if dtype == np.float32:
+            self._check(self.lib.hcc_download_state_f32(self._h, _ptr(out, C.c_float)), "hcc_download_state_f32")
+        else:
+            self._check(self.lib.hcc_download_state(self._h, _ptr(out, C.c_double)), "hcc_download_state")
+        return out
+
+    def time_step(self) -> float:
+        dt = C.c_double()
+        self._check(self.lib.hcc_time_step(self._h, C.byref(dt)), "hcc_time_step")
+        return dt.value
+
+    def compute_rhs(self) -> np.ndarray:
+        K = np.zeros((self.n, self.M), dtype=np.float64)
+        self._check(self.lib.hcc_compute_rhs(self._h, _ptr(K, C.c_double)), "hcc_compute_rhs")
+        return K
+
+    def step(self, t: float, dt: float):
+        self._check(self.lib.hcc_step(self._h, float(t), float(dt)), "hcc_step")
+
+    def orders(self) -> np.ndarray:
+        o = np.zeros(self.n, dtype=np.int32)
+        self._check(self.lib.hcc_download_orders(self._h, _ptr(o, C.c_int32)), "hcc_download_orders")
+        return o
+
+    def mood_flags(self) -> np.ndarray:
+        f = np.zeros(self.n, dtype=np.uint8)
+        self._check(self.lib.hcc_download_mood_flags(self._h, _ptr(f, C.c_uint8)), "hcc_download_mood_flags")
+        return f
+
+    def counters(self) -> dict:
+        c = HccCounters()
+        self._check(self.lib.hcc_get_counters(self._h, C.byref(c)), "hcc_get_counters")
+        return c.as_dict()
+
+    def total_mass(self) -> np.ndarray:
+        out = np.zeros(self.M, dtype=np.float64)
+        self._check(self.lib.hcc_total_mass(self._h, _ptr(out, C.c_double)), "hcc_total_mass")
+        return out
+
+    def synchronize(self):
+        self._check(self.lib.hcc_synchronize(self._h), "hcc_synchronize")
+
+    def stream(self) -> int:
+        return int(self.lib.hcc_stream(self._h) or 0)
+
+
+class GB300RKTimeStepper:
+    """The GB300 counterpart of GeneralRKTimeStepper(pde, MUSCL(...), MOOD(...), tableau) on a fixed cloud.
+
+    ``ts(t, dt)`` advances the state one step; ``ts.get_time_step()`` is the CFL step at CFL number 1."""
+
+    def __init__(self, pde, cloud: Cloud, scheme: MUSCL = None, mood: MOOD = None, tableau: str = "RK3_SSP",
+                 precision: str = "fp64", bc_map: Optional[dict] = None, **kw):
+        self.pde, self.cloud = pde, cloud
+        self.cfg = make_config(pde, cloud, scheme=scheme, mood=mood, tableau=tableau, precision=precision,
+                               bc_map=bc_map, **kw)
+        self.ctx = Context(self.cfg)
+        self.ctx.upload_cloud(cloud)
+        self.ctx.build_neighbours()
+        self.ctx.prepare_geometry()
+
+    def set_state(self, U: np.ndarray):
+        self.ctx.upload_state(U)
+
+    def state(self) -> np.ndarray:
+        return self.ctx.download_state()
+
+    def get_time_step(self) -> float:
+        return self.ctx.time_step()
+
+    def __call__(self, t: float, dt: float):
+        self.ctx.step(t, dt)
+
+    def mood_flags(self) -> np.ndarray:
+        return self.ctx.mood_flags()
+
+    def particle_orders(self) -> np.ndarray:
+        return self.ctx.orders()
+
+
+__all__ = [
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "MOOD", "MOODu1",
+    "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
+    "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
+    "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",
+]

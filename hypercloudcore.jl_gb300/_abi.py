@@ -1,0 +1,101 @@
+"""ctypes mirror of include/hcc.h (structures, enums and prototypes)."""
+from __future__ import annotations
+
+import ctypes as C
+
+HCC_ABI_VERSION = 1
+HCC_MAX_DIM = 3
+HCC_MAX_VARS = 16
+HCC_MAX_TAGS = 16
+
+# hcc_status
+HCC_OK, HCC_ERR_INVALID, HCC_ERR_CAPACITY, HCC_ERR_CUDA, HCC_ERR_STATE, HCC_ERR_NONFINITE, HCC_ERR_TIMEOUT, \
+    HCC_ERR_UNSUPPORTED = range(8)
+STATUS_NAMES = ["HCC_OK", "HCC_ERR_INVALID", "HCC_ERR_CAPACITY", "HCC_ERR_CUDA", "HCC_ERR_STATE",
+                "HCC_ERR_NONFINITE", "HCC_ERR_TIMEOUT", "HCC_ERR_UNSUPPORTED"]
+# hcc_pde_kind
+PDE_ADVECTION, PDE_EULER, PDE_BGK = 0, 1, 2
+# hcc_precision
+FP64, FP32 = 0, 1
+# hcc_mood_criterion
+MOOD_NONE, MOOD_U1, MOOD_PAD, MOOD_ONLY = 0, 1, 2, 3
+# hcc_mood_strategy
+EPD_NONE, EPD0, EPD1, EPD2 = 0, 1, 2, 3
+# hcc_tableau
+TABLEAUS = {
+    "RK1_Euler": 0, "RK2_SSP": 1, "RK2_Ralston": 2, "RK3_SSP": 3, "RK4_Classical": 4, "RK4_SSP": 5,
+    "IMEX_Euler": 6, "IMEX_ARS233": 7, "IMEX_ARS222": 8, "IMEX_PRSSP3": 9, "IMEX_SSP2332": 10,
+}
+# hcc_bc_kind
+BC_KEEP, BC_DIRICHLET, BC_OUTFLOW = 0, 1, 2
+
+
+class HccConfig(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32), ("dim", C.c_int32), ("n_vars", C.c_int32), ("pde", C.c_int32),
+        ("precision", C.c_int32), ("muscl_order", C.c_int32), ("div_order", C.c_int32),
+        ("mood_criterion", C.c_int32), ("mood_strategy", C.c_int32), ("tableau", C.c_int32),
+        ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
+        ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
+        ("reserved_i", C.c_int32 * 8),
+        ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
+        ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
+        ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),
+        ("mood_delta", C.c_double), ("velocity", (C.c_double * HCC_MAX_VARS) * HCC_MAX_DIM),
+        ("gamma", C.c_double), ("bgk_epsilon", C.c_double), ("bgk_macro_velocity", C.c_double * HCC_MAX_DIM),
+        ("bgk_coefficient", C.c_double), ("bgk_interior_factor", C.c_double), ("reserved_d", C.c_double * 8),
+    ]
+
+
+class HccCounters(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_int64), ("n_interior", C.c_int64), ("max_neighbours", C.c_int32),
+        ("min_neighbours_interior", C.c_int32), ("total_neighbours", C.c_int64), ("mood_iterations", C.c_int64),
+        ("mood_flagged", C.c_int64), ("inadmissible", C.c_int64), ("kernel_launches", C.c_int64),
+        ("steps", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+P = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_u8p = C.POINTER(C.c_uint8)
+
+# (name, restype, argtypes) of every entry point of include/hcc.h
+PROTOTYPES = [
+    ("hcc_config_defaults", None, [C.POINTER(HccConfig)]),
+    ("hcc_create", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.POINTER(P)]),
+    ("hcc_destroy", C.c_int, [P]),
+    ("hcc_last_error", C.c_char_p, [P]),
+    ("hcc_status_string", C.c_char_p, [C.c_int]),
+    ("hcc_upload_cloud", C.c_int, [P, C.c_int64, _dp, _u8p, _i32p, _dp]),
+    ("hcc_build_neighbours", C.c_int, [P]),
+    ("hcc_download_neighbours", C.c_int, [P, _i32p, _i32p, _dp, _dp]),
+    ("hcc_prepare_geometry", C.c_int, [P]),
+    ("hcc_download_geometry", C.c_int, [P, _dp, _u8p, _u8p]),
+    ("hcc_upload_state", C.c_int, [P, _dp]),
+    ("hcc_download_state", C.c_int, [P, _dp]),
+    ("hcc_upload_state_f32", C.c_int, [P, _fp]),
+    ("hcc_download_state_f32", C.c_int, [P, _fp]),
+    ("hcc_time_step", C.c_int, [P, _dp]),
+    ("hcc_compute_rhs", C.c_int, [P, _dp]),
+    ("hcc_step", C.c_int, [P, C.c_double, C.c_double]),
+    ("hcc_download_orders", C.c_int, [P, _i32p]),
+    ("hcc_download_mood_flags", C.c_int, [P, _u8p]),
+    ("hcc_get_counters", C.c_int, [P, C.POINTER(HccCounters)]),
+    ("hcc_total_mass", C.c_int, [P, _dp]),
+    ("hcc_synchronize", C.c_int, [P]),
+    ("hcc_stream", P, [P]),
+]
+
+
+def bind(lib: C.CDLL, prototypes=PROTOTYPES) -> C.CDLL:
+    for name, res, args in prototypes:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib

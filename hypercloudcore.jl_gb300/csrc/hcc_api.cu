@@ -1,0 +1,1021 @@
+// hcc_api.cu — the C ABI (include/hcc.h): context lifecycle, device buffers and the host orchestration of one
+// time step (the GeneralRKTimeStepper functor, src/TimeStepping/TimeSteppers.jl:531-577) on one CUDA stream.
+#include "hcc_internal.cuh"
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+
+using namespace hcc;
+
+namespace {
+
+// ----------------------------------------------------------------------------------- tableaus
+// The built-in Butcher tableaus of src/TimeStepping/ButcherTableaus.jl (explicit part a_t, b_t, c_t; implicit
+// part a, b, c), stored as plain data.
+struct Tableau {
+    int s = 0;
+    double a[5][5]{}, at[5][5]{}, c[5]{}, ct[5]{}, b[5]{}, bt[5]{};
+};
+
+Tableau make_tableau(int id) {
+    Tableau t;
+    auto expl = [&](int s, std::initializer_list<double> A, std::initializer_list<double> bb,
+                    std::initializer_list<double> cc) {
+        t.s = s;
+        int k = 0;
+        for (double v : A) { t.at[k / s][k % s] = v; ++k; }
+        k = 0; for (double v : bb) t.bt[k++] = v;
+        k = 0; for (double v : cc) { t.c[k] = v; t.ct[k] = v; ++k; }
+    };
+    const double g2 = 1.0 - 1.0 / std::sqrt(2.0);
+    switch (id) {
+    case HCC_TAB_RK1_EULER: expl(1, {0.0}, {1.0}, {0.0}); break;
+    case HCC_TAB_RK2_SSP: expl(2, {0, 0, 1.0, 0}, {0.5, 0.5}, {0.0, 1.0}); break;
+    case HCC_TAB_RK2_RALSTON: expl(2, {0, 0, 2.0 / 3, 0}, {0.25, 0.75}, {0.0, 2.0 / 3}); break;
+    case HCC_TAB_RK3_SSP: expl(3, {0, 0, 0, 1.0, 0, 0, 0.25, 0.25, 0}, {1.0 / 6, 1.0 / 6, 2.0 / 3}, {0.0, 1.0, 0.5}); break;
+    case HCC_TAB_RK4_CLASSICAL:
+        expl(4, {0, 0, 0, 0, 0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1.0, 0}, {1.0 / 6, 1.0 / 3, 1.0 / 3, 1.0 / 6},
+             {0.0, 0.5, 0.5, 1.0});
+        break;
+    case HCC_TAB_RK4_SSP:   // Spiteri & Ruuth SSPRK(5,4)
+        expl(5,
+             {0, 0, 0, 0, 0, 0.39175222657189002, 0, 0, 0, 0, 0.21766909626116876, 0.36841059305037099, 0, 0, 0,
+              0.082692086657810582, 0.13995850219189535, 0.25189177427169401, 0, 0, 0.067966283637114752,
+              0.11503469850463156, 0.20703489859738566, 0.54497475022852104, 0},
+             {0.14681187608478657, 0.24848290944497617, 0.10425883033198098, 0.2744389009013507, 0.226007483236906},
+             {0.0, 0.39175222657189002, 0.58607968931153975, 0.47454236312139997, 0.93501063096765302});
+        break;
+    case HCC_TAB_IMEX_EULER:
+        t.s = 2; t.at[1][0] = 1; t.a[1][1] = 1; t.c[1] = 1; t.ct[1] = 1; t.b[1] = 1; t.bt[0] = 1;
+        break;
+    case HCC_TAB_IMEX_ARS233: {
+        double g = (3.0 + std::sqrt(3.0)) / 6.0;
+        t.s = 3;
+        t.a[1][1] = g; t.a[2][1] = 1.0 - 2 * g; t.a[2][2] = g;
+        t.at[1][0] = g; t.at[2][0] = g - 1.0; t.at[2][1] = 2.0 * (1 - g);
+        t.c[1] = g; t.c[2] = 1.0 - g;
+        for (int i = 0; i < 3; ++i) t.ct[i] = t.c[i];
+        t.b[1] = 0.5; t.b[2] = 0.5;
+        for (int i = 0; i < 3; ++i) t.bt[i] = t.b[i];
+        break;
+    }
+    case HCC_TAB_IMEX_ARS222: {
+        double g = g2, dl = 1 - 1 / (2 * g);
+        t.s = 3;
+        t.a[1][1] = g; t.a[2][1] = 1 - g; t.a[2][2] = g;
+        t.at[1][0] = g; t.at[2][0] = dl; t.at[2][1] = 1 - dl;
+        t.c[1] = g; t.c[2] = 1;
+        for (int i = 0; i < 3; ++i) t.ct[i] = t.c[i];
+        t.b[1] = 1 - g; t.b[2] = g;
+        t.bt[0] = dl; t.bt[1] = 1 - dl;
+        break;
+    }
+    case HCC_TAB_IMEX_PRSSP3: {
+        double g = g2;
+        t.s = 3;
+        t.at[1][0] = 1; t.at[2][0] = 0.25; t.at[2][1] = 0.25;
+        t.a[0][0] = g; t.a[1][0] = 1 - 2 * g; t.a[1][1] = g; t.a[2][0] = 0.5 - g; t.a[2][2] = g;
+        t.b[0] = 1.0 / 6; t.b[1] = 1.0 / 6; t.b[2] = 2.0 / 3;
+        for (int i = 0; i < 3; ++i) t.bt[i] = t.b[i];
+        t.c[0] = g; t.c[1] = 1 - g; t.c[2] = 0.5;
+        t.ct[1] = 1; t.ct[2] = 0.5;
+        break;
+    }
+    case HCC_TAB_IMEX_SSP2332:
+        t.s = 3;
+        t.a[0][0] = 0.25; t.a[1][1] = 0.25; t.a[2][0] = 1.0 / 3; t.a[2][1] = 1.0 / 3; t.a[2][2] = 1.0 / 3;
+        t.at[1][0] = 0.5; t.at[2][0] = 0.5; t.at[2][1] = 0.5;
+        t.b[0] = t.b[1] = t.b[2] = 1.0 / 3;
+        for (int i = 0; i < 3; ++i) t.bt[i] = t.b[i];
+        t.c[0] = 0.25; t.c[1] = 0.25; t.c[2] = 1.0;
+        t.ct[1] = 0.5; t.ct[2] = 1.0;
+        break;
+    default: t.s = 0;
+    }
+    return t;
+}
+
+// ssp_coefficient (ButcherTableaus.jl:86-118): bisection on r for non-negative canonical Shu–Osher
+// coefficients alpha = rK (I + rK)^-1, v = (I - alpha) 1 (tolerance -1e-13); 0 for tableaus with an implicit part.
+double ssp_coefficient(const Tableau &t) {
+    for (int i = 0; i < t.s; ++i)
+        for (int j = 0; j < t.s; ++j)
+            if (t.a[i][j] != 0.0) return 0.0;
+    const int s = t.s, n = s + 1;
+    double K[6][6] = {};
+    for (int i = 0; i < s; ++i) for (int j = 0; j < s; ++j) K[i][j] = t.at[i][j];
+    for (int j = 0; j < s; ++j) K[s][j] = t.bt[j];
+    auto ok = [&](double r) {
+        double A[6][6], Inv[6][6];
+        for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) A[i][j] = (i == j ? 1.0 : 0.0) + r * K[i][j];
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                double v = (i == j) ? 1.0 : 0.0;
+                for (int k = 0; k < i; ++k) v -= A[i][k] * Inv[k][j];
+                Inv[i][j] = v / A[i][i];
+            }
+        double al[6][6];
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                double v = 0.0;
+                for (int k = 0; k < n; ++k) v += r * K[i][k] * Inv[k][j];
+                al[i][j] = v;
+                if (v < -1e-13) return false;
+            }
+        for (int i = 0; i < n; ++i) {
+            double v = 0.0;
+            for (int j = 0; j < n; ++j) v += (i == j ? 1.0 : 0.0) - al[i][j];
+            if (v < -1e-13) return false;
+        }
+        return true;
+    };
+    double lo = 1e-3, hi = 1e-3;
+    if (!ok(lo)) return 0.0;
+    while (ok(hi) && hi < 1e3) hi *= 2;
+    lo = hi / 2;
+    for (int it = 0; it < 60; ++it) {
+        double mid = (lo + hi) / 2;
+        if (ok(mid)) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+bool has_implicit_part(const Tableau &t) {
+    for (int i = 0; i < t.s; ++i) {
+        if (t.b[i] != 0.0) return true;
+        for (int j = 0; j < t.s; ++j) if (t.a[i][j] != 0.0) return true;
+    }
+    return false;
+}
+
+const char *kStatusNames[] = {"HCC_OK", "HCC_ERR_INVALID", "HCC_ERR_CAPACITY", "HCC_ERR_CUDA", "HCC_ERR_STATE",
+                              "HCC_ERR_NONFINITE", "HCC_ERR_TIMEOUT", "HCC_ERR_UNSUPPORTED"};
+
+template <typename P> void dfree(P *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct hcc_ctx {
+    hcc_config cfg{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int D = 2, M = 1, f32 = 0;
+    int64_t capacity = 0, n = 0, npad = 0, n_interior = 0;
+    int kmax = 0;
+    int64_t total_nb = 0;
+    const StageOps *ops = nullptr;
+    // scheme
+    int max_order = 2, DO = 0, rdeg = 1, Br = 1, full_div = 2, ddeg = 1, Bd = 2, need_dw1 = 0;
+    double invL = 1.0;
+    Tableau tab;
+    double ssp_C = 0.0, ratio = 0.0;
+    int has_source = 0;
+    // cloud
+    double *pos = nullptr; uint8_t *bnd = nullptr; int32_t *tags = nullptr; double *vol = nullptr;
+    std::vector<uint8_t> h_bnd; std::vector<int32_t> h_tags;
+    // cell list
+    int dims[3] = {1, 1, 1}; double csize[3] = {1, 1, 1};
+    int64_t nbins = 0; int noff = 1;
+    int64_t *binnb = nullptr; int32_t *bin_of = nullptr, *cell_count = nullptr, *cell_cursor = nullptr, *cellp = nullptr;
+    int64_t *cell_start = nullptr; int32_t *cnt = nullptr;
+    // neighbours (FP64 master copy, slot-major)
+    int32_t *nidx = nullptr; double *w64 = nullptr, *dist64 = nullptr;
+    // geometry
+    double *inv_r64 = nullptr, *inv_d64 = nullptr, *dw64 = nullptr, *dw1_64 = nullptr;
+    uint8_t *ok_r = nullptr, *ok_d = nullptr, *ok_1 = nullptr;
+    float *dist32 = nullptr, *w32 = nullptr, *dw32 = nullptr, *dw1_32 = nullptr, *inv_r32 = nullptr;
+    int32_t *status = nullptr, *status2 = nullptr, *root = nullptr;
+    int32_t *blist = nullptr, *bsrc = nullptr; int64_t nbnd = 0;
+    // state (element type double or float)
+    void *rhos = nullptr, *cand = nullptr, *grad = nullptr;
+    void *Y[HCC_MAX_STAGES] = {}, *KE[HCC_MAX_STAGES] = {}, *KI[HCC_MAX_STAGES] = {};
+    int8_t *orders = nullptr, *nbmin = nullptr;
+    uint8_t *triggered = nullptr, *changed = nullptr, *dirty = nullptr, *scratch = nullptr, *trig_step = nullptr,
+            *inadm = nullptr;
+    unsigned long long *d_counters = nullptr;   // [0..1] drop counters, [2] dt bits, [3..4] search stats
+    unsigned long long *h_counters = nullptr;   // pinned mirror
+    double *d_mass = nullptr;
+    bool have_cloud = false, have_nb = false, have_geom = false, have_state = false;
+    // statistics
+    int64_t launches = 0, mood_iters = 0, flagged = 0, inadmissible = 0, steps = 0;
+
+    size_t esz() const { return f32 ? sizeof(float) : sizeof(double); }
+
+    hcc_status fail(hcc_status st, const std::string &msg) {
+        err = msg;
+        return st;
+    }
+    hcc_status cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return HCC_OK;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return HCC_ERR_CUDA;
+    }
+    template <typename P> hcc_status alloc(P *&p, size_t count, const char *what) {
+        dfree(p);
+        if (count == 0) count = 1;
+        return cuda(cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(P)), what);
+    }
+    hcc_status valloc(void *&p, size_t bytes, const char *what) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        return cuda(cudaMalloc(&p, bytes ? bytes : 1), what);
+    }
+    hcc_status sync(const char *what) { return cuda(cudaStreamSynchronize(stream), what); }
+
+    void free_particles() {
+        dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
+        dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
+        dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
+        for (void **p : {&rhos, &cand, &grad}) { if (*p) cudaFree(*p); *p = nullptr; }
+        for (int s = 0; s < HCC_MAX_STAGES; ++s)
+            for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
+        dfree(orders); dfree(nbmin); dfree(triggered); dfree(changed); dfree(dirty); dfree(scratch); dfree(trig_step);
+        dfree(inadm);
+    }
+    void free_slots() {
+        dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
+        dfree(dw1_32);
+    }
+    void free_bins() { dfree(binnb); dfree(cell_count); dfree(cell_cursor); dfree(cell_start); }
+};
+
+namespace {
+
+const char *g_null_ctx_error = "null context";
+
+// ------------------------------------------------------------------ argument assembly
+template <typename T> PhysParams<T> phys_params(const hcc_ctx *c) {
+    PhysParams<T> p{};
+    const hcc_config &f = c->cfg;
+    for (int d = 0; d < c->D; ++d) {
+        double am = 0.0;
+        for (int m = 0; m < c->M; ++m) {
+            p.c[d][m] = T(f.velocity[d][m]);
+            am = std::max(am, std::fabs(f.velocity[d][m]));
+        }
+        p.amax[d] = T(am);
+        p.a_macro[d] = T(f.bgk_macro_velocity[d]);
+    }
+    p.gamma = T(f.gamma);
+    p.gm1 = T(f.gamma - 1.0);
+    if (f.pde == HCC_PDE_BGK) {
+        p.inv_eps = T(1.0 / f.bgk_epsilon);
+        p.coeff = T(f.bgk_coefficient);
+        double fac = f.bgk_interior_factor;
+        for (int k = 0; k < c->M; ++k)
+            for (int d = 0; d < c->D; ++d) {
+                double v = f.velocity[d][k];
+                p.sinv[k][d] = T(std::fabs(v) > 1e-14 ? fac / v : 0.0);
+            }
+    }
+    return p;
+}
+
+template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
+    StageArgs<T> a{};
+    Geometry<T> &g = a.g;
+    g.n = c->n;
+    g.npad = c->npad;
+    g.cnt = c->cnt;
+    g.nidx = c->nidx;
+    if constexpr (sizeof(T) == 8) {
+        g.dist = c->dist64; g.wt = c->w64; g.dw = c->dw64; g.dw1 = c->need_dw1 ? c->dw1_64 : nullptr;
+        g.inv_r = c->inv_r64;
+    } else {
+        g.dist = c->dist32; g.wt = c->w32; g.dw = c->dw32; g.dw1 = c->need_dw1 ? c->dw1_32 : nullptr;
+        g.inv_r = c->inv_r32;
+    }
+    g.ok_r = c->ok_r; g.ok_d = c->ok_d; g.ok_1 = c->ok_1;
+    g.bnd = c->bnd;
+    g.invL = T(c->invL);
+    a.ph = phys_params<T>(c);
+    a.sc.max_order = c->max_order;
+    a.sc.DO = c->DO;
+    a.sc.strategy = c->cfg.mood_strategy;
+    a.sc.criterion = c->cfg.mood_criterion;
+    a.sc.has_source = c->has_source;
+    a.orders = c->orders;
+    a.nbmin = c->nbmin;
+    a.grad = static_cast<T *>(c->grad);
+    a.triggered = c->triggered;
+    a.inadm = c->inadm;
+    a.delta = T(c->cfg.mood_delta);
+    return a;
+}
+
+template <typename T> hcc_status run_step(hcc_ctx *c, double dt);
+template <typename T> hcc_status run_rhs(hcc_ctx *c);
+template <typename T> hcc_status run_cfl(hcc_ctx *c, double *dt_out);
+
+hcc_status launch_check(hcc_ctx *c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return c->cuda(e, what);
+    return HCC_OK;
+}
+
+hcc_status read_counters(hcc_ctx *c, int count) {
+    hcc_status st = c->cuda(cudaMemcpyAsync(c->h_counters, c->d_counters, sizeof(unsigned long long) * count,
+                                            cudaMemcpyDeviceToHost, c->stream), "counter copy");
+    if (st != HCC_OK) return st;
+    return c->sync("counter sync");
+}
+
+// Implicit-part mode of the candidate of stage `i` (0-based): 1 solve, 2 explicit source evaluation, 0 none.
+int implicit_mode(const hcc_ctx *c, int i) {
+    if (!c->has_source) return 0;
+    return std::fabs(c->tab.a[i][i]) > 1e-14 ? 1 : 2;
+}
+
+template <typename T> void apply_bcs(hcc_ctx *c, void *Y) {
+    launch_bc_apply(Y, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, c->stream);
+    c->launches += c->nbnd > 0;
+}
+
+// The MOOD fixed point of one checkpoint (mood_checkpoint!, TimeSteppers.jl:454-477) after its full flux pass.
+template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
+    const int64_t n = c->n;
+    const int reach = (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
+    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
+    for (int it = 0;; ++it) {
+        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, n, c->d_counters, c->stream);
+        c->launches += 1;
+        hcc_status st = read_counters(c, 2);
+        if (st != HCC_OK) return st;
+        const unsigned long long changed = c->h_counters[0];
+        if (changed == 0) {
+            c->inadmissible += int64_t(c->h_counters[1]);
+            return HCC_OK;
+        }
+        c->flagged += int64_t(changed);
+        if (it >= cap) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
+        ++c->mood_iters;
+        // dirty = changed ⊕ reach hops (expand_mask!, MOOD.jl:343-351)
+        if (reach == 1) {
+            launch_expand(c->changed, c->dirty, c->cnt, c->nidx, n, c->npad, c->stream);
+        } else {
+            launch_expand(c->changed, c->scratch, c->cnt, c->nidx, n, c->npad, c->stream);
+            launch_expand(c->scratch, c->dirty, c->cnt, c->nidx, n, c->npad, c->stream);
+        }
+        c->launches += reach;
+        StageArgs<T> ga = a;
+        ga.full = 0;
+        ga.mask = c->changed;
+        c->ops->gather(&ga, n, c->stream);
+        if (c->cfg.mood_strategy == HCC_EPD2) {
+            launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
+            c->launches += 1;
+        }
+        StageArgs<T> fa = a;
+        fa.full = 0;
+        fa.mask = c->dirty;
+        c->ops->flux(&fa, n, c->stream);
+        apply_bcs<T>(c, fa.Ynext);
+        c->launches += 2;
+        if ((st = launch_check(c, "MOOD recompute")) != HCC_OK) return st;
+    }
+}
+
+template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
+    const int64_t n = c->n;
+    const int S = c->tab.s;
+    c->launches = 0;
+    c->mood_iters = 0;
+    c->flagged = 0;
+    c->inadmissible = 0;
+    launch_fill_i8(c->orders, int8_t(c->max_order), n, c->stream);
+    cudaMemsetAsync(c->trig_step, 0, n, c->stream);
+    c->launches += 1;
+    StageArgs<T> base = base_args<T>(c);
+    base.Un = static_cast<const T *>(c->rhos);
+    for (int s = 0; s < S; ++s) {
+        base.KE[s] = static_cast<const T *>(c->KE[s]);
+        base.KI[s] = static_cast<const T *>(c->KI[s]);
+    }
+    // stage 1: form_candidate!(ts, eq, pg, 1, dt, t)
+    {
+        StageArgs<T> a = base;
+        a.Ynext = static_cast<T *>(c->Y[0]);
+        a.KInext = static_cast<T *>(c->KI[0]);
+        a.implicit_mode = implicit_mode(c, 0);
+        a.dt_ii = T(dt * c->tab.a[0][0]);
+        a.inv_dt_ii = T(a.implicit_mode == 1 ? 1.0 / (dt * c->tab.a[0][0]) : 0.0);
+        c->ops->stage1(&a, n, c->stream);
+        apply_bcs<T>(c, c->Y[0]);
+        c->launches += 1;
+    }
+    const bool check = c->cfg.mood_criterion != HCC_MOOD_NONE;
+    for (int s = 0; s < S; ++s) {
+        StageArgs<T> a = base;
+        a.U = static_cast<const T *>(c->Y[s]);
+        a.K = static_cast<T *>(c->KE[s]);
+        a.full = 1;
+        a.mask = nullptr;
+        a.form_next = 1;
+        const bool fin = (s + 1 == S);
+        a.n_prev = s + 1;
+        a.self_slot = s;
+        for (int j = 0; j <= s; ++j) {
+            const double at = fin ? c->tab.bt[j] : c->tab.at[s + 1][j];
+            const double ai = fin ? c->tab.b[j] : c->tab.a[s + 1][j];
+            a.hE[j] = at != 0.0 ? T(dt * at) : T(0);
+            a.hI[j] = (ai != 0.0 && c->has_source) ? T(dt * ai) : T(0);
+        }
+        a.Ynext = static_cast<T *>(fin ? c->cand : c->Y[s + 1]);
+        if (!fin) {
+            a.KInext = static_cast<T *>(c->KI[s + 1]);
+            a.implicit_mode = implicit_mode(c, s + 1);
+            a.dt_ii = T(dt * c->tab.a[s + 1][s + 1]);
+            a.inv_dt_ii = T(a.implicit_mode == 1 ? 1.0 / (dt * c->tab.a[s + 1][s + 1]) : 0.0);
+        }
+        a.check = check;
+        a.check_substep = c->ratio > 0.0;
+        a.h_sub = T(c->ratio * dt);
+        a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
+        c->ops->gather(&a, n, c->stream);
+        c->launches += 1;
+        if (c->cfg.mood_strategy == HCC_EPD2) {
+            launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
+            c->launches += 1;
+        }
+        c->ops->flux(&a, n, c->stream);
+        c->launches += 1;
+        apply_bcs<T>(c, a.Ynext);
+        hcc_status st = launch_check(c, "stage kernels");
+        if (st != HCC_OK) return st;
+        if (check && (st = mood_fixed_point<T>(c, a)) != HCC_OK) return st;
+    }
+    std::swap(c->rhos, c->cand);
+    ++c->steps;
+    return c->sync("step");
+}
+
+template <typename T> hcc_status run_rhs(hcc_ctx *c) {
+    const int64_t n = c->n;
+    launch_fill_i8(c->orders, int8_t(c->max_order), n, c->stream);
+    StageArgs<T> a = base_args<T>(c);
+    a.U = static_cast<const T *>(c->rhos);
+    a.K = static_cast<T *>(c->KE[0]);
+    a.full = 1;
+    c->ops->gather(&a, n, c->stream);
+    if (c->cfg.mood_strategy == HCC_EPD2) launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
+    c->ops->flux(&a, n, c->stream);
+    hcc_status st = launch_check(c, "rhs kernels");
+    if (st != HCC_OK) return st;
+    return c->sync("rhs");
+}
+
+template <typename T> hcc_status run_cfl(hcc_ctx *c, double *dt_out) {
+    StageArgs<T> a = base_args<T>(c);
+    a.U = static_cast<const T *>(c->rhos);
+    const unsigned long long inf_bits = 0x7ff0000000000000ull;
+    hcc_status st = c->cuda(cudaMemcpyAsync(c->d_counters + 2, &inf_bits, sizeof(inf_bits), cudaMemcpyHostToDevice,
+                                            c->stream), "dt init");
+    if (st != HCC_OK) return st;
+    c->ops->cfl(&a, c->n, c->d_counters + 2, c->stream);
+    c->launches = 1;
+    if ((st = launch_check(c, "cfl kernel")) != HCC_OK) return st;
+    st = c->cuda(cudaMemcpyAsync(c->h_counters + 2, c->d_counters + 2, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, c->stream), "dt copy");
+    if (st != HCC_OK) return st;
+    if ((st = c->sync("cfl")) != HCC_OK) return st;
+    double v;
+    std::memcpy(&v, &c->h_counters[2], sizeof(v));
+    *dt_out = v;
+    return HCC_OK;
+}
+
+const StageOps *find_ops(const hcc_config &f, int rdeg) {
+    if (f.precision == HCC_FP32)
+        return rdeg == 1 ? stage_ops_f32_r1(f.dim, f.n_vars, f.pde) : stage_ops_f32_r2(f.dim, f.n_vars, f.pde);
+    return rdeg == 1 ? stage_ops_f64_r1(f.dim, f.n_vars, f.pde) : stage_ops_f64_r2(f.dim, f.n_vars, f.pde);
+}
+
+}  // namespace
+
+extern "C" {
+
+void hcc_config_defaults(hcc_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->abi_version = HCC_ABI_VERSION;
+    cfg->dim = 2;
+    cfg->n_vars = 1;
+    cfg->pde = HCC_PDE_ADVECTION;
+    cfg->precision = HCC_FP64;
+    cfg->muscl_order = 2;
+    cfg->div_order = 0;
+    cfg->mood_criterion = HCC_MOOD_U1;
+    cfg->mood_strategy = HCC_EPD1;
+    cfg->tableau = HCC_TAB_RK3_SSP;
+    cfg->mood_substeps = 1;
+    cfg->max_mood_iterations = 64;
+    cfg->weight_alpha = 1.0;
+    cfg->gamma = 1.4;
+    cfg->bgk_epsilon = 1e-4;
+    cfg->bgk_coefficient = 1.0;
+    cfg->bgk_interior_factor = 2.0;
+    for (int d = 0; d < HCC_MAX_DIM; ++d) { cfg->dx[d] = 1.0; cfg->canvas_max[d] = 1.0; cfg->domain_max[d] = 1.0; }
+}
+
+const char *hcc_status_string(hcc_status s) {
+    int k = int(s);
+    return (k >= 0 && k < 8) ? kStatusNames[k] : "HCC_UNKNOWN";
+}
+
+const char *hcc_last_error(const hcc_ctx *ctx) { return ctx ? ctx->err.c_str() : g_null_ctx_error; }
+
+hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
+    if (!cfg || !out) return HCC_ERR_INVALID;
+    *out = nullptr;
+    hcc_ctx *c = new (std::nothrow) hcc_ctx();
+    if (!c) return HCC_ERR_INVALID;
+    *out = c;
+    c->cfg = *cfg;
+    const hcc_config &f = c->cfg;
+    if (f.abi_version != HCC_ABI_VERSION) return c->fail(HCC_ERR_INVALID, "abi_version mismatch");
+    c->D = f.dim;
+    c->M = f.n_vars;
+    c->f32 = f.precision == HCC_FP32;
+    c->capacity = capacity;
+    if (c->D < 1 || c->D > 3) return c->fail(HCC_ERR_INVALID, "dim must be 1, 2 or 3");
+    if (c->M < 1 || c->M > HCC_MAX_VARS) return c->fail(HCC_ERR_INVALID, "n_vars out of range");
+    if (f.pde == HCC_PDE_EULER && c->M != c->D + 2) return c->fail(HCC_ERR_INVALID, "Euler needs n_vars = dim + 2");
+    if (f.precision != HCC_FP64 && f.precision != HCC_FP32) return c->fail(HCC_ERR_INVALID, "unknown precision");
+    if (!(f.radius > 0.0)) return c->fail(HCC_ERR_INVALID, "radius must be positive");
+    if (f.muscl_order < 1 || f.muscl_order > 3) return c->fail(HCC_ERR_UNSUPPORTED, "muscl_order must be 1, 2 or 3");
+    if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_EPD2) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
+    if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_ONLY) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
+    if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
+    c->max_order = f.muscl_order;
+    c->DO = f.div_order > c->max_order ? c->max_order : f.div_order;
+    if (c->DO < 0) return c->fail(HCC_ERR_INVALID, "div_order must be >= 0");
+    c->rdeg = std::max(1, c->max_order - 1);
+    c->Br = basis_count(c->D, c->rdeg);
+    c->full_div = div_idx(c->D, c->DO == 0 ? c->max_order : c->DO);
+    c->ddeg = c->full_div - 1;
+    c->Bd = basis_count(c->D, c->ddeg) + 1;
+    if (c->ddeg > 3) return c->fail(HCC_ERR_UNSUPPORTED, "divergence degree above 3");
+    c->need_dw1 = (c->DO == 0 && c->full_div > 2) ? 1 : 0;
+    double h = f.dx[0];
+    for (int d = 1; d < c->D; ++d) h = std::min(h, f.dx[d]);
+    if (!(h > 0.0)) return c->fail(HCC_ERR_INVALID, "dx must be positive");
+    c->invL = 1.0 / h;
+    c->tab = make_tableau(f.tableau);
+    if (c->tab.s == 0) return c->fail(HCC_ERR_INVALID, "unknown tableau");
+    c->has_source = f.pde == HCC_PDE_BGK;
+    c->ssp_C = ssp_coefficient(c->tab);
+    if (c->has_source && !has_implicit_part(c->tab)) {
+        // implicit sources with an explicit tableau: applied explicitly with the explicit weights
+        // (_explicit_implicit_part, TimeSteppers.jl:236-237)
+        for (int i = 0; i < c->tab.s; ++i) {
+            for (int j = 0; j < c->tab.s; ++j) c->tab.a[i][j] = c->tab.at[i][j];
+            c->tab.c[i] = c->tab.ct[i];
+            c->tab.b[i] = c->tab.bt[i];
+        }
+    }
+    c->ratio = (f.mood_substeps && c->ssp_C > 0.0 && f.mood_criterion != HCC_MOOD_NONE) ? 1.0 / c->ssp_C : 0.0;
+    c->ops = find_ops(f, c->rdeg);
+    if (!c->ops) return c->fail(HCC_ERR_UNSUPPORTED, "this (dim, n_vars, pde) combination is not instantiated");
+    hcc_status st = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+    if (st != HCC_OK) return st;
+    if ((st = c->alloc(c->d_counters, 8, "counters")) != HCC_OK) return st;
+    if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->h_counters), 8 * sizeof(unsigned long long)),
+                      "pinned counters")) != HCC_OK) return st;
+    if ((st = c->alloc(c->d_mass, HCC_MAX_VARS, "mass")) != HCC_OK) return st;
+    return HCC_OK;
+}
+
+hcc_status hcc_destroy(hcc_ctx *ctx) {
+    if (!ctx) return HCC_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->free_particles();
+    ctx->free_slots();
+    ctx->free_bins();
+    dfree(ctx->d_counters);
+    dfree(ctx->d_mass);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return HCC_OK;
+}
+
+hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint8_t *is_boundary, const int32_t *tags,
+                            const double *volumes) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->ops) return c->fail(HCC_ERR_STATE, "context was not created successfully");
+    if (n < 0 || (n > 0 && (!pos || !is_boundary || !tags))) return c->fail(HCC_ERR_INVALID, "bad cloud arguments");
+    if (c->capacity > 0 && n > c->capacity) return c->fail(HCC_ERR_CAPACITY, "particle count above the capacity");
+    if (n > int64_t(INT32_MAX) - 64) return c->fail(HCC_ERR_CAPACITY, "particle count above 2^31");
+    c->free_particles();
+    c->free_slots();
+    c->have_cloud = c->have_nb = c->have_geom = c->have_state = false;
+    c->n = n;
+    c->npad = ((n + 31) / 32) * 32;
+    const int D = c->D, M = c->M;
+    const int64_t np = c->npad;
+    std::vector<double> soa(size_t(D) * np, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < D; ++d) soa[d * np + i] = pos[i * D + d];
+    c->h_bnd.assign(is_boundary, is_boundary + n);
+    c->h_tags.assign(tags, tags + n);
+    c->n_interior = 0;
+    for (int64_t i = 0; i < n; ++i) c->n_interior += is_boundary[i] ? 0 : 1;
+    std::vector<double> v(size_t(std::max<int64_t>(n, 1)), 1.0);
+    double v0 = 1.0;
+    for (int d = 0; d < D; ++d) v0 *= c->cfg.dx[d];
+    for (int64_t i = 0; i < n; ++i) v[i] = volumes ? volumes[i] : v0;
+    hcc_status st;
+#define HCC_TRY(x) do { if ((st = (x)) != HCC_OK) return st; } while (0)
+    HCC_TRY(c->alloc(c->pos, size_t(D) * np, "positions"));
+    HCC_TRY(c->alloc(c->bnd, np, "is_boundary"));
+    HCC_TRY(c->alloc(c->tags, np, "tags"));
+    HCC_TRY(c->alloc(c->vol, np, "volumes"));
+    HCC_TRY(c->alloc(c->bin_of, np, "bin_of"));
+    HCC_TRY(c->alloc(c->cellp, np, "cell particles"));
+    HCC_TRY(c->alloc(c->cnt, np, "counts"));
+    HCC_TRY(c->alloc(c->ok_r, np, "ok_r"));
+    HCC_TRY(c->alloc(c->ok_d, np, "ok_d"));
+    HCC_TRY(c->alloc(c->ok_1, np, "ok_1"));
+    HCC_TRY(c->alloc(c->inv_r64, size_t(np) * c->Br * c->Br, "inv_r"));
+    HCC_TRY(c->alloc(c->inv_d64, size_t(np) * c->Bd * c->Bd, "inv_d"));
+    if (c->f32) HCC_TRY(c->alloc(c->inv_r32, size_t(np) * c->Br * c->Br, "inv_r32"));
+    HCC_TRY(c->alloc(c->status, np, "status"));
+    HCC_TRY(c->alloc(c->status2, np, "status2"));
+    HCC_TRY(c->alloc(c->root, np, "root"));
+    const size_t sb = size_t(np) * M * c->esz();
+    HCC_TRY(c->valloc(c->rhos, sb, "rhos"));
+    HCC_TRY(c->valloc(c->cand, sb, "candidate"));
+    HCC_TRY(c->valloc(c->grad, size_t(np) * c->Br * M * c->esz(), "gradients"));
+    for (int s = 0; s < c->tab.s; ++s) {
+        HCC_TRY(c->valloc(c->Y[s], sb, "stage states"));
+        HCC_TRY(c->valloc(c->KE[s], sb, "stage K_E"));
+        HCC_TRY(c->valloc(c->KI[s], sb, "stage K_I"));
+        cudaMemsetAsync(c->KE[s], 0, sb, c->stream);
+        cudaMemsetAsync(c->KI[s], 0, sb, c->stream);
+    }
+    cudaMemsetAsync(c->grad, 0, size_t(np) * c->Br * M * c->esz(), c->stream);
+    cudaMemsetAsync(c->rhos, 0, sb, c->stream);
+    HCC_TRY(c->alloc(c->orders, np, "orders"));
+    HCC_TRY(c->alloc(c->nbmin, np, "nbmin"));
+    for (uint8_t **p : {&c->triggered, &c->changed, &c->dirty, &c->scratch, &c->trig_step, &c->inadm}) {
+        HCC_TRY(c->alloc(*p, np, "masks"));
+        cudaMemsetAsync(*p, 0, np, c->stream);
+    }
+    launch_fill_i8(c->orders, int8_t(c->max_order), np, c->stream);
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->pos, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "upload positions"));
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->bnd, is_boundary, n, cudaMemcpyHostToDevice, c->stream), "upload is_boundary"));
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->tags, tags, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream), "upload tags"));
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->vol, v.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "upload volumes"));
+    HCC_TRY(c->sync("upload cloud"));
+    c->have_cloud = true;
+    return HCC_OK;
+}
+
+hcc_status hcc_build_neighbours(hcc_ctx *c) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud uploaded");
+    const hcc_config &f = c->cfg;
+    const int D = c->D;
+    hcc_status st;
+    // GlobalBins (NeighborLogic.jl:123-141) and the 3^D window of every bin (:144-177), on the host
+    c->nbins = 1;
+    for (int d = 0; d < 3; ++d) { c->dims[d] = 1; c->csize[d] = 1.0; }
+    for (int d = 0; d < D; ++d) {
+        double sz = f.canvas_max[d] - f.canvas_min[d];
+        if (!(sz > 0.0)) return c->fail(HCC_ERR_INVALID, "empty canvas");
+        c->dims[d] = std::max(1, int(std::floor(sz / f.radius)));
+        c->csize[d] = sz / double(c->dims[d]);
+        c->nbins *= c->dims[d];
+    }
+    if (c->nbins > (int64_t(1) << 30)) return c->fail(HCC_ERR_CAPACITY, "too many cell-list bins");
+    c->noff = D == 1 ? 3 : (D == 2 ? 9 : 27);
+    std::vector<int64_t> binnb(size_t(c->nbins) * c->noff);
+    for (int64_t b = 0; b < c->nbins; ++b) {
+        int cart[3] = {0, 0, 0};
+        int64_t r = b;
+        for (int d = 0; d < D; ++d) { cart[d] = int(r % c->dims[d]); r /= c->dims[d]; }
+        int64_t raw[27];
+        for (int w = 0; w < c->noff; ++w) {
+            int q = w;
+            bool valid = true;
+            int64_t lin = 0, stride = 1;
+            for (int d = 0; d < D; ++d) {
+                int off = q % 3 - 1;
+                q /= 3;
+                int nc = cart[d] + off;
+                if (nc < 0 || nc >= c->dims[d]) {
+                    if (f.periodic[d]) nc = ((nc % c->dims[d]) + c->dims[d]) % c->dims[d];
+                    else { valid = false; nc = 0; }
+                }
+                lin += nc * stride;
+                stride *= c->dims[d];
+            }
+            raw[w] = valid ? lin : c->nbins;
+        }
+        for (int w = 0; w < c->noff; ++w) {
+            bool rep = false;
+            for (int k = 0; k < w; ++k) rep = rep || raw[k] == raw[w];
+            binnb[size_t(b) * c->noff + w] = rep ? c->nbins : raw[w];
+        }
+    }
+    c->free_bins();
+    HCC_TRY(c->alloc(c->binnb, binnb.size(), "bin windows"));
+    HCC_TRY(c->alloc(c->cell_count, c->nbins + 1, "cell counts"));
+    HCC_TRY(c->alloc(c->cell_cursor, c->nbins + 1, "cell cursor"));
+    HCC_TRY(c->alloc(c->cell_start, c->nbins + 2, "cell start"));
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->binnb, binnb.data(), binnb.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                    c->stream), "upload bin windows"));
+    SearchArgs a{};
+    a.n = c->n; a.npad = c->npad; a.D = D; a.pos = c->pos;
+    const double R = f.radius;
+    for (int d = 0; d < 3; ++d) {
+        a.periodic[d] = d < D ? f.periodic[d] : 0;
+        a.cmin[d] = f.canvas_min[d];
+        a.csize[d] = c->csize[d];
+        a.dims[d] = c->dims[d];
+        double L = f.domain_max[d] - f.domain_min[d];
+        a.Lphys[d] = L;
+        a.Lwrap[d] = (d < D && f.periodic[d]) ? L : 0.0;
+        a.invLwrap[d] = (d < D && f.periodic[d]) ? 1.0 / L : 0.0;
+    }
+    a.nbins = c->nbins; a.noff = c->noff; a.binnb = c->binnb;
+    a.bin_of = c->bin_of; a.cell_count = c->cell_count; a.cell_start = c->cell_start; a.cell_cursor = c->cell_cursor;
+    a.cellp = c->cellp; a.cnt = c->cnt;
+    a.R_sq = R * R;
+    a.alpha = f.weight_alpha;
+    a.invR2 = 1.0 / (R * R);
+    if ((st = search_bins(a, c->stream, c->err)) != HCC_OK) return st;
+    if ((st = search_count(a, c->stream, c->d_counters + 3, c->err)) != HCC_OK) return st;
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->h_counters + 3, c->d_counters + 3, 2 * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, c->stream), "search stats"));
+    HCC_TRY(c->sync("neighbour count"));
+    const int64_t kmax = int64_t(c->h_counters[3]);
+    c->total_nb = int64_t(c->h_counters[4]);
+    if (f.reserved_i[0] > 0 && kmax > f.reserved_i[0])
+        return c->fail(HCC_ERR_CAPACITY, "max neighbours above the reserved slot capacity");
+    c->free_slots();
+    c->kmax = int(kmax);
+    const size_t slots = size_t(std::max<int64_t>(kmax, 1)) * c->npad;
+    HCC_TRY(c->alloc(c->nidx, slots, "neighbour indices"));
+    HCC_TRY(c->alloc(c->w64, slots, "neighbour weights"));
+    HCC_TRY(c->alloc(c->dist64, slots * D, "neighbour distances"));
+    a.nidx = c->nidx; a.w = c->w64; a.dist = c->dist64; a.kmax = c->kmax;
+    if ((st = search_write(a, c->stream, c->err)) != HCC_OK) return st;
+    HCC_TRY(c->sync("neighbour write"));
+    c->have_nb = true;
+    c->have_geom = false;
+    return HCC_OK;
+}
+
+hcc_status hcc_download_neighbours(hcc_ctx *c, int32_t *counts, int32_t *idx, double *w, double *dist) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
+    const int64_t n = c->n;
+    std::vector<int32_t> cnt(n);
+    hcc_status st;
+    HCC_TRY(c->cuda(cudaMemcpy(cnt.data(), c->cnt, n * sizeof(int32_t), cudaMemcpyDeviceToHost), "counts"));
+    if (counts) std::memcpy(counts, cnt.data(), n * sizeof(int32_t));
+    if (!idx && !w && !dist) return HCC_OK;
+    std::vector<int64_t> rs(n);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < n; ++i) { rs[i] = tot; tot += cnt[i]; }
+    int64_t *d_rs = nullptr;
+    void *tmp = nullptr;
+    HCC_TRY(c->alloc(d_rs, n, "row starts"));
+    HCC_TRY(c->valloc(tmp, size_t(std::max<int64_t>(tot, 1)) * 8 * c->D, "row buffer"));
+    cudaMemcpy(d_rs, rs.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice);
+    auto pull = [&](const void *src, void *dst, int width, int eb) -> hcc_status {
+        launch_gather_rows(src, tmp, c->cnt, d_rs, n, c->npad, width, eb, c->stream);
+        hcc_status s2 = c->sync("row gather");
+        if (s2 != HCC_OK) return s2;
+        return c->cuda(cudaMemcpy(dst, tmp, size_t(tot) * width * eb, cudaMemcpyDeviceToHost), "row copy");
+    };
+    st = HCC_OK;
+    if (idx && st == HCC_OK) st = pull(c->nidx, idx, 1, 4);
+    if (w && st == HCC_OK) st = pull(c->w64, w, 1, 8);
+    if (dist && st == HCC_OK) st = pull(c->dist64, dist, c->D, 8);
+    cudaFree(d_rs);
+    cudaFree(tmp);
+    return st;
+}
+
+hcc_status hcc_prepare_geometry(hcc_ctx *c) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
+    hcc_status st;
+    const int D = c->D;
+    const size_t slots = size_t(std::max(c->kmax, 1)) * c->npad;
+    HCC_TRY(c->alloc(c->dw64, slots * D, "divergence weights"));
+    if (c->need_dw1) HCC_TRY(c->alloc(c->dw1_64, slots * D, "degree-1 weights"));
+    cudaMemsetAsync(c->dw64, 0, slots * D * sizeof(double), c->stream);
+    MlsArgs m{};
+    m.n = c->n; m.npad = c->npad; m.D = D; m.rdeg = c->rdeg; m.Br = c->Br; m.ddeg = c->ddeg; m.Bd = c->Bd;
+    m.max_order = c->max_order; m.DO = c->DO; m.need_dw1 = c->need_dw1;
+    m.cnt = c->cnt; m.nidx = c->nidx; m.dist = c->dist64; m.w = c->w64; m.invL = c->invL;
+    m.inv_r = c->inv_r64; m.ok_r = c->ok_r; m.inv_d = c->inv_d64; m.ok_d = c->ok_d;
+    m.dw = c->dw64; m.dw1 = c->dw1_64; m.ok_1 = c->ok_1;
+    if ((st = mls_prepare(m, c->stream, c->err)) != HCC_OK) return st;
+    if (c->f32) {
+        HCC_TRY(c->alloc(c->dist32, slots * D, "distances f32"));
+        HCC_TRY(c->alloc(c->w32, slots, "weights f32"));
+        HCC_TRY(c->alloc(c->dw32, slots * D, "divergence weights f32"));
+        launch_cast_f64_to_f32(c->dist64, c->dist32, int64_t(slots) * D, c->stream);
+        launch_cast_f64_to_f32(c->w64, c->w32, int64_t(slots), c->stream);
+        launch_cast_f64_to_f32(c->dw64, c->dw32, int64_t(slots) * D, c->stream);
+        launch_cast_f64_to_f32(c->inv_r64, c->inv_r32, c->npad * c->Br * c->Br, c->stream);
+        if (c->need_dw1) {
+            HCC_TRY(c->alloc(c->dw1_32, slots * D, "degree-1 weights f32"));
+            launch_cast_f64_to_f32(c->dw1_64, c->dw1_32, int64_t(slots) * D, c->stream);
+        }
+    }
+    // outflow donor roots, then the boundary list (tag -> condition)
+    DonorArgs da{};
+    da.n = c->n; da.npad = c->npad; da.D = D; da.cnt = c->cnt; da.nidx = c->nidx; da.dist = c->dist64;
+    da.bnd = c->bnd; da.tags = c->tags; da.status = c->status; da.status_prev = c->status2; da.root = c->root;
+    if ((st = donor_map(da, -1, c->stream, c->err)) != HCC_OK) return st;
+    for (int tag = 1; tag <= HCC_MAX_TAGS; ++tag)
+        if (c->cfg.bc_by_tag[tag - 1] == HCC_BC_OUTFLOW)
+            if ((st = donor_map(da, tag, c->stream, c->err)) != HCC_OK) return st;
+    std::vector<int32_t> root(c->n);
+    HCC_TRY(c->sync("geometry kernels"));
+    if (c->n) HCC_TRY(c->cuda(cudaMemcpy(root.data(), c->root, c->n * sizeof(int32_t), cudaMemcpyDeviceToHost), "donor roots"));
+    std::vector<int32_t> bl, bs;
+    for (int64_t i = 0; i < c->n; ++i) {
+        if (!c->h_bnd[i]) continue;
+        int tag = c->h_tags[i];
+        int kind = (tag >= 1 && tag <= HCC_MAX_TAGS) ? c->cfg.bc_by_tag[tag - 1] : HCC_BC_KEEP;
+        bl.push_back(int32_t(i));
+        bs.push_back(kind == HCC_BC_OUTFLOW ? root[i] : -1);
+    }
+    c->nbnd = int64_t(bl.size());
+    HCC_TRY(c->alloc(c->blist, std::max<size_t>(bl.size(), 1), "boundary list"));
+    HCC_TRY(c->alloc(c->bsrc, std::max<size_t>(bs.size(), 1), "boundary sources"));
+    if (!bl.empty()) {
+        HCC_TRY(c->cuda(cudaMemcpy(c->blist, bl.data(), bl.size() * 4, cudaMemcpyHostToDevice), "boundary list"));
+        HCC_TRY(c->cuda(cudaMemcpy(c->bsrc, bs.data(), bs.size() * 4, cudaMemcpyHostToDevice), "boundary sources"));
+    }
+    c->have_geom = true;
+    return HCC_OK;
+}
+
+hcc_status hcc_download_geometry(hcc_ctx *c, double *dweights, uint8_t *ok_recon, uint8_t *ok_div) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->have_geom) return c->fail(HCC_ERR_STATE, "geometry not prepared");
+    hcc_status st;
+    const int64_t n = c->n;
+    if (ok_recon) HCC_TRY(c->cuda(cudaMemcpy(ok_recon, c->ok_r, n, cudaMemcpyDeviceToHost), "ok_r"));
+    if (ok_div) HCC_TRY(c->cuda(cudaMemcpy(ok_div, c->ok_d, n, cudaMemcpyDeviceToHost), "ok_d"));
+    if (!dweights) return HCC_OK;
+    std::vector<int32_t> cnt(n);
+    HCC_TRY(c->cuda(cudaMemcpy(cnt.data(), c->cnt, n * 4, cudaMemcpyDeviceToHost), "counts"));
+    std::vector<int64_t> rs(n);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < n; ++i) { rs[i] = tot; tot += cnt[i]; }
+    int64_t *d_rs = nullptr;
+    void *tmp = nullptr;
+    HCC_TRY(c->alloc(d_rs, n, "row starts"));
+    HCC_TRY(c->valloc(tmp, size_t(std::max<int64_t>(tot, 1)) * 8 * c->D, "row buffer"));
+    cudaMemcpy(d_rs, rs.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice);
+    launch_gather_rows(c->dw64, tmp, c->cnt, d_rs, n, c->npad, c->D, 8, c->stream);
+    st = c->sync("row gather");
+    if (st == HCC_OK) st = c->cuda(cudaMemcpy(dweights, tmp, size_t(tot) * c->D * 8, cudaMemcpyDeviceToHost), "dweights");
+    cudaFree(d_rs);
+    cudaFree(tmp);
+    return st;
+}
+
+static hcc_status upload_state_impl(hcc_ctx *c, const void *U, int src_f32) {
+    if (!c || !U) return c ? c->fail(HCC_ERR_INVALID, "null state") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud uploaded");
+    const int64_t cnt = c->n * c->M;
+    hcc_status st;
+    if (bool(src_f32) == bool(c->f32)) {
+        HCC_TRY(c->cuda(cudaMemcpyAsync(c->rhos, U, size_t(cnt) * c->esz(), cudaMemcpyHostToDevice, c->stream), "upload state"));
+    } else {
+        // convert through the candidate buffer (free between steps)
+        HCC_TRY(c->cuda(cudaMemcpyAsync(c->KE[0], U, size_t(cnt) * (src_f32 ? 4 : 8), cudaMemcpyHostToDevice, c->stream),
+                        "upload state"));
+        if (src_f32) launch_cast_f32_to_f64(static_cast<const float *>(c->KE[0]), static_cast<double *>(c->rhos), cnt, c->stream);
+        else launch_cast_f64_to_f32(static_cast<const double *>(c->KE[0]), static_cast<float *>(c->rhos), cnt, c->stream);
+    }
+    HCC_TRY(c->sync("upload state"));
+    c->have_state = true;
+    return HCC_OK;
+}
+
+static hcc_status download_state_impl(hcc_ctx *c, void *U, int dst_f32) {
+    if (!c || !U) return c ? c->fail(HCC_ERR_INVALID, "null state") : HCC_ERR_INVALID;
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    const int64_t cnt = c->n * c->M;
+    hcc_status st;
+    if (bool(dst_f32) == bool(c->f32)) {
+        HCC_TRY(c->cuda(cudaMemcpyAsync(U, c->rhos, size_t(cnt) * c->esz(), cudaMemcpyDeviceToHost, c->stream), "download state"));
+    } else {
+        if (dst_f32) launch_cast_f64_to_f32(static_cast<const double *>(c->rhos), static_cast<float *>(c->cand), cnt, c->stream);
+        else launch_cast_f32_to_f64(static_cast<const float *>(c->rhos), static_cast<double *>(c->KE[0]), cnt, c->stream);
+        const void *src = dst_f32 ? c->cand : c->KE[0];
+        HCC_TRY(c->cuda(cudaMemcpyAsync(U, src, size_t(cnt) * (dst_f32 ? 4 : 8), cudaMemcpyDeviceToHost, c->stream),
+                        "download state"));
+    }
+    return c->sync("download state");
+}
+
+hcc_status hcc_upload_state(hcc_ctx *c, const double *U) { return upload_state_impl(c, U, 0); }
+hcc_status hcc_download_state(hcc_ctx *c, double *U) { return download_state_impl(c, U, 0); }
+hcc_status hcc_upload_state_f32(hcc_ctx *c, const float *U) { return upload_state_impl(c, U, 1); }
+hcc_status hcc_download_state_f32(hcc_ctx *c, float *U) { return download_state_impl(c, U, 1); }
+
+hcc_status hcc_time_step(hcc_ctx *c, double *dt_out) {
+    if (!c || !dt_out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (c->n == 0) { *dt_out = std::numeric_limits<double>::infinity(); return HCC_OK; }
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    return c->f32 ? run_cfl<float>(c, dt_out) : run_cfl<double>(c, dt_out);
+}
+
+hcc_status hcc_compute_rhs(hcc_ctx *c, double *K) {
+    if (!c || !K) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    hcc_status st = c->f32 ? run_rhs<float>(c) : run_rhs<double>(c);
+    if (st != HCC_OK) return st;
+    const int64_t cnt = c->n * c->M;
+    if (c->f32) {
+        launch_cast_f32_to_f64(static_cast<const float *>(c->KE[0]), static_cast<double *>(c->cand), cnt, c->stream);
+        HCC_TRY(c->sync("rhs cast"));
+        return c->cuda(cudaMemcpy(K, c->cand, cnt * 8, cudaMemcpyDeviceToHost), "download rhs");
+    }
+    return c->cuda(cudaMemcpy(K, c->KE[0], cnt * 8, cudaMemcpyDeviceToHost), "download rhs");
+}
+
+hcc_status hcc_step(hcc_ctx *c, double t, double dt) {
+    (void)t;
+    if (!c) return HCC_ERR_INVALID;
+    if (!std::isfinite(dt) || !(dt >= 0.0)) return c->fail(HCC_ERR_NONFINITE, "dt must be finite and >= 0");
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    if (c->n == 0) return HCC_OK;
+    return c->f32 ? run_step<float>(c, dt) : run_step<double>(c, dt);
+}
+
+hcc_status hcc_download_orders(hcc_ctx *c, int32_t *orders) {
+    if (!c || !orders) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud");
+    std::vector<int8_t> o(c->n);
+    hcc_status st;
+    HCC_TRY(c->cuda(cudaMemcpy(o.data(), c->orders, c->n, cudaMemcpyDeviceToHost), "orders"));
+    for (int64_t i = 0; i < c->n; ++i) orders[i] = o[i];
+    return HCC_OK;
+}
+
+hcc_status hcc_download_mood_flags(hcc_ctx *c, uint8_t *flags) {
+    if (!c || !flags) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud");
+    return c->cuda(cudaMemcpy(flags, c->trig_step, c->n, cudaMemcpyDeviceToHost), "mood flags");
+}
+
+hcc_status hcc_get_counters(hcc_ctx *c, hcc_counters *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    std::memset(out, 0, sizeof(*out));
+    out->n_particles = c->n;
+    out->n_interior = c->n_interior;
+    out->max_neighbours = c->kmax;
+    out->total_neighbours = c->total_nb;
+    out->mood_iterations = c->mood_iters;
+    out->mood_flagged = c->flagged;
+    out->inadmissible = c->inadmissible;
+    out->kernel_launches = c->launches;
+    out->steps = c->steps;
+    if (c->have_nb && c->n) {
+        std::vector<int32_t> cnt(c->n);
+        if (cudaMemcpy(cnt.data(), c->cnt, c->n * 4, cudaMemcpyDeviceToHost) == cudaSuccess) {
+            int32_t mn = INT32_MAX;
+            for (int64_t i = 0; i < c->n; ++i) if (!c->h_bnd[i]) mn = std::min(mn, cnt[i]);
+            out->min_neighbours_interior = mn == INT32_MAX ? 0 : mn;
+        }
+    }
+    return HCC_OK;
+}
+
+hcc_status hcc_total_mass(hcc_ctx *c, double *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    launch_total_mass(c->rhos, c->vol, c->n, c->M, c->f32, c->d_mass, c->stream);
+    hcc_status st;
+    HCC_TRY(c->sync("mass"));
+    return c->cuda(cudaMemcpy(out, c->d_mass, c->M * sizeof(double), cudaMemcpyDeviceToHost), "mass copy");
+}
+
+hcc_status hcc_synchronize(hcc_ctx *c) {
+    if (!c) return HCC_ERR_INVALID;
+    return c->sync("synchronize");
+}
+
+void *hcc_stream(hcc_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
+
+}  // extern "C"

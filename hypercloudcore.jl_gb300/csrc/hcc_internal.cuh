@@ -1,0 +1,229 @@
+// hcc_internal.cuh — shared declarations of the GB300 explicit-RHS library (not part of the public ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include <string>
+#include <vector>
+#include "../../include/hcc.h"
+
+#define HCC_MAX_STAGES 5
+#define HCC_BLOCK 256
+
+namespace hcc {
+
+// ----------------------------------------------------------------------------------- float helpers
+// Base.min / Base.max of Julia for IEEE floats: NaN-propagating, -0 below +0 (src/Utils.jl:259-262).
+template <typename T> __host__ __device__ __forceinline__ bool is_nan(T x) { return x != x; }
+template <typename T> __host__ __device__ __forceinline__ T jmin(T x, T y) {
+    bool take_y = (y < x) || (signbit(y) && !signbit(x));
+    return take_y ? (is_nan(x) ? x : y) : (is_nan(y) ? y : x);
+}
+template <typename T> __host__ __device__ __forceinline__ T jmax(T x, T y) {
+    bool take_y = (y > x) || (!signbit(y) && signbit(x));
+    return take_y ? (is_nan(x) ? x : y) : (is_nan(y) ? y : x);
+}
+
+// basis_count(D, degree) (src/Interpolation/Interpolators.jl:170-177)
+__host__ __device__ __forceinline__ int basis_count(int D, int degree) {
+    if (degree <= 0) return 0;
+    long n = 1;
+    for (int k = 1; k <= degree; ++k) n = (n * (D + k)) / k;
+    return int(n - 1);
+}
+// _div_idx / _divergence_index (src/Interpolation/MUSCL.jl:11-32)
+__host__ __device__ __forceinline__ int div_idx(int D, int o) {
+    if (o <= 2) return 2;
+    return ((o % 2 == 1) && (D < 3 || o <= 3)) ? o + 1 : o;
+}
+__host__ __device__ __forceinline__ int divergence_index(int DO, int D, int p_order, int num_nb) {
+    int idx = (DO == 0) ? div_idx(D, p_order) : div_idx(D, DO);
+    int b0 = (DO == 0) ? p_order : DO;
+    int base = b0 > 2 ? b0 : 2;
+    if (idx > base && 2 * num_nb < 3 * (basis_count(D, idx - 1) + 1)) idx = base;
+    while (idx > 2 && num_nb < basis_count(D, idx - 1) + 1) idx -= 1;
+    return idx;
+}
+
+// Reconstruction basis of degree 1 or 2 (build_basis, Interpolators.jl:194-218), in the order of
+// _generate_exponents: degree-1 terms x, y, z; then x²/2, y²/2, z²/2; then xy, xz, yz.
+template <int D, int DEG> struct RBasis { static constexpr int B = (DEG == 1) ? D : (D == 1 ? 2 : (D == 2 ? 5 : 9)); };
+
+template <int D, int DEG, typename T>
+__host__ __device__ __forceinline__ void recon_basis(const T *x, T *p) {
+    if constexpr (DEG == 1) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) p[d] = x[d];
+    } else {
+        if constexpr (D == 1) { p[0] = x[0]; p[1] = T(0.5) * (x[0] * x[0]); }
+        if constexpr (D == 2) {
+            p[0] = x[0]; p[1] = x[1];
+            p[2] = T(0.5) * (x[0] * x[0]); p[3] = T(0.5) * (x[1] * x[1]); p[4] = x[0] * x[1];
+        }
+        if constexpr (D == 3) {
+            p[0] = x[0]; p[1] = x[1]; p[2] = x[2];
+            p[3] = T(0.5) * (x[0] * x[0]); p[4] = T(0.5) * (x[1] * x[1]); p[5] = T(0.5) * (x[2] * x[2]);
+            p[6] = x[0] * x[1]; p[7] = x[0] * x[2]; p[8] = x[1] * x[2];
+        }
+    }
+}
+// build_scale_factors (Interpolators.jl:236-247) for degree 1/2 bases
+template <int D, int DEG, typename T>
+__host__ __device__ __forceinline__ T recon_scale(int b, T invL) {
+    return (b < D) ? invL : invL * invL;
+}
+
+// ----------------------------------------------------------------------------------- physics
+// Parameters of the compiled-in HyperbolicPDE modules (selected by trait at hcc_create).
+template <typename T> struct PhysParams {
+    T c[HCC_MAX_DIM][HCC_MAX_VARS];   // advection speeds (BGK: kinetic speeds v_k,d)
+    T amax[HCC_MAX_DIM];              // spectral radius per axis
+    T gamma, gm1;
+    T inv_eps, coeff;                 // BGK
+    T a_macro[HCC_MAX_DIM];
+    T sinv[HCC_MAX_VARS][HCC_MAX_DIM];
+};
+
+// Scheme-wide constants of the stage kernels.
+struct SchemeParams {
+    int max_order, DO, strategy, criterion;
+    int has_source;                   // BGK relaxation source present
+};
+
+// Device view of the neighbour lists and geometry caches (slot-major, stride = npad).
+template <typename T> struct Geometry {
+    int64_t n, npad;
+    const int32_t *cnt;               // [n]
+    const int32_t *nidx;              // [kmax * npad]
+    const T *dist;                    // [(k*D + d) * npad + i]
+    const T *wt;                      // [k * npad + i]
+    const T *dw;                      // [(k*D + d) * npad + i]  divergence weights of the cached fit
+    const T *dw1;                     // degree-1 dynamic set (schemes whose full divergence degree is > 1)
+    const uint8_t *ok_r, *ok_d, *ok_1;
+    const T *inv_r;                   // [i * Br * Br]
+    const uint8_t *bnd;
+    T invL;
+};
+
+// Arguments of the gather (reconstruction) and flux kernels.
+template <typename T> struct StageArgs {
+    Geometry<T> g;
+    PhysParams<T> ph;
+    SchemeParams sc;
+    int8_t *orders;
+    const int8_t *nbmin;              // EPD2: neighbourhood minimum of the orders
+    T *grad;                          // [i * Br * M]
+    const T *U;                       // stage state Y_s
+    T *K;                             // K_E[s]
+    const uint8_t *mask;              // gather: changed; flux: dirty
+    int full;
+    // epilogue: next candidate (Y_{s+1} or the final state) and the MOOD check of checkpoint s+1
+    int form_next;
+    const T *Un;                      // start-of-step state (pg.rhos)
+    const T *KE[HCC_MAX_STAGES];
+    const T *KI[HCC_MAX_STAGES];
+    T hE[HCC_MAX_STAGES];             // dt * a_t (0: skipped)
+    T hI[HCC_MAX_STAGES];             // dt * a   (0: skipped)
+    int n_prev;                       // stages entering the candidate (K_E[s] is this kernel's own)
+    int self_slot;                    // index of K_E[s] among KE (its value comes from registers)
+    T *Ynext;
+    T *KInext;
+    int implicit_mode;                // 0 none, 1 implicit solve (a_ii != 0), 2 explicit source evaluation
+    T dt_ii, inv_dt_ii;
+    int check;                        // run the MOOD check of the candidate
+    int check_substep;                // 1: W = Y_s + h_sub (K + KI_s), 0: the candidate itself
+    const T *KIs;                     // K_I[s] for the substep of implicit-source tableaus
+    T h_sub;
+    T delta;
+    uint8_t *triggered;
+    uint8_t *inadm;
+};
+
+// Launchers of one (precision, D, M, pde, reconstruction degree) instantiation.
+struct StageOps {
+    int D, M, pde, rdeg, Br;
+    void (*gather)(const void *args, int64_t n, cudaStream_t s);
+    void (*flux)(const void *args, int64_t n, cudaStream_t s);
+    void (*stage1)(const void *args, int64_t n, cudaStream_t s);   // Y_1 (predictor + implicit part)
+    void (*cfl)(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s);
+    void (*admissible_count)(const void *args, int64_t n, unsigned long long *count, cudaStream_t s);
+};
+
+const StageOps *stage_ops_f64_r1(int D, int M, int pde);
+const StageOps *stage_ops_f64_r2(int D, int M, int pde);
+const StageOps *stage_ops_f32_r1(int D, int M, int pde);
+const StageOps *stage_ops_f32_r2(int D, int M, int pde);
+
+// ----------------------------------------------------------------------------------- search / geometry
+struct SearchArgs {
+    int64_t n, npad;
+    int D;
+    double *pos;                      // SoA [d * npad + i]
+    int periodic[3];
+    double cmin[3], csize[3], Lphys[3], Lwrap[3], invLwrap[3];
+    int dims[3];
+    int64_t nbins;
+    int noff;
+    const int64_t *binnb;             // [nbins * noff]
+    int32_t *bin_of;                  // [n]
+    int32_t *cell_count;              // [nbins + 1]
+    int64_t *cell_start;              // [nbins + 2]
+    int32_t *cell_cursor;             // [nbins]
+    int32_t *cellp;                   // [n]
+    int32_t *cnt;                     // [n]
+    double R_sq, alpha, invR2;
+    // output (slot-major)
+    int32_t *nidx;
+    double *w;
+    double *dist;
+    int kmax;
+};
+
+hcc_status search_bins(SearchArgs &a, cudaStream_t s, std::string &err);
+hcc_status search_count(SearchArgs &a, cudaStream_t s, unsigned long long *d_stats, std::string &err);
+hcc_status search_write(SearchArgs &a, cudaStream_t s, std::string &err);
+
+struct MlsArgs {
+    int64_t n, npad;
+    int D, rdeg, Br, ddeg, Bd, max_order, DO;
+    int need_dw1;
+    const int32_t *cnt, *nidx;
+    const double *dist, *w;
+    double invL;
+    double *inv_r; uint8_t *ok_r;
+    double *inv_d; uint8_t *ok_d;
+    double *dw; double *dw1; uint8_t *ok_1;
+};
+hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err);
+
+// Outflow donor map (BoundaryConditions.jl:82-130 with the state-free part precomputed per geometry).
+struct DonorArgs {
+    int64_t n, npad;
+    int D;
+    const int32_t *cnt, *nidx;
+    const double *dist;
+    const uint8_t *bnd;
+    const int32_t *tags;
+    int32_t *status, *status_prev, *root;
+};
+hcc_status donor_map(DonorArgs &a, int tag, cudaStream_t s, std::string &err);
+
+// Small utility kernels (hcc_util.cu).
+void launch_cast_f64_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s);
+void launch_cast_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s);
+void launch_fill_i8(int8_t *p, int8_t v, int64_t n, cudaStream_t s);
+void launch_bc_apply(void *Y, const void *rhos, const int32_t *blist, const int32_t *bsrc, int64_t nb, int M,
+                     int is_f32, cudaStream_t s);
+void launch_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint8_t *trig_step,
+                      const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *counters,
+                      cudaStream_t s);
+void launch_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n,
+                   int64_t npad, cudaStream_t s);
+void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
+                  int64_t npad, cudaStream_t s);
+void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out,
+                       cudaStream_t s);
+void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
+                        int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
+
+}  // namespace hcc

@@ -1,0 +1,590 @@
+// hcc_stage_impl.cuh — the per-stage kernels, templated on the arithmetic type T (double: plain FP64 path,
+// float: FP32 bulk path), the dimension D, the number of state components M, the physics module PDE and the
+// reconstruction degree RDEG. Included once per precision by hcc_stage_f64.cu / hcc_stage_f32.cu.
+//
+// Thread per particle over slot-major neighbour arrays: the 32 threads of a warp read slot k of 32 consecutive
+// particles from consecutive addresses; neighbour states, gradients and orders are gathered through L1/L2
+// (the Morton numbering keeps a warp's stencils overlapping).
+#pragma once
+#include "hcc_internal.cuh"
+
+namespace hcc {
+
+// ----------------------------------------------------------------------------------- physics (device)
+template <typename T> struct Accum;    // FP32: Kahan-compensated sums; FP64: plain sums
+template <> struct Accum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s = s + x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct Accum<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        float y = x - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s; }
+};
+
+template <typename T> __device__ __forceinline__ T floatmin_of();
+template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2250738585072014e-308; }
+template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
+
+// Euler primitives: inv_rho = 1/rho, u_d = m_d inv_rho, p = (gamma-1)(E - 0.5 (rho |u|^2)), c = sqrt(gamma p inv_rho).
+template <typename T, int D>
+__device__ __forceinline__ void euler_prim(const PhysParams<T> &ph, const T *U, T &inv_rho, T *u, T &p) {
+    T rho = U[0];
+    inv_rho = T(1) / rho;
+    T q2 = T(0);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        u[d] = U[1 + d] * inv_rho;
+        q2 = (d == 0) ? u[d] * u[d] : q2 + u[d] * u[d];
+    }
+    p = ph.gm1 * (U[D + 1] - T(0.5) * (rho * q2));
+}
+
+// flux(eq, U) (API.jl:23) for the compiled-in modules; lam[d] = max_eigenvalue(eq, U, d) (API.jl:38).
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T *U, T (*F)[M], T *lam) {
+    if constexpr (PDE == HCC_PDE_EULER) {
+        T inv_rho, u[D], p;
+        euler_prim<T, D>(ph, U, inv_rho, u, p);
+        T c = sqrt(ph.gamma * p * inv_rho);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            F[d][0] = U[1 + d];
+#pragma unroll
+            for (int e = 0; e < D; ++e) {
+                T v = U[1 + e] * u[d];
+                F[d][1 + e] = (e == d) ? v + p : v;
+            }
+            F[d][D + 1] = (U[D + 1] + p) * u[d];
+            lam[d] = fabs(u[d]) + c;
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) F[d][m] = ph.c[d][m] * U[m];
+            lam[d] = ph.amax[d];
+        }
+    }
+}
+
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void speeds(const PhysParams<T> &ph, const T *U, T *lam) {
+    if constexpr (PDE == HCC_PDE_EULER) {
+        T inv_rho, u[D], p;
+        euler_prim<T, D>(ph, U, inv_rho, u, p);
+        T c = sqrt(ph.gamma * p * inv_rho);
+#pragma unroll
+        for (int d = 0; d < D; ++d) lam[d] = fabs(u[d]) + c;
+    } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) lam[d] = ph.amax[d];
+    }
+}
+
+// is_admissible (API.jl:48): finite; Euler also rho > 0 and p > 0.
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ bool admissible(const PhysParams<T> &ph, const T *U) {
+    bool ok = true;
+#pragma unroll
+    for (int m = 0; m < M; ++m) ok = ok && isfinite(U[m]);
+    if constexpr (PDE == HCC_PDE_EULER) {
+        if (!ok) return false;
+        T inv_rho, u[D], p;
+        euler_prim<T, D>(ph, U, inv_rho, u, p);
+        return U[0] > T(0) && p > T(0);
+    }
+    return ok;
+}
+
+// BGK Maxwellian of the single macro moment (test/kinetic_source.jl:194-231).
+template <typename T, int D, int M>
+__device__ __forceinline__ void maxwellian(const PhysParams<T> &ph, const T *U, T *Mk) {
+    T u = U[0];
+#pragma unroll
+    for (int k = 1; k < M; ++k) u = u + U[k];
+    T F[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[d] = ph.a_macro[d] * u;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        T fd = F[0] * ph.sinv[k][0];
+#pragma unroll
+        for (int d = 1; d < D; ++d) fd = fd + F[d] * ph.sinv[k][d];
+        Mk[k] = ph.coeff * (u + fd);
+    }
+}
+
+// Implicit part of a stage (TimeSteppers.jl:427-444): mode 1 solves U_out - dt a_ii S(U_out) = U_in and sets
+// K_I = (U_out - U_in) / (dt a_ii); mode 2 evaluates K_I = S(Y) explicitly.
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void implicit_part(const StageArgs<T> &a, T *Y, T *KIout) {
+    if constexpr (PDE == HCC_PDE_BGK) {
+        T Mk[M];
+        maxwellian<T, D, M>(a.ph, Y, Mk);
+        if (a.implicit_mode == 1) {
+            T dto = a.dt_ii * a.ph.inv_eps;
+            T denom = T(1) / (T(1) + dto);
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+                T out = (Y[k] + dto * Mk[k]) * denom;
+                KIout[k] = (out - Y[k]) * a.inv_dt_ii;
+                Y[k] = out;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < M; ++k) KIout[k] = (Mk[k] - Y[k]) * a.ph.inv_eps;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < M; ++k) KIout[k] = T(0);
+    }
+}
+
+// ----------------------------------------------------------------------------------- gather pass
+// update_content! of MUSCL (MUSCL.jl:351-384) with NoLimiter: starved-order lowering, cached full-order fit
+// (apply_weights, Interpolators.jl:585-602), dynamic lower-degree fit, or zero (order 1).
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.g.n) return;
+    if (a.g.bnd[i] || !(a.full || a.mask[i])) return;
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    int p = a.orders[i];
+    const int p0 = p;
+    while (p > 1 && cnt < basis_count(D, p - 1)) --p;
+    if (p < p0) a.orders[i] = int8_t(p);
+    T *g = a.grad + i * (BR * M);
+    T fi[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) fi[m] = a.U[i * M + m];
+    T out[BR][M];
+#pragma unroll
+    for (int b = 0; b < BR; ++b)
+#pragma unroll
+        for (int m = 0; m < M; ++m) out[b][m] = T(0);
+    const T invL = a.g.invL;
+    if (p == a.sc.max_order && p > 1 && a.g.ok_r[i]) {
+        T bs[BR][M];
+#pragma unroll
+        for (int b = 0; b < BR; ++b)
+#pragma unroll
+            for (int m = 0; m < M; ++m) bs[b][m] = T(0);
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t s = int64_t(k) * np + i;
+            const int32_t j = a.g.nidx[s];
+            T x[D], pb[BR];
+#pragma unroll
+            for (int d = 0; d < D; ++d) x[d] = a.g.dist[(int64_t(k) * D + d) * np + i] * invL;
+            recon_basis<D, RDEG, T>(x, pb);
+            const T w = a.g.wt[s];
+            T df[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) df[m] = a.U[int64_t(j) * M + m] - fi[m];
+#pragma unroll
+            for (int b = 0; b < BR; ++b)
+#pragma unroll
+                for (int m = 0; m < M; ++m) bs[b][m] = bs[b][m] + w * (pb[b] * df[m]);
+        }
+        const T *inv = a.g.inv_r + i * (BR * BR);
+        T invm[BR][BR];
+#pragma unroll
+        for (int b = 0; b < BR; ++b)
+#pragma unroll
+            for (int c = 0; c < BR; ++c) invm[b][c] = inv[b * BR + c];
+#pragma unroll
+        for (int b = 0; b < BR; ++b) {
+            const T sc = recon_scale<D, RDEG, T>(b, invL);
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                T acc = invm[b][0] * bs[0][m];
+#pragma unroll
+                for (int c = 1; c < BR; ++c) acc = acc + invm[b][c] * bs[c][m];
+                out[b][m] = acc * sc;
+            }
+        }
+    } else if (p > 1 && p - 1 < RDEG) {
+        // Interpolator{D, 1, 1} (_mls_solve, Interpolators.jl:372-400): moment matrix and Cholesky in FP64
+        constexpr int B1 = D;
+        double N[B1 * B1];
+        T bs[B1][M];
+#pragma unroll
+        for (int q = 0; q < B1 * B1; ++q) N[q] = 0.0;
+#pragma unroll
+        for (int b = 0; b < B1; ++b)
+#pragma unroll
+            for (int m = 0; m < M; ++m) bs[b][m] = T(0);
+        const double invLd = double(invL);
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t s = int64_t(k) * np + i;
+            const int32_t j = a.g.nidx[s];
+            double xd[D];
+            T xt[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                T dk = a.g.dist[(int64_t(k) * D + d) * np + i];
+                xd[d] = double(dk) * invLd;
+                xt[d] = dk * invL;
+            }
+            const T w = a.g.wt[s];
+            const double wd = double(w);
+#pragma unroll
+            for (int r = 0; r < B1; ++r)
+#pragma unroll
+                for (int c = 0; c < B1; ++c) N[r * B1 + c] = N[r * B1 + c] + wd * (xd[r] * xd[c]);
+#pragma unroll
+            for (int b = 0; b < B1; ++b)
+#pragma unroll
+                for (int m = 0; m < M; ++m) bs[b][m] = bs[b][m] + w * (xt[b] * (a.U[int64_t(j) * M + m] - fi[m]));
+        }
+        // _cholesky_moment
+        double U[B1 * B1];
+        bool ok = true;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            ok = true;
+            for (int r = 0; r < B1 * B1; ++r) U[r] = 0.0;
+            for (int r = 0; r < B1 && ok; ++r)
+                for (int c = r; c < B1; ++c) {
+                    double sm = N[r * B1 + c];
+                    for (int q = 0; q < r; ++q) sm = sm - U[q * B1 + r] * U[q * B1 + c];
+                    if (r == c) {
+                        if (!(sm > 0.0)) { ok = false; break; }
+                        U[r * B1 + r] = sqrt(sm);
+                    } else U[r * B1 + c] = sm / U[r * B1 + r];
+                }
+            if (attempt == 0 && ok) {
+                for (int q = 0; q < B1; ++q) {
+                    double u = U[q * B1 + q];
+                    if (!(u * u > 10.0 * 2.220446049250313e-16 * N[q * B1 + q])) { ok = false; break; }
+                }
+                if (ok) break;
+            }
+            if (attempt == 0) {
+                double tr = 0.0;
+                for (int q = 0; q < B1; ++q) tr = tr + N[q * B1 + q];
+                double er = 1.4901161193847656e-08 * tr / double(B1);
+                for (int q = 0; q < B1; ++q) N[q * B1 + q] = N[q * B1 + q] + er;
+            }
+        }
+        if (ok) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                double y[B1], x[B1];
+                for (int r = 0; r < B1; ++r) {
+                    double t = double(bs[r][m]);
+                    for (int q = 0; q < r; ++q) t = t - U[q * B1 + r] * y[q];
+                    y[r] = t / U[r * B1 + r];
+                }
+                for (int r = B1 - 1; r >= 0; --r) {
+                    double t = y[r];
+                    for (int q = r + 1; q < B1; ++q) t = t - U[r * B1 + q] * x[q];
+                    x[r] = t / U[r * B1 + r];
+                }
+#pragma unroll
+                for (int b = 0; b < B1; ++b) out[b][m] = T(x[b] * invLd);
+            }
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < BR; ++b)
+#pragma unroll
+        for (int m = 0; m < M; ++m) g[b * M + m] = out[b][m];
+}
+
+// ----------------------------------------------------------------------------------- flux pass
+// The MUSCL functor (MUSCL.jl:390-508) in its streamed form: per slot, EPD interface reconstruction, physical
+// fluxes, Rusanov (FluxFunctions.jl:90-100) with sort_flux (Utils.jl:270-278), the flux difference ΔF and its
+// contraction with the divergence weights; K_E = -2 Σ c·ΔF (TimeSteppers.jl:354). Fused epilogue: the next
+// candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
+// check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.g.n) return;
+    if (a.g.bnd[i]) {
+        if (a.full) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) a.K[i * M + m] = T(0);
+        }
+        return;
+    }
+    if (!(a.full || a.mask[i])) return;
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    const T invL = a.g.invL;
+    (void)invL;
+    T fi[M], gi[BR][M], Fi[D][M], lami[D];
+#pragma unroll
+    for (int m = 0; m < M; ++m) fi[m] = a.U[i * M + m];
+#pragma unroll
+    for (int b = 0; b < BR; ++b)
+#pragma unroll
+        for (int m = 0; m < M; ++m) gi[b][m] = a.grad[i * (BR * M) + b * M + m];
+    flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami);
+    const int oi_own = a.orders[i];
+    const int didx = divergence_index(a.sc.DO, D, oi_own, cnt);
+    const bool cached = a.g.ok_d[i] && didx == divergence_index(a.sc.DO, D, a.sc.max_order, cnt);
+    const T *wsl = cached ? a.g.dw : a.g.dw1;
+    const bool wok = cnt > 0 && (cached || (a.g.dw1 != nullptr && didx == 2 && a.g.ok_1[i]));
+    const bool need_ext = a.check && a.sc.criterion == HCC_MOOD_U1;
+    const int nbmin_i = (a.sc.strategy == HCC_EPD2) ? a.nbmin[i] : 0;
+    Accum<T> acc[M];
+    T mn[M], mx[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) { mn[m] = fi[m]; mx[m] = fi[m]; }
+
+    if (wok) {
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t s = int64_t(k) * np + i;
+            const int32_t j = a.g.nidx[s];
+            T dk[D], wk[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                dk[d] = a.g.dist[(int64_t(k) * D + d) * np + i];
+                wk[d] = wsl[(int64_t(k) * D + d) * np + i];
+            }
+            T fj[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) fj[m] = a.U[int64_t(j) * M + m];
+            if (need_ext) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) { mn[m] = jmin(mn[m], fj[m]); mx[m] = jmax(mx[m], fj[m]); }
+            }
+            const int oj_own = a.orders[j];
+            int oi, oj;
+            if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
+            else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
+            else { oi = oi_own; oj = oj_own; }
+            const int keep_i = (oi >= 2 && oi <= RDEG + 1) ? basis_count(D, oi - 1) : 0;
+            const int keep_j = (oj >= 2 && oj <= RDEG + 1) ? basis_count(D, oj - 1) : 0;
+            T hx[D], pi[BR], pj[BR];
+#pragma unroll
+            for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
+            recon_basis<D, RDEG, T>(hx, pi);
+#pragma unroll
+            for (int d = 0; d < D; ++d) hx[d] = T(-0.5) * dk[d];
+            recon_basis<D, RDEG, T>(hx, pj);
+#pragma unroll
+            for (int b = 0; b < BR; ++b) {
+                if (b >= keep_i) pi[b] = T(0);
+                if (b >= keep_j) pj[b] = T(0);
+            }
+            const T *gjp = a.grad + int64_t(j) * (BR * M);
+            T fij[M], fji[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                T si = gi[0][m] * pi[0];
+                T sj = gjp[m] * pj[0];
+#pragma unroll
+                for (int b = 1; b < BR; ++b) {
+                    si = si + gi[b][m] * pi[b];
+                    sj = sj + gjp[b * M + m] * pj[b];
+                }
+                fij[m] = fi[m] + si;
+                fji[m] = fj[m] + sj;
+            }
+            T Fij[D][M], Fji[D][M], lij[D], lji[D];
+            flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij);
+            flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji);
+            T t[M];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const bool pos = dk[d] > T(0);
+                const T sdd = pos ? jmax(lij[d], lji[d]) : jmax(lji[d], lij[d]);
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const T fL = pos ? fij[m] : fji[m];
+                    const T fR = pos ? fji[m] : fij[m];
+                    const T FL = pos ? Fij[d][m] : Fji[d][m];
+                    const T FR = pos ? Fji[d][m] : Fij[d][m];
+                    const T Fn = T(0.5) * ((FL + FR) - sdd * (fR - fL));
+                    const T dF = Fn - Fi[d][m];
+                    t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < M; ++m) acc[m].add(t[m]);
+        }
+    } else if (need_ext) {
+        for (int k = 0; k < cnt; ++k) {
+            const int32_t j = a.g.nidx[int64_t(k) * np + i];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                T fj = a.U[int64_t(j) * M + m];
+                mn[m] = jmin(mn[m], fj);
+                mx[m] = jmax(mx[m], fj);
+            }
+        }
+    }
+    T Kv[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        Kv[m] = -(T(2) * acc[m].value());
+        a.K[i * M + m] = Kv[m];
+    }
+    if (!a.form_next) return;
+    // _stage_predictor! for the next candidate
+    T Y[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
+    for (int j = 0; j < a.n_prev; ++j) {
+        if (a.hE[j] != T(0)) {
+            const T h = a.hE[j];
+            if (j == a.self_slot) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * Kv[m];
+            } else {
+#pragma unroll
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KE[j][i * M + m];
+            }
+        }
+        if (a.hI[j] != T(0)) {
+            const T h = a.hI[j];
+#pragma unroll
+            for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KI[j][i * M + m];
+        }
+    }
+    if (a.implicit_mode) {
+        T KIo[M];
+        implicit_part<T, D, M, PDE>(a, Y, KIo);
+#pragma unroll
+        for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
+    if (!a.check) return;
+    T cand[M];
+    if (a.check_substep) {
+        if (a.KIs) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * (Kv[m] + a.KIs[i * M + m]);
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * Kv[m];
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < M; ++m) cand[m] = Y[m];
+    }
+    const bool adm = admissible<T, D, M, PDE>(a.ph, cand);
+    bool flag = !adm;
+    if (a.sc.criterion == HCC_MOOD_ONLY) flag = true;
+    else if (a.sc.criterion == HCC_MOOD_U1 && !flag) {
+        const T dl = a.delta, d3 = dl * dl * dl;
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+            if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - dl || cand[m] > mx[m] + dl)) flag = true;
+    }
+    a.triggered[i] = flag;
+    a.inadm[i] = !adm;
+}
+
+// form_candidate!(ts, eq, pg, 1, dt, t) (TimeSteppers.jl:365-397) for stage 1: Y_1 = Uⁿ (interior),
+// the start-of-step state (boundary), then the implicit part. Boundary conditions follow in their own kernel.
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void k_stage1(const StageArgs<T> a) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.g.n) return;
+    T Y[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
+    if (!a.g.bnd[i] && a.implicit_mode) {
+        T KIo[M];
+        implicit_part<T, D, M, PDE>(a, Y, KIo);
+#pragma unroll
+        for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
+}
+
+// _cfl_weights_body! (ParticleGrids.jl:439-450) + the minimum over particles (:414).
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void k_cfl(const StageArgs<T> a, unsigned long long *dt_bits) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double dti = INFINITY;
+    if (i < a.g.n && !a.g.bnd[i]) {
+        const int cnt = a.g.cnt[i];
+        if (cnt > 0) {
+            const int64_t np = a.g.npad;
+            T Li[D];
+            speeds<T, D, M, PDE>(a.ph, a.U + i * M, Li);
+            T sum_c = T(0);
+            for (int k = 0; k < cnt; ++k) {
+                const int32_t j = a.g.nidx[int64_t(k) * np + i];
+                T Lj[D];
+                speeds<T, D, M, PDE>(a.ph, a.U + int64_t(j) * M, Lj);
+                T dot = T(0);
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    T pr = fabs(a.g.dw[(int64_t(k) * D + d) * np + i]) * jmax(Li[d], Lj[d]);
+                    dot = (d == 0) ? pr : dot + pr;
+                }
+                sum_c = sum_c + dot;
+            }
+            if (sum_c > floatmin_of<T>()) dti = double((T(1) / T(D)) / sum_c);
+        }
+    }
+    // positive doubles order like their bit patterns
+    unsigned long long b = __double_as_longlong(dti);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long ob = __shfl_down_sync(0xffffffffu, b, o);
+        b = ob < b ? ob : b;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMin(dt_bits, b);
+}
+
+// ----------------------------------------------------------------------------------- launchers / registry
+template <typename T, int D, int M, int PDE, int RDEG>
+struct StageInst {
+    static unsigned grid(int64_t n, int bs) { return unsigned((n + bs - 1) / bs); }
+    static void gather(const void *args, int64_t n, cudaStream_t s) {
+        k_gather<T, D, M, PDE, RDEG><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+    }
+    static void flux(const void *args, int64_t n, cudaStream_t s) {
+        k_flux<T, D, M, PDE, RDEG><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+    }
+    static void stage1(const void *args, int64_t n, cudaStream_t s) {
+        k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+    }
+    static void cfl(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s) {
+        k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args), dt_bits);
+    }
+    static const StageOps *ops() {
+        static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl, nullptr};
+        return &o;
+    }
+};
+
+template <typename T, int RDEG>
+const StageOps *lookup_rdeg(int D, int M, int pde) {
+    if (pde == HCC_PDE_EULER) {
+        if (D == 1 && M == 3) return StageInst<T, 1, 3, HCC_PDE_EULER, RDEG>::ops();
+        if (D == 2 && M == 4) return StageInst<T, 2, 4, HCC_PDE_EULER, RDEG>::ops();
+        if (D == 3 && M == 5) return StageInst<T, 3, 5, HCC_PDE_EULER, RDEG>::ops();
+        return nullptr;
+    }
+    if (pde == HCC_PDE_BGK) {
+        if (D == 2 && M == 16) return StageInst<T, 2, 16, HCC_PDE_BGK, RDEG>::ops();
+        if (D == 1 && M == 2) return StageInst<T, 1, 2, HCC_PDE_BGK, RDEG>::ops();
+        return nullptr;
+    }
+    if (D == 1 && M == 1) return StageInst<T, 1, 1, HCC_PDE_ADVECTION, RDEG>::ops();
+    if (D == 2 && M == 1) return StageInst<T, 2, 1, HCC_PDE_ADVECTION, RDEG>::ops();
+    if (D == 3 && M == 1) return StageInst<T, 3, 1, HCC_PDE_ADVECTION, RDEG>::ops();
+    if (D == 2 && M == 2) return StageInst<T, 2, 2, HCC_PDE_ADVECTION, RDEG>::ops();
+    return nullptr;
+}
+
+
+}  // namespace hcc

@@ -1,0 +1,200 @@
+/*
+ * hcc.h — C ABI of the GB300 explicit right-hand-side library (libhcc_gb300.so).
+ *
+ * The library runs the hot path of the meshless solver HyperCloudCore.jl on one GPU:
+ * cell-list neighbour search -> MLS moment/divergence weights -> MUSCL reconstruction ->
+ * Rusanov flux -> streamed divergence -> SSP-RK / IMEX stage update with MOOD -> CFL time step.
+ *
+ * Conventions
+ *  - Every call returns an hcc_status; hcc_last_error() gives the message of the last failure
+ *    of a context (a static string for a NULL context).
+ *  - Pointers are HOST pointers; the caller's buffers are read or written only during the call.
+ *  - Particle-indexed host arrays use 0-based particle numbers in the caller's order; the library
+ *    keeps that numbering (it is the reference's Morton numbering when the caller reorders first).
+ *  - Positions and states are row-major: pos[i*D + d], U[i*M + m].
+ *  - One CUDA stream per context. A context is not thread-safe; distinct contexts are independent.
+ *  - All device memory is owned by the context and sized at hcc_create / hcc_upload_cloud.
+ *
+ * Reference interfaces each entry point replaces are cited as file:line of HyperCloudCore.jl.
+ */
+#ifndef HCC_GB300_H
+#define HCC_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HCC_ABI_VERSION 1
+#define HCC_MAX_DIM 3
+#define HCC_MAX_VARS 16
+#define HCC_MAX_TAGS 16
+
+typedef enum {
+    HCC_OK = 0,
+    HCC_ERR_INVALID = 1,     /* bad argument or configuration (ArgumentError in the reference) */
+    HCC_ERR_CAPACITY = 2,    /* particle or neighbour count above the reservation (CapacityError) */
+    HCC_ERR_CUDA = 3,        /* a CUDA call failed */
+    HCC_ERR_STATE = 4,       /* call out of order (e.g. a step before the neighbour search) */
+    HCC_ERR_NONFINITE = 5,   /* non-finite time step or state where one is required */
+    HCC_ERR_TIMEOUT = 6,     /* an iteration cap was reached (MOOD fixed point) */
+    HCC_ERR_UNSUPPORTED = 7  /* a combination this build does not instantiate */
+} hcc_status;
+
+/* Physics modules compiled into the kernels (HyperbolicPDE subtypes of the reference). */
+typedef enum {
+    HCC_PDE_ADVECTION = 0,   /* diagonal linear advection: F_d(U)_m = c[d][m] U_m (test/PDEs/linear_advection.jl:24-32) */
+    HCC_PDE_EULER = 1,       /* compressible Euler, ideal gas, M = D + 2 (not in the reference; PAD = rho>0, p>0, finite) */
+    HCC_PDE_BGK = 2          /* discrete-velocity kinetic relaxation: advection with speeds v_k + implicit
+                                Maxwellian relaxation (test/kinetic_source.jl:194-231) */
+} hcc_pde_kind;
+
+typedef enum {
+    HCC_FP64 = 0,            /* plain FP64 path */
+    HCC_FP32 = 1             /* FP32 bulk: states, reconstruction, fluxes and updates in FP32, Kahan-compensated
+                                divergence; MLS assembly and Cholesky stay FP64 */
+} hcc_precision;
+
+typedef enum {               /* MOOD criterion (src/TimeStepping/MOOD.jl) */
+    HCC_MOOD_NONE = 0,       /* NoMOOD: MOOD() */
+    HCC_MOOD_U1 = 1,         /* MOODu1(delta): relaxed DMP + PAD */
+    HCC_MOOD_PAD = 2,        /* MOODPAD(): admissibility only */
+    HCC_MOOD_ONLY = 3        /* OnlyMOOD(): flags everything (testing) */
+} hcc_mood_criterion;
+
+typedef enum {               /* MOOD strategy (interface orders), MOOD.jl:20-28, :76-87 */
+    HCC_EPD_NONE = 0,        /* NoStrategy: own orders (o_i, o_j) */
+    HCC_EPD0 = 1,            /* (o_i, o_j) */
+    HCC_EPD1 = 2,            /* min(o_i, o_j) on both sides */
+    HCC_EPD2 = 3             /* min over N(i) u N(j) on both sides */
+} hcc_mood_strategy;
+
+typedef enum {               /* src/TimeStepping/ButcherTableaus.jl */
+    HCC_TAB_RK1_EULER = 0, HCC_TAB_RK2_SSP = 1, HCC_TAB_RK2_RALSTON = 2, HCC_TAB_RK3_SSP = 3,
+    HCC_TAB_RK4_CLASSICAL = 4, HCC_TAB_RK4_SSP = 5,
+    HCC_TAB_IMEX_EULER = 6, HCC_TAB_IMEX_ARS233 = 7, HCC_TAB_IMEX_ARS222 = 8,
+    HCC_TAB_IMEX_PRSSP3 = 9, HCC_TAB_IMEX_SSP2332 = 10
+} hcc_tableau;
+
+typedef enum {               /* src/Grid/BoundaryConditions.jl */
+    HCC_BC_KEEP = 0,         /* no condition for the tag: the particle keeps its start-of-step state */
+    HCC_BC_DIRICHLET = 1,    /* FixedDirichlet */
+    HCC_BC_OUTFLOW = 2       /* OutflowBC: nearest resolved donor, <= 5 passes */
+} hcc_bc_kind;
+
+/* Plain-old-data configuration. Zero-initialise, then fill. */
+typedef struct {
+    int32_t abi_version;               /* HCC_ABI_VERSION */
+    int32_t dim;                       /* D in {1,2,3} */
+    int32_t n_vars;                    /* M */
+    int32_t pde;                       /* hcc_pde_kind */
+    int32_t precision;                 /* hcc_precision */
+    int32_t muscl_order;               /* MUSCL max_order in {1,2,3} (MUSCL.jl:116) */
+    int32_t div_order;                 /* MUSCL div_order (0 = adaptive) */
+    int32_t mood_criterion;            /* hcc_mood_criterion */
+    int32_t mood_strategy;             /* hcc_mood_strategy */
+    int32_t tableau;                   /* hcc_tableau */
+    int32_t mood_substeps;             /* 1: check the Euler substeps of SSP tableaus (default of the reference) */
+    int32_t periodic[HCC_MAX_DIM];     /* per axis */
+    int32_t bc_by_tag[HCC_MAX_TAGS];   /* hcc_bc_kind per boundary tag 1..16 (index tag-1) */
+    int32_t max_mood_iterations;       /* cap of the MOOD fixed point per checkpoint (0 -> 64) */
+    int32_t reserved_i[8];
+    double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
+    double  radius;                    /* support radius R of ExponentialWeightFunction */
+    double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */
+    double  canvas_min[HCC_MAX_DIM];   /* box of the cell list (ghost canvas) */
+    double  canvas_max[HCC_MAX_DIM];
+    double  domain_min[HCC_MAX_DIM];   /* physical box (periodic wrap length = domain_max - domain_min) */
+    double  domain_max[HCC_MAX_DIM];
+    double  mood_delta;                /* delta of MOODu1 */
+    double  velocity[HCC_MAX_DIM][HCC_MAX_VARS]; /* advection speeds c[d][m]; BGK: kinetic speeds v_k,d */
+    double  gamma;                     /* Euler adiabatic index */
+    double  bgk_epsilon;               /* BGK relaxation time */
+    double  bgk_macro_velocity[HCC_MAX_DIM]; /* BGK macro flux: scalar linear advection with this velocity */
+    double  bgk_coefficient;           /* Maxwellian coefficient of the single macro moment (1/NK) */
+    double  bgk_interior_factor;       /* RelaxationSourceTerm interior_factor (default D) */
+    double  reserved_d[8];
+} hcc_config;
+
+typedef struct {
+    int64_t n_particles;
+    int64_t n_interior;
+    int32_t max_neighbours;
+    int32_t min_neighbours_interior;
+    int64_t total_neighbours;
+    int64_t mood_iterations;           /* MOOD recompute passes in the last step */
+    int64_t mood_flagged;              /* particles that dropped an order in the last step (mood_flags) */
+    int64_t inadmissible;              /* mood_inadmissible(ts) of the last step (TimeSteppers.jl:272) */
+    int64_t kernel_launches;           /* kernels launched by the last hcc_step / hcc_time_step */
+    int64_t steps;                     /* steps taken by the context */
+} hcc_counters;
+
+typedef struct hcc_ctx hcc_ctx;
+
+/* Fills *cfg with the reference's defaults (MUSCL 2, SSP-RK3, EPD1/MOODu1, alpha 1, mood_substeps 1). */
+void hcc_config_defaults(hcc_config *cfg);
+
+/* Context = GeneralRKTimeStepper(pde, MUSCL(...; storage), MOOD(...), tableau) (TimeSteppers.jl:195-229)
+   + the ParticleGrid metadata (ParticleGrids.jl:221-279). `capacity` reserves particles (MemoryBudget.jl:110). */
+hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out);
+hcc_status hcc_destroy(hcc_ctx *ctx);
+const char *hcc_last_error(const hcc_ctx *ctx);
+const char *hcc_status_string(hcc_status s);
+
+/* Device copy of the cloud: device_grid(ArrayType, pg) (DeviceAdapt.jl:73). pos: N*D, is_boundary: N (0/1),
+   tags: N, volumes: N (may be NULL -> prod(dx)). */
+hcc_status hcc_upload_cloud(hcc_ctx *ctx, int64_t n, const double *pos, const uint8_t *is_boundary,
+                            const int32_t *tags, const double *volumes);
+
+/* Neighbour search: (nd::NeighborData)(pg) (NeighborLogic.jl:336-375) with the cell list of
+   build_global_bins! (:217-237). Slot-major device layout (:283). */
+hcc_status hcc_build_neighbours(hcc_ctx *ctx);
+
+/* Neighbour lists in the reference's row-major order (ranges as counts, NeighborLogic.jl:282):
+   counts[N]; then idx/w/dist of total_neighbours slots (dist: total*D). Any output may be NULL. */
+hcc_status hcc_download_neighbours(hcc_ctx *ctx, int32_t *counts, int32_t *idx, double *w, double *dist);
+
+/* prepare_geometry!(muscl, pg) (MUSCL.jl:172-187): cached inverse moments, ok flags, per-slot
+   divergence weights (update_divergence_weights!, MUSCL.jl:197-223) and the outflow donor map. */
+hcc_status hcc_prepare_geometry(hcc_ctx *ctx);
+
+/* Per-slot divergence weights (dweights), row-major like hcc_download_neighbours: total*D. ok_r/ok_d: N each. */
+hcc_status hcc_download_geometry(hcc_ctx *ctx, double *dweights, uint8_t *ok_recon, uint8_t *ok_div);
+
+/* pg.rhos (N*M). FP32 contexts convert. */
+hcc_status hcc_upload_state(hcc_ctx *ctx, const double *U);
+hcc_status hcc_download_state(hcc_ctx *ctx, double *U);
+hcc_status hcc_upload_state_f32(hcc_ctx *ctx, const float *U);
+hcc_status hcc_download_state_f32(hcc_ctx *ctx, float *U);
+
+/* get_time_step(pg, eq, interp) (ParticleGrids.jl:386-415): CFL number 1, cached slot weights. */
+hcc_status hcc_time_step(hcc_ctx *ctx, double *dt_out);
+
+/* One explicit right-hand side K = -2 div + sources at the current state, all particles at full order:
+   compute_explicit_rhs!(..., full = true) (TimeSteppers.jl:312-356). K: N*M. */
+hcc_status hcc_compute_rhs(hcc_ctx *ctx, double *K);
+
+/* One time step: (ts::GeneralRKTimeStepper)(eq, pg, t, dt) (TimeSteppers.jl:531-577). */
+hcc_status hcc_step(hcc_ctx *ctx, double t, double dt);
+
+/* pg.core.particle_orders (N) and mood_flags(ts) (TimeSteppers.jl:258) of the last step. */
+hcc_status hcc_download_orders(hcc_ctx *ctx, int32_t *orders);
+hcc_status hcc_download_mood_flags(hcc_ctx *ctx, uint8_t *flags);
+
+hcc_status hcc_get_counters(hcc_ctx *ctx, hcc_counters *out);
+
+/* total_mass(pg) (Volumes.jl:103-107) accumulated in FP64 on the device: out[M]. */
+hcc_status hcc_total_mass(hcc_ctx *ctx, double *out);
+
+/* Waits for the context's stream. */
+hcc_status hcc_synchronize(hcc_ctx *ctx);
+
+/* The context's CUDA stream (cudaStream_t) so a caller can time or order work on it. */
+void *hcc_stream(hcc_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HCC_GB300_H */

@@ -1,0 +1,63 @@
+"""The C-ABI library loads and exports every entry point of include/hcc.h; host-side checks that need no GPU."""
+import ctypes as C
+import re
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "hcc.h").read_text()
+    return sorted(set(re.findall(r"\b(hcc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_entry_points():
+    names = _declared_symbols()
+    for required in ("hcc_create", "hcc_destroy", "hcc_upload_cloud", "hcc_build_neighbours", "hcc_prepare_geometry",
+                     "hcc_upload_state", "hcc_time_step", "hcc_step", "hcc_download_state", "hcc_last_error"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(cuda_lib):
+    for name in _declared_symbols():
+        assert hasattr(cuda_lib, name), name
+
+
+def test_status_strings_and_defaults(hcc, cuda_lib):
+    assert cuda_lib.hcc_status_string(0) == b"HCC_OK"
+    assert cuda_lib.hcc_status_string(2) == b"HCC_ERR_CAPACITY"
+    assert cuda_lib.hcc_last_error(None) == b"null context"
+    cfg_c = hcc.HccConfig()
+    cuda_lib.hcc_config_defaults(C.byref(cfg_c))
+    cfg_py = hcc.config_defaults()
+    assert bytes(cfg_c) == bytes(cfg_py)        # the Python twin matches the C defaults field for field
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("dim", 4, 1), ("n_vars", 0, 1), ("muscl_order", 5, 7), ("radius", 0.0, 1), ("abi_version", 99, 1),
+])
+def test_create_rejects_bad_configs_before_touching_the_gpu(hcc, cuda_lib, field, value, status):
+    cfg = hcc.config_defaults()
+    cfg.radius = 0.025
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    st = cuda_lib.hcc_create(C.byref(cfg), 0, C.byref(h))
+    assert st == status
+    assert cuda_lib.hcc_last_error(h)            # a message is available
+    cuda_lib.hcc_destroy(h)
+
+
+def test_euler_needs_matching_n_vars(hcc, cuda_lib):
+    cfg = hcc.config_defaults()
+    cfg.radius, cfg.pde, cfg.dim, cfg.n_vars = 0.025, 1, 2, 3
+    h = C.c_void_p()
+    assert cuda_lib.hcc_create(C.byref(cfg), 0, C.byref(h)) == 1
+    assert b"n_vars" in cuda_lib.hcc_last_error(h)
+    cuda_lib.hcc_destroy(h)
+
+
+def test_missing_library_fails_loudly(hcc, tmp_path):
+    with pytest.raises(hcc.HCCError):
+        hcc.load_library(tmp_path / "nope.so")
