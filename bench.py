@@ -1,0 +1,386 @@
+"""Throughput of the explicit right-hand-side path: point-updates/s per RK stage.
+
+Workload (default): 2-D compressible Euler, gamma 1.4, on [0,1]^2, jittered lattice h = 1e-3 (±0.25h), about 1.0M
+interior particles plus ghosts; four-quadrant Riemann initial state split at (0.5, 0.5); transmissive (outflow)
+boundaries; MUSCL order 2 with the MLS divergence fit of order 2; MOOD (EPD1, MOODu1 with delta = 1e-4 h^2);
+Rusanov flux; SSP-RK3; dt = 0.4 x the CFL step at the initial state. Synthetic, seeded inputs (no dataset).
+
+`value` is the FP32 bulk path (the headline), measured with the state resident in HBM; `e2e` is the same metric
+through the C ABI with host buffers (state uploaded from pinned memory and downloaded every step); `fp64_plain` is
+the plain FP64 path on the same cloud. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's
+CPU path) on a bounded sample of the same workload. `--impl reference` runs only that CPU path.
+
+Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under torch.distributed.run (one rank per GPU,
+independent replicas: the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "hypercloudcore.jl_gb300"
+METRIC = "point-updates/s per RK stage, FP32+learned vs plain FP64 on 1 GB300 at equal L1"
+STAGES = 3
+
+
+def _load(name, path, pkg_dir=None):
+    if name in sys.modules:
+        return sys.modules[name]
+    kw = {"submodule_search_locations": [str(pkg_dir)]} if pkg_dir else {}
+    spec = importlib.util.spec_from_file_location(name, path, **kw)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def package():
+    return _load("hcc_gb300", PKG / "__init__.py", PKG)
+
+
+# --------------------------------------------------------------------------------------------- workload
+WORKLOADS = {
+    # name: (dim, h, description)
+    "euler2d_quadrant_1M": (2, 1e-3, "2-D Euler quadrant Riemann, h=1e-3 (1.0M interior), MUSCL2+MOOD, SSP-RK3"),
+    "euler2d_quadrant_250k": (2, 2e-3, "2-D Euler quadrant Riemann, h=2e-3 (250k interior), MUSCL2+MOOD, SSP-RK3"),
+}
+
+
+def quadrant_state(cloud, gamma=1.4):
+    x, y = cloud.pos[:, 0], cloud.pos[:, 1]
+    vals = {"NE": (1.5, 0.0, 0.0, 1.5), "NW": (0.5323, 1.206, 0.0, 0.3),
+            "SW": (0.138, 1.206, 1.206, 0.029), "SE": (0.5323, 0.0, 1.206, 0.3)}
+    rho, u, v, p = (np.empty(cloud.n) for _ in range(4))
+    for key, (r0, u0, v0, p0) in vals.items():
+        sel = ((x >= 0.5) if key[1] == "E" else (x < 0.5)) & ((y >= 0.5) if key[0] == "N" else (y < 0.5))
+        rho[sel], u[sel], v[sel], p[sel] = r0, u0, v0, p0
+    E = p / (gamma - 1) + 0.5 * rho * (u * u + v * v)
+    return np.ascontiguousarray(np.stack([rho, rho * u, rho * v, E], axis=1))
+
+
+def make_workload(hcc, name):
+    D, h, _ = WORKLOADS[name]
+    cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, jitter=0.25 * h, seed=42)
+    U0 = quadrant_state(cloud)
+    return cloud, U0, h
+
+
+def make_cfg(hcc, cloud, h, precision):
+    return hcc.make_config(hcc.Euler(2, 1.4), cloud, scheme=hcc.MUSCL(2, 2),
+                           mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), tableau="RK3_SSP",
+                           bc_map={t: hcc.BC_OUTFLOW for t in (1, 2, 3, 4)}, precision=precision)
+
+
+# --------------------------------------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def recorded_traffic():
+    """Per-point-stage DRAM bytes of the flux kernel from the committed ncu summary (profiles/traffic.txt)."""
+    p = ROOT / "profiles" / "traffic.txt"
+    out = {}
+    if p.exists():
+        for ln in p.read_text().splitlines():
+            ln = ln.strip()
+            if ln and not ln.startswith("#"):
+                k, v = ln.split()[:2]
+                out[k] = float(v)
+    return out
+
+
+def algorithmic_bytes(K, D, M, Br, Bd, s):
+    """Bytes per point and RK stage that the two passes must move (the model of the measurement plan):
+    flux pass 4K + 8D + 8 Bd^2 + s M (5 + Br); gather pass 4K + 8D + 8 Br^2 + s M (1 + Br)."""
+    flux = 4 * K + 8 * D + 8 * Bd * Bd + s * M * (5 + Br)
+    gather = 4 * K + 8 * D + 8 * Br * Br + s * M * (1 + Br)
+    return flux, gather
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------------------------- GPU arm
+def time_device_steps(hcc, ctx, dt, steps, world):
+    """K steps with the state resident in HBM, CUDA events on the context's stream, max over ranks."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.counters()["kernel_launches_total"]
+    barrier(world)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.step(0.0, dt)
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    launches = ctx.counters()["kernel_launches_total"] - launches0
+    return reduce_max(ms, world), launches
+
+
+def time_e2e(hcc, ctx, U_host, dt, steps, world, f32):
+    """The same steps through the C ABI with host buffers: upload (pinned) -> step -> download, every step."""
+    import torch
+    dtype = torch.float32 if f32 else torch.float64
+    pinned = torch.empty(U_host.shape, dtype=dtype, pin_memory=True)
+    pinned.copy_(torch.from_numpy(U_host.astype(np.float32 if f32 else np.float64)))
+    host = pinned.numpy()
+    out = np.empty_like(host)
+    barrier(world)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.upload_state(host)
+        ctx.step(0.0, dt)
+        out[...] = ctx.download_state(dtype=host.dtype)
+    ctx.synchronize()
+    el = time.perf_counter() - t0
+    barrier(world)
+    return reduce_max(el, world), host.nbytes, out.nbytes
+
+
+def run_gpu(args):
+    world, rank, local = dist_setup()
+    hcc = package()
+    if not hcc.LIB_PATH.exists():
+        _load("hcc_gb300_build", PKG / "build.py").build()
+    import torch
+    torch.cuda.set_device(local)
+    cloud, U0, h = make_workload(hcc, args.workload)
+    n_int = cloud.n_interior
+    results = {}
+    for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
+        f32 = prec == "fp32"
+        ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+        ctx.upload_cloud(cloud)
+        ctx.build_neighbours()
+        ctx.prepare_geometry()
+        ctx.upload_state(U0.astype(np.float32) if f32 else U0)
+        dt = 0.4 * ctx.time_step()
+        for _ in range(args.warmup):
+            ctx.step(0.0, dt)
+        ctx.upload_state(U0.astype(np.float32) if f32 else U0)
+        ctx.set_profiling(True)
+        ctx.kernel_times(reset=True)
+        with ClockSampler(local) as clk:
+            ms, launches = time_device_steps(hcc, ctx, dt, args.steps, world)
+        ctx.set_profiling(False)
+        kt = ctx.kernel_times(reset=True)
+        cnt = ctx.counters()
+        e2e_s, h2d, d2h = time_e2e(hcc, ctx, U0, dt, args.steps, world, f32)
+        results[prec] = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt,
+                         "e2e_s": e2e_s, "h2d": h2d, "d2h": d2h, "dt": dt}
+        ctx.close()
+    r = results["fp32"]
+    units = n_int * STAGES * args.steps * world
+    value = units / (r["ms"] / 1e3)
+    cnt = r["counters"]
+    K = cnt["total_neighbours"] / max(cloud.n, 1)
+    flux_b, gather_b = algorithmic_bytes(K, 2, 4, 2, 3, 4)
+    peak, peak_kind = measured_peaks()
+    kt = r["kt"]
+    flux_ms = kt["flux_ms"] / max(kt["flux_launches"], 1)
+    achieved = flux_b * n_int / (flux_ms / 1e3) / 1e9
+    traffic = recorded_traffic().get("flux_f32_euler2d_bytes_per_point_stage")
+    line = {
+        "metric": METRIC, "value": value, "unit": "point-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
+                   "n_particles": cloud.n, "n_interior": n_int, "mean_neighbours": K, "stages_per_step": STAGES,
+                   "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": False,
+                   "l2": "inputs larger than L2 (per-slot arrays ~0.5 GB)", "parallelism": f"replicas x{world}",
+                   "dt": r["dt"]},
+        "gpu_launches": r["launches"],
+        "e2e": {"value": units / r["e2e_s"], "unit": "point-updates/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "roofline": {"bound": "hbm", "kernel": "k_flux<float,2,4,EULER,1>", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": (traffic * n_int) if traffic else None,
+                     "algorithmic_bytes_per_point_stage": {"flux": flux_b, "gather": gather_b},
+                     "flux_ms_per_launch": flux_ms,
+                     "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
+                     "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"]},
+        "clocks": r["clocks"],
+        "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"]},
+    }
+    if "fp64" in results:
+        r64 = results["fp64"]
+        line["fp64_plain"] = {"value": units / (r64["ms"] / 1e3), "ms_per_step": r64["ms"] / args.steps,
+                              "flux_ms_per_launch": r64["kt"]["flux_ms"] / max(r64["kt"]["flux_launches"], 1),
+                              "gather_ms_per_launch": r64["kt"]["gather_ms"] / max(r64["kt"]["gather_launches"], 1),
+                              "e2e": units / r64["e2e_s"], "clocks": r64["clocks"]}
+        line["fp32_over_fp64"] = line["value"] / line["fp64_plain"]["value"]
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(hcc, cloud, U0, h, args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------------- CPU (reference) arm
+def cpu_baseline(hcc, cloud, U0, h, steps):
+    """The oracle (C++ restatement of the reference CPU path, OpenMP on all host cores) on a bounded sample:
+    `steps` steps of the same cloud after one warm-up step."""
+    orc = _load("hcc_oracle_py", ROOT / "oracle" / "oracle.py")
+    abi = sys.modules["hcc_gb300._abi"]
+    cores = os.cpu_count() or 1
+    orc.load(abi)
+    orc.OracleContext.set_threads(cores)
+    o = orc.OracleContext(make_cfg(hcc, cloud, h, "fp64"), abi)
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    o.prepare_geometry()
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    o.step(0.0, dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step(0.0, dt)
+    el = time.perf_counter() - t0
+    v = cloud.n_interior * STAGES * steps / el
+    o.close()
+    return {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} SSP-RK3 step(s) of the full {cloud.n}-particle cloud after 1 warm-up step, FP64"}
+
+
+def run_reference(args):
+    world, rank, local = (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+                          int(os.environ.get("LOCAL_RANK", "0")))
+    if rank != 0:
+        return
+    hcc = package()
+    cloud, U0, h = make_workload(hcc, args.workload)
+    steps = max(1, min(args.steps, args.cpu_steps))
+    base = cpu_baseline(hcc, cloud, U0, h, steps)
+    line = {"metric": METRIC, "value": base["value"], "unit": "point-updates/s", "n_gpus": world, "steps": steps,
+            "warmup": 1, "ms_per_step": cloud.n_interior * STAGES / base["value"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
+                       "n_particles": cloud.n, "n_interior": cloud.n_interior},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "point-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "Julia is not available on this box; the reference CPU path is its C++ restatement (oracle/)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="euler2d_quadrant_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp32-only", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -339,6 +339,14 @@ class Context:
     def synchronize(self):
         self._check(self.lib.hcc_synchronize(self._h), "hcc_synchronize")
 
+    def set_profiling(self, enable: bool = True):
+        self._check(self.lib.hcc_set_profiling(self._h, int(bool(enable))), "hcc_set_profiling")
+
+    def kernel_times(self, reset: bool = False) -> dict:
+        t = _abi.HccKernelTimes()
+        self._check(self.lib.hcc_get_kernel_times(self._h, C.byref(t), int(bool(reset))), "hcc_get_kernel_times")
+        return t.as_dict()
+
     def stream(self) -> int:
         return int(self.lib.hcc_stream(self._h) or 0)
 

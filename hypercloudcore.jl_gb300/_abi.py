@@ -52,8 +52,17 @@ class HccCounters(C.Structure):
         ("n_particles", C.c_int64), ("n_interior", C.c_int64), ("max_neighbours", C.c_int32),
         ("min_neighbours_interior", C.c_int32), ("total_neighbours", C.c_int64), ("mood_iterations", C.c_int64),
         ("mood_flagged", C.c_int64), ("inadmissible", C.c_int64), ("kernel_launches", C.c_int64),
-        ("steps", C.c_int64),
+        ("steps", C.c_int64), ("kernel_launches_total", C.c_int64),
     ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class HccKernelTimes(C.Structure):
+    _fields_ = [("gather_ms", C.c_double), ("gather_launches", C.c_int64), ("flux_ms", C.c_double),
+                ("flux_launches", C.c_int64), ("recompute_ms", C.c_double), ("recompute_launches", C.c_int64),
+                ("steps", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -88,6 +97,8 @@ PROTOTYPES = [
     ("hcc_download_mood_flags", C.c_int, [P, _u8p]),
     ("hcc_get_counters", C.c_int, [P, C.POINTER(HccCounters)]),
     ("hcc_total_mass", C.c_int, [P, _dp]),
+    ("hcc_set_profiling", C.c_int, [P, C.c_int]),
+    ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_synchronize", C.c_int, [P]),
     ("hcc_stream", P, [P]),
 ]

@@ -193,6 +193,7 @@ struct hcc_ctx {
     int32_t *blist = nullptr, *bsrc = nullptr; int64_t nbnd = 0;
     // state (element type double or float)
     void *rhos = nullptr, *cand = nullptr, *grad = nullptr;
+    void *xfer = nullptr;                        // n*M doubles: staging of host-precision conversions
     void *Y[HCC_MAX_STAGES] = {}, *KE[HCC_MAX_STAGES] = {}, *KI[HCC_MAX_STAGES] = {};
     int8_t *orders = nullptr, *nbmin = nullptr;
     uint8_t *triggered = nullptr, *changed = nullptr, *dirty = nullptr, *scratch = nullptr, *trig_step = nullptr,
@@ -202,7 +203,43 @@ struct hcc_ctx {
     double *d_mass = nullptr;
     bool have_cloud = false, have_nb = false, have_geom = false, have_state = false;
     // statistics
-    int64_t launches = 0, mood_iters = 0, flagged = 0, inadmissible = 0, steps = 0;
+    int64_t launches = 0, mood_iters = 0, flagged = 0, inadmissible = 0, steps = 0, launches_total = 0;
+    int32_t min_nb_interior = 0;
+    // profiling: event pairs around gather (kind 0) and flux (kind 1) launches of the current step
+    int prof = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_kind;
+    size_t ev_used = 0;
+    hcc_kernel_times times{};
+
+    void prof_begin(int kind) {
+        if (!prof) return;
+        if (ev_used + 2 > ev_pool.size()) {
+            for (int k = 0; k < 64; ++k) {
+                cudaEvent_t e;
+                if (cudaEventCreate(&e) != cudaSuccess) { prof = 0; return; }
+                ev_pool.push_back(e);
+            }
+        }
+        if (ev_kind.size() < ev_pool.size() / 2) ev_kind.resize(ev_pool.size() / 2);
+        ev_kind[ev_used / 2] = kind;
+        cudaEventRecord(ev_pool[ev_used], stream);
+    }
+    void prof_end() {
+        if (!prof) return;
+        cudaEventRecord(ev_pool[ev_used + 1], stream);
+        ev_used += 2;
+    }
+    void prof_collect() {   // after the stream was synchronised
+        for (size_t q = 0; q < ev_used; q += 2) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev_pool[q], ev_pool[q + 1]);
+            if (ev_kind[q / 2] == 0) { times.gather_ms += ms; times.gather_launches += 1; }
+            else if (ev_kind[q / 2] == 1) { times.flux_ms += ms; times.flux_launches += 1; }
+            else { times.recompute_ms += ms; times.recompute_launches += 1; }
+        }
+        ev_used = 0;
+    }
 
     size_t esz() const { return f32 ? sizeof(float) : sizeof(double); }
 
@@ -231,7 +268,7 @@ struct hcc_ctx {
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
-        for (void **p : {&rhos, &cand, &grad}) { if (*p) cudaFree(*p); *p = nullptr; }
+        for (void **p : {&rhos, &cand, &grad, &xfer}) { if (*p) cudaFree(*p); *p = nullptr; }
         for (int s = 0; s < HCC_MAX_STAGES; ++s)
             for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
         dfree(orders); dfree(nbmin); dfree(triggered); dfree(changed); dfree(dirty); dfree(scratch); dfree(trig_step);
@@ -365,7 +402,9 @@ template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
         StageArgs<T> ga = a;
         ga.full = 0;
         ga.mask = c->changed;
+        c->prof_begin(2);
         c->ops->gather(&ga, n, c->stream);
+        c->prof_end();
         if (c->cfg.mood_strategy == HCC_EPD2) {
             launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
             c->launches += 1;
@@ -373,7 +412,9 @@ template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
         StageArgs<T> fa = a;
         fa.full = 0;
         fa.mask = c->dirty;
+        c->prof_begin(2);
         c->ops->flux(&fa, n, c->stream);
+        c->prof_end();
         apply_bcs<T>(c, fa.Ynext);
         c->launches += 2;
         if ((st = launch_check(c, "MOOD recompute")) != HCC_OK) return st;
@@ -436,13 +477,17 @@ template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
         a.check_substep = c->ratio > 0.0;
         a.h_sub = T(c->ratio * dt);
         a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
+        c->prof_begin(0);
         c->ops->gather(&a, n, c->stream);
+        c->prof_end();
         c->launches += 1;
         if (c->cfg.mood_strategy == HCC_EPD2) {
             launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
             c->launches += 1;
         }
+        c->prof_begin(1);
         c->ops->flux(&a, n, c->stream);
+        c->prof_end();
         c->launches += 1;
         apply_bcs<T>(c, a.Ynext);
         hcc_status st = launch_check(c, "stage kernels");
@@ -451,7 +496,13 @@ template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
     }
     std::swap(c->rhos, c->cand);
     ++c->steps;
-    return c->sync("step");
+    c->launches_total += c->launches;
+    hcc_status st = c->sync("step");
+    if (st == HCC_OK && c->prof) {
+        c->prof_collect();
+        c->times.steps += 1;
+    }
+    return st;
 }
 
 template <typename T> hcc_status run_rhs(hcc_ctx *c) {
@@ -478,6 +529,7 @@ template <typename T> hcc_status run_cfl(hcc_ctx *c, double *dt_out) {
     if (st != HCC_OK) return st;
     c->ops->cfl(&a, c->n, c->d_counters + 2, c->stream);
     c->launches = 1;
+    c->launches_total += 1;
     if ((st = launch_check(c, "cfl kernel")) != HCC_OK) return st;
     st = c->cuda(cudaMemcpyAsync(c->h_counters + 2, c->d_counters + 2, sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, c->stream), "dt copy");
@@ -599,6 +651,7 @@ hcc_status hcc_destroy(hcc_ctx *ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_mass);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HCC_OK;
@@ -651,6 +704,7 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
     HCC_TRY(c->valloc(c->rhos, sb, "rhos"));
     HCC_TRY(c->valloc(c->cand, sb, "candidate"));
     HCC_TRY(c->valloc(c->grad, size_t(np) * c->Br * M * c->esz(), "gradients"));
+    HCC_TRY(c->valloc(c->xfer, size_t(np) * M * sizeof(double), "conversion buffer"));
     for (int s = 0; s < c->tab.s; ++s) {
         HCC_TRY(c->valloc(c->Y[s], sb, "stage states"));
         HCC_TRY(c->valloc(c->KE[s], sb, "stage K_E"));
@@ -767,6 +821,14 @@ hcc_status hcc_build_neighbours(hcc_ctx *c) {
     a.nidx = c->nidx; a.w = c->w64; a.dist = c->dist64; a.kmax = c->kmax;
     if ((st = search_write(a, c->stream, c->err)) != HCC_OK) return st;
     HCC_TRY(c->sync("neighbour write"));
+    c->launches_total += 7;
+    {
+        std::vector<int32_t> cnt(c->n);
+        HCC_TRY(c->cuda(cudaMemcpy(cnt.data(), c->cnt, c->n * 4, cudaMemcpyDeviceToHost), "counts"));
+        int32_t mn = INT32_MAX;
+        for (int64_t i = 0; i < c->n; ++i) if (!c->h_bnd[i]) mn = std::min(mn, cnt[i]);
+        c->min_nb_interior = mn == INT32_MAX ? 0 : mn;
+    }
     c->have_nb = true;
     c->have_geom = false;
     return HCC_OK;
@@ -897,11 +959,11 @@ static hcc_status upload_state_impl(hcc_ctx *c, const void *U, int src_f32) {
     if (bool(src_f32) == bool(c->f32)) {
         HCC_TRY(c->cuda(cudaMemcpyAsync(c->rhos, U, size_t(cnt) * c->esz(), cudaMemcpyHostToDevice, c->stream), "upload state"));
     } else {
-        // convert through the candidate buffer (free between steps)
-        HCC_TRY(c->cuda(cudaMemcpyAsync(c->KE[0], U, size_t(cnt) * (src_f32 ? 4 : 8), cudaMemcpyHostToDevice, c->stream),
+        // convert through the staging buffer (n*M doubles)
+        HCC_TRY(c->cuda(cudaMemcpyAsync(c->xfer, U, size_t(cnt) * (src_f32 ? 4 : 8), cudaMemcpyHostToDevice, c->stream),
                         "upload state"));
-        if (src_f32) launch_cast_f32_to_f64(static_cast<const float *>(c->KE[0]), static_cast<double *>(c->rhos), cnt, c->stream);
-        else launch_cast_f64_to_f32(static_cast<const double *>(c->KE[0]), static_cast<float *>(c->rhos), cnt, c->stream);
+        if (src_f32) launch_cast_f32_to_f64(static_cast<const float *>(c->xfer), static_cast<double *>(c->rhos), cnt, c->stream);
+        else launch_cast_f64_to_f32(static_cast<const double *>(c->xfer), static_cast<float *>(c->rhos), cnt, c->stream);
     }
     HCC_TRY(c->sync("upload state"));
     c->have_state = true;
@@ -916,9 +978,9 @@ static hcc_status download_state_impl(hcc_ctx *c, void *U, int dst_f32) {
     if (bool(dst_f32) == bool(c->f32)) {
         HCC_TRY(c->cuda(cudaMemcpyAsync(U, c->rhos, size_t(cnt) * c->esz(), cudaMemcpyDeviceToHost, c->stream), "download state"));
     } else {
-        if (dst_f32) launch_cast_f64_to_f32(static_cast<const double *>(c->rhos), static_cast<float *>(c->cand), cnt, c->stream);
-        else launch_cast_f32_to_f64(static_cast<const float *>(c->rhos), static_cast<double *>(c->KE[0]), cnt, c->stream);
-        const void *src = dst_f32 ? c->cand : c->KE[0];
+        if (dst_f32) launch_cast_f64_to_f32(static_cast<const double *>(c->rhos), static_cast<float *>(c->xfer), cnt, c->stream);
+        else launch_cast_f32_to_f64(static_cast<const float *>(c->rhos), static_cast<double *>(c->xfer), cnt, c->stream);
+        const void *src = c->xfer;
         HCC_TRY(c->cuda(cudaMemcpyAsync(U, src, size_t(cnt) * (dst_f32 ? 4 : 8), cudaMemcpyDeviceToHost, c->stream),
                         "download state"));
     }
@@ -946,9 +1008,9 @@ hcc_status hcc_compute_rhs(hcc_ctx *c, double *K) {
     if (st != HCC_OK) return st;
     const int64_t cnt = c->n * c->M;
     if (c->f32) {
-        launch_cast_f32_to_f64(static_cast<const float *>(c->KE[0]), static_cast<double *>(c->cand), cnt, c->stream);
+        launch_cast_f32_to_f64(static_cast<const float *>(c->KE[0]), static_cast<double *>(c->xfer), cnt, c->stream);
         HCC_TRY(c->sync("rhs cast"));
-        return c->cuda(cudaMemcpy(K, c->cand, cnt * 8, cudaMemcpyDeviceToHost), "download rhs");
+        return c->cuda(cudaMemcpy(K, c->xfer, cnt * 8, cudaMemcpyDeviceToHost), "download rhs");
     }
     return c->cuda(cudaMemcpy(K, c->KE[0], cnt * 8, cudaMemcpyDeviceToHost), "download rhs");
 }
@@ -987,18 +1049,19 @@ hcc_status hcc_get_counters(hcc_ctx *c, hcc_counters *out) {
     out->max_neighbours = c->kmax;
     out->total_neighbours = c->total_nb;
     out->mood_iterations = c->mood_iters;
-    out->mood_flagged = c->flagged;
+    if (c->have_cloud && c->n) {
+        std::vector<uint8_t> ts(c->n);
+        if (cudaMemcpy(ts.data(), c->trig_step, c->n, cudaMemcpyDeviceToHost) == cudaSuccess) {
+            int64_t f = 0;
+            for (uint8_t v : ts) f += v;
+            out->mood_flagged = f;
+        }
+    }
     out->inadmissible = c->inadmissible;
     out->kernel_launches = c->launches;
     out->steps = c->steps;
-    if (c->have_nb && c->n) {
-        std::vector<int32_t> cnt(c->n);
-        if (cudaMemcpy(cnt.data(), c->cnt, c->n * 4, cudaMemcpyDeviceToHost) == cudaSuccess) {
-            int32_t mn = INT32_MAX;
-            for (int64_t i = 0; i < c->n; ++i) if (!c->h_bnd[i]) mn = std::min(mn, cnt[i]);
-            out->min_neighbours_interior = mn == INT32_MAX ? 0 : mn;
-        }
-    }
+    out->kernel_launches_total = c->launches_total;
+    out->min_neighbours_interior = c->min_nb_interior;
     return HCC_OK;
 }
 
@@ -1009,6 +1072,20 @@ hcc_status hcc_total_mass(hcc_ctx *c, double *out) {
     hcc_status st;
     HCC_TRY(c->sync("mass"));
     return c->cuda(cudaMemcpy(out, c->d_mass, c->M * sizeof(double), cudaMemcpyDeviceToHost), "mass copy");
+}
+
+hcc_status hcc_set_profiling(hcc_ctx *c, int enable) {
+    if (!c) return HCC_ERR_INVALID;
+    c->prof = enable ? 1 : 0;
+    c->ev_used = 0;
+    return HCC_OK;
+}
+
+hcc_status hcc_get_kernel_times(hcc_ctx *c, hcc_kernel_times *out, int reset) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    *out = c->times;
+    if (reset) c->times = hcc_kernel_times{};
+    return HCC_OK;
 }
 
 hcc_status hcc_synchronize(hcc_ctx *c) {

@@ -139,8 +139,9 @@ __device__ bool cholesky_moment(int B, double *N, double *U) {
     return cholesky_upper(B, N, U);
 }
 
+template <int BM>
 __device__ void chol_solve(int B, const double *U, const double *b, double *x) {
-    double y[kMaxB];
+    double y[BM];
     for (int r = 0; r < B; ++r) {
         double t = b[r];
         for (int k = 0; k < r; ++k) t = t - U[k * B + r] * y[k];
@@ -154,9 +155,10 @@ __device__ void chol_solve(int B, const double *U, const double *b, double *x) {
 }
 
 // Moment matrix of particle i for a fit of degree q (optionally with intercept): N = Σ w (p p').
+template <int BM>
 __device__ void assemble(const MlsArgs &a, int64_t i, int cnt, int q, bool intercept, int B, double *N) {
     for (int k = 0; k < B * B; ++k) N[k] = 0.0;
-    double x[3], p[kMaxB];
+    double x[3], p[BM];
     for (int k = 0; k < cnt; ++k) {
         int64_t s = int64_t(k) * a.npad + i;
         for (int d = 0; d < a.D; ++d) x[d] = a.dist[(int64_t(k) * a.D + d) * a.npad + i] * a.invL;
@@ -168,36 +170,40 @@ __device__ void assemble(const MlsArgs &a, int64_t i, int cnt, int q, bool inter
 }
 
 // Inverse moment matrix (C \ e_j per column), padded into a Bpad×Bpad block.
+template <int BM>
 __device__ bool inverse_moment(const MlsArgs &a, int64_t i, int cnt, int q, bool intercept, int Bpad, double *out) {
     const int B = c_tabs[a.D][q].B + (intercept ? 1 : 0);
-    double N[kMaxB * kMaxB], U[kMaxB * kMaxB];
-    assemble(a, i, cnt, q, intercept, B, N);
+    double N[BM * BM], U[BM * BM];
+    assemble<BM>(a, i, cnt, q, intercept, B, N);
     for (int k = 0; k < Bpad * Bpad; ++k) out[k] = 0.0;
     if (!cholesky_moment(B, N, U)) return false;
-    double e[kMaxB], x[kMaxB];
+    double e[BM], x[BM];
     for (int j = 0; j < B; ++j) {
         for (int r = 0; r < B; ++r) e[r] = (r == j) ? 1.0 : 0.0;
-        chol_solve(B, U, e, x);
+        chol_solve<BM>(B, U, e, x);
         for (int r = 0; r < B; ++r) out[r * Bpad + j] = x[r];
     }
     return true;
 }
 
+// One instantiation per basis capacity BM (4: degree-1 fits in 3-D; 10: degree 3 in 2-D; 20: degree 3 in 3-D),
+// so that the per-thread arrays stay as small as the context's largest fit.
+template <int BM>
 __global__ void k_mls(MlsArgs a) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int cnt = a.cnt[i];
-    double inv[kMaxB * kMaxB];
+    double inv[BM * BM];
     // reconstruction fit (every particle, MLSWeights without intercept)
-    bool okr = inverse_moment(a, i, cnt, a.rdeg, false, a.Br, inv);
+    bool okr = inverse_moment<BM>(a, i, cnt, a.rdeg, false, a.Br, inv);
     for (int k = 0; k < a.Br * a.Br; ++k) a.inv_r[i * a.Br * a.Br + k] = inv[k];
     a.ok_r[i] = okr;
     // divergence fit of the degree the stencil carries at full order, padded to Bd
     int q = divergence_index(a.DO, a.D, a.max_order, cnt) - 1;
-    bool okd = inverse_moment(a, i, cnt, q, true, a.Bd, inv);
+    bool okd = inverse_moment<BM>(a, i, cnt, q, true, a.Bd, inv);
     for (int k = 0; k < a.Bd * a.Bd; ++k) a.inv_d[i * a.Bd * a.Bd + k] = inv[k];
     a.ok_d[i] = okd;
-    double x[3], p[kMaxB], v[kMaxB];
+    double x[3], p[BM], v[BM];
     for (int k = 0; k < cnt; ++k) {
         int64_t s = int64_t(k) * a.npad + i;
         if (!okd) {
@@ -218,8 +224,8 @@ __global__ void k_mls(MlsArgs a) {
     if (!a.need_dw1) return;
     // degree-1 fit with intercept: per-slot weights C \ (w p~), rows 2..D+1, times invL
     const int B1 = a.D + 1;
-    double N[kMaxB * kMaxB], U[kMaxB * kMaxB];
-    assemble(a, i, cnt, 1, true, B1, N);
+    double N[BM * BM], U[BM * BM];
+    assemble<BM>(a, i, cnt, 1, true, B1, N);
     bool ok1 = cholesky_moment(B1, N, U);
     a.ok_1[i] = ok1;
     for (int k = 0; k < cnt; ++k) {
@@ -232,7 +238,7 @@ __global__ void k_mls(MlsArgs a) {
         gen_basis(a.D, 1, true, x, p);
         double w = a.w[s];
         for (int b = 0; b < B1; ++b) p[b] = w * p[b];
-        chol_solve(B1, U, p, v);
+        chol_solve<BM>(B1, U, p, v);
         for (int d = 0; d < a.D; ++d) a.dw1[(int64_t(k) * a.D + d) * a.npad + i] = v[d + 1] * a.invL;
     }
 }
@@ -271,7 +277,7 @@ __global__ void k_donor_pass(DonorArgs a, int pass) {
     }
 }
 
-inline unsigned grid_for(int64_t n) { return unsigned((n + HCC_BLOCK - 1) / HCC_BLOCK); }
+inline unsigned grid_for(int64_t n, int bs = HCC_BLOCK) { return unsigned((n + bs - 1) / bs); }
 
 }  // namespace
 
@@ -279,9 +285,13 @@ hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err) {
     std::call_once(g_tabs_once, upload_tables);
     if (g_tabs_err != cudaSuccess) { err = std::string("basis tables: ") + cudaGetErrorString(g_tabs_err); return HCC_ERR_CUDA; }
     if (a.n == 0) return HCC_OK;
-    if (a.Bd > kMaxB || a.Br > kMaxB) { err = "basis too large for the MLS kernel"; return HCC_ERR_UNSUPPORTED; }
-    k_mls<<<grid_for(a.n), 128, 0, s>>>(a);
+    const int need = std::max(std::max(a.Bd, a.Br), a.D + 1);
+    if (need > kMaxB) { err = "basis too large for the MLS kernel"; return HCC_ERR_UNSUPPORTED; }
+    if (need <= 4) k_mls<4><<<grid_for(a.n, 128), 128, 0, s>>>(a);
+    else if (need <= 10) k_mls<10><<<grid_for(a.n, 128), 128, 0, s>>>(a);
+    else k_mls<kMaxB><<<grid_for(a.n, 64), 64, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { err = std::string("mls kernel: ") + cudaGetErrorString(e); return HCC_ERR_CUDA; }
     return HCC_OK;
 }

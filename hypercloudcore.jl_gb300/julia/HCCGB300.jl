@@ -1,0 +1,123 @@
+# HCCGB300.jl — the Julia side of the drop-in: a `TimeStepper` whose functor calls libhcc_gb300.so through
+# `ccall`, behind HyperCloudCore's own API (HyperbolicPDE traits, MUSCL, MOOD, tableaus, ParticleGrid).
+#
+# Usage (mirrors GeneralRKTimeStepper, src/TimeStepping/TimeSteppers.jl:195-229):
+#
+#   using HyperCloudCore, HCCGB300
+#   ts = GB300RKTimeStepper(eq, pg, MUSCL(Float64, 2, 4, 2, NoLimiter(), RusanovFlux(); div_order = 2),
+#                           MOOD(EPD1(), MOODu1(1e-4 * prod(pg.meta.dx))), RK3_SSP_Tableau(Float64);
+#                           bc_map = Dict(1 => HCCGB300.OUTFLOW, 2 => HCCGB300.OUTFLOW, 3 => HCCGB300.OUTFLOW,
+#                                         4 => HCCGB300.OUTFLOW), precision = :fp64)
+#   while t < tmax
+#       dt = min(0.4 * get_time_step(pg, eq, ts), tmax - t)
+#       ts(eq, pg, t, dt)
+#       t += dt
+#   end
+#
+# The grid's positions, tags and states are uploaded at construction; `ts(eq, pg, t, dt)` runs the step on the
+# GPU and writes `pg.rhos` and `pg.core.particle_orders` back, so every host-side consumer of the reference
+# (snapshot writers, diagnostics) keeps working.
+module HCCGB300
+
+using HyperCloudCore
+using StaticArrays
+
+export GB300RKTimeStepper, hcc_pde_kind
+
+const libhcc = get(ENV, "HCC_GB300_LIB", joinpath(@__DIR__, "..", "libhcc_gb300.so"))
+
+const KEEP, DIRICHLET, OUTFLOW = Int32(0), Int32(1), Int32(2)
+
+# hcc_config (include/hcc.h), field for field
+mutable struct HccConfig
+    abi_version::Int32; dim::Int32; n_vars::Int32; pde::Int32; precision::Int32; muscl_order::Int32
+    div_order::Int32; mood_criterion::Int32; mood_strategy::Int32; tableau::Int32; mood_substeps::Int32
+    periodic::NTuple{3, Int32}; bc_by_tag::NTuple{16, Int32}; max_mood_iterations::Int32
+    reserved_i::NTuple{8, Int32}
+    dx::NTuple{3, Float64}; radius::Float64; weight_alpha::Float64
+    canvas_min::NTuple{3, Float64}; canvas_max::NTuple{3, Float64}
+    domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
+    mood_delta::Float64; velocity::NTuple{48, Float64}; gamma::Float64; bgk_epsilon::Float64
+    bgk_macro_velocity::NTuple{3, Float64}; bgk_coefficient::Float64; bgk_interior_factor::Float64
+    reserved_d::NTuple{8, Float64}
+    HccConfig() = (c = new(); ccall((:hcc_config_defaults, libhcc), Cvoid, (Ref{HccConfig},), c); c)
+end
+
+# PDE -> physics module of the library (the trait the kernels are selected by). Euler is a user HyperbolicPDE
+# that declares itself with `hcc_pde_kind(::MyEuler) = 1` and `hcc_gamma(::MyEuler) = γ`.
+hcc_pde_kind(::HyperbolicPDE) = error("this HyperbolicPDE has no GB300 physics module")
+hcc_gamma(eq) = 1.4
+
+_check(st, h, call) = st == 0 || error("$call: " * unsafe_string(ccall((:hcc_last_error, libhcc), Cstring, (Ptr{Cvoid},), h)))
+
+mutable struct GB300RKTimeStepper{D, M} <: TimeStepper
+    handle::Ptr{Cvoid}
+    N::Int
+end
+
+_tableau_id(bt) = error("unknown tableau")
+_strategy_id(::EPD0) = Int32(1); _strategy_id(::EPD1) = Int32(2); _strategy_id(::EPD2) = Int32(3)
+_strategy_id(::MOODStrategy) = Int32(0)
+_criterion(c::MOODu1) = (Int32(1), Float64(c.d))
+_criterion(::MOODPAD) = (Int32(2), 0.0)
+_criterion(::OnlyMOOD) = (Int32(3), 0.0)
+_criterion(::NoMOOD) = (Int32(0), 0.0)
+
+function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T}, interp::MUSCL, mood::MOOD,
+                            tableau_id::Integer; bc_map = Dict{Int, Int32}(), precision::Symbol = :fp64) where {D, M, T}
+    cfg = HccConfig()
+    cfg.dim, cfg.n_vars, cfg.pde = D, M, hcc_pde_kind(eq)
+    cfg.precision = precision === :fp32 ? 1 : 0
+    cfg.muscl_order = HyperCloudCore._extract_order(interp)
+    cfg.tableau = tableau_id
+    cfg.mood_strategy = _strategy_id(mood.strategy)
+    cfg.mood_criterion, cfg.mood_delta = _criterion(mood.criterion)
+    pad3(v, z) = ntuple(d -> d <= length(v) ? Float64(v[d]) : z, 3)
+    cfg.dx = pad3(pg.meta.dx, 1.0); cfg.radius = pg.meta.R
+    cfg.weight_alpha = pg.neighbor.weight_func.alpha
+    cfg.canvas_min = pad3(pg.domain.canvas_mins, 0.0); cfg.canvas_max = pad3(pg.domain.canvas_maxs, 1.0)
+    cfg.domain_min = pad3(pg.geometry.mins, 0.0); cfg.domain_max = pad3(pg.geometry.maxs, 1.0)
+    cfg.periodic = ntuple(d -> d <= D ? Int32(pg.domain.is_periodic[d]) : Int32(0), 3)
+    cfg.bc_by_tag = ntuple(t -> Int32(get(bc_map, t, KEEP)), 16)
+    cfg.gamma = hcc_gamma(eq)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:hcc_create, libhcc), Cint, (Ref{HccConfig}, Int64, Ref{Ptr{Cvoid}}), cfg, 0, h)
+    _check(st, h[], "hcc_create")
+    N = pg.meta.N
+    pos = reinterpret(Float64, pg.core.positions[1:N])
+    bnd = UInt8.(pg.core.is_boundary[1:N]); tags = Int32.(pg.core.tags[1:N]); vol = Float64.(pg.core.volumes[1:N])
+    _check(ccall((:hcc_upload_cloud, libhcc), Cint, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{UInt8}, Ptr{Int32}, Ptr{Float64}),
+                 h[], N, pos, bnd, tags, vol), h[], "hcc_upload_cloud")
+    _check(ccall((:hcc_build_neighbours, libhcc), Cint, (Ptr{Cvoid},), h[]), h[], "hcc_build_neighbours")
+    _check(ccall((:hcc_prepare_geometry, libhcc), Cint, (Ptr{Cvoid},), h[]), h[], "hcc_prepare_geometry")
+    ts = GB300RKTimeStepper{D, M}(h[], N)
+    finalizer(t -> ccall((:hcc_destroy, libhcc), Cint, (Ptr{Cvoid},), t.handle), ts)
+    return ts
+end
+
+# (ts::GeneralRKTimeStepper)(eq, pg, t, dt) (TimeSteppers.jl:531): one step on the GPU, pg.rhos written back.
+function (ts::GB300RKTimeStepper{D, M})(eq::HyperbolicPDE, pg::ParticleGrid, t::Real, dt::Real) where {D, M}
+    U = reinterpret(Float64, pg.rhos[1:ts.N])
+    _check(ccall((:hcc_upload_state, libhcc), Cint, (Ptr{Cvoid}, Ptr{Float64}), ts.handle, U), ts.handle, "hcc_upload_state")
+    _check(ccall((:hcc_step, libhcc), Cint, (Ptr{Cvoid}, Cdouble, Cdouble), ts.handle, t, dt), ts.handle, "hcc_step")
+    out = Vector{Float64}(undef, ts.N * M)
+    _check(ccall((:hcc_download_state, libhcc), Cint, (Ptr{Cvoid}, Ptr{Float64}), ts.handle, out), ts.handle, "hcc_download_state")
+    for i in 1:ts.N
+        pg.rhos[i] = State{M, Float64}(ntuple(m -> out[(i - 1) * M + m], Val(M)))
+    end
+    orders = Vector{Int32}(undef, ts.N)
+    _check(ccall((:hcc_download_orders, libhcc), Cint, (Ptr{Cvoid}, Ptr{Int32}), ts.handle, orders), ts.handle, "hcc_download_orders")
+    pg.core.particle_orders[1:ts.N] .= orders
+    return nothing
+end
+
+# get_time_step(pg, eq, interp) (ParticleGrids.jl:386) on the GPU stepper's cached weights.
+function HyperCloudCore.get_time_step(pg::ParticleGrid, eq::HyperbolicPDE, ts::GB300RKTimeStepper{D, M}) where {D, M}
+    U = reinterpret(Float64, pg.rhos[1:ts.N])
+    _check(ccall((:hcc_upload_state, libhcc), Cint, (Ptr{Cvoid}, Ptr{Float64}), ts.handle, U), ts.handle, "hcc_upload_state")
+    dt = Ref{Float64}(0.0)
+    _check(ccall((:hcc_time_step, libhcc), Cint, (Ptr{Cvoid}, Ref{Float64}), ts.handle, dt), ts.handle, "hcc_time_step")
+    return dt[]
+end
+
+end # module

@@ -129,6 +129,7 @@ typedef struct {
     int64_t inadmissible;              /* mood_inadmissible(ts) of the last step (TimeSteppers.jl:272) */
     int64_t kernel_launches;           /* kernels launched by the last hcc_step / hcc_time_step */
     int64_t steps;                     /* steps taken by the context */
+    int64_t kernel_launches_total;     /* kernels launched since the context was created */
 } hcc_counters;
 
 typedef struct hcc_ctx hcc_ctx;
@@ -187,6 +188,21 @@ hcc_status hcc_get_counters(hcc_ctx *ctx, hcc_counters *out);
 
 /* total_mass(pg) (Volumes.jl:103-107) accumulated in FP64 on the device: out[M]. */
 hcc_status hcc_total_mass(hcc_ctx *ctx, double *out);
+
+/* Per-kernel device time of the steps taken while profiling is on (CUDA events around every gather and flux
+   launch on the context's stream). No counterpart in the reference (it times whole steps with @elapsed,
+   benchmark/step.jl:77). */
+typedef struct {
+    double gather_ms;            /* full reconstruction passes */
+    int64_t gather_launches;
+    double flux_ms;              /* full flux passes */
+    int64_t flux_launches;
+    double recompute_ms;         /* MOOD recompute passes (masked gather + flux) */
+    int64_t recompute_launches;
+    int64_t steps;
+} hcc_kernel_times;
+hcc_status hcc_set_profiling(hcc_ctx *ctx, int enable);
+hcc_status hcc_get_kernel_times(hcc_ctx *ctx, hcc_kernel_times *out, int reset);
 
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);

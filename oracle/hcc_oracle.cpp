@@ -826,7 +826,7 @@ struct Solver {
         }
         double Uc[400];
         if (!cholesky_moment(B, Nm, Uc)) return;
-        double sc[32], col[32], x[32];
+        double sc[32] = {0}, col[32] = {0}, x[32] = {0};
         build_scales(bt, invL, sc);
         for (int m = 0; m < M; ++m) {
             for (int b = 0; b < B; ++b) col[b] = bs[b * M + m];
@@ -1388,6 +1388,19 @@ hcc_status orc_compute_rhs(orc_ctx *ctx, double *K) {
     std::memcpy(K, Kv.data(), Kv.size() * sizeof(double));
     return HCC_OK;
 }
+hcc_status orc_compute_rhs_orders(orc_ctx *ctx, const int32_t *orders, double *K) {
+    if (!ctx || !K || !orders) return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    if (!s.have_nb) return HCC_ERR_STATE;
+    if (!s.have_geom && !s.prepare_geometry()) return HCC_ERR_STATE;
+    if ((int64_t)s.rho_n.size() != s.N * s.M) s.size_buffers();
+    std::fill(s.grads.begin(), s.grads.end(), 0.0);
+    s.orders.assign(orders, orders + s.N);
+    std::vector<double> Kv(s.N * s.M, 0.0);
+    s.compute_rhs(Kv, s.rhos.data(), true);
+    std::memcpy(K, Kv.data(), Kv.size() * sizeof(double));
+    return HCC_OK;
+}
 hcc_status orc_step(orc_ctx *ctx, double t, double dt) {
     if (!ctx) return HCC_ERR_INVALID;
     if (!ctx->s.have_nb) return HCC_ERR_STATE;
@@ -1514,7 +1527,7 @@ int32_t orc_mls_solve(int32_t D, int32_t M, int32_t q, int32_t K, const double *
         for (int b = 0; b < B; ++b)
             for (int m = 0; m < M; ++m) bs[b * M + m] = bs[b * M + m] + w[k] * (p[b] * df[k * M + m]);
     }
-    double U[400], sc[32], col[32], x[32];
+    double U[400], sc[32] = {0}, col[32] = {0}, x[32] = {0};
     for (int k = 0; k < B * M; ++k) out[k] = 0.0;
     if (!cholesky_moment(B, Nm.data(), U)) return 0;
     build_scales(bt, invL, sc);

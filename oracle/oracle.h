@@ -39,6 +39,8 @@ hcc_status orc_upload_state(orc_ctx *ctx, const double *U);
 hcc_status orc_download_state(orc_ctx *ctx, double *U);
 hcc_status orc_time_step(orc_ctx *ctx, double *dt_out);
 hcc_status orc_compute_rhs(orc_ctx *ctx, double *K);
+/* The same with given particle orders (starved lowering still applies). */
+hcc_status orc_compute_rhs_orders(orc_ctx *ctx, const int32_t *orders, double *K);
 hcc_status orc_step(orc_ctx *ctx, double t, double dt);
 hcc_status orc_download_orders(orc_ctx *ctx, int32_t *orders);
 hcc_status orc_upload_orders(orc_ctx *ctx, const int32_t *orders);

@@ -54,6 +54,7 @@ def load(abi) -> C.CDLL:
         ("orc_download_state", C.c_int, [P, dp]),
         ("orc_time_step", C.c_int, [P, dp]),
         ("orc_compute_rhs", C.c_int, [P, dp]),
+        ("orc_compute_rhs_orders", C.c_int, [P, ip, dp]),
         ("orc_step", C.c_int, [P, C.c_double, C.c_double]),
         ("orc_download_orders", C.c_int, [P, ip]),
         ("orc_upload_orders", C.c_int, [P, ip]),
@@ -187,6 +188,13 @@ class OracleContext:
     def compute_rhs(self):
         K = np.zeros((self.n, self.M), dtype=np.float64)
         self._check(self.lib.orc_compute_rhs(self._h, _p(K, C.c_double)), "orc_compute_rhs")
+        return K
+
+    def compute_rhs_orders(self, orders):
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        K = np.zeros((self.n, self.M), dtype=np.float64)
+        self._check(self.lib.orc_compute_rhs_orders(self._h, _p(o, C.c_int32), _p(K, C.c_double)),
+                    "orc_compute_rhs_orders")
         return K
 
     def step(self, t, dt):

@@ -1,0 +1,520 @@
+"""The oracle against the reference's own known-answer tests (test/unit_core.jl, test/unit_schemes.jl).
+
+The reference ships no golden-vector files and cannot run here (Julia); these analytic, structural and cross-path
+checks are what pins the CPU restatement to it. Each test names the reference test it ports.
+"""
+import math
+import sys
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def abi(hcc):
+    return sys.modules["hcc_gb300._abi"]
+
+
+@pytest.fixture(scope="module")
+def olib(oracle, abi):
+    return oracle.load(abi)
+
+
+def make(hcc, oracle, abi, cloud, pde, **kw):
+    cfg = hcc.make_config(pde, cloud, **kw)
+    o = oracle.OracleContext(cfg, abi)
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    return o
+
+
+def lattice_1d(hcc, N, rng=2.5):
+    """make_pg_1d (test/runtests.jl:37-43): uniform periodic grid on [-1, 1] with N particles."""
+    dx = 2.0 / N
+    return hcc.rectangular_cloud((-1.0,), (1.0,), dx, rng * dx, periodic=True)
+
+
+# ----------------------------------------------------------------------------------------------- basis tables
+def test_basis_order_and_counts(olib):
+    """_generate_exponents: index 1 is x, 2 is y, 3 is z; within a degree sorted by (-max, reverse)."""
+    import ctypes as C
+    ex = (C.c_int32 * 60)()
+    B = olib.orc_basis_exponents(2, 2, ex)
+    assert B == 5
+    assert [tuple(ex[2 * k:2 * k + 2]) for k in range(B)] == [(1, 0), (0, 1), (2, 0), (0, 2), (1, 1)]
+    B = olib.orc_basis_exponents(3, 2, ex)
+    assert [tuple(ex[3 * k:3 * k + 3]) for k in range(B)] == [
+        (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (0, 2, 0), (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]
+    for D in (1, 2, 3):
+        for q in range(0, 5):
+            assert olib.orc_basis_count(D, q) == (math.comb(D + q, q) - 1 if q > 0 else 0)
+
+
+def test_divergence_degree_rules(olib):
+    """unit_core.jl:401-419: _div_idx and _divergence_index."""
+    assert olib.orc_div_idx(2, 1) == 2 and olib.orc_div_idx(2, 2) == 2
+    assert olib.orc_div_idx(2, 3) == 4 and olib.orc_div_idx(2, 4) == 4
+    assert olib.orc_div_idx(2, 5) == 6 and olib.orc_div_idx(3, 5) == 5
+    assert olib.orc_divergence_index(0, 1, 3, 4) == 3
+    assert olib.orc_divergence_index(0, 1, 3, 6) == 4
+    assert olib.orc_divergence_index(3, 1, 1, 6) == 4
+    assert olib.orc_divergence_index(0, 1, 4, 3) == 3
+
+
+def test_ssp_coefficients(olib, abi):
+    """unit_schemes.jl:203-213."""
+    T = abi.TABLEAUS
+    assert abs(olib.orc_ssp_coefficient(T["RK1_Euler"]) - 1) < 1e-9
+    assert abs(olib.orc_ssp_coefficient(T["RK2_SSP"]) - 1) < 1e-9
+    assert abs(olib.orc_ssp_coefficient(T["RK2_Ralston"]) - 0.5) < 1e-9
+    assert abs(olib.orc_ssp_coefficient(T["RK3_SSP"]) - 1) < 1e-9
+    assert abs(olib.orc_ssp_coefficient(T["RK4_SSP"]) - 1.50818004918983) < 1e-8
+    assert olib.orc_ssp_coefficient(T["RK4_Classical"]) == 0
+    assert olib.orc_ssp_coefficient(T["IMEX_ARS222"]) == 0
+
+
+# ----------------------------------------------------------------------------------------------- grids / search
+@pytest.mark.parametrize("D", [1, 2])
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_jittered_periodic_grid_has_no_boundary(hcc, D, seed):
+    """unit_core.jl:319-329: N = 20^D, no boundary particles, positions in [0, 1)."""
+    cl = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, 0.05, 0.125, periodic=True, jitter=0.01, seed=seed)
+    assert cl.n == 20 ** D and cl.is_boundary.sum() == 0
+    assert np.all((cl.pos >= 0) & (cl.pos < 1))
+
+
+@pytest.mark.parametrize("R", [0.45, 0.6])
+def test_small_periodic_domains_do_not_duplicate(hcc, oracle, abi, R):
+    """unit_core.jl:331-341: two and one coarse bins; no duplicates, no self, counts = brute force."""
+    cl = hcc.rectangular_cloud((0.0,), (1.0,), 0.1, R, periodic=True)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)))
+    counts, idx, _, _ = o.neighbours()
+    x = o.positions()[:, 0]
+    start = np.concatenate([[0], np.cumsum(counts)])
+    for i in range(cl.n):
+        lst = idx[start[i]:start[i + 1]]
+        assert len(set(lst)) == len(lst) and i not in lst
+        dd = x - x[i]
+        brute = sum(1 for j in range(cl.n) if j != i and abs(dd[j] - np.round(dd[j])) <= R + 1e-12)
+        assert counts[i] == brute
+
+
+@pytest.mark.parametrize("D,periodic", [(2, False), (2, True), (3, False)])
+def test_neighbour_lists_match_brute_force(hcc, oracle, abi, D, periodic):
+    """Fixed-radius lists: every pair with r^2 <= R^2 (wrapped when periodic), j != i, in window order with
+    descending indices within a bin (NeighborLogic.jl:153-167, :288-329)."""
+    h = 0.1 if D == 2 else 0.2
+    cl = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=periodic, jitter=0.25 * h, seed=9)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(tuple((1.0,) for _ in range(D))))
+    counts, idx, w, dist = o.neighbours()
+    pos = o.positions()
+    L = np.array([1.0 if periodic else 0.0] * D)
+    invL = np.array([1.0 if periodic else 0.0] * D)
+    start = np.concatenate([[0], np.cumsum(counts)])
+    R2 = (2.5 * h) ** 2
+    for i in range(cl.n):
+        d = pos - pos[i]
+        d = d - L * np.round(d * invL)
+        r2 = (d ** 2).sum(axis=1)
+        expect = set(np.nonzero(r2 <= R2)[0]) - {i}
+        got = idx[start[i]:start[i + 1]]
+        assert set(got) == expect
+        np.testing.assert_array_equal(dist[start[i]:start[i + 1]], d[got])
+        y = (d[got] ** 2).sum(axis=1) / R2
+        np.testing.assert_allclose(w[start[i]:start[i + 1]],
+                                   1 / (1 + y * (1 + y * (0.5 + y * (1 / 6 + y / 24)))), rtol=1e-14)
+
+
+def test_morton_numbering_is_z_order(hcc):
+    """Reordering.jl:55-102: the permutation sorts by interleaved 16-bit keys (2-D)."""
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), 0.05, 0.125, jitter=0.01, seed=4)
+    kx = np.clip(np.floor((cl.pos[:, 0] - cl.canvas_min[0]) / (cl.canvas_max[0] - cl.canvas_min[0]) * 65535), 0, 65535)
+    ky = np.clip(np.floor((cl.pos[:, 1] - cl.canvas_min[1]) / (cl.canvas_max[1] - cl.canvas_min[1]) * 65535), 0, 65535)
+
+    def spread(v):
+        out = 0
+        for b in range(16):
+            out |= ((int(v) >> b) & 1) << (2 * b)
+        return out
+
+    codes = [spread(a) | (spread(b) << 1) for a, b in zip(kx, ky)]
+    assert all(codes[i] <= codes[i + 1] for i in range(len(codes) - 1))
+
+
+def test_rectangle_tags_and_ghost_band(hcc):
+    """Domains.jl:59-94, :268-270: face tags of the box, ghosts only within R + dx of an interior point."""
+    h = 0.05
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=2)
+    inner = cl.pos[cl.is_boundary == 0]
+    ghosts = cl.pos[cl.is_boundary == 1]
+    assert set(np.unique(cl.tags[cl.is_boundary == 1])) == {1, 2, 3, 4}
+    x, y = ghosts[:, 0], ghosts[:, 1]
+    t = cl.tags[cl.is_boundary == 1]
+    assert np.all(x[t == 1] < 0) and np.all(x[t == 2] > 1) and np.all(y[t == 3] < 0) and np.all(y[t == 4] > 1)
+    from scipy.spatial import cKDTree
+    dmin, _ = cKDTree(inner).query(ghosts)
+    assert np.all(dmin <= 2.5 * h + h + 1e-12)
+
+
+# ----------------------------------------------------------------------------------------------- MLS
+def test_mls_divergence_exact_for_linear_flux(hcc, oracle, abi, olib):
+    """unit_core.jl:361-380: ΔF = ((1.5dx, -0.5dx + 2dy), (2dy, 3dy - dx)) -> divergence (3.5, 2.5), degrees 1..3."""
+    import ctypes as C
+    dx = 1 / 20
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 2.5 * dx, periodic=True)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0, 1.0), (1.0, 1.0))))
+    counts, idx, w, dist = o.neighbours()
+    start = np.concatenate([[0], np.cumsum(counts)])
+    for i in (0, cl.n // 2):
+        d = np.ascontiguousarray(dist[start[i]:start[i + 1]])
+        wt = np.ascontiguousarray(w[start[i]:start[i + 1]])
+        dF = np.stack([1.5 * d[:, 0], -0.5 * d[:, 0] + 2 * d[:, 1], 2.0 * d[:, 1], 3.0 * d[:, 1] - d[:, 0]], axis=1)
+        dF = np.ascontiguousarray(dF)
+        for q in (1, 2, 3):
+            out = np.zeros(2)
+            ok = olib.orc_mls_divergence(2, 2, q, len(wt), d.ctypes.data_as(C.POINTER(C.c_double)),
+                                         wt.ctypes.data_as(C.POINTER(C.c_double)),
+                                         dF.ctypes.data_as(C.POINTER(C.c_double)), dx,
+                                         out.ctypes.data_as(C.POINTER(C.c_double)))
+            assert ok
+            np.testing.assert_allclose(out, [3.5, 2.5], atol=1e-8)
+
+
+def test_constant_flux_has_zero_divergence(hcc, oracle, abi, olib):
+    """unit_core.jl:392-400: the intercept fit gives zero divergence of a constant flux on any stencil."""
+    import ctypes as C
+    dx = 1 / 24
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 2.5 * dx, periodic=True, jitter=0.2 * dx, seed=3)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0, 1.0), (1.0, 1.0))))
+    counts, idx, w, dist = o.neighbours()
+    start = np.concatenate([[0], np.cumsum(counts)])
+    for i in (0, cl.n // 2, cl.n - 1):
+        d = np.ascontiguousarray(dist[start[i]:start[i + 1]])
+        wt = np.ascontiguousarray(w[start[i]:start[i + 1]])
+        dF = np.ascontiguousarray(np.tile([1.0, -2.0, 0.5, 3.0], (len(wt), 1)))
+        for q in (1, 2, 3):
+            out = np.zeros(2)
+            olib.orc_mls_divergence(2, 2, q, len(wt), d.ctypes.data_as(C.POINTER(C.c_double)),
+                                    wt.ctypes.data_as(C.POINTER(C.c_double)), dF.ctypes.data_as(C.POINTER(C.c_double)),
+                                    dx, out.ctypes.data_as(C.POINTER(C.c_double)))
+            assert np.abs(out).max() < 1e-9
+
+
+def _basis(olib, D, q, x):
+    import ctypes as C
+    ex = (C.c_int32 * 64)()
+    B = olib.orc_basis_exponents(D, q, ex)
+    e = np.array(ex[:B * D]).reshape(B, D)
+    fac = np.array([np.prod([math.factorial(int(t)) for t in row]) for row in e], dtype=float)
+    return np.prod(x[None, :] ** e, axis=1) / fac
+
+
+def test_conditional_regularisation(olib):
+    """unit_core.jl:443-463: healthy stencils keep the plain factorisation; collinear ones get the retry and
+    still the right x-derivative (within 100 sqrt(eps))."""
+    import ctypes as C
+    dists = np.array([[0.37 * np.cos(k), 0.37 * np.sin(k) + 0.1 * k] for k in range(1, 13)])
+    wts = np.exp(-(dists ** 2).sum(axis=1))
+    Nm = sum(w * np.outer(_basis(olib, 2, 2, d), _basis(olib, 2, 2, d)) for w, d in zip(wts, dists))
+    Nm = np.ascontiguousarray(Nm)
+    U = np.zeros_like(Nm)
+    plain = C.c_int32()
+    ok = olib.orc_cholesky_moment(5, Nm.ctypes.data_as(C.POINTER(C.c_double)), U.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.byref(plain))
+    assert ok and plain.value == 1
+    np.testing.assert_allclose(U.T @ U, Nm, rtol=1e-12, atol=1e-14)
+    xd = np.array([[0.3 * k, 0.0] for k in range(-4, 5) if k != 0])
+    xw = np.ones(len(xd))
+    Nx = np.ascontiguousarray(sum(w * np.outer(_basis(olib, 2, 2, d), _basis(olib, 2, 2, d)) for w, d in zip(xw, xd)))
+    ok = olib.orc_cholesky_moment(5, Nx.ctypes.data_as(C.POINTER(C.c_double)), U.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.byref(plain))
+    assert ok and plain.value == 0
+    f = np.ascontiguousarray((2 * xd[:, 0] + xd[:, 0] ** 2)[:, None])
+    out = np.zeros(5)
+    ok = olib.orc_mls_solve(2, 1, 2, len(xd), np.ascontiguousarray(xd).ctypes.data_as(C.POINTER(C.c_double)),
+                            xw.ctypes.data_as(C.POINTER(C.c_double)), f.ctypes.data_as(C.POINTER(C.c_double)), 1.0,
+                            out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert ok and np.all(np.isfinite(out))
+    assert abs(out[0] - 2) < 100 * np.sqrt(np.finfo(float).eps) and abs(out[1]) < 100 * np.sqrt(np.finfo(float).eps)
+
+
+def test_divergence_weights_are_face_vectors(hcc, oracle, abi):
+    """dweights of the intercept fit (MUSCL.jl:197-223, unit_schemes.jl:429-460): Σ_j c_ij = 0 and
+    Σ_j c_ij x_ij^T = I (the fit reproduces constants and linear functions)."""
+    dx = 1 / 16
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 2.5 * dx, periodic=True, jitter=0.25 * dx, seed=5)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (1.0,))), scheme=hcc.MUSCL(3, 0))
+    o.prepare_geometry()
+    counts, idx, w, dist = o.neighbours()
+    dw, okr, okd = o.geometry(len(idx))
+    start = np.concatenate([[0], np.cumsum(counts)])
+    assert okd.all()
+    for i in range(0, cl.n, 7):
+        c = dw[start[i]:start[i + 1]]
+        x = dist[start[i]:start[i + 1]]
+        np.testing.assert_allclose(c.sum(axis=0), 0, atol=1e-9 / dx)
+        np.testing.assert_allclose(c.T @ x, np.eye(2), atol=1e-9)
+
+
+def test_cached_fit_equals_direct_solve(hcc, oracle, abi, olib):
+    """unit_core.jl:463-495: the cached inverse moment (apply_weights) equals the direct solve within 1e-9."""
+    import ctypes as C
+    dx = 1 / 24
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 2.5 * dx, periodic=True, jitter=0.2 * dx, seed=3)
+    pde = hcc.LinearAdvection(((1.0, 0.5), (0.7, -0.3)))
+    for order in (2, 3):
+        o = make(hcc, oracle, abi, cl, pde, scheme=hcc.MUSCL(order, 0))
+        x, y = cl.pos[:, 0], cl.pos[:, 1]
+        U = np.stack([np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y), np.exp(-((x - .5) ** 2 + (y - .5) ** 2) / .05)], 1)
+        o.upload_state(U)
+        o.compute_rhs()
+        g = o.gradients()
+        counts, idx, w, dist = o.neighbours()
+        start = np.concatenate([[0], np.cumsum(counts)])
+        pos = o.positions()
+        for i in (0, cl.n // 3, cl.n - 1):
+            sl = slice(start[i], start[i + 1])
+            df = np.ascontiguousarray(U[idx[sl]] - U[i])
+            d = np.ascontiguousarray(dist[sl])
+            wt = np.ascontiguousarray(w[sl])
+            B = g.shape[1]
+            out = np.zeros(B * 2)
+            assert olib.orc_mls_solve(2, 2, order - 1, len(wt), d.ctypes.data_as(C.POINTER(C.c_double)),
+                                      wt.ctypes.data_as(C.POINTER(C.c_double)), df.ctypes.data_as(C.POINTER(C.c_double)),
+                                      dx, out.ctypes.data_as(C.POINTER(C.c_double)))
+            np.testing.assert_allclose(g[i].ravel(), out, atol=1e-9 * max(1, np.abs(out).max()))
+        assert pos.shape == (cl.n, 2)
+
+
+# ----------------------------------------------------------------------------------------------- MOOD
+@pytest.fixture(scope="module")
+def mood_grid(hcc, oracle, abi):
+    cl = lattice_1d(hcc, 40)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+             mood=hcc.MOOD(hcc.EPD1, hcc.OnlyMOOD()))
+    return cl, o
+
+
+def test_uniform_1d_grid_has_four_neighbours(mood_grid):
+    """unit_core.jl:675-686: N = 40 (no duplicated seam point), R = 2.5dx -> ±1, ±2."""
+    cl, o = mood_grid
+    counts, _, _, _ = o.neighbours()
+    assert cl.n == 40 and np.all(counts == 4)
+
+
+def test_interface_orders(hcc, oracle, abi):
+    """unit_core.jl:688-697: EPD0 (3,1); EPD1 (1,1) on the edge, (3,3) off it; EPD2 (1,1) through N(i)."""
+    cl = lattice_1d(hcc, 40)
+    x = cl.pos[:, 0]
+    order_of_x = np.argsort(x)
+    i = order_of_x[9]
+    j = order_of_x[11]
+    k = order_of_x[7]
+    res = {}
+    for name, strat in (("EPD0", hcc.EPD0), ("EPD1", hcc.EPD1), ("EPD2", hcc.EPD2)):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+                 mood=hcc.MOOD(strat, hcc.OnlyMOOD()))
+        orders = np.full(cl.n, 3, dtype=np.int32)
+        orders[j] = 1
+        o.set_orders(orders)
+        res[name] = (o.interface_orders(i, j), o.interface_orders(i, k))
+    assert res["EPD0"][0] == (3, 1)
+    assert res["EPD1"][0] == (1, 1) and res["EPD1"][1] == (3, 3)
+    assert res["EPD2"][1] == (1, 1)
+
+
+def test_mask_expansion(mood_grid):
+    """unit_core.jl:707-714: one hop adds the 4 neighbours, two hops 8."""
+    cl, o = mood_grid
+    mask = np.zeros(cl.n, dtype=np.uint8)
+    mask[7] = 1
+    assert o.expand_mask(mask, 1).sum() == 1 + 4
+    assert o.expand_mask(mask, 2).sum() == 1 + 8
+
+
+def test_detect_and_drop_terminates_at_order_one(hcc, oracle, abi):
+    """unit_core.jl:748-764: OnlyMOOD 3 -> 2 -> 1, then nothing changes; an empty dirty mask checks nobody."""
+    cl = lattice_1d(hcc, 40)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+             mood=hcc.MOOD(hcc.EPD1, hcc.OnlyMOOD()))
+    U = np.zeros((cl.n, 1))
+    o.set_orders(np.full(cl.n, 3))
+    assert o.detect_and_drop(U, U, full=True) and np.all(o.orders() == 2)
+    assert not o.detect_and_drop(U, U, full=False, dirty=np.zeros(cl.n, np.uint8))
+    assert o.detect_and_drop(U, U, full=False, dirty=np.ones(cl.n, np.uint8)) and np.all(o.orders() == 1)
+    assert not o.detect_and_drop(U, U, full=True) and np.all(o.orders() == 1)
+
+
+def test_detect_and_drop_flags_inadmissible_candidates(hcc, oracle, abi):
+    """unit_core.jl:766-779: a NaN candidate passes the DMP but fails PAD, only with the equation."""
+    cl = lattice_1d(hcc, 40)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+             mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(0.0)))
+    U = np.exp(-cl.pos[:, :1] ** 2 / 0.1)
+    cand = U.copy()
+    q = 5
+    cand[q] = np.nan
+    o.set_orders(np.full(cl.n, 3))
+    assert not o.detect_and_drop(U, cand, full=True, with_eq=False)
+    o.set_orders(np.full(cl.n, 3))
+    assert o.detect_and_drop(U, cand, full=True, with_eq=True)
+    orders = o.orders()
+    assert orders[q] == 2 and (orders == 2).sum() == 1
+
+
+# ----------------------------------------------------------------------------------------------- CFL
+def test_cfl_equals_host_formula(hcc, oracle, abi):
+    """unit_schemes.jl:496-510: get_time_step with cached weights equals the host sum (rtol 1e-12); Inf for zero
+    speeds."""
+    h = 0.05
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=8)
+    o = make(hcc, oracle, abi, cl, hcc.Euler(2), scheme=hcc.MUSCL(2, 2))
+    o.prepare_geometry()
+    rng = np.random.default_rng(0)
+    rho = 1 + 0.5 * rng.random(cl.n)
+    u = rng.standard_normal((cl.n, 2)) * 0.3
+    p = 1 + rng.random(cl.n)
+    U = np.column_stack([rho, rho * u[:, 0], rho * u[:, 1], p / 0.4 + 0.5 * rho * (u ** 2).sum(1)])
+    o.upload_state(U)
+    counts, idx, w, dist = o.neighbours()
+    dw, _, _ = o.geometry(len(idx))
+    c = np.sqrt(1.4 * p / rho)
+    lam = np.abs(u) + c[:, None]
+    start = np.concatenate([[0], np.cumsum(counts)])
+    best = np.inf
+    for i in range(cl.n):
+        if cl.is_boundary[i]:
+            continue
+        sl = slice(start[i], start[i + 1])
+        s = (np.abs(dw[sl]) * np.maximum(lam[i][None, :], lam[idx[sl]])).sum()
+        if s > np.finfo(float).tiny:
+            best = min(best, 0.5 / s)
+    assert o.time_step() == pytest.approx(best, rel=1e-12)
+    o0 = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((0.0,), (0.0,))), scheme=hcc.MUSCL(2, 2))
+    o0.upload_state(np.ones((cl.n, 1)))
+    assert o0.time_step() == np.inf
+
+
+# ----------------------------------------------------------------------------------------------- schemes
+@pytest.mark.parametrize("drop", [False, True])
+def test_streamed_equals_buffered(hcc, oracle, abi, drop):
+    """unit_schemes.jl:398-427: streamed divergence = buffered fit within 1e-11 * scale (also with dropped orders)."""
+    dx = 1 / 24
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 3.5 * dx, periodic=True, jitter=0.2 * dx, seed=21)
+    pde = hcc.LinearAdvection(((1.0, 0.5), (0.7, -0.3)))
+    x, y = cl.pos[:, 0], cl.pos[:, 1]
+    U = np.stack([np.exp(-((x - .5) ** 2 + (y - .5) ** 2) / .05), np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y)], 1)
+    orders = np.full(cl.n, 3, dtype=np.int32)
+    if drop:
+        orders[np.abs(x - 0.5) < 0.1] = 2
+    K = {}
+    for streamed in (False, True):
+        o = make(hcc, oracle, abi, cl, pde, scheme=hcc.MUSCL(3, 0))
+        o.set_streamed(streamed)
+        o.upload_state(U)
+        K[streamed] = o.compute_rhs_orders(orders)
+    scale = np.abs(K[False]).max()
+    assert np.abs(K[False] - K[True]).max() < 1e-11 * scale
+
+
+# ----------------------------------------------------------------------------------------------- boundary conditions
+def _bc_grid(hcc, oracle, abi, bc_map):
+    N = 60
+    dx = 2.0 / N
+    cl = hcc.rectangular_cloud((-1.0,), (1.0,), dx, 2.5 * dx)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0), bc_map=bc_map)
+    x = cl.pos[:, 0]
+    o.upload_state(x[:, None].copy())
+    return cl, o, x
+
+
+def test_dirichlet_restores_the_initial_state(hcc, oracle, abi):
+    """unit_core.jl:525-533."""
+    cl, o, x = _bc_grid(hcc, oracle, abi, {1: hcc.BC_DIRICHLET, 2: hcc.BC_DIRICHLET})
+    buf = o.apply_bcs(np.full((cl.n, 1), 99.0))
+    g = cl.is_boundary == 1
+    assert g.any() and np.all(buf[g, 0] == x[g]) and np.all(buf[~g, 0] == 99.0)
+
+
+def test_outflow_copies_the_nearest_resolved_donor(hcc, oracle, abi):
+    """unit_core.jl:535-555: zero gradient, the outermost interior value."""
+    cl, o, x = _bc_grid(hcc, oracle, abi, {1: hcc.BC_OUTFLOW, 2: hcc.BC_OUTFLOW})
+    buf = o.apply_bcs(x[:, None].copy())
+    inner = cl.is_boundary == 0
+    lo, hi = x[inner].min(), x[inner].max()
+    for i in np.nonzero(~inner)[0]:
+        assert buf[i, 0] == (lo if x[i] < 0 else hi)
+
+
+def test_dirichlet_left_outflow_right(hcc, oracle, abi):
+    """unit_core.jl:557-573 (the Sod-tube map)."""
+    cl, o, x = _bc_grid(hcc, oracle, abi, {1: hcc.BC_DIRICHLET, 2: hcc.BC_OUTFLOW})
+    start = np.full((cl.n, 1), 99.0)
+    inner = cl.is_boundary == 0
+    start[inner, 0] = x[inner]
+    buf = o.apply_bcs(start)
+    hi = x[inner].max()
+    for i in np.nonzero(~inner)[0]:
+        assert buf[i, 0] == (x[i] if x[i] < 0 else hi)
+
+
+# ----------------------------------------------------------------------------------------------- time stepper
+def test_only_mood_drives_every_particle_to_order_one(hcc, oracle, abi):
+    """unit_core.jl:930-936 (MUSCL of the highest order built here, RK2_SSP)."""
+    cl = lattice_1d(hcc, 60)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+             mood=hcc.MOOD(hcc.EPD1, hcc.OnlyMOOD()), tableau="RK2_SSP")
+    o.upload_state(np.exp(-cl.pos[:, :1] ** 2 / 0.02))
+    o.step(0.0, 0.4 * 2 / 60)
+    assert np.all(o.orders() == 1) and np.all(o.mood_flags() == 1)
+
+
+@pytest.mark.parametrize("tab,mood", [("RK3_SSP", "none"), ("RK3_SSP", "u1"), ("IMEX_PRSSP3", "u1"),
+                                      ("RK4_SSP", "u1"), ("RK2_Ralston", "pad")])
+def test_steppers_run_and_stay_finite(hcc, oracle, abi, tab, mood):
+    """unit_core.jl:905-928: explicit, IMEX and MOOD fixed points run, stay finite, keep the mass within 1e-2."""
+    cl = lattice_1d(hcc, 60)
+    crit = {"none": hcc.NoMOOD(), "u1": hcc.MOODu1(1e-4 * 2 / 60), "pad": hcc.MOODPAD()}[mood]
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+             mood=hcc.MOOD(hcc.EPD1, crit), tableau=tab)
+    U0 = np.exp(-cl.pos[:, :1] ** 2 / 0.02)
+    o.upload_state(U0)
+    dt = 0.4 * 2 / 60
+    for k in range(5):
+        o.step(k * dt, dt)
+    U = o.download_state()
+    assert np.all(np.isfinite(U))
+    assert abs(U.sum() - U0.sum()) <= 1e-2 * abs(U0.sum())
+    assert np.all((o.orders() >= 1) & (o.orders() <= 3))
+
+
+def test_first_order_muscl_advances(hcc, oracle, abi):
+    """unit_core.jl:938-945 (first half): MUSCL order 1 with forward Euler moves the solution."""
+    cl = lattice_1d(hcc, 60)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(1, 0), tableau="RK1_Euler")
+    U0 = np.exp(-cl.pos[:, :1] ** 2 / 0.02)
+    o.upload_state(U0)
+    o.step(0.0, 0.4 * 2 / 60)
+    assert np.abs(o.download_state() - U0).max() > 1e-4
+
+
+def test_advection_converges_to_the_analytic_solution(hcc, oracle, abi):
+    """Linear advection against the characteristic solution (analytic_closure, test/PDEs/linear_advection.jl:61-128):
+    MUSCL2 on a periodic cloud, error ratio between h and h/2 above 2.5 (second order: 4)."""
+    errs = []
+    for n in (40, 80):
+        h = 1.0 / n
+        cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.1 * h, seed=3)
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (0.5,))), scheme=hcc.MUSCL(2, 2))
+        f = lambda x, y: np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
+        o.upload_state(f(cl.pos[:, 0], cl.pos[:, 1])[:, None])
+        T = 0.1
+        dt = 0.25 * o.time_step()
+        steps = int(np.ceil(T / dt))
+        dt = T / steps
+        for k in range(steps):
+            o.step(k * dt, dt)
+        pos = o.positions()
+        ex = f(pos[:, 0] - T, pos[:, 1] - 0.5 * T)
+        errs.append(np.abs(o.download_state()[:, 0] - ex).mean())
+    assert errs[0] / errs[1] > 2.5, errs
