@@ -7,6 +7,7 @@ HCC_ABI_VERSION = 1
 HCC_MAX_DIM = 3
 HCC_MAX_VARS = 16
 HCC_MAX_TAGS = 16
+HCC_NOALLOC_MAX_PARTICLES = 65536 * 256
 
 # hcc_status
 HCC_OK, HCC_ERR_INVALID, HCC_ERR_CAPACITY, HCC_ERR_CUDA, HCC_ERR_STATE, HCC_ERR_NONFINITE, HCC_ERR_TIMEOUT, \
@@ -99,6 +100,7 @@ PROTOTYPES = [
     ("hcc_total_mass", C.c_int, [P, _dp]),
     ("hcc_set_profiling", C.c_int, [P, C.c_int]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
+    ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_synchronize", C.c_int, [P]),
     ("hcc_stream", P, [P]),
 ]

@@ -28,6 +28,7 @@ UNITS = {
     "hcc_stage_f64_r2.cu": ["-fmad=false"],
     "hcc_stage_f32_r1.cu": [],
     "hcc_stage_f32_r2.cu": [],
+    "hcc_noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -204,6 +204,23 @@ typedef struct {
 hcc_status hcc_set_profiling(hcc_ctx *ctx, int enable);
 hcc_status hcc_get_kernel_times(hcc_ctx *ctx, hcc_kernel_times *out, int reset);
 
+/* CFL time step of caller-owned device arrays WITHOUT allocating device memory. No counterpart in the reference.
+   For callers that cannot allocate GPU memory when they need a time step: a code that reserves its device memory
+   up front and then freezes it, or one that routes all device memory through its own pool and forbids
+   cudaMalloc/cudaFree inside its time loop. Same value as hcc_time_step (ParticleGrids.jl:386-450 arithmetic, FP64).
+   Inputs are DEVICE pointers in the library's slot-major layout: counts[n], nidx[k*npad + i],
+   dweights[(k*dim + d)*npad + i], is_boundary[n], U[i*n_vars + m] (FP64); physics parameters come from cfg
+   (pde, dim, n_vars, velocity, gamma). stream is a cudaStream_t (NULL = default stream); *dt_out is written on
+   return (the call synchronises the stream).
+   Scratch: a fixed file-scope device array (about 512 KiB, held by every GPU that loads the library until exit);
+   n above HCC_NOALLOC_MAX_PARTICLES returns HCC_ERR_CAPACITY. All calls share it: calls that overlap on the GPU
+   race and must be serialised by the caller. The first call on each device looks up the array's device address
+   (a CUDA runtime query) and should come before any stream capture. */
+#define HCC_NOALLOC_MAX_PARTICLES (65536 * 256)
+hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n, int64_t npad, const int32_t *counts,
+                                     const int32_t *nidx, const double *dweights, const uint8_t *is_boundary,
+                                     const double *U, void *stream, double *dt_out);
+
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);
 
