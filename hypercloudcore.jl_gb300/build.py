@@ -46,9 +46,13 @@ def _stale(obj: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, jobs: int | None = None, extra_flags=None) -> Path:
-    """Compile every CUDA translation unit and link the shared library; returns its path."""
-    BUILD.mkdir(exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, extra_flags=None, lib_path=None, build_dir=None) -> Path:
+    """Compile every CUDA translation unit and link the shared library; returns its path. `extra_flags`,
+    `lib_path` and `build_dir` build a variant (e.g. other launch shapes) next to the default library."""
+    global BUILD, LIB
+    BUILD = Path(build_dir) if build_dir else PKG / "_build"
+    LIB = Path(lib_path) if lib_path else PKG / "libhcc_gb300.so"
+    BUILD.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "hcc.h"]
     extra = list(extra_flags or [])
     cmds = []

@@ -8,6 +8,14 @@
 #pragma once
 #include "hcc_internal.cuh"
 
+// Launch shape of the flux pass (threads per block, minimum resident blocks per SM for the register budget).
+#ifndef HCC_FLUX_BLOCK
+#define HCC_FLUX_BLOCK 128
+#endif
+#ifndef HCC_FLUX_MINB
+#define HCC_FLUX_MINB 6
+#endif
+
 namespace hcc {
 
 // ----------------------------------------------------------------------------------- physics (device)
@@ -32,11 +40,45 @@ template <typename T> __device__ __forceinline__ T floatmin_of();
 template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2250738585072014e-308; }
 template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
 
+// Arithmetic kernels of the two paths. FP64 (plain path): IEEE division and square root, Julia's NaN-propagating
+// min/max — the oracle's exact sequence. FP32 (bulk path): the fast reciprocal and reciprocal square root of the
+// special-function unit (≤ 2 ulp) and fminf/fmaxf; its results are compared with the FP64 oracle to tolerance.
+template <typename T> __device__ __forceinline__ T recip(T x) { return T(1) / x; }
+template <> __device__ __forceinline__ float recip<float>(float x) { return __fdividef(1.0f, x); }
+template <typename T> __device__ __forceinline__ T root(T x) { return sqrt(x); }
+template <> __device__ __forceinline__ float root<float>(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
+template <typename T> __device__ __forceinline__ T vmin(T x, T y) { return jmin(x, y); }
+template <> __device__ __forceinline__ float vmin<float>(float x, float y) { return fminf(x, y); }
+template <typename T> __device__ __forceinline__ T vmax(T x, T y) { return jmax(x, y); }
+template <> __device__ __forceinline__ float vmax<float>(float x, float y) { return fmaxf(x, y); }
+
+// Load N contiguous elements with 16-byte vectors where the layout guarantees the alignment (particle-major
+// arrays of 4 floats / 2 doubles per vector from a 256-byte-aligned base).
+template <typename T, int N>
+__device__ __forceinline__ void load_vec(const T *__restrict__ p, T *out) {
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 4; ++q) {
+            float4 v = reinterpret_cast<const float4 *>(p)[q];
+            out[4 * q] = v.x; out[4 * q + 1] = v.y; out[4 * q + 2] = v.z; out[4 * q + 3] = v.w;
+        }
+    } else if constexpr (sizeof(T) == 8 && N % 2 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 2; ++q) {
+            double2 v = reinterpret_cast<const double2 *>(p)[q];
+            out[2 * q] = v.x; out[2 * q + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < N; ++q) out[q] = p[q];
+    }
+}
+
 // Euler primitives: inv_rho = 1/rho, u_d = m_d inv_rho, p = (gamma-1)(E - 0.5 (rho |u|^2)), c = sqrt(gamma p inv_rho).
 template <typename T, int D>
 __device__ __forceinline__ void euler_prim(const PhysParams<T> &ph, const T *U, T &inv_rho, T *u, T &p) {
     T rho = U[0];
-    inv_rho = T(1) / rho;
+    inv_rho = recip(rho);
     T q2 = T(0);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -52,7 +94,7 @@ __device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T 
     if constexpr (PDE == HCC_PDE_EULER) {
         T inv_rho, u[D], p;
         euler_prim<T, D>(ph, U, inv_rho, u, p);
-        T c = sqrt(ph.gamma * p * inv_rho);
+        T c = root(ph.gamma * p * inv_rho);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             F[d][0] = U[1 + d];
@@ -79,7 +121,7 @@ __device__ __forceinline__ void speeds(const PhysParams<T> &ph, const T *U, T *l
     if constexpr (PDE == HCC_PDE_EULER) {
         T inv_rho, u[D], p;
         euler_prim<T, D>(ph, U, inv_rho, u, p);
-        T c = sqrt(ph.gamma * p * inv_rho);
+        T c = root(ph.gamma * p * inv_rho);
 #pragma unroll
         for (int d = 0; d < D; ++d) lam[d] = fabs(u[d]) + c;
     } else {
@@ -178,17 +220,28 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
         for (int b = 0; b < BR; ++b)
 #pragma unroll
             for (int m = 0; m < M; ++m) bs[b][m] = T(0);
+        int32_t jn = cnt > 0 ? a.g.nidx[i] : 0;
+        T dn[D], wn = cnt > 0 ? a.g.wt[i] : T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) dn[d] = cnt > 0 ? a.g.dist[int64_t(d) * np + i] : T(0);
         for (int k = 0; k < cnt; ++k) {
-            const int64_t s = int64_t(k) * np + i;
-            const int32_t j = a.g.nidx[s];
+            const int32_t j = jn;
             T x[D], pb[BR];
 #pragma unroll
-            for (int d = 0; d < D; ++d) x[d] = a.g.dist[(int64_t(k) * D + d) * np + i] * invL;
-            recon_basis<D, RDEG, T>(x, pb);
-            const T w = a.g.wt[s];
-            T df[M];
+            for (int d = 0; d < D; ++d) x[d] = dn[d] * invL;
+            const T w = wn;
+            if (k + 1 < cnt) {
+                const int64_t s1 = int64_t(k + 1) * np + i;
+                jn = a.g.nidx[s1];
+                wn = a.g.wt[s1];
 #pragma unroll
-            for (int m = 0; m < M; ++m) df[m] = a.U[int64_t(j) * M + m] - fi[m];
+                for (int d = 0; d < D; ++d) dn[d] = a.g.dist[(int64_t(k + 1) * D + d) * np + i];
+            }
+            recon_basis<D, RDEG, T>(x, pb);
+            T df[M];
+            load_vec<T, M>(a.U + int64_t(j) * M, df);
+#pragma unroll
+            for (int m = 0; m < M; ++m) df[m] = df[m] - fi[m];
 #pragma unroll
             for (int b = 0; b < BR; ++b)
 #pragma unroll
@@ -306,7 +359,7 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
 template <typename T, int D, int M, int PDE, int RDEG>
-__global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
+__global__ void __launch_bounds__(HCC_FLUX_BLOCK, HCC_FLUX_MINB) k_flux(const StageArgs<T> a) {
     constexpr int BR = RBasis<D, RDEG>::B;
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.g.n) return;
@@ -323,12 +376,8 @@ __global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
     const T invL = a.g.invL;
     (void)invL;
     T fi[M], gi[BR][M], Fi[D][M], lami[D];
-#pragma unroll
-    for (int m = 0; m < M; ++m) fi[m] = a.U[i * M + m];
-#pragma unroll
-    for (int b = 0; b < BR; ++b)
-#pragma unroll
-        for (int m = 0; m < M; ++m) gi[b][m] = a.grad[i * (BR * M) + b * M + m];
+    load_vec<T, M>(a.U + i * M, fi);
+    load_vec<T, BR * M>(a.grad + i * (BR * M), &gi[0][0]);
     flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami);
     const int oi_own = a.orders[i];
     const int didx = divergence_index(a.sc.DO, D, oi_own, cnt);
@@ -343,21 +392,34 @@ __global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
     for (int m = 0; m < M; ++m) { mn[m] = fi[m]; mx[m] = fi[m]; }
 
     if (wok) {
+        // slot data of slot k+1 are loaded while slot k is computed (one-deep software pipeline)
+        int32_t jn = a.g.nidx[i];
+        T dkn[D], wkn[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            dkn[d] = a.g.dist[int64_t(d) * np + i];
+            wkn[d] = wsl[int64_t(d) * np + i];
+        }
         for (int k = 0; k < cnt; ++k) {
-            const int64_t s = int64_t(k) * np + i;
-            const int32_t j = a.g.nidx[s];
+            const int32_t j = jn;
             T dk[D], wk[D];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                dk[d] = a.g.dist[(int64_t(k) * D + d) * np + i];
-                wk[d] = wsl[(int64_t(k) * D + d) * np + i];
+            for (int d = 0; d < D; ++d) { dk[d] = dkn[d]; wk[d] = wkn[d]; }
+            if (k + 1 < cnt) {
+                jn = a.g.nidx[int64_t(k + 1) * np + i];
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    dkn[d] = a.g.dist[(int64_t(k + 1) * D + d) * np + i];
+                    wkn[d] = wsl[(int64_t(k + 1) * D + d) * np + i];
+                }
             }
             T fj[M];
-#pragma unroll
-            for (int m = 0; m < M; ++m) fj[m] = a.U[int64_t(j) * M + m];
+            load_vec<T, M>(a.U + int64_t(j) * M, fj);
+            T gj[BR * M];
+            load_vec<T, BR * M>(a.grad + int64_t(j) * (BR * M), gj);
             if (need_ext) {
 #pragma unroll
-                for (int m = 0; m < M; ++m) { mn[m] = jmin(mn[m], fj[m]); mx[m] = jmax(mx[m], fj[m]); }
+                for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], fj[m]); mx[m] = vmax(mx[m], fj[m]); }
             }
             const int oj_own = a.orders[j];
             int oi, oj;
@@ -378,16 +440,15 @@ __global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
                 if (b >= keep_i) pi[b] = T(0);
                 if (b >= keep_j) pj[b] = T(0);
             }
-            const T *gjp = a.grad + int64_t(j) * (BR * M);
             T fij[M], fji[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 T si = gi[0][m] * pi[0];
-                T sj = gjp[m] * pj[0];
+                T sj = gj[m] * pj[0];
 #pragma unroll
                 for (int b = 1; b < BR; ++b) {
                     si = si + gi[b][m] * pi[b];
-                    sj = sj + gjp[b * M + m] * pj[b];
+                    sj = sj + gj[b * M + m] * pj[b];
                 }
                 fij[m] = fi[m] + si;
                 fji[m] = fj[m] + sj;
@@ -420,8 +481,8 @@ __global__ void __launch_bounds__(128) k_flux(const StageArgs<T> a) {
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 T fj = a.U[int64_t(j) * M + m];
-                mn[m] = jmin(mn[m], fj);
-                mx[m] = jmax(mx[m], fj);
+                mn[m] = vmin(mn[m], fj);
+                mx[m] = vmax(mx[m], fj);
             }
         }
     }
@@ -552,7 +613,8 @@ struct StageInst {
         k_gather<T, D, M, PDE, RDEG><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
     }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
-        k_flux<T, D, M, PDE, RDEG><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+        k_flux<T, D, M, PDE, RDEG><<<grid(n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(
+            *static_cast<const StageArgs<T> *>(args));
     }
     static void stage1(const void *args, int64_t n, cudaStream_t s) {
         k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));

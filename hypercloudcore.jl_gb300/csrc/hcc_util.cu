@@ -58,18 +58,17 @@ __global__ void k_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed
     }
 }
 
-// _expand_body! (MOOD.jl:323-335): dst = src or any neighbour in src.
+// One hop of expand_mask! (_expand_body!, MOOD.jl:323-335: a particle is marked if it or a neighbour was), as a
+// push from the marked particles: the neighbour relation is symmetric (one radius, exactly antisymmetric
+// distances), so marking every neighbour of a marked particle marks the same set as the pull over all particles,
+// while only the few marked particles read their lists. dst must be cleared before.
 __global__ void k_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n,
                          int64_t npad) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint8_t m = src[i];
-    if (!m) {
-        int c = cnt[i];
-        for (int k = 0; k < c; ++k)
-            if (src[nidx[int64_t(k) * npad + i]]) { m = 1; break; }
-    }
-    dst[i] = m;
+    if (i >= n || !src[i]) return;
+    dst[i] = 1;
+    const int c = cnt[i];
+    for (int k = 0; k < c; ++k) dst[nidx[int64_t(k) * npad + i]] = 1;
 }
 
 // _nb_min_order (MOOD.jl:66-74) for EPD2.
@@ -144,7 +143,9 @@ void launch_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint
 }
 void launch_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n, int64_t npad,
                    cudaStream_t s) {
-    if (n > 0) k_expand<<<grid_for(n), HCC_BLOCK, 0, s>>>(src, dst, cnt, nidx, n, npad);
+    if (n <= 0) return;
+    cudaMemsetAsync(dst, 0, size_t(n), s);
+    k_expand<<<grid_for(n), HCC_BLOCK, 0, s>>>(src, dst, cnt, nidx, n, npad);
 }
 void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n, int64_t npad,
                   cudaStream_t s) {
