@@ -13,7 +13,10 @@
 #define HCC_FLUX_BLOCK 128
 #endif
 #ifndef HCC_FLUX_MINB
-#define HCC_FLUX_MINB 6
+#define HCC_FLUX_MINB 6            // FP32: caps the flux kernel at 80 registers
+#endif
+#ifndef HCC_FLUX_MINB64
+#define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
 #endif
 
 namespace hcc {
@@ -353,13 +356,20 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
 }
 
 // ----------------------------------------------------------------------------------- flux pass
+// Resident blocks per SM the flux kernel is compiled for: as many as its registers allow without spilling
+// (FP32 2-D scalar/Euler: 80 registers; wider states and FP64 need more).
+template <typename T, int D, int M> constexpr int flux_min_blocks() {
+    if (sizeof(T) == 8) return M >= 8 ? 1 : (D * M >= 12 ? 2 : HCC_FLUX_MINB64);
+    return M >= 8 ? 2 : (D * M >= 12 ? 4 : HCC_FLUX_MINB);
+}
+
 // The MUSCL functor (MUSCL.jl:390-508) in its streamed form: per slot, EPD interface reconstruction, physical
 // fluxes, Rusanov (FluxFunctions.jl:90-100) with sort_flux (Utils.jl:270-278), the flux difference ΔF and its
 // contraction with the divergence weights; K_E = -2 Σ c·ΔF (TimeSteppers.jl:354). Fused epilogue: the next
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
 template <typename T, int D, int M, int PDE, int RDEG>
-__global__ void __launch_bounds__(HCC_FLUX_BLOCK, HCC_FLUX_MINB) k_flux(const StageArgs<T> a) {
+__global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_flux(const StageArgs<T> a) {
     constexpr int BR = RBasis<D, RDEG>::B;
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.g.n) return;
