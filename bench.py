@@ -310,10 +310,56 @@ def run_gpu(args):
                               "gather_ms_per_launch": r64["kt"]["gather_ms"] / max(r64["kt"]["gather_launches"], 1),
                               "e2e": units / r64["e2e_s"], "clocks": r64["clocks"]}
         line["fp32_over_fp64"] = line["value"] / line["fp64_plain"]["value"]
+    if not args.no_published:
+        line["published_case"] = run_published_case(hcc, args.steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(hcc, cloud, U0, h, args.cpu_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------------- published case
+# The reference's own benchmark (benchmark/step.jl, defaults): scalar advection with speeds (1, 0.5) on a uniform
+# periodic 1000 x 1000 cloud, R = 2.5dx, MUSCL3 + VenkatakrishnanLimiter(:hard) + MOOD(EPD1, MOODu1(1e-6)), SSP-RK3,
+# dt = 0.3 x get_time_step. Published ms/step on an RX 9070 XT / i5-13600K (8 cores): gpu_roadmap.md:215.
+PUBLISHED_1M = {"f64_gpu_ms": 29.0, "f32_gpu_ms": 9.8, "f64_cpu8_ms": 387.0, "f32_cpu8_ms": 284.0,
+                "hardware": "AMD RX 9070 XT (GPU), i5-13600K 8 cores (CPU)"}
+
+
+def run_published_case(hcc, steps, n_side=1000):
+    import torch
+    h = 1.0 / n_side
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True)
+    U0 = np.exp(-((cloud.pos - 0.5) ** 2).sum(axis=1) / 0.02)[:, None].copy()
+    out = {"workload": f"advection2d_muscl3_vk_mood_periodic_{n_side}x{n_side}", "n_particles": cloud.n,
+           "published": PUBLISHED_1M}
+    for prec in ("fp32", "fp64"):
+        cfg = hcc.make_config(hcc.LinearAdvection(((1.0,), (0.5,))), cloud, scheme=hcc.MUSCL(3, 0, "vk_hard"),
+                              mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-6)), precision=prec)
+        ctx = hcc.Context(cfg)
+        ctx.upload_cloud(cloud)
+        ctx.build_neighbours()
+        ctx.prepare_geometry()
+        ctx.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
+        dt = 0.3 * ctx.time_step()
+        for _ in range(3):
+            ctx.step(0.0, dt)
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ctx.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.step(0.0, dt)
+        e1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[f"{prec}_ms_per_step"] = ms
+        out[f"{prec}_point_updates_per_s"] = 3 * cloud.n / (ms / 1e3)
+        ctx.close()
+    out["speedup_vs_published_gpu"] = {"f32": PUBLISHED_1M["f32_gpu_ms"] / out["fp32_ms_per_step"],
+                                       "f64": PUBLISHED_1M["f64_gpu_ms"] / out["fp64_ms_per_step"]}
+    return out
 
 
 # --------------------------------------------------------------------------------------------- CPU (reference) arm
@@ -373,6 +419,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--no-published", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -110,6 +110,16 @@ class KineticRelaxation:
 
 @dataclass
 class MUSCL:
+    """MUSCL(T, D, M, order, limiter, RusanovFlux(); div_order) (src/Interpolation/MUSCL.jl:116). `limiter` is one
+    of "none", "bj_soft", "bj_hard", "vk_soft", "vk_hard" (BarthJespersen / Venkatakrishnan, :soft / :hard)."""
+    order: int = 2
+    div_order: int = 0
+    limiter: str = "none"
+
+
+@dataclass
+class WENO:
+    """WENO(T, D, 1, order; div_order) (src/Interpolation/WENO.jl:43): scalar equations only."""
     order: int = 2
     div_order: int = 0
 
@@ -168,6 +178,11 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
     cfg.precision = FP32 if str(precision).lower() in ("fp32", "f32", "float32") else FP64
     cfg.muscl_order = scheme.order
     cfg.div_order = scheme.div_order
+    if isinstance(scheme, WENO):
+        cfg.scheme = _abi.SCHEME_WENO
+    else:
+        cfg.scheme = _abi.SCHEME_MUSCL
+        cfg.limiter = _abi.LIMITERS[scheme.limiter]
     cfg.tableau = TABLEAUS[tableau] if isinstance(tableau, str) else int(tableau)
     cfg.mood_substeps = 1 if mood_substeps else 0
     cfg.max_mood_iterations = max_mood_iterations
@@ -386,7 +401,7 @@ class GB300RKTimeStepper:
 
 
 __all__ = [
-    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "MOOD", "MOODu1",
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "WENO", "MOOD", "MOODu1",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",

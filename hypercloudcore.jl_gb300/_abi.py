@@ -27,6 +27,9 @@ TABLEAUS = {
     "RK1_Euler": 0, "RK2_SSP": 1, "RK2_Ralston": 2, "RK3_SSP": 3, "RK4_Classical": 4, "RK4_SSP": 5,
     "IMEX_Euler": 6, "IMEX_ARS233": 7, "IMEX_ARS222": 8, "IMEX_PRSSP3": 9, "IMEX_SSP2332": 10,
 }
+# hcc_scheme / hcc_limiter
+SCHEME_MUSCL, SCHEME_WENO = 0, 1
+LIMITERS = {"none": 0, "bj_soft": 1, "bj_hard": 2, "vk_soft": 3, "vk_hard": 4}
 # hcc_bc_kind
 BC_KEEP, BC_DIRICHLET, BC_OUTFLOW = 0, 1, 2
 
@@ -38,7 +41,7 @@ class HccConfig(C.Structure):
         ("mood_criterion", C.c_int32), ("mood_strategy", C.c_int32), ("tableau", C.c_int32),
         ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
         ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
-        ("reserved_i", C.c_int32 * 8),
+        ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("reserved_i", C.c_int32 * 5),
         ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
         ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),

@@ -171,7 +171,8 @@ struct hcc_ctx {
     const StageOps *ops = nullptr;
     // scheme
     int max_order = 2, DO = 0, rdeg = 1, Br = 1, full_div = 2, ddeg = 1, Bd = 2, need_dw1 = 0;
-    double invL = 1.0;
+    double invL = 1.0, h = 1.0;
+    int weno = 0;
     Tableau tab;
     double ssp_C = 0.0, ratio = 0.0;
     int has_source = 0;
@@ -330,12 +331,15 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     g.ok_r = c->ok_r; g.ok_d = c->ok_d; g.ok_1 = c->ok_1;
     g.bnd = c->bnd;
     g.invL = T(c->invL);
+    g.invL64 = c->invL;
+    g.h64 = c->h;
     a.ph = phys_params<T>(c);
     a.sc.max_order = c->max_order;
     a.sc.DO = c->DO;
     a.sc.strategy = c->cfg.mood_strategy;
     a.sc.criterion = c->cfg.mood_criterion;
     a.sc.has_source = c->has_source;
+    a.sc.limiter = c->cfg.limiter;
     a.orders = c->orders;
     a.nbmin = c->nbmin;
     a.grad = static_cast<T *>(c->grad);
@@ -391,8 +395,10 @@ template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
         c->flagged += int64_t(changed);
         if (it >= cap) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
         ++c->mood_iters;
-        // dirty = changed ⊕ reach hops (expand_mask!, MOOD.jl:343-351)
-        if (reach == 1) {
+        // dirty = changed ⊕ reach hops (expand_mask!, MOOD.jl:343-351); WENO reads no neighbour orders (reach 0)
+        if (c->weno) {
+            cudaMemcpyAsync(c->dirty, c->changed, size_t(n), cudaMemcpyDeviceToDevice, c->stream);
+        } else if (reach == 1) {
             launch_expand(c->changed, c->dirty, c->cnt, c->nidx, n, c->npad, c->stream);
         } else {
             launch_expand(c->changed, c->scratch, c->cnt, c->nidx, n, c->npad, c->stream);
@@ -402,9 +408,11 @@ template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
         StageArgs<T> ga = a;
         ga.full = 0;
         ga.mask = c->changed;
-        c->prof_begin(2);
-        c->ops->gather(&ga, n, c->stream);
-        c->prof_end();
+        if (!c->weno) {
+            c->prof_begin(2);
+            c->ops->gather(&ga, n, c->stream);
+            c->prof_end();
+        }
         if (c->cfg.mood_strategy == HCC_EPD2) {
             launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
             c->launches += 1;
@@ -413,7 +421,7 @@ template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
         fa.full = 0;
         fa.mask = c->dirty;
         c->prof_begin(2);
-        c->ops->flux(&fa, n, c->stream);
+        (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, c->stream);
         c->prof_end();
         apply_bcs<T>(c, fa.Ynext);
         c->launches += 2;
@@ -477,16 +485,18 @@ template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
         a.check_substep = c->ratio > 0.0;
         a.h_sub = T(c->ratio * dt);
         a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
-        c->prof_begin(0);
-        c->ops->gather(&a, n, c->stream);
-        c->prof_end();
-        c->launches += 1;
+        if (!c->weno) {
+            c->prof_begin(0);
+            c->ops->gather(&a, n, c->stream);
+            c->prof_end();
+            c->launches += 1;
+        }
         if (c->cfg.mood_strategy == HCC_EPD2) {
             launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
             c->launches += 1;
         }
         c->prof_begin(1);
-        c->ops->flux(&a, n, c->stream);
+        (c->weno ? c->ops->weno : c->ops->flux)(&a, n, c->stream);
         c->prof_end();
         c->launches += 1;
         apply_bcs<T>(c, a.Ynext);
@@ -512,9 +522,9 @@ template <typename T> hcc_status run_rhs(hcc_ctx *c) {
     a.U = static_cast<const T *>(c->rhos);
     a.K = static_cast<T *>(c->KE[0]);
     a.full = 1;
-    c->ops->gather(&a, n, c->stream);
+    if (!c->weno) c->ops->gather(&a, n, c->stream);
     if (c->cfg.mood_strategy == HCC_EPD2) launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
-    c->ops->flux(&a, n, c->stream);
+    (c->weno ? c->ops->weno : c->ops->flux)(&a, n, c->stream);
     hcc_status st = launch_check(c, "rhs kernels");
     if (st != HCC_OK) return st;
     return c->sync("rhs");
@@ -603,6 +613,8 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_EPD2) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
     if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_ONLY) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
     if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
+    if (f.limiter < HCC_LIMITER_NONE || f.limiter > HCC_LIMITER_VK_HARD) return c->fail(HCC_ERR_INVALID, "unknown limiter");
+    if (f.scheme != HCC_SCHEME_MUSCL && f.scheme != HCC_SCHEME_WENO) return c->fail(HCC_ERR_INVALID, "unknown scheme");
     c->max_order = f.muscl_order;
     c->DO = f.div_order > c->max_order ? c->max_order : f.div_order;
     if (c->DO < 0) return c->fail(HCC_ERR_INVALID, "div_order must be >= 0");
@@ -617,6 +629,10 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     for (int d = 1; d < c->D; ++d) h = std::min(h, f.dx[d]);
     if (!(h > 0.0)) return c->fail(HCC_ERR_INVALID, "dx must be positive");
     c->invL = 1.0 / h;
+    c->h = h;
+    c->weno = f.scheme == HCC_SCHEME_WENO;
+    if (c->weno && (c->M != 1 || f.pde != HCC_PDE_ADVECTION))
+        return c->fail(HCC_ERR_INVALID, "WENO is a scalar scheme: linear advection with n_vars = 1");
     c->tab = make_tableau(f.tableau);
     if (c->tab.s == 0) return c->fail(HCC_ERR_INVALID, "unknown tableau");
     c->has_source = f.pde == HCC_PDE_BGK;
@@ -633,6 +649,8 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     c->ratio = (f.mood_substeps && c->ssp_C > 0.0 && f.mood_criterion != HCC_MOOD_NONE) ? 1.0 / c->ssp_C : 0.0;
     c->ops = find_ops(f, c->rdeg);
     if (!c->ops) return c->fail(HCC_ERR_UNSUPPORTED, "this (dim, n_vars, pde) combination is not instantiated");
+    if (c->weno && (!c->ops->weno || c->max_order > 3))
+        return c->fail(HCC_ERR_UNSUPPORTED, "WENO of this dimension / order is not instantiated");
     hcc_status st = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
     if (st != HCC_OK) return st;
     if ((st = c->alloc(c->d_counters, 8, "counters")) != HCC_OK) return st;
@@ -810,7 +828,7 @@ hcc_status hcc_build_neighbours(hcc_ctx *c) {
     HCC_TRY(c->sync("neighbour count"));
     const int64_t kmax = int64_t(c->h_counters[3]);
     c->total_nb = int64_t(c->h_counters[4]);
-    if (f.reserved_i[0] > 0 && kmax > f.reserved_i[0])
+    if (f.slot_capacity > 0 && kmax > f.slot_capacity)
         return c->fail(HCC_ERR_CAPACITY, "max neighbours above the reserved slot capacity");
     c->free_slots();
     c->kmax = int(kmax);
@@ -881,6 +899,7 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
     m.cnt = c->cnt; m.nidx = c->nidx; m.dist = c->dist64; m.w = c->w64; m.invL = c->invL;
     m.inv_r = c->inv_r64; m.ok_r = c->ok_r; m.inv_d = c->inv_d64; m.ok_d = c->ok_d;
     m.dw = c->dw64; m.dw1 = c->dw1_64; m.ok_1 = c->ok_1;
+    m.weno_cfl_degree = c->weno ? std::min(c->max_order, c->D == 3 ? 3 : 4) : 0;
     if ((st = mls_prepare(m, c->stream, c->err)) != HCC_OK) return st;
     if (c->f32) {
         HCC_TRY(c->alloc(c->dist32, slots * D, "distances f32"));

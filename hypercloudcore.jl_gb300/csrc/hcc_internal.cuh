@@ -45,6 +45,76 @@ __host__ __device__ __forceinline__ int divergence_index(int DO, int D, int p_or
     return idx;
 }
 
+// Compile-time exponent table of the MLS basis of degree Q in D variables (_generate_exponents,
+// Interpolators.jl:138-155): per degree, the tuples in Iterators.product order sorted by (-max(t), reverse(t)), with
+// the Taylor prefactors 1/prod(t!).
+constexpr int cbasis_count(int D, int q) {
+    if (q <= 0) return 0;
+    long n = 1;
+    for (int k = 1; k <= q; ++k) n = (n * (D + k)) / k;
+    return int(n - 1);
+}
+template <int D, int Q> struct ExpTable {
+    static constexpr int B = cbasis_count(D, Q);
+    int e[B > 0 ? B : 1][3];
+    double pref[B > 0 ? B : 1];
+    bool hp[B > 0 ? B : 1];
+    constexpr ExpTable() : e{}, pref{}, hp{} {
+        int k = 0;
+        for (int order = 1; order <= Q; ++order) {
+            const int first = k, n = order + 1;
+            int total = 1;
+            for (int d = 0; d < D; ++d) total *= n;
+            for (int lin = 0; lin < total; ++lin) {
+                int r = lin, sum = 0, t[3] = {0, 0, 0};
+                for (int d = 0; d < D; ++d) { t[d] = r % n; r /= n; sum += t[d]; }
+                if (sum != order) continue;
+                for (int d = 0; d < 3; ++d) e[k][d] = t[d];
+                ++k;
+            }
+            for (int q = first + 1; q < k; ++q)           // insertion sort of this degree's tuples
+                for (int j = q; j > first; --j) {
+                    int ma = 0, mb = 0;
+                    for (int d = 0; d < D; ++d) { ma = e[j][d] > ma ? e[j][d] : ma; mb = e[j - 1][d] > mb ? e[j - 1][d] : mb; }
+                    bool less = false, decided = ma != mb;
+                    if (decided) less = ma > mb;
+                    for (int d = D - 1; d >= 0 && !decided; --d)
+                        if (e[j][d] != e[j - 1][d]) { less = e[j][d] < e[j - 1][d]; decided = true; }
+                    if (!less) break;
+                    for (int d = 0; d < 3; ++d) { int tmp = e[j][d]; e[j][d] = e[j - 1][d]; e[j - 1][d] = tmp; }
+                }
+        }
+        for (int q = 0; q < B; ++q) {
+            int den = 1;
+            for (int d = 0; d < D; ++d)
+                for (int f = 2; f <= e[q][d]; ++f) den *= f;
+            pref[q] = 1.0 / double(den);
+            hp[q] = den != 1;
+        }
+    }
+};
+
+// build_basis of degree Q (Interpolators.jl:194-218) from the compile-time table: prefactor first, then the
+// factors x_d or x_d^t in axis order (x^2 = x*x, x^3 = x*x*x, Base.literal_pow).
+template <int D, int Q, typename T>
+__host__ __device__ __forceinline__ void table_basis(const T *x, T *p) {
+    constexpr ExpTable<D, Q> tab{};
+#pragma unroll
+    for (int k = 0; k < ExpTable<D, Q>::B; ++k) {
+        bool have = tab.hp[k];
+        T v = have ? T(tab.pref[k]) : T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int t = tab.e[k][d];
+            if (t == 0) continue;
+            const T f = (t == 1) ? x[d] : (t == 2 ? x[d] * x[d] : x[d] * x[d] * x[d]);
+            v = have ? v * f : f;
+            have = true;
+        }
+        p[k] = v;
+    }
+}
+
 // Reconstruction basis of degree 1 or 2 (build_basis, Interpolators.jl:194-218), in the order of
 // _generate_exponents: degree-1 terms x, y, z; then x²/2, y²/2, z²/2; then xy, xz, yz.
 template <int D, int DEG> struct RBasis { static constexpr int B = (DEG == 1) ? D : (D == 1 ? 2 : (D == 2 ? 5 : 9)); };
@@ -88,6 +158,7 @@ template <typename T> struct PhysParams {
 struct SchemeParams {
     int max_order, DO, strategy, criterion;
     int has_source;                   // BGK relaxation source present
+    int limiter;                      // hcc_limiter
 };
 
 // Device view of the neighbour lists and geometry caches (slot-major, stride = npad).
@@ -103,6 +174,8 @@ template <typename T> struct Geometry {
     const T *inv_r;                   // [i * Br * Br]
     const uint8_t *bnd;
     T invL;
+    double invL64;                    // 1/min(dx) in FP64 (the MLS fits of both paths)
+    double h64;                       // min(dx)
 };
 
 // Arguments of the gather (reconstruction) and flux kernels.
@@ -146,7 +219,7 @@ struct StageOps {
     void (*flux)(const void *args, int64_t n, cudaStream_t s);
     void (*stage1)(const void *args, int64_t n, cudaStream_t s);   // Y_1 (predictor + implicit part)
     void (*cfl)(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s);
-    void (*admissible_count)(const void *args, int64_t n, unsigned long long *count, cudaStream_t s);
+    void (*weno)(const void *args, int64_t n, cudaStream_t s);   // WENO flux pass (scalar advection only)
 };
 
 const StageOps *stage_ops_f64_r1(int D, int M, int pde);
@@ -193,6 +266,7 @@ struct MlsArgs {
     double *inv_r; uint8_t *ok_r;
     double *inv_d; uint8_t *ok_d;
     double *dw; double *dw1; uint8_t *ok_1;
+    int weno_cfl_degree;              // > 0: per-slot CFL weights of the assembled Taylor fit (WENO), not MUSCL caches
 };
 hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err);
 

@@ -194,6 +194,28 @@ __global__ void k_mls(MlsArgs a) {
     if (i >= a.n) return;
     const int cnt = a.cnt[i];
     double inv[BM * BM];
+    if (a.weno_cfl_degree > 0) {
+        // per-slot CFL weights of the assembled Taylor fit (_compute_cfl_coeffs, ParticleGrids.jl:296-329):
+        // rows 1..D of inv(N) times p, times w and invL (the CFL pass takes their absolute values)
+        const int qc = a.weno_cfl_degree;
+        const int Bq = c_tabs[a.D][qc].B;
+        const bool ok = inverse_moment<BM>(a, i, cnt, qc, false, Bq, inv);
+        a.ok_r[i] = ok;
+        a.ok_d[i] = ok;
+        double x[3], p[BM];
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t s = int64_t(k) * a.npad + i;
+            for (int d = 0; d < a.D; ++d) x[d] = a.dist[(int64_t(k) * a.D + d) * a.npad + i] * a.invL;
+            gen_basis(a.D, qc, false, x, p);
+            const double w = a.w[s];
+            for (int d = 0; d < a.D; ++d) {
+                double cv = inv[d * Bq + 0] * p[0];
+                for (int jb = 1; jb < Bq; ++jb) cv = cv + inv[d * Bq + jb] * p[jb];
+                a.dw[(int64_t(k) * a.D + d) * a.npad + i] = ok ? cv * w * a.invL : 0.0;
+            }
+        }
+        return;
+    }
     // reconstruction fit (every particle, MLSWeights without intercept)
     bool okr = inverse_moment<BM>(a, i, cnt, a.rdeg, false, a.Br, inv);
     for (int k = 0; k < a.Br * a.Br; ++k) a.inv_r[i * a.Br * a.Br + k] = inv[k];
@@ -285,7 +307,8 @@ hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err) {
     std::call_once(g_tabs_once, upload_tables);
     if (g_tabs_err != cudaSuccess) { err = std::string("basis tables: ") + cudaGetErrorString(g_tabs_err); return HCC_ERR_CUDA; }
     if (a.n == 0) return HCC_OK;
-    const int need = std::max(std::max(a.Bd, a.Br), a.D + 1);
+    const int need = a.weno_cfl_degree > 0 ? basis_count(a.D, a.weno_cfl_degree)
+                                           : std::max(std::max(a.Bd, a.Br), a.D + 1);
     if (need > kMaxB) { err = "basis too large for the MLS kernel"; return HCC_ERR_UNSUPPORTED; }
     if (need <= 4) k_mls<4><<<grid_for(a.n, 128), 128, 0, s>>>(a);
     else if (need <= 10) k_mls<10><<<grid_for(a.n, 128), 128, 0, s>>>(a);

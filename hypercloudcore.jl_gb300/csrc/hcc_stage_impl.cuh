@@ -192,6 +192,66 @@ __device__ __forceinline__ void implicit_part(const StageArgs<T> &a, T *Y, T *KI
     }
 }
 
+// ----------------------------------------------------------------------------------- slope limiters
+// limiter_phi (Limiter.jl:35-46): Barth-Jespersen min(1, r); Venkatakrishnan (r² + 2r)/(r² + r + 2), for r > 1 in
+// s = 1/r.
+template <typename T>
+__device__ __forceinline__ T limiter_phi(int lim, T r) {
+    if (lim == HCC_LIMITER_BJ_SOFT || lim == HCC_LIMITER_BJ_HARD) return vmin(T(1), r);
+    const T rp = vmax(T(0), r);
+    const T sv = T(1) / vmax(T(1), rp);
+    const T small = (rp * rp + T(2) * rp) / (rp * rp + rp + T(2));
+    const T large = (T(1) + T(2) * sv) / (T(1) + sv + T(2) * (sv * sv));
+    return rp > T(1) ? large : small;
+}
+
+template <typename T> __device__ __forceinline__ T eps16();
+template <> __device__ __forceinline__ double eps16<double>() { return 16.0 * 2.220446049250313e-16; }
+template <> __device__ __forceinline__ float eps16<float>() { return 16.0f * 1.1920929e-7f; }
+
+// _limit_slopes for BJ / VK (Limiter.jl:120-143): local extrema over {i} ∪ N(i) (_local_extrema, :61-69), the
+// bounding coefficient over the interface reconstructions (_bounding_phi / _update_phi, :76-100), then the
+// gradient terms (hard: every term; soft: the first-degree ones) scaled by it.
+template <typename T, int D, int M, int RDEG>
+__device__ __forceinline__ void limit_slopes(const StageArgs<T> &a, int64_t i, int cnt, const T *fi,
+                                             T (*out)[M]) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    const int64_t np = a.g.npad;
+    T umax[M], umin[M], phi[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) { umax[m] = fi[m]; umin[m] = fi[m]; phi[m] = T(1); }
+    for (int k = 0; k < cnt; ++k) {
+        const int32_t j = a.g.nidx[int64_t(k) * np + i];
+        T fj[M];
+        load_vec<T, M>(a.U + int64_t(j) * M, fj);
+#pragma unroll
+        for (int m = 0; m < M; ++m) { umax[m] = vmax(umax[m], fj[m]); umin[m] = vmin(umin[m], fj[m]); }
+    }
+    const T tol16 = eps16<T>();
+    for (int k = 0; k < cnt; ++k) {
+        T hx[D], p[BR];
+#pragma unroll
+        for (int d = 0; d < D; ++d) hx[d] = T(0.5) * a.g.dist[(int64_t(k) * D + d) * np + i];
+        recon_basis<D, RDEG, T>(hx, p);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            T recon = out[0][m] * p[0];
+#pragma unroll
+            for (int b = 1; b < BR; ++b) recon = recon + out[b][m] * p[b];
+            const T bound = recon > T(0) ? umax[m] : umin[m];
+            const T tol = tol16 * vmax(fabs(fi[m]), fabs(bound));
+            if (fabs(recon) > tol) phi[m] = vmin(phi[m], limiter_phi<T>(a.sc.limiter, (bound - fi[m]) / recon));
+        }
+    }
+    const bool hard = a.sc.limiter == HCC_LIMITER_BJ_HARD || a.sc.limiter == HCC_LIMITER_VK_HARD;
+#pragma unroll
+    for (int b = 0; b < BR; ++b)
+        if (hard || b < D) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) out[b][m] = out[b][m] * phi[m];
+        }
+}
+
 // ----------------------------------------------------------------------------------- gather pass
 // update_content! of MUSCL (MUSCL.jl:351-384) with NoLimiter: starved-order lowering, cached full-order fit
 // (apply_weights, Interpolators.jl:585-602), dynamic lower-degree fit, or zero (order 1).
@@ -349,10 +409,76 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
             }
         }
     }
+    if (a.sc.limiter != HCC_LIMITER_NONE && p > 1) limit_slopes<T, D, M, RDEG>(a, i, cnt, fi, out);
 #pragma unroll
     for (int b = 0; b < BR; ++b)
 #pragma unroll
         for (int m = 0; m < M; ++m) g[b * M + m] = out[b][m];
+}
+
+// Epilogue of a flux pass for particle i: K_E[s] stored, the next candidate formed (_stage_predictor!,
+// TimeSteppers.jl:400-421, and the implicit part), the Euler substep (:511-518) and the MOOD check of the next
+// checkpoint (_mood_flag!, MOOD.jl:289-295) against the extrema mn/mx of {i} ∪ N(i) of the stage state.
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i, const T *fi, const T *Kv,
+                                               const T *mn, const T *mx) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) a.K[i * M + m] = Kv[m];
+    if (!a.form_next) return;
+    // _stage_predictor! for the next candidate
+    T Y[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
+    for (int j = 0; j < a.n_prev; ++j) {
+        if (a.hE[j] != T(0)) {
+            const T h = a.hE[j];
+            if (j == a.self_slot) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * Kv[m];
+            } else {
+#pragma unroll
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KE[j][i * M + m];
+            }
+        }
+        if (a.hI[j] != T(0)) {
+            const T h = a.hI[j];
+#pragma unroll
+            for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KI[j][i * M + m];
+        }
+    }
+    if (a.implicit_mode) {
+        T KIo[M];
+        implicit_part<T, D, M, PDE>(a, Y, KIo);
+#pragma unroll
+        for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
+    if (!a.check) return;
+    T cand[M];
+    if (a.check_substep) {
+        if (a.KIs) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * (Kv[m] + a.KIs[i * M + m]);
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * Kv[m];
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < M; ++m) cand[m] = Y[m];
+    }
+    const bool adm = admissible<T, D, M, PDE>(a.ph, cand);
+    bool flag = !adm;
+    if (a.sc.criterion == HCC_MOOD_ONLY) flag = true;
+    else if (a.sc.criterion == HCC_MOOD_U1 && !flag) {
+        const T dl = a.delta, d3 = dl * dl * dl;
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+            if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - dl || cand[m] > mx[m] + dl)) flag = true;
+    }
+    a.triggered[i] = flag;
+    a.inadm[i] = !adm;
 }
 
 // ----------------------------------------------------------------------------------- flux pass
@@ -498,65 +624,170 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
     }
     T Kv[M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-        Kv[m] = -(T(2) * acc[m].value());
-        a.K[i * M + m] = Kv[m];
-    }
-    if (!a.form_next) return;
-    // _stage_predictor! for the next candidate
-    T Y[M];
-#pragma unroll
-    for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
-    for (int j = 0; j < a.n_prev; ++j) {
-        if (a.hE[j] != T(0)) {
-            const T h = a.hE[j];
-            if (j == a.self_slot) {
-#pragma unroll
-                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * Kv[m];
+    for (int m = 0; m < M; ++m) Kv[m] = -(T(2) * acc[m].value());
+    stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
+}
+
+// ----------------------------------------------------------------------------------- WENO (scalar)
+// _cholesky_moment (Interpolators.jl:31-64) and C \ b for a fixed basis size B (FP64).
+template <int B>
+__device__ __forceinline__ bool chol_upper_fixed(const double *A, double *U) {
+    for (int q = 0; q < B * B; ++q) U[q] = 0.0;
+    for (int r = 0; r < B; ++r)
+        for (int c = r; c < B; ++c) {
+            double sm = A[r * B + c];
+            for (int q = 0; q < r; ++q) sm = sm - U[q * B + r] * U[q * B + c];
+            if (r == c) {
+                if (!(sm > 0.0)) return false;
+                U[r * B + r] = sqrt(sm);
             } else {
-#pragma unroll
-                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KE[j][i * M + m];
+                U[r * B + c] = sm / U[r * B + r];
             }
         }
-        if (a.hI[j] != T(0)) {
-            const T h = a.hI[j];
-#pragma unroll
-            for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KI[j][i * M + m];
+    return true;
+}
+template <int B>
+__device__ __forceinline__ bool chol_moment_fixed(double *N, double *U) {
+    bool ok = chol_upper_fixed<B>(N, U);
+    if (ok) {
+        for (int q = 0; q < B; ++q) {
+            const double u = U[q * B + q];
+            if (!(u * u > 10.0 * 2.220446049250313e-16 * N[q * B + q])) { ok = false; break; }
         }
     }
-    if (a.implicit_mode) {
-        T KIo[M];
-        implicit_part<T, D, M, PDE>(a, Y, KIo);
-#pragma unroll
-        for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
+    if (ok) return true;
+    double tr = 0.0;
+    for (int q = 0; q < B; ++q) tr = tr + N[q * B + q];
+    const double er = 1.4901161193847656e-08 * tr / double(B);
+    for (int q = 0; q < B; ++q) N[q * B + q] = N[q * B + q] + er;
+    return chol_upper_fixed<B>(N, U);
+}
+template <int B>
+__device__ __forceinline__ void chol_solve_fixed(const double *U, const double *b, double *x) {
+    double y[B];
+    for (int r = 0; r < B; ++r) {
+        double t = b[r];
+        for (int q = 0; q < r; ++q) t = t - U[q * B + r] * y[q];
+        y[r] = t / U[r * B + r];
     }
-#pragma unroll
-    for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
-    if (!a.check) return;
-    T cand[M];
-    if (a.check_substep) {
-        if (a.KIs) {
-#pragma unroll
-            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * (Kv[m] + a.KIs[i * M + m]);
-        } else {
-#pragma unroll
-            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * Kv[m];
+    for (int r = B - 1; r >= 0; --r) {
+        double t = y[r];
+        for (int q = r + 1; q < B; ++q) t = t - U[r * B + q] * x[q];
+        x[r] = t / U[r * B + r];
+    }
+}
+
+// _mls_solve_masked of degree Q (Interpolators.jl:412-443) over the slots of particle i, all of them (dsel < 0) or
+// the one-sided stencil along axis dsel (upwind side of the velocity); out[0..D) = the first-derivative
+// coefficients (scaled by invL). Returns the factorisation status (out = 0 when it fails).
+template <typename T, int D, int Q>
+__device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, bool use_left, double fi,
+                         double *out) {
+    constexpr int B = ExpTable<D, Q>::B;
+    const int64_t np = a.g.npad;
+    double N[B * B], bs[B];
+    for (int q = 0; q < B * B; ++q) N[q] = 0.0;
+    for (int q = 0; q < B; ++q) bs[q] = 0.0;
+    for (int k = 0; k < cnt; ++k) {
+        if (dsel >= 0) {
+            const double dd = double(a.g.dist[(int64_t(k) * D + dsel) * np + i]);
+            if (!((use_left && dd < 0.0) || (!use_left && dd >= 0.0))) continue;
         }
-    } else {
+        const int64_t s = int64_t(k) * np + i;
+        double x[D], p[B];
 #pragma unroll
-        for (int m = 0; m < M; ++m) cand[m] = Y[m];
+        for (int d = 0; d < D; ++d) x[d] = double(a.g.dist[(int64_t(k) * D + d) * np + i]) * a.g.invL64;
+        table_basis<D, Q, double>(x, p);
+        const double w = double(a.g.wt[s]);
+        const double df = double(a.U[a.g.nidx[s]]) - fi;
+        for (int r = 0; r < B; ++r)
+            for (int c = 0; c < B; ++c) N[r * B + c] = N[r * B + c] + w * (p[r] * p[c]);
+        for (int r = 0; r < B; ++r) bs[r] = bs[r] + w * (p[r] * df);
     }
-    const bool adm = admissible<T, D, M, PDE>(a.ph, cand);
-    bool flag = !adm;
-    if (a.sc.criterion == HCC_MOOD_ONLY) flag = true;
-    else if (a.sc.criterion == HCC_MOOD_U1 && !flag) {
-        const T dl = a.delta, d3 = dl * dl * dl;
 #pragma unroll
-        for (int m = 0; m < M; ++m)
-            if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - dl || cand[m] > mx[m] + dl)) flag = true;
+    for (int d = 0; d < D; ++d) out[d] = 0.0;
+    double U[B * B], xs[B];
+    if (!chol_moment_fixed<B>(N, U)) return false;
+    chol_solve_fixed<B>(U, bs, xs);
+#pragma unroll
+    for (int d = 0; d < D; ++d) out[d] = xs[d] * a.g.invL64;   // degree-1 scale factors
+    return true;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void weno_fit_q(int q, const StageArgs<T> &a, int64_t i, int cnt, int dsel, bool left,
+                                           double fi, double *out) {
+    if (q == 1) weno_fit<T, D, 1>(a, i, cnt, dsel, left, fi, out);
+    else if (q == 2) weno_fit<T, D, 2>(a, i, cnt, dsel, left, fi, out);
+    else weno_fit<T, D, 3>(a, i, cnt, dsel, left, fi, out);
+}
+
+// The WENO functor (WENO.jl:55-165): central fit over the whole stencil and one upwind one-sided fit per axis,
+// blended with w_S = 1 / (1 + (a_S / a_C)^2) on smoothness indicators IS = Σ_d (∂_d u)^2 h^2 normalised by
+// max(u_i^2, IS_C); the result is Σ_d v_d ∂_d u and K_E = -that. Fits in FP64 in both paths.
+template <typename T, int D>
+__global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.g.n) return;
+    if (a.g.bnd[i]) {
+        if (a.full) a.K[i] = T(0);
+        return;
     }
-    a.triggered[i] = flag;
-    a.inadm[i] = !adm;
+    if (!(a.full || a.mask[i])) return;
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    const T fiT = a.U[i];
+    T mn = fiT, mx = fiT;
+    if (a.check && a.sc.criterion == HCC_MOOD_U1)
+        for (int k = 0; k < cnt; ++k) {
+            const T fj = a.U[a.g.nidx[int64_t(k) * np + i]];
+            mn = vmin(mn, fj);
+            mx = vmax(mx, fj);
+        }
+    const double fi = double(fiT);
+    double div_total = 0.0;
+    int p_order = a.orders[i];
+    while (p_order > 1 && cnt < basis_count(D, p_order)) --p_order;
+    if (cnt >= basis_count(D, p_order)) {
+        const int DO = a.sc.DO;
+        const double dx2 = a.g.h64 * a.g.h64;
+        double resC[D];
+        weno_fit_q<T, D>(DO == 0 ? p_order : (DO < p_order ? DO : p_order), a, i, cnt, -1, false, fi, resC);
+        double smoothC = (resC[0] * resC[0]) * dx2;
+#pragma unroll
+        for (int d = 1; d < D; ++d) smoothC = smoothC + (resC[d] * resC[d]) * dx2;
+        double s2 = jmax(fi * fi, smoothC);
+        s2 = s2 > 0.0 ? s2 : 1.0;
+        const double aC = smoothC / s2 + 1e-12;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double vel = double(a.ph.c[d][0]);
+            const bool use_left = vel > 0.0;
+            int stencil = 0;
+            for (int k = 0; k < cnt; ++k) {
+                const double dd = double(a.g.dist[(int64_t(k) * D + d) * np + i]);
+                stencil += (use_left && dd < 0.0) || (!use_left && dd >= 0.0);
+            }
+            int p_d = p_order;
+            while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
+            if (stencil < basis_count(D, p_d)) {
+                div_total = div_total + resC[d] * vel;
+                continue;
+            }
+            double resS[D];
+            weno_fit_q<T, D>(DO == 0 ? p_d : (DO < p_d ? DO : p_d), a, i, cnt, d, use_left, fi, resS);
+            double smoothS = (resS[0] * resS[0]) * dx2;
+#pragma unroll
+            for (int e = 1; e < D; ++e) smoothS = smoothS + (resS[e] * resS[e]) * dx2;
+            const double q = (smoothS / s2 + 1e-12) / aC;
+            const double wS = 1.0 / (1.0 + q * q);
+            const double wC = 1.0 - wS;
+            const double div_d = wS * resS[d] + wC * resC[d];
+            div_total = div_total + div_d * vel;
+        }
+    }
+    const T Kv = T(-div_total);
+    stage_epilogue<T, D, 1, HCC_PDE_ADVECTION>(a, i, &fiT, &Kv, &mn, &mx);
 }
 
 // form_candidate!(ts, eq, pg, 1, dt, t) (TimeSteppers.jl:365-397) for stage 1: Y_1 = Uⁿ (interior),
@@ -632,8 +863,13 @@ struct StageInst {
     static void cfl(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s) {
         k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args), dt_bits);
     }
+    static void weno(const void *args, int64_t n, cudaStream_t s) {
+        if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION)
+            k_weno<T, D><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+    }
     static const StageOps *ops() {
-        static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl, nullptr};
+        static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,
+                                   (M == 1 && PDE == HCC_PDE_ADVECTION) ? &weno : nullptr};
         return &o;
     }
 };

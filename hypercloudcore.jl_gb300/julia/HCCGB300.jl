@@ -33,7 +33,7 @@ mutable struct HccConfig
     abi_version::Int32; dim::Int32; n_vars::Int32; pde::Int32; precision::Int32; muscl_order::Int32
     div_order::Int32; mood_criterion::Int32; mood_strategy::Int32; tableau::Int32; mood_substeps::Int32
     periodic::NTuple{3, Int32}; bc_by_tag::NTuple{16, Int32}; max_mood_iterations::Int32
-    reserved_i::NTuple{8, Int32}
+    scheme::Int32; limiter::Int32; slot_capacity::Int32; reserved_i::NTuple{5, Int32}
     dx::NTuple{3, Float64}; radius::Float64; weight_alpha::Float64
     canvas_min::NTuple{3, Float64}; canvas_max::NTuple{3, Float64}
     domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
@@ -58,6 +58,11 @@ end
 _tableau_id(bt) = error("unknown tableau")
 _strategy_id(::EPD0) = Int32(1); _strategy_id(::EPD1) = Int32(2); _strategy_id(::EPD2) = Int32(3)
 _strategy_id(::MOODStrategy) = Int32(0)
+_limiter_id(::NoLimiter) = Int32(0)
+_limiter_id(::BarthJespersenLimiter{:soft}) = Int32(1)
+_limiter_id(::BarthJespersenLimiter{:hard}) = Int32(2)
+_limiter_id(::VenkatakrishnanLimiter{:soft}) = Int32(3)
+_limiter_id(::VenkatakrishnanLimiter{:hard}) = Int32(4)
 _criterion(c::MOODu1) = (Int32(1), Float64(c.d))
 _criterion(::MOODPAD) = (Int32(2), 0.0)
 _criterion(::OnlyMOOD) = (Int32(3), 0.0)
@@ -69,6 +74,7 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     cfg.dim, cfg.n_vars, cfg.pde = D, M, hcc_pde_kind(eq)
     cfg.precision = precision === :fp32 ? 1 : 0
     cfg.muscl_order = HyperCloudCore._extract_order(interp)
+    cfg.limiter = _limiter_id(interp.limiter)
     cfg.tableau = tableau_id
     cfg.mood_strategy = _strategy_id(mood.strategy)
     cfg.mood_criterion, cfg.mood_delta = _criterion(mood.criterion)

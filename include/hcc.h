@@ -78,6 +78,19 @@ typedef enum {               /* src/TimeStepping/ButcherTableaus.jl */
     HCC_TAB_IMEX_PRSSP3 = 9, HCC_TAB_IMEX_SSP2332 = 10
 } hcc_tableau;
 
+typedef enum {               /* divergence interpolator (src/Interpolation/) */
+    HCC_SCHEME_MUSCL = 0,    /* MUSCL (MUSCL.jl), streamed divergence */
+    HCC_SCHEME_WENO = 1      /* meshless WENO, scalar equations only (WENO.jl) */
+} hcc_scheme;
+
+typedef enum {               /* slope limiters of the MUSCL pre-pass (Limiter.jl) */
+    HCC_LIMITER_NONE = 0,    /* NoLimiter */
+    HCC_LIMITER_BJ_SOFT = 1, /* BarthJespersenLimiter(:soft): limits the first-degree terms */
+    HCC_LIMITER_BJ_HARD = 2, /* BarthJespersenLimiter(:hard): limits every term */
+    HCC_LIMITER_VK_SOFT = 3, /* VenkatakrishnanLimiter(:soft) */
+    HCC_LIMITER_VK_HARD = 4  /* VenkatakrishnanLimiter(:hard) */
+} hcc_limiter;
+
 typedef enum {               /* src/Grid/BoundaryConditions.jl */
     HCC_BC_KEEP = 0,         /* no condition for the tag: the particle keeps its start-of-step state */
     HCC_BC_DIRICHLET = 1,    /* FixedDirichlet */
@@ -100,7 +113,10 @@ typedef struct {
     int32_t periodic[HCC_MAX_DIM];     /* per axis */
     int32_t bc_by_tag[HCC_MAX_TAGS];   /* hcc_bc_kind per boundary tag 1..16 (index tag-1) */
     int32_t max_mood_iterations;       /* cap of the MOOD fixed point per checkpoint (0 -> 64) */
-    int32_t reserved_i[8];
+    int32_t scheme;                    /* hcc_scheme */
+    int32_t limiter;                   /* hcc_limiter (MUSCL only) */
+    int32_t slot_capacity;             /* neighbours per particle the lists may hold (0: no limit) */
+    int32_t reserved_i[5];
     double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
     double  radius;                    /* support radius R of ExponentialWeightFunction */
     double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */

@@ -516,6 +516,7 @@ struct Solver {
 
     // scheme
     int max_order = 2, DO = 0, rdeg = 1, Br = 1, full_div = 2, ddeg = 1, Bd = 2;
+    bool weno = false;
     double invL = 1.0;
     bool streamed = true;
     bool have_geom = false;
@@ -552,7 +553,9 @@ struct Solver {
             invLwrap[d] = per[d] ? 1.0 / Lphys[d] : 0.0;
         }
         max_order = c.muscl_order;
+        weno = c.scheme == HCC_SCHEME_WENO;
         if (max_order < 1 || max_order > 3) { err = "muscl_order must be 1..3"; return false; }
+        if (weno && (M != 1 || c.pde == HCC_PDE_EULER)) { err = "WENO is a scalar scheme (n_vars = 1)"; return false; }
         DO = c.div_order > max_order ? max_order : c.div_order;
         rdeg = std::max(1, max_order - 1);
         Br = basis_count(D, rdeg);
@@ -805,6 +808,7 @@ struct Solver {
                     for (int c = 1; c < Br; ++c) acc = acc + inv[b * Br + c] * bs[c * M + m];
                     g[b * M + m] = acc * sc[b];
                 }
+            if (cfg.limiter != HCC_LIMITER_NONE) limit_slopes(i, U, g);
             return;
         }
         // dispatch_interpolator: Interpolator{D, p_order-1, 1} _mls_solve (Interpolators.jl:372-400), padded
@@ -825,14 +829,16 @@ struct Solver {
                 for (int m = 0; m < M; ++m) bs[b * M + m] = bs[b * M + m] + w * (p[b] * df[m]);
         }
         double Uc[400];
-        if (!cholesky_moment(B, Nm, Uc)) return;
-        double sc[32] = {0}, col[32] = {0}, x[32] = {0};
-        build_scales(bt, invL, sc);
-        for (int m = 0; m < M; ++m) {
-            for (int b = 0; b < B; ++b) col[b] = bs[b * M + m];
-            chol_solve(B, Uc, col, x);
-            for (int b = 0; b < B; ++b) g[b * M + m] = x[b] * sc[b];
+        if (cholesky_moment(B, Nm, Uc)) {
+            double sc[32] = {0}, col[32] = {0}, x[32] = {0};
+            build_scales(bt, invL, sc);
+            for (int m = 0; m < M; ++m) {
+                for (int b = 0; b < B; ++b) col[b] = bs[b * M + m];
+                chol_solve(B, Uc, col, x);
+                for (int b = 0; b < B; ++b) g[b * M + m] = x[b] * sc[b];
+            }
         }
+        if (cfg.limiter != HCC_LIMITER_NONE) limit_slopes(i, U, g);
     }
 
     // ------------------------------------------------------------ MOOD interface orders (MOOD.jl:66-87)
@@ -854,6 +860,50 @@ struct Solver {
         int max_spatial = rdeg + 1;
         int keep = (order >= 2 && order <= max_spatial) ? basis_count(D, order - 1) : 0;
         for (int b = keep; b < Br; ++b) p[b] = 0.0;
+    }
+
+    // ------------------------------------------------------------ slope limiters (Limiter.jl:35-143)
+    // limiter_phi: Barth-Jespersen min(1, r); Venkatakrishnan (r^2 + 2r)/(r^2 + r + 2), its r > 1 branch
+    // written in s = 1/r (Limiter.jl:37-46).
+    double limiter_phi(double r) const {
+        int lim = cfg.limiter;
+        if (lim == HCC_LIMITER_BJ_SOFT || lim == HCC_LIMITER_BJ_HARD) return jmin(1.0, r);
+        double rp = jmax(0.0, r);
+        double sv = 1.0 / jmax(1.0, rp);
+        double small = (rp * rp + 2.0 * rp) / (rp * rp + rp + 2.0);
+        double large = (1.0 + 2.0 * sv) / (1.0 + sv + 2.0 * (sv * sv));
+        return rp > 1.0 ? large : small;
+    }
+    // _limit_slopes for BJ / VK (Limiter.jl:120-143) with _local_extrema, _bounding_phi and _update_phi (:61-100).
+    void limit_slopes(int64_t i, const double *U, double *g) const {
+        const double *fi = &U[i * M];
+        double umax[HCC_MAX_VARS], umin[HCC_MAX_VARS], phi[HCC_MAX_VARS];
+        for (int m = 0; m < M; ++m) { umax[m] = umin[m] = fi[m]; phi[m] = 1.0; }
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            const double *rj = &U[int64_t(nidx[s]) * M];
+            for (int m = 0; m < M; ++m) { umax[m] = jmax(umax[m], rj[m]); umin[m] = jmin(umin[m], rj[m]); }
+        }
+        const BasisTable &bt = basis_table(D, rdeg);
+        const double tol16 = 16.0 * kEps;
+        double p[32], hd[3];
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            for (int d = 0; d < D; ++d) hd[d] = 0.5 * ndist[s * D + d];
+            build_basis(bt, hd, p);
+            for (int m = 0; m < M; ++m) {
+                double recon = g[0 * M + m] * p[0];
+                for (int b = 1; b < Br; ++b) recon = recon + g[b * M + m] * p[b];
+                double bound = recon > 0.0 ? umax[m] : umin[m];
+                double tol = tol16 * jmax(std::fabs(fi[m]), std::fabs(bound));
+                if (std::fabs(recon) > tol) {
+                    double r = (bound - fi[m]) / recon;
+                    phi[m] = jmin(phi[m], limiter_phi(r));
+                }
+            }
+        }
+        bool hard = cfg.limiter == HCC_LIMITER_BJ_HARD || cfg.limiter == HCC_LIMITER_VK_HARD;
+        for (int b = 0; b < Br; ++b)
+            if (hard || b < D)
+                for (int m = 0; m < M; ++m) g[b * M + m] = g[b * M + m] * phi[m];
     }
 
     // ------------------------------------------------------------ flux pass (MUSCL.jl:390-508)
@@ -1017,8 +1067,135 @@ struct Solver {
         }
     }
 
+    // ------------------------------------------------------------ WENO (WENO.jl:55-165), scalar
+    // _mls_solve_masked (Interpolators.jl:412-443) of degree q over the slots with mask[k]; out[0..B) scaled.
+    bool masked_fit(int64_t i, const double *U, int q, const std::vector<uint8_t> &mask, double *out) const {
+        const BasisTable &bt = basis_table(D, q);
+        const int B = bt.B;
+        double Nm[400], bs[32], p[32], sd[3];
+        for (int k = 0; k < B * B; ++k) Nm[k] = 0.0;
+        for (int b = 0; b < B; ++b) bs[b] = 0.0;
+        const double fi = U[i];
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            if (!mask[s - start[i]]) continue;
+            for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
+            build_basis(bt, sd, p);
+            double w = nw[s];
+            double df = U[nidx[s]] - fi;
+            for (int r = 0; r < B; ++r)
+                for (int c = 0; c < B; ++c) Nm[r * B + c] = Nm[r * B + c] + w * (p[r] * p[c]);
+            for (int b = 0; b < B; ++b) bs[b] = bs[b] + w * (p[b] * df);
+        }
+        for (int b = 0; b < B; ++b) out[b] = 0.0;
+        double Uc[400], x[32], sc[32];
+        if (!cholesky_moment(B, Nm, Uc)) return false;
+        chol_solve(B, Uc, bs, x);
+        build_scales(bt, invL, sc);
+        for (int b = 0; b < B; ++b) out[b] = x[b] * sc[b];
+        return true;
+    }
+
+    double weno_particle(int64_t i, const double *U) const {
+        const int num = nnb(i);
+        int p_order = orders[i];
+        while (p_order > 1) {
+            if (num >= basis_count(D, p_order)) break;
+            p_order -= 1;
+        }
+        if (num < basis_count(D, p_order)) return 0.0;
+        const double fi = U[i];
+        double hmin = cfg.dx[0];                         // scale_val = minimum(pg.meta.dx)
+        for (int d = 1; d < D; ++d) hmin = std::min(hmin, cfg.dx[d]);
+        const double dx2 = hmin * hmin;
+        std::vector<uint8_t> mask(num, 1);
+        double resC[32];
+        int div_idx_C = DO == 0 ? p_order : std::min(DO, p_order);
+        masked_fit(i, U, div_idx_C, mask, resC);
+        double smoothC = (resC[0] * resC[0]) * dx2;
+        for (int k = 1; k < D; ++k) smoothC = smoothC + (resC[k] * resC[k]) * dx2;
+        double s2 = jmax(fi * fi, smoothC);
+        s2 = s2 > 0.0 ? s2 : 1.0;
+        const double aC = smoothC / s2 + 1e-12;
+        double div_total = 0.0;
+        for (int d = 0; d < D; ++d) {
+            const double vel = phys.c[d][0];
+            const bool use_left = vel > 0.0;
+            int stencil = 0;
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                double dk = ndist[s * D + d];
+                bool in = (use_left && dk < 0.0) || (!use_left && dk >= 0.0);
+                mask[s - start[i]] = in;
+                stencil += in;
+            }
+            int p_d = p_order;
+            while (p_d > 1) {
+                if (stencil >= basis_count(D, p_d)) break;
+                p_d -= 1;
+            }
+            if (stencil < basis_count(D, p_d)) {
+                div_total = div_total + resC[d] * vel;
+                continue;
+            }
+            int div_idx_S = DO == 0 ? p_d : std::min(DO, p_d);
+            double resS[32];
+            masked_fit(i, U, div_idx_S, mask, resS);
+            double smoothS = (resS[0] * resS[0]) * dx2;
+            for (int k = 1; k < D; ++k) smoothS = smoothS + (resS[k] * resS[k]) * dx2;
+            double q = (smoothS / s2 + 1e-12) / aC;
+            double wS = 1.0 / (1.0 + q * q);
+            double wC = 1.0 - wS;
+            double div_d = wS * resS[d] + wC * resC[d];
+            div_total = div_total + div_d * vel;
+        }
+        return div_total;
+    }
+
+    // _cfl_body! (ParticleGrids.jl:427-436) with _compute_cfl_coeffs (:296-329): the assembled Taylor fit of
+    // degree `degree` per particle (schemes without cached per-slot weights, WENO).
+    double cfl_sum_assembled(int64_t i, const double *Lambda_i, int degree) const {
+        const BasisTable &bt = basis_table(D, degree);
+        const int B = bt.B;
+        double Nm[400], Uc[400], Inv[400], p[32], sd[3];
+        for (int k = 0; k < B * B; ++k) Nm[k] = 0.0;
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
+            build_basis(bt, sd, p);
+            double w = nw[s];
+            for (int r = 0; r < B; ++r)
+                for (int c = 0; c < B; ++c) Nm[r * B + c] = Nm[r * B + c] + w * (p[r] * p[c]);
+        }
+        if (!cholesky_moment(B, Nm, Uc)) return 0.0;
+        chol_inverse(B, Uc, Inv);
+        double sum_c = 0.0;
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
+            build_basis(bt, sd, p);
+            double w = nw[s];
+            const double *Uj = &rhos[int64_t(nidx[s]) * M];
+            double dot = 0.0;
+            for (int d = 0; d < D; ++d) {
+                double cv = Inv[d * B + 0] * p[0];
+                for (int jb = 1; jb < B; ++jb) cv = cv + Inv[d * B + jb] * p[jb];
+                double c = std::fabs(cv * w * invL);
+                double pr = c * jmax(Lambda_i[d], phys.lam(Uj, d));
+                dot = (d == 0) ? pr : dot + pr;
+            }
+            sum_c = sum_c + dot;
+        }
+        return sum_c;
+    }
+
     // compute_explicit_rhs! (TimeSteppers.jl:312-356)
     void compute_rhs(std::vector<double> &K, const double *Ystate, bool full) {
+        if (weno) {
+#pragma omp parallel for schedule(dynamic, 256)
+            for (int64_t p = 0; p < N; ++p) {
+                if (bnd[p]) { if (full) K[p] = 0.0; continue; }
+                if (!(full || dirty[p])) continue;
+                K[p] = -weno_particle(p, Ystate);
+            }
+            return;
+        }
 #pragma omp parallel for schedule(dynamic, 256)
         for (int64_t p = 0; p < N; ++p) {
             if (bnd[p] || !(full || changed[p])) continue;
@@ -1195,7 +1372,8 @@ struct Solver {
         }
     }
 
-    int order_reach() const { return cfg.mood_strategy == HCC_EPD2 ? 2 : 1; }
+    // _order_reach (MUSCL_hooks.jl:10-11; API.jl:250 default 0 for schemes that read no neighbour orders: WENO)
+    int order_reach() const { return weno ? 0 : (cfg.mood_strategy == HCC_EPD2 ? 2 : 1); }
 
     bool mood_checkpoint(int i, double dt) {
         const std::vector<double> &Yprev = Y[i - 2];
@@ -1261,6 +1439,13 @@ struct Solver {
             const double *Ui = &rhos[i * M];
             double Li[3];
             for (int d = 0; d < D; ++d) Li[d] = phys.lam(Ui, d);
+            if (weno) {
+                // dispatch_cfl: degree _divergence_degree(WENO) = its order, clamped to 3 in 3-D / 4 otherwise
+                int degree = std::min(max_order, D == 3 ? 3 : 4);
+                double sc = cfl_sum_assembled(i, Li, degree);
+                if (sc > tol) best = std::min(best, inv_dim / sc);
+                continue;
+            }
             double sum_c = 0.0;
             for (int64_t s = start[i]; s < start[i + 1]; ++s) {
                 const double *Uj = &rhos[int64_t(nidx[s]) * M];

@@ -10,7 +10,8 @@ from conftest import ROOT
 
 def _declared_symbols():
     text = (ROOT / "include" / "hcc.h").read_text()
-    return sorted(set(re.findall(r"\b(hcc_[a-z0-9_]+)\s*\(", text)))
+    # function declarations: a line that starts with a return type and names an hcc_ function
+    return sorted(set(re.findall(r"(?m)^(?:const\s+)?[a-z_]+\s*\**\s*(hcc_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_declares_the_entry_points():

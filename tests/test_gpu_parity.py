@@ -171,3 +171,67 @@ def test_fp32_bulk_within_tolerance(hcc, oracle, cuda_lib):
     interior = cloud.is_boundary == 0
     l1 = np.abs(Ug[interior, 0] - Uo[interior, 0]).sum() / np.abs(Uo[interior, 0]).sum()
     assert l1 < 1e-4, l1
+
+
+@pytest.mark.parametrize("order,limiter", [(3, "vk_hard"), (2, "bj_soft"), (3, "bj_hard")])
+def test_limited_muscl_steps_bit_exact(hcc, oracle, cuda_lib, order, limiter):
+    """MUSCL with Barth-Jespersen / Venkatakrishnan limiting (Limiter.jl:120-143) + MOOD: states, orders, flags."""
+    h = 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=13)
+    mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(order, 0, limiter), mood=mood, bc_map=OUTFLOW)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    U0 = quadrant_ic(cloud)
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.orders(), o.orders())
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+
+
+def test_published_benchmark_case_bit_exact(hcc, oracle, cuda_lib):
+    """The reference benchmark's scheme (benchmark/step.jl:56-74): periodic lattice, advection speeds (1, 0.5),
+    MUSCL3 + VK(:hard) + MOOD(EPD1, MOODu1(1e-6)), SSP-RK3, dt = 0.3 x the CFL step; a 64^2 cloud."""
+    n = 64
+    h = 1.0 / n
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True)
+    cfg = hcc.make_config(hcc.LinearAdvection(((1.0,), (0.5,))), cloud, scheme=hcc.MUSCL(3, 0, "vk_hard"),
+                          mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-6)))
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    U0 = np.exp(-((cloud.pos - 0.5) ** 2).sum(axis=1) / 0.02)[:, None]
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.3 * o.time_step()
+    assert g.time_step() == o.time_step()
+    for k in range(4):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+    assert _bits_equal(g.download_state(), o.download_state())
+    np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+
+
+@pytest.mark.parametrize("D,order", [(1, 2), (2, 2), (2, 3), (3, 2)])
+def test_weno_steps_bit_exact(hcc, oracle, cuda_lib, D, order):
+    """Scalar meshless WENO (WENO.jl:55-165) with MOOD u1: RHS, CFL (assembled Taylor fit) and states."""
+    h = {1: 0.02, 2: 0.04, 3: 0.1}[D]
+    cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=17)
+    vel = tuple(((1.0, 0.5, -0.3)[d],) for d in range(D))
+    cfg = hcc.make_config(hcc.LinearAdvection(vel), cloud, scheme=hcc.WENO(order),
+                          mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D)))
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    r2 = ((cloud.pos - 0.5) ** 2).sum(axis=1)
+    U0 = np.where(r2 < 0.04, 1.0, 0.0)[:, None] + 0.1 * np.exp(-r2 / 0.02)[:, None]
+    g.upload_state(U0)
+    o.upload_state(U0)
+    assert _bits_equal(g.compute_rhs(), o.compute_rhs())
+    assert g.time_step() == o.time_step()
+    dt = 0.3 * o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())

@@ -518,3 +518,117 @@ def test_advection_converges_to_the_analytic_solution(hcc, oracle, abi):
         ex = f(pos[:, 0] - T, pos[:, 1] - 0.5 * T)
         errs.append(np.abs(o.download_state()[:, 0] - ex).mean())
     assert errs[0] / errs[1] > 2.5, errs
+
+
+# ----------------------------------------------------------------------------------------------- limiters
+def _box(x):
+    return np.where(np.abs(x) < 0.3, 1.0, 0.0)
+
+
+def test_limited_runs_are_scale_invariant_and_bounded(hcc, oracle, abi):
+    """unit_schemes.jl:519-542: MUSCL3 + VK(:hard), a box scaled by 2^-50 gives bitwise scaled results, and the
+    limited scheme stays within [0, 1]."""
+    cl = lattice_1d(hcc, 60)
+
+    def run(a):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0, "vk_hard"),
+                 tableau="RK2_SSP")
+        o.upload_state(a * _box(cl.pos[:, :1]))
+        dt = 0.4 * 2 / 60
+        for k in range(10):
+            o.step(k * dt, dt)
+        return o.download_state()[:, 0]
+
+    u1 = run(1.0)
+    us = run(2.0 ** -50)
+    assert np.array_equal(us, 2.0 ** -50 * u1)
+    assert u1.min() >= -1e-12 and u1.max() <= 1 + 1e-12
+
+
+@pytest.mark.parametrize("limiter", ["bj_soft", "vk_hard", "none"])
+def test_limited_reconstructions_stay_in_local_bounds(hcc, oracle, abi, olib, limiter):
+    """unit_schemes.jl:607-639: the midpoint reconstructions of limited MUSCL3 lie within the neighbourhood's
+    [min, max] (<= 1e-12) for steps, kinks, peaks and ramps; unlimited, the box overshoots by more than 0.1."""
+    cl = lattice_1d(hcc, 60)
+    ics = [lambda x: 0.5 * (1 + np.tanh(x / 0.04)), _box, np.abs, lambda x: np.exp(-x ** 2 / 0.002),
+           lambda x: np.where(x < 0, 0.0, np.where(x < 0.2, 5 * x, 0.5))]
+    worst_box = None
+    for n_ic, ic in enumerate(ics):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0, limiter))
+        U = ic(cl.pos[:, 0])[:, None]
+        o.upload_state(U)
+        o.compute_rhs()
+        g = o.gradients()
+        counts, idx, w, dist = o.neighbours()
+        start = np.concatenate([[0], np.cumsum(counts)])
+        worst = 0.0
+        for i in range(cl.n):
+            sl = slice(start[i], start[i + 1])
+            vals = np.concatenate([U[idx[sl], 0], [U[i, 0]]])
+            lo, hi = vals.min(), vals.max()
+            for k in range(start[i], start[i + 1]):
+                x = 0.5 * dist[k, 0]
+                r = U[i, 0] + g[i, 0, 0] * x + g[i, 1, 0] * (0.5 * x * x)
+                worst = max(worst, r - hi, lo - r)
+        if limiter == "none":
+            if n_ic == 1:
+                worst_box = worst
+        else:
+            assert worst <= 1e-12, (n_ic, worst)
+    if limiter == "none":
+        assert worst_box > 0.1
+
+
+# ----------------------------------------------------------------------------------------------- WENO
+def test_weno_is_scale_invariant(hcc, oracle, abi):
+    """unit_schemes.jl:519-542 (WENO2): a box scaled by 2^-50 gives bitwise scaled results."""
+    cl = lattice_1d(hcc, 60)
+
+    def run(a):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.WENO(2), tableau="RK2_SSP")
+        o.upload_state(a * _box(cl.pos[:, :1]))
+        dt = 0.4 * 2 / 60
+        for k in range(10):
+            o.step(k * dt, dt)
+        return o.download_state()[:, 0]
+
+    u1 = run(1.0)
+    us = run(2.0 ** -50)
+    assert np.array_equal(us, 2.0 ** -50 * u1)
+    assert np.all(np.isfinite(u1))
+
+
+def test_weno_converges_on_smooth_advection(hcc, oracle, abi):
+    """WENO2 (degree-2 fits) on a periodic 2-D cloud: the error against the characteristic solution falls by more
+    than 2.5 when h halves."""
+    errs = []
+    for n in (24, 48):
+        h = 1.0 / n
+        cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.1 * h, seed=5)
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (0.5,))), scheme=hcc.WENO(2))
+        f = lambda x, y: np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
+        o.upload_state(f(cl.pos[:, 0], cl.pos[:, 1])[:, None])
+        T = 0.1
+        dt = 0.2 * o.time_step()
+        steps = int(np.ceil(T / dt))
+        dt = T / steps
+        for k in range(steps):
+            o.step(k * dt, dt)
+        pos = o.positions()
+        errs.append(np.abs(o.download_state()[:, 0] - f(pos[:, 0] - T, pos[:, 1] - 0.5 * T)).mean())
+    assert errs[0] / errs[1] > 2.5, errs
+
+
+def test_weno_cfl_uses_the_assembled_fit(hcc, oracle, abi):
+    """get_time_step without cached weights (_cfl_body!, ParticleGrids.jl:427-436): finite and positive, and the
+    lattice value (1/D) / (Σ|c| λ) is reproduced by numpy from the same degree-2 fit."""
+    cl = lattice_1d(hcc, 40)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((2.0,),)), scheme=hcc.WENO(2))
+    o.upload_state(np.zeros((cl.n, 1)))
+    dt = o.time_step()
+    counts, idx, w, dist = o.neighbours()
+    d = dist[:4, 0] / (2 / 40)
+    P = np.stack([d, 0.5 * d * d], axis=1)
+    Nm = (w[:4, None, None] * P[:, :, None] * P[:, None, :]).sum(0)
+    c = np.abs((np.linalg.inv(Nm)[0] @ P.T) * w[:4] / (2 / 40))
+    assert dt == pytest.approx(1.0 / (c.sum() * 2.0), rel=1e-12)
