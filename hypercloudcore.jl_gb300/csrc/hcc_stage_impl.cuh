@@ -482,6 +482,14 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
 }
 
 // ----------------------------------------------------------------------------------- flux pass
+// Number of reconstruction terms an interface of order o keeps (mask_basis, Interpolators.jl:265-284):
+// basis_count(D, o - 1) for 2 <= o <= RDEG + 1, else 0 — compile-time values, no integer division per slot.
+template <int D, int RDEG>
+__device__ __forceinline__ int interface_terms(int o) {
+    constexpr int b1 = cbasis_count(D, 1), b2 = cbasis_count(D, 2);
+    return (o == 2) ? b1 : ((o == 3 && RDEG >= 2) ? b2 : 0);
+}
+
 // Resident blocks per SM the flux kernel is compiled for: as many as its registers allow without spilling
 // (FP32 2-D scalar/Euler: 80 registers; wider states and FP64 need more).
 template <typename T, int D, int M> constexpr int flux_min_blocks() {
@@ -562,8 +570,8 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
             if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
             else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
             else { oi = oi_own; oj = oj_own; }
-            const int keep_i = (oi >= 2 && oi <= RDEG + 1) ? basis_count(D, oi - 1) : 0;
-            const int keep_j = (oj >= 2 && oj <= RDEG + 1) ? basis_count(D, oj - 1) : 0;
+            const int keep_i = interface_terms<D, RDEG>(oi);
+            const int keep_j = interface_terms<D, RDEG>(oj);
             T hx[D], pi[BR], pj[BR];
 #pragma unroll
             for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
@@ -596,14 +604,13 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const bool pos = dk[d] > T(0);
-                const T sdd = pos ? jmax(lij[d], lji[d]) : jmax(lji[d], lij[d]);
+                // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
+                // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its orientation
+                const T sdd = vmax(lij[d], lji[d]);
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
-                    const T fL = pos ? fij[m] : fji[m];
-                    const T fR = pos ? fji[m] : fij[m];
-                    const T FL = pos ? Fij[d][m] : Fji[d][m];
-                    const T FR = pos ? Fji[d][m] : Fij[d][m];
-                    const T Fn = T(0.5) * ((FL + FR) - sdd * (fR - fL));
+                    const T jump = pos ? (fji[m] - fij[m]) : (fij[m] - fji[m]);
+                    const T Fn = T(0.5) * ((Fij[d][m] + Fji[d][m]) - sdd * jump);
                     const T dF = Fn - Fi[d][m];
                     t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
                 }
