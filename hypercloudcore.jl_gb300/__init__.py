@@ -357,6 +357,10 @@ class Context:
     def set_profiling(self, enable: bool = True):
         self._check(self.lib.hcc_set_profiling(self._h, int(bool(enable))), "hcc_set_profiling")
 
+    def set_step_graphs(self, enable: bool = True):
+        """Take each step as one captured CUDA graph (default) or drive the MOOD fixed points from the host."""
+        self._check(self.lib.hcc_set_step_graphs(self._h, int(bool(enable))), "hcc_set_step_graphs")
+
     def kernel_times(self, reset: bool = False) -> dict:
         t = _abi.HccKernelTimes()
         self._check(self.lib.hcc_get_kernel_times(self._h, C.byref(t), int(bool(reset))), "hcc_get_kernel_times")

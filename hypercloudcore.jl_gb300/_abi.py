@@ -57,6 +57,7 @@ class HccCounters(C.Structure):
         ("min_neighbours_interior", C.c_int32), ("total_neighbours", C.c_int64), ("mood_iterations", C.c_int64),
         ("mood_flagged", C.c_int64), ("inadmissible", C.c_int64), ("kernel_launches", C.c_int64),
         ("steps", C.c_int64), ("kernel_launches_total", C.c_int64),
+        ("graph_steps", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -102,6 +103,7 @@ PROTOTYPES = [
     ("hcc_get_counters", C.c_int, [P, C.POINTER(HccCounters)]),
     ("hcc_total_mass", C.c_int, [P, _dp]),
     ("hcc_set_profiling", C.c_int, [P, C.c_int]),
+    ("hcc_set_step_graphs", C.c_int, [P, C.c_int]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_synchronize", C.c_int, [P]),

@@ -204,8 +204,26 @@ struct hcc_ctx {
     double *d_mass = nullptr;
     bool have_cloud = false, have_nb = false, have_geom = false, have_state = false;
     // statistics
-    int64_t launches = 0, mood_iters = 0, flagged = 0, inadmissible = 0, steps = 0, launches_total = 0;
+    int64_t launches = 0, mood_iters = 0, flagged = 0, inadmissible = 0, steps = 0, launches_total = 0,
+            graph_steps = 0;
     int32_t min_nb_interior = 0;
+    // step graphs
+    cudaStream_t stream2 = nullptr;       // capture stream of the conditional bodies
+    void *coef_dev = nullptr, *coef_host = nullptr;
+    MoodStats *mood_stats = nullptr, *mood_stats_host = nullptr;
+    struct StepGraphT {
+        cudaGraphExec_t exec = nullptr;
+        void *rhos = nullptr;
+        int launches = 0, body_launches = 0;
+        void reset() {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            rhos = nullptr;
+        }
+    } graphs[2];
+    bool use_graphs = true, graphs_failed = false;
+    int n_checkpoints() const { return cfg.mood_criterion != HCC_MOOD_NONE ? tab.s : 0; }
+    void drop_graphs() { graphs[0].reset(); graphs[1].reset(); }
     // profiling: event pairs around gather (kind 0) and flux (kind 1) launches of the current step
     int prof = 0;
     std::vector<cudaEvent_t> ev_pool;
@@ -266,6 +284,7 @@ struct hcc_ctx {
     hcc_status sync(const char *what) { return cuda(cudaStreamSynchronize(stream), what); }
 
     void free_particles() {
+        drop_graphs();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
@@ -276,6 +295,7 @@ struct hcc_ctx {
         dfree(inadm);
     }
     void free_slots() {
+        drop_graphs();
         dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
         dfree(dw1_32);
     }
@@ -377,142 +397,294 @@ template <typename T> void apply_bcs(hcc_ctx *c, void *Y) {
     c->launches += c->nbnd > 0;
 }
 
-// The MOOD fixed point of one checkpoint (mood_checkpoint!, TimeSteppers.jl:454-477) after its full flux pass.
-template <typename T> hcc_status mood_fixed_point(hcc_ctx *c, StageArgs<T> a) {
-    const int64_t n = c->n;
-    const int reach = (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
-    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
-    for (int it = 0;; ++it) {
-        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, n, c->d_counters, c->stream);
-        c->launches += 1;
-        hcc_status st = read_counters(c, 2);
-        if (st != HCC_OK) return st;
-        const unsigned long long changed = c->h_counters[0];
-        if (changed == 0) {
-            c->inadmissible += int64_t(c->h_counters[1]);
-            return HCC_OK;
+// Coefficients of every candidate of the step (entry 0: stage 1; entry s+1: the candidate the flux pass of stage s
+// forms), from dt and the tableau, into the pinned mirror and then to the device on the context stream.
+template <typename T> hcc_status upload_coeffs(hcc_ctx *c, double dt) {
+    StageCoeffs<T> *h = static_cast<StageCoeffs<T> *>(c->coef_host);
+    const int S = c->tab.s;
+    std::memset(h, 0, sizeof(StageCoeffs<T>) * (S + 1));
+    h[0].dt_ii = T(dt * c->tab.a[0][0]);
+    h[0].inv_dt_ii = T(implicit_mode(c, 0) == 1 ? 1.0 / (dt * c->tab.a[0][0]) : 0.0);
+    for (int s = 0; s < S; ++s) {
+        StageCoeffs<T> &e = h[s + 1];
+        const bool fin = (s + 1 == S);
+        for (int j = 0; j <= s; ++j) {
+            const double at = fin ? c->tab.bt[j] : c->tab.at[s + 1][j];
+            const double ai = fin ? c->tab.b[j] : c->tab.a[s + 1][j];
+            e.hE[j] = at != 0.0 ? T(dt * at) : T(0);
+            e.hI[j] = (ai != 0.0 && c->has_source) ? T(dt * ai) : T(0);
         }
-        c->flagged += int64_t(changed);
-        if (it >= cap) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
-        ++c->mood_iters;
-        // dirty = changed ⊕ reach hops (expand_mask!, MOOD.jl:343-351); WENO reads no neighbour orders (reach 0)
-        if (c->weno) {
-            cudaMemcpyAsync(c->dirty, c->changed, size_t(n), cudaMemcpyDeviceToDevice, c->stream);
-        } else if (reach == 1) {
-            launch_expand(c->changed, c->dirty, c->cnt, c->nidx, n, c->npad, c->stream);
-        } else {
-            launch_expand(c->changed, c->scratch, c->cnt, c->nidx, n, c->npad, c->stream);
-            launch_expand(c->scratch, c->dirty, c->cnt, c->nidx, n, c->npad, c->stream);
+        if (!fin) {
+            e.dt_ii = T(dt * c->tab.a[s + 1][s + 1]);
+            e.inv_dt_ii = T(implicit_mode(c, s + 1) == 1 ? 1.0 / (dt * c->tab.a[s + 1][s + 1]) : 0.0);
         }
-        c->launches += reach;
-        StageArgs<T> ga = a;
-        ga.full = 0;
-        ga.mask = c->changed;
-        if (!c->weno) {
-            c->prof_begin(2);
-            c->ops->gather(&ga, n, c->stream);
-            c->prof_end();
-        }
-        if (c->cfg.mood_strategy == HCC_EPD2) {
-            launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
-            c->launches += 1;
-        }
-        StageArgs<T> fa = a;
-        fa.full = 0;
-        fa.mask = c->dirty;
-        c->prof_begin(2);
-        (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, c->stream);
-        c->prof_end();
-        apply_bcs<T>(c, fa.Ynext);
-        c->launches += 2;
-        if ((st = launch_check(c, "MOOD recompute")) != HCC_OK) return st;
+        e.h_sub = T(c->ratio * dt);
     }
+    return c->cuda(cudaMemcpyAsync(c->coef_dev, h, sizeof(StageCoeffs<T>) * (S + 1), cudaMemcpyHostToDevice, c->stream),
+                   "coefficient upload");
 }
 
-template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
+// Kernel arguments of stage s (s = -1: the stage-1 candidate) for the current buffer assignment.
+template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
+    const int S = c->tab.s;
+    StageArgs<T> a = base_args<T>(c);
+    a.Un = static_cast<const T *>(c->rhos);
+    for (int q = 0; q < S; ++q) {
+        a.KE[q] = static_cast<const T *>(c->KE[q]);
+        a.KI[q] = static_cast<const T *>(c->KI[q]);
+    }
+    const StageCoeffs<T> *coef = static_cast<const StageCoeffs<T> *>(c->coef_dev);
+    if (s < 0) {
+        a.Ynext = static_cast<T *>(c->Y[0]);
+        a.KInext = static_cast<T *>(c->KI[0]);
+        a.implicit_mode = implicit_mode(c, 0);
+        a.coef = coef;
+        return a;
+    }
+    const bool fin = (s + 1 == S);
+    a.U = static_cast<const T *>(c->Y[s]);
+    a.K = static_cast<T *>(c->KE[s]);
+    a.full = 1;
+    a.mask = nullptr;
+    a.form_next = 1;
+    a.n_prev = s + 1;
+    a.self_slot = s;
+    a.coef = coef + (s + 1);
+    a.Ynext = static_cast<T *>(fin ? c->cand : c->Y[s + 1]);
+    if (!fin) {
+        a.KInext = static_cast<T *>(c->KI[s + 1]);
+        a.implicit_mode = implicit_mode(c, s + 1);
+    }
+    a.check = c->cfg.mood_criterion != HCC_MOOD_NONE;
+    a.check_substep = c->ratio > 0.0;
+    a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
+    return a;
+}
+
+// Full pass of stage s: reconstruction, (EPD2 neighbourhood orders), flux with its fused epilogue, boundary
+// conditions of the new candidate. Returns the kernels launched.
+template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
+    const int64_t n = c->n;
+    int k = 0;
+    if (!c->weno) {
+        if (prof) c->prof_begin(0);
+        c->ops->gather(&a, n, st);
+        if (prof) c->prof_end();
+        ++k;
+    }
+    if (c->cfg.mood_strategy == HCC_EPD2) { launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, st); ++k; }
+    if (prof) c->prof_begin(1);
+    (c->weno ? c->ops->weno : c->ops->flux)(&a, n, st);
+    if (prof) c->prof_end();
+    ++k;
+    launch_bc_apply(a.Ynext, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
+    return k + (c->nbnd > 0);
+}
+
+// One MOOD recompute (mood_checkpoint!, TimeSteppers.jl:471-475): dirty = changed ⊕ reach hops
+// (expand_mask!, MOOD.jl:343-351; WENO reads no neighbour orders: reach 0), reconstruction on `changed`, flux
+// and candidate on `dirty`, boundary conditions. Returns the kernels launched.
+template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
+    const int64_t n = c->n;
+    const int reach = (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
+    int k = 0;
+    if (c->weno) {
+        cudaMemcpyAsync(c->dirty, c->changed, size_t(n), cudaMemcpyDeviceToDevice, st);
+    } else if (reach == 1) {
+        launch_expand(c->changed, c->dirty, c->cnt, c->nidx, n, c->npad, st);
+        ++k;
+    } else {
+        launch_expand(c->changed, c->scratch, c->cnt, c->nidx, n, c->npad, st);
+        launch_expand(c->scratch, c->dirty, c->cnt, c->nidx, n, c->npad, st);
+        k += 2;
+    }
+    StageArgs<T> ga = a;
+    ga.full = 0;
+    ga.mask = c->changed;
+    if (!c->weno) {
+        if (prof) c->prof_begin(2);
+        c->ops->gather(&ga, n, st);
+        if (prof) c->prof_end();
+        ++k;
+    }
+    if (c->cfg.mood_strategy == HCC_EPD2) { launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, st); ++k; }
+    StageArgs<T> fa = a;
+    fa.full = 0;
+    fa.mask = c->dirty;
+    if (prof) c->prof_begin(2);
+    (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, st);
+    if (prof) c->prof_end();
+    ++k;
+    launch_bc_apply(fa.Ynext, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
+    return k + (c->nbnd > 0);
+}
+
+int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
+    launch_fill_i8(c->orders, int8_t(c->max_order), c->n, st);
+    cudaMemsetAsync(c->trig_step, 0, size_t(c->n), st);
+    c->ops->stage1(args, c->n, st);
+    launch_bc_apply(c->Y[0], c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
+    return 2 + (c->nbnd > 0);
+}
+
+// The step with the MOOD fixed points driven from the host (one counter read per decrement).
+template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
     const int64_t n = c->n;
     const int S = c->tab.s;
+    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
     c->launches = 0;
     c->mood_iters = 0;
     c->flagged = 0;
     c->inadmissible = 0;
-    launch_fill_i8(c->orders, int8_t(c->max_order), n, c->stream);
-    cudaMemsetAsync(c->trig_step, 0, n, c->stream);
-    c->launches += 1;
-    StageArgs<T> base = base_args<T>(c);
-    base.Un = static_cast<const T *>(c->rhos);
+    hcc_status st = upload_coeffs<T>(c, dt);
+    if (st != HCC_OK) return st;
+    StageArgs<T> a1 = stage_args<T>(c, -1);
+    c->launches += enqueue_prologue(c, &a1, c->stream);
     for (int s = 0; s < S; ++s) {
-        base.KE[s] = static_cast<const T *>(c->KE[s]);
-        base.KI[s] = static_cast<const T *>(c->KI[s]);
-    }
-    // stage 1: form_candidate!(ts, eq, pg, 1, dt, t)
-    {
-        StageArgs<T> a = base;
-        a.Ynext = static_cast<T *>(c->Y[0]);
-        a.KInext = static_cast<T *>(c->KI[0]);
-        a.implicit_mode = implicit_mode(c, 0);
-        a.dt_ii = T(dt * c->tab.a[0][0]);
-        a.inv_dt_ii = T(a.implicit_mode == 1 ? 1.0 / (dt * c->tab.a[0][0]) : 0.0);
-        c->ops->stage1(&a, n, c->stream);
-        apply_bcs<T>(c, c->Y[0]);
-        c->launches += 1;
-    }
-    const bool check = c->cfg.mood_criterion != HCC_MOOD_NONE;
-    for (int s = 0; s < S; ++s) {
-        StageArgs<T> a = base;
-        a.U = static_cast<const T *>(c->Y[s]);
-        a.K = static_cast<T *>(c->KE[s]);
-        a.full = 1;
-        a.mask = nullptr;
-        a.form_next = 1;
-        const bool fin = (s + 1 == S);
-        a.n_prev = s + 1;
-        a.self_slot = s;
-        for (int j = 0; j <= s; ++j) {
-            const double at = fin ? c->tab.bt[j] : c->tab.at[s + 1][j];
-            const double ai = fin ? c->tab.b[j] : c->tab.a[s + 1][j];
-            a.hE[j] = at != 0.0 ? T(dt * at) : T(0);
-            a.hI[j] = (ai != 0.0 && c->has_source) ? T(dt * ai) : T(0);
-        }
-        a.Ynext = static_cast<T *>(fin ? c->cand : c->Y[s + 1]);
-        if (!fin) {
-            a.KInext = static_cast<T *>(c->KI[s + 1]);
-            a.implicit_mode = implicit_mode(c, s + 1);
-            a.dt_ii = T(dt * c->tab.a[s + 1][s + 1]);
-            a.inv_dt_ii = T(a.implicit_mode == 1 ? 1.0 / (dt * c->tab.a[s + 1][s + 1]) : 0.0);
-        }
-        a.check = check;
-        a.check_substep = c->ratio > 0.0;
-        a.h_sub = T(c->ratio * dt);
-        a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
-        if (!c->weno) {
-            c->prof_begin(0);
-            c->ops->gather(&a, n, c->stream);
-            c->prof_end();
+        StageArgs<T> a = stage_args<T>(c, s);
+        c->launches += enqueue_full<T>(c, a, c->stream, c->prof != 0);
+        if ((st = launch_check(c, "stage kernels")) != HCC_OK) return st;
+        if (!a.check) continue;
+        for (int it = 0;; ++it) {
+            launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, n, c->d_counters,
+                             c->stream);
             c->launches += 1;
+            if ((st = read_counters(c, 2)) != HCC_OK) return st;
+            const unsigned long long changed = c->h_counters[0];
+            if (changed == 0) {
+                c->inadmissible += int64_t(c->h_counters[1]);
+                break;
+            }
+            c->flagged += int64_t(changed);
+            if (it >= cap) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
+            ++c->mood_iters;
+            c->launches += enqueue_recompute<T>(c, a, c->stream, c->prof != 0);
+            if ((st = launch_check(c, "MOOD recompute")) != HCC_OK) return st;
         }
-        if (c->cfg.mood_strategy == HCC_EPD2) {
-            launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
-            c->launches += 1;
-        }
-        c->prof_begin(1);
-        (c->weno ? c->ops->weno : c->ops->flux)(&a, n, c->stream);
-        c->prof_end();
-        c->launches += 1;
-        apply_bcs<T>(c, a.Ynext);
-        hcc_status st = launch_check(c, "stage kernels");
-        if (st != HCC_OK) return st;
-        if (check && (st = mood_fixed_point<T>(c, a)) != HCC_OK) return st;
     }
     std::swap(c->rhos, c->cand);
     ++c->steps;
     c->launches_total += c->launches;
-    hcc_status st = c->sync("step");
+    st = c->sync("step");
     if (st == HCC_OK && c->prof) {
         c->prof_collect();
         c->times.steps += 1;
     }
     return st;
+}
+
+// Capture of one step as a CUDA graph: every MOOD fixed point is a conditional WHILE node whose body (recompute,
+// decrement, decision) repeats until the decision kernel finds no changed order, so the host never waits inside
+// the step. The dt-dependent coefficients are read from device memory, so one graph serves every dt; two graphs
+// alternate with the start-of-step / candidate buffers.
+template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
+    const int S = c->tab.s;
+    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
+    auto &G = c->graphs[parity];
+    G.reset();
+    cudaStream_t st = c->stream;
+    hcc_status rs = c->cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (rs != HCC_OK) return rs;
+    int launches = 0, body_launches = 0;
+    cudaError_t err = cudaSuccess;
+    cudaMemsetAsync(c->mood_stats, 0, sizeof(MoodStats), st);
+    StageArgs<T> a1 = stage_args<T>(c, -1);
+    launches += enqueue_prologue(c, &a1, st);
+    for (int s = 0; s < S && err == cudaSuccess; ++s) {
+        StageArgs<T> a = stage_args<T>(c, s);
+        launches += enqueue_full<T>(c, a, st, false);
+        if (!a.check) continue;
+        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, c->n, c->d_counters, st);
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        err = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
+        if (err != cudaSuccess) break;
+        cudaGraphConditionalHandle h;
+        err = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+        if (err != cudaSuccess) break;
+        launch_mood_decide(c->d_counters, c->mood_stats, h, cap, st);
+        launches += 2;
+        err = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+        if (err != cudaSuccess) break;
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        err = cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np);
+        if (err != cudaSuccess) break;
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        err = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (err != cudaSuccess) break;
+        err = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
+        int bl = enqueue_recompute<T>(c, a, c->stream2, false);
+        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, c->n, c->d_counters,
+                         c->stream2);
+        launch_mood_decide(c->d_counters, c->mood_stats, h, cap, c->stream2);
+        body_launches += bl + 2;
+        cudaGraph_t body_out = nullptr;
+        err = cudaStreamEndCapture(c->stream2, &body_out);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (err == cudaSuccess) err = e2;
+    if (err == cudaSuccess) err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&G.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        G.reset();
+        return c->cuda(err, "step graph capture");
+    }
+    G.rhos = c->rhos;
+    G.launches = launches;
+    G.body_launches = body_launches;
+    return HCC_OK;
+}
+
+template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
+    int parity = -1;
+    for (int q = 0; q < 2; ++q)
+        if (c->graphs[q].exec && c->graphs[q].rhos == c->rhos) parity = q;
+    hcc_status st;
+    if (parity < 0) {
+        parity = (c->graphs[0].exec == nullptr) ? 0 : 1;
+        if ((st = capture_step<T>(c, parity)) != HCC_OK) return st;
+    }
+    auto &G = c->graphs[parity];
+    if ((st = upload_coeffs<T>(c, dt)) != HCC_OK) return st;
+    if ((st = c->cuda(cudaGraphLaunch(G.exec, c->stream), "step graph launch")) != HCC_OK) return st;
+    if ((st = c->cuda(cudaMemcpyAsync(c->mood_stats_host, c->mood_stats, sizeof(MoodStats), cudaMemcpyDeviceToHost,
+                                      c->stream), "MOOD statistics")) != HCC_OK) return st;
+    if ((st = c->sync("step")) != HCC_OK) return st;
+    const MoodStats ms = *c->mood_stats_host;
+    const int nchk = c->n_checkpoints();
+    c->mood_iters = int64_t(ms.iterations);
+    c->flagged = int64_t(ms.flagged);
+    c->inadmissible = int64_t(ms.inadmissible);
+    c->launches = G.launches + (nchk > 0 ? int64_t(ms.iterations) * (G.body_launches / nchk) : 0);
+    c->launches_total += c->launches;
+    if (ms.timeout) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
+    std::swap(c->rhos, c->cand);
+    ++c->steps;
+    ++c->graph_steps;
+    return HCC_OK;
+}
+
+template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
+    if (c->use_graphs && !c->prof) {
+        hcc_status st = run_step_graph<T>(c, dt);
+        if (st != HCC_ERR_CUDA || c->graphs_failed) return st;
+        // a graph that cannot be captured or launched on this driver: the host-driven step for this context
+        c->graphs_failed = true;
+        c->use_graphs = false;
+        cudaGetLastError();
+    }
+    return run_step_host<T>(c, dt);
 }
 
 template <typename T> hcc_status run_rhs(hcc_ctx *c) {
@@ -657,6 +829,14 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->h_counters), 8 * sizeof(unsigned long long)),
                       "pinned counters")) != HCC_OK) return st;
     if ((st = c->alloc(c->d_mass, HCC_MAX_VARS, "mass")) != HCC_OK) return st;
+    if ((st = c->cuda(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking), "capture stream")) != HCC_OK)
+        return st;
+    const size_t coef_bytes = sizeof(StageCoeffs<double>) * (HCC_MAX_STAGES + 1);
+    if ((st = c->valloc(c->coef_dev, coef_bytes, "stage coefficients")) != HCC_OK) return st;
+    if ((st = c->cuda(cudaMallocHost(&c->coef_host, coef_bytes), "pinned stage coefficients")) != HCC_OK) return st;
+    if ((st = c->alloc(c->mood_stats, 1, "MOOD statistics")) != HCC_OK) return st;
+    if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->mood_stats_host), sizeof(MoodStats)),
+                      "pinned MOOD statistics")) != HCC_OK) return st;
     return HCC_OK;
 }
 
@@ -669,6 +849,12 @@ hcc_status hcc_destroy(hcc_ctx *ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_mass);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    ctx->drop_graphs();
+    if (ctx->coef_dev) cudaFree(ctx->coef_dev);
+    if (ctx->coef_host) cudaFreeHost(ctx->coef_host);
+    dfree(ctx->mood_stats);
+    if (ctx->mood_stats_host) cudaFreeHost(ctx->mood_stats_host);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -749,6 +935,7 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
 }
 
 hcc_status hcc_build_neighbours(hcc_ctx *c) {
+    if (c) c->drop_graphs();
     if (!c) return HCC_ERR_INVALID;
     if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud uploaded");
     const hcc_config &f = c->cfg;
@@ -885,6 +1072,7 @@ hcc_status hcc_download_neighbours(hcc_ctx *c, int32_t *counts, int32_t *idx, do
 }
 
 hcc_status hcc_prepare_geometry(hcc_ctx *c) {
+    if (c) c->drop_graphs();
     if (!c) return HCC_ERR_INVALID;
     if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
     hcc_status st;
@@ -1080,6 +1268,7 @@ hcc_status hcc_get_counters(hcc_ctx *c, hcc_counters *out) {
     out->kernel_launches = c->launches;
     out->steps = c->steps;
     out->kernel_launches_total = c->launches_total;
+    out->graph_steps = c->graph_steps;
     out->min_neighbours_interior = c->min_nb_interior;
     return HCC_OK;
 }
@@ -1097,6 +1286,14 @@ hcc_status hcc_set_profiling(hcc_ctx *c, int enable) {
     if (!c) return HCC_ERR_INVALID;
     c->prof = enable ? 1 : 0;
     c->ev_used = 0;
+    return HCC_OK;
+}
+
+hcc_status hcc_set_step_graphs(hcc_ctx *c, int enable) {
+    if (!c) return HCC_ERR_INVALID;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->drop_graphs();
+    c->use_graphs = enable != 0 && !c->graphs_failed;
     return HCC_OK;
 }
 

@@ -178,6 +178,16 @@ template <typename T> struct Geometry {
     double h64;                       // min(dx)
 };
 
+// dt-dependent coefficients of one candidate, read by the kernels from device memory so that one captured step
+// graph serves every dt: hE[j] = dt a_t (0 = skipped), hI[j] = dt a (0 = skipped), h_sub = dt / C of the Euler
+// substep, dt_ii = dt a_ii and its inverse for the implicit part.
+template <typename T> struct StageCoeffs {
+    T hE[HCC_MAX_STAGES];
+    T hI[HCC_MAX_STAGES];
+    T h_sub;
+    T dt_ii, inv_dt_ii;
+};
+
 // Arguments of the gather (reconstruction) and flux kernels.
 template <typename T> struct StageArgs {
     Geometry<T> g;
@@ -195,18 +205,15 @@ template <typename T> struct StageArgs {
     const T *Un;                      // start-of-step state (pg.rhos)
     const T *KE[HCC_MAX_STAGES];
     const T *KI[HCC_MAX_STAGES];
-    T hE[HCC_MAX_STAGES];             // dt * a_t (0: skipped)
-    T hI[HCC_MAX_STAGES];             // dt * a   (0: skipped)
+    const StageCoeffs<T> *coef;       // device: the dt-dependent coefficients of this candidate
     int n_prev;                       // stages entering the candidate (K_E[s] is this kernel's own)
     int self_slot;                    // index of K_E[s] among KE (its value comes from registers)
     T *Ynext;
     T *KInext;
     int implicit_mode;                // 0 none, 1 implicit solve (a_ii != 0), 2 explicit source evaluation
-    T dt_ii, inv_dt_ii;
     int check;                        // run the MOOD check of the candidate
     int check_substep;                // 1: W = Y_s + h_sub (K + KI_s), 0: the candidate itself
     const T *KIs;                     // K_I[s] for the substep of implicit-source tableaus
-    T h_sub;
     T delta;
     uint8_t *triggered;
     uint8_t *inadm;
@@ -297,6 +304,14 @@ void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const
                   int64_t npad, cudaStream_t s);
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out,
                        cudaStream_t s);
+// Device-side continuation of a MOOD fixed point inside a step graph: reads the change / inadmissible counters of
+// the last decrement, accumulates the step statistics and sets the WHILE node's condition.
+struct MoodStats {
+    unsigned long long iterations, flagged, inadmissible, timeout;
+    unsigned int iter_in_checkpoint, pad;
+};
+void launch_mood_decide(const unsigned long long *counters, MoodStats *stats, cudaGraphConditionalHandle h, int cap,
+                        cudaStream_t s);
 void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
                         int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
 

@@ -43,17 +43,17 @@ template <typename T> __device__ __forceinline__ T floatmin_of();
 template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2250738585072014e-308; }
 template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
 
-// Arithmetic kernels of the two paths. FP64 (plain path): IEEE division and square root, Julia's NaN-propagating
-// min/max — the oracle's exact sequence. FP32 (bulk path): the fast reciprocal and reciprocal square root of the
-// special-function unit (≤ 2 ulp) and fminf/fmaxf; its results are compared with the FP64 oracle to tolerance.
+// Arithmetic kernels of the two paths. FP64 (plain path): IEEE division and square root — the oracle's exact
+// sequence. FP32 (bulk path): the fast reciprocal and reciprocal square root of the special-function unit
+// (≤ 2 ulp); its results are compared with the FP64 oracle to tolerance. Both keep Julia's NaN-propagating min/max:
+// a reconstruction with negative pressure has a NaN sound speed, and the NaN must reach the candidate so that the
+// admissibility check flags it (fmaxf would drop it and keep the high order).
 template <typename T> __device__ __forceinline__ T recip(T x) { return T(1) / x; }
 template <> __device__ __forceinline__ float recip<float>(float x) { return __fdividef(1.0f, x); }
 template <typename T> __device__ __forceinline__ T root(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float root<float>(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
 template <typename T> __device__ __forceinline__ T vmin(T x, T y) { return jmin(x, y); }
-template <> __device__ __forceinline__ float vmin<float>(float x, float y) { return fminf(x, y); }
 template <typename T> __device__ __forceinline__ T vmax(T x, T y) { return jmax(x, y); }
-template <> __device__ __forceinline__ float vmax<float>(float x, float y) { return fmaxf(x, y); }
 
 // Load N contiguous elements with 16-byte vectors where the layout guarantees the alignment (particle-major
 // arrays of 4 floats / 2 doubles per vector from a 256-byte-aligned base).
@@ -174,12 +174,13 @@ __device__ __forceinline__ void implicit_part(const StageArgs<T> &a, T *Y, T *KI
         T Mk[M];
         maxwellian<T, D, M>(a.ph, Y, Mk);
         if (a.implicit_mode == 1) {
-            T dto = a.dt_ii * a.ph.inv_eps;
+            T dto = a.coef->dt_ii * a.ph.inv_eps;
             T denom = T(1) / (T(1) + dto);
+            const T inv_dt_ii = a.coef->inv_dt_ii;
 #pragma unroll
             for (int k = 0; k < M; ++k) {
                 T out = (Y[k] + dto * Mk[k]) * denom;
-                KIout[k] = (out - Y[k]) * a.inv_dt_ii;
+                KIout[k] = (out - Y[k]) * inv_dt_ii;
                 Y[k] = out;
             }
         } else {
@@ -429,9 +430,11 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
     T Y[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
+    const StageCoeffs<T> *cf = a.coef;
     for (int j = 0; j < a.n_prev; ++j) {
-        if (a.hE[j] != T(0)) {
-            const T h = a.hE[j];
+        const T hE = cf->hE[j], hI = cf->hI[j];
+        if (hE != T(0)) {
+            const T h = hE;
             if (j == a.self_slot) {
 #pragma unroll
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * Kv[m];
@@ -440,8 +443,8 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KE[j][i * M + m];
             }
         }
-        if (a.hI[j] != T(0)) {
-            const T h = a.hI[j];
+        if (hI != T(0)) {
+            const T h = hI;
 #pragma unroll
             for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KI[j][i * M + m];
         }
@@ -459,10 +462,10 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
     if (a.check_substep) {
         if (a.KIs) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * (Kv[m] + a.KIs[i * M + m]);
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + cf->h_sub * (Kv[m] + a.KIs[i * M + m]);
         } else {
 #pragma unroll
-            for (int m = 0; m < M; ++m) cand[m] = fi[m] + a.h_sub * Kv[m];
+            for (int m = 0; m < M; ++m) cand[m] = fi[m] + cf->h_sub * Kv[m];
         }
     } else {
 #pragma unroll
@@ -473,9 +476,20 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
     if (a.sc.criterion == HCC_MOOD_ONLY) flag = true;
     else if (a.sc.criterion == HCC_MOOD_U1 && !flag) {
         const T dl = a.delta, d3 = dl * dl * dl;
+        if constexpr (sizeof(T) == 8) {
 #pragma unroll
-        for (int m = 0; m < M; ++m)
-            if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - dl || cand[m] > mx[m] + dl)) flag = true;
+            for (int m = 0; m < M; ++m)
+                if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - dl || cand[m] > mx[m] + dl)) flag = true;
+        } else {
+            // FP32: the bounds are padded by 16 unit round-offs of their magnitude on top of delta, so the round-off
+            // of the FP32 update (a few units on a flat state) is not read as a new extremum.
+            constexpr T kPad = T(16) * T(1.1920928955078125e-7);
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const T pad = dl + kPad * vmax(fabs(mn[m]), fabs(mx[m]));
+                if (fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - pad || cand[m] > mx[m] + pad)) flag = true;
+            }
+        }
     }
     a.triggered[i] = flag;
     a.inadm[i] = !adm;

@@ -115,6 +115,31 @@ __global__ void k_rows(const E *src, E *dst, const int32_t *cnt, const int64_t *
         for (int q = 0; q < width; ++q) dst[(r0 + k) * width + q] = src[(int64_t(k) * width + q) * npad + i];
 }
 
+// Decision of one MOOD fixed-point iteration inside a step graph, after a drop pass (the loop condition of
+// mood_checkpoint!, TimeSteppers.jl:461-476): no changed order ends the loop and adds the inadmissible count;
+// otherwise the flagged count grows and the loop repeats, unless the checkpoint already ran `cap` recomputes
+// (the timeout flag ends it). One thread.
+__global__ void k_mood_decide(const unsigned long long *counters, MoodStats *st, cudaGraphConditionalHandle h,
+                              int cap) {
+    const unsigned long long changed = counters[0];
+    unsigned go = 0;
+    if (changed == 0) {
+        st->inadmissible += counters[1];
+        st->iter_in_checkpoint = 0;
+    } else {
+        st->flagged += changed;
+        if (st->iter_in_checkpoint >= unsigned(cap)) {
+            st->timeout = 1;
+            st->iter_in_checkpoint = 0;
+        } else {
+            st->iter_in_checkpoint += 1;
+            st->iterations += 1;
+            go = 1;
+        }
+    }
+    cudaGraphSetConditional(h, go);
+}
+
 }  // namespace
 
 void launch_cast_f64_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s) {
@@ -140,6 +165,10 @@ void launch_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint
                       const uint8_t *bnd, int64_t n, unsigned long long *counters, cudaStream_t s) {
     cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s);
     if (n > 0) k_mood_drop<<<grid_for(n), HCC_BLOCK, 0, s>>>(orders, triggered, changed, trig_step, inadm, bnd, n, counters);
+}
+void launch_mood_decide(const unsigned long long *counters, MoodStats *stats, cudaGraphConditionalHandle h, int cap,
+                        cudaStream_t s) {
+    k_mood_decide<<<1, 1, 0, s>>>(counters, stats, h, cap);
 }
 void launch_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n, int64_t npad,
                    cudaStream_t s) {

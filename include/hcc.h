@@ -146,6 +146,7 @@ typedef struct {
     int64_t kernel_launches;           /* kernels launched by the last hcc_step / hcc_time_step */
     int64_t steps;                     /* steps taken by the context */
     int64_t kernel_launches_total;     /* kernels launched since the context was created */
+    int64_t graph_steps;               /* steps taken as one captured CUDA graph (hcc_set_step_graphs) */
 } hcc_counters;
 
 typedef struct hcc_ctx hcc_ctx;
@@ -195,6 +196,12 @@ hcc_status hcc_compute_rhs(hcc_ctx *ctx, double *K);
 
 /* One time step: (ts::GeneralRKTimeStepper)(eq, pg, t, dt) (TimeSteppers.jl:531-577). */
 hcc_status hcc_step(hcc_ctx *ctx, double t, double dt);
+
+/* Run hcc_step as one captured CUDA graph (default on): each MOOD fixed point is a conditional WHILE node decided
+   on the device, with no host wait inside the step. Off: the host drives the fixed points (one counter read per
+   drop pass). Both give identical results; steps taken while profiling is on always use the host-driven form.
+   No counterpart in the reference (its loop is host-driven, TimeSteppers.jl:454-477). */
+hcc_status hcc_set_step_graphs(hcc_ctx *ctx, int enable);
 
 /* pg.core.particle_orders (N) and mood_flags(ts) (TimeSteppers.jl:258) of the last step. */
 hcc_status hcc_download_orders(hcc_ctx *ctx, int32_t *orders);

@@ -145,14 +145,11 @@ def test_bgk_imex_steps_bit_exact(hcc, oracle, cuda_lib):
         assert _bits_equal(g.download_state(), o.download_state())
 
 
-def test_fp32_bulk_within_tolerance(hcc, oracle, cuda_lib):
-    """FP32 bulk path vs the FP64 oracle after 5 steps of the quadrant problem: L1 density error below 1e-4
-    relative (FP32 round-off; MOOD decisions may differ where a candidate sits within round-off of a bound)."""
-    h = 0.02
-    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
-    mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
-    cfg64 = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=OUTFLOW)
-    cfg32 = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=OUTFLOW, precision="fp32")
+def _fp32_pair(hcc, oracle, cloud, mood, bc, pde=None, scheme=None):
+    pde = pde or hcc.Euler(2)
+    scheme = scheme or hcc.MUSCL(2, 2)
+    cfg64 = hcc.make_config(pde, cloud, scheme=scheme, mood=mood, bc_map=bc)
+    cfg32 = hcc.make_config(pde, cloud, scheme=scheme, mood=mood, bc_map=bc, precision="fp32")
     abi = __import__("sys").modules["hcc_gb300._abi"]
     o = oracle.OracleContext(cfg64, abi)
     g = hcc.Context(cfg32)
@@ -160,17 +157,102 @@ def test_fp32_bulk_within_tolerance(hcc, oracle, cuda_lib):
         c.upload_cloud(cloud)
         c.build_neighbours()
         c.prepare_geometry()
+    return g, o
+
+
+def _rel_l1(a, b, sel):
+    return np.abs(a[sel] - b[sel]).sum() / np.abs(b[sel]).sum()
+
+
+def _density_wave(cloud, t=0.0, u=1.0, v=0.5, p=1.0):
+    """Smooth Euler state: a density wave advected by a uniform flow at uniform pressure (exact solution of the
+    periodic problem: the initial wave shifted by (u, v) t)."""
+    x = (cloud.pos[:, 0] - u * t) % 1.0
+    y = (cloud.pos[:, 1] - v * t) % 1.0
+    rho = 1.0 + 0.2 * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
+    return np.stack([rho, rho * u, rho * v, p / 0.4 + 0.5 * rho * (u * u + v * v)], axis=1)
+
+
+def test_fp32_rhs_matches_fp64_oracle(hcc, oracle, cuda_lib):
+    """FP32 bulk right-hand side (FP32 reconstruction/flux/contraction with Kahan sums, FP64-built weights) vs the FP64
+    oracle on a smooth state: relative L1 below 1e-4 per component; CFL step within 1e-5."""
+    h = 0.025
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=8)
+    g, o = _fp32_pair(hcc, oracle, cloud, hcc.MOOD(hcc.EPD1, hcc.NoMOOD()), {})
+    U0 = _density_wave(cloud)
+    o.upload_state(U0)
+    g.upload_state(U0.astype(np.float32))
+    K64, K32 = o.compute_rhs(), g.compute_rhs()
+    assert np.isfinite(K64).all()
+    allp = np.ones(cloud.n, bool)
+    for m in range(4):
+        assert _rel_l1(K32[:, m], K64[:, m], allp) < 1e-4, m
+    assert abs(g.time_step() / o.time_step() - 1) < 1e-5
+
+
+def test_fp32_density_error_within_1p1_of_fp64(hcc, oracle, cuda_lib):
+    """The FP32 bulk path's L1 density error against the exact solution of the advected density wave is within
+    1.1x of the FP64 oracle's after 20 steps (the FP32 accuracy target of the path)."""
+    h = 0.025
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=8)
+    g, o = _fp32_pair(hcc, oracle, cloud, hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), {},
+                      scheme=hcc.MUSCL(3, 0))
+    U0 = _density_wave(cloud)
+    o.upload_state(U0)
+    g.upload_state(U0.astype(np.float32))
+    dt = 0.4 * o.time_step()
+    for k in range(20):
+        o.step(k * dt, dt)
+        g.step(k * dt, dt)
+    exact = _density_wave(cloud, t=20 * dt)[:, 0]
+    vol = cloud.volumes
+    e64 = np.sum(vol * np.abs(o.download_state()[:, 0] - exact))
+    e32 = np.sum(vol * np.abs(g.download_state()[:, 0] - exact))
+    assert e64 > 0 and e32 <= 1.1 * e64, (e32, e64)
+
+
+def test_fp32_smooth_steps_within_tolerance(hcc, oracle, cuda_lib):
+    """A smooth density wave advected by a uniform flow (periodic, MOOD PAD never triggers): after 10 steps the FP32
+    bulk path stays within 1e-5 relative L1 of the FP64 oracle (round-off only)."""
+    h = 0.025
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=8)
+    g, o = _fp32_pair(hcc, oracle, cloud, hcc.MOOD(hcc.EPD1, hcc.MOODPAD()), {})
+    U0 = _density_wave(cloud)
+    o.upload_state(U0)
+    g.upload_state(U0.astype(np.float32))
+    dt = 0.4 * o.time_step()
+    for k in range(10):
+        o.step(k * dt, dt)
+        g.step(k * dt, dt)
+    assert o.mood_flags().sum() == 0 and g.mood_flags().sum() == 0
+    Uo, Ug = o.download_state(), g.download_state()
+    assert _rel_l1(Ug[:, 0], Uo[:, 0], np.ones(cloud.n, bool)) < 1e-5
+
+
+@pytest.mark.parametrize("rel_delta,min_agree", [(None, 0.95), (1e-3, 0.99)])
+def test_fp32_shock_steps_close_to_fp64(hcc, oracle, cuda_lib, rel_delta, min_agree):
+    """Quadrant Riemann problem with MOOD u1 (delta = 1e-4 h^2, below FP32 resolution of the state, and 1e-3). The
+    FP32 DMP check pads the bounds by 16 FP32 unit round-offs of their magnitude, so sub-round-off oscillations that
+    FP64 flags at the tiny delta are not flagged in FP32; NaN sound speeds of inadmissible reconstructions
+    propagate to the candidate in both paths. After 5 steps the density stays within 1e-5 relative L1 of the FP64
+    oracle and the flags agree on the stated share of the particles."""
+    h = 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    delta = rel_delta if rel_delta is not None else 1e-4 * h * h
+    g, o = _fp32_pair(hcc, oracle, cloud, hcc.MOOD(hcc.EPD1, hcc.MOODu1(delta)), OUTFLOW)
     U0 = quadrant_ic(cloud)
     o.upload_state(U0)
     g.upload_state(U0.astype(np.float32))
     dt = 0.4 * o.time_step()
+    agree = []
     for k in range(5):
         o.step(k * dt, dt)
         g.step(k * dt, dt)
+        agree.append((o.mood_flags() == g.mood_flags()).mean())
     Uo, Ug = o.download_state(), g.download_state()
-    interior = cloud.is_boundary == 0
-    l1 = np.abs(Ug[interior, 0] - Uo[interior, 0]).sum() / np.abs(Uo[interior, 0]).sum()
-    assert l1 < 1e-4, l1
+    inner = cloud.is_boundary == 0
+    assert _rel_l1(Ug[:, 0], Uo[:, 0], inner) < 1e-5
+    assert min(agree) > min_agree, agree
 
 
 @pytest.mark.parametrize("order,limiter", [(3, "vk_hard"), (2, "bj_soft"), (3, "bj_hard")])
@@ -235,3 +317,71 @@ def test_weno_steps_bit_exact(hcc, oracle, cuda_lib, D, order):
         o.step(k * dt, dt)
         assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
         np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+
+
+@pytest.mark.parametrize("strategy,scheme", [("EPD1", "muscl3"), ("EPD2", "muscl2"), ("EPD0", "weno2")])
+def test_step_graph_matches_host_driven_step(hcc, oracle, cuda_lib, strategy, scheme):
+    """The captured step (MOOD fixed points as conditional WHILE nodes) and the host-driven step give the same
+    bits as the oracle, with the same MOOD statistics."""
+    weno = scheme == "weno2"
+    h = 0.04 if weno else 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=weno, jitter=0.25 * h, seed=3)
+    mood = hcc.MOOD(getattr(hcc, strategy), hcc.MOODu1(1e-4 * h * h))
+    sch = hcc.WENO(2, 0) if weno else hcc.MUSCL(int(scheme[-1]), 0)
+    pde = hcc.LinearAdvection(((1.0,), (0.5,))) if weno else hcc.Euler(2)
+    cfg = hcc.make_config(pde, cloud, scheme=sch, mood=mood, bc_map={} if weno else OUTFLOW)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    gh = hcc.Context(cfg)
+    gh.upload_cloud(cloud)
+    gh.build_neighbours()
+    gh.prepare_geometry()
+    gh.set_step_graphs(False)
+    if weno:
+        r2 = ((cloud.pos - 0.5) ** 2).sum(axis=1)
+        U0 = np.where(r2 < 0.04, 1.0, 0.0)[:, None] + 0.1 * np.exp(-r2 / 0.02)[:, None]
+    else:
+        U0 = quadrant_ic(cloud)
+    for c in (g, gh, o):
+        c.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    for k in range(5):
+        for c in (g, gh, o):
+            c.step(k * dt, dt)
+        ref = o.download_state()
+        assert _bits_equal(g.download_state(), ref), f"graph step {k}"
+        assert _bits_equal(gh.download_state(), ref), f"host step {k}"
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+        cg, ch, co = g.counters(), gh.counters(), o.counters()
+        for key in ("mood_iterations", "mood_flagged", "inadmissible"):
+            assert cg[key] == ch[key] == co[key], (k, key)
+    assert co["steps"] == 5
+    assert cg["graph_steps"] == 5 and ch["graph_steps"] == 0      # the graph form really ran
+
+
+def test_step_graph_reports_the_mood_iteration_cap(hcc, oracle, cuda_lib):
+    """A MOOD fixed point that needs more recomputes than max_mood_iterations ends the step with HCC_ERR_TIMEOUT
+    (the oracle stops the same step) and leaves the start-of-step state in place, in both step forms."""
+    h = 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(3, 0), mood=mood, bc_map=OUTFLOW,
+                          max_mood_iterations=1)
+    o = oracle.OracleContext(cfg, __import__("sys").modules["hcc_gb300._abi"])
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    o.prepare_geometry()
+    o.upload_state(quadrant_ic(cloud))
+    with pytest.raises(Exception, match="did not converge"):
+        o.step(0.0, 0.4 * o.time_step())
+    for graphs in (True, False):
+        g = hcc.Context(cfg)
+        g.upload_cloud(cloud)
+        g.build_neighbours()
+        g.prepare_geometry()
+        g.set_step_graphs(graphs)
+        U0 = quadrant_ic(cloud)
+        g.upload_state(U0)
+        dt = 0.4 * g.time_step()
+        with pytest.raises(hcc.HCCError, match="iteration cap"):
+            g.step(0.0, dt)
+        assert _bits_equal(g.download_state(), U0)
