@@ -197,8 +197,12 @@ struct hcc_ctx {
     void *xfer = nullptr;                        // n*M doubles: staging of host-precision conversions
     void *Y[HCC_MAX_STAGES] = {}, *KE[HCC_MAX_STAGES] = {}, *KI[HCC_MAX_STAGES] = {};
     int8_t *orders = nullptr, *nbmin = nullptr;
-    uint8_t *triggered = nullptr, *changed = nullptr, *dirty = nullptr, *scratch = nullptr, *trig_step = nullptr,
-            *inadm = nullptr;
+    uint8_t *trig_step = nullptr, *inadm = nullptr;
+    // MOOD tile worklists (failed candidates, changed orders, their reach): tile lists and member words
+    int32_t *ttiles = nullptr, *ctiles = nullptr, *dtiles = nullptr;
+    uint32_t *tmask = nullptr, *cmask = nullptr, *dmask = nullptr, *words1 = nullptr;
+    ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
+    int list_blocks = 1, drop_blocks = 1;
     unsigned long long *d_counters = nullptr;   // [0..1] drop counters, [2] dt bits, [3..4] search stats
     unsigned long long *h_counters = nullptr;   // pinned mirror
     double *d_mass = nullptr;
@@ -291,8 +295,8 @@ struct hcc_ctx {
         for (void **p : {&rhos, &cand, &grad, &xfer}) { if (*p) cudaFree(*p); *p = nullptr; }
         for (int s = 0; s < HCC_MAX_STAGES; ++s)
             for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
-        dfree(orders); dfree(nbmin); dfree(triggered); dfree(changed); dfree(dirty); dfree(scratch); dfree(trig_step);
-        dfree(inadm);
+        dfree(orders); dfree(nbmin); dfree(trig_step); dfree(inadm);
+        dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
     }
     void free_slots() {
         drop_graphs();
@@ -363,8 +367,11 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.orders = c->orders;
     a.nbmin = c->nbmin;
     a.grad = static_cast<T *>(c->grad);
-    a.triggered = c->triggered;
+    a.tmask = c->tmask;
+    a.ttiles = c->ttiles;
+    a.tcount = &c->lcounts->t;
     a.inadm = c->inadm;
+    a.list_blocks = c->list_blocks;
     a.delta = T(c->cfg.mood_delta);
     return a;
 }
@@ -445,7 +452,6 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
     a.U = static_cast<const T *>(c->Y[s]);
     a.K = static_cast<T *>(c->KE[s]);
     a.full = 1;
-    a.mask = nullptr;
     a.form_next = 1;
     a.n_prev = s + 1;
     a.self_slot = s;
@@ -461,8 +467,9 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
     return a;
 }
 
-// Full pass of stage s: reconstruction, (EPD2 neighbourhood orders), flux with its fused epilogue, boundary
-// conditions of the new candidate. Returns the kernels launched.
+// Full pass of stage s: reconstruction, (EPD2 neighbourhood orders), flux with its fused epilogue (the failed
+// candidates go to the t list), and — without the MOOD check — the boundary conditions of the new candidate (with
+// the check they are part of the decrement launch). Returns the kernels launched.
 template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
     const int64_t n = c->n;
     int k = 0;
@@ -472,54 +479,91 @@ template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaSt
         if (prof) c->prof_end();
         ++k;
     }
-    if (c->cfg.mood_strategy == HCC_EPD2) { launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, st); ++k; }
+    if (c->cfg.mood_strategy == HCC_EPD2) {
+        launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, nullptr, nullptr, nullptr, 0, st);
+        ++k;
+    }
     if (prof) c->prof_begin(1);
     (c->weno ? c->ops->weno : c->ops->flux)(&a, n, st);
     if (prof) c->prof_end();
     ++k;
-    launch_bc_apply(a.Ynext, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
-    return k + (c->nbnd > 0);
+    if (!a.check) {
+        launch_bc_apply(a.Ynext, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
+        k += (c->nbnd > 0);
+    }
+    return k;
 }
 
-// One MOOD recompute (mood_checkpoint!, TimeSteppers.jl:471-475): dirty = changed ⊕ reach hops
-// (expand_mask!, MOOD.jl:343-351; WENO reads no neighbour orders: reach 0), reconstruction on `changed`, flux
-// and candidate on `dirty`, boundary conditions. Returns the kernels launched.
+// Boundary conditions of the candidate Y + MOOD decrement + decision (one launch). Returns the kernels launched.
+int enqueue_drop(hcc_ctx *c, void *Y, cudaStream_t st, const cudaGraphConditionalHandle *h) {
+    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
+    DropArgs d{};
+    d.Y = Y;
+    d.rhos = c->rhos;
+    d.blist = c->blist;
+    d.bsrc = c->bsrc;
+    d.nb = c->nbnd;
+    d.M = c->M;
+    d.bc_blocks = c->nbnd > 0 ? int(std::min<int64_t>((c->nbnd + HCC_BLOCK - 1) / HCC_BLOCK, 64)) : 0;
+    d.orders = c->orders;
+    d.trig_step = c->trig_step;
+    d.ttiles = c->ttiles;
+    d.tmask = c->tmask;
+    d.ctiles = c->ctiles;
+    d.cmask = c->cmask;
+    d.counts = c->lcounts;
+    d.stats = c->mood_stats;
+    d.has_handle = h != nullptr;
+    if (h) d.h = *h;
+    d.cap = cap;
+    launch_drop_decide(d, c->f32, c->drop_blocks, st);
+    return 1;
+}
+
+// One MOOD recompute (mood_checkpoint!, TimeSteppers.jl:471-475) over worklists: reconstruction of the changed
+// particles, which also pushes their reach (one hop; a second for EPD2; expand_mask!, MOOD.jl:343-351; none for
+// WENO, which reads no neighbour orders), then the flux and candidate of the reach. Its boundary conditions come
+// with the decrement launch that follows. Returns the kernels launched.
 template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
     const int64_t n = c->n;
-    const int reach = (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
+    const int hops = c->weno ? 0 : (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
     int k = 0;
-    if (c->weno) {
-        cudaMemcpyAsync(c->dirty, c->changed, size_t(n), cudaMemcpyDeviceToDevice, st);
-    } else if (reach == 1) {
-        launch_expand(c->changed, c->dirty, c->cnt, c->nidx, n, c->npad, st);
-        ++k;
-    } else {
-        launch_expand(c->changed, c->scratch, c->cnt, c->nidx, n, c->npad, st);
-        launch_expand(c->scratch, c->dirty, c->cnt, c->nidx, n, c->npad, st);
-        k += 2;
-    }
-    StageArgs<T> ga = a;
-    ga.full = 0;
-    ga.mask = c->changed;
     if (!c->weno) {
+        StageArgs<T> ga = a;
+        ga.full = 0;
+        ga.wtiles = c->ctiles;
+        ga.wcount = &c->lcounts->c;
+        ga.wmask = c->cmask;
+        ga.rmask = c->dmask;
+        ga.rtiles = c->dtiles;
+        ga.rcount = &c->lcounts->d;
         if (prof) c->prof_begin(2);
         c->ops->gather(&ga, n, st);
         if (prof) c->prof_end();
         ++k;
     }
-    if (c->cfg.mood_strategy == HCC_EPD2) { launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, st); ++k; }
+    if (hops == 2) {
+        launch_reach_hop2(c->lcounts, c->dtiles, c->dtiles, c->dmask, c->words1, c->cnt, c->nidx, c->npad,
+                          c->list_blocks, st);
+        launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->dtiles, c->words1, &c->lcounts->d1,
+                     c->list_blocks, st);
+        k += 3;
+    }
     StageArgs<T> fa = a;
     fa.full = 0;
-    fa.mask = c->dirty;
+    fa.wtiles = hops > 0 ? c->dtiles : c->ctiles;
+    fa.wcount = hops > 0 ? &c->lcounts->d : &c->lcounts->c;
+    fa.wmask = hops > 0 ? c->dmask : c->cmask;
+    fa.clear_wmask = hops > 0;
     if (prof) c->prof_begin(2);
     (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, st);
     if (prof) c->prof_end();
-    ++k;
-    launch_bc_apply(fa.Ynext, c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
-    return k + (c->nbnd > 0);
+    return k + 1;
 }
 
 int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
+    cudaMemsetAsync(c->lcounts, 0, sizeof(ListCounts), st);
+    cudaMemsetAsync(c->mood_stats, 0, sizeof(MoodStats), st);
     launch_fill_i8(c->orders, int8_t(c->max_order), c->n, st);
     cudaMemsetAsync(c->trig_step, 0, size_t(c->n), st);
     c->ops->stage1(args, c->n, st);
@@ -528,14 +572,23 @@ int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
 }
 
 // The step with the MOOD fixed points driven from the host (one counter read per decrement).
+// Statistics of the step from the device record (both step forms).
+hcc_status read_mood_stats(hcc_ctx *c, cudaStream_t st) {
+    return c->cuda(cudaMemcpyAsync(c->mood_stats_host, c->mood_stats, sizeof(MoodStats), cudaMemcpyDeviceToHost, st),
+                   "MOOD statistics");
+}
+void take_mood_stats(hcc_ctx *c) {
+    const MoodStats &ms = *c->mood_stats_host;
+    c->mood_iters = int64_t(ms.iterations);
+    c->flagged = int64_t(ms.flagged);
+    c->inadmissible = int64_t(ms.inadmissible);
+}
+
+// The step with the MOOD fixed points driven from the host (one read of the decision per decrement).
 template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
     const int64_t n = c->n;
     const int S = c->tab.s;
-    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
     c->launches = 0;
-    c->mood_iters = 0;
-    c->flagged = 0;
-    c->inadmissible = 0;
     hcc_status st = upload_coeffs<T>(c, dt);
     if (st != HCC_OK) return st;
     StageArgs<T> a1 = stage_args<T>(c, -1);
@@ -545,41 +598,43 @@ template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
         c->launches += enqueue_full<T>(c, a, c->stream, c->prof != 0);
         if ((st = launch_check(c, "stage kernels")) != HCC_OK) return st;
         if (!a.check) continue;
-        for (int it = 0;; ++it) {
-            launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, n, c->d_counters,
-                             c->stream);
-            c->launches += 1;
-            if ((st = read_counters(c, 2)) != HCC_OK) return st;
-            const unsigned long long changed = c->h_counters[0];
-            if (changed == 0) {
-                c->inadmissible += int64_t(c->h_counters[1]);
-                break;
+        for (;;) {
+            c->launches += enqueue_drop(c, a.Ynext, c->stream, nullptr);
+            if ((st = c->cuda(cudaMemcpyAsync(c->h_lcounts, c->lcounts, sizeof(ListCounts), cudaMemcpyDeviceToHost,
+                                              c->stream), "MOOD counts")) != HCC_OK) return st;
+            if ((st = read_mood_stats(c, c->stream)) != HCC_OK) return st;
+            if ((st = c->sync("MOOD counts")) != HCC_OK) return st;
+            if (c->h_lcounts->c == 0) break;
+            if (c->mood_stats_host->timeout) {
+                take_mood_stats(c);
+                return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
             }
-            c->flagged += int64_t(changed);
-            if (it >= cap) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
-            ++c->mood_iters;
             c->launches += enqueue_recompute<T>(c, a, c->stream, c->prof != 0);
             if ((st = launch_check(c, "MOOD recompute")) != HCC_OK) return st;
         }
+        launch_count_inadmissible(c->inadm, c->bnd, n, &c->mood_stats->inadmissible, c->stream);
+        c->launches += 1;
     }
+    if ((st = read_mood_stats(c, c->stream)) != HCC_OK) return st;
+    st = c->sync("step");
+    if (st != HCC_OK) return st;
+    take_mood_stats(c);
     std::swap(c->rhos, c->cand);
     ++c->steps;
     c->launches_total += c->launches;
-    st = c->sync("step");
-    if (st == HCC_OK && c->prof) {
+    if (c->prof) {
         c->prof_collect();
         c->times.steps += 1;
     }
-    return st;
+    return HCC_OK;
 }
 
 // Capture of one step as a CUDA graph: every MOOD fixed point is a conditional WHILE node whose body (recompute,
-// decrement, decision) repeats until the decision kernel finds no changed order, so the host never waits inside
-// the step. The dt-dependent coefficients are read from device memory, so one graph serves every dt; two graphs
-// alternate with the start-of-step / candidate buffers.
+// then the decrement launch that also decides) repeats until the decision finds no changed order, so the host never
+// waits inside the step. The dt-dependent coefficients are read from device memory, so one graph serves every dt;
+// two graphs alternate with the start-of-step / candidate buffers.
 template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
     const int S = c->tab.s;
-    const int cap = c->cfg.max_mood_iterations > 0 ? c->cfg.max_mood_iterations : 64;
     auto &G = c->graphs[parity];
     G.reset();
     cudaStream_t st = c->stream;
@@ -587,14 +642,12 @@ template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
     if (rs != HCC_OK) return rs;
     int launches = 0, body_launches = 0;
     cudaError_t err = cudaSuccess;
-    cudaMemsetAsync(c->mood_stats, 0, sizeof(MoodStats), st);
     StageArgs<T> a1 = stage_args<T>(c, -1);
     launches += enqueue_prologue(c, &a1, st);
     for (int s = 0; s < S && err == cudaSuccess; ++s) {
         StageArgs<T> a = stage_args<T>(c, s);
         launches += enqueue_full<T>(c, a, st, false);
         if (!a.check) continue;
-        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, c->n, c->d_counters, st);
         cudaStreamCaptureStatus cs;
         cudaGraph_t cg = nullptr;
         const cudaGraphNode_t *deps = nullptr;
@@ -604,8 +657,7 @@ template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
         cudaGraphConditionalHandle h;
         err = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
         if (err != cudaSuccess) break;
-        launch_mood_decide(c->d_counters, c->mood_stats, h, cap, st);
-        launches += 2;
+        launches += enqueue_drop(c, a.Ynext, st, &h);
         err = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
         if (err != cudaSuccess) break;
         cudaGraphNodeParams np = {};
@@ -622,13 +674,17 @@ template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
         err = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) break;
         int bl = enqueue_recompute<T>(c, a, c->stream2, false);
-        launch_mood_drop(c->orders, c->triggered, c->changed, c->trig_step, c->inadm, c->bnd, c->n, c->d_counters,
-                         c->stream2);
-        launch_mood_decide(c->d_counters, c->mood_stats, h, cap, c->stream2);
-        body_launches += bl + 2;
+        bl += enqueue_drop(c, a.Ynext, c->stream2, &h);
+        body_launches += bl;
         cudaGraph_t body_out = nullptr;
         err = cudaStreamEndCapture(c->stream2, &body_out);
+        if (err != cudaSuccess) break;
+        // interior candidates that are not admissible once the fixed point has converged
+        launch_count_inadmissible(c->inadm, c->bnd, c->n, &c->mood_stats->inadmissible, st);
+        launches += 1;
     }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(c->mood_stats_host, c->mood_stats, sizeof(MoodStats),
+                                                  cudaMemcpyDeviceToHost, st);
     cudaGraph_t graph = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(st, &graph);
     if (err == cudaSuccess) err = e2;
@@ -658,17 +714,12 @@ template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
     auto &G = c->graphs[parity];
     if ((st = upload_coeffs<T>(c, dt)) != HCC_OK) return st;
     if ((st = c->cuda(cudaGraphLaunch(G.exec, c->stream), "step graph launch")) != HCC_OK) return st;
-    if ((st = c->cuda(cudaMemcpyAsync(c->mood_stats_host, c->mood_stats, sizeof(MoodStats), cudaMemcpyDeviceToHost,
-                                      c->stream), "MOOD statistics")) != HCC_OK) return st;
     if ((st = c->sync("step")) != HCC_OK) return st;
-    const MoodStats ms = *c->mood_stats_host;
+    take_mood_stats(c);
     const int nchk = c->n_checkpoints();
-    c->mood_iters = int64_t(ms.iterations);
-    c->flagged = int64_t(ms.flagged);
-    c->inadmissible = int64_t(ms.inadmissible);
-    c->launches = G.launches + (nchk > 0 ? int64_t(ms.iterations) * (G.body_launches / nchk) : 0);
+    c->launches = G.launches + (nchk > 0 ? c->mood_iters * (G.body_launches / nchk) : 0);
     c->launches_total += c->launches;
-    if (ms.timeout) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
+    if (c->mood_stats_host->timeout) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
     std::swap(c->rhos, c->cand);
     ++c->steps;
     ++c->graph_steps;
@@ -695,7 +746,8 @@ template <typename T> hcc_status run_rhs(hcc_ctx *c) {
     a.K = static_cast<T *>(c->KE[0]);
     a.full = 1;
     if (!c->weno) c->ops->gather(&a, n, c->stream);
-    if (c->cfg.mood_strategy == HCC_EPD2) launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, c->stream);
+    if (c->cfg.mood_strategy == HCC_EPD2)
+        launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, nullptr, nullptr, nullptr, 0, c->stream);
     (c->weno ? c->ops->weno : c->ops->flux)(&a, n, c->stream);
     hcc_status st = launch_check(c, "rhs kernels");
     if (st != HCC_OK) return st;
@@ -835,6 +887,18 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if ((st = c->valloc(c->coef_dev, coef_bytes, "stage coefficients")) != HCC_OK) return st;
     if ((st = c->cuda(cudaMallocHost(&c->coef_host, coef_bytes), "pinned stage coefficients")) != HCC_OK) return st;
     if ((st = c->alloc(c->mood_stats, 1, "MOOD statistics")) != HCC_OK) return st;
+    if ((st = c->alloc(c->lcounts, 1, "MOOD worklist counts")) != HCC_OK) return st;
+    cudaMemsetAsync(c->lcounts, 0, sizeof(ListCounts), c->stream);
+    if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->h_lcounts), sizeof(ListCounts)),
+                      "pinned MOOD worklist counts")) != HCC_OK) return st;
+    {
+        int dev = 0, sms = 0;
+        if ((st = c->cuda(cudaGetDevice(&dev), "device")) != HCC_OK) return st;
+        if ((st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) != HCC_OK)
+            return st;
+        c->list_blocks = std::max(1, sms) * 8;   // worklist passes: a few resident blocks per SM, grid-stride
+        c->drop_blocks = std::max(1, sms) * 2;
+    }
     if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->mood_stats_host), sizeof(MoodStats)),
                       "pinned MOOD statistics")) != HCC_OK) return st;
     return HCC_OK;
@@ -853,6 +917,8 @@ hcc_status hcc_destroy(hcc_ctx *ctx) {
     if (ctx->coef_dev) cudaFree(ctx->coef_dev);
     if (ctx->coef_host) cudaFreeHost(ctx->coef_host);
     dfree(ctx->mood_stats);
+    dfree(ctx->lcounts);
+    if (ctx->h_lcounts) cudaFreeHost(ctx->h_lcounts);
     if (ctx->mood_stats_host) cudaFreeHost(ctx->mood_stats_host);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -920,9 +986,15 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
     cudaMemsetAsync(c->rhos, 0, sb, c->stream);
     HCC_TRY(c->alloc(c->orders, np, "orders"));
     HCC_TRY(c->alloc(c->nbmin, np, "nbmin"));
-    for (uint8_t **p : {&c->triggered, &c->changed, &c->dirty, &c->scratch, &c->trig_step, &c->inadm}) {
+    for (uint8_t **p : {&c->trig_step, &c->inadm}) {
         HCC_TRY(c->alloc(*p, np, "masks"));
         cudaMemsetAsync(*p, 0, np, c->stream);
+    }
+    const int64_t ntiles = np / 32;
+    for (int32_t **p : {&c->ttiles, &c->ctiles, &c->dtiles}) HCC_TRY(c->alloc(*p, ntiles, "MOOD tile lists"));
+    for (uint32_t **p : {&c->tmask, &c->cmask, &c->dmask, &c->words1}) {
+        HCC_TRY(c->alloc(*p, ntiles, "MOOD tile words"));
+        cudaMemsetAsync(*p, 0, size_t(ntiles) * sizeof(uint32_t), c->stream);
     }
     launch_fill_i8(c->orders, int8_t(c->max_order), np, c->stream);
     HCC_TRY(c->cuda(cudaMemcpyAsync(c->pos, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "upload positions"));

@@ -198,8 +198,17 @@ template <typename T> struct StageArgs {
     T *grad;                          // [i * Br * M]
     const T *U;                       // stage state Y_s
     T *K;                             // K_E[s]
-    const uint8_t *mask;              // gather: changed; flux: dirty
-    int full;
+    int full;                         // 1: every particle; 0: the members of a tile worklist
+    // Worklist pass: tiles of 32 consecutive particles (one warp each, coalesced slot-major loads), the tiles to
+    // visit, their count (device) and one member bit per particle (a word per tile).
+    const int32_t *wtiles;
+    const unsigned *wcount;
+    uint32_t *wmask;
+    int clear_wmask;                  // flux pass over the reach: clear each tile's word once read
+    uint32_t *rmask;                  // gather pass over the changed orders: the reach of its members (the member
+    int32_t *rtiles;                  // and its neighbours) is marked here, each tile listed once
+    unsigned *rcount;
+    int list_blocks;                  // grid of a worklist pass (warp-stride over the tiles)
     // epilogue: next candidate (Y_{s+1} or the final state) and the MOOD check of checkpoint s+1
     int form_next;
     const T *Un;                      // start-of-step state (pg.rhos)
@@ -215,9 +224,37 @@ template <typename T> struct StageArgs {
     int check_substep;                // 1: W = Y_s + h_sub (K + KI_s), 0: the candidate itself
     const T *KIs;                     // K_I[s] for the substep of implicit-source tableaus
     T delta;
-    uint8_t *triggered;
+    uint32_t *tmask;                  // MOOD check: failed candidates (a ballot word per tile) ...
+    int32_t *ttiles;                  // ... the tiles with a failure ...
+    unsigned *tcount;                 // ... and their count
     uint8_t *inadm;
 };
+
+// Device-side tile worklists of the MOOD fixed point: t = tiles with failed candidates, c = tiles with a dropped
+// order (cn: the list being filled by the current decrement, published as c by the decision), d = the reach of the
+// changed orders (one or two hops), d1 = its one-hop part; done = blocks finished in the decrement launch.
+struct ListCounts {
+    unsigned t, c, cn, d, d1, done, pad0, pad1;
+};
+
+// Append v to a device list; warp-aggregated: one atomic per group of converged lanes.
+__device__ __forceinline__ void list_append(int32_t *list, unsigned *count, int32_t v) {
+    const unsigned act = __activemask();
+    const int lane = int(threadIdx.x & 31);
+    const int leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    list[base + unsigned(__popc(act & ((1u << lane) - 1u)))] = v;
+}
+
+// Reach of the changed orders (expand_mask!, MOOD.jl:343-351; _expand_body!, :323-335: a particle is marked if it
+// or a neighbour was), pushed from the changed particles: the neighbour relation is symmetric (one radius, exactly
+// antisymmetric distances), so marking every neighbour of a changed particle marks the same set as the pull over
+// all particles. The first bit set in a tile's word lists the tile (once).
+__device__ __forceinline__ void reach_mark(uint32_t *mask, int32_t *tiles, unsigned *count, int32_t j) {
+    if (atomicOr(&mask[j >> 5], 1u << (j & 31)) == 0u) list_append(tiles, count, j >> 5);
+}
 
 // Launchers of one (precision, D, M, pde, reconstruction degree) instantiation.
 struct StageOps {
@@ -295,23 +332,47 @@ void launch_cast_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream
 void launch_fill_i8(int8_t *p, int8_t v, int64_t n, cudaStream_t s);
 void launch_bc_apply(void *Y, const void *rhos, const int32_t *blist, const int32_t *bsrc, int64_t nb, int M,
                      int is_f32, cudaStream_t s);
-void launch_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint8_t *trig_step,
-                      const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *counters,
-                      cudaStream_t s);
-void launch_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n,
-                   int64_t npad, cudaStream_t s);
+// Second hop of the reach (EPD2): d1 = the one-hop tiles and their words (copied to words1), then the neighbours
+// of their members are marked; the neighbourhood minimum of the orders over the one-hop members.
+void launch_reach_hop2(ListCounts *counts, const int32_t *dtiles, int32_t *dtiles_out, uint32_t *dmask,
+                       uint32_t *words1, const int32_t *cnt, const int32_t *nidx, int64_t npad, int blocks,
+                       cudaStream_t s);
+// Neighbourhood minimum of the orders: every particle (tiles == nullptr) or the members of the tiles.
 void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
-                  int64_t npad, cudaStream_t s);
+                  int64_t npad, const int32_t *tiles, const uint32_t *words, const unsigned *count, int blocks,
+                  cudaStream_t s);
+void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
+                               cudaStream_t s);
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out,
                        cudaStream_t s);
-// Device-side continuation of a MOOD fixed point inside a step graph: reads the change / inadmissible counters of
-// the last decrement, accumulates the step statistics and sets the WHILE node's condition.
+// Statistics of the MOOD fixed points of one step (device; zeroed at the start of the step).
 struct MoodStats {
     unsigned long long iterations, flagged, inadmissible, timeout;
     unsigned int iter_in_checkpoint, pad;
 };
-void launch_mood_decide(const unsigned long long *counters, MoodStats *stats, cudaGraphConditionalHandle h, int cap,
-                        cudaStream_t s);
+
+// One launch after a flux pass with the MOOD check: boundary conditions of the new candidate (first bc_blocks
+// blocks), the MOOD decrement of the failed candidates into the changed list (the other blocks), and — in the last
+// block to finish — the decision of the fixed point (publish the changed list, reset the other lists, update the
+// statistics, and set the WHILE condition of a step graph when has_handle).
+struct DropArgs {
+    void *Y;
+    const void *rhos;
+    const int32_t *blist, *bsrc;
+    int64_t nb;
+    int M, bc_blocks;
+    int8_t *orders;
+    uint8_t *trig_step;
+    const int32_t *ttiles;
+    const uint32_t *tmask;
+    int32_t *ctiles;
+    uint32_t *cmask;
+    ListCounts *counts;
+    MoodStats *stats;
+    cudaGraphConditionalHandle h;
+    int has_handle, cap;
+};
+void launch_drop_decide(const DropArgs &a, int is_f32, int drop_blocks, cudaStream_t s);
 void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
                         int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
 

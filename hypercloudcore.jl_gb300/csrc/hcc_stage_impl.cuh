@@ -6,6 +6,8 @@
 // particles from consecutive addresses; neighbour states, gradients and orders are gathered through L1/L2
 // (the Morton numbering keeps a warp's stencils overlapping).
 #pragma once
+#include <algorithm>
+
 #include "hcc_internal.cuh"
 
 // Launch shape of the flux pass (threads per block, minimum resident blocks per SM for the register budget).
@@ -54,6 +56,17 @@ template <typename T> __device__ __forceinline__ T root(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float root<float>(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
 template <typename T> __device__ __forceinline__ T vmin(T x, T y) { return jmin(x, y); }
 template <typename T> __device__ __forceinline__ T vmax(T x, T y) { return jmax(x, y); }
+// FP32: the NaN-propagating forms of the min/max instructions (one instruction each)
+template <> __device__ __forceinline__ float vmin<float>(float x, float y) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
+}
+template <> __device__ __forceinline__ float vmax<float>(float x, float y) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
+}
 
 // Load N contiguous elements with 16-byte vectors where the layout guarantees the alignment (particle-major
 // arrays of 4 floats / 2 doubles per vector from a 256-byte-aligned base).
@@ -257,11 +270,9 @@ __device__ __forceinline__ void limit_slopes(const StageArgs<T> &a, int64_t i, i
 // update_content! of MUSCL (MUSCL.jl:351-384) with NoLimiter: starved-order lowering, cached full-order fit
 // (apply_weights, Interpolators.jl:585-602), dynamic lower-degree fit, or zero (order 1).
 template <typename T, int D, int M, int PDE, int RDEG>
-__global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
+__device__ __forceinline__ void gather_one(const StageArgs<T> &a, const int64_t i) {
     constexpr int BR = RBasis<D, RDEG>::B;
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= a.g.n) return;
-    if (a.g.bnd[i] || !(a.full || a.mask[i])) return;
+    if (a.g.bnd[i]) return;
     const int cnt = a.g.cnt[i];
     const int64_t np = a.g.npad;
     int p = a.orders[i];
@@ -417,15 +428,41 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
         for (int m = 0; m < M; ++m) g[b * M + m] = out[b][m];
 }
 
+// A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word)
+// that also marks the one-hop reach of each member in rmask / rtiles.
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (i < a.g.n) gather_one<T, D, M, PDE, RDEG>(a, i);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const int64_t np = a.g.npad;
+    const int lane = int(threadIdx.x & 31);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        if (!((a.wmask[tile] >> lane) & 1u)) continue;
+        const int32_t i = tile * 32 + lane;
+        gather_one<T, D, M, PDE, RDEG>(a, i);
+        if (a.rmask) {
+            reach_mark(a.rmask, a.rtiles, a.rcount, i);
+            const int c = a.g.cnt[i];
+            for (int k = 0; k < c; ++k) reach_mark(a.rmask, a.rtiles, a.rcount, a.g.nidx[int64_t(k) * np + i]);
+        }
+    }
+}
+
 // Epilogue of a flux pass for particle i: K_E[s] stored, the next candidate formed (_stage_predictor!,
 // TimeSteppers.jl:400-421, and the implicit part), the Euler substep (:511-518) and the MOOD check of the next
 // checkpoint (_mood_flag!, MOOD.jl:289-295) against the extrema mn/mx of {i} ∪ N(i) of the stage state.
 template <typename T, int D, int M, int PDE>
-__device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i, const T *fi, const T *Kv,
+__device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i, const T *fi, const T *Kv,
                                                const T *mn, const T *mx) {
 #pragma unroll
     for (int m = 0; m < M; ++m) a.K[i * M + m] = Kv[m];
-    if (!a.form_next) return;
+    if (!a.form_next) return false;
     // _stage_predictor! for the next candidate
     T Y[M];
 #pragma unroll
@@ -457,7 +494,7 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
     }
 #pragma unroll
     for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
-    if (!a.check) return;
+    if (!a.check) return false;
     T cand[M];
     if (a.check_substep) {
         if (a.KIs) {
@@ -491,8 +528,8 @@ __device__ __forceinline__ void stage_epilogue(const StageArgs<T> &a, int64_t i,
             }
         }
     }
-    a.triggered[i] = flag;
     a.inadm[i] = !adm;
+    return flag;
 }
 
 // ----------------------------------------------------------------------------------- flux pass
@@ -517,18 +554,15 @@ template <typename T, int D, int M> constexpr int flux_min_blocks() {
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
 template <typename T, int D, int M, int PDE, int RDEG>
-__global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_flux(const StageArgs<T> a) {
+__device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i) {
     constexpr int BR = RBasis<D, RDEG>::B;
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= a.g.n) return;
     if (a.g.bnd[i]) {
         if (a.full) {
 #pragma unroll
             for (int m = 0; m < M; ++m) a.K[i * M + m] = T(0);
         }
-        return;
+        return false;
     }
-    if (!(a.full || a.mask[i])) return;
     const int cnt = a.g.cnt[i];
     const int64_t np = a.g.npad;
     const T invL = a.g.invL;
@@ -537,6 +571,13 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
     load_vec<T, M>(a.U + i * M, fi);
     load_vec<T, BR * M>(a.grad + i * (BR * M), &gi[0][0]);
     flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami);
+    constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form (below)
+    if constexpr (kFast) {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int m = 0; m < M; ++m) Fi[d][m] = T(2) * Fi[d][m];
+    }
     const int oi_own = a.orders[i];
     const int didx = divergence_index(a.sc.DO, D, oi_own, cnt);
     const bool cached = a.g.ok_d[i] && didx == divergence_index(a.sc.DO, D, a.sc.max_order, cnt);
@@ -615,18 +656,36 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
             flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij);
             flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji);
             T t[M];
+            if constexpr (kFast) {
+                // FP32: 2 (F_n - F_i) = (F_ij + F_ji) - s_d max(λ) (f_ji - f_ij) - 2 F_i with s_d = sign of the
+                // axis component (the sort_flux orientation folded into the speed); the factor 2 leaves K = -Σ.
+                T jump[M];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                const bool pos = dk[d] > T(0);
-                // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
-                // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its orientation
-                const T sdd = vmax(lij[d], lji[d]);
+                for (int m = 0; m < M; ++m) jump[m] = fji[m] - fij[m];
 #pragma unroll
-                for (int m = 0; m < M; ++m) {
-                    const T jump = pos ? (fji[m] - fij[m]) : (fij[m] - fji[m]);
-                    const T Fn = T(0.5) * ((Fij[d][m] + Fji[d][m]) - sdd * jump);
-                    const T dF = Fn - Fi[d][m];
-                    t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
+                for (int d = 0; d < D; ++d) {
+                    const T ssd = dk[d] > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const T dF2 = ((Fij[d][m] + Fji[d][m]) - ssd * jump[m]) - Fi[d][m];
+                        t[m] = (d == 0) ? wk[0] * dF2 : t[m] + wk[d] * dF2;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const bool pos = dk[d] > T(0);
+                    // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
+                    // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its
+                    // orientation
+                    const T sdd = vmax(lij[d], lji[d]);
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const T jump = pos ? (fji[m] - fij[m]) : (fij[m] - fji[m]);
+                        const T Fn = T(0.5) * ((Fij[d][m] + Fji[d][m]) - sdd * jump);
+                        const T dF = Fn - Fi[d][m];
+                        t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
+                    }
                 }
             }
 #pragma unroll
@@ -645,8 +704,40 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
     }
     T Kv[M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) Kv[m] = -(T(2) * acc[m].value());
-    stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
+    for (int m = 0; m < M; ++m) Kv[m] = kFast ? -acc[m].value() : -(T(2) * acc[m].value());
+    return stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
+}
+
+// Failed candidates of one tile (a warp's ballot) into the t list.
+template <typename T> __device__ __forceinline__ void tile_failures(const StageArgs<T> &a, int64_t tile, bool f) {
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && b) {
+        a.tmask[tile] = b;
+        a.ttiles[atomicAdd(a.tcount, 1u)] = int32_t(tile);
+    }
+}
+
+// A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word;
+// the reach marks are cleared once read). Either way each warp reports the failed candidates of its tile.
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_flux(const StageArgs<T> a) {
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG>(a, i) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG>(a, i) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
 }
 
 // ----------------------------------------------------------------------------------- WENO (scalar)
@@ -747,14 +838,11 @@ __device__ __forceinline__ void weno_fit_q(int q, const StageArgs<T> &a, int64_t
 // blended with w_S = 1 / (1 + (a_S / a_C)^2) on smoothness indicators IS = Σ_d (∂_d u)^2 h^2 normalised by
 // max(u_i^2, IS_C); the result is Σ_d v_d ∂_d u and K_E = -that. Fits in FP64 in both paths.
 template <typename T, int D>
-__global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= a.g.n) return;
+__device__ __forceinline__ bool weno_one(const StageArgs<T> &a, const int64_t i) {
     if (a.g.bnd[i]) {
         if (a.full) a.K[i] = T(0);
-        return;
+        return false;
     }
-    if (!(a.full || a.mask[i])) return;
     const int cnt = a.g.cnt[i];
     const int64_t np = a.g.npad;
     const T fiT = a.U[i];
@@ -808,7 +896,29 @@ __global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
         }
     }
     const T Kv = T(-div_total);
-    stage_epilogue<T, D, 1, HCC_PDE_ADVECTION>(a, i, &fiT, &Kv, &mn, &mx);
+    return stage_epilogue<T, D, 1, HCC_PDE_ADVECTION>(a, i, &fiT, &Kv, &mn, &mx);
+}
+
+// A full pass or a worklist pass over tiles, as the MUSCL flux pass.
+template <typename T, int D>
+__global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? weno_one<T, D>(a, i) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? weno_one<T, D>(a, i) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
 }
 
 // form_candidate!(ts, eq, pg, 1, dt, t) (TimeSteppers.jl:365-397) for stage 1: Y_1 = Uⁿ (interior),
@@ -871,12 +981,17 @@ __global__ void k_cfl(const StageArgs<T> a, unsigned long long *dt_bits) {
 template <typename T, int D, int M, int PDE, int RDEG>
 struct StageInst {
     static unsigned grid(int64_t n, int bs) { return unsigned((n + bs - 1) / bs); }
+    static unsigned pass_grid(const StageArgs<T> &a, int64_t n, int bs) {
+        const unsigned g = grid(n, bs);
+        return a.full ? g : std::max(1u, std::min(g, unsigned(a.list_blocks)));
+    }
     static void gather(const void *args, int64_t n, cudaStream_t s) {
-        k_gather<T, D, M, PDE, RDEG><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+        const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        k_gather<T, D, M, PDE, RDEG><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
     }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
-        k_flux<T, D, M, PDE, RDEG><<<grid(n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(
-            *static_cast<const StageArgs<T> *>(args));
+        const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        k_flux<T, D, M, PDE, RDEG><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
     }
     static void stage1(const void *args, int64_t n, cudaStream_t s) {
         k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
@@ -885,8 +1000,10 @@ struct StageInst {
         k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args), dt_bits);
     }
     static void weno(const void *args, int64_t n, cudaStream_t s) {
-        if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION)
-            k_weno<T, D><<<grid(n, 128), 128, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
+        if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
+            const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+            k_weno<T, D><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+        }
     }
     static const StageOps *ops() {
         static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,

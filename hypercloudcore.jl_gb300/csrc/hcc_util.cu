@@ -1,5 +1,7 @@
 // hcc_util.cu — small device passes of the time stepper: boundary conditions, MOOD decrement / mask dilation /
 // neighbourhood orders, conserved totals, conversions and the row-major export of slot-major arrays.
+#include <algorithm>
+
 #include "hcc_internal.cuh"
 
 namespace hcc {
@@ -31,58 +33,137 @@ __global__ void k_bc(T *Y, const T *rhos, const int32_t *blist, const int32_t *b
     for (int m = 0; m < M; ++m) Y[b * M + m] = (src >= 0) ? Y[int64_t(src) * M + m] : rhos[b * M + m];
 }
 
-// _mood_drop! (MOOD.jl:299-309) + the change count; also counts the interior candidates that are not admissible
-// (_count_inadmissible, TimeSteppers.jl:481-490). counters: [0] changed, [1] inadmissible.
-__global__ void k_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint8_t *trig_step,
-                            const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *counters) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    unsigned ch = 0, ia = 0;
-    if (i < n) {
-        uint8_t c = 0;
-        if (triggered[i]) {
-            if (orders[i] > 1) {
-                orders[i] = int8_t(orders[i] - 1);
-                c = 1;
-                trig_step[i] = 1;
-            }
-            triggered[i] = 0;
+// After a flux pass with the MOOD check, one launch: the boundary conditions of the new candidate (blocks below
+// bc_blocks; apply_boundary_conditions!, BoundaryConditions.jl:43-130), _mood_drop! (MOOD.jl:299-309) over the
+// failed candidates — an order above 1 drops by one and the particle joins the changed list — and, in the last
+// block to finish, the loop condition of mood_checkpoint! (TimeSteppers.jl:461-476): no changed order ends the loop;
+// otherwise the flagged count grows and the loop repeats, unless the checkpoint already ran `cap` recomputes (the
+// timeout flag ends it). The decision publishes the changed list and clears the other lists for the next pass.
+template <typename T>
+__global__ void k_drop_decide(const DropArgs a) {
+    if (int(blockIdx.x) < a.bc_blocks) {
+        T *Y = static_cast<T *>(a.Y);
+        const T *rhos = static_cast<const T *>(a.rhos);
+        for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.nb;
+             q += int64_t(a.bc_blocks) * blockDim.x) {
+            const int64_t b = a.blist[q];
+            const int32_t src = a.bsrc[q];
+            for (int m = 0; m < a.M; ++m) Y[b * a.M + m] = (src >= 0) ? Y[int64_t(src) * a.M + m] : rhos[b * a.M + m];
         }
-        changed[i] = c;
-        ch = c;
-        ia = (!bnd[i] && inadm[i]) ? 1u : 0u;
+    } else {
+        // one warp per tile of failed candidates; the changed members form the tile's word of the c list
+        const unsigned nt = a.counts->t;
+        const int lane = int(threadIdx.x & 31);
+        const unsigned warp = ((blockIdx.x - unsigned(a.bc_blocks)) * blockDim.x + threadIdx.x) >> 5;
+        const unsigned nwarps = ((gridDim.x - unsigned(a.bc_blocks)) * blockDim.x) >> 5;
+        for (unsigned q = warp; q < nt; q += nwarps) {
+            const int32_t tile = a.ttiles[q];
+            const uint32_t word = a.tmask[tile];
+            const int64_t i = int64_t(tile) * 32 + lane;
+            bool ch = false;
+            if ((word >> lane) & 1u) {
+                const int8_t o = a.orders[i];
+                if (o > 1) {
+                    a.orders[i] = int8_t(o - 1);
+                    a.trig_step[i] = 1;
+                    ch = true;
+                }
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, ch);
+            if (lane == 0 && b) {
+                a.cmask[tile] = b;
+                a.ctiles[atomicAdd(&a.counts->cn, 1u)] = tile;
+            }
+        }
     }
-    unsigned bc = __ballot_sync(0xffffffffu, ch), bi = __ballot_sync(0xffffffffu, ia);
-    if ((threadIdx.x & 31) == 0) {
-        if (bc) atomicAdd(&counters[0], (unsigned long long)__popc(bc));
-        if (bi) atomicAdd(&counters[1], (unsigned long long)__popc(bi));
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&a.counts->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    ListCounts *ct = a.counts;
+    MoodStats *st = a.stats;
+    const unsigned changed = atomicAdd(&ct->cn, 0u);
+    ct->c = changed;
+    ct->cn = 0;
+    ct->t = 0;
+    ct->d = 0;
+    ct->done = 0;
+    unsigned go = 0;
+    if (changed == 0) {
+        st->iter_in_checkpoint = 0;
+    } else {
+        st->flagged += changed;
+        if (st->iter_in_checkpoint >= unsigned(a.cap)) {
+            st->timeout = 1;
+            st->iter_in_checkpoint = 0;
+        } else {
+            st->iter_in_checkpoint += 1;
+            st->iterations += 1;
+            go = 1;
+        }
+    }
+    __threadfence();
+    if (a.has_handle) cudaGraphSetConditional(a.h, go);
+}
+
+// Second hop of the reach (EPD2): the one-hop tiles d[0, d1) and their words are fixed first (the words are
+// copied before the second hop sets more bits in them), then the neighbours of their members are marked.
+__global__ void k_reach_fix(ListCounts *counts, const int32_t *dtiles, const uint32_t *dmask, uint32_t *words1) {
+    const unsigned n1 = counts->d;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts->d1 = n1;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n1; q += gridDim.x * blockDim.x)
+        words1[q] = dmask[dtiles[q]];
+}
+__global__ void k_reach_hop2(ListCounts *counts, int32_t *dtiles, uint32_t *dmask, const uint32_t *words1,
+                             const int32_t *cnt, const int32_t *nidx, int64_t npad) {
+    const unsigned n1 = counts->d1;
+    const int lane = int(threadIdx.x & 31);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < n1; q += nwarps) {
+        if (!((words1[q] >> lane) & 1u)) continue;
+        const int64_t i = int64_t(dtiles[q]) * 32 + lane;
+        const int c = cnt[i];
+        for (int k = 0; k < c; ++k) reach_mark(dmask, dtiles, &counts->d, nidx[int64_t(k) * npad + i]);
     }
 }
 
-// One hop of expand_mask! (_expand_body!, MOOD.jl:323-335: a particle is marked if it or a neighbour was), as a
-// push from the marked particles: the neighbour relation is symmetric (one radius, exactly antisymmetric
-// distances), so marking every neighbour of a marked particle marks the same set as the pull over all particles,
-// while only the few marked particles read their lists. dst must be cleared before.
-__global__ void k_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n,
-                         int64_t npad) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n || !src[i]) return;
-    dst[i] = 1;
-    const int c = cnt[i];
-    for (int k = 0; k < c; ++k) dst[nidx[int64_t(k) * npad + i]] = 1;
-}
-
-// _nb_min_order (MOOD.jl:66-74) for EPD2.
-__global__ void k_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
-                        int64_t npad) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// _nb_min_order (MOOD.jl:66-74) for EPD2, for every particle (list == nullptr) or the listed ones.
+__device__ __forceinline__ void nbmin_one(const int8_t *orders, int8_t *nbmin, const int32_t *cnt,
+                                          const int32_t *nidx, int64_t npad, int64_t i) {
     int8_t o = orders[i];
-    int c = cnt[i];
+    const int c = cnt[i];
     for (int k = 0; k < c; ++k) {
         int8_t oj = orders[nidx[int64_t(k) * npad + i]];
         o = oj < o ? oj : o;
     }
     nbmin[i] = o;
+}
+__global__ void k_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
+                        int64_t npad) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) nbmin_one(orders, nbmin, cnt, nidx, npad, i);
+}
+__global__ void k_nbmin_tiles(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx,
+                              int64_t npad, const int32_t *tiles, const uint32_t *words, const unsigned *count) {
+    const unsigned nt = *count;
+    const int lane = int(threadIdx.x & 31);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps)
+        if ((words[q] >> lane) & 1u) nbmin_one(orders, nbmin, cnt, nidx, npad, int64_t(tiles[q]) * 32 + lane);
+}
+
+// Interior candidates that are not admissible once a fixed point has converged (_count_inadmissible,
+// TimeSteppers.jl:481-490).
+__global__ void k_count_inadm(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned ia = (i < n && !bnd[i] && inadm[i]) ? 1u : 0u;
+    const unsigned b = __ballot_sync(0xffffffffu, ia);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
 }
 
 // total_mass (Volumes.jl:103-107) in FP64.
@@ -115,31 +196,6 @@ __global__ void k_rows(const E *src, E *dst, const int32_t *cnt, const int64_t *
         for (int q = 0; q < width; ++q) dst[(r0 + k) * width + q] = src[(int64_t(k) * width + q) * npad + i];
 }
 
-// Decision of one MOOD fixed-point iteration inside a step graph, after a drop pass (the loop condition of
-// mood_checkpoint!, TimeSteppers.jl:461-476): no changed order ends the loop and adds the inadmissible count;
-// otherwise the flagged count grows and the loop repeats, unless the checkpoint already ran `cap` recomputes
-// (the timeout flag ends it). One thread.
-__global__ void k_mood_decide(const unsigned long long *counters, MoodStats *st, cudaGraphConditionalHandle h,
-                              int cap) {
-    const unsigned long long changed = counters[0];
-    unsigned go = 0;
-    if (changed == 0) {
-        st->inadmissible += counters[1];
-        st->iter_in_checkpoint = 0;
-    } else {
-        st->flagged += changed;
-        if (st->iter_in_checkpoint >= unsigned(cap)) {
-            st->timeout = 1;
-            st->iter_in_checkpoint = 0;
-        } else {
-            st->iter_in_checkpoint += 1;
-            st->iterations += 1;
-            go = 1;
-        }
-    }
-    cudaGraphSetConditional(h, go);
-}
-
 }  // namespace
 
 void launch_cast_f64_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s) {
@@ -161,24 +217,28 @@ void launch_bc_apply(void *Y, const void *rhos, const int32_t *blist, const int3
         k_bc<double><<<grid_for(nb), HCC_BLOCK, 0, s>>>(static_cast<double *>(Y), static_cast<const double *>(rhos),
                                                          blist, bsrc, nb, M);
 }
-void launch_mood_drop(int8_t *orders, uint8_t *triggered, uint8_t *changed, uint8_t *trig_step, const uint8_t *inadm,
-                      const uint8_t *bnd, int64_t n, unsigned long long *counters, cudaStream_t s) {
-    cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s);
-    if (n > 0) k_mood_drop<<<grid_for(n), HCC_BLOCK, 0, s>>>(orders, triggered, changed, trig_step, inadm, bnd, n, counters);
+void launch_drop_decide(const DropArgs &a, int is_f32, int drop_blocks, cudaStream_t s) {
+    const unsigned blocks = unsigned(a.bc_blocks + std::max(1, drop_blocks));
+    if (is_f32) k_drop_decide<float><<<blocks, HCC_BLOCK, 0, s>>>(a);
+    else k_drop_decide<double><<<blocks, HCC_BLOCK, 0, s>>>(a);
 }
-void launch_mood_decide(const unsigned long long *counters, MoodStats *stats, cudaGraphConditionalHandle h, int cap,
-                        cudaStream_t s) {
-    k_mood_decide<<<1, 1, 0, s>>>(counters, stats, h, cap);
+void launch_reach_hop2(ListCounts *counts, const int32_t *dtiles, int32_t *dtiles_out, uint32_t *dmask,
+                       uint32_t *words1, const int32_t *cnt, const int32_t *nidx, int64_t npad, int blocks,
+                       cudaStream_t s) {
+    k_reach_fix<<<blocks, HCC_BLOCK, 0, s>>>(counts, dtiles, dmask, words1);
+    k_reach_hop2<<<blocks, HCC_BLOCK, 0, s>>>(counts, dtiles_out, dmask, words1, cnt, nidx, npad);
 }
-void launch_expand(const uint8_t *src, uint8_t *dst, const int32_t *cnt, const int32_t *nidx, int64_t n, int64_t npad,
-                   cudaStream_t s) {
-    if (n <= 0) return;
-    cudaMemsetAsync(dst, 0, size_t(n), s);
-    k_expand<<<grid_for(n), HCC_BLOCK, 0, s>>>(src, dst, cnt, nidx, n, npad);
-}
-void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n, int64_t npad,
+void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
+                  int64_t npad, const int32_t *tiles, const uint32_t *words, const unsigned *count, int blocks,
                   cudaStream_t s) {
-    if (n > 0) k_nbmin<<<grid_for(n), HCC_BLOCK, 0, s>>>(orders, nbmin, cnt, nidx, n, npad);
+    if (tiles)
+        k_nbmin_tiles<<<blocks, HCC_BLOCK, 0, s>>>(orders, nbmin, cnt, nidx, npad, tiles, words, count);
+    else if (n > 0)
+        k_nbmin<<<grid_for(n), HCC_BLOCK, 0, s>>>(orders, nbmin, cnt, nidx, n, npad);
+}
+void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
+                               cudaStream_t s) {
+    if (n > 0) k_count_inadm<<<grid_for(n), HCC_BLOCK, 0, s>>>(inadm, bnd, n, out);
 }
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out, cudaStream_t s) {
     cudaMemsetAsync(out, 0, sizeof(double) * M, s);
