@@ -26,8 +26,8 @@ UNITS = {
     "hcc_mls.cu": ["-fmad=false"],
     "hcc_stage_f64_r1.cu": ["-fmad=false"],
     "hcc_stage_f64_r2.cu": ["-fmad=false"],
-    "hcc_stage_f32_r1.cu": [],
-    "hcc_stage_f32_r2.cu": [],
+    "hcc_stage_f32_r1.cu": ["-ftz=true"],
+    "hcc_stage_f32_r2.cu": ["-ftz=true"],
     "hcc_noalloc.cu": ["-fmad=false"],
 }
 

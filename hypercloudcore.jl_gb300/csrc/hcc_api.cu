@@ -189,7 +189,7 @@ struct hcc_ctx {
     // geometry
     double *inv_r64 = nullptr, *inv_d64 = nullptr, *dw64 = nullptr, *dw1_64 = nullptr;
     uint8_t *ok_r = nullptr, *ok_d = nullptr, *ok_1 = nullptr;
-    float *dist32 = nullptr, *w32 = nullptr, *dw32 = nullptr, *dw1_32 = nullptr, *inv_r32 = nullptr;
+    float *dist32 = nullptr, *w32 = nullptr, *dw32 = nullptr, *dw1_32 = nullptr, *inv_r32 = nullptr, *gw32 = nullptr;
     int32_t *status = nullptr, *status2 = nullptr, *root = nullptr;
     int32_t *blist = nullptr, *bsrc = nullptr; int64_t nbnd = 0;
     // state (element type double or float)
@@ -301,7 +301,7 @@ struct hcc_ctx {
     void free_slots() {
         drop_graphs();
         dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
-        dfree(dw1_32);
+        dfree(dw1_32); dfree(gw32);
     }
     void free_bins() { dfree(binnb); dfree(cell_count); dfree(cell_cursor); dfree(cell_start); }
 };
@@ -351,6 +351,7 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     } else {
         g.dist = c->dist32; g.wt = c->w32; g.dw = c->dw32; g.dw1 = c->need_dw1 ? c->dw1_32 : nullptr;
         g.inv_r = c->inv_r32;
+        g.gw = c->gw32;
     }
     g.ok_r = c->ok_r; g.ok_d = c->ok_d; g.ok_1 = c->ok_1;
     g.bnd = c->bnd;
@@ -1169,6 +1170,11 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
         launch_cast_f64_to_f32(c->w64, c->w32, int64_t(slots), c->stream);
         launch_cast_f64_to_f32(c->dw64, c->dw32, int64_t(slots) * D, c->stream);
         launch_cast_f64_to_f32(c->inv_r64, c->inv_r32, c->npad * c->Br * c->Br, c->stream);
+        if (c->rdeg == 1 && !c->weno) {
+            HCC_TRY(c->alloc(c->gw32, slots * D, "gradient weights f32"));
+            launch_grad_weights(c->n, c->npad, D, std::max(c->kmax, 1), c->cnt, c->dist64, c->w64, c->inv_r64, c->ok_r,
+                                c->invL, c->gw32, c->stream);
+        }
         if (c->need_dw1) {
             HCC_TRY(c->alloc(c->dw1_32, slots * D, "degree-1 weights f32"));
             launch_cast_f64_to_f32(c->dw1_64, c->dw1_32, int64_t(slots) * D, c->stream);

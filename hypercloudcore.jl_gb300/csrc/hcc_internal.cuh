@@ -172,6 +172,8 @@ template <typename T> struct Geometry {
     const T *dw1;                     // degree-1 dynamic set (schemes whose full divergence degree is > 1)
     const uint8_t *ok_r, *ok_d, *ok_1;
     const T *inv_r;                   // [i * Br * Br]
+    const T *gw;                      // FP32, degree-1 reconstruction: gradient weights of the cached fit,
+                                      // [(k*D + b) * npad + i] = invL Σ_c inv_r[b][c] w_k x_k[c] (else nullptr)
     const uint8_t *bnd;
     T invL;
     double invL64;                    // 1/min(dx) in FP64 (the MLS fits of both paths)
@@ -343,6 +345,11 @@ void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const
                   cudaStream_t s);
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s);
+// Gradient weights of the cached degree-1 fit (FP64 sums, FP32 store): gw[(k*D + b) * npad + i] =
+// invL Σ_c inv_r[b][c] w_k (dist_k[c] invL) for particles with ok_r, 0 elsewhere.
+void launch_grad_weights(int64_t n, int64_t npad, int D, int kmax, const int32_t *cnt, const double *dist,
+                         const double *w, const double *inv_r, const uint8_t *ok_r, double invL, float *gw,
+                         cudaStream_t s);
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out,
                        cudaStream_t s);
 // Statistics of the MOOD fixed points of one step (device; zeroed at the start of the step).

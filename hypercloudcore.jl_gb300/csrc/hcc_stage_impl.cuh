@@ -46,14 +46,15 @@ template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2
 template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
 
 // Arithmetic kernels of the two paths. FP64 (plain path): IEEE division and square root — the oracle's exact
-// sequence. FP32 (bulk path): the fast reciprocal and reciprocal square root of the special-function unit
-// (≤ 2 ulp); its results are compared with the FP64 oracle to tolerance. Both keep Julia's NaN-propagating min/max:
+// sequence. FP32 (bulk path, compiled with denormals flushed to zero): the fast reciprocal and reciprocal square
+// root of the special-function unit (≤ 2 ulp; sqrt(x) = x rsqrt(x), 0 at 0, NaN below); its results are compared
+// with the FP64 oracle to tolerance. Both keep Julia's NaN-propagating min/max:
 // a reconstruction with negative pressure has a NaN sound speed, and the NaN must reach the candidate so that the
 // admissibility check flags it (fmaxf would drop it and keep the high order).
 template <typename T> __device__ __forceinline__ T recip(T x) { return T(1) / x; }
 template <> __device__ __forceinline__ float recip<float>(float x) { return __fdividef(1.0f, x); }
 template <typename T> __device__ __forceinline__ T root(T x) { return sqrt(x); }
-template <> __device__ __forceinline__ float root<float>(float x) { return x > 0.0f ? x * rsqrtf(x) : sqrtf(x); }
+template <> __device__ __forceinline__ float root<float>(float x) { return x == 0.0f ? 0.0f : x * rsqrtf(x); }
 template <typename T> __device__ __forceinline__ T vmin(T x, T y) { return jmin(x, y); }
 template <typename T> __device__ __forceinline__ T vmax(T x, T y) { return jmax(x, y); }
 // FP32: the NaN-propagating forms of the min/max instructions (one instruction each)
@@ -289,7 +290,38 @@ __device__ __forceinline__ void gather_one(const StageArgs<T> &a, const int64_t 
 #pragma unroll
         for (int m = 0; m < M; ++m) out[b][m] = T(0);
     const T invL = a.g.invL;
-    if (p == a.sc.max_order && p > 1 && a.g.ok_r[i]) {
+    bool done = false;
+    if constexpr (sizeof(T) == 4 && RDEG == 1) {
+        // FP32, degree 1: the cached fit as one weight vector per slot (nidx + D floats per slot)
+        if (p == a.sc.max_order && p > 1 && a.g.ok_r[i] && a.g.gw) {
+            int32_t jn = cnt > 0 ? a.g.nidx[i] : 0;
+            T gn[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) gn[d] = cnt > 0 ? a.g.gw[int64_t(d) * np + i] : T(0);
+            for (int k = 0; k < cnt; ++k) {
+                const int32_t j = jn;
+                T gk[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) gk[d] = gn[d];
+                if (k + 1 < cnt) {
+                    jn = a.g.nidx[int64_t(k + 1) * np + i];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) gn[d] = a.g.gw[(int64_t(k + 1) * D + d) * np + i];
+                }
+                T df[M];
+                load_vec<T, M>(a.U + int64_t(j) * M, df);
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const T dm = df[m] - fi[m];
+#pragma unroll
+                    for (int b = 0; b < BR; ++b) out[b][m] = out[b][m] + gk[b] * dm;
+                }
+            }
+            done = true;
+        }
+    }
+    if (done) {
+    } else if (p == a.sc.max_order && p > 1 && a.g.ok_r[i]) {
         T bs[BR][M];
 #pragma unroll
         for (int b = 0; b < BR; ++b)

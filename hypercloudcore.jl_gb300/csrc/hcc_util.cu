@@ -166,6 +166,26 @@ __global__ void k_count_inadm(const uint8_t *inadm, const uint8_t *bnd, int64_t 
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
 }
 
+// Gradient weights of the cached degree-1 fit: the reconstruction pre-pass (apply_weights, Interpolators.jl:585-602)
+// computes g_b = invL Σ_c inv_r[b][c] Σ_k w_k x_k[c] (f_j - f_i); regrouped per slot, g_b = Σ_k gw_k[b] (f_j - f_i).
+__global__ void k_grad_weights(int64_t n, int64_t npad, int D, int kmax, const int32_t *cnt, const double *dist,
+                               const double *w, const double *inv_r, const uint8_t *ok_r, double invL, float *gw) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = ok_r[i] ? cnt[i] : 0;
+    const double *inv = inv_r + i * D * D;
+    for (int k = 0; k < kmax; ++k) {
+        double x[3] = {0.0, 0.0, 0.0};
+        const double wk = k < c ? w[int64_t(k) * npad + i] : 0.0;
+        for (int d = 0; d < D; ++d) x[d] = k < c ? dist[(int64_t(k) * D + d) * npad + i] * invL : 0.0;
+        for (int b = 0; b < D; ++b) {
+            double acc = 0.0;
+            for (int q = 0; q < D; ++q) acc += inv[b * D + q] * x[q];
+            gw[(int64_t(k) * D + b) * npad + i] = float(invL * (wk * acc));
+        }
+    }
+}
+
 // total_mass (Volumes.jl:103-107) in FP64.
 template <typename T>
 __global__ void k_total_mass(const T *U, const double *vol, int64_t n, int M, double *out) {
@@ -239,6 +259,11 @@ void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s) {
     if (n > 0) k_count_inadm<<<grid_for(n), HCC_BLOCK, 0, s>>>(inadm, bnd, n, out);
+}
+void launch_grad_weights(int64_t n, int64_t npad, int D, int kmax, const int32_t *cnt, const double *dist,
+                         const double *w, const double *inv_r, const uint8_t *ok_r, double invL, float *gw,
+                         cudaStream_t s) {
+    if (n > 0) k_grad_weights<<<grid_for(n), HCC_BLOCK, 0, s>>>(n, npad, D, kmax, cnt, dist, w, inv_r, ok_r, invL, gw);
 }
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out, cudaStream_t s) {
     cudaMemsetAsync(out, 0, sizeof(double) * M, s);
