@@ -41,6 +41,51 @@ template <> struct Accum<float> {
     __device__ __forceinline__ float value() const { return s; }
 };
 
+// FP32 component vectors in pairs: the packed FP32x2 instructions of sm_100+ (per component identical to the scalar
+// operations; a - b as fma(b, -1, a) is the same rounding of the same exact value).
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 p_bc(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 p_ld(const float *x, int q) { return make_float2(x[2 * q], x[2 * q + 1]); }
+__device__ __forceinline__ void p_st(float *x, int q, float2 v) { x[2 * q] = v.x; x[2 * q + 1] = v.y; }
+
+// Per-component sums of the flux pass: FP64 plain; FP32 Kahan-compensated, in pairs (scalar tail for odd M).
+template <typename T, int M> struct AccumV {
+    T s[M];
+    __device__ __forceinline__ AccumV() {
+#pragma unroll
+        for (int m = 0; m < M; ++m) s[m] = T(0);
+    }
+    __device__ __forceinline__ void add(const T *t) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) s[m] = s[m] + t[m];
+    }
+};
+template <int M> struct AccumV<float, M> {
+    float s[M], c[M];
+    __device__ __forceinline__ AccumV() {
+#pragma unroll
+        for (int m = 0; m < M; ++m) { s[m] = 0.0f; c[m] = 0.0f; }
+    }
+    __device__ __forceinline__ void add(const float *t) {
+#pragma unroll
+        for (int q = 0; q < M / 2; ++q) {
+            const float2 y = p_sub(p_ld(t, q), p_ld(c, q));
+            const float2 u = p_add(p_ld(s, q), y);
+            p_st(c, q, p_sub(p_sub(u, p_ld(s, q)), y));
+            p_st(s, q, u);
+        }
+        if constexpr (M & 1) {
+            const float y = t[M - 1] - c[M - 1];
+            const float u = s[M - 1] + y;
+            c[M - 1] = (u - s[M - 1]) - y;
+            s[M - 1] = u;
+        }
+    }
+};
+
 template <typename T> __device__ __forceinline__ T floatmin_of();
 template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2250738585072014e-308; }
 template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
@@ -88,6 +133,22 @@ __device__ __forceinline__ void load_vec(const T *__restrict__ p, T *out) {
     } else {
 #pragma unroll
         for (int q = 0; q < N; ++q) out[q] = p[q];
+    }
+}
+
+// Store N contiguous elements with 16-byte vectors under the same alignment guarantee.
+template <typename T, int N>
+__device__ __forceinline__ void store_vec(T *__restrict__ p, const T *v) {
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 4; ++q)
+            reinterpret_cast<float4 *>(p)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else if constexpr (sizeof(T) == 8 && N % 2 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 2; ++q) reinterpret_cast<double2 *>(p)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < N; ++q) p[q] = v[q];
     }
 }
 
@@ -294,21 +355,34 @@ __device__ __forceinline__ void gather_one(const StageArgs<T> &a, const int64_t 
     if constexpr (sizeof(T) == 4 && RDEG == 1) {
         // FP32, degree 1: the cached fit as one weight vector per slot (nidx + D floats per slot)
         if (p == a.sc.max_order && p > 1 && a.g.ok_r[i] && a.g.gw) {
-            int32_t jn = cnt > 0 ? a.g.nidx[i] : 0;
-            T gn[D];
+            // slots in groups of G: the group's indices, weights and neighbour states are all in flight together
+            constexpr int G = 4;
+            int k = 0;
+            for (; k + G <= cnt; k += G) {
+                int32_t j[G];
+                T gk[G][D], df[G][M];
 #pragma unroll
-            for (int d = 0; d < D; ++d) gn[d] = cnt > 0 ? a.g.gw[int64_t(d) * np + i] : T(0);
-            for (int k = 0; k < cnt; ++k) {
-                const int32_t j = jn;
-                T gk[D];
+                for (int q = 0; q < G; ++q) {
+                    j[q] = a.g.nidx[int64_t(k + q) * np + i];
 #pragma unroll
-                for (int d = 0; d < D; ++d) gk[d] = gn[d];
-                if (k + 1 < cnt) {
-                    jn = a.g.nidx[int64_t(k + 1) * np + i];
-#pragma unroll
-                    for (int d = 0; d < D; ++d) gn[d] = a.g.gw[(int64_t(k + 1) * D + d) * np + i];
+                    for (int d = 0; d < D; ++d) gk[q][d] = a.g.gw[(int64_t(k + q) * D + d) * np + i];
                 }
-                T df[M];
+#pragma unroll
+                for (int q = 0; q < G; ++q) load_vec<T, M>(a.U + int64_t(j[q]) * M, df[q]);
+#pragma unroll
+                for (int q = 0; q < G; ++q)
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const T dm = df[q][m] - fi[m];
+#pragma unroll
+                        for (int b = 0; b < BR; ++b) out[b][m] = out[b][m] + gk[q][b] * dm;
+                    }
+            }
+            for (; k < cnt; ++k) {
+                const int32_t j = a.g.nidx[int64_t(k) * np + i];
+                T gk[D], df[M];
+#pragma unroll
+                for (int d = 0; d < D; ++d) gk[d] = a.g.gw[(int64_t(k) * D + d) * np + i];
                 load_vec<T, M>(a.U + int64_t(j) * M, df);
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
@@ -454,10 +528,7 @@ __device__ __forceinline__ void gather_one(const StageArgs<T> &a, const int64_t 
         }
     }
     if (a.sc.limiter != HCC_LIMITER_NONE && p > 1) limit_slopes<T, D, M, RDEG>(a, i, cnt, fi, out);
-#pragma unroll
-    for (int b = 0; b < BR; ++b)
-#pragma unroll
-        for (int m = 0; m < M; ++m) g[b * M + m] = out[b][m];
+    store_vec<T, BR * M>(g, &out[0][0]);
 }
 
 // A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word)
@@ -492,13 +563,11 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
 template <typename T, int D, int M, int PDE>
 __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i, const T *fi, const T *Kv,
                                                const T *mn, const T *mx) {
-#pragma unroll
-    for (int m = 0; m < M; ++m) a.K[i * M + m] = Kv[m];
+    store_vec<T, M>(a.K + i * M, Kv);
     if (!a.form_next) return false;
     // _stage_predictor! for the next candidate
     T Y[M];
-#pragma unroll
-    for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
+    load_vec<T, M>(a.Un + i * M, Y);
     const StageCoeffs<T> *cf = a.coef;
     for (int j = 0; j < a.n_prev; ++j) {
         const T hE = cf->hE[j], hI = cf->hI[j];
@@ -508,24 +577,26 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i,
 #pragma unroll
                 for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * Kv[m];
             } else {
+                T kv[M];
+                load_vec<T, M>(a.KE[j] + i * M, kv);
 #pragma unroll
-                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KE[j][i * M + m];
+                for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * kv[m];
             }
         }
         if (hI != T(0)) {
             const T h = hI;
+            T kv[M];
+            load_vec<T, M>(a.KI[j] + i * M, kv);
 #pragma unroll
-            for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * a.KI[j][i * M + m];
+            for (int m = 0; m < M; ++m) Y[m] = Y[m] + h * kv[m];
         }
     }
     if (a.implicit_mode) {
         T KIo[M];
         implicit_part<T, D, M, PDE>(a, Y, KIo);
-#pragma unroll
-        for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
+        store_vec<T, M>(a.KInext + i * M, KIo);
     }
-#pragma unroll
-    for (int m = 0; m < M; ++m) a.Ynext[i * M + m] = Y[m];
+    store_vec<T, M>(a.Ynext + i * M, Y);
     if (!a.check) return false;
     T cand[M];
     if (a.check_substep) {
@@ -617,7 +688,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     const bool wok = cnt > 0 && (cached || (a.g.dw1 != nullptr && didx == 2 && a.g.ok_1[i]));
     const bool need_ext = a.check && a.sc.criterion == HCC_MOOD_U1;
     const int nbmin_i = (a.sc.strategy == HCC_EPD2) ? a.nbmin[i] : 0;
-    Accum<T> acc[M];
+    AccumV<T, M> acc;
     T mn[M], mx[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) { mn[m] = fi[m]; mx[m] = fi[m]; }
@@ -657,23 +728,46 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
             if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
             else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
             else { oi = oi_own; oj = oj_own; }
-            const int keep_i = interface_terms<D, RDEG>(oi);
-            const int keep_j = interface_terms<D, RDEG>(oj);
-            T hx[D], pi[BR], pj[BR];
+            T pi[BR], pj[BR];
+            if constexpr (kFast && RDEG == 1) {
+                // degree 1: an interface of order 2 keeps the linear terms, order 1 none (the midpoint offsets
+                // ±dk/2 scaled by 0 or ±1/2)
+                const T si = oi >= 2 ? T(0.5) : T(0), sj = oj >= 2 ? T(-0.5) : T(0);
 #pragma unroll
-            for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
-            recon_basis<D, RDEG, T>(hx, pi);
+                for (int d = 0; d < D; ++d) { pi[d] = si * dk[d]; pj[d] = sj * dk[d]; }
+            } else {
+                const int keep_i = interface_terms<D, RDEG>(oi);
+                const int keep_j = interface_terms<D, RDEG>(oj);
+                T hx[D];
 #pragma unroll
-            for (int d = 0; d < D; ++d) hx[d] = T(-0.5) * dk[d];
-            recon_basis<D, RDEG, T>(hx, pj);
+                for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
+                recon_basis<D, RDEG, T>(hx, pi);
 #pragma unroll
-            for (int b = 0; b < BR; ++b) {
-                if (b >= keep_i) pi[b] = T(0);
-                if (b >= keep_j) pj[b] = T(0);
+                for (int d = 0; d < D; ++d) hx[d] = T(-0.5) * dk[d];
+                recon_basis<D, RDEG, T>(hx, pj);
+#pragma unroll
+                for (int b = 0; b < BR; ++b) {
+                    if (b >= keep_i) pi[b] = T(0);
+                    if (b >= keep_j) pj[b] = T(0);
+                }
             }
             T fij[M], fji[M];
+            if constexpr (kFast) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
+                for (int q = 0; q < M / 2; ++q) {
+                    float2 si = p_mul(p_ld(gi[0], q), p_bc(pi[0]));
+                    float2 sj = p_mul(p_ld(gj, q), p_bc(pj[0]));
+#pragma unroll
+                    for (int b = 1; b < BR; ++b) {
+                        si = p_fma(p_ld(gi[b], q), p_bc(pi[b]), si);
+                        sj = p_fma(p_ld(gj + b * M, q), p_bc(pj[b]), sj);
+                    }
+                    p_st(fij, q, p_add(p_ld(fi, q), si));
+                    p_st(fji, q, p_add(p_ld(fj, q), sj));
+                }
+            }
+#pragma unroll
+            for (int m = kFast ? (M / 2) * 2 : 0; m < M; ++m) {
                 T si = gi[0][m] * pi[0];
                 T sj = gj[m] * pj[0];
 #pragma unroll
@@ -691,16 +785,24 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
             if constexpr (kFast) {
                 // FP32: 2 (F_n - F_i) = (F_ij + F_ji) - s_d max(λ) (f_ji - f_ij) - 2 F_i with s_d = sign of the
                 // axis component (the sort_flux orientation folded into the speed); the factor 2 leaves K = -Σ.
+                // (pairs of components with the packed instructions, a scalar tail for odd M)
                 T jump[M];
 #pragma unroll
-                for (int m = 0; m < M; ++m) jump[m] = fji[m] - fij[m];
+                for (int q = 0; q < M / 2; ++q) p_st(jump, q, p_sub(p_ld(fji, q), p_ld(fij, q)));
+                if constexpr (M & 1) jump[M - 1] = fji[M - 1] - fij[M - 1];
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
                     const T ssd = dk[d] > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
+                    const float2 nssd = p_bc(-ssd), w2 = p_bc(wk[d]);
 #pragma unroll
-                    for (int m = 0; m < M; ++m) {
-                        const T dF2 = ((Fij[d][m] + Fji[d][m]) - ssd * jump[m]) - Fi[d][m];
-                        t[m] = (d == 0) ? wk[0] * dF2 : t[m] + wk[d] * dF2;
+                    for (int q = 0; q < M / 2; ++q) {
+                        const float2 Fs = p_add(p_ld(Fij[d], q), p_ld(Fji[d], q));
+                        const float2 dF2 = p_sub(p_fma(nssd, p_ld(jump, q), Fs), p_ld(Fi[d], q));
+                        p_st(t, q, (d == 0) ? p_mul(w2, dF2) : p_fma(w2, dF2, p_ld(t, q)));
+                    }
+                    if constexpr (M & 1) {
+                        const T dF2 = ((Fij[d][M - 1] + Fji[d][M - 1]) - ssd * jump[M - 1]) - Fi[d][M - 1];
+                        t[M - 1] = (d == 0) ? wk[0] * dF2 : t[M - 1] + wk[d] * dF2;
                     }
                 }
             } else {
@@ -720,8 +822,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
                     }
                 }
             }
-#pragma unroll
-            for (int m = 0; m < M; ++m) acc[m].add(t[m]);
+            acc.add(t);
         }
     } else if (need_ext) {
         for (int k = 0; k < cnt; ++k) {
@@ -736,7 +837,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     }
     T Kv[M];
 #pragma unroll
-    for (int m = 0; m < M; ++m) Kv[m] = kFast ? -acc[m].value() : -(T(2) * acc[m].value());
+    for (int m = 0; m < M; ++m) Kv[m] = kFast ? -acc.s[m] : -(T(2) * acc.s[m]);
     return stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
 }
 
