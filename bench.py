@@ -32,6 +32,7 @@ ROOT = Path(__file__).resolve().parent
 PKG = ROOT / "hypercloudcore.jl_gb300"
 METRIC = "point-updates/s per RK stage, FP32+learned vs plain FP64 on 1 GB300 at equal L1"
 STAGES = 3
+HOST_DRIVEN = False     # --host-driven: steps without the step graph (e.g. for kernel profilers)
 
 
 def _load(name, path, pkg_dir=None):
@@ -54,6 +55,8 @@ WORKLOADS = {
     # name: (dim, h, description)
     "euler2d_quadrant_1M": (2, 1e-3, "2-D Euler quadrant Riemann, h=1e-3 (1.0M interior), MUSCL2+MOOD, SSP-RK3"),
     "euler2d_quadrant_250k": (2, 2e-3, "2-D Euler quadrant Riemann, h=2e-3 (250k interior), MUSCL2+MOOD, SSP-RK3"),
+    "euler3d_blast_8M": (3, 1 / 200, "3-D Euler spherical blast, h=1/200 (8.0M interior), MUSCL2+MOOD, SSP-RK3"),
+    "euler3d_blast_1M": (3, 1 / 100, "3-D Euler spherical blast, h=1/100 (1.0M interior), MUSCL2+MOOD, SSP-RK3"),
 }
 
 
@@ -69,17 +72,30 @@ def quadrant_state(cloud, gamma=1.4):
     return np.ascontiguousarray(np.stack([rho, rho * u, rho * v, E], axis=1))
 
 
+def blast_state(cloud, gamma=1.4):
+    """Spherical blast: rho = 1, p = 1 for r < 0.2 about the centre, else rho = 0.125, p = 0.1; zero velocity."""
+    r2 = ((cloud.pos - 0.5) ** 2).sum(axis=1)
+    inside = r2 < 0.04
+    rho = np.where(inside, 1.0, 0.125)
+    p = np.where(inside, 1.0, 0.1)
+    D = cloud.pos.shape[1]
+    return np.ascontiguousarray(np.column_stack([rho] + [np.zeros_like(rho)] * D + [p / (gamma - 1)]))
+
+
 def make_workload(hcc, name):
     D, h, _ = WORKLOADS[name]
     cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, jitter=0.25 * h, seed=42)
-    U0 = quadrant_state(cloud)
+    U0 = quadrant_state(cloud) if D == 2 else blast_state(cloud)
     return cloud, U0, h
 
 
 def make_cfg(hcc, cloud, h, precision):
-    return hcc.make_config(hcc.Euler(2, 1.4), cloud, scheme=hcc.MUSCL(2, 2),
-                           mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), tableau="RK3_SSP",
-                           bc_map={t: hcc.BC_OUTFLOW for t in (1, 2, 3, 4)}, precision=precision)
+    """MUSCL order 2 with the divergence fit of order 2, MOOD (EPD1, MOODu1(1e-4 h^D)), Rusanov, SSP-RK3,
+    transmissive boundaries on every wall."""
+    D = cloud.pos.shape[1]
+    return hcc.make_config(hcc.Euler(D, 1.4), cloud, scheme=hcc.MUSCL(2, 2),
+                           mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D)), tableau="RK3_SSP",
+                           bc_map={t: hcc.BC_OUTFLOW for t in range(1, 2 * D + 1)}, precision=precision)
 
 
 # --------------------------------------------------------------------------------------------- helpers
@@ -238,6 +254,75 @@ def time_e2e(hcc, ctx, U_host, dt, steps, world, f32):
     return reduce_max(el, world), host.nbytes, out.nbytes
 
 
+def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_dt=None, acc_steps=0):
+    """One precision on one workload: K device-timed steps (the step graph, no profiling), the same K steps again
+    with per-kernel CUDA events (host-driven step) for the roofline, the end-to-end C-ABI leg, and — when asked —
+    `acc_steps` steps from the initial state with a fixed dt whose final density is returned for the L1 check."""
+    f32 = prec == "fp32"
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+    if HOST_DRIVEN:
+        ctx.set_step_graphs(False)
+    ctx.upload_cloud(cloud)
+    ctx.build_neighbours()
+    ctx.prepare_geometry()
+    U_in = U0.astype(np.float32) if f32 else U0
+    ctx.upload_state(U_in)
+    dt = 0.4 * ctx.time_step()
+    for _ in range(warmup):
+        ctx.step(0.0, dt)
+    ctx.upload_state(U_in)
+    with ClockSampler(local) as clk:
+        ms, launches = time_device_steps(hcc, ctx, dt, steps, world)
+    cnt = ctx.counters()
+    ctx.upload_state(U_in)
+    ctx.set_profiling(True)
+    ctx.kernel_times(reset=True)
+    for _ in range(steps):
+        ctx.step(0.0, dt)
+    ctx.synchronize()
+    ctx.set_profiling(False)
+    kt = ctx.kernel_times(reset=True)
+    out = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt, "dt": dt}
+    if e2e:
+        out["e2e_s"], out["h2d"], out["d2h"] = time_e2e(hcc, ctx, U0, dt, steps, world, f32)
+    if acc_steps:
+        ctx.upload_state(U_in)
+        for _ in range(acc_steps):
+            ctx.step(0.0, acc_dt)
+        out["rho"] = ctx.download_state(dtype=np.float64)[:, 0].copy()
+    ctx.close()
+    return out
+
+
+def rel_l1(a, b, sel):
+    return float(np.abs(a[sel] - b[sel]).sum() / np.abs(b[sel]).sum())
+
+
+def run_3d(hcc, args, world, local):
+    """The 3-D Euler blast at 8.0M interior particles (K ~ 67): FP32 bulk and FP64 plain step rates and the FP32
+    density's relative L1 distance from the FP64 run after the same steps."""
+    name = "euler3d_blast_8M"
+    cloud, U0, h = make_workload(hcc, name)
+    n_int = cloud.n_interior
+    steps32, steps64, acc = max(3, min(args.steps, 10)), 2, 5
+    r32 = measure(hcc, cloud, U0, h, "fp32", steps32, 2, world, local, e2e=False)
+    dt = r32["dt"]
+    r32a = measure(hcc, cloud, U0, h, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt, acc_steps=acc)
+    r64 = measure(hcc, cloud, U0, h, "fp64", steps64, 1, world, local, e2e=False, acc_dt=dt, acc_steps=acc)
+    inner = cloud.is_boundary == 0
+    K = r32["counters"]["total_neighbours"] / max(cloud.n, 1)
+    kt = r32["kt"]
+    return {"workload": name, "description": WORKLOADS[name][2], "n_particles": cloud.n, "n_interior": n_int,
+            "mean_neighbours": K,
+            "fp32": {"value": n_int * STAGES * steps32 * world / (r32["ms"] / 1e3), "ms_per_step": r32["ms"] / steps32,
+                     "flux_ms_per_launch": kt["flux_ms"] / max(kt["flux_launches"], 1),
+                     "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
+                     "mood_iterations_last_step": r32["counters"]["mood_iterations"], "clocks": r32["clocks"]},
+            "fp64_plain": {"value": n_int * STAGES * steps64 * world / (r64["ms"] / 1e3),
+                           "ms_per_step": r64["ms"] / steps64, "clocks": r64["clocks"]},
+            "l1_density_fp32_vs_fp64": {"value": rel_l1(r32a["rho"], r64["rho"], inner), "steps": acc, "dt": dt}}
+
+
 def run_gpu(args):
     world, rank, local = dist_setup()
     hcc = package()
@@ -246,41 +331,29 @@ def run_gpu(args):
     import torch
     torch.cuda.set_device(local)
     cloud, U0, h = make_workload(hcc, args.workload)
+    D = cloud.pos.shape[1]
     n_int = cloud.n_interior
     results = {}
+    acc_steps, acc_dt = 10, None
     for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
-        f32 = prec == "fp32"
-        ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
-        ctx.upload_cloud(cloud)
-        ctx.build_neighbours()
-        ctx.prepare_geometry()
-        ctx.upload_state(U0.astype(np.float32) if f32 else U0)
-        dt = 0.4 * ctx.time_step()
-        for _ in range(args.warmup):
-            ctx.step(0.0, dt)
-        ctx.upload_state(U0.astype(np.float32) if f32 else U0)
-        ctx.set_profiling(True)
-        ctx.kernel_times(reset=True)
-        with ClockSampler(local) as clk:
-            ms, launches = time_device_steps(hcc, ctx, dt, args.steps, world)
-        ctx.set_profiling(False)
-        kt = ctx.kernel_times(reset=True)
-        cnt = ctx.counters()
-        e2e_s, h2d, d2h = time_e2e(hcc, ctx, U0, dt, args.steps, world, f32)
-        results[prec] = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt,
-                         "e2e_s": e2e_s, "h2d": h2d, "d2h": d2h, "dt": dt}
-        ctx.close()
+        results[prec] = measure(hcc, cloud, U0, h, prec, args.steps, args.warmup, world, local,
+                                acc_dt=acc_dt, acc_steps=acc_steps if acc_dt else 0)
+        if acc_dt is None:
+            acc_dt = results[prec]["dt"]
+            r = measure(hcc, cloud, U0, h, prec, 1, 0, world, local, e2e=False, acc_dt=acc_dt, acc_steps=acc_steps)
+            results[prec]["rho"] = r["rho"]
     r = results["fp32"]
     units = n_int * STAGES * args.steps * world
     value = units / (r["ms"] / 1e3)
     cnt = r["counters"]
     K = cnt["total_neighbours"] / max(cloud.n, 1)
-    flux_b, gather_b = algorithmic_bytes(K, 2, 4, 2, 3, 4)
+    M = D + 2
+    flux_b, gather_b = algorithmic_bytes(K, D, M, D, D + 1, 4)
     peak, peak_kind = measured_peaks()
     kt = r["kt"]
     flux_ms = kt["flux_ms"] / max(kt["flux_launches"], 1)
     achieved = flux_b * n_int / (flux_ms / 1e3) / 1e9
-    traffic = recorded_traffic().get("flux_f32_euler2d_bytes_per_point_stage")
+    traffic = recorded_traffic().get("flux_f32_euler2d_bytes_per_point_stage") if D == 2 else None
     line = {
         "metric": METRIC, "value": value, "unit": "point-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
@@ -288,18 +361,20 @@ def run_gpu(args):
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
                    "n_particles": cloud.n, "n_interior": n_int, "mean_neighbours": K, "stages_per_step": STAGES,
                    "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": False,
+                   "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
                    "l2": "inputs larger than L2 (per-slot arrays ~0.5 GB)", "parallelism": f"replicas x{world}",
                    "dt": r["dt"]},
         "gpu_launches": r["launches"],
         "e2e": {"value": units / r["e2e_s"], "unit": "point-updates/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
-        "roofline": {"bound": "hbm", "kernel": "k_flux<float,2,4,EULER,1>", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": f"k_flux<float,{D},{M},EULER,1>", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": (traffic * n_int) if traffic else None,
                      "algorithmic_bytes_per_point_stage": {"flux": flux_b, "gather": gather_b},
                      "flux_ms_per_launch": flux_ms,
                      "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
-                     "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"]},
+                     "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
+                     "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps"},
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"]},
     }
@@ -310,8 +385,13 @@ def run_gpu(args):
                               "gather_ms_per_launch": r64["kt"]["gather_ms"] / max(r64["kt"]["gather_launches"], 1),
                               "e2e": units / r64["e2e_s"], "clocks": r64["clocks"]}
         line["fp32_over_fp64"] = line["value"] / line["fp64_plain"]["value"]
+        inner = cloud.is_boundary == 0
+        line["l1_density_fp32_vs_fp64"] = {"value": rel_l1(r["rho"], r64["rho"], inner), "steps": acc_steps,
+                                           "dt": acc_dt, "note": "relative L1 over interior particles, same dt"}
     if not args.no_published:
         line["published_case"] = run_published_case(hcc, args.steps)
+    if not args.no_3d and D == 2:
+        line["euler3d_blast_8M"] = run_3d(hcc, args, world, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(hcc, cloud, U0, h, args.cpu_steps)
     if rank == 0:
@@ -420,9 +500,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp32-only", action="store_true")
     ap.add_argument("--no-published", action="store_true")
+    ap.add_argument("--no-3d", action="store_true")
+    ap.add_argument("--host-driven", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global HOST_DRIVEN
+    HOST_DRIVEN = args.host_driven
     if args.impl == "reference":
         run_reference(args)
     else:
