@@ -5,7 +5,7 @@ Host mirror of the reference's interface for this path (names and argument meani
   * physics modules   ``LinearAdvection`` (test/PDEs/linear_advection.jl), ``Euler`` (new), ``KineticRelaxation``
                       (test/kinetic_source.jl) — the ``HyperbolicPDE`` subtypes compiled into the kernels;
   * schemes           ``MUSCL(order, div_order)`` (src/Interpolation/MUSCL.jl:116), ``MOOD(strategy, criterion)``
-                      with ``MOODu1`` / ``MOODPAD`` / ``OnlyMOOD`` / ``NoMOOD`` and ``EPD0/EPD1/EPD2``
+                      with ``MOODu1`` / ``MOODu2`` / ``MOODPAD`` / ``OnlyMOOD`` / ``NoMOOD`` and ``EPD0/EPD1/EPD2``
                       (src/TimeStepping/MOOD.jl);
   * stepper           ``GB300RKTimeStepper`` — ``ts(t, dt)`` is ``(ts::GeneralRKTimeStepper)(eq, pg, t, dt)``
                       (src/TimeStepping/TimeSteppers.jl:531) and ``ts.get_time_step()`` is
@@ -129,6 +129,15 @@ class MOODu1:
     delta: float
 
 
+@dataclass
+class MOODu2:
+    """MOODu2(d; plateau = 1e-3, ratio = 1/2) (src/TimeStepping/MOOD.jl:104-130): MOODu1 plus the plateau test and
+    the smooth-extremum override from the curvature terms of a degree-2 reconstruction."""
+    delta: float
+    plateau: float = 1e-3
+    ratio: float = 0.5
+
+
 class MOODPAD:
     pass
 
@@ -157,6 +166,7 @@ def config_defaults() -> HccConfig:
     cfg.tableau, cfg.mood_substeps, cfg.max_mood_iterations = TABLEAUS["RK3_SSP"], 1, 64
     cfg.weight_alpha, cfg.gamma = 1.0, 1.4
     cfg.bgk_epsilon, cfg.bgk_coefficient, cfg.bgk_interior_factor = 1e-4, 1.0, 2.0
+    cfg.u2_plateau, cfg.u2_ratio = 1e-3, 0.5
     for d in range(_abi.HCC_MAX_DIM):
         cfg.dx[d], cfg.canvas_max[d], cfg.domain_max[d] = 1.0, 1.0, 1.0
     return cfg
@@ -190,6 +200,9 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
     crit = mood.criterion
     if isinstance(crit, MOODu1):
         cfg.mood_criterion, cfg.mood_delta = MOOD_U1, float(crit.delta)
+    elif isinstance(crit, MOODu2):
+        cfg.mood_criterion, cfg.mood_delta = _abi.MOOD_U2, float(crit.delta)
+        cfg.u2_plateau, cfg.u2_ratio = float(crit.plateau), float(crit.ratio)
     elif isinstance(crit, MOODPAD):
         cfg.mood_criterion = MOOD_PAD
     elif isinstance(crit, OnlyMOOD):
@@ -405,7 +418,7 @@ class GB300RKTimeStepper:
 
 
 __all__ = [
-    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "WENO", "MOOD", "MOODu1",
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "WENO", "MOOD", "MOODu1", "MOODu2",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",

@@ -19,7 +19,7 @@ PDE_ADVECTION, PDE_EULER, PDE_BGK = 0, 1, 2
 # hcc_precision
 FP64, FP32 = 0, 1
 # hcc_mood_criterion
-MOOD_NONE, MOOD_U1, MOOD_PAD, MOOD_ONLY = 0, 1, 2, 3
+MOOD_NONE, MOOD_U1, MOOD_PAD, MOOD_ONLY, MOOD_U2 = 0, 1, 2, 3, 4
 # hcc_mood_strategy
 EPD_NONE, EPD0, EPD1, EPD2 = 0, 1, 2, 3
 # hcc_tableau
@@ -47,7 +47,8 @@ class HccConfig(C.Structure):
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),
         ("mood_delta", C.c_double), ("velocity", (C.c_double * HCC_MAX_VARS) * HCC_MAX_DIM),
         ("gamma", C.c_double), ("bgk_epsilon", C.c_double), ("bgk_macro_velocity", C.c_double * HCC_MAX_DIM),
-        ("bgk_coefficient", C.c_double), ("bgk_interior_factor", C.c_double), ("reserved_d", C.c_double * 8),
+        ("bgk_coefficient", C.c_double), ("bgk_interior_factor", C.c_double), ("u2_plateau", C.c_double),
+        ("u2_ratio", C.c_double), ("reserved_d", C.c_double * 6),
     ]
 
 

@@ -203,6 +203,8 @@ struct hcc_ctx {
     uint32_t *tmask = nullptr, *cmask = nullptr, *dmask = nullptr, *words1 = nullptr;
     ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
     int list_blocks = 1, drop_blocks = 1;
+    unsigned long long *u2_keys = nullptr;       // MOODu2 global range of the stage state (ordered keys)
+    bool u2_plateau_on() const { return cfg.mood_criterion == HCC_MOOD_U2 && cfg.u2_plateau > 0.0; }
     unsigned long long *d_counters = nullptr;   // [0..1] drop counters, [2] dt bits, [3..4] search stats
     unsigned long long *h_counters = nullptr;   // pinned mirror
     double *d_mass = nullptr;
@@ -374,6 +376,10 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.inadm = c->inadm;
     a.list_blocks = c->list_blocks;
     a.delta = T(c->cfg.mood_delta);
+    a.u2_plateau = T(c->cfg.u2_plateau);
+    a.u2_ratio = T(c->cfg.u2_ratio);
+    a.u2_h = T(c->h);
+    a.u2_range = c->u2_plateau_on() ? c->u2_keys : nullptr;
     return a;
 }
 
@@ -482,6 +488,10 @@ template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaSt
     }
     if (c->cfg.mood_strategy == HCC_EPD2) {
         launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, nullptr, nullptr, nullptr, 0, st);
+        ++k;
+    }
+    if (a.check && c->u2_plateau_on()) {
+        launch_u2_range(a.U, n, c->M, c->f32, c->u2_keys, st);
         ++k;
     }
     if (prof) c->prof_begin(1);
@@ -806,6 +816,8 @@ void hcc_config_defaults(hcc_config *cfg) {
     cfg->bgk_epsilon = 1e-4;
     cfg->bgk_coefficient = 1.0;
     cfg->bgk_interior_factor = 2.0;
+    cfg->u2_plateau = 1e-3;
+    cfg->u2_ratio = 0.5;
     for (int d = 0; d < HCC_MAX_DIM; ++d) { cfg->dx[d] = 1.0; cfg->canvas_max[d] = 1.0; cfg->domain_max[d] = 1.0; }
 }
 
@@ -836,7 +848,7 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if (!(f.radius > 0.0)) return c->fail(HCC_ERR_INVALID, "radius must be positive");
     if (f.muscl_order < 1 || f.muscl_order > 3) return c->fail(HCC_ERR_UNSUPPORTED, "muscl_order must be 1, 2 or 3");
     if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_EPD2) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
-    if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_ONLY) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
+    if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_U2) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
     if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
     if (f.limiter < HCC_LIMITER_NONE || f.limiter > HCC_LIMITER_VK_HARD) return c->fail(HCC_ERR_INVALID, "unknown limiter");
     if (f.scheme != HCC_SCHEME_MUSCL && f.scheme != HCC_SCHEME_WENO) return c->fail(HCC_ERR_INVALID, "unknown scheme");
@@ -889,6 +901,7 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if ((st = c->cuda(cudaMallocHost(&c->coef_host, coef_bytes), "pinned stage coefficients")) != HCC_OK) return st;
     if ((st = c->alloc(c->mood_stats, 1, "MOOD statistics")) != HCC_OK) return st;
     if ((st = c->alloc(c->lcounts, 1, "MOOD worklist counts")) != HCC_OK) return st;
+    if ((st = c->alloc(c->u2_keys, 2 * HCC_MAX_VARS + 1, "MOODu2 range")) != HCC_OK) return st;
     cudaMemsetAsync(c->lcounts, 0, sizeof(ListCounts), c->stream);
     if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->h_lcounts), sizeof(ListCounts)),
                       "pinned MOOD worklist counts")) != HCC_OK) return st;
@@ -919,6 +932,7 @@ hcc_status hcc_destroy(hcc_ctx *ctx) {
     if (ctx->coef_host) cudaFreeHost(ctx->coef_host);
     dfree(ctx->mood_stats);
     dfree(ctx->lcounts);
+    dfree(ctx->u2_keys);
     if (ctx->h_lcounts) cudaFreeHost(ctx->h_lcounts);
     if (ctx->mood_stats_host) cudaFreeHost(ctx->mood_stats_host);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);

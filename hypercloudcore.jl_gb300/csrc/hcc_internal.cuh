@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 #include "../../include/hcc.h"
@@ -226,6 +227,9 @@ template <typename T> struct StageArgs {
     int check_substep;                // 1: W = Y_s + h_sub (K + KI_s), 0: the candidate itself
     const T *KIs;                     // K_I[s] for the substep of implicit-source tableaus
     T delta;
+    T u2_plateau, u2_ratio, u2_h;     // MOODu2: plateau and curvature-ratio parameters, h = min(dx)
+    const unsigned long long *u2_range;   // MOODu2 global range of the stage state (ordered keys: lo[M], hi[M],
+                                          // NaN bits), nullptr when the plateau test is off
     uint32_t *tmask;                  // MOOD check: failed candidates (a ballot word per tile) ...
     int32_t *ttiles;                  // ... the tiles with a failure ...
     unsigned *tcount;                 // ... and their count
@@ -343,6 +347,21 @@ void launch_reach_hop2(ListCounts *counts, const int32_t *dtiles, int32_t *dtile
 void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const int32_t *nidx, int64_t n,
                   int64_t npad, const int32_t *tiles, const uint32_t *words, const unsigned *count, int blocks,
                   cudaStream_t s);
+// MOODu2 global range of a state (_global_range, MOOD.jl:215-221): keys[0, M) = ordered keys of the minima,
+// keys[M, 2M) of the maxima, keys[2M] = bit m set if component m holds a NaN. Clears the keys first.
+void launch_u2_range(const void *U, int64_t n, int M, int is_f32, unsigned long long *keys, cudaStream_t s);
+// Ordered 64-bit key of a double (monotone in the value, -0 below +0) and back.
+__host__ __device__ __forceinline__ unsigned long long order_key(double v) {
+    unsigned long long b;
+    memcpy(&b, &v, sizeof(b));
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double order_value(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    double v;
+    memcpy(&v, &b, sizeof(v));
+    return v;
+}
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s);
 // Gradient weights of the cached degree-1 fit (FP64 sums, FP32 store): gw[(k*D + b) * npad + i] =

@@ -15,7 +15,10 @@
 #define HCC_FLUX_BLOCK 128
 #endif
 #ifndef HCC_FLUX_MINB
-#define HCC_FLUX_MINB 6            // FP32: caps the flux kernel at 80 registers
+#define HCC_FLUX_MINB 7            // FP32, D*M < 12: caps the flux kernel at 72 registers
+#endif
+#ifndef HCC_FLUX_MINB_WIDE
+#define HCC_FLUX_MINB_WIDE 4       // FP32, D*M >= 12 (3-D Euler): 128 registers
 #endif
 #ifndef HCC_FLUX_MINB64
 #define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
@@ -560,7 +563,54 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
 // Epilogue of a flux pass for particle i: K_E[s] stored, the next candidate formed (_stage_predictor!,
 // TimeSteppers.jl:400-421, and the implicit part), the Euler substep (:511-518) and the MOOD check of the next
 // checkpoint (_mood_flag!, MOOD.jl:289-295) against the extrema mn/mx of {i} ∪ N(i) of the stage state.
-template <typename T, int D, int M, int PDE>
+// MOODu2 override (_u2_fails, MOOD.jl:241-271), for the DMP-violating components of a particle of order >= 3: per
+// axis the curvature terms (reconstruction terms D + d) over {i} ∪ N(i) keep one sign, and over the neighbours within
+// 1.5h comparable magnitudes, or are negligible; otherwise the candidate is flagged. A rare path (DMP violators only).
+template <typename T, int D, int M, int RDEG>
+__device__ __noinline__ bool u2_curvature_fails(const StageArgs<T> &a, int64_t i, const bool *viol) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    const T h = a.u2_h, h2 = h * h, r15 = T(1.5) * h, near_sq = r15 * r15, dl = a.delta;
+    for (int d = 0; d < D; ++d) {
+        const int b = D + d;
+        T mini[M], maxi[M], minA[M], maxA[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const T ci = a.grad[(i * BR + b) * M + m];
+            mini[m] = maxi[m] = ci;
+            minA[m] = maxA[m] = fabs(ci);
+        }
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t j = a.g.nidx[int64_t(k) * np + i];
+            T r2 = T(0);
+#pragma unroll
+            for (int e = 0; e < D; ++e) {
+                const T x = a.g.dist[(int64_t(k) * D + e) * np + i];
+                r2 = (e == 0) ? x * x : r2 + x * x;
+            }
+            const bool near = r2 <= near_sq;
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const T cj = a.grad[(j * BR + b) * M + m];
+                mini[m] = vmin(mini[m], cj);
+                maxi[m] = vmax(maxi[m], cj);
+                if (near) { minA[m] = vmin(minA[m], fabs(cj)); maxA[m] = vmax(maxA[m], fabs(cj)); }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            if (!viol[m]) continue;
+            if (vmax(fabs(mini[m]), fabs(maxi[m])) * h2 < dl) continue;    // negligible curvature
+            const bool same_sign = (mini[m] * h2) * (maxi[m] * h2) > -(dl * dl);
+            const bool comparable = a.u2_ratio <= T(0) || minA[m] >= a.u2_ratio * maxA[m];
+            if (!(same_sign && comparable)) return true;
+        }
+    }
+    return false;
+}
+
+template <typename T, int D, int M, int PDE, int RDEG = 0>
 __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i, const T *fi, const T *Kv,
                                                const T *mn, const T *mx) {
     store_vec<T, M>(a.K + i * M, Kv);
@@ -631,6 +681,32 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i,
             }
         }
     }
+    else if (a.sc.criterion == HCC_MOOD_U2 && !flag) {
+        // DMP violators that are not a plateau (the u1 test, plus max - min < plateau x global range)
+        const T dl = a.delta, d3 = dl * dl * dl;
+        bool viol[M], any = false;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            T pad = dl;
+            if constexpr (sizeof(T) == 4) pad = dl + T(16) * T(1.1920928955078125e-7) * vmax(fabs(mn[m]), fabs(mx[m]));
+            bool v = fabs(mx[m] - mn[m]) >= d3 && (cand[m] < mn[m] - pad || cand[m] > mx[m] + pad);
+            if (v && a.u2_range) {
+                const unsigned long long nanbits = a.u2_range[2 * M];
+                const T range = ((nanbits >> m) & 1ull) ? T(NAN)
+                                                        : T(order_value(a.u2_range[M + m])) - T(order_value(a.u2_range[m]));
+                v = !(mx[m] - mn[m] < a.u2_plateau * range);
+            }
+            viol[m] = v;
+            any = any || v;
+        }
+        if (any) {
+            if constexpr (RDEG >= 2) {
+                flag = (a.sc.max_order < 3 || a.orders[i] < 3) ? true : u2_curvature_fails<T, D, M, RDEG>(a, i, viol);
+            } else {
+                flag = true;
+            }
+        }
+    }
     a.inadm[i] = !adm;
     return flag;
 }
@@ -645,10 +721,10 @@ __device__ __forceinline__ int interface_terms(int o) {
 }
 
 // Resident blocks per SM the flux kernel is compiled for: as many as its registers allow without spilling
-// (FP32 2-D scalar/Euler: 80 registers; wider states and FP64 need more).
+// (FP32 2-D scalar/Euler: 72 registers; wider states and FP64 need more).
 template <typename T, int D, int M> constexpr int flux_min_blocks() {
     if (sizeof(T) == 8) return M >= 8 ? 1 : (D * M >= 12 ? 2 : HCC_FLUX_MINB64);
-    return M >= 8 ? 2 : (D * M >= 12 ? 4 : HCC_FLUX_MINB);
+    return M >= 8 ? 2 : (D * M >= 12 ? HCC_FLUX_MINB_WIDE : HCC_FLUX_MINB);
 }
 
 // The MUSCL functor (MUSCL.jl:390-508) in its streamed form: per slot, EPD interface reconstruction, physical
@@ -686,7 +762,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     const bool cached = a.g.ok_d[i] && didx == divergence_index(a.sc.DO, D, a.sc.max_order, cnt);
     const T *wsl = cached ? a.g.dw : a.g.dw1;
     const bool wok = cnt > 0 && (cached || (a.g.dw1 != nullptr && didx == 2 && a.g.ok_1[i]));
-    const bool need_ext = a.check && a.sc.criterion == HCC_MOOD_U1;
+    const bool need_ext = a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2);
     const int nbmin_i = (a.sc.strategy == HCC_EPD2) ? a.nbmin[i] : 0;
     AccumV<T, M> acc;
     T mn[M], mx[M];
@@ -838,7 +914,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     T Kv[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) Kv[m] = kFast ? -acc.s[m] : -(T(2) * acc.s[m]);
-    return stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
+    return stage_epilogue<T, D, M, PDE, RDEG>(a, i, fi, Kv, mn, mx);
 }
 
 // Failed candidates of one tile (a warp's ballot) into the t list.
@@ -980,7 +1056,7 @@ __device__ __forceinline__ bool weno_one(const StageArgs<T> &a, const int64_t i)
     const int64_t np = a.g.npad;
     const T fiT = a.U[i];
     T mn = fiT, mx = fiT;
-    if (a.check && a.sc.criterion == HCC_MOOD_U1)
+    if (a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2))
         for (int k = 0; k < cnt; ++k) {
             const T fj = a.U[a.g.nidx[int64_t(k) * np + i]];
             mn = vmin(mn, fj);

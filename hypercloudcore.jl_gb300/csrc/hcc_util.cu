@@ -157,6 +157,34 @@ __global__ void k_nbmin_tiles(const int8_t *orders, int8_t *nbmin, const int32_t
         if ((words[q] >> lane) & 1u) nbmin_one(orders, nbmin, cnt, nidx, npad, int64_t(tiles[q]) * 32 + lane);
 }
 
+// MOODu2 global range: per component, the minimum and maximum ordered keys over every particle (boundary ones
+// included, as view(U, 1:N)), NaNs recorded separately (Julia's min/max propagate them).
+template <typename T>
+__global__ void k_u2_range(const T *U, int64_t n, int M, unsigned long long *keys) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (int m = 0; m < M; ++m) {
+        unsigned long long lo = ~0ull, hi = 0ull;
+        unsigned nan = 0;
+        if (i < n) {
+            const double v = double(U[i * M + m]);
+            if (v != v) nan = 1;
+            else lo = hi = order_key(v);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long l2 = __shfl_down_sync(0xffffffffu, lo, o), h2 = __shfl_down_sync(0xffffffffu, hi, o);
+            lo = l2 < lo ? l2 : lo;
+            hi = h2 > hi ? h2 : hi;
+        }
+        const unsigned anynan = __any_sync(0xffffffffu, nan);
+        if ((threadIdx.x & 31) == 0) {
+            if (lo != ~0ull) atomicMin(&keys[m], lo);
+            if (hi != 0ull) atomicMax(&keys[M + m], hi);
+            if (anynan) atomicOr(&keys[2 * M], 1ull << m);
+        }
+    }
+}
+
 // Interior candidates that are not admissible once a fixed point has converged (_count_inadmissible,
 // TimeSteppers.jl:481-490).
 __global__ void k_count_inadm(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out) {
@@ -255,6 +283,13 @@ void launch_nbmin(const int8_t *orders, int8_t *nbmin, const int32_t *cnt, const
         k_nbmin_tiles<<<blocks, HCC_BLOCK, 0, s>>>(orders, nbmin, cnt, nidx, npad, tiles, words, count);
     else if (n > 0)
         k_nbmin<<<grid_for(n), HCC_BLOCK, 0, s>>>(orders, nbmin, cnt, nidx, n, npad);
+}
+void launch_u2_range(const void *U, int64_t n, int M, int is_f32, unsigned long long *keys, cudaStream_t s) {
+    cudaMemsetAsync(keys, 0xff, size_t(M) * sizeof(unsigned long long), s);
+    cudaMemsetAsync(keys + M, 0, size_t(M + 1) * sizeof(unsigned long long), s);
+    if (n <= 0) return;
+    if (is_f32) k_u2_range<float><<<grid_for(n), HCC_BLOCK, 0, s>>>(static_cast<const float *>(U), n, M, keys);
+    else k_u2_range<double><<<grid_for(n), HCC_BLOCK, 0, s>>>(static_cast<const double *>(U), n, M, keys);
 }
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s) {

@@ -39,7 +39,9 @@ mutable struct HccConfig
     domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
     mood_delta::Float64; velocity::NTuple{48, Float64}; gamma::Float64; bgk_epsilon::Float64
     bgk_macro_velocity::NTuple{3, Float64}; bgk_coefficient::Float64; bgk_interior_factor::Float64
-    reserved_d::NTuple{8, Float64}
+    u2_plateau::Float64
+    u2_ratio::Float64
+    reserved_d::NTuple{6, Float64}
     HccConfig() = (c = new(); ccall((:hcc_config_defaults, libhcc), Cvoid, (Ref{HccConfig},), c); c)
 end
 
@@ -64,6 +66,7 @@ _limiter_id(::BarthJespersenLimiter{:hard}) = Int32(2)
 _limiter_id(::VenkatakrishnanLimiter{:soft}) = Int32(3)
 _limiter_id(::VenkatakrishnanLimiter{:hard}) = Int32(4)
 _criterion(c::MOODu1) = (Int32(1), Float64(c.d))
+_criterion(c::MOODu2) = (Int32(4), Float64(c.d))
 _criterion(::MOODPAD) = (Int32(2), 0.0)
 _criterion(::OnlyMOOD) = (Int32(3), 0.0)
 _criterion(::NoMOOD) = (Int32(0), 0.0)
@@ -78,6 +81,9 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     cfg.tableau = tableau_id
     cfg.mood_strategy = _strategy_id(mood.strategy)
     cfg.mood_criterion, cfg.mood_delta = _criterion(mood.criterion)
+    if mood.criterion isa MOODu2
+        cfg.u2_plateau, cfg.u2_ratio = Float64(mood.criterion.plateau), Float64(mood.criterion.ratio)
+    end
     pad3(v, z) = ntuple(d -> d <= length(v) ? Float64(v[d]) : z, 3)
     cfg.dx = pad3(pg.meta.dx, 1.0); cfg.radius = pg.meta.R
     cfg.weight_alpha = pg.neighbor.weight_func.alpha

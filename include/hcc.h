@@ -61,7 +61,9 @@ typedef enum {               /* MOOD criterion (src/TimeStepping/MOOD.jl) */
     HCC_MOOD_NONE = 0,       /* NoMOOD: MOOD() */
     HCC_MOOD_U1 = 1,         /* MOODu1(delta): relaxed DMP + PAD */
     HCC_MOOD_PAD = 2,        /* MOODPAD(): admissibility only */
-    HCC_MOOD_ONLY = 3        /* OnlyMOOD(): flags everything (testing) */
+    HCC_MOOD_ONLY = 3,       /* OnlyMOOD(): flags everything (testing) */
+    HCC_MOOD_U2 = 4          /* MOODu2(delta; plateau, ratio): u1 + plateau test + smooth-extremum override from the
+                                curvature terms of a degree-2 reconstruction (MOOD.jl:104-130, :223-271) */
 } hcc_mood_criterion;
 
 typedef enum {               /* MOOD strategy (interface orders), MOOD.jl:20-28, :76-87 */
@@ -131,7 +133,9 @@ typedef struct {
     double  bgk_macro_velocity[HCC_MAX_DIM]; /* BGK macro flux: scalar linear advection with this velocity */
     double  bgk_coefficient;           /* Maxwellian coefficient of the single macro moment (1/NK) */
     double  bgk_interior_factor;       /* RelaxationSourceTerm interior_factor (default D) */
-    double  reserved_d[8];
+    double  u2_plateau;                /* MOODu2 plateau (default 1e-3; 0 disables the plateau test) */
+    double  u2_ratio;                  /* MOODu2 curvature ratio (default 0.5; 0 disables the magnitude test) */
+    double  reserved_d[6];
 } hcc_config;
 
 typedef struct {

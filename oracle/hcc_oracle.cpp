@@ -1335,12 +1335,79 @@ struct Solver {
                 if (std::fabs(mx[m] - mn[m]) >= d3 && (nr[m] < mn[m] - dlt || nr[m] > mx[m] + dlt)) return true;
             return false;
         }
+        case HCC_MOOD_U2: return u2_fails(p, prev, &cand[p * M]);
         default: return false;
         }
     }
 
+    // _global_range(::MOODu2, U, N) (MOOD.jl:215-221): max - min per component over all particles of the stage
+    // state, NaN-propagating; empty when the plateau test is off.
+    std::vector<double> u2_range;
+    void global_range(const double *prev) {
+        u2_range.clear();
+        if (!(cfg.mood_criterion == HCC_MOOD_U2 && cfg.u2_plateau > 0.0) || N == 0) return;
+        std::vector<double> lo(prev, prev + M), hi(prev, prev + M);
+        for (int64_t p = 1; p < N; ++p)
+            for (int m = 0; m < M; ++m) {
+                lo[m] = jmin(lo[m], prev[p * M + m]);
+                hi[m] = jmax(hi[m], prev[p * M + m]);
+            }
+        u2_range.resize(M);
+        for (int m = 0; m < M; ++m) u2_range[m] = hi[m] - lo[m];
+    }
+
+    // _u2_fails (MOOD.jl:223-271): the DMP-violating components that are not a plateau; below order 3 (no curvature
+    // terms) any such component flags; otherwise per axis the curvature terms of the cached reconstruction over
+    // {p} ∪ N(p) must keep one sign and, over the neighbours within 1.5h, comparable magnitudes.
+    bool u2_fails(int64_t p, const double *prev, const double *nr) const {
+        const double dlt = cfg.mood_delta, d3 = dlt * dlt * dlt;
+        double mn[HCC_MAX_VARS], mx[HCC_MAX_VARS];
+        for (int m = 0; m < M; ++m) mn[m] = mx[m] = prev[p * M + m];
+        for (int64_t s = start[p]; s < start[p + 1]; ++s) {
+            const double *rj = &prev[int64_t(nidx[s]) * M];
+            for (int m = 0; m < M; ++m) { mn[m] = jmin(mn[m], rj[m]); mx[m] = jmax(mx[m], rj[m]); }
+        }
+        bool viol[HCC_MAX_VARS], any = false;
+        for (int m = 0; m < M; ++m) {
+            viol[m] = std::fabs(mx[m] - mn[m]) >= d3 && (nr[m] < mn[m] - dlt || nr[m] > mx[m] + dlt) &&
+                      !(!u2_range.empty() && mx[m] - mn[m] < cfg.u2_plateau * u2_range[m]);
+            any = any || viol[m];
+        }
+        if (!any) return false;
+        if (max_order < 3 || orders[p] < 3) return true;
+        double h = cfg.dx[0];
+        for (int d = 1; d < D; ++d) h = std::min(h, cfg.dx[d]);
+        const double h2 = h * h, near_sq = (1.5 * h) * (1.5 * h);
+        for (int d = 0; d < D; ++d) {
+            const int b = D + d;                                    // curvature term of axis d
+            const double *ci = &grads[(size_t(p) * Br + b) * M];
+            double mini[HCC_MAX_VARS], maxi[HCC_MAX_VARS], minA[HCC_MAX_VARS], maxA[HCC_MAX_VARS];
+            for (int m = 0; m < M; ++m) { mini[m] = maxi[m] = ci[m]; minA[m] = maxA[m] = std::fabs(ci[m]); }
+            for (int64_t s = start[p]; s < start[p + 1]; ++s) {
+                const double *cj = &grads[(size_t(nidx[s]) * Br + b) * M];
+                double r2 = 0.0;
+                for (int e = 0; e < D; ++e) r2 = (e == 0) ? ndist[s * D] * ndist[s * D] : r2 + ndist[s * D + e] * ndist[s * D + e];
+                const bool near = r2 <= near_sq;
+                for (int m = 0; m < M; ++m) {
+                    mini[m] = jmin(mini[m], cj[m]);
+                    maxi[m] = jmax(maxi[m], cj[m]);
+                    if (near) { minA[m] = jmin(minA[m], std::fabs(cj[m])); maxA[m] = jmax(maxA[m], std::fabs(cj[m])); }
+                }
+            }
+            for (int m = 0; m < M; ++m) {
+                if (!viol[m]) continue;
+                if (jmax(std::fabs(mini[m]), std::fabs(maxi[m])) * h2 < dlt) continue;   // negligible curvature
+                const bool same_sign = (mini[m] * h2) * (maxi[m] * h2) > -(dlt * dlt);
+                const bool comparable = cfg.u2_ratio <= 0.0 || minA[m] >= cfg.u2_ratio * maxA[m];
+                if (!(same_sign && comparable)) return true;
+            }
+        }
+        return false;
+    }
+
     bool detect_and_drop(const double *prev, const double *cand, bool full, bool with_eq) {
         if (cfg.mood_criterion == HCC_MOOD_NONE) return false;
+        global_range(prev);
         std::fill(triggered.begin(), triggered.end(), 0);
         std::fill(changed.begin(), changed.end(), 0);
 #pragma omp parallel for schedule(dynamic, 256)
@@ -1755,6 +1822,22 @@ hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *c
     if (changed_any) *changed_any = any ? 1 : 0;
     return HCC_OK;
 }
+// The MOOD criterion of particle p for hand-set stage states (N x M), reconstruction gradients (N x Br x M, the
+// layout of orc_download_gradients), orders and a candidate state (M): the known-answer tests of MOODu2.
+hcc_status orc_criterion_flags(orc_ctx *ctx, int64_t p, const double *prev, const double *grads, const int32_t *orders,
+                               const double *cand, int32_t *flag) {
+    if (!ctx || !prev || !grads || !orders || !cand || !flag) return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    if (p < 0 || p >= s.N || !s.have_nb) return HCC_ERR_INVALID;
+    s.grads.assign(grads, grads + size_t(s.N) * s.Br * s.M);
+    s.orders.assign(orders, orders + s.N);
+    s.global_range(prev);
+    std::vector<double> c(size_t(s.N) * s.M, 0.0);
+    for (int m = 0; m < s.M; ++m) c[size_t(p) * s.M + m] = cand[m];
+    *flag = s.criterion_flags(p, prev, c.data()) ? 1 : 0;
+    return HCC_OK;
+}
+
 hcc_status orc_apply_bcs(orc_ctx *ctx, double *buf) {
     if (!ctx || !buf || !ctx->s.have_nb) return HCC_ERR_INVALID;
     ctx->s.apply_bcs(buf);

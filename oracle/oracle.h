@@ -81,6 +81,10 @@ hcc_status orc_interface_orders(orc_ctx *ctx, int64_t i, int64_t j, int32_t *oi,
 /* detect_and_drop! (MOOD.jl:375-405) against explicit prev/cand states; dirty may be NULL (full). */
 hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *cand, int32_t full,
                                const uint8_t *dirty, int32_t with_eq, int32_t *changed_any);
+/* The MOOD criterion of particle p (MOOD.jl:175-271) for hand-set stage states (N*M), gradients (N*Br*M), orders
+   and a candidate (M): *flag = 1 if flagged. */
+hcc_status orc_criterion_flags(orc_ctx *ctx, int64_t p, const double *prev, const double *grads, const int32_t *orders,
+                               const double *cand, int32_t *flag);
 /* apply_boundary_conditions! (BoundaryConditions.jl:43-130) on buf (N*M) with rhos = the context state. */
 hcc_status orc_apply_bcs(orc_ctx *ctx, double *buf);
 

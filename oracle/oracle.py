@@ -75,6 +75,7 @@ def load(abi) -> C.CDLL:
         ("orc_interface_orders", C.c_int, [P, C.c_int64, C.c_int64, ip, ip]),
         ("orc_detect_and_drop", C.c_int, [P, dp, dp, C.c_int32, up, C.c_int32, ip]),
         ("orc_apply_bcs", C.c_int, [P, dp]),
+        ("orc_criterion_flags", C.c_int, [P, C.c_int64, dp, dp, ip, dp, ip]),
     ]
     for name, res, args in protos:
         fn = getattr(lib, name)
@@ -254,6 +255,18 @@ class OracleContext:
         self._check(self.lib.orc_detect_and_drop(self._h, _p(p, C.c_double), _p(c, C.c_double), int(bool(full)), dptr,
                                                  int(bool(with_eq)), C.byref(ch)), "orc_detect_and_drop")
         return bool(ch.value)
+
+    def criterion_flags(self, p, prev, grads, orders, cand) -> bool:
+        """The MOOD criterion of particle p for hand-set states, gradients (N x Br x M), orders and candidate."""
+        pv = np.ascontiguousarray(prev, dtype=np.float64)
+        g = np.ascontiguousarray(grads, dtype=np.float64)
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        c = np.ascontiguousarray(cand, dtype=np.float64)
+        f = C.c_int32()
+        self._check(self.lib.orc_criterion_flags(self._h, int(p), _p(pv, C.c_double), _p(g, C.c_double),
+                                                 _p(o, C.c_int32), _p(c, C.c_double), C.byref(f)),
+                    "orc_criterion_flags")
+        return bool(f.value)
 
     def apply_bcs(self, buf):
         b = np.ascontiguousarray(buf, dtype=np.float64).copy()

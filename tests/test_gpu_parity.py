@@ -385,3 +385,51 @@ def test_step_graph_reports_the_mood_iteration_cap(hcc, oracle, cuda_lib):
         with pytest.raises(hcc.HCCError, match="iteration cap"):
             g.step(0.0, dt)
         assert _bits_equal(g.download_state(), U0)
+
+
+@pytest.mark.parametrize("case", ["advection_u2", "advection_u2_vk", "euler_u2_noplateau", "euler_u2"])
+def test_mood_u2_steps_bit_exact(hcc, oracle, cuda_lib, case):
+    """MOODu2 (MOOD.jl:104-130, :215-271): plateau test with the global range of the stage state and the
+    smooth-extremum override from the curvature terms of MUSCL3 — states, orders and flags bit for bit
+    (the reference's GPU case "MUSCL3 MOODu2 EPD1 RK3", test/gpu_tests.jl:20, and its limited variant)."""
+    h = 0.02
+    if case.startswith("advection"):
+        cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=21)
+        pde = hcc.LinearAdvection(((1.0,), (0.5,)))
+        lim = "vk_hard" if case.endswith("vk") else "none"
+        x = cloud.pos
+        box = (x[:, 0] > 0.55) & (x[:, 0] < 0.8) & (x[:, 1] > 0.5)
+        U0 = (np.exp(-((x - 0.3) ** 2).sum(axis=1) / 0.01) + np.where(box, 1.0, 0.0))[:, None]
+        bc, scheme = {}, hcc.MUSCL(3, 0, lim)
+        u2 = hcc.MOODu2(1e-8)
+    else:
+        cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+        pde, bc, scheme = hcc.Euler(2), OUTFLOW, hcc.MUSCL(3, 0)
+        U0 = quadrant_ic(cloud)
+        u2 = hcc.MOODu2(1e-4 * h * h, plateau=0.0 if case.endswith("noplateau") else 1e-3)
+    cfg = hcc.make_config(pde, cloud, scheme=scheme, mood=hcc.MOOD(hcc.EPD1, u2), bc_map=bc)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.3 * o.time_step()
+    flagged = 0
+    for k in range(4):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.orders(), o.orders())
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+        flagged += int(o.mood_flags().sum())
+    assert flagged > 0
+    # the same run under MOODu1 flags at least as many particles (more where the override accepted candidates)
+    cfg1 = hcc.make_config(pde, cloud, scheme=scheme, mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(u2.delta)), bc_map=bc)
+    o1 = oracle.OracleContext(cfg1, __import__("sys").modules["hcc_gb300._abi"])
+    o1.upload_cloud(cloud)
+    o1.build_neighbours()
+    o1.prepare_geometry()
+    o1.upload_state(U0)
+    flagged1 = 0
+    for k in range(4):
+        o1.step(k * dt, dt)
+        flagged1 += int(o1.mood_flags().sum())
+    assert flagged1 >= flagged and (case == "euler_u2_noplateau" or flagged1 > flagged), (flagged1, flagged)

@@ -632,3 +632,108 @@ def test_weno_cfl_uses_the_assembled_fit(hcc, oracle, abi):
     Nm = (w[:4, None, None] * P[:, :, None] * P[:, None, :]).sum(0)
     c = np.abs((np.linalg.inv(Nm)[0] @ P.T) * w[:4] / (2 / 40))
     assert dt == pytest.approx(1.0 / (c.sum() * 2.0), rel=1e-12)
+
+
+class _U2Lattice:
+    """unit_core.jl:781-878: a 2-D periodic 20 x 20 lattice with hand-set states (M = 2) and curvature coefficients
+    (the degree-2 terms D+1, D+2 of the cached reconstruction of MUSCL order 3); the criterion on its own."""
+
+    def __init__(self, hcc, oracle, abi, crit):
+        n = 20
+        self.dx = dx = 1.0 / n
+        self.cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), dx, 2.5 * dx, periodic=True)
+        self.o = make(hcc, oracle, abi, self.cl, hcc.LinearAdvection(((1.0, 1.0), (0.0, 0.0))),
+                      scheme=hcc.MUSCL(3, 2), mood=hcc.MOOD(hcc.EPD2, crit))
+        self.N = self.cl.n
+        counts, idx, _, _ = self.o.neighbours()
+        self.start = np.concatenate([[0], np.cumsum(counts)])
+        self.idx = idx
+        self.orders = np.full(self.N, 3, dtype=np.int32)
+
+    def nearest(self, c):
+        return int(np.argmin(((self.cl.pos - np.asarray(c)) ** 2).sum(axis=1)))
+
+    def set_fields(self, f1, d1, f2, d2):
+        x = self.cl.pos
+        self.U = np.stack([f1(x), f2(x)], axis=1)
+        self.G = np.zeros((self.N, 5, 2))
+        c1, c2 = d1(x), d2(x)
+        self.G[:, 2, 0], self.G[:, 2, 1] = c1[0], c2[0]
+        self.G[:, 3, 0], self.G[:, 3, 1] = c1[1], c2[1]
+
+    def local_extrema(self, p, m):
+        v = self.U[np.concatenate([[p], self.idx[self.start[p]:self.start[p + 1]]]), m]
+        return v.min(), v.max()
+
+    def flags(self, p, cand):
+        return self.o.criterion_flags(p, self.U, self.G, self.orders, np.asarray(cand, dtype=np.float64))
+
+
+@pytest.mark.parametrize("plateau", [0.0, 1e-3])
+def test_mood_u2_smooth_minimum_next_to_an_inflection_line(hcc, oracle, abi, plateau):
+    """unit_core.jl:815-833: an undershoot of a smooth minimum is accepted (one-signed, comparable curvature); the
+    same undershoot of a component at its inflection line is rejected; below order 3 the plain DMP applies."""
+    d = 1e-8
+    L = _U2Lattice(hcc, oracle, abi, hcc.MOODu2(d, plateau=plateau))
+    w, c0 = 0.1, (0.5, 0.5)
+    gauss = lambda x: np.exp(-((x[:, 0] - c0[0]) ** 2 + (x[:, 1] - c0[1]) ** 2) / w)
+    f1 = lambda x: 1 - 0.5 * gauss(x)
+    d1 = lambda x: (-0.5 * gauss(x) * (4 * (x[:, 0] - c0[0]) ** 2 / w ** 2 - 2 / w),
+                    -0.5 * gauss(x) * (4 * (x[:, 1] - c0[1]) ** 2 / w ** 2 - 2 / w))
+    f2 = lambda x: np.sin(2 * np.pi * x[:, 0])
+    d2 = lambda x: (-(2 * np.pi) ** 2 * np.sin(2 * np.pi * x[:, 0]), np.zeros(len(x)))
+    L.set_fields(f1, d1, f2, d2)
+    p = L.nearest(c0)
+    lo1, _ = L.local_extrema(p, 0)
+    cand = (lo1 - 10 * d, L.U[p, 1])
+    assert not L.flags(p, cand)
+    lo2, _ = L.local_extrema(p, 1)
+    assert L.flags(p, (L.U[p, 0], lo2 - 10 * d))
+    L.orders[p] = 2
+    assert L.flags(p, cand)
+
+
+def test_mood_u2_plateau(hcc, oracle, abi):
+    """unit_core.jl:835-853: a ripple of amplitude 1e-6 (curvature changing sign) overshot by 5 delta is flagged
+    without the plateau test and accepted with it (local range 2e-6 < 1e-3 x global range 0.5), also below order 3."""
+    d = 1e-8
+    c0, q = (0.5, 0.5), (0.1, 0.1)
+    narrow = lambda x: np.exp(-((x[:, 0] - c0[0]) ** 2 + (x[:, 1] - c0[1]) ** 2) / 0.01)
+    ripple = lambda x: 1e-6 * np.sin(20 * np.pi * x[:, 0] + 0.7)
+    g1 = lambda x: 1 - 0.5 * narrow(x) + ripple(x)
+    dg1 = lambda x: (-1e-6 * (20 * np.pi) ** 2 * np.sin(20 * np.pi * x[:, 0] + 0.7), np.zeros(len(x)))
+    zero = lambda x: np.zeros(len(x))
+    for plateau, expect in ((0.0, True), (1e-3, False)):
+        L = _U2Lattice(hcc, oracle, abi, hcc.MOODu2(d, plateau=plateau))
+        L.set_fields(g1, dg1, zero, lambda x: (zero(x), zero(x)))
+        p = L.nearest(q)
+        lo, hi = L.local_extrema(p, 0)
+        assert hi - lo < 1e-5
+        assert L.flags(p, (hi + 5 * d, 0.0)) == expect
+        if plateau > 0:
+            L.orders[p] = 1
+            assert not L.flags(p, (hi + 5 * d, 0.0))
+
+
+def test_mood_u2_jump_is_flagged(hcc, oracle, abi):
+    """unit_core.jl:855-875: a jump with Gibbs-like curvature is flagged with or without the plateau test; at the
+    corner of a jump (zero curvature next to it) only the magnitude test among the nearest neighbours sees it."""
+    d = 1e-8
+    dx = 1.0 / 20
+    step = lambda x: np.where(x[:, 0] < 0.5, 0.0, 1.0)
+    dstep = lambda x: (np.where(np.abs(x[:, 0] - 0.5) < 2.5 * dx, np.where(x[:, 0] < 0.5, 1 / dx ** 2, -1 / dx ** 2), 0.0),
+                       np.zeros(len(x)))
+    zero = lambda x: np.zeros(len(x))
+    for crit in (dict(plateau=0.0), dict(), dict(plateau=1e-2)):
+        L = _U2Lattice(hcc, oracle, abi, hcc.MOODu2(d, **crit))
+        L.set_fields(step, dstep, zero, lambda x: (zero(x), zero(x)))
+        p = L.nearest((0.5 - dx / 2, 0.5))
+        _, hi = L.local_extrema(p, 0)
+        assert L.flags(p, (hi + 1e-3, 0.0)), crit
+    corner = lambda x: (np.where((0.5 <= x[:, 0]) & (x[:, 0] < 0.5 + dx / 2), -1 / dx ** 2, 0.0), np.zeros(len(x)))
+    for ratio, expect in ((0.5, True), (0.0, False)):
+        L = _U2Lattice(hcc, oracle, abi, hcc.MOODu2(d, ratio=ratio))
+        L.set_fields(step, corner, zero, lambda x: (zero(x), zero(x)))
+        p = L.nearest((0.5 + dx, 0.5))
+        _, hi = L.local_extrema(p, 0)
+        assert L.flags(p, (hi + 1e-3, 0.0)) == expect
