@@ -110,11 +110,20 @@ class KineticRelaxation:
 
 @dataclass
 class MUSCL:
-    """MUSCL(T, D, M, order, limiter, RusanovFlux(); div_order) (src/Interpolation/MUSCL.jl:116). `limiter` is one
-    of "none", "bj_soft", "bj_hard", "vk_soft", "vk_hard" (BarthJespersen / Venkatakrishnan, :soft / :hard)."""
+    """MUSCL(T, D, M, order, limiter, flux; div_order) (src/Interpolation/MUSCL.jl:116). `limiter` is one
+    of "none", "bj_soft", "bj_hard", "vk_soft", "vk_hard" (BarthJespersen / Venkatakrishnan, :soft / :hard);
+    `flux` is "rusanov" (RusanovFlux) or "aligned" (AlignedRusanovFlux, FluxFunctions.jl:103-111)."""
     order: int = 2
     div_order: int = 0
     limiter: str = "none"
+    flux: str = "rusanov"
+
+
+def Upwind(div_order: int = 0, flux: str = "rusanov") -> MUSCL:
+    """UpwindDivergence(T, D, M, 1, :Classic, flux; div_order) (src/Interpolation/Upwind.jl): piecewise-constant
+    states, the numerical flux per pair and the MLS divergence of degree 1 — the first-order MUSCL scheme (the
+    reference's unit test unit_core.jl:937-945 holds the two equal to 1e-12)."""
+    return MUSCL(1, div_order, "none", flux)
 
 
 @dataclass
@@ -193,6 +202,7 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
     else:
         cfg.scheme = _abi.SCHEME_MUSCL
         cfg.limiter = _abi.LIMITERS[scheme.limiter]
+        cfg.flux = _abi.FLUXES[scheme.flux]
     cfg.tableau = TABLEAUS[tableau] if isinstance(tableau, str) else int(tableau)
     cfg.mood_substeps = 1 if mood_substeps else 0
     cfg.max_mood_iterations = max_mood_iterations
@@ -418,7 +428,7 @@ class GB300RKTimeStepper:
 
 
 __all__ = [
-    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "WENO", "MOOD", "MOODu1", "MOODu2",
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "MOOD", "MOODu1", "MOODu2",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",

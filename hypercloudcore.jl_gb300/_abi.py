@@ -20,6 +20,7 @@ PDE_ADVECTION, PDE_EULER, PDE_BGK = 0, 1, 2
 FP64, FP32 = 0, 1
 # hcc_mood_criterion
 MOOD_NONE, MOOD_U1, MOOD_PAD, MOOD_ONLY, MOOD_U2 = 0, 1, 2, 3, 4
+FLUXES = {"rusanov": 0, "aligned": 1}
 # hcc_mood_strategy
 EPD_NONE, EPD0, EPD1, EPD2 = 0, 1, 2, 3
 # hcc_tableau
@@ -41,7 +42,8 @@ class HccConfig(C.Structure):
         ("mood_criterion", C.c_int32), ("mood_strategy", C.c_int32), ("tableau", C.c_int32),
         ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
         ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
-        ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("reserved_i", C.c_int32 * 5),
+        ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("flux", C.c_int32),
+        ("reserved_i", C.c_int32 * 4),
         ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
         ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),

@@ -367,6 +367,7 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.sc.criterion = c->cfg.mood_criterion;
     a.sc.has_source = c->has_source;
     a.sc.limiter = c->cfg.limiter;
+    a.sc.aligned = c->cfg.flux == HCC_FLUX_ALIGNED;
     a.orders = c->orders;
     a.nbmin = c->nbmin;
     a.grad = static_cast<T *>(c->grad);
@@ -849,6 +850,7 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if (f.muscl_order < 1 || f.muscl_order > 3) return c->fail(HCC_ERR_UNSUPPORTED, "muscl_order must be 1, 2 or 3");
     if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_EPD2) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
     if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_U2) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
+    if (f.flux < HCC_FLUX_RUSANOV || f.flux > HCC_FLUX_ALIGNED) return c->fail(HCC_ERR_INVALID, "unknown numerical flux");
     if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
     if (f.limiter < HCC_LIMITER_NONE || f.limiter > HCC_LIMITER_VK_HARD) return c->fail(HCC_ERR_INVALID, "unknown limiter");
     if (f.scheme != HCC_SCHEME_MUSCL && f.scheme != HCC_SCHEME_WENO) return c->fail(HCC_ERR_INVALID, "unknown scheme");

@@ -160,6 +160,7 @@ struct SchemeParams {
     int max_order, DO, strategy, criterion;
     int has_source;                   // BGK relaxation source present
     int limiter;                      // hcc_limiter
+    int aligned;                      // AlignedRusanovFlux
 };
 
 // Device view of the neighbour lists and geometry caches (slot-major, stride = npad).

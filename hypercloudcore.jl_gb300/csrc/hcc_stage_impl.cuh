@@ -804,6 +804,10 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
             if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
             else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
             else { oi = oi_own; oj = oj_own; }
+            // AlignedRusanovFlux (MUSCL.jl:331-338): where either particle is below the full order (every pair at
+            // order 1) the states are sorted by the signs of the slot's divergence weights instead of the distance
+            const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
+                                                oj_own < a.sc.max_order);
             T pi[BR], pj[BR];
             if constexpr (kFast && RDEG == 1) {
                 // degree 1: an interface of order 2 keeps the linear terms, order 1 none (the midpoint offsets
@@ -868,7 +872,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
                 if constexpr (M & 1) jump[M - 1] = fji[M - 1] - fij[M - 1];
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    const T ssd = dk[d] > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
+                    const T ssd = (below ? wk[d] : dk[d]) > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
                     const float2 nssd = p_bc(-ssd), w2 = p_bc(wk[d]);
 #pragma unroll
                     for (int q = 0; q < M / 2; ++q) {
@@ -884,7 +888,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
             } else {
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    const bool pos = dk[d] > T(0);
+                    const bool pos = (below ? wk[d] : dk[d]) > T(0);
                     // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
                     // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its
                     // orientation

@@ -33,7 +33,7 @@ mutable struct HccConfig
     abi_version::Int32; dim::Int32; n_vars::Int32; pde::Int32; precision::Int32; muscl_order::Int32
     div_order::Int32; mood_criterion::Int32; mood_strategy::Int32; tableau::Int32; mood_substeps::Int32
     periodic::NTuple{3, Int32}; bc_by_tag::NTuple{16, Int32}; max_mood_iterations::Int32
-    scheme::Int32; limiter::Int32; slot_capacity::Int32; reserved_i::NTuple{5, Int32}
+    scheme::Int32; limiter::Int32; slot_capacity::Int32; flux::Int32; reserved_i::NTuple{4, Int32}
     dx::NTuple{3, Float64}; radius::Float64; weight_alpha::Float64
     canvas_min::NTuple{3, Float64}; canvas_max::NTuple{3, Float64}
     domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
@@ -60,6 +60,8 @@ end
 _tableau_id(bt) = error("unknown tableau")
 _strategy_id(::EPD0) = Int32(1); _strategy_id(::EPD1) = Int32(2); _strategy_id(::EPD2) = Int32(3)
 _strategy_id(::MOODStrategy) = Int32(0)
+_flux_id(::RusanovFlux) = Int32(0)
+_flux_id(::AlignedRusanovFlux) = Int32(1)
 _limiter_id(::NoLimiter) = Int32(0)
 _limiter_id(::BarthJespersenLimiter{:soft}) = Int32(1)
 _limiter_id(::BarthJespersenLimiter{:hard}) = Int32(2)
@@ -78,6 +80,7 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     cfg.precision = precision === :fp32 ? 1 : 0
     cfg.muscl_order = HyperCloudCore._extract_order(interp)
     cfg.limiter = _limiter_id(interp.limiter)
+    cfg.flux = _flux_id(interp.flux)
     cfg.tableau = tableau_id
     cfg.mood_strategy = _strategy_id(mood.strategy)
     cfg.mood_criterion, cfg.mood_delta = _criterion(mood.criterion)

@@ -93,6 +93,12 @@ typedef enum {               /* slope limiters of the MUSCL pre-pass (Limiter.jl
     HCC_LIMITER_VK_HARD = 4  /* VenkatakrishnanLimiter(:hard) */
 } hcc_limiter;
 
+typedef enum {               /* numerical flux of MUSCL (FluxFunctions.jl) */
+    HCC_FLUX_RUSANOV = 0,    /* RusanovFlux: states sorted per axis by the sign of the distance */
+    HCC_FLUX_ALIGNED = 1     /* AlignedRusanovFlux: sorted by the sign of the slot's divergence weight where either
+                                particle is below the full order (and on every pair of a first-order scheme) */
+} hcc_flux;
+
 typedef enum {               /* src/Grid/BoundaryConditions.jl */
     HCC_BC_KEEP = 0,         /* no condition for the tag: the particle keeps its start-of-step state */
     HCC_BC_DIRICHLET = 1,    /* FixedDirichlet */
@@ -118,7 +124,8 @@ typedef struct {
     int32_t scheme;                    /* hcc_scheme */
     int32_t limiter;                   /* hcc_limiter (MUSCL only) */
     int32_t slot_capacity;             /* neighbours per particle the lists may hold (0: no limit) */
-    int32_t reserved_i[5];
+    int32_t flux;                      /* hcc_flux (MUSCL numerical flux) */
+    int32_t reserved_i[4];
     double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
     double  radius;                    /* support radius R of ExponentialWeightFunction */
     double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */

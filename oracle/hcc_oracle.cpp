@@ -519,6 +519,7 @@ struct Solver {
     bool weno = false;
     double invL = 1.0;
     bool streamed = true;
+    bool aligned = false;            // AlignedRusanovFlux
     bool have_geom = false;
     std::vector<double> inv_r, inv_d, dw;
     std::vector<uint8_t> ok_r, ok_d;
@@ -553,6 +554,7 @@ struct Solver {
             invLwrap[d] = per[d] ? 1.0 / Lphys[d] : 0.0;
         }
         max_order = c.muscl_order;
+        aligned = c.flux == HCC_FLUX_ALIGNED;
         weno = c.scheme == HCC_SCHEME_WENO;
         if (max_order < 1 || max_order > 3) { err = "muscl_order must be 1..3"; return false; }
         if (weno && (M != 1 || c.pde == HCC_PDE_EULER)) { err = "WENO is a scalar scheme (n_vars = 1)"; return false; }
@@ -939,8 +941,10 @@ struct Solver {
                     for (int c = 0; c < Bq; ++c) Nm[r * Bq + c] = Nm[r * Bq + c] + w * (p[r] * p[c]);
             }
             dyn_ok = cholesky_moment(Bq, Nm, Ucd);
-            if (streamed && !dyn_ok) return;            // singular moment matrix: zero divergence
+            if ((streamed || aligned) && !dyn_ok) return;   // singular moment matrix: zero divergence
         }
+        // the streamed form, and the aligned flux off the cached fit, contract per slot (MUSCL.jl:405-409)
+        const bool per_slot = streamed || (aligned && !cached);
         // buffered: per-slot flux differences
         std::vector<double> buf;
         if (!streamed) buf.assign(size_t(num) * D * M, 0.0);
@@ -972,21 +976,10 @@ struct Solver {
             }
             phys.flux(fij, Fij);
             phys.flux(fji, Fji);
-            // sort_flux (Utils.jl:270-278) + RusanovFlux (FluxFunctions.jl:90-100)
-            for (int d = 0; d < D; ++d) {
-                bool pos_ = dk[d] > 0.0;
-                const double *fL = pos_ ? fij : fji;
-                const double *fR = pos_ ? fji : fij;
-                const double *FL = pos_ ? &Fij[d * M] : &Fji[d * M];
-                const double *FR = pos_ ? &Fji[d * M] : &Fij[d * M];
-                double sdd = jmax(phys.lam(fL, d), phys.lam(fR, d));
-                for (int m = 0; m < M; ++m) {
-                    double Fn = 0.5 * ((FL[m] + FR[m]) - sdd * (fR[m] - fL[m]));
-                    dF[d * M + m] = Fn - Fi[d * M + m];
-                }
-            }
-            if (streamed) {
-                double wk[3];
+            // the slot's divergence weights c_ij (_slot_weight, MUSCL.jl:429-445): the cached fit, or the dynamic
+            // fit solved per slot; the streamed contraction and the aligned orientation use them
+            double wk[3] = {0.0, 0.0, 0.0};
+            if (streamed || aligned) {
                 if (cached) {
                     for (int d = 0; d < D; ++d) wk[d] = dw[s * D + d];
                 } else {
@@ -999,6 +992,25 @@ struct Solver {
                     chol_solve(Bq, Ucd, p, c);
                     for (int d = 0; d < D; ++d) wk[d] = c[d + 1] * invL;
                 }
+            }
+            // AlignedRusanovFlux (FluxFunctions.jl:103-111, MUSCL.jl:331-338): where either particle is below the
+            // full order, or always at order 1, the states are sorted by the signs of c_ij instead of the distance
+            const bool below = max_order == 1 || eff < max_order || orders[j] < max_order;
+            const double *dir = (aligned && below) ? wk : dk;
+            // sort_flux (Utils.jl:270-278) + RusanovFlux (FluxFunctions.jl:90-100)
+            for (int d = 0; d < D; ++d) {
+                bool pos_ = dir[d] > 0.0;
+                const double *fL = pos_ ? fij : fji;
+                const double *fR = pos_ ? fji : fij;
+                const double *FL = pos_ ? &Fij[d * M] : &Fji[d * M];
+                const double *FR = pos_ ? &Fji[d * M] : &Fij[d * M];
+                double sdd = jmax(phys.lam(fL, d), phys.lam(fR, d));
+                for (int m = 0; m < M; ++m) {
+                    double Fn = 0.5 * ((FL[m] + FR[m]) - sdd * (fR[m] - fL[m]));
+                    dF[d * M + m] = Fn - Fi[d * M + m];
+                }
+            }
+            if (per_slot) {
                 // _contract (MUSCL.jl:452-458)
                 for (int m = 0; m < M; ++m) {
                     double t = wk[0] * dF[0 * M + m];
@@ -1010,7 +1022,7 @@ struct Solver {
                 for (int q = 0; q < D * M; ++q) dst[q] = dF[q];
             }
         }
-        if (streamed) return;
+        if (per_slot) return;
         // buffered fits
         if (cached) {
             // apply_weights_divergence (Interpolators.jl:610-626)

@@ -62,3 +62,11 @@ def test_euler_needs_matching_n_vars(hcc, cuda_lib):
 def test_missing_library_fails_loudly(hcc, tmp_path):
     with pytest.raises(hcc.HCCError):
         hcc.load_library(tmp_path / "nope.so")
+
+
+def test_upwind_is_first_order_muscl(hcc):
+    """UpwindDivergence(:Classic) is the first-order MUSCL scheme (unit_core.jl:937-945)."""
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), 0.05, 0.125, periodic=True)
+    a = hcc.make_config(hcc.LinearAdvection(((1.0,), (1.0,))), cl, scheme=hcc.Upwind(2))
+    b = hcc.make_config(hcc.LinearAdvection(((1.0,), (1.0,))), cl, scheme=hcc.MUSCL(1, 2))
+    assert bytes(a) == bytes(b)

@@ -433,3 +433,44 @@ def test_mood_u2_steps_bit_exact(hcc, oracle, cuda_lib, case):
         o1.step(k * dt, dt)
         flagged1 += int(o1.mood_flags().sum())
     assert flagged1 >= flagged and (case == "euler_u2_noplateau" or flagged1 > flagged), (flagged1, flagged)
+
+
+@pytest.mark.parametrize("case", ["euler_muscl3_aligned", "euler_muscl2_aligned_fp32", "upwind_aligned"])
+def test_aligned_rusanov_steps(hcc, oracle, cuda_lib, case):
+    """AlignedRusanovFlux (FluxFunctions.jl:103-111; MUSCL.jl:331-338, :405-409): interface states sorted by the
+    signs of the slot's divergence weights on pairs below the full order (every pair of a first-order scheme, the
+    Upwind classic scheme). FP64 bit for bit; FP32 within 1e-5 relative L1 of the FP64 oracle."""
+    h = 0.02
+    if case.startswith("euler"):
+        cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+        pde, bc, U0 = hcc.Euler(2), OUTFLOW, quadrant_ic(cloud)
+        order = 3 if "muscl3" in case else 2
+        scheme = hcc.MUSCL(order, 0, "none", "aligned")
+        mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
+    else:
+        cloud = c1_cloud(hcc)
+        pde, bc, U0 = hcc.LinearAdvection(((1.0,), (1.0,))), ADV_BC, gaussian_ic(cloud)
+        scheme, mood = hcc.Upwind(2, "aligned"), hcc.MOOD(hcc.EPD1, hcc.NoMOOD())
+    fp32 = case.endswith("fp32")
+    cfg = hcc.make_config(pde, cloud, scheme=scheme, mood=mood, bc_map=bc)
+    abi = __import__("sys").modules["hcc_gb300._abi"]
+    o = oracle.OracleContext(cfg, abi)
+    g = hcc.Context(hcc.make_config(pde, cloud, scheme=scheme, mood=mood, bc_map=bc,
+                                    precision="fp32" if fp32 else "fp64"))
+    for c in (g, o):
+        c.upload_cloud(cloud)
+        c.build_neighbours()
+        c.prepare_geometry()
+    o.upload_state(U0)
+    g.upload_state(U0.astype(np.float32) if fp32 else U0)
+    dt = 0.4 * o.time_step()
+    for k in range(4):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        if not fp32:
+            assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+            np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+    if fp32:
+        inner = cloud.is_boundary == 0
+        assert _rel_l1(g.download_state()[:, 0], o.download_state()[:, 0], inner) < 1e-5
+
