@@ -165,6 +165,19 @@ class MOOD:
     criterion: object = field(default_factory=NoMOOD)
 
 
+def mover(kind: str = "none", *, alpha: float = 1.0, velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0),
+          center=(0.0, 0.0, 0.0), full_search_per_stage: bool = False) -> "_abi.HccMover":
+    """Grid mover (src/TimeStepping/GridMovers.jl): "none" (NoGridMover), "lagrangian" (LagrangianMover), "scaled"
+    (ScaledLagrangianMover(alpha)) or "prescribed" (PrescribedMover with w(x) = velocity + omega x (x - center))."""
+    m = _abi.HccMover()
+    m.kind = _abi.MOVERS[kind]
+    m.full_search_per_stage = int(bool(full_search_per_stage))
+    m.alpha = float(alpha)
+    for d in range(3):
+        m.velocity[d], m.omega[d], m.center[d] = float(velocity[d]), float(omega[d]), float(center[d])
+    return m
+
+
 def config_defaults() -> HccConfig:
     """Python twin of hcc_config_defaults (include/hcc.h): the reference's defaults."""
     cfg = HccConfig()
@@ -380,6 +393,15 @@ class Context:
     def set_profiling(self, enable: bool = True):
         self._check(self.lib.hcc_set_profiling(self._h, int(bool(enable))), "hcc_set_profiling")
 
+    def set_mover(self, m):
+        """Select the grid mover (see `mover`)."""
+        self._check(self.lib.hcc_set_mover(self._h, C.byref(m)), "hcc_set_mover")
+
+    def positions(self) -> np.ndarray:
+        out = np.zeros((self.n, self.D), dtype=np.float64)
+        self._check(self.lib.hcc_download_positions(self._h, _ptr(out, C.c_double)), "hcc_download_positions")
+        return out
+
     def set_step_graphs(self, enable: bool = True):
         """Take each step as one captured CUDA graph (default) or drive the MOOD fixed points from the host."""
         self._check(self.lib.hcc_set_step_graphs(self._h, int(bool(enable))), "hcc_set_step_graphs")
@@ -428,7 +450,7 @@ class GB300RKTimeStepper:
 
 
 __all__ = [
-    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "MOOD", "MOODu1", "MOODu2",
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "mover", "MOOD", "MOODu1", "MOODu2",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",

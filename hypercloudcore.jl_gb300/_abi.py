@@ -67,6 +67,15 @@ class HccCounters(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class HccMover(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("full_search_per_stage", C.c_int32), ("alpha", C.c_double),
+                ("velocity", C.c_double * HCC_MAX_DIM), ("omega", C.c_double * HCC_MAX_DIM),
+                ("center", C.c_double * HCC_MAX_DIM)]
+
+
+MOVERS = {"none": 0, "lagrangian": 1, "scaled": 2, "prescribed": 3}
+
+
 class HccKernelTimes(C.Structure):
     _fields_ = [("gather_ms", C.c_double), ("gather_launches", C.c_int64), ("flux_ms", C.c_double),
                 ("flux_launches", C.c_int64), ("recompute_ms", C.c_double), ("recompute_launches", C.c_int64),
@@ -107,6 +116,8 @@ PROTOTYPES = [
     ("hcc_total_mass", C.c_int, [P, _dp]),
     ("hcc_set_profiling", C.c_int, [P, C.c_int]),
     ("hcc_set_step_graphs", C.c_int, [P, C.c_int]),
+    ("hcc_set_mover", C.c_int, [P, C.POINTER(HccMover)]),
+    ("hcc_download_positions", C.c_int, [P, C.POINTER(C.c_double)]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_synchronize", C.c_int, [P]),

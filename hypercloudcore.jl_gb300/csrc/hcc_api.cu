@@ -204,6 +204,14 @@ struct hcc_ctx {
     ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
     int list_blocks = 1, drop_blocks = 1;
     unsigned long long *u2_keys = nullptr;       // MOODu2 global range of the stage state (ordered keys)
+    // moving grid: mover, start-of-step / stage / final positions and the stage grid velocities (SoA FP64)
+    hcc_mover mover{};
+    double *x_n = nullptr, *x_cand = nullptr, *Xs[HCC_MAX_STAGES] = {}, *KXs[HCC_MAX_STAGES] = {};
+    bool moving() const { return mover.kind != HCC_MOVER_NONE; }
+    void free_mover_buffers() {
+        dfree(x_n); dfree(x_cand);
+        for (int q = 0; q < HCC_MAX_STAGES; ++q) { dfree(Xs[q]); dfree(KXs[q]); }
+    }
     bool u2_plateau_on() const { return cfg.mood_criterion == HCC_MOOD_U2 && cfg.u2_plateau > 0.0; }
     unsigned long long *d_counters = nullptr;   // [0..1] drop counters, [2] dt bits, [3..4] search stats
     unsigned long long *h_counters = nullptr;   // pinned mirror
@@ -291,6 +299,7 @@ struct hcc_ctx {
 
     void free_particles() {
         drop_graphs();
+        free_mover_buffers();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
@@ -427,6 +436,7 @@ template <typename T> hcc_status upload_coeffs(hcc_ctx *c, double dt) {
             const double at = fin ? c->tab.bt[j] : c->tab.at[s + 1][j];
             const double ai = fin ? c->tab.b[j] : c->tab.a[s + 1][j];
             e.hE[j] = at != 0.0 ? T(dt * at) : T(0);
+            e.hEd[j] = at != 0.0 ? dt * at : 0.0;
             e.hI[j] = (ai != 0.0 && c->has_source) ? T(dt * ai) : T(0);
         }
         if (!fin) {
@@ -449,6 +459,18 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
         a.KI[q] = static_cast<const T *>(c->KI[q]);
     }
     const StageCoeffs<T> *coef = static_cast<const StageCoeffs<T> *>(c->coef_dev);
+    if (c->moving()) {
+        a.mover = c->mover.kind;
+        a.mv_alpha = T(c->mover.alpha);
+        for (int d = 0; d < 3; ++d) {
+            a.mv_v[d] = c->mover.velocity[d];
+            a.mv_om[d] = c->mover.omega[d];
+            a.mv_c[d] = c->mover.center[d];
+        }
+        a.pos = c->pos;
+        a.x_n = c->x_n;
+        for (int q = 0; q < S; ++q) a.KX[q] = c->KXs[q];
+    }
     if (s < 0) {
         a.Ynext = static_cast<T *>(c->Y[0]);
         a.KInext = static_cast<T *>(c->KI[0]);
@@ -470,6 +492,10 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
         a.implicit_mode = implicit_mode(c, s + 1);
     }
     a.check = c->cfg.mood_criterion != HCC_MOOD_NONE;
+    if (c->moving()) {
+        a.KXout = c->KXs[s];
+        a.Xnext = fin ? c->x_cand : c->Xs[s + 1];
+    }
     a.check_substep = c->ratio > 0.0;
     a.KIs = c->has_source ? static_cast<const T *>(c->KI[s]) : nullptr;
     return a;
@@ -596,20 +622,46 @@ void take_mood_stats(hcc_ctx *c) {
     c->inadmissible = int64_t(ms.inadmissible);
 }
 
-// The step with the MOOD fixed points driven from the host (one read of the decision per decrement).
+hcc_status apply_positions(hcc_ctx *c, const double *src, bool full_search);
+
+// The step with the MOOD fixed points driven from the host (one read of the decision per decrement). On a moving
+// grid the positions are stage variables: after the fixed point of a candidate its stage geometry is applied
+// (distances, weights and MLS caches at the new positions), and a full search follows the step.
 template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
     const int64_t n = c->n;
     const int S = c->tab.s;
+    const bool mv = c->moving();
     c->launches = 0;
     hcc_status st = upload_coeffs<T>(c, dt);
     if (st != HCC_OK) return st;
+    if (mv) {
+        const size_t pb = size_t(c->npad) * c->D * sizeof(double);
+        if (!c->x_n) {
+            const size_t cnt = size_t(c->npad) * c->D;
+            if ((st = c->alloc(c->x_n, cnt, "start-of-step positions")) != HCC_OK) return st;
+            if ((st = c->alloc(c->x_cand, cnt, "final positions")) != HCC_OK) return st;
+            for (int q = 0; q < S; ++q) {
+                if ((st = c->alloc(c->Xs[q], cnt, "stage positions")) != HCC_OK) return st;
+                if ((st = c->alloc(c->KXs[q], cnt, "grid velocities")) != HCC_OK) return st;
+                cudaMemsetAsync(c->KXs[q], 0, cnt * sizeof(double), c->stream);
+            }
+        }
+        cudaMemcpyAsync(c->x_n, c->pos, pb, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->x_cand, c->pos, pb, cudaMemcpyDeviceToDevice, c->stream);
+        for (int q = 0; q < S; ++q) cudaMemcpyAsync(c->Xs[q], c->pos, pb, cudaMemcpyDeviceToDevice, c->stream);
+    }
     StageArgs<T> a1 = stage_args<T>(c, -1);
     c->launches += enqueue_prologue(c, &a1, c->stream);
     for (int s = 0; s < S; ++s) {
         StageArgs<T> a = stage_args<T>(c, s);
         c->launches += enqueue_full<T>(c, a, c->stream, c->prof != 0);
         if ((st = launch_check(c, "stage kernels")) != HCC_OK) return st;
-        if (!a.check) continue;
+        if (!a.check) {
+            if (mv && s + 1 < S &&
+                (st = apply_positions(c, c->Xs[s + 1], c->mover.full_search_per_stage != 0)) != HCC_OK)
+                return st;
+            continue;
+        }
         for (;;) {
             c->launches += enqueue_drop(c, a.Ynext, c->stream, nullptr);
             if ((st = c->cuda(cudaMemcpyAsync(c->h_lcounts, c->lcounts, sizeof(ListCounts), cudaMemcpyDeviceToHost,
@@ -626,6 +678,12 @@ template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
         }
         launch_count_inadmissible(c->inadm, c->bnd, n, &c->mood_stats->inadmissible, c->stream);
         c->launches += 1;
+        if (mv && s + 1 < S && (st = apply_positions(c, c->Xs[s + 1], c->mover.full_search_per_stage != 0)) != HCC_OK)
+            return st;
+    }
+    if (mv) {
+        // final positions; full search with periodic re-wrap for the next step (TimeSteppers.jl:571-575)
+        if ((st = apply_positions(c, c->x_cand, true)) != HCC_OK) return st;
     }
     if ((st = read_mood_stats(c, c->stream)) != HCC_OK) return st;
     st = c->sync("step");
@@ -739,7 +797,7 @@ template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
 }
 
 template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
-    if (c->use_graphs && !c->prof) {
+    if (c->use_graphs && !c->prof && !c->moving()) {
         hcc_status st = run_step_graph<T>(c, dt);
         if (st != HCC_ERR_CUDA || c->graphs_failed) return st;
         // a graph that cannot be captured or launched on this driver: the host-driven step for this context
@@ -1128,6 +1186,33 @@ hcc_status hcc_build_neighbours(hcc_ctx *c) {
     return HCC_OK;
 }
 
+hcc_status hcc_set_mover(hcc_ctx *c, const hcc_mover *mv) {
+    if (!c || !mv) return c ? c->fail(HCC_ERR_INVALID, "null mover") : HCC_ERR_INVALID;
+    if (mv->kind < HCC_MOVER_NONE || mv->kind > HCC_MOVER_PRESCRIBED) return c->fail(HCC_ERR_INVALID, "unknown mover");
+    const bool fluid = c->cfg.pde == HCC_PDE_EULER || (c->cfg.pde == HCC_PDE_ADVECTION && c->M == 1);
+    if ((mv->kind == HCC_MOVER_LAGRANGIAN || mv->kind == HCC_MOVER_SCALED) && !fluid)
+        return c->fail(HCC_ERR_UNSUPPORTED, "this system defines no fluid velocity (Lagrangian movers)");
+    if (mv->kind != HCC_MOVER_NONE && c->weno) return c->fail(HCC_ERR_UNSUPPORTED, "moving grids with WENO");
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->drop_graphs();
+    c->mover = *mv;
+    c->free_mover_buffers();
+    return HCC_OK;
+}
+
+hcc_status hcc_download_positions(hcc_ctx *c, double *pos) {
+    if (!c || !pos) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud");
+    const int D = c->D;
+    std::vector<double> soa(size_t(D) * c->npad);
+    hcc_status st;
+    HCC_TRY(c->sync("positions"));
+    HCC_TRY(c->cuda(cudaMemcpy(soa.data(), c->pos, soa.size() * sizeof(double), cudaMemcpyDeviceToHost), "positions"));
+    for (int64_t i = 0; i < c->n; ++i)
+        for (int d = 0; d < D; ++d) pos[i * D + d] = soa[size_t(d) * c->npad + i];
+    return HCC_OK;
+}
+
 hcc_status hcc_download_neighbours(hcc_ctx *c, int32_t *counts, int32_t *idx, double *w, double *dist) {
     if (!c) return HCC_ERR_INVALID;
     if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
@@ -1406,3 +1491,37 @@ hcc_status hcc_synchronize(hcc_ctx *c) {
 void *hcc_stream(hcc_ctx *c) { return c ? static_cast<void *>(c->stream) : nullptr; }
 
 }  // extern "C"
+
+namespace {
+
+// _apply_stage_geometry! / set_positions! (TimeSteppers.jl:521-525, GridMovers.jl:123-133): the positions src
+// become the grid's, then a full search (with periodic re-wrap) or the refresh of the existing slots, then the
+// geometry caches (MLS inverses, divergence and gradient weights, donor map) at the new positions.
+hcc_status apply_positions(hcc_ctx *c, const double *src, bool full_search) {
+    hcc_status st;
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->pos, src, size_t(c->npad) * c->D * sizeof(double), cudaMemcpyDeviceToDevice,
+                                    c->stream), "stage positions"));
+    if (full_search) {
+        HCC_TRY(hcc_build_neighbours(c));
+    } else {
+        const hcc_config &f = c->cfg;
+        SearchArgs a{};
+        a.n = c->n; a.npad = c->npad; a.D = c->D; a.pos = c->pos;
+        for (int d = 0; d < 3; ++d) {
+            const bool per = d < c->D && f.periodic[d];
+            const double L = f.domain_max[d] - f.domain_min[d];
+            a.periodic[d] = per ? 1 : 0;
+            a.Lwrap[d] = per ? L : 0.0;
+            a.invLwrap[d] = per ? 1.0 / L : 0.0;
+        }
+        a.cnt = c->cnt; a.nidx = c->nidx; a.w = c->w64; a.dist = c->dist64; a.kmax = c->kmax;
+        a.R_sq = f.radius * f.radius;
+        a.alpha = f.weight_alpha;
+        a.invR2 = 1.0 / (f.radius * f.radius);
+        HCC_TRY(search_refresh(a, c->stream, c->err));
+        c->launches += 1;
+    }
+    return hcc_prepare_geometry(c);
+}
+
+}  // namespace

@@ -186,6 +186,7 @@ template <typename T> struct Geometry {
 // graph serves every dt: hE[j] = dt a_t (0 = skipped), hI[j] = dt a (0 = skipped), h_sub = dt / C of the Euler
 // substep, dt_ii = dt a_ii and its inverse for the implicit part.
 template <typename T> struct StageCoeffs {
+    double hEd[HCC_MAX_STAGES];       // dt a_t in FP64: the stage positions of a moving grid
     T hE[HCC_MAX_STAGES];
     T hI[HCC_MAX_STAGES];
     T h_sub;
@@ -231,6 +232,16 @@ template <typename T> struct StageArgs {
     T u2_plateau, u2_ratio, u2_h;     // MOODu2: plateau and curvature-ratio parameters, h = min(dx)
     const unsigned long long *u2_range;   // MOODu2 global range of the stage state (ordered keys: lo[M], hi[M],
                                           // NaN bits), nullptr when the plateau test is off
+    // moving grid (GridMovers.jl): mover kind and parameters, the current positions (SoA FP64), this stage's grid
+    // velocities (out), the start-of-step positions, the grid velocities of earlier stages and the next positions
+    int mover;
+    T mv_alpha;
+    double mv_v[3], mv_om[3], mv_c[3];
+    const double *pos;
+    double *KXout;
+    const double *x_n;
+    const double *KX[HCC_MAX_STAGES];
+    double *Xnext;
     uint32_t *tmask;                  // MOOD check: failed candidates (a ballot word per tile) ...
     int32_t *ttiles;                  // ... the tiles with a failure ...
     unsigned *tcount;                 // ... and their count
@@ -306,6 +317,7 @@ struct SearchArgs {
 hcc_status search_bins(SearchArgs &a, cudaStream_t s, std::string &err);
 hcc_status search_count(SearchArgs &a, cudaStream_t s, unsigned long long *d_stats, std::string &err);
 hcc_status search_write(SearchArgs &a, cudaStream_t s, std::string &err);
+hcc_status search_refresh(SearchArgs &a, cudaStream_t s, std::string &err);
 
 struct MlsArgs {
     int64_t n, npad;

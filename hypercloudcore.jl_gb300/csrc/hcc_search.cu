@@ -184,6 +184,23 @@ __global__ void k_write(SearchArgs a) {
     }
 }
 
+// refresh_geometry! (GridMovers.jl:95-121): distances and weights of the existing slots at the current positions
+// (start-of-step topology), weight 0 for pairs that drifted beyond R
+template <int D>
+__global__ void k_refresh(SearchArgs a) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int c = a.cnt[i];
+    double dist[3];
+    for (int k = 0; k < c; ++k) {
+        const int64_t slot = int64_t(k) * a.npad + i;
+        const double d2 = pair_distance<D>(a, i, a.nidx[slot], dist);
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.dist[(int64_t(k) * D + d) * a.npad + i] = dist[d];
+        a.w[slot] = d2 <= a.R_sq ? exp_weight(d2, a.alpha, a.invR2) : 0.0;
+    }
+}
+
 inline unsigned grid_for(int64_t n) { return unsigned((n + HCC_BLOCK - 1) / HCC_BLOCK); }
 
 hcc_status check_launch(std::string &err, const char *what) {
@@ -217,6 +234,16 @@ hcc_status search_count(SearchArgs &a, cudaStream_t s, unsigned long long *d_sta
     default: k_count<3><<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a, d_stats); break;
     }
     return check_launch(err, "neighbour search (count)");
+}
+
+hcc_status search_refresh(SearchArgs &a, cudaStream_t s, std::string &err) {
+    if (a.n == 0) return HCC_OK;
+    switch (a.D) {
+    case 1: k_refresh<1><<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a); break;
+    case 2: k_refresh<2><<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a); break;
+    default: k_refresh<3><<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a); break;
+    }
+    return check_launch(err, "geometry refresh");
 }
 
 hcc_status search_write(SearchArgs &a, cudaStream_t s, std::string &err) {

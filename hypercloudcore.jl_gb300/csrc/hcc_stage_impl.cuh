@@ -170,8 +170,12 @@ __device__ __forceinline__ void euler_prim(const PhysParams<T> &ph, const T *U, 
 }
 
 // flux(eq, U) (API.jl:23) for the compiled-in modules; lam[d] = max_eigenvalue(eq, U, d) (API.jl:38).
+// On a moving grid (w != nullptr) the flux and speeds of ALEFrame(eq, w) (GridMovers.jl:77-83): F_d - w_d U and
+// max_eigenvalue(eq, U, d, w_d) (API.jl:51-58): |u_d - w_d| + c (Euler), |c_d - w_d| (scalar advection,
+// test/PDEs/linear_advection.jl:35), else max_eigenvalue + |w_d|.
 template <typename T, int D, int M, int PDE>
-__device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T *U, T (*F)[M], T *lam) {
+__device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T *U, T (*F)[M], T *lam,
+                                               const T *w = nullptr) {
     if constexpr (PDE == HCC_PDE_EULER) {
         T inv_rho, u[D], p;
         euler_prim<T, D>(ph, U, inv_rho, u, p);
@@ -185,15 +189,50 @@ __device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T 
                 F[d][1 + e] = (e == d) ? v + p : v;
             }
             F[d][D + 1] = (U[D + 1] + p) * u[d];
-            lam[d] = fabs(u[d]) + c;
+            lam[d] = fabs(w ? u[d] - w[d] : u[d]) + c;
         }
     } else {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
 #pragma unroll
             for (int m = 0; m < M; ++m) F[d][m] = ph.c[d][m] * U[m];
-            lam[d] = ph.amax[d];
+            lam[d] = !w ? ph.amax[d]
+                        : ((PDE == HCC_PDE_ADVECTION && M == 1) ? fabs(ph.c[d][0] - w[d]) : ph.amax[d] + fabs(w[d]));
         }
+    }
+    if (w) {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int m = 0; m < M; ++m) F[d][m] = F[d][m] - w[d] * U[m];
+    }
+}
+
+// grid_velocity (GridMovers.jl:60-63) of particle i: fluid velocity (Euler m_d / rho, scalar advection c_d), scaled,
+// or the prescribed field velocity + omega x (x - center) at its current position
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void grid_velocity(const StageArgs<T> &a, int64_t i, const T *U, T *w) {
+    if (a.mover == HCC_MOVER_PRESCRIBED) {
+        double r[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) r[d] = a.pos[int64_t(d) * a.g.npad + i] - a.mv_c[d];
+        if constexpr (D == 1) {
+            w[0] = T(a.mv_v[0]);
+        } else if constexpr (D == 2) {
+            w[0] = T(a.mv_v[0] - a.mv_om[2] * r[1]);
+            w[1] = T(a.mv_v[1] + a.mv_om[2] * r[0]);
+        } else {
+            w[0] = T(a.mv_v[0] + (a.mv_om[1] * r[2] - a.mv_om[2] * r[1]));
+            w[1] = T(a.mv_v[1] + (a.mv_om[2] * r[0] - a.mv_om[0] * r[2]));
+            w[2] = T(a.mv_v[2] + (a.mv_om[0] * r[1] - a.mv_om[1] * r[0]));
+        }
+        return;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        if constexpr (PDE == HCC_PDE_EULER) w[d] = U[1 + d] / U[0];
+        else w[d] = a.ph.c[d][0];
+        if (a.mover == HCC_MOVER_SCALED) w[d] = a.mv_alpha * w[d];
     }
 }
 
@@ -647,6 +686,22 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i,
         store_vec<T, M>(a.KInext + i * M, KIo);
     }
     store_vec<T, M>(a.Ynext + i * M, Y);
+    if (a.Xnext) {
+        // moving grid: the next stage positions X = x_n + Σ_j dt ã_j K_X[j] (_stage_predictor!, :403-421)
+        const int64_t np = a.g.npad;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            double X = a.x_n[int64_t(d) * np + i];
+            for (int j = 0; j < a.n_prev; ++j) {
+                const double h = cf->hEd[j];
+                if (h != 0.0) {
+                    const double kx = (j == a.self_slot) ? a.KXout[int64_t(d) * np + i] : a.KX[j][int64_t(d) * np + i];
+                    X = X + h * kx;
+                }
+            }
+            a.Xnext[int64_t(d) * np + i] = X;
+        }
+    }
     if (!a.check) return false;
     T cand[M];
     if (a.check_substep) {
@@ -732,13 +787,16 @@ template <typename T, int D, int M> constexpr int flux_min_blocks() {
 // contraction with the divergence weights; K_E = -2 Σ c·ΔF (TimeSteppers.jl:354). Fused epilogue: the next
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
-template <typename T, int D, int M, int PDE, int RDEG>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
 __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i) {
     constexpr int BR = RBasis<D, RDEG>::B;
     if (a.g.bnd[i]) {
         if (a.full) {
 #pragma unroll
             for (int m = 0; m < M; ++m) a.K[i * M + m] = T(0);
+            if (a.mover)
+#pragma unroll
+                for (int d = 0; d < D; ++d) a.KXout[int64_t(d) * a.g.npad + i] = 0.0;
         }
         return false;
     }
@@ -749,7 +807,16 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     T fi[M], gi[BR][M], Fi[D][M], lami[D];
     load_vec<T, M>(a.U + i * M, fi);
     load_vec<T, BR * M>(a.grad + i * (BR * M), &gi[0][0]);
-    flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami);
+    // moving grid: this particle's grid velocity (K_X of the stage) and every flux in its frame
+    T wv[D];
+    const T *wp = nullptr;
+    if constexpr (ALE) {
+        grid_velocity<T, D, M, PDE>(a, i, fi, wv);
+        wp = wv;
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.KXout[int64_t(d) * a.g.npad + i] = double(wv[d]);
+    }
+    flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami, wp);
     constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form (below)
     if constexpr (kFast) {
 #pragma unroll
@@ -859,8 +926,8 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
                 fji[m] = fj[m] + sj;
             }
             T Fij[D][M], Fji[D][M], lij[D], lji[D];
-            flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij);
-            flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji);
+            flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij, wp);
+            flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji, wp);
             T t[M];
             if constexpr (kFast) {
                 // FP32: 2 (F_n - F_i) = (F_ij + F_ji) - s_d max(λ) (f_ji - f_ij) - 2 F_i with s_d = sign of the
@@ -932,12 +999,12 @@ template <typename T> __device__ __forceinline__ void tile_failures(const StageA
 
 // A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word;
 // the reach marks are cleared once read). Either way each warp reports the failed candidates of its tile.
-template <typename T, int D, int M, int PDE, int RDEG>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
 __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_flux(const StageArgs<T> a) {
     const int lane = int(threadIdx.x & 31);
     if (a.full) {
         const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG>(a, i) : false;
+        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG, ALE>(a, i) : false;
         if (a.check) tile_failures(a, i >> 5, f);
         return;
     }
@@ -947,7 +1014,7 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
         const int32_t tile = a.wtiles[q];
         const uint32_t word = a.wmask[tile];
         const int64_t i = int64_t(tile) * 32 + lane;
-        const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG>(a, i) : false;
+        const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG, ALE>(a, i) : false;
         if (a.check) tile_failures(a, tile, f);
         if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
     }
@@ -1204,7 +1271,10 @@ struct StageInst {
     }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
-        k_flux<T, D, M, PDE, RDEG><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+        if (a.mover)     // moving grid: the ALE-frame instantiation (grid velocities, shifted fluxes and speeds)
+            k_flux<T, D, M, PDE, RDEG, true><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+        else
+            k_flux<T, D, M, PDE, RDEG, false><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
     }
     static void stage1(const void *args, int64_t n, cudaStream_t s) {
         k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));

@@ -205,6 +205,33 @@ hcc_status hcc_time_step(hcc_ctx *ctx, double *dt_out);
    compute_explicit_rhs!(..., full = true) (TimeSteppers.jl:312-356). K: N*M. */
 hcc_status hcc_compute_rhs(hcc_ctx *ctx, double *K);
 
+/* Grid movers (GridMovers.jl): positions become stage variables of the tableau (explicit part), the flux is taken in
+   the frame of each particle's grid velocity w (ALEFrame: F - w U, wave speeds shifted), distances, weights and MLS
+   caches are refreshed at every stage position with the start-of-step topology (or a full search per stage), and a
+   full neighbour search (with periodic re-wrap) follows every step. No counterpart for PrescribedMover's arbitrary
+   Julia function: the prescribed field here is w(x) = velocity + omega x (x - center). */
+typedef enum {
+    HCC_MOVER_NONE = 0,        /* NoGridMover */
+    HCC_MOVER_LAGRANGIAN = 1,  /* LagrangianMover: w = fluid_velocity(eq, U) (scalar advection, Euler) */
+    HCC_MOVER_SCALED = 2,      /* ScaledLagrangianMover(alpha): w = alpha fluid_velocity(eq, U) */
+    HCC_MOVER_PRESCRIBED = 3   /* PrescribedMover: w = velocity + omega x (x - center) (2-D: omega[2] about z) */
+} hcc_mover_kind;
+
+typedef struct {
+    int32_t kind;                      /* hcc_mover_kind */
+    int32_t full_search_per_stage;     /* 1: rebuild the neighbour topology at every stage position */
+    double alpha;                      /* ScaledLagrangianMover */
+    double velocity[HCC_MAX_DIM];      /* prescribed translation */
+    double omega[HCC_MAX_DIM];         /* prescribed angular velocity */
+    double center[HCC_MAX_DIM];        /* centre of the prescribed rotation */
+} hcc_mover;
+
+/* Select the grid mover of the context (default HCC_MOVER_NONE); before hcc_step. */
+hcc_status hcc_set_mover(hcc_ctx *ctx, const hcc_mover *mover);
+
+/* Current particle positions (N x D row-major, the caller's numbering; moved by hcc_step on moving grids). */
+hcc_status hcc_download_positions(hcc_ctx *ctx, double *pos);
+
 /* One time step: (ts::GeneralRKTimeStepper)(eq, pg, t, dt) (TimeSteppers.jl:531-577). */
 hcc_status hcc_step(hcc_ctx *ctx, double t, double dt);
 

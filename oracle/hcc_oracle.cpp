@@ -449,6 +449,29 @@ struct Physics {
         }
         return amax[d];
     }
+    // fluid_velocity (API.jl:104-109): scalar advection c_d (test/PDEs/linear_advection.jl:41-43); Euler m_d / rho
+    // (a module of this implementation); no other system defines one.
+    bool has_fluid_velocity() const { return kind == HCC_PDE_EULER || (kind == HCC_PDE_ADVECTION && M == 1); }
+    void fluid_velocity(const double *U, double *w) const {
+        for (int d = 0; d < D; ++d) w[d] = (kind == HCC_PDE_EULER) ? U[1 + d] / U[0] : c[d][0];
+    }
+    // max_eigenvalue(eq, U, d, shift) (API.jl:51-58): scalar advection |c_d - w_d| (linear_advection.jl:35), Euler
+    // |u_d - w_d| + c, otherwise the default max_eigenvalue + |w_d|.
+    double lam_shift(const double *U, int d, double w) const {
+        if (kind == HCC_PDE_EULER) {
+            double inv_rho, u[3], p;
+            euler_prim(U, inv_rho, u, p);
+            return std::fabs(u[d] - w) + std::sqrt(gamma * p * inv_rho);
+        }
+        if (kind == HCC_PDE_ADVECTION && M == 1) return std::fabs(c[d][0] - w);
+        return amax[d] + std::fabs(w);
+    }
+    // flux(ALEFrame(eq, w), U) (GridMovers.jl:77-81): F_d - w_d U
+    void flux_ale(const double *U, const double *w, double *F) const {
+        flux(U, F);
+        for (int d = 0; d < D; ++d)
+            for (int m = 0; m < M; ++m) F[d * M + m] = F[d * M + m] - w[d] * U[m];
+    }
     // is_admissible (API.jl:48): finite; Euler additionally rho > 0 and p > 0.
     bool admissible(const double *U) const {
         for (int m = 0; m < M; ++m) if (!std::isfinite(U[m])) return false;
@@ -520,6 +543,10 @@ struct Solver {
     double invL = 1.0;
     bool streamed = true;
     bool aligned = false;            // AlignedRusanovFlux
+    // moving grid (GridMovers.jl): mover kind, its parameters, positions as stage variables
+    hcc_mover mover{};
+    std::vector<double> x_n, x_cand, Xst[5], KX[5];
+    bool moving() const { return mover.kind != HCC_MOVER_NONE; }
     bool have_geom = false;
     std::vector<double> inv_r, inv_d, dw;
     std::vector<uint8_t> ok_r, ok_d;
@@ -921,7 +948,16 @@ struct Solver {
         const double *fi = &U[i * M];
         const double *gi = &grads[i * Br * M];
         double Fi[3 * HCC_MAX_VARS];
-        phys.flux(fi, Fi);
+        // moving grid: the flux of particle i in the frame of its grid velocity (ALEFrame(eq, w_i))
+        const bool ale = moving();
+        double wv[3] = {0.0, 0.0, 0.0};
+        if (ale) {
+            grid_velocity(i, fi, wv);
+            for (int d = 0; d < D; ++d) (*KX_cur)[i * D + d] = wv[d];
+            phys.flux_ale(fi, wv, Fi);
+        } else {
+            phys.flux(fi, Fi);
+        }
 
         // dynamic fit data (streamed dynamic: MUSCL.jl:514-538; buffered: Interpolators.jl:308-334)
         int qdyn = didx - 1;
@@ -974,8 +1010,13 @@ struct Solver {
                 fij[m] = fi[m] + si;
                 fji[m] = fj[m] + sj;
             }
-            phys.flux(fij, Fij);
-            phys.flux(fji, Fji);
+            if (ale) {
+                phys.flux_ale(fij, wv, Fij);
+                phys.flux_ale(fji, wv, Fji);
+            } else {
+                phys.flux(fij, Fij);
+                phys.flux(fji, Fji);
+            }
             // the slot's divergence weights c_ij (_slot_weight, MUSCL.jl:429-445): the cached fit, or the dynamic
             // fit solved per slot; the streamed contraction and the aligned orientation use them
             double wk[3] = {0.0, 0.0, 0.0};
@@ -1004,7 +1045,8 @@ struct Solver {
                 const double *fR = pos_ ? fji : fij;
                 const double *FL = pos_ ? &Fij[d * M] : &Fji[d * M];
                 const double *FR = pos_ ? &Fji[d * M] : &Fij[d * M];
-                double sdd = jmax(phys.lam(fL, d), phys.lam(fR, d));
+                double sdd = ale ? jmax(phys.lam_shift(fL, d, wv[d]), phys.lam_shift(fR, d, wv[d]))
+                                 : jmax(phys.lam(fL, d), phys.lam(fR, d));
                 for (int m = 0; m < M; ++m) {
                     double Fn = 0.5 * ((FL[m] + FR[m]) - sdd * (fR[m] - fL[m]));
                     dF[d * M + m] = Fn - Fi[d * M + m];
@@ -1197,7 +1239,48 @@ struct Solver {
         return sum_c;
     }
 
-    // compute_explicit_rhs! (TimeSteppers.jl:312-356)
+    // grid_velocity (GridMovers.jl:60-63) of particle p at its current (stage) position
+    void grid_velocity(int64_t p, const double *U, double *w) const {
+        double r[3] = {0.0, 0.0, 0.0};
+        switch (mover.kind) {
+        case HCC_MOVER_LAGRANGIAN: phys.fluid_velocity(U, w); break;
+        case HCC_MOVER_SCALED:
+            phys.fluid_velocity(U, w);
+            for (int d = 0; d < D; ++d) w[d] = mover.alpha * w[d];
+            break;
+        case HCC_MOVER_PRESCRIBED:
+            for (int d = 0; d < D; ++d) r[d] = pos[p * D + d] - mover.center[d];
+            if (D == 1) {
+                w[0] = mover.velocity[0];
+            } else if (D == 2) {
+                w[0] = mover.velocity[0] - mover.omega[2] * r[1];
+                w[1] = mover.velocity[1] + mover.omega[2] * r[0];
+            } else {
+                w[0] = mover.velocity[0] + (mover.omega[1] * r[2] - mover.omega[2] * r[1]);
+                w[1] = mover.velocity[1] + (mover.omega[2] * r[0] - mover.omega[0] * r[2]);
+                w[2] = mover.velocity[2] + (mover.omega[0] * r[1] - mover.omega[1] * r[0]);
+            }
+            break;
+        default: for (int d = 0; d < D; ++d) w[d] = 0.0;
+        }
+    }
+
+    // refresh_geometry! (GridMovers.jl:95-121): distances and weights of the existing slots at the current positions,
+    // weight 0 beyond R
+    void refresh_geometry() {
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < N; ++i)
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                double dist[3];
+                distance(i, nidx[s], dist);
+                for (int d = 0; d < D; ++d) ndist[s * D + d] = dist[d];
+                double d2 = sumsq(dist);
+                nw[s] = d2 <= R_sq ? weight(d2) : 0.0;
+            }
+    }
+
+    // compute_explicit_rhs! (TimeSteppers.jl:312-356); on a moving grid K_X = w and the flux in the ALE frame
+    std::vector<double> *KX_cur = nullptr;
     void compute_rhs(std::vector<double> &K, const double *Ystate, bool full) {
         if (weno) {
 #pragma omp parallel for schedule(dynamic, 256)
@@ -1216,7 +1299,10 @@ struct Solver {
 #pragma omp parallel for schedule(dynamic, 256)
         for (int64_t p = 0; p < N; ++p) {
             if (bnd[p]) {
-                if (full) for (int m = 0; m < M; ++m) K[p * M + m] = 0.0;
+                if (full) {
+                    for (int m = 0; m < M; ++m) K[p * M + m] = 0.0;
+                    if (moving()) for (int d = 0; d < D; ++d) (*KX_cur)[p * D + d] = 0.0;
+                }
                 continue;
             }
             if (!(full || dirty[p])) continue;
@@ -1272,16 +1358,25 @@ struct Solver {
         bool fin = i > s;
         std::vector<double> &target = fin ? rho_cand : Y[i - 1];
         int n_prev = fin ? s : i - 1;
+        const bool mv = moving();
+        std::vector<double> *xt = mv ? (fin ? &x_cand : &Xst[i - 1]) : nullptr;
         for (int64_t p = 0; p < N; ++p) {
             double *Yp = &target[p * M];
-            if (bnd[p]) { for (int m = 0; m < M; ++m) Yp[m] = rhos[p * M + m]; continue; }
+            if (bnd[p]) {
+                for (int m = 0; m < M; ++m) Yp[m] = rhos[p * M + m];
+                if (mv) for (int d = 0; d < D; ++d) (*xt)[p * D + d] = x_n[p * D + d];
+                continue;
+            }
             for (int m = 0; m < M; ++m) Yp[m] = rho_n[p * M + m];
+            double *Xp = mv ? &(*xt)[p * D] : nullptr;
+            if (mv) for (int d = 0; d < D; ++d) Xp[d] = x_n[p * D + d];
             for (int j = 1; j <= n_prev; ++j) {
                 double a_t = fin ? tab.bt[j - 1] : tab.at[i - 1][j - 1];
                 double a = fin ? tab.b[j - 1] : tab.a[i - 1][j - 1];
                 if (a_t != 0.0) {
                     double h = dt * a_t;
                     for (int m = 0; m < M; ++m) Yp[m] = Yp[m] + h * KE[j - 1][p * M + m];
+                    if (mv) for (int d = 0; d < D; ++d) Xp[d] = Xp[d] + h * KX[j - 1][p * D + d];
                 }
                 if (a != 0.0 && phys.has_implicit_source()) {
                     double h = dt * a;
@@ -1494,13 +1589,35 @@ struct Solver {
         std::fill(trig_step.begin(), trig_step.end(), 0);
         inadmissible = 0; mood_iters = 0;
         const int s = tab.s;
+        const bool mv = moving();
+        if (mv) {
+            x_n = pos;
+            x_cand.assign(N * D, 0.0);
+            for (int q = 0; q < s; ++q) { Xst[q].assign(N * D, 0.0); KX[q].assign(N * D, 0.0); }
+        }
         for (int i = 1; i <= s; ++i) {
-            if (i == 1) form_candidate(1, dt);
-            else if (!mood_checkpoint(i, dt)) return false;
+            if (i == 1) {
+                form_candidate(1, dt);                     // X_1 == x_n: the grid is already there
+            } else {
+                if (!mood_checkpoint(i, dt)) return false; // geometry of stage i - 1
+                if (mv) {
+                    // _apply_stage_geometry! (TimeSteppers.jl:521-525): stage positions, then the geometry caches
+                    pos = Xst[i - 1];
+                    if (mover.full_search_per_stage) { if (!build_neighbours()) return false; }
+                    else refresh_geometry();
+                    if (!prepare_geometry()) return false;
+                }
+            }
+            KX_cur = mv ? &KX[i - 1] : nullptr;
             compute_rhs(KE[i - 1], Y[i - 1].data(), true);
         }
-        if (!mood_checkpoint(s + 1, dt)) return false;
+        if (!mood_checkpoint(s + 1, dt)) return false;     // geometry of stage s
         rhos = rho_cand;
+        if (mv) {
+            // final positions, full search with periodic re-wrap for the next step (TimeSteppers.jl:571-575)
+            pos = x_cand;
+            if (!build_neighbours() || !prepare_geometry()) return false;
+        }
         ++steps;
         return true;
     }
@@ -1834,6 +1951,17 @@ hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *c
     if (changed_any) *changed_any = any ? 1 : 0;
     return HCC_OK;
 }
+hcc_status orc_set_mover(orc_ctx *ctx, const hcc_mover *mv) {
+    if (!ctx || !mv) return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    if (mv->kind < HCC_MOVER_NONE || mv->kind > HCC_MOVER_PRESCRIBED) return HCC_ERR_INVALID;
+    if ((mv->kind == HCC_MOVER_LAGRANGIAN || mv->kind == HCC_MOVER_SCALED) && !s.phys.has_fluid_velocity())
+        return HCC_ERR_UNSUPPORTED;
+    if (mv->kind != HCC_MOVER_NONE && s.weno) return HCC_ERR_UNSUPPORTED;
+    s.mover = *mv;
+    return HCC_OK;
+}
+
 // The MOOD criterion of particle p for hand-set stage states (N x M), reconstruction gradients (N x Br x M, the
 // layout of orc_download_gradients), orders and a candidate state (M): the known-answer tests of MOODu2.
 hcc_status orc_criterion_flags(orc_ctx *ctx, int64_t p, const double *prev, const double *grads, const int32_t *orders,

@@ -81,6 +81,8 @@ hcc_status orc_interface_orders(orc_ctx *ctx, int64_t i, int64_t j, int32_t *oi,
 /* detect_and_drop! (MOOD.jl:375-405) against explicit prev/cand states; dirty may be NULL (full). */
 hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *cand, int32_t full,
                                const uint8_t *dirty, int32_t with_eq, int32_t *changed_any);
+/* Grid mover of the context (GridMovers.jl). */
+hcc_status orc_set_mover(orc_ctx *ctx, const hcc_mover *mover);
 /* The MOOD criterion of particle p (MOOD.jl:175-271) for hand-set stage states (N*M), gradients (N*Br*M), orders
    and a candidate (M): *flag = 1 if flagged. */
 hcc_status orc_criterion_flags(orc_ctx *ctx, int64_t p, const double *prev, const double *grads, const int32_t *orders,

@@ -76,6 +76,7 @@ def load(abi) -> C.CDLL:
         ("orc_detect_and_drop", C.c_int, [P, dp, dp, C.c_int32, up, C.c_int32, ip]),
         ("orc_apply_bcs", C.c_int, [P, dp]),
         ("orc_criterion_flags", C.c_int, [P, C.c_int64, dp, dp, ip, dp, ip]),
+        ("orc_set_mover", C.c_int, [P, C.POINTER(abi.HccMover)]),
     ]
     for name, res, args in protos:
         fn = getattr(lib, name)
@@ -255,6 +256,10 @@ class OracleContext:
         self._check(self.lib.orc_detect_and_drop(self._h, _p(p, C.c_double), _p(c, C.c_double), int(bool(full)), dptr,
                                                  int(bool(with_eq)), C.byref(ch)), "orc_detect_and_drop")
         return bool(ch.value)
+
+    def set_mover(self, mover):
+        """mover: an HccMover (see hcc_gb300.mover())."""
+        self._check(self.lib.orc_set_mover(self._h, C.byref(mover)), "orc_set_mover")
 
     def criterion_flags(self, p, prev, grads, orders, cand) -> bool:
         """The MOOD criterion of particle p for hand-set states, gradients (N x Br x M), orders and candidate."""
