@@ -73,6 +73,24 @@ _criterion(::MOODPAD) = (Int32(2), 0.0)
 _criterion(::OnlyMOOD) = (Int32(3), 0.0)
 _criterion(::NoMOOD) = (Int32(0), 0.0)
 
+# pg.mover (GridMovers.jl:28-63) -> hcc_set_mover; PrescribedMover takes a rigid motion (velocity, omega, center)
+struct HccMover
+    kind::Int32; full_search_per_stage::Int32; alpha::Float64
+    velocity::NTuple{3, Float64}; omega::NTuple{3, Float64}; center::NTuple{3, Float64}
+end
+struct RigidMotion
+    velocity::NTuple{3, Float64}; omega::NTuple{3, Float64}; center::NTuple{3, Float64}
+end
+function _set_mover(h, mv; full_search_per_stage::Bool = false)
+    z = (0.0, 0.0, 0.0)
+    m = mv isa LagrangianMover ? HccMover(1, full_search_per_stage, 1.0, z, z, z) :
+        mv isa ScaledLagrangianMover ? HccMover(2, full_search_per_stage, Float64(mv.alpha), z, z, z) :
+        mv isa PrescribedMover && mv.velocity isa RigidMotion ?
+            HccMover(3, full_search_per_stage, 1.0, mv.velocity.velocity, mv.velocity.omega, mv.velocity.center) :
+        mv isa NoGridMover ? HccMover(0, 0, 1.0, z, z, z) : error("unsupported mover $(typeof(mv))")
+    _check(ccall((:hcc_set_mover, libhcc), Cint, (Ptr{Cvoid}, Ref{HccMover}), h, m), h, "hcc_set_mover")
+end
+
 function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T}, interp::MUSCL, mood::MOOD,
                             tableau_id::Integer; bc_map = Dict{Int, Int32}(), precision::Symbol = :fp64) where {D, M, T}
     cfg = HccConfig()
@@ -105,6 +123,7 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
                  h[], N, pos, bnd, tags, vol), h[], "hcc_upload_cloud")
     _check(ccall((:hcc_build_neighbours, libhcc), Cint, (Ptr{Cvoid},), h[]), h[], "hcc_build_neighbours")
     _check(ccall((:hcc_prepare_geometry, libhcc), Cint, (Ptr{Cvoid},), h[]), h[], "hcc_prepare_geometry")
+    _set_mover(h[], pg.mover)
     ts = GB300RKTimeStepper{D, M}(h[], N)
     finalizer(t -> ccall((:hcc_destroy, libhcc), Cint, (Ptr{Cvoid},), t.handle), ts)
     return ts
