@@ -5,7 +5,7 @@ Host mirror of the reference's interface for this path (names and argument meani
   * physics modules   ``LinearAdvection`` (test/PDEs/linear_advection.jl), ``Euler`` (new), ``KineticRelaxation``
                       (test/kinetic_source.jl) — the ``HyperbolicPDE`` subtypes compiled into the kernels;
   * schemes           ``MUSCL(order, div_order)`` (src/Interpolation/MUSCL.jl:116), ``MOOD(strategy, criterion)``
-                      with ``MOODu1`` / ``MOODu2`` / ``MOODPAD`` / ``OnlyMOOD`` / ``NoMOOD`` and ``EPD0/EPD1/EPD2``
+                      with ``MOODu1`` / ``MOODu2`` / ``MOODPAD`` / ``OnlyMOOD`` / ``NoMOOD`` and ``EPD0/EPD1/EPD2/STRICT_EPD0``
                       (src/TimeStepping/MOOD.jl);
   * stepper           ``GB300RKTimeStepper`` — ``ts(t, dt)`` is ``(ts::GeneralRKTimeStepper)(eq, pg, t, dt)``
                       (src/TimeStepping/TimeSteppers.jl:531) and ``ts.get_time_step()`` is
@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import (HccConfig, HccCounters, FP32, FP64, PDE_ADVECTION, PDE_BGK, PDE_EULER, MOOD_NONE, MOOD_ONLY,
-                   MOOD_PAD, MOOD_U1, EPD_NONE, EPD0, EPD1, EPD2, TABLEAUS, BC_KEEP, BC_DIRICHLET, BC_OUTFLOW)
+                   MOOD_PAD, MOOD_U1, EPD_NONE, EPD0, EPD1, EPD2, STRICT_EPD0, TABLEAUS, BC_KEEP, BC_DIRICHLET, BC_OUTFLOW)
 from .cloud import Cloud, rectangular_cloud, morton_permutation, splitmix64_uniform
 
 PKG_DIR = Path(__file__).resolve().parent
@@ -451,7 +451,7 @@ class GB300RKTimeStepper:
 
 __all__ = [
     "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "mover", "MOOD", "MOODu1", "MOODu2",
-    "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "make_config", "Context",
+    "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "STRICT_EPD0", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",
 ]

@@ -22,7 +22,7 @@ FP64, FP32 = 0, 1
 MOOD_NONE, MOOD_U1, MOOD_PAD, MOOD_ONLY, MOOD_U2 = 0, 1, 2, 3, 4
 FLUXES = {"rusanov": 0, "aligned": 1}
 # hcc_mood_strategy
-EPD_NONE, EPD0, EPD1, EPD2 = 0, 1, 2, 3
+EPD_NONE, EPD0, EPD1, EPD2, STRICT_EPD0 = 0, 1, 2, 3, 4
 # hcc_tableau
 TABLEAUS = {
     "RK1_Euler": 0, "RK2_SSP": 1, "RK2_Ralston": 2, "RK3_SSP": 3, "RK4_Classical": 4, "RK4_SSP": 5,

@@ -199,8 +199,9 @@ struct hcc_ctx {
     int8_t *orders = nullptr, *nbmin = nullptr;
     uint8_t *trig_step = nullptr, *inadm = nullptr;
     // MOOD tile worklists (failed candidates, changed orders, their reach): tile lists and member words
-    int32_t *ttiles = nullptr, *ctiles = nullptr, *dtiles = nullptr;
-    uint32_t *tmask = nullptr, *cmask = nullptr, *dmask = nullptr, *words1 = nullptr;
+    int32_t *ttiles = nullptr, *ctiles = nullptr, *dtiles = nullptr, *ftiles = nullptr;
+    uint32_t *tmask = nullptr, *cmask = nullptr, *dmask = nullptr, *words1 = nullptr, *fmask = nullptr;
+    int32_t *forced = nullptr;                    // StrictEPD0 order offers (0x7f7f7f7f: none)
     ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
     int list_blocks = 1, drop_blocks = 1;
     unsigned long long *u2_keys = nullptr;       // MOODu2 global range of the stage state (ordered keys)
@@ -308,6 +309,7 @@ struct hcc_ctx {
             for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
         dfree(orders); dfree(nbmin); dfree(trig_step); dfree(inadm);
         dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
+        dfree(ftiles); dfree(fmask); dfree(forced);
     }
     void free_slots() {
         drop_graphs();
@@ -566,12 +568,18 @@ template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, c
     const int64_t n = c->n;
     const int hops = c->weno ? 0 : (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
     int k = 0;
+    if (c->cfg.mood_strategy == HCC_STRICT_EPD0) {
+        launch_force(c->ctiles, c->cmask, c->lcounts, c->ctiles, c->orders, c->bnd, c->cnt, c->nidx, c->npad, c->forced,
+                     c->fmask, c->ftiles, c->list_blocks, st);
+        k += 2;
+    }
     if (!c->weno) {
         StageArgs<T> ga = a;
         ga.full = 0;
         ga.wtiles = c->ctiles;
         ga.wcount = &c->lcounts->c;
         ga.wmask = c->cmask;
+        ga.clear_wmask = 1;
         ga.rmask = c->dmask;
         ga.rtiles = c->dtiles;
         ga.rcount = &c->lcounts->d;
@@ -592,7 +600,7 @@ template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, c
     fa.wtiles = hops > 0 ? c->dtiles : c->ctiles;
     fa.wcount = hops > 0 ? &c->lcounts->d : &c->lcounts->c;
     fa.wmask = hops > 0 ? c->dmask : c->cmask;
-    fa.clear_wmask = hops > 0;
+    fa.clear_wmask = 1;
     if (prof) c->prof_begin(2);
     (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, st);
     if (prof) c->prof_end();
@@ -906,8 +914,8 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if (f.precision != HCC_FP64 && f.precision != HCC_FP32) return c->fail(HCC_ERR_INVALID, "unknown precision");
     if (!(f.radius > 0.0)) return c->fail(HCC_ERR_INVALID, "radius must be positive");
     if (f.muscl_order < 1 || f.muscl_order > 3) return c->fail(HCC_ERR_UNSUPPORTED, "muscl_order must be 1, 2 or 3");
-    if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_EPD2) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
     if (f.mood_criterion < HCC_MOOD_NONE || f.mood_criterion > HCC_MOOD_U2) return c->fail(HCC_ERR_INVALID, "unknown MOOD criterion");
+    if (f.mood_strategy < HCC_EPD_NONE || f.mood_strategy > HCC_STRICT_EPD0) return c->fail(HCC_ERR_INVALID, "unknown MOOD strategy");
     if (f.flux < HCC_FLUX_RUSANOV || f.flux > HCC_FLUX_ALIGNED) return c->fail(HCC_ERR_INVALID, "unknown numerical flux");
     if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
     if (f.limiter < HCC_LIMITER_NONE || f.limiter > HCC_LIMITER_VK_HARD) return c->fail(HCC_ERR_INVALID, "unknown limiter");
@@ -1066,8 +1074,10 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
         cudaMemsetAsync(*p, 0, np, c->stream);
     }
     const int64_t ntiles = np / 32;
-    for (int32_t **p : {&c->ttiles, &c->ctiles, &c->dtiles}) HCC_TRY(c->alloc(*p, ntiles, "MOOD tile lists"));
-    for (uint32_t **p : {&c->tmask, &c->cmask, &c->dmask, &c->words1}) {
+    for (int32_t **p : {&c->ttiles, &c->ctiles, &c->dtiles, &c->ftiles}) HCC_TRY(c->alloc(*p, ntiles, "MOOD tile lists"));
+    HCC_TRY(c->alloc(c->forced, np, "StrictEPD0 offers"));
+    cudaMemsetAsync(c->forced, 0x7f, size_t(np) * sizeof(int32_t), c->stream);
+    for (uint32_t **p : {&c->tmask, &c->cmask, &c->dmask, &c->words1, &c->fmask}) {
         HCC_TRY(c->alloc(*p, ntiles, "MOOD tile words"));
         cudaMemsetAsync(*p, 0, size_t(ntiles) * sizeof(uint32_t), c->stream);
     }

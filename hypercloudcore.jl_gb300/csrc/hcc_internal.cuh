@@ -250,9 +250,10 @@ template <typename T> struct StageArgs {
 
 // Device-side tile worklists of the MOOD fixed point: t = tiles with failed candidates, c = tiles with a dropped
 // order (cn: the list being filled by the current decrement, published as c by the decision), d = the reach of the
-// changed orders (one or two hops), d1 = its one-hop part; done = blocks finished in the decrement launch.
+// changed orders (one or two hops), d1 = its one-hop part; done = blocks finished in the decrement launch; f = tiles
+// offered a lower order by StrictEPD0 forcing.
 struct ListCounts {
-    unsigned t, c, cn, d, d1, done, pad0, pad1;
+    unsigned t, c, cn, d, d1, done, f, pad1;
 };
 
 // Append v to a device list; warp-aggregated: one atomic per group of converged lanes.
@@ -375,6 +376,12 @@ __host__ __device__ __forceinline__ double order_value(unsigned long long k) {
     memcpy(&v, &b, sizeof(v));
     return v;
 }
+// StrictEPD0 forcing (forced_order(::Halo{1}), MOOD.jl:54-64; _mood_force!, :312-320): the particles dropped in the
+// last decrement (c tiles) offer their order to their interior neighbours, which take it where it is lower and join
+// the changed list. forced[] holds 0x7f7f7f7f between calls.
+void launch_force(const int32_t *ctiles, uint32_t *cmask, ListCounts *counts, int32_t *ctiles_out, int8_t *orders,
+                  const uint8_t *bnd, const int32_t *cnt, const int32_t *nidx, int64_t npad, int32_t *forced,
+                  uint32_t *fmask, int32_t *ftiles, int blocks, cudaStream_t s);
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s);
 // Gradient weights of the cached degree-1 fit (FP64 sums, FP32 store): gw[(k*D + b) * npad + i] =

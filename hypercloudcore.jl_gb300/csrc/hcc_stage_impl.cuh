@@ -588,7 +588,10 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
     const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     for (unsigned q = warp; q < nt; q += nwarps) {
         const int32_t tile = a.wtiles[q];
-        if (!((a.wmask[tile] >> lane) & 1u)) continue;
+        const uint32_t word = a.wmask[tile];
+        __syncwarp();
+        if (a.clear_wmask && lane == 0) a.wmask[tile] = 0u;     // the changed list is consumed here
+        if (!((word >> lane) & 1u)) continue;
         const int32_t i = tile * 32 + lane;
         gather_one<T, D, M, PDE, RDEG>(a, i);
         if (a.rmask) {

@@ -92,6 +92,7 @@ __global__ void k_drop_decide(const DropArgs a) {
     ct->cn = 0;
     ct->t = 0;
     ct->d = 0;
+    ct->f = 0;
     ct->done = 0;
     unsigned go = 0;
     if (changed == 0) {
@@ -109,6 +110,56 @@ __global__ void k_drop_decide(const DropArgs a) {
     }
     __threadfence();
     if (a.has_handle) cudaGraphSetConditional(a.h, go);
+}
+
+// StrictEPD0 forcing, push half: every member of a c tile (dropped in the last decrement) offers its order to its
+// interior neighbours (atomicMin), which are marked in the f tiles.
+__global__ void k_force_push(const int32_t *ctiles, const uint32_t *cmask, ListCounts *counts, const int8_t *orders,
+                             const uint8_t *bnd, const int32_t *cnt, const int32_t *nidx, int64_t npad, int32_t *forced,
+                             uint32_t *fmask, int32_t *ftiles) {
+    const unsigned nt = counts->c;
+    const int lane = int(threadIdx.x & 31);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = ctiles[q];
+        if (!((cmask[tile] >> lane) & 1u)) continue;
+        const int64_t p = int64_t(tile) * 32 + lane;
+        const int32_t v = orders[p];
+        const int c = cnt[p];
+        for (int k = 0; k < c; ++k) {
+            const int32_t j = nidx[int64_t(k) * npad + p];
+            if (bnd[j]) continue;
+            atomicMin(&forced[j], v);
+            reach_mark(fmask, ftiles, &counts->f, j);
+        }
+    }
+}
+// Pull half: a marked particle takes the offered order where it is lower than its own (post-decrement) order and joins
+// the changed list; the offers and marks are cleared.
+__global__ void k_force_apply(ListCounts *counts, const int32_t *ftiles, uint32_t *fmask, int32_t *forced,
+                              int8_t *orders, uint32_t *cmask, int32_t *ctiles) {
+    const unsigned nt = counts->f;
+    const int lane = int(threadIdx.x & 31);
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = ftiles[q];
+        const uint32_t word = fmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        bool ch = false;
+        if ((word >> lane) & 1u) {
+            const int32_t o = forced[i];
+            forced[i] = 0x7f7f7f7f;
+            if (o < int32_t(orders[i])) {
+                orders[i] = int8_t(o);
+                ch = true;
+            }
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, ch);
+        if (lane == 0) {
+            fmask[tile] = 0u;
+            if (b && atomicOr(&cmask[tile], b) == 0u) ctiles[atomicAdd(&counts->c, 1u)] = tile;
+        }
+    }
 }
 
 // Second hop of the reach (EPD2): the one-hop tiles d[0, d1) and their words are fixed first (the words are
@@ -290,6 +341,12 @@ void launch_u2_range(const void *U, int64_t n, int M, int is_f32, unsigned long 
     if (n <= 0) return;
     if (is_f32) k_u2_range<float><<<grid_for(n), HCC_BLOCK, 0, s>>>(static_cast<const float *>(U), n, M, keys);
     else k_u2_range<double><<<grid_for(n), HCC_BLOCK, 0, s>>>(static_cast<const double *>(U), n, M, keys);
+}
+void launch_force(const int32_t *ctiles, uint32_t *cmask, ListCounts *counts, int32_t *ctiles_out, int8_t *orders,
+                  const uint8_t *bnd, const int32_t *cnt, const int32_t *nidx, int64_t npad, int32_t *forced,
+                  uint32_t *fmask, int32_t *ftiles, int blocks, cudaStream_t s) {
+    k_force_push<<<blocks, HCC_BLOCK, 0, s>>>(ctiles, cmask, counts, orders, bnd, cnt, nidx, npad, forced, fmask, ftiles);
+    k_force_apply<<<blocks, HCC_BLOCK, 0, s>>>(counts, ftiles, fmask, forced, orders, cmask, ctiles_out);
 }
 void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t n, unsigned long long *out,
                                cudaStream_t s) {

@@ -59,6 +59,7 @@ end
 
 _tableau_id(bt) = error("unknown tableau")
 _strategy_id(::EPD0) = Int32(1); _strategy_id(::EPD1) = Int32(2); _strategy_id(::EPD2) = Int32(3)
+_strategy_id(::StrictEPD0) = Int32(4)
 _strategy_id(::MOODStrategy) = Int32(0)
 _flux_id(::RusanovFlux) = Int32(0)
 _flux_id(::AlignedRusanovFlux) = Int32(1)

@@ -70,7 +70,9 @@ typedef enum {               /* MOOD strategy (interface orders), MOOD.jl:20-28,
     HCC_EPD_NONE = 0,        /* NoStrategy: own orders (o_i, o_j) */
     HCC_EPD0 = 1,            /* (o_i, o_j) */
     HCC_EPD1 = 2,            /* min(o_i, o_j) on both sides */
-    HCC_EPD2 = 3             /* min over N(i) u N(j) on both sides */
+    HCC_EPD2 = 3,            /* min over N(i) u N(j) on both sides */
+    HCC_STRICT_EPD0 = 4      /* (o_i, o_j) + one-hop forcing: the neighbours of a dropped particle are lowered to its
+                                order (MOOD.jl:28-64, :312-320) */
 } hcc_mood_strategy;
 
 typedef enum {               /* src/TimeStepping/ButcherTableaus.jl */

@@ -1529,6 +1529,20 @@ struct Solver {
             if (orders[p] > 1) { orders[p] -= 1; changed[p] = 1; trig_step[p] = 1; any = true; }
             else triggered[p] = 0;
         }
+        if (!any || cfg.mood_strategy != HCC_STRICT_EPD0) return any;
+        // StrictEPD0 forcing from the post-decrement snapshot (forced_order(::Halo{1}), MOOD.jl:54-64; _mood_force!,
+        // :312-320): each interior particle takes the lowest order of its dropped neighbours, without cascade
+        std::vector<int32_t> snap = orders;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t j = 0; j < N; ++j) {
+            if (bnd[j]) continue;
+            int32_t o = snap[j];
+            for (int64_t s = start[j]; s < start[j + 1]; ++s) {
+                const int64_t p = nidx[s];
+                if (triggered[p]) o = std::min(o, snap[p]);
+            }
+            if (o < snap[j]) { orders[j] = o; changed[j] = 1; }
+        }
         return any;
     }
 

@@ -319,7 +319,8 @@ def test_weno_steps_bit_exact(hcc, oracle, cuda_lib, D, order):
         np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
 
 
-@pytest.mark.parametrize("strategy,scheme", [("EPD1", "muscl3"), ("EPD2", "muscl2"), ("EPD0", "weno2")])
+@pytest.mark.parametrize("strategy,scheme", [("EPD1", "muscl3"), ("EPD2", "muscl2"), ("EPD0", "weno2"),
+                                             ("STRICT_EPD0", "muscl3"), ("STRICT_EPD0", "weno2")])
 def test_step_graph_matches_host_driven_step(hcc, oracle, cuda_lib, strategy, scheme):
     """The captured step (MOOD fixed points as conditional WHILE nodes) and the host-driven step give the same
     bits as the oracle, with the same MOOD statistics."""
@@ -533,3 +534,24 @@ def test_moving_grid_fp32_close_to_fp64(hcc, oracle, cuda_lib):
     inner = cloud.is_boundary == 0
     assert _rel_l1(g.download_state()[:, 0], o.download_state()[:, 0], inner) < 1e-5
     assert np.abs(g.positions() - o.positions()).max() < 1e-6
+
+
+def test_strict_epd0_rk2_bit_exact(hcc, oracle, cuda_lib):
+    """The reference's GPU case "MUSCL3 MOODu1 SEPD0 RK2" (test/gpu_tests.jl:21): EPD0 interface orders with one-hop
+    forcing of the neighbours of dropped particles, SSP-RK2 — states, orders and flags bit for bit."""
+    h = 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(3, 0),
+                          mood=hcc.MOOD(hcc.STRICT_EPD0, hcc.MOODu1(1e-6)), tableau="RK2_SSP", bc_map=OUTFLOW)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    U0 = quadrant_ic(cloud)
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.3 * o.time_step()
+    for k in range(4):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.orders(), o.orders())
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+    assert o.counters()["mood_iterations"] > 0

@@ -737,3 +737,41 @@ def test_mood_u2_jump_is_flagged(hcc, oracle, abi):
         p = L.nearest((0.5 + dx, 0.5))
         _, hi = L.local_extrema(p, 0)
         assert L.flags(p, (hi + 1e-3, 0.0)) == expect
+
+
+def test_strict_epd0_forcing_uses_the_snapshot(hcc, oracle, abi):
+    """unit_core.jl:719-746: StrictEPD0 lowers the neighbours of a dropped particle to its order from the
+    post-decrement snapshot (one hop, no cascade); a neighbour that dropped itself is forced from the snapshot; the
+    EPD strategies never force."""
+    cl = lattice_1d(hcc, 40)
+    U = np.zeros((cl.n, 1))
+    for strategy, forces in ((hcc.STRICT_EPD0, True), (hcc.EPD2, False)):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.MUSCL(3, 0),
+                 mood=hcc.MOOD(strategy, hcc.OnlyMOOD()))
+        counts, idx, _, _ = o.neighbours()
+        start = np.concatenate([[0], np.cumsum(counts)])
+        p = 20
+        nbs = idx[start[p]:start[p + 1]]
+        orders = np.full(cl.n, 3)
+        orders[p] = 2                                    # p drops to 1 in this pass
+        o.set_orders(orders)
+        dirty = np.zeros(cl.n, np.uint8)
+        dirty[p] = 1
+        assert o.detect_and_drop(U, U, full=False, dirty=dirty)
+        got = o.orders()
+        assert got[p] == 1
+        if forces:
+            assert all(got[j] == 1 for j in nbs)
+            assert got[(p + 3) % cl.n] == 3             # two hops away: untouched
+        else:
+            assert all(got[j] == 3 for j in nbs)
+        if forces:
+            # a neighbour that dropped itself (3 -> 2) is forced down to 1 from the snapshot
+            q = nbs[0]
+            orders = np.full(cl.n, 3)
+            orders[p] = 2
+            o.set_orders(orders)
+            dirty[q] = 1
+            assert o.detect_and_drop(U, U, full=False, dirty=dirty)
+            got = o.orders()
+            assert got[q] == 1 and got[p] == 1
