@@ -196,7 +196,8 @@ def config_defaults() -> HccConfig:
 
 def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, tableau: str = "RK3_SSP",
                 precision: str = "fp64", bc_map: Optional[dict] = None, alpha: float = 1.0,
-                mood_substeps: bool = True, max_mood_iterations: int = 64) -> HccConfig:
+                mood_substeps: bool = True, max_mood_iterations: int = 64,
+                reset_orders_per_stage: bool = False) -> HccConfig:
     """The hcc_config of a stepper (the arguments of GeneralRKTimeStepper / MUSCL / ParticleGrid)."""
     scheme = scheme or MUSCL()
     mood = mood or MOOD()
@@ -219,6 +220,7 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
     cfg.tableau = TABLEAUS[tableau] if isinstance(tableau, str) else int(tableau)
     cfg.mood_substeps = 1 if mood_substeps else 0
     cfg.max_mood_iterations = max_mood_iterations
+    cfg.reset_orders_per_stage = 1 if reset_orders_per_stage else 0
     cfg.mood_strategy = mood.strategy
     crit = mood.criterion
     if isinstance(crit, MOODu1):
@@ -401,6 +403,14 @@ class Context:
         out = np.zeros((self.n, self.D), dtype=np.float64)
         self._check(self.lib.hcc_download_positions(self._h, _ptr(out, C.c_double)), "hcc_download_positions")
         return out
+
+    def save_snapshot(self, path):
+        """Checkpoint: positions, state, orders, MOOD flags and the step count to a binary file."""
+        self._check(self.lib.hcc_save_snapshot(self._h, str(path).encode()), "hcc_save_snapshot")
+
+    def load_snapshot(self, path):
+        """Resume from a snapshot of a context with the same configuration and particle count."""
+        self._check(self.lib.hcc_load_snapshot(self._h, str(path).encode()), "hcc_load_snapshot")
 
     def set_step_graphs(self, enable: bool = True):
         """Take each step as one captured CUDA graph (default) or drive the MOOD fixed points from the host."""

@@ -43,7 +43,7 @@ class HccConfig(C.Structure):
         ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
         ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
         ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("flux", C.c_int32),
-        ("reserved_i", C.c_int32 * 4),
+        ("reset_orders_per_stage", C.c_int32), ("reserved_i", C.c_int32 * 3),
         ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
         ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),
@@ -118,6 +118,8 @@ PROTOTYPES = [
     ("hcc_set_step_graphs", C.c_int, [P, C.c_int]),
     ("hcc_set_mover", C.c_int, [P, C.POINTER(HccMover)]),
     ("hcc_download_positions", C.c_int, [P, C.POINTER(C.c_double)]),
+    ("hcc_save_snapshot", C.c_int, [P, C.c_char_p]),
+    ("hcc_load_snapshot", C.c_int, [P, C.c_char_p]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_synchronize", C.c_int, [P]),

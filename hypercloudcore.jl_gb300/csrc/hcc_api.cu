@@ -662,6 +662,10 @@ template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
     c->launches += enqueue_prologue(c, &a1, c->stream);
     for (int s = 0; s < S; ++s) {
         StageArgs<T> a = stage_args<T>(c, s);
+        if (s > 0 && c->cfg.reset_orders_per_stage) {     // TimeSteppers.jl:556
+            launch_fill_i8(c->orders, int8_t(c->max_order), n, c->stream);
+            c->launches += 1;
+        }
         c->launches += enqueue_full<T>(c, a, c->stream, c->prof != 0);
         if ((st = launch_check(c, "stage kernels")) != HCC_OK) return st;
         if (!a.check) {
@@ -724,6 +728,10 @@ template <typename T> hcc_status capture_step(hcc_ctx *c, int parity) {
     launches += enqueue_prologue(c, &a1, st);
     for (int s = 0; s < S && err == cudaSuccess; ++s) {
         StageArgs<T> a = stage_args<T>(c, s);
+        if (s > 0 && c->cfg.reset_orders_per_stage) {     // TimeSteppers.jl:556
+            launch_fill_i8(c->orders, int8_t(c->max_order), c->n, st);
+            launches += 1;
+        }
         launches += enqueue_full<T>(c, a, st, false);
         if (!a.check) continue;
         cudaStreamCaptureStatus cs;
@@ -1220,6 +1228,75 @@ hcc_status hcc_download_positions(hcc_ctx *c, double *pos) {
     HCC_TRY(c->cuda(cudaMemcpy(soa.data(), c->pos, soa.size() * sizeof(double), cudaMemcpyDeviceToHost), "positions"));
     for (int64_t i = 0; i < c->n; ++i)
         for (int d = 0; d < D; ++d) pos[i * D + d] = soa[size_t(d) * c->npad + i];
+    return HCC_OK;
+}
+
+// Snapshot file: magic, then a header of int64 fields, then positions (n x D FP64, SoA as held), state (n x M in the
+// context's precision), orders (int8 n), MOOD flags (uint8 n).
+static const char kSnapMagic[8] = {'H', 'C', 'C', 'S', 'N', 'A', 'P', '1'};
+struct SnapHeader {
+    int64_t abi, dim, n_vars, pde, precision, n, npad, steps;
+};
+
+hcc_status hcc_save_snapshot(hcc_ctx *c, const char *path) {
+    if (!c || !path) return c ? c->fail(HCC_ERR_INVALID, "null path") : HCC_ERR_INVALID;
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    hcc_status st;
+    HCC_TRY(c->sync("snapshot"));
+    const int64_t n = c->n, np = c->npad;
+    std::vector<double> pos(size_t(np) * c->D);
+    std::vector<char> U(size_t(n) * c->M * c->esz());
+    std::vector<int8_t> ord(n);
+    std::vector<uint8_t> flags(n);
+    HCC_TRY(c->cuda(cudaMemcpy(pos.data(), c->pos, pos.size() * sizeof(double), cudaMemcpyDeviceToHost), "positions"));
+    HCC_TRY(c->cuda(cudaMemcpy(U.data(), c->rhos, U.size(), cudaMemcpyDeviceToHost), "state"));
+    HCC_TRY(c->cuda(cudaMemcpy(ord.data(), c->orders, n, cudaMemcpyDeviceToHost), "orders"));
+    HCC_TRY(c->cuda(cudaMemcpy(flags.data(), c->trig_step, n, cudaMemcpyDeviceToHost), "flags"));
+    SnapHeader h{HCC_ABI_VERSION, c->D, c->M, c->cfg.pde, c->cfg.precision, n, np, c->steps};
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return c->fail(HCC_ERR_INVALID, std::string("cannot open ") + path);
+    bool ok = std::fwrite(kSnapMagic, 1, 8, f) == 8 && std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+              std::fwrite(pos.data(), sizeof(double), pos.size(), f) == pos.size() &&
+              std::fwrite(U.data(), 1, U.size(), f) == U.size() && std::fwrite(ord.data(), 1, n, f) == size_t(n) &&
+              std::fwrite(flags.data(), 1, n, f) == size_t(n);
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? HCC_OK : c->fail(HCC_ERR_INVALID, std::string("write failed: ") + path);
+}
+
+hcc_status hcc_load_snapshot(hcc_ctx *c, const char *path) {
+    if (!c || !path) return c ? c->fail(HCC_ERR_INVALID, "null path") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud uploaded");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return c->fail(HCC_ERR_INVALID, std::string("cannot open ") + path);
+    char magic[8];
+    SnapHeader h{};
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kSnapMagic, 8) == 0 &&
+              std::fread(&h, sizeof(h), 1, f) == 1;
+    if (!ok || h.abi != HCC_ABI_VERSION || h.dim != c->D || h.n_vars != c->M || h.pde != c->cfg.pde ||
+        h.precision != c->cfg.precision || h.n != c->n || h.npad != c->npad) {
+        std::fclose(f);
+        return c->fail(HCC_ERR_INVALID, "snapshot does not match this context");
+    }
+    const int64_t n = c->n;
+    std::vector<double> pos(size_t(c->npad) * c->D);
+    std::vector<char> U(size_t(n) * c->M * c->esz());
+    std::vector<int8_t> ord(n);
+    std::vector<uint8_t> flags(n);
+    ok = std::fread(pos.data(), sizeof(double), pos.size(), f) == pos.size() &&
+         std::fread(U.data(), 1, U.size(), f) == U.size() && std::fread(ord.data(), 1, n, f) == size_t(n) &&
+         std::fread(flags.data(), 1, n, f) == size_t(n);
+    std::fclose(f);
+    if (!ok) return c->fail(HCC_ERR_INVALID, "truncated snapshot");
+    hcc_status st;
+    HCC_TRY(c->sync("snapshot"));
+    HCC_TRY(c->cuda(cudaMemcpy(c->pos, pos.data(), pos.size() * sizeof(double), cudaMemcpyHostToDevice), "positions"));
+    HCC_TRY(hcc_build_neighbours(c));
+    HCC_TRY(hcc_prepare_geometry(c));
+    HCC_TRY(c->cuda(cudaMemcpy(c->rhos, U.data(), U.size(), cudaMemcpyHostToDevice), "state"));
+    HCC_TRY(c->cuda(cudaMemcpy(c->orders, ord.data(), n, cudaMemcpyHostToDevice), "orders"));
+    HCC_TRY(c->cuda(cudaMemcpy(c->trig_step, flags.data(), n, cudaMemcpyHostToDevice), "flags"));
+    c->steps = h.steps;
+    c->have_state = true;
     return HCC_OK;
 }
 

@@ -33,7 +33,8 @@ mutable struct HccConfig
     abi_version::Int32; dim::Int32; n_vars::Int32; pde::Int32; precision::Int32; muscl_order::Int32
     div_order::Int32; mood_criterion::Int32; mood_strategy::Int32; tableau::Int32; mood_substeps::Int32
     periodic::NTuple{3, Int32}; bc_by_tag::NTuple{16, Int32}; max_mood_iterations::Int32
-    scheme::Int32; limiter::Int32; slot_capacity::Int32; flux::Int32; reserved_i::NTuple{4, Int32}
+    scheme::Int32; limiter::Int32; slot_capacity::Int32; flux::Int32; reset_orders_per_stage::Int32
+    reserved_i::NTuple{3, Int32}
     dx::NTuple{3, Float64}; radius::Float64; weight_alpha::Float64
     canvas_min::NTuple{3, Float64}; canvas_max::NTuple{3, Float64}
     domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
@@ -93,7 +94,8 @@ function _set_mover(h, mv; full_search_per_stage::Bool = false)
 end
 
 function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T}, interp::MUSCL, mood::MOOD,
-                            tableau_id::Integer; bc_map = Dict{Int, Int32}(), precision::Symbol = :fp64) where {D, M, T}
+                            tableau_id::Integer; bc_map = Dict{Int, Int32}(), precision::Symbol = :fp64,
+                            reset_orders_per_stage::Bool = false, mood_substeps::Bool = true) where {D, M, T}
     cfg = HccConfig()
     cfg.dim, cfg.n_vars, cfg.pde = D, M, hcc_pde_kind(eq)
     cfg.precision = precision === :fp32 ? 1 : 0
@@ -101,6 +103,8 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     cfg.limiter = _limiter_id(interp.limiter)
     cfg.flux = _flux_id(interp.flux)
     cfg.tableau = tableau_id
+    cfg.reset_orders_per_stage = Int32(reset_orders_per_stage)
+    cfg.mood_substeps = Int32(mood_substeps)
     cfg.mood_strategy = _strategy_id(mood.strategy)
     cfg.mood_criterion, cfg.mood_delta = _criterion(mood.criterion)
     if mood.criterion isa MOODu2
@@ -127,6 +131,20 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     _set_mover(h[], pg.mover)
     ts = GB300RKTimeStepper{D, M}(h[], N)
     finalizer(t -> ccall((:hcc_destroy, libhcc), Cint, (Ptr{Cvoid},), t.handle), ts)
+    return ts
+end
+
+# build_timestepper(context; time_conf) (Builders/timestepper.jl:15-35) for the GB300 stepper: the same context keys
+# (:Equation, :Scheme, :MOOD, :Tableau, :Grid) and Time options (reset_orders_per_stage, full_search_per_stage,
+# mood_substeps), plus :Precision (:fp64 / :fp32) and :BCMap (tag => HCC_BC_* kind).
+function build_gb300_timestepper(context::Dict; time_conf::Dict = Dict{Symbol, Any}())
+    pg = context[:Grid]::ParticleGrid
+    ts = GB300RKTimeStepper(context[:Equation], pg, context[:Scheme], context[:MOOD], _tableau_id(context[:Tableau]);
+                            bc_map = get(context, :BCMap, Dict{Int, Int32}()),
+                            precision = get(context, :Precision, :fp64),
+                            reset_orders_per_stage = get(time_conf, :reset_orders_per_stage, false)::Bool,
+                            mood_substeps = get(time_conf, :mood_substeps, true)::Bool)
+    _set_mover(ts.handle, pg.mover; full_search_per_stage = get(time_conf, :full_search_per_stage, false)::Bool)
     return ts
 end
 

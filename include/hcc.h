@@ -127,7 +127,8 @@ typedef struct {
     int32_t limiter;                   /* hcc_limiter (MUSCL only) */
     int32_t slot_capacity;             /* neighbours per particle the lists may hold (0: no limit) */
     int32_t flux;                      /* hcc_flux (MUSCL numerical flux) */
-    int32_t reserved_i[4];
+    int32_t reset_orders_per_stage;    /* 1: restore the maximum order before each stage's full pass */
+    int32_t reserved_i[3];
     double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
     double  radius;                    /* support radius R of ExponentialWeightFunction */
     double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */
@@ -233,6 +234,13 @@ hcc_status hcc_set_mover(hcc_ctx *ctx, const hcc_mover *mover);
 
 /* Current particle positions (N x D row-major, the caller's numbering; moved by hcc_step on moving grids). */
 hcc_status hcc_download_positions(hcc_ctx *ctx, double *pos);
+
+/* Checkpoint / resume. hcc_save_snapshot writes the context's particle positions, state (in its precision), orders
+   and MOOD flags of the last step and its step count to a binary file; hcc_load_snapshot reads one written by a
+   context of the same configuration (dim, n_vars, pde, precision) and particle count, rebuilds the neighbour lists
+   and geometry at the saved positions and restores the rest. No counterpart in the reference. */
+hcc_status hcc_save_snapshot(hcc_ctx *ctx, const char *path);
+hcc_status hcc_load_snapshot(hcc_ctx *ctx, const char *path);
 
 /* One time step: (ts::GeneralRKTimeStepper)(eq, pg, t, dt) (TimeSteppers.jl:531-577). */
 hcc_status hcc_step(hcc_ctx *ctx, double t, double dt);

@@ -1622,6 +1622,8 @@ struct Solver {
                     if (!prepare_geometry()) return false;
                 }
             }
+            // reset_orders_per_stage (TimeSteppers.jl:556)
+            if (cfg.reset_orders_per_stage) std::fill(orders.begin(), orders.end(), max_order);
             KX_cur = mv ? &KX[i - 1] : nullptr;
             compute_rhs(KE[i - 1], Y[i - 1].data(), true);
         }

@@ -555,3 +555,59 @@ def test_strict_epd0_rk2_bit_exact(hcc, oracle, cuda_lib):
         np.testing.assert_array_equal(g.orders(), o.orders())
         np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
     assert o.counters()["mood_iterations"] > 0
+
+
+def test_reset_orders_per_stage_bit_exact(hcc, oracle, cuda_lib):
+    """GeneralRKTimeStepper(...; reset_orders_per_stage = true) (TimeSteppers.jl:142, :556): the maximum order is
+    restored before every stage's full pass."""
+    h = 0.02
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(3, 0), mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)),
+                          bc_map=OUTFLOW, reset_orders_per_stage=True)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    U0 = quadrant_ic(cloud)
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+
+
+@pytest.mark.parametrize("moving,precision", [(False, "fp32"), (True, "fp64")])
+def test_snapshot_resume(hcc, cuda_lib, tmp_path, moving, precision):
+    """Checkpoint / resume: a context restored from a snapshot continues bit for bit like the one that wrote it
+    (positions, state, orders, flags; a moving grid's neighbour lists rebuilt at the saved positions)."""
+    h = 0.04
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.2 * h, seed=5)
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)),
+                          bc_map=OUTFLOW, precision=precision)
+
+    def ctx():
+        c = hcc.Context(cfg)
+        c.upload_cloud(cloud)
+        c.build_neighbours()
+        c.prepare_geometry()
+        if moving:
+            c.set_mover(hcc.mover("scaled", alpha=0.5))
+        return c
+    a = ctx()
+    U0 = quadrant_ic(cloud)
+    a.upload_state(U0.astype(np.float32) if precision == "fp32" else U0)
+    dt = 0.3 * a.time_step()
+    for k in range(2):
+        a.step(k * dt, dt)
+    path = tmp_path / "snap.bin"
+    a.save_snapshot(path)
+    for k in range(2, 4):
+        a.step(k * dt, dt)
+    b = ctx()
+    b.load_snapshot(path)
+    assert b.counters()["steps"] == 2
+    for k in range(2, 4):
+        b.step(k * dt, dt)
+    assert _bits_equal(a.download_state(), b.download_state())
+    assert _bits_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.mood_flags(), b.mood_flags())
