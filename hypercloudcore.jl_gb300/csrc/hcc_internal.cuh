@@ -275,6 +275,24 @@ __device__ __forceinline__ void reach_mark(uint32_t *mask, int32_t *tiles, unsig
     if (atomicOr(&mask[j >> 5], 1u << (j & 31)) == 0u) list_append(tiles, count, j >> 5);
 }
 
+// reach_mark for a whole warp (all 32 lanes call it; j < 0: no mark): lanes whose particles share a tile combine their
+// bits first, one atomic per distinct tile word, and the newly listed tiles are appended together.
+__device__ __forceinline__ void reach_mark_warp(uint32_t *mask, int32_t *tiles, unsigned *count, int32_t j) {
+    const int lane = int(threadIdx.x & 31);
+    const int32_t t = j >= 0 ? (j >> 5) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, t);
+    const unsigned bits = __reduce_or_sync(grp, j >= 0 ? (1u << (j & 31)) : 0u);
+    bool fresh = false;
+    if (lane == __ffs(grp) - 1 && t >= 0) fresh = atomicOr(&mask[t], bits) == 0u;
+    const unsigned nb = __ballot_sync(0xffffffffu, fresh);
+    if (nb) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(count, unsigned(__popc(nb)));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (fresh) tiles[base + unsigned(__popc(nb & ((1u << lane) - 1u)))] = t;
+    }
+}
+
 // Launchers of one (precision, D, M, pde, reconstruction degree) instantiation.
 struct StageOps {
     int D, M, pde, rdeg, Br;

@@ -573,6 +573,94 @@ __device__ __forceinline__ void gather_one(const StageArgs<T> &a, const int64_t 
     store_vec<T, BR * M>(g, &out[0][0]);
 }
 
+// FP32 degree-1 worklist pass of the reconstruction with four warps per tile: warp 0 lowers starved orders and picks
+// the path; on the cached gradient-weight path warp w sums the slots k = w, w + 4, ... and marks their neighbours'
+// reach, warp 0 adds the four partial sums in a fixed order, applies the limiter and stores the gradients; any
+// other particle is reconstructed whole by warp 0.
+template <typename T, int D, int M, int PDE, int RDEG>
+__global__ void __launch_bounds__(128) k_gather_tiles(const StageArgs<T> a) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    __shared__ T parts[4][32][BR * M];
+    __shared__ int path[32];
+    const int lane = int(threadIdx.x & 31), w = int(threadIdx.x >> 5);
+    const unsigned nt = *a.wcount;
+    const int64_t np = a.g.npad;
+    for (unsigned q = blockIdx.x; q < nt; q += gridDim.x) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool live = ((word >> lane) & 1u) && !a.g.bnd[i];
+        const int cnt = live ? a.g.cnt[i] : 0;
+        if (w == 0) {
+            int gp = 0;
+            if (live) {
+                int p = a.orders[i];
+                const int p0 = p;
+                while (p > 1 && cnt < basis_count(D, p - 1)) --p;
+                if (p < p0) a.orders[i] = int8_t(p);
+                gp = (p == a.sc.max_order && p > 1 && a.g.ok_r[i] && a.g.gw) ? 1 : 0;
+            }
+            path[lane] = gp;
+        }
+        __syncthreads();
+        const int gp = path[lane];
+        {
+            // warp-uniform slot loop (the reach marks are combined across the warp)
+            const int myc = (live && gp) ? cnt : 0;
+            const int kw = __reduce_max_sync(0xffffffffu, myc);
+            T fi[M], out[BR * M];
+            if (myc > 0) load_vec<T, M>(a.U + i * M, fi);
+#pragma unroll
+            for (int b = 0; b < BR * M; ++b) out[b] = T(0);
+            for (int k = w; k < kw; k += 4) {
+                const bool on = k < myc;
+                int32_t j = -1;
+                if (on) {
+                    j = a.g.nidx[int64_t(k) * np + i];
+                    T gk[D], df[M];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) gk[d] = a.g.gw[(int64_t(k) * D + d) * np + i];
+                    load_vec<T, M>(a.U + int64_t(j) * M, df);
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const T dm = df[m] - fi[m];
+#pragma unroll
+                        for (int b = 0; b < BR; ++b) out[b * M + m] = out[b * M + m] + gk[b] * dm;
+                    }
+                }
+                if (a.rmask) reach_mark_warp(a.rmask, a.rtiles, a.rcount, j);
+            }
+            if (myc > 0 || (live && gp))
+#pragma unroll
+                for (int b = 0; b < BR * M; ++b) parts[w][lane][b] = out[b];
+        }
+        __syncthreads();
+        if (w == 0 && a.rmask) reach_mark_warp(a.rmask, a.rtiles, a.rcount, (live && gp) ? int32_t(i) : -1);
+        if (w == 0 && live) {
+            if (gp) {
+                T fi[M], out[BR][M];
+                load_vec<T, M>(a.U + i * M, fi);
+#pragma unroll
+                for (int b = 0; b < BR; ++b)
+#pragma unroll
+                    for (int m = 0; m < M; ++m)
+                        out[b][m] = ((parts[0][lane][b * M + m] + parts[1][lane][b * M + m]) + parts[2][lane][b * M + m]) +
+                                    parts[3][lane][b * M + m];
+                if (a.sc.limiter != HCC_LIMITER_NONE) limit_slopes<T, D, M, RDEG>(a, i, cnt, fi, out);
+                store_vec<T, BR * M>(a.grad + i * (BR * M), &out[0][0]);
+            } else {
+                gather_one<T, D, M, PDE, RDEG>(a, i);
+                if (a.rmask) {
+                    reach_mark(a.rmask, a.rtiles, a.rcount, int32_t(i));
+                    for (int k = 0; k < cnt; ++k) reach_mark(a.rmask, a.rtiles, a.rcount, a.g.nidx[int64_t(k) * np + i]);
+                }
+            }
+        }
+        if (threadIdx.x == 0 && a.clear_wmask) a.wmask[tile] = 0u;   // every lane read the word before the barrier
+        __syncthreads();
+    }
+}
+
 // A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word)
 // that also marks the one-hop reach of each member in rmask / rtiles.
 template <typename T, int D, int M, int PDE, int RDEG>
@@ -790,8 +878,16 @@ template <typename T, int D, int M> constexpr int flux_min_blocks() {
 // contraction with the divergence weights; K_E = -2 Σ c·ΔF (TimeSteppers.jl:354). Fused epilogue: the next
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).
-template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
-__device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i) {
+// Partial sums of a particle's slots handled by one warp of a split tile (FP32 worklist passes).
+template <typename T, int M> struct FluxPart {
+    T s[M], c[M], mn[M], mx[M];
+};
+
+// The flux pass of particle i over its slots k0, k0 + KSTEP, ... With KSTEP = 1 the whole pass and its epilogue;
+// with KSTEP > 1 (FP32) the partial sums and extrema go to `part` for the caller to combine.
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, int KSTEP = 1>
+__device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i, const int k0 = 0,
+                                         FluxPart<T, M> *part = nullptr) {
     constexpr int BR = RBasis<D, RDEG>::B;
     if (a.g.bnd[i]) {
         if (a.full) {
@@ -816,8 +912,9 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
     if constexpr (ALE) {
         grid_velocity<T, D, M, PDE>(a, i, fi, wv);
         wp = wv;
+        if (k0 == 0)
 #pragma unroll
-        for (int d = 0; d < D; ++d) a.KXout[int64_t(d) * a.g.npad + i] = double(wv[d]);
+            for (int d = 0; d < D; ++d) a.KXout[int64_t(d) * a.g.npad + i] = double(wv[d]);
     }
     flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami, wp);
     constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form (below)
@@ -839,26 +936,26 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
 #pragma unroll
     for (int m = 0; m < M; ++m) { mn[m] = fi[m]; mx[m] = fi[m]; }
 
-    if (wok) {
-        // slot data of slot k+1 are loaded while slot k is computed (one-deep software pipeline)
-        int32_t jn = a.g.nidx[i];
+    if (wok && k0 < cnt) {
+        // slot data of the next slot are loaded while this one is computed (one-deep software pipeline)
+        int32_t jn = a.g.nidx[int64_t(k0) * np + i];
         T dkn[D], wkn[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            dkn[d] = a.g.dist[int64_t(d) * np + i];
-            wkn[d] = wsl[int64_t(d) * np + i];
+            dkn[d] = a.g.dist[(int64_t(k0) * D + d) * np + i];
+            wkn[d] = wsl[(int64_t(k0) * D + d) * np + i];
         }
-        for (int k = 0; k < cnt; ++k) {
+        for (int k = k0; k < cnt; k += KSTEP) {
             const int32_t j = jn;
             T dk[D], wk[D];
 #pragma unroll
             for (int d = 0; d < D; ++d) { dk[d] = dkn[d]; wk[d] = wkn[d]; }
-            if (k + 1 < cnt) {
-                jn = a.g.nidx[int64_t(k + 1) * np + i];
+            if (k + KSTEP < cnt) {
+                jn = a.g.nidx[int64_t(k + KSTEP) * np + i];
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    dkn[d] = a.g.dist[(int64_t(k + 1) * D + d) * np + i];
-                    wkn[d] = wsl[(int64_t(k + 1) * D + d) * np + i];
+                    dkn[d] = a.g.dist[(int64_t(k + KSTEP) * D + d) * np + i];
+                    wkn[d] = wsl[(int64_t(k + KSTEP) * D + d) * np + i];
                 }
             }
             T fj[M];
@@ -975,7 +1072,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
             acc.add(t);
         }
     } else if (need_ext) {
-        for (int k = 0; k < cnt; ++k) {
+        for (int k = k0; k < cnt; k += KSTEP) {
             const int32_t j = a.g.nidx[int64_t(k) * np + i];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
@@ -984,6 +1081,17 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i)
                 mx[m] = vmax(mx[m], fj);
             }
         }
+    }
+    if constexpr (KSTEP > 1) {
+        static_assert(sizeof(T) == 4, "split tiles are the FP32 path");
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            part->s[m] = acc.s[m];
+            part->c[m] = acc.c[m];
+            part->mn[m] = mn[m];
+            part->mx[m] = mx[m];
+        }
+        return false;
     }
     T Kv[M];
 #pragma unroll
@@ -1020,6 +1128,53 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
         const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG, ALE>(a, i) : false;
         if (a.check) tile_failures(a, tile, f);
         if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
+}
+
+// FP32 worklist pass with four warps per tile: warp w takes the slots k = w, w + 4, ... of every member of the tile
+// (a quarter of the serial slot chain, the latency that bounds the short worklist passes), warp 0 combines the four
+// compensated partial sums (Kahan over the partials, minus their compensations) and the extrema, and runs the
+// epilogue. One block per tile, block-stride over the list.
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
+__global__ void __launch_bounds__(128) k_flux_tiles(const StageArgs<T> a) {
+    __shared__ FluxPart<T, M> parts[4][32];
+    const int lane = int(threadIdx.x & 31), w = int(threadIdx.x >> 5);
+    const unsigned nt = *a.wcount;
+    for (unsigned q = blockIdx.x; q < nt; q += gridDim.x) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool live = ((word >> lane) & 1u) && !a.g.bnd[i];
+        if (live) flux_one<T, D, M, PDE, RDEG, ALE, 4>(a, i, w, &parts[w][lane]);
+        __syncthreads();
+        if (w == 0) {
+            bool f = false;
+            if (live) {
+                T Kv[M], mn[M], mx[M], fi[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    T sm = T(0), cm = T(0), comp = T(0);
+                    mn[m] = parts[0][lane].mn[m];
+                    mx[m] = parts[0][lane].mx[m];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        const T y = parts[v][lane].s[m] - cm;
+                        const T u = sm + y;
+                        cm = (u - sm) - y;
+                        sm = u;
+                        comp = comp + parts[v][lane].c[m];
+                        mn[m] = vmin(mn[m], parts[v][lane].mn[m]);
+                        mx[m] = vmax(mx[m], parts[v][lane].mx[m]);
+                    }
+                    Kv[m] = -(sm - comp);
+                }
+                load_vec<T, M>(a.U + i * M, fi);
+                f = stage_epilogue<T, D, M, PDE, RDEG>(a, i, fi, Kv, mn, mx);
+            }
+            if (a.check) tile_failures(a, tile, f);
+            if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+        }
+        __syncthreads();
     }
 }
 
@@ -1270,10 +1425,24 @@ struct StageInst {
     }
     static void gather(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        if constexpr (sizeof(T) == 4 && RDEG == 1) {
+            if (!a.full) {   // FP32 degree-1 worklist pass: split tiles (four warps a tile)
+                k_gather_tiles<T, D, M, PDE, RDEG><<<std::max(1u, unsigned(a.list_blocks)), 128, 0, s>>>(a);
+                return;
+            }
+        }
         k_gather<T, D, M, PDE, RDEG><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
     }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        if constexpr (sizeof(T) == 4) {
+            if (!a.full) {   // FP32 worklist pass: split tiles (four warps a tile)
+                const unsigned g = std::max(1u, unsigned(a.list_blocks));
+                if (a.mover) k_flux_tiles<T, D, M, PDE, RDEG, true><<<g, 128, 0, s>>>(a);
+                else k_flux_tiles<T, D, M, PDE, RDEG, false><<<g, 128, 0, s>>>(a);
+                return;
+            }
+        }
         if (a.mover)     // moving grid: the ALE-frame instantiation (grid velocities, shifted fluxes and speeds)
             k_flux<T, D, M, PDE, RDEG, true><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
         else
