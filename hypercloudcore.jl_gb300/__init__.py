@@ -424,6 +424,29 @@ class Context:
     def stream(self) -> int:
         return int(self.lib.hcc_stream(self._h) or 0)
 
+    # -- learned troubled-point predictor
+    def set_predictor(self, predictor, threshold: float = 0.5):
+        """Attach a TroubledPointPredictor (None detaches): each step pre-lowers the particles it predicts."""
+        self._predictor = predictor
+        h = predictor.handle if predictor is not None else None
+        self._check(self.lib.hcc_set_predictor(self._h, h, float(threshold)), "hcc_set_predictor")
+
+    def set_feature_capture(self, enable: bool = True):
+        """Keep each step's start-of-step stencil features (for TroubledPointPredictor.collect)."""
+        self._check(self.lib.hcc_set_feature_capture(self._h, int(bool(enable))), "hcc_set_feature_capture")
+
+    def features(self) -> np.ndarray:
+        """The 24 stencil features (N x 24, FP32) of the current state."""
+        out = np.zeros((self.n, _abi.HCC_MLP_FEATURES), dtype=np.float32)
+        self._check(self.lib.hcc_download_features(self._h, _ptr(out, C.c_float)), "hcc_download_features")
+        return out
+
+    def predicted(self) -> np.ndarray:
+        """The particles the predictor pre-lowered in the last step (0/1)."""
+        out = np.zeros(self.n, dtype=np.uint8)
+        self._check(self.lib.hcc_download_predicted(self._h, _ptr(out, C.c_uint8)), "hcc_download_predicted")
+        return out
+
 
 class GB300RKTimeStepper:
     """The GB300 counterpart of GeneralRKTimeStepper(pde, MUSCL(...), MOOD(...), tableau) on a fixed cloud.
@@ -459,7 +482,10 @@ class GB300RKTimeStepper:
         return self.ctx.orders()
 
 
+from .learned import TroubledPointPredictor  # noqa: E402
+
 __all__ = [
+    "TroubledPointPredictor",
     "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "mover", "MOOD", "MOODu1", "MOODu2",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "STRICT_EPD0", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",

@@ -60,7 +60,7 @@ class HccCounters(C.Structure):
         ("min_neighbours_interior", C.c_int32), ("total_neighbours", C.c_int64), ("mood_iterations", C.c_int64),
         ("mood_flagged", C.c_int64), ("inadmissible", C.c_int64), ("kernel_launches", C.c_int64),
         ("steps", C.c_int64), ("kernel_launches_total", C.c_int64),
-        ("graph_steps", C.c_int64),
+        ("graph_steps", C.c_int64), ("predicted", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -74,6 +74,17 @@ class HccMover(C.Structure):
 
 
 MOVERS = {"none": 0, "lagrangian": 1, "scaled": 2, "prescribed": 3}
+
+
+HCC_MLP_FEATURES = 24
+HCC_MLP_HIDDEN = 64
+HCC_MLP_NPARAMS = 64 * 24 + 64 + 64 * 64 + 64 + 64 + 1
+
+
+class HccMlpConfig(C.Structure):
+    _fields_ = [("capacity", C.c_int64), ("neg_keep", C.c_double), ("seed", C.c_uint64), ("lr", C.c_double),
+                ("beta1", C.c_double), ("beta2", C.c_double), ("adam_eps", C.c_double), ("pos_weight", C.c_double),
+                ("reserved", C.c_double * 4)]
 
 
 class HccKernelTimes(C.Structure):
@@ -122,6 +133,24 @@ PROTOTYPES = [
     ("hcc_load_snapshot", C.c_int, [P, C.c_char_p]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
+    ("hcc_mlp_create", C.c_int, [C.POINTER(HccMlpConfig), C.POINTER(P)]),
+    ("hcc_mlp_destroy", None, [P]),
+    ("hcc_mlp_last_error", C.c_char_p, [P]),
+    ("hcc_mlp_get_params", C.c_int, [P, _fp, _fp]),
+    ("hcc_mlp_set_params", C.c_int, [P, _fp, _fp]),
+    ("hcc_mlp_collect", C.c_int, [P, P]),
+    ("hcc_mlp_add_rows", C.c_int, [P, _fp, _u8p, C.c_int64]),
+    ("hcc_mlp_rows", C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("hcc_mlp_clear", C.c_int, [P]),
+    ("hcc_mlp_fit_norm", C.c_int, [P, C.c_double]),
+    ("hcc_mlp_train", C.c_int, [P, C.c_int64, C.c_int64, C.c_double, _dp]),
+    ("hcc_mlp_evaluate", C.c_int, [P, C.c_double, C.c_double, C.POINTER(C.c_int64)]),
+    ("hcc_mlp_loss_grad", C.c_int, [P, _fp, _u8p, C.c_int64, _fp, _dp]),
+    ("hcc_mlp_predict_rows", C.c_int, [P, _fp, C.c_int64, _fp]),
+    ("hcc_set_predictor", C.c_int, [P, P, C.c_double]),
+    ("hcc_set_feature_capture", C.c_int, [P, C.c_int]),
+    ("hcc_download_features", C.c_int, [P, _fp]),
+    ("hcc_download_predicted", C.c_int, [P, _u8p]),
     ("hcc_synchronize", C.c_int, [P]),
     ("hcc_stream", P, [P]),
 ]

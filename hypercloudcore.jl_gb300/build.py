@@ -2,7 +2,8 @@
 
 The FP64 translation units (neighbour search, MLS geometry, FP64 stage kernels) are compiled with -fmad=false so
 that no multiply-add is contracted: their results follow the reference's rounding step for step. The FP32 bulk
-kernels keep the default contraction.
+kernels keep the default contraction. The learned predictor's unit is compiled with -fmad=false too: its FP32
+stencil features follow the oracle's operation sequence bit for bit.
 """
 from __future__ import annotations
 
@@ -29,6 +30,7 @@ UNITS = {
     "hcc_stage_f32_r1.cu": ["-ftz=true"],
     "hcc_stage_f32_r2.cu": ["-ftz=true"],
     "hcc_noalloc.cu": ["-fmad=false"],
+    "hcc_learn.cu": ["-fmad=false"],
 }
 
 

@@ -205,6 +205,15 @@ struct hcc_ctx {
     ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
     int list_blocks = 1, drop_blocks = 1;
     unsigned long long *u2_keys = nullptr;       // MOODu2 global range of the stage state (ordered keys)
+    // learned troubled-point predictor: the attached network, its threshold (logit), the start-of-step features
+    // (captured for training) and the mask of the particles it pre-lowered
+    hcc_mlp *mlp = nullptr;
+    float thr_logit = 0.f;
+    int capture_feat = 0;
+    float *feat = nullptr;
+    uint8_t *pred = nullptr;
+    int64_t predicted = 0;
+    bool feat_valid = false;
     // moving grid: mover, start-of-step / stage / final positions and the stage grid velocities (SoA FP64)
     hcc_mover mover{};
     double *x_n = nullptr, *x_cand = nullptr, *Xs[HCC_MAX_STAGES] = {}, *KXs[HCC_MAX_STAGES] = {};
@@ -309,7 +318,8 @@ struct hcc_ctx {
             for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
         dfree(orders); dfree(nbmin); dfree(trig_step); dfree(inadm);
         dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
-        dfree(ftiles); dfree(fmask); dfree(forced);
+        dfree(ftiles); dfree(fmask); dfree(forced); dfree(feat); dfree(pred);
+        feat_valid = false;
     }
     void free_slots() {
         drop_graphs();
@@ -607,14 +617,61 @@ template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, c
     return k + 1;
 }
 
+// Stencil-feature inputs of the current state.
+FeatArgs feat_args(const hcc_ctx *c, const void *U) {
+    FeatArgs fa{};
+    fa.U = U;
+    fa.f32 = c->f32;
+    fa.D = c->D;
+    fa.M = c->M;
+    fa.pde = c->cfg.pde;
+    fa.n = c->n;
+    fa.npad = c->npad;
+    fa.cnt = c->cnt;
+    fa.nidx = c->nidx;
+    fa.dist = c->f32 ? static_cast<const void *>(c->dist32) : static_cast<const void *>(c->dist64);
+    fa.bnd = c->bnd;
+    fa.h = float(c->h);
+    fa.gm1 = float(c->cfg.gamma - 1.0);
+    return fa;
+}
+
+// Buffers of the predictor and of the feature capture (before a step is enqueued or captured).
+hcc_status ensure_learn_buffers(hcc_ctx *c) {
+    hcc_status st = HCC_OK;
+    if (c->capture_feat && !c->feat) st = c->alloc(c->feat, size_t(c->n) * HCC_MLP_FEATURES, "features");
+    if (st == HCC_OK && c->mlp && !c->pred) {
+        st = c->alloc(c->pred, size_t(c->n), "predicted mask");
+        if (st == HCC_OK) st = c->cuda(cudaMemset(c->pred, 0, size_t(c->n)), "predicted mask");
+    }
+    return st;
+}
+
 int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
     cudaMemsetAsync(c->lcounts, 0, sizeof(ListCounts), st);
     cudaMemsetAsync(c->mood_stats, 0, sizeof(MoodStats), st);
     launch_fill_i8(c->orders, int8_t(c->max_order), c->n, st);
     cudaMemsetAsync(c->trig_step, 0, size_t(c->n), st);
+    int k = 0;
+    if (c->capture_feat || c->mlp) {
+        const FeatArgs fa = feat_args(c, c->rhos);
+        if (c->capture_feat && launch_features(fa, c->feat, st)) k += 1;
+        if (c->mlp) {
+            // the predicted particles start the step one order lower (MOOD still judges every particle)
+            PredictOut po{};
+            po.orders = c->orders;
+            po.lowered = int8_t(std::max(1, c->max_order - 1));
+            po.pred = c->pred;
+            po.count = &c->mood_stats->predicted;
+            po.thr_logit = c->thr_logit;
+            if (launch_predict(fa, mlp_weights(c->mlp), po, std::max(1, c->list_blocks / 8) * 4,
+                               &c->mood_stats->tc_error, st))
+                k += 1;
+        }
+    }
     c->ops->stage1(args, c->n, st);
     launch_bc_apply(c->Y[0], c->rhos, c->blist, c->bsrc, c->nbnd, c->M, c->f32, st);
-    return 2 + (c->nbnd > 0);
+    return k + 2 + (c->nbnd > 0);
 }
 
 // The step with the MOOD fixed points driven from the host (one counter read per decrement).
@@ -628,6 +685,7 @@ void take_mood_stats(hcc_ctx *c) {
     c->mood_iters = int64_t(ms.iterations);
     c->flagged = int64_t(ms.flagged);
     c->inadmissible = int64_t(ms.inadmissible);
+    c->predicted = int64_t(ms.predicted);
 }
 
 hcc_status apply_positions(hcc_ctx *c, const double *src, bool full_search);
@@ -701,6 +759,8 @@ template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
     st = c->sync("step");
     if (st != HCC_OK) return st;
     take_mood_stats(c);
+    if (c->mood_stats_host->tc_error) return c->fail(HCC_ERR_TIMEOUT, "predictor: a tensor-core wait gave up");
+    c->feat_valid = c->capture_feat != 0;
     std::swap(c->rhos, c->cand);
     ++c->steps;
     c->launches_total += c->launches;
@@ -806,6 +866,8 @@ template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
     c->launches = G.launches + (nchk > 0 ? c->mood_iters * (G.body_launches / nchk) : 0);
     c->launches_total += c->launches;
     if (c->mood_stats_host->timeout) return c->fail(HCC_ERR_TIMEOUT, "MOOD fixed point reached the iteration cap");
+    if (c->mood_stats_host->tc_error) return c->fail(HCC_ERR_TIMEOUT, "predictor: a tensor-core wait gave up");
+    c->feat_valid = c->capture_feat != 0;
     std::swap(c->rhos, c->cand);
     ++c->steps;
     ++c->graph_steps;
@@ -813,6 +875,9 @@ template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
 }
 
 template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
+    c->feat_valid = false;
+    hcc_status lst = ensure_learn_buffers(c);
+    if (lst != HCC_OK) return lst;
     if (c->use_graphs && !c->prof && !c->moving()) {
         hcc_status st = run_step_graph<T>(c, dt);
         if (st != HCC_ERR_CUDA || c->graphs_failed) return st;
@@ -1535,6 +1600,7 @@ hcc_status hcc_get_counters(hcc_ctx *c, hcc_counters *out) {
     out->steps = c->steps;
     out->kernel_launches_total = c->launches_total;
     out->graph_steps = c->graph_steps;
+    out->predicted = c->predicted;
     out->min_neighbours_interior = c->min_nb_interior;
     return HCC_OK;
 }
@@ -1567,6 +1633,64 @@ hcc_status hcc_get_kernel_times(hcc_ctx *c, hcc_kernel_times *out, int reset) {
     if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
     *out = c->times;
     if (reset) c->times = hcc_kernel_times{};
+    return HCC_OK;
+}
+
+hcc_status hcc_set_predictor(hcc_ctx *c, hcc_mlp *mlp, double thr) {
+    if (!c) return HCC_ERR_INVALID;
+    if (mlp && !(thr > 0.0 && thr < 1.0)) return c->fail(HCC_ERR_INVALID, "predictor threshold outside (0, 1)");
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->drop_graphs();
+    c->mlp = mlp;
+    c->thr_logit = mlp ? float(std::log(thr / (1.0 - thr))) : 0.f;
+    return HCC_OK;
+}
+
+hcc_status hcc_set_feature_capture(hcc_ctx *c, int enable) {
+    if (!c) return HCC_ERR_INVALID;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->drop_graphs();
+    c->capture_feat = enable ? 1 : 0;
+    c->feat_valid = false;
+    return HCC_OK;
+}
+
+hcc_status hcc_download_features(hcc_ctx *c, float *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    if (!c->have_geom) { hcc_status gs = hcc_prepare_geometry(c); if (gs != HCC_OK) return gs; }
+    if (c->n == 0) return HCC_OK;
+    float *tmp = nullptr;
+    hcc_status st = c->alloc(tmp, size_t(c->n) * HCC_MLP_FEATURES, "features");
+    if (st != HCC_OK) return st;
+    if (!launch_features(feat_args(c, c->rhos), tmp, c->stream)) {
+        dfree(tmp);
+        return c->fail(HCC_ERR_UNSUPPORTED, "no feature kernel for this physics");
+    }
+    st = c->sync("features");
+    if (st == HCC_OK)
+        st = c->cuda(cudaMemcpy(out, tmp, size_t(c->n) * HCC_MLP_FEATURES * sizeof(float), cudaMemcpyDeviceToHost),
+                     "features");
+    dfree(tmp);
+    return st;
+}
+
+hcc_status hcc_download_predicted(hcc_ctx *c, uint8_t *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud");
+    if (!c->pred) {
+        std::memset(out, 0, size_t(c->n));
+        return HCC_OK;
+    }
+    return c->cuda(cudaMemcpy(out, c->pred, size_t(c->n), cudaMemcpyDeviceToHost), "predicted mask");
+}
+
+hcc_status hcc_mlp_collect(hcc_mlp *m, hcc_ctx *c) {
+    if (!m || !c) return c ? c->fail(HCC_ERR_INVALID, "null predictor") : HCC_ERR_INVALID;
+    if (!c->feat_valid || !c->feat)
+        return c->fail(HCC_ERR_STATE, "collect: the last step did not capture features (hcc_set_feature_capture)");
+    hcc_status st = mlp_append(m, c->feat, c->trig_step, c->bnd, c->n, c->stream);
+    if (st != HCC_OK) return c->fail(st, hcc_mlp_last_error(m));
     return HCC_OK;
 }
 

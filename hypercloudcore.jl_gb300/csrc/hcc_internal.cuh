@@ -413,6 +413,8 @@ void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int i
 struct MoodStats {
     unsigned long long iterations, flagged, inadmissible, timeout;
     unsigned int iter_in_checkpoint, pad;
+    unsigned long long predicted;     // particles the troubled-point predictor pre-lowered
+    unsigned int tc_error, pad2;      // a tensor-core wait of the predictor gave up
 };
 
 // One launch after a flux pass with the MOOD check: boundary conditions of the new candidate (first bc_blocks
@@ -439,5 +441,39 @@ struct DropArgs {
 void launch_drop_decide(const DropArgs &a, int is_f32, int drop_blocks, cudaStream_t s);
 void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
                         int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
+
+
+// ----------------------------------------------------------------------------------- learned predictor
+// Inputs of the stencil features (state in the context's precision, slot-major neighbour lists and offsets).
+struct FeatArgs {
+    const void *U;
+    int f32, D, M, pde;
+    int64_t n, npad;
+    const int32_t *cnt, *nidx;
+    const void *dist;                 // [(k*D + d) * npad + i], element type of U
+    const uint8_t *bnd;
+    float h, gm1;                     // min(dx); gamma - 1 (Euler)
+};
+// Device view of the network: BF16 images of W1 [64][24] and W2 [64][64] (row-major), the FP32 master parameters
+// (biases and w3 are read from it) and the input normalisation mean[24], inv_std[24].
+struct MlpWeights {
+    const uint16_t *W1, *W2;
+    const float *params, *norm;
+};
+// Outputs of the in-step prediction.
+struct PredictOut {
+    int8_t *orders;
+    int8_t lowered;                   // order of a predicted particle (one below the maximum)
+    uint8_t *pred;                    // [n] 0/1
+    float *logits;                    // [n] or nullptr
+    unsigned long long *count;        // predicted particles (accumulated)
+    float thr_logit;
+};
+bool launch_features(const FeatArgs &fa, float *out, cudaStream_t s);
+bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, int grid, unsigned *err,
+                    cudaStream_t s);
+MlpWeights mlp_weights(const hcc_mlp *m);
+hcc_status mlp_append(hcc_mlp *m, const float *feat, const uint8_t *labels, const uint8_t *bnd, int64_t n,
+                      cudaStream_t s);
 
 }  // namespace hcc

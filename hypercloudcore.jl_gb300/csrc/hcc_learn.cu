@@ -1,0 +1,1126 @@
+// hcc_learn.cu — learned troubled-point predictor: stencil features, a 24-64-64-1 GELU MLP on the tcgen05 tensor
+// cores (BF16 operands in shared memory, FP32 accumulators in TMEM), its training kernels (forward, backward, Adam)
+// and the hcc_mlp object of the C ABI.
+//
+// The predictor has no counterpart in the reference: its MOOD loop computes every particle at full order, checks,
+// drops and recomputes (src/TimeStepping/MOOD.jl:375-405, TimeSteppers.jl:454-477). Here the start-of-step state is
+// first run through the network and the particles it predicts to be troubled start the step one order lower; the
+// MOOD judge still checks every particle afterwards, so the predictor changes which particles are recomputed, not
+// what is admissible.
+//
+// Compiled with -fmad=false: the features follow the oracle's FP32 operation sequence bit for bit.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hcc_internal.cuh"
+#include "hcc_tc.cuh"
+
+namespace hcc {
+namespace {
+
+constexpr int NF = HCC_MLP_FEATURES;   // 24 features
+constexpr int KF = 32;                 // layer-1 K (features padded with zeros)
+constexpr int NH = HCC_MLP_HIDDEN;     // 64 hidden units per layer
+constexpr int OFF_W1 = 0, OFF_B1 = NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH,
+              OFF_B3 = OFF_W3 + NH, NPARAM = OFF_B3 + 1;
+static_assert(NPARAM == HCC_MLP_NPARAMS, "parameter layout");
+constexpr int PSTRIDE = NPARAM + 7;    // one training CTA's partial sums: gradient, then the loss at NPARAM
+constexpr uint32_t WAIT_LIMIT = 1u << 20;
+
+// --------------------------------------------------------------------------------------------- features
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ void quantities(const T *u, float gm1, float q[4]) {
+    if constexpr (PDE == HCC_PDE_EULER) {
+        const float rho = float(u[0]);
+        float msq = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const float md = float(u[1 + d]);
+            msq = msq + md * md;
+        }
+        const float E = float(u[D + 1]);
+        q[0] = rho;
+        q[1] = gm1 * (E - (0.5f * msq) / rho);
+        q[2] = sqrtf(msq);
+        q[3] = E;
+    } else {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) q[m] = float(u[m < M ? m : M - 1]);
+    }
+}
+
+__device__ __forceinline__ float clamp_feature(float f) {
+    if (!(f == f)) return 0.f;
+    return f > 8.f ? 8.f : (f < -8.f ? -8.f : f);
+}
+
+// The 24 features of particle i (definitions in hcc.h).
+template <typename T, int D, int M, int PDE>
+__device__ void point_features(const FeatArgs &a, int64_t i, float *f) {
+    const T *U = static_cast<const T *>(a.U);
+    const T *dist = static_cast<const T *>(a.dist);
+    const int64_t np = a.npad;
+    constexpr int NG = D * (D + 1) / 2;
+    float qi[4], qmax[4], qmin[4], s1[4], s2[4], b[4][D], G[NG];
+    quantities<T, D, M, PDE>(U + i * M, a.gm1, qi);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        qmax[m] = qi[m];
+        qmin[m] = qi[m];
+        s1[m] = 0.f;
+        s2[m] = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) b[m][d] = 0.f;
+    }
+#pragma unroll
+    for (int e = 0; e < NG; ++e) G[e] = 0.f;
+    const int c = a.cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int32_t j = a.nidx[int64_t(k) * np + i];
+        float x[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] = float(dist[(int64_t(k) * D + d) * np + i]);
+        int e = 0;
+#pragma unroll
+        for (int p = 0; p < D; ++p)
+#pragma unroll
+            for (int q = p; q < D; ++q) G[e++] += x[p] * x[q];
+        float qj[4];
+        quantities<T, D, M, PDE>(U + int64_t(j) * M, a.gm1, qj);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const float dq = qj[m] - qi[m];
+            s1[m] += dq;
+            s2[m] += dq * dq;
+#pragma unroll
+            for (int d = 0; d < D; ++d) b[m][d] += dq * x[d];
+            qmax[m] = qj[m] > qmax[m] ? qj[m] : qmax[m];
+            qmin[m] = qj[m] < qmin[m] ? qj[m] : qmin[m];
+        }
+    }
+    // least-squares gradient g = G^-1 b (cofactors; no solve where det <= 0)
+    float Gi[NG];
+    float det;
+    if constexpr (D == 1) {
+        det = G[0];
+        Gi[0] = 1.f;
+    } else if constexpr (D == 2) {
+        det = G[0] * G[2] - G[1] * G[1];
+        Gi[0] = G[2];
+        Gi[1] = -G[1];
+        Gi[2] = G[0];
+    } else {
+        Gi[0] = G[3] * G[5] - G[4] * G[4];
+        Gi[1] = G[2] * G[4] - G[1] * G[5];
+        Gi[2] = G[1] * G[4] - G[2] * G[3];
+        Gi[3] = G[0] * G[5] - G[2] * G[2];
+        Gi[4] = G[1] * G[2] - G[0] * G[4];
+        Gi[5] = G[0] * G[3] - G[1] * G[1];
+        det = (G[0] * Gi[0] + G[1] * Gi[1]) + G[2] * Gi[2];
+    }
+    const bool solve = det > 0.f;
+    const float h = a.h;
+    const float ic = c > 0 ? 1.f / float(c) : 0.f;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        float g[D];
+        if constexpr (D == 1) {
+            g[0] = solve ? b[m][0] / det : 0.f;
+        } else if constexpr (D == 2) {
+            g[0] = solve ? (Gi[0] * b[m][0] + Gi[1] * b[m][1]) / det : 0.f;
+            g[1] = solve ? (Gi[1] * b[m][0] + Gi[2] * b[m][1]) / det : 0.f;
+        } else {
+            g[0] = solve ? ((Gi[0] * b[m][0] + Gi[1] * b[m][1]) + Gi[2] * b[m][2]) / det : 0.f;
+            g[1] = solve ? ((Gi[1] * b[m][0] + Gi[3] * b[m][1]) + Gi[4] * b[m][2]) / det : 0.f;
+            g[2] = solve ? ((Gi[2] * b[m][0] + Gi[4] * b[m][1]) + Gi[5] * b[m][2]) / det : 0.f;
+        }
+        float bgb = 0.f, gg = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            bgb += b[m][d] * g[d];
+            gg += g[d] * g[d];
+        }
+        const float r = qmax[m] - qmin[m];
+        const float sc = fabsf(qmax[m]) + fabsf(qmin[m]);
+        float *o = f + 6 * m;
+        o[0] = sc > 0.f ? r / sc : 0.f;
+        if (c > 0 && r > 1e-6f * sc) {
+            const float ir = 1.f / r;
+            const float mean = s1[m] * ic;
+            const float res = (s2[m] - bgb) * ic;
+            const float var = s2[m] * ic - mean * mean;
+            o[1] = ((2.f * qi[m] - qmax[m]) - qmin[m]) * ir;
+            o[2] = -(mean * ir);
+            o[3] = (res > 0.f ? sqrtf(res) : 0.f) * ir;
+            o[4] = (sqrtf(gg) * h) * ir;
+            o[5] = (var > 0.f ? sqrtf(var) : 0.f) * ir;
+        } else {
+            o[1] = o[2] = o[3] = o[4] = o[5] = 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 6; ++t) o[t] = clamp_feature(o[t]);
+    }
+}
+
+template <typename T, int D, int M, int PDE>
+__global__ void __launch_bounds__(128) k_features(FeatArgs a, float *out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    float f[NF];
+    point_features<T, D, M, PDE>(a, i, f);
+#pragma unroll
+    for (int t = 0; t < NF; ++t) out[i * NF + t] = f[t];
+}
+
+// --------------------------------------------------------------------------------------------- the network
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * (0.39894228040143268f * expf(-0.5f * x * x));
+}
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+__device__ __forceinline__ void store_bf16(uint8_t *p, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(p) = __float2bfloat16_rn(v);
+}
+__device__ __forceinline__ float softplus(float x) { return fmaxf(x, 0.f) + log1pf(expf(-fabsf(x))); }
+
+// fp32 copies of the small parameters in shared memory
+constexpr int P_B1 = 0, P_B2 = 64, P_W3 = 128, P_B3 = 192, P_MEAN = 196, P_ISTD = 220, P_COUNT = 256;
+
+__device__ void load_small_params(const MlpWeights &w, float *par) {
+    for (int e = threadIdx.x; e < NH; e += blockDim.x) {
+        par[P_B1 + e] = w.params[OFF_B1 + e];
+        par[P_B2 + e] = w.params[OFF_B2 + e];
+        par[P_W3 + e] = w.params[OFF_W3 + e];
+    }
+    for (int e = threadIdx.x; e < NF; e += blockDim.x) {
+        par[P_MEAN + e] = w.norm[e];
+        par[P_ISTD + e] = w.norm[NF + e];
+    }
+    if (threadIdx.x == 0) par[P_B3] = w.params[OFF_B3];
+}
+
+// BF16 weight images in the K-major operand layouts: W1 as B of layer 1 (N = hidden, K = feature),
+// W2 as B of layer 2 (N = output unit, K = input unit) and, when w2n != nullptr, as B of the backward product
+// dH1 = dZ2 W2 (N = input unit, K = output unit).
+__device__ void load_weight_images(const MlpWeights &w, uint8_t *w1, uint8_t *w2, uint8_t *w2n) {
+    const __nv_bfloat16 *W1 = reinterpret_cast<const __nv_bfloat16 *>(w.W1);
+    const __nv_bfloat16 *W2 = reinterpret_cast<const __nv_bfloat16 *>(w.W2);
+    for (int e = threadIdx.x; e < NH * KF; e += blockDim.x) {
+        const int h = e / KF, f = e % KF;
+        *reinterpret_cast<__nv_bfloat16 *>(w1 + tc::kmajor_offset(h, f, KF)) =
+            f < NF ? W1[h * NF + f] : __float2bfloat16_rn(0.f);
+    }
+    for (int e = threadIdx.x; e < NH * NH; e += blockDim.x) {
+        const int o = e / NH, h = e % NH;
+        *reinterpret_cast<__nv_bfloat16 *>(w2 + tc::kmajor_offset(o, h, NH)) = W2[e];
+        if (w2n) *reinterpret_cast<__nv_bfloat16 *>(w2n + tc::kmajor_offset(h, o, NH)) = W2[e];
+    }
+}
+
+// Normalised features of one row into the row's 16-byte core-matrix segments of a K = 32 operand.
+__device__ __forceinline__ void store_feature_row(uint8_t *tile, int r, const float *f, bool valid, const float *par,
+                                                  float *xn) {
+#pragma unroll
+    for (int c8 = 0; c8 < KF / 8; ++c8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int f0 = c8 * 8 + 2 * q;
+            const float x0 = (valid && f0 < NF) ? (f[f0] - par[P_MEAN + f0]) * par[P_ISTD + f0] : 0.f;
+            const float x1 = (valid && f0 + 1 < NF) ? (f[f0 + 1] - par[P_MEAN + f0 + 1]) * par[P_ISTD + f0 + 1] : 0.f;
+            pk[q] = pack_bf16(x0, x1);
+            if (xn && f0 < NF) {
+                xn[f0] = x0;
+                xn[f0 + 1] = x1;
+            }
+        }
+        *reinterpret_cast<uint4 *>(tile + tc::kmajor_offset(r, c8 * 8, KF)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+}
+
+// Inference: shared-memory layout (bytes) of one CTA. The activation tile holds X (128 x 32) for layer 1, then H1
+// (128 x 64) for layer 2; TMEM columns [0, 64) hold Z1, then Z2.
+struct InferSmem {
+    static constexpr uint32_t W1 = 0;
+    static constexpr uint32_t W2 = W1 + NH * KF * 2;
+    static constexpr uint32_t ACT = W2 + NH * NH * 2;
+    static constexpr uint32_t PAR = ACT + 128 * NH * 2;
+    static constexpr uint32_t BAR = PAR + P_COUNT * 4;
+    static constexpr uint32_t SIZE = BAR + 64 + 1024;   // + slack past the last operand
+};
+static_assert(InferSmem::SIZE <= 48 * 1024, "inference tiles launch without a shared-memory opt-in (graph capture)");
+
+// Persistent inference over 128-row tiles: Src supplies the features of row i and consumes its logit.
+template <class Src>
+__global__ void __launch_bounds__(128) k_mlp_infer(Src src, MlpWeights w, int ntiles, unsigned *err) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    const int r = threadIdx.x, warp = r >> 5;
+    float *par = reinterpret_cast<float *>(sm + InferSmem::PAR);
+    load_weight_images(w, sm + InferSmem::W1, sm + InferSmem::W2, nullptr);
+    load_small_params(w, par);
+    const uint32_t bar = tc::smem_addr(sm + InferSmem::BAR);
+    if (warp == 0) tc::tmem_alloc(bar + 8, 64);
+    if (r == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + InferSmem::BAR + 8);
+    const uint32_t tl = tmem + (uint32_t(warp * 32) << 16);
+    const uint32_t aACT = tc::smem_addr(sm + InferSmem::ACT), aW1 = tc::smem_addr(sm + InferSmem::W1),
+                   aW2 = tc::smem_addr(sm + InferSmem::W2);
+    constexpr uint32_t ID = tc::idesc_bf16(128, NH);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t i = int64_t(tile) * 128 + r;
+        float f[NF];
+        const bool valid = src.features(i, f);
+        store_feature_row(sm + InferSmem::ACT, r, f, valid, par, nullptr);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (r == 0) {
+#pragma unroll
+            for (int s = 0; s < KF / 16; ++s)
+                tc::mma_bf16(tmem, tc::kslice_desc(aACT, KF, s), tc::kslice_desc(aW1, KF, s), ID, s > 0);
+            tc::commit(bar);
+        }
+        ok = tc::mbar_wait(bar, phase, WAIT_LIMIT) && ok;
+        phase ^= 1u;
+        tc::fence_after_sync();
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float z[16];
+            tc::tmem_ld16(tl + uint32_t(c * 16), z);
+            uint32_t pk[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                pk[q] = pack_bf16(gelu(z[2 * q] + par[P_B1 + c * 16 + 2 * q]),
+                                  gelu(z[2 * q + 1] + par[P_B1 + c * 16 + 2 * q + 1]));
+            *reinterpret_cast<uint4 *>(sm + InferSmem::ACT + tc::kmajor_offset(r, c * 16, NH)) =
+                make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4 *>(sm + InferSmem::ACT + tc::kmajor_offset(r, c * 16 + 8, NH)) =
+                make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (r == 0) {
+#pragma unroll
+            for (int s = 0; s < NH / 16; ++s)
+                tc::mma_bf16(tmem, tc::kslice_desc(aACT, NH, s), tc::kslice_desc(aW2, NH, s), ID, s > 0);
+            tc::commit(bar);
+        }
+        ok = tc::mbar_wait(bar, phase, WAIT_LIMIT) && ok;
+        phase ^= 1u;
+        tc::fence_after_sync();
+        float logit = par[P_B3];
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float z[16];
+            tc::tmem_ld16(tl + uint32_t(c * 16), z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) logit += par[P_W3 + c * 16 + q] * gelu(z[q] + par[P_B2 + c * 16 + q]);
+        }
+        src.emit(i, valid, logit);
+        tc::fence_before_sync();
+    }
+    if (!ok && err) atomicOr(err, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 64);
+    }
+}
+
+// Features from the cloud; pre-lowers the predicted interior particles.
+template <typename T, int D, int M, int PDE> struct CloudSrc {
+    FeatArgs a;
+    PredictOut o;
+    __device__ bool features(int64_t i, float *f) const {
+        if (i >= a.n || a.bnd[i]) return false;
+        point_features<T, D, M, PDE>(a, i, f);
+        return true;
+    }
+    __device__ void emit(int64_t i, bool valid, float logit) const {
+        const bool hit = valid && logit > o.thr_logit;
+        if (i < a.n) {
+            o.pred[i] = hit ? 1 : 0;
+            if (o.logits) o.logits[i] = valid ? logit : 0.f;
+            if (hit) o.orders[i] = o.lowered;
+        }
+        const unsigned bits = __ballot_sync(0xffffffffu, hit);
+        if ((threadIdx.x & 31) == 0 && bits) atomicAdd(o.count, (unsigned long long)__popc(bits));
+    }
+};
+
+// Features from rows X[start + i][24]; logits out and/or confusion counts {tp, fp, fn, tn} against labels Y.
+struct RowSrc {
+    const float *X;
+    const uint8_t *Y;
+    int64_t start, n;
+    float *logits;
+    unsigned long long *counts;
+    float thr_logit;
+    __device__ bool features(int64_t i, float *f) const {
+        if (i >= n) return false;
+#pragma unroll
+        for (int t = 0; t < NF; ++t) f[t] = X[(start + i) * NF + t];
+        return true;
+    }
+    __device__ void emit(int64_t i, bool valid, float logit) const {
+        if (valid && logits) logits[i] = logit;
+        if (counts) {
+            const bool p = valid && logit > thr_logit, y = valid && Y[start + i] != 0;
+            const unsigned tp = __ballot_sync(0xffffffffu, valid && p && y);
+            const unsigned fp = __ballot_sync(0xffffffffu, valid && p && !y);
+            const unsigned fn = __ballot_sync(0xffffffffu, valid && !p && y);
+            const unsigned tn = __ballot_sync(0xffffffffu, valid && !p && !y);
+            if ((threadIdx.x & 31) == 0) {
+                if (tp) atomicAdd(counts + 0, (unsigned long long)__popc(tp));
+                if (fp) atomicAdd(counts + 1, (unsigned long long)__popc(fp));
+                if (fn) atomicAdd(counts + 2, (unsigned long long)__popc(fn));
+                if (tn) atomicAdd(counts + 3, (unsigned long long)__popc(tn));
+            }
+        }
+    }
+};
+
+// --------------------------------------------------------------------------------------------- training
+// One CTA of 128 threads runs mini-batch tiles of 128 rows: layer 1, layer 2 (forward), the loss, dH1 = dZ2 W2
+// (backward) and the weight gradients of both layers as ONE accumulating product over the tiles:
+//   [dZ2^T ; dZ1^T] (128 x rows) * [H1 | X | 1]  (rows x 112) -> TMEM columns [128, 240):
+// rows 0-63 give dW2 (columns 0-63) and db2 (column 96), rows 64-127 give dW1 (columns 64-87) and db1 (column 96).
+struct TrainSmem {
+    static constexpr uint32_t W1 = 0;                     // 64 x 32
+    static constexpr uint32_t W2 = W1 + NH * KF * 2;      // 64 x 64 (o, h)
+    static constexpr uint32_t W2N = W2 + NH * NH * 2;     // 64 x 64 (h, o)
+    static constexpr uint32_t X = W2N + NH * NH * 2;      // 128 x 32
+    static constexpr uint32_t H1 = X + 128 * KF * 2;      // 128 x 64
+    static constexpr uint32_t DZ2 = H1 + 128 * NH * 2;    // 128 x 64
+    static constexpr uint32_t GA = DZ2 + 128 * NH * 2;    // 128 x 128 (K = rows of the tile)
+    static constexpr uint32_t GB = GA + 128 * 128 * 2;    // 112 x 128
+    static constexpr uint32_t PAR = GB + 112 * 128 * 2;
+    static constexpr uint32_t BAR = PAR + P_COUNT * 4;
+    static constexpr uint32_t SIZE = BAR + 64 + 1024;
+};
+constexpr int GB_ROWS = 112, GB_X = 64, GB_ONE = 96;
+constexpr uint32_t T_Z1 = 0, T_Z2 = 64, T_G = 128;   // TMEM columns
+
+struct TrainArgs {
+    MlpWeights w;
+    const float *X;
+    const uint8_t *Y;
+    int64_t nrows;            // rows to draw from (random mode) / rows of the batch (identity mode)
+    int64_t nbatch;
+    int random;               // 1: rows drawn uniformly with replacement; 0: rows 0..nbatch-1
+    unsigned long long seed, iter;
+    float inv_batch, pos_weight;
+    float *part;              // [gridDim.x][PSTRIDE]
+    unsigned *err;
+};
+
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(128) k_train(TrainArgs A, int ntiles) {
+    extern __shared__ __align__(128) uint8_t sm[];
+    const int r = threadIdx.x, warp = r >> 5;
+    float *par = reinterpret_cast<float *>(sm + TrainSmem::PAR);
+    load_weight_images(A.w, sm + TrainSmem::W1, sm + TrainSmem::W2, sm + TrainSmem::W2N);
+    load_small_params(A.w, par);
+    // constant rows of the gradient operand: features 24-31 (zero), the ones row, zero rows 97-111
+    for (int e = r; e < (GB_ROWS - (GB_X + NF)) * 128; e += 128) {
+        const int row = GB_X + NF + e / 128, col = e % 128;
+        store_bf16(sm + TrainSmem::GB + tc::kmajor_offset(row, col, 128), row == GB_ONE ? 1.f : 0.f);
+    }
+    const uint32_t bar = tc::smem_addr(sm + TrainSmem::BAR);
+    if (warp == 0) tc::tmem_alloc(bar + 8, 256);
+    if (r == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(sm + TrainSmem::BAR + 8);
+    const uint32_t tl = tmem + (uint32_t(warp * 32) << 16);
+    const uint32_t aW1 = tc::smem_addr(sm + TrainSmem::W1), aW2 = tc::smem_addr(sm + TrainSmem::W2),
+                   aW2N = tc::smem_addr(sm + TrainSmem::W2N), aX = tc::smem_addr(sm + TrainSmem::X),
+                   aH1 = tc::smem_addr(sm + TrainSmem::H1), aDZ2 = tc::smem_addr(sm + TrainSmem::DZ2),
+                   aGA = tc::smem_addr(sm + TrainSmem::GA), aGB = tc::smem_addr(sm + TrainSmem::GB);
+    uint32_t phase = 0;
+    bool ok = true;
+    float dw3[NH];
+#pragma unroll
+    for (int o = 0; o < NH; ++o) dw3[o] = 0.f;
+    float db3 = 0.f, loss = 0.f;
+    int done = 0;
+    auto sync_then = [&](auto issue) {
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (r == 0) {
+            issue();
+            tc::commit(bar);
+        }
+        ok = tc::mbar_wait(bar, phase, WAIT_LIMIT) && ok;
+        phase ^= 1u;
+        tc::fence_after_sync();
+    };
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++done) {
+        const int64_t bidx = int64_t(tile) * 128 + r;
+        const bool valid = bidx < A.nbatch;
+        int64_t row = 0;
+        if (valid)
+            row = A.random ? int64_t(mix64(A.seed ^ mix64(A.iter * 0x100000001B3ull + uint64_t(bidx))) %
+                                     uint64_t(A.nrows))
+                           : bidx;
+        float f[NF], xn[NF];
+#pragma unroll
+        for (int t = 0; t < NF; ++t) f[t] = valid ? A.X[row * NF + t] : 0.f;
+        const float y = (valid && A.Y[row]) ? 1.f : 0.f;
+        store_feature_row(sm + TrainSmem::X, r, f, valid, par, xn);
+#pragma unroll
+        for (int t = 0; t < NF; ++t)
+            store_bf16(sm + TrainSmem::GB + tc::kmajor_offset(GB_X + t, r, 128), valid ? xn[t] : 0.f);
+        // layer 1
+        sync_then([&] {
+            for (int s = 0; s < KF / 16; ++s)
+                tc::mma_bf16(tmem + T_Z1, tc::kslice_desc(aX, KF, s), tc::kslice_desc(aW1, KF, s),
+                             tc::idesc_bf16(128, NH), s > 0);
+        });
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float z[16];
+            tc::tmem_ld16(tl + T_Z1 + uint32_t(c * 16), z);
+            uint32_t pk[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int h0 = c * 16 + 2 * q;
+                const float g0 = gelu(z[2 * q] + par[P_B1 + h0]), g1 = gelu(z[2 * q + 1] + par[P_B1 + h0 + 1]);
+                pk[q] = pack_bf16(g0, g1);
+                store_bf16(sm + TrainSmem::GB + tc::kmajor_offset(h0, r, 128), g0);
+                store_bf16(sm + TrainSmem::GB + tc::kmajor_offset(h0 + 1, r, 128), g1);
+            }
+            *reinterpret_cast<uint4 *>(sm + TrainSmem::H1 + tc::kmajor_offset(r, c * 16, NH)) =
+                make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4 *>(sm + TrainSmem::H1 + tc::kmajor_offset(r, c * 16 + 8, NH)) =
+                make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+        // layer 2
+        sync_then([&] {
+            for (int s = 0; s < NH / 16; ++s)
+                tc::mma_bf16(tmem + T_Z2, tc::kslice_desc(aH1, NH, s), tc::kslice_desc(aW2, NH, s),
+                             tc::idesc_bf16(128, NH), s > 0);
+        });
+        float logit = par[P_B3];
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float z[16];
+            tc::tmem_ld16(tl + T_Z2 + uint32_t(c * 16), z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) logit += par[P_W3 + c * 16 + q] * gelu(z[q] + par[P_B2 + c * 16 + q]);
+        }
+        // weighted binary cross-entropy with logits, mean over the batch
+        const float p = 1.f / (1.f + expf(-logit));
+        const float dz = valid ? (y > 0.f ? A.pos_weight * (p - 1.f) : p) * A.inv_batch : 0.f;
+        if (valid) loss += (y > 0.f ? A.pos_weight * softplus(-logit) : softplus(logit)) * A.inv_batch;
+        db3 += dz;
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float z[16];
+            tc::tmem_ld16(tl + T_Z2 + uint32_t(c * 16), z);
+            uint32_t pk[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float d2[2];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int o = c * 16 + 2 * q + e;
+                    const float zz = z[2 * q + e] + par[P_B2 + o];
+                    dw3[o] += dz * gelu(zz);
+                    d2[e] = (dz * par[P_W3 + o]) * gelu_grad(zz);
+                    store_bf16(sm + TrainSmem::GA + tc::kmajor_offset(o, r, 128), d2[e]);
+                }
+                pk[q] = pack_bf16(d2[0], d2[1]);
+            }
+            *reinterpret_cast<uint4 *>(sm + TrainSmem::DZ2 + tc::kmajor_offset(r, c * 16, NH)) =
+                make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4 *>(sm + TrainSmem::DZ2 + tc::kmajor_offset(r, c * 16 + 8, NH)) =
+                make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+        // dH1 = dZ2 W2 into the Z2 columns
+        sync_then([&] {
+            for (int s = 0; s < NH / 16; ++s)
+                tc::mma_bf16(tmem + T_Z2, tc::kslice_desc(aDZ2, NH, s), tc::kslice_desc(aW2N, NH, s),
+                             tc::idesc_bf16(128, NH), s > 0);
+        });
+#pragma unroll
+        for (int c = 0; c < NH / 16; ++c) {
+            float dh[16], z[16];
+            tc::tmem_ld16(tl + T_Z2 + uint32_t(c * 16), dh);
+            tc::tmem_ld16(tl + T_Z1 + uint32_t(c * 16), z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int hh = c * 16 + q;
+                store_bf16(sm + TrainSmem::GA + tc::kmajor_offset(NH + hh, r, 128),
+                           dh[q] * gelu_grad(z[q] + par[P_B1 + hh]));
+            }
+        }
+        // weight and bias gradients of both layers, accumulated over this CTA's tiles
+        const int acc = done > 0;
+        sync_then([&] {
+            for (int s = 0; s < 128 / 16; ++s)
+                tc::mma_bf16(tmem + T_G, tc::kslice_desc(aGA, 128, s), tc::kslice_desc(aGB, 128, s),
+                             tc::idesc_bf16(128, GB_ROWS), (acc || s > 0) ? 1u : 0u);
+        });
+        tc::fence_before_sync();
+    }
+    float *part = A.part + int64_t(blockIdx.x) * PSTRIDE;
+    // gradient rows of the accumulator
+#pragma unroll 1
+    for (int c = 0; c < GB_ROWS / 16; ++c) {
+        float g[16];
+        tc::tmem_ld16(tl + T_G + uint32_t(c * 16), g);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int col = c * 16 + q;
+            const float v = done > 0 ? g[q] : 0.f;
+            if (r < NH) {
+                if (col < NH) part[OFF_W2 + r * NH + col] = v;
+                else if (col == GB_ONE) part[OFF_B2 + r] = v;
+            } else {
+                const int hh = r - NH;
+                if (col >= GB_X && col < GB_X + NF) part[OFF_W1 + hh * NF + (col - GB_X)] = v;
+                else if (col == GB_ONE) part[OFF_B1 + hh] = v;
+            }
+        }
+    }
+    // dw3, db3 and the loss: reductions over the CTA's rows (the GA tile is free now)
+    __syncthreads();
+    float *red = reinterpret_cast<float *>(sm + TrainSmem::GA);
+#pragma unroll
+    for (int o = 0; o < NH; ++o) red[o * 128 + r] = dw3[o];
+    red[NH * 128 + r] = db3;
+    red[(NH + 1) * 128 + r] = loss;
+    __syncthreads();
+    if (r < NH + 2) {
+        float s = 0.f;
+        for (int q = 0; q < 128; ++q) s += red[r * 128 + q];
+        if (r < NH) part[OFF_W3 + r] = s;
+        else if (r == NH) part[OFF_B3] = s;
+        else part[NPARAM] = s;
+    }
+    if (!ok && A.err) atomicOr(A.err, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 256);
+    }
+}
+
+// Sum of the CTAs' partials (fixed order: deterministic), then Adam (update != 0) and the BF16 weight images.
+__global__ void k_adam(float *params, float *m, float *v, const float *part, int nparts, int update, float lr,
+                       float b1, float b2, float eps, float c1, float c2, uint16_t *W1b, uint16_t *W2b, float *grad,
+                       float *loss) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > NPARAM) return;
+    float g = 0.f;
+    for (int q = 0; q < nparts; ++q) g += part[int64_t(q) * PSTRIDE + p];
+    if (p == NPARAM) {
+        if (loss) *loss = g;
+        return;
+    }
+    if (grad) grad[p] = g;
+    float w = params[p];
+    if (update) {
+        const float mm = b1 * m[p] + (1.f - b1) * g;
+        const float vv = b2 * v[p] + (1.f - b2) * g * g;
+        m[p] = mm;
+        v[p] = vv;
+        w = w - lr * (mm * c1) / (sqrtf(vv * c2) + eps);
+        params[p] = w;
+    }
+    const __nv_bfloat16 wb = __float2bfloat16_rn(w);
+    if (p < OFF_B1) W1b[p - OFF_W1] = *reinterpret_cast<const uint16_t *>(&wb);
+    else if (p >= OFF_W2 && p < OFF_B2) W2b[p - OFF_W2] = *reinterpret_cast<const uint16_t *>(&wb);
+}
+
+// Training-set append: every flagged interior particle, unflagged ones with probability keep.
+__global__ void k_collect(const float *feat, const uint8_t *labels, const uint8_t *bnd, int64_t n, float *X,
+                          uint8_t *Y, int64_t cap, unsigned long long *counters, unsigned long long salt,
+                          float keep) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool take = false, y = false;
+    if (i < n && !bnd[i]) {
+        y = labels[i] != 0;
+        const float u = float(mix64(salt ^ uint64_t(i)) >> 40) * (1.f / 16777216.f);
+        take = y || u < keep;
+    }
+    const unsigned bits = __ballot_sync(0xffffffffu, take);
+    if (!bits) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == __ffs(bits) - 1) base = atomicAdd(counters, (unsigned long long)__popc(bits));
+    base = __shfl_sync(0xffffffffu, base, __ffs(bits) - 1);
+    if (take) {
+        const unsigned long long slot = base + __popc(bits & ((1u << lane) - 1u));
+        if (int64_t(slot) < cap) {
+#pragma unroll
+            for (int t = 0; t < NF; ++t) X[int64_t(slot) * NF + t] = feat[i * NF + t];
+            Y[slot] = y ? 1 : 0;
+            if (y) atomicAdd(counters + 1, 1ull);
+        }
+    }
+}
+
+// Per-feature sums and sums of squares (FP64) of rows [0, n).
+__global__ void k_norm_sums(const float *X, int64_t n, double *sums) {
+    __shared__ double s[2 * NF];
+    for (int t = threadIdx.x; t < 2 * NF; t += blockDim.x) s[t] = 0.0;
+    __syncthreads();
+    double a[NF], q[NF];
+#pragma unroll
+    for (int t = 0; t < NF; ++t) a[t] = q[t] = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+#pragma unroll
+        for (int t = 0; t < NF; ++t) {
+            const double v = X[i * NF + t];
+            a[t] += v;
+            q[t] += v * v;
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < NF; ++t) {
+        atomicAdd(&s[t], a[t]);
+        atomicAdd(&s[NF + t], q[t]);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 2 * NF; t += blockDim.x) atomicAdd(&sums[t], s[t]);
+}
+
+// ------------------------------------------------------------------------------------------ dispatch
+template <typename V> struct Tag { using type = V; };
+template <int V> struct IntC { static constexpr int value = V; };
+
+template <typename F> bool with_physics(int f32, int D, int M, int pde, F &&f) {
+    auto go = [&](auto t) -> bool {
+        if (pde == HCC_PDE_EULER) {
+            if (D == 1 && M == 3) return f(t, IntC<1>{}, IntC<3>{}, IntC<HCC_PDE_EULER>{}), true;
+            if (D == 2 && M == 4) return f(t, IntC<2>{}, IntC<4>{}, IntC<HCC_PDE_EULER>{}), true;
+            if (D == 3 && M == 5) return f(t, IntC<3>{}, IntC<5>{}, IntC<HCC_PDE_EULER>{}), true;
+            return false;
+        }
+        if (pde == HCC_PDE_BGK) {
+            if (D == 2 && M == 16) return f(t, IntC<2>{}, IntC<16>{}, IntC<HCC_PDE_BGK>{}), true;
+            if (D == 1 && M == 2) return f(t, IntC<1>{}, IntC<2>{}, IntC<HCC_PDE_BGK>{}), true;
+            return false;
+        }
+        if (D == 1 && M == 1) return f(t, IntC<1>{}, IntC<1>{}, IntC<HCC_PDE_ADVECTION>{}), true;
+        if (D == 2 && M == 1) return f(t, IntC<2>{}, IntC<1>{}, IntC<HCC_PDE_ADVECTION>{}), true;
+        if (D == 3 && M == 1) return f(t, IntC<3>{}, IntC<1>{}, IntC<HCC_PDE_ADVECTION>{}), true;
+        if (D == 2 && M == 2) return f(t, IntC<2>{}, IntC<2>{}, IntC<HCC_PDE_ADVECTION>{}), true;
+        return false;
+    };
+    return f32 ? go(Tag<float>{}) : go(Tag<double>{});
+}
+
+template <class Src> void launch_infer(const Src &src, const MlpWeights &w, int64_t n, int grid, unsigned *err,
+                                       cudaStream_t s) {
+    const int ntiles = int((n + 127) / 128);
+    if (ntiles == 0) return;
+    k_mlp_infer<Src><<<std::max(1, std::min(grid, ntiles)), 128, InferSmem::SIZE, s>>>(src, w, ntiles, err);
+}
+
+}  // namespace
+
+bool launch_features(const FeatArgs &fa, float *out, cudaStream_t s) {
+    if (fa.n == 0) return true;
+    return with_physics(fa.f32, fa.D, fa.M, fa.pde, [&](auto t, auto d, auto m, auto p) {
+        using T = typename decltype(t)::type;
+        k_features<T, decltype(d)::value, decltype(m)::value, decltype(p)::value>
+            <<<unsigned((fa.n + 127) / 128), 128, 0, s>>>(fa, out);
+    });
+}
+
+bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, int grid, unsigned *err,
+                    cudaStream_t s) {
+    return with_physics(fa.f32, fa.D, fa.M, fa.pde, [&](auto t, auto d, auto m, auto p) {
+        using T = typename decltype(t)::type;
+        CloudSrc<T, decltype(d)::value, decltype(m)::value, decltype(p)::value> src{fa, po};
+        launch_infer(src, w, fa.n, grid, err, s);
+    });
+}
+
+}  // namespace hcc
+
+// ============================================================================================== C ABI
+using namespace hcc;
+
+struct hcc_mlp {
+    hcc_mlp_config cfg{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int sms = 1;
+    float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr, *norm = nullptr, *part = nullptr,
+          *grad = nullptr, *loss = nullptr;
+    uint16_t *W1b = nullptr, *W2b = nullptr;
+    float *X = nullptr;
+    uint8_t *Y = nullptr;
+    unsigned long long *counters = nullptr;   // [0] rows appended, [1] flagged rows kept, [2..5] confusion counts
+    unsigned *d_err = nullptr;
+    double *d_sums = nullptr;
+    float *sX = nullptr, *sL = nullptr;       // scratch for host rows
+    uint8_t *sY = nullptr;
+    int64_t scap = 0;
+    int64_t adam_t = 0;
+    unsigned long long collect_calls = 0;
+
+    hcc_status fail(hcc_status st, const std::string &m) {
+        err = m;
+        return st;
+    }
+    hcc_status cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return HCC_OK;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return HCC_ERR_CUDA;
+    }
+    MlpWeights weights() const {
+        MlpWeights w;
+        w.W1 = W1b;
+        w.W2 = W2b;
+        w.params = params;
+        w.norm = norm;
+        return w;
+    }
+    int64_t rows() const {
+        unsigned long long h = 0;
+        cudaMemcpy(&h, counters, sizeof(h), cudaMemcpyDeviceToHost);
+        return std::min<int64_t>(int64_t(h), cfg.capacity);
+    }
+    hcc_status check_err(const char *what) {
+        unsigned h = 0;
+        hcc_status st = cuda(cudaMemcpy(&h, d_err, sizeof(h), cudaMemcpyDeviceToHost), what);
+        if (st != HCC_OK) return st;
+        if (h) {
+            cudaMemset(d_err, 0, sizeof(unsigned));
+            return fail(HCC_ERR_TIMEOUT, std::string(what) + ": a tensor-core wait gave up");
+        }
+        return HCC_OK;
+    }
+    hcc_status refresh_images() {   // BF16 weight images from the master, without an update
+        k_adam<<<(NPARAM + 1 + 255) / 256, 256, 0, stream>>>(params, adam_m, adam_v, part, 0, 0, 0.f, 0.f, 0.f,
+                                                               0.f, 0.f, 0.f, W1b, W2b, nullptr, nullptr);
+        return cuda(cudaStreamSynchronize(stream), "weight images");
+    }
+    hcc_status scratch(int64_t n) {
+        if (n <= scap) return HCC_OK;
+        if (sX) cudaFree(sX);
+        if (sY) cudaFree(sY);
+        if (sL) cudaFree(sL);
+        sX = nullptr; sY = nullptr; sL = nullptr; scap = 0;
+        hcc_status st = cuda(cudaMalloc(&sX, size_t(n) * NF * sizeof(float)), "row scratch");
+        if (st == HCC_OK) st = cuda(cudaMalloc(&sY, size_t(n)), "row scratch");
+        if (st == HCC_OK) st = cuda(cudaMalloc(&sL, size_t(n) * sizeof(float)), "row scratch");
+        if (st == HCC_OK) scap = n;
+        return st;
+    }
+    ~hcc_mlp() {
+        for (void *p : {(void *)params, (void *)adam_m, (void *)adam_v, (void *)norm, (void *)part, (void *)grad,
+                        (void *)loss, (void *)W1b, (void *)W2b, (void *)X, (void *)Y, (void *)counters,
+                        (void *)d_err, (void *)d_sums, (void *)sX, (void *)sY, (void *)sL})
+            if (p) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace hcc {
+MlpWeights mlp_weights(const hcc_mlp *m) { return m->weights(); }
+
+hcc_status mlp_append(hcc_mlp *m, const float *feat, const uint8_t *labels, const uint8_t *bnd, int64_t n,
+                      cudaStream_t s) {
+    if (n == 0) return HCC_OK;
+    const unsigned long long salt = mix64(m->cfg.seed ^ (0xC0FFEEull + m->collect_calls++));
+    k_collect<<<unsigned((n + 255) / 256), 256, 0, s>>>(feat, labels, bnd, n, m->X, m->Y, m->cfg.capacity,
+                                                         m->counters, salt, float(m->cfg.neg_keep));
+    return m->cuda(cudaStreamSynchronize(s), "training-set append");
+}
+}  // namespace hcc
+
+namespace {
+uint64_t host_mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+}  // namespace
+
+extern "C" {
+
+hcc_status hcc_mlp_create(const hcc_mlp_config *cfg, hcc_mlp **out) {
+    if (!cfg || !out) return HCC_ERR_INVALID;
+    *out = nullptr;
+    if (cfg->capacity < 0 || !(cfg->neg_keep >= 0.0 && cfg->neg_keep <= 1.0) || !(cfg->lr > 0.0) ||
+        !(cfg->beta1 >= 0.0 && cfg->beta1 < 1.0) || !(cfg->beta2 >= 0.0 && cfg->beta2 < 1.0) ||
+        !(cfg->adam_eps > 0.0) || !(cfg->pos_weight > 0.0))
+        return HCC_ERR_INVALID;
+    hcc_mlp *m = new hcc_mlp();
+    m->cfg = *cfg;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, dev);
+    m->sms = std::max(1, m->sms);
+    hcc_status st = m->cuda(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "stream");
+    auto A = [&](auto *&p, size_t count, const char *what) {
+        if (st == HCC_OK) st = m->cuda(cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(count, 1) *
+                                                      sizeof(*p)), what);
+    };
+    A(m->params, NPARAM, "parameters");
+    A(m->adam_m, NPARAM, "Adam moments");
+    A(m->adam_v, NPARAM, "Adam moments");
+    A(m->norm, 2 * NF, "normalisation");
+    A(m->part, size_t(m->sms) * PSTRIDE, "gradient partials");
+    A(m->grad, NPARAM, "gradient");
+    A(m->loss, 1, "loss");
+    A(m->W1b, NH * NF, "weight images");
+    A(m->W2b, NH * NH, "weight images");
+    A(m->X, size_t(cfg->capacity) * NF, "training rows");
+    A(m->Y, size_t(cfg->capacity), "training labels");
+    A(m->counters, 8, "counters");
+    A(m->d_err, 1, "error flag");
+    A(m->d_sums, 2 * NF, "feature sums");
+    if (st != HCC_OK) {
+        delete m;
+        return st;
+    }
+    cudaMemset(m->counters, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(m->d_err, 0, sizeof(unsigned));
+    // Glorot-uniform weights from the seed, zero biases, identity normalisation
+    std::vector<float> p(NPARAM, 0.f), nrm(2 * NF, 0.f);
+    uint64_t s = cfg->seed ^ 0x5EEDull;
+    auto uni = [&](float a) {
+        s = host_mix(s);
+        return float((double(s >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0) * a);
+    };
+    const float a1 = std::sqrt(6.f / float(NF + NH)), a2 = std::sqrt(6.f / float(2 * NH)),
+                a3 = std::sqrt(6.f / float(NH + 1));
+    for (int e = 0; e < NH * NF; ++e) p[OFF_W1 + e] = uni(a1);
+    for (int e = 0; e < NH * NH; ++e) p[OFF_W2 + e] = uni(a2);
+    for (int e = 0; e < NH; ++e) p[OFF_W3 + e] = uni(a3);
+    for (int t = 0; t < NF; ++t) nrm[NF + t] = 1.f;
+    st = hcc_mlp_set_params(m, p.data(), nrm.data());
+    if (st != HCC_OK) {
+        delete m;
+        return st;
+    }
+    *out = m;
+    return HCC_OK;
+}
+
+void hcc_mlp_destroy(hcc_mlp *m) { delete m; }
+
+const char *hcc_mlp_last_error(const hcc_mlp *m) { return m ? m->err.c_str() : "null predictor"; }
+
+hcc_status hcc_mlp_get_params(hcc_mlp *m, float *params, float *norm) {
+    if (!m) return HCC_ERR_INVALID;
+    hcc_status st = HCC_OK;
+    if (params) st = m->cuda(cudaMemcpy(params, m->params, NPARAM * sizeof(float), cudaMemcpyDeviceToHost), "params");
+    if (st == HCC_OK && norm) st = m->cuda(cudaMemcpy(norm, m->norm, 2 * NF * sizeof(float), cudaMemcpyDeviceToHost),
+                                           "normalisation");
+    return st;
+}
+
+hcc_status hcc_mlp_set_params(hcc_mlp *m, const float *params, const float *norm) {
+    if (!m) return HCC_ERR_INVALID;
+    hcc_status st = HCC_OK;
+    if (params) {
+        st = m->cuda(cudaMemcpy(m->params, params, NPARAM * sizeof(float), cudaMemcpyHostToDevice), "params");
+        if (st == HCC_OK) st = m->cuda(cudaMemset(m->adam_m, 0, NPARAM * sizeof(float)), "Adam reset");
+        if (st == HCC_OK) st = m->cuda(cudaMemset(m->adam_v, 0, NPARAM * sizeof(float)), "Adam reset");
+        m->adam_t = 0;
+    }
+    if (st == HCC_OK && norm)
+        st = m->cuda(cudaMemcpy(m->norm, norm, 2 * NF * sizeof(float), cudaMemcpyHostToDevice), "normalisation");
+    if (st == HCC_OK) st = m->refresh_images();
+    return st;
+}
+
+hcc_status hcc_mlp_add_rows(hcc_mlp *m, const float *X, const uint8_t *y, int64_t n) {
+    if (!m || n < 0 || (n > 0 && (!X || !y))) return HCC_ERR_INVALID;
+    unsigned long long h[2] = {0, 0};
+    hcc_status st = m->cuda(cudaMemcpy(h, m->counters, sizeof(h), cudaMemcpyDeviceToHost), "counters");
+    if (st != HCC_OK) return st;
+    const int64_t at = std::min<int64_t>(int64_t(h[0]), m->cfg.capacity);
+    const int64_t take = std::min<int64_t>(n, m->cfg.capacity - at);
+    if (take > 0) {
+        st = m->cuda(cudaMemcpy(m->X + at * NF, X, size_t(take) * NF * sizeof(float), cudaMemcpyHostToDevice), "rows");
+        if (st == HCC_OK) st = m->cuda(cudaMemcpy(m->Y + at, y, size_t(take), cudaMemcpyHostToDevice), "labels");
+        if (st != HCC_OK) return st;
+        for (int64_t q = 0; q < take; ++q) h[1] += y[q] ? 1 : 0;
+    }
+    h[0] = uint64_t(at + take);
+    return m->cuda(cudaMemcpy(m->counters, h, sizeof(h), cudaMemcpyHostToDevice), "counters");
+}
+
+hcc_status hcc_mlp_rows(hcc_mlp *m, int64_t *rows, int64_t *flagged) {
+    if (!m) return HCC_ERR_INVALID;
+    unsigned long long h[2] = {0, 0};
+    hcc_status st = m->cuda(cudaMemcpy(h, m->counters, sizeof(h), cudaMemcpyDeviceToHost), "counters");
+    if (st != HCC_OK) return st;
+    if (rows) *rows = std::min<int64_t>(int64_t(h[0]), m->cfg.capacity);
+    if (flagged) *flagged = int64_t(h[1]);
+    return HCC_OK;
+}
+
+hcc_status hcc_mlp_clear(hcc_mlp *m) {
+    if (!m) return HCC_ERR_INVALID;
+    return m->cuda(cudaMemset(m->counters, 0, 2 * sizeof(unsigned long long)), "counters");
+}
+
+hcc_status hcc_mlp_fit_norm(hcc_mlp *m, double holdout) {
+    if (!m || !(holdout >= 0.0 && holdout < 1.0)) return HCC_ERR_INVALID;
+    const int64_t n = int64_t(double(m->rows()) * (1.0 - holdout));
+    if (n < 2) return m->fail(HCC_ERR_STATE, "fit_norm: fewer than two training rows");
+    hcc_status st = m->cuda(cudaMemsetAsync(m->d_sums, 0, 2 * NF * sizeof(double), m->stream), "sums");
+    if (st != HCC_OK) return st;
+    k_norm_sums<<<unsigned(std::min<int64_t>((n + 255) / 256, int64_t(m->sms) * 4)), 256, 0, m->stream>>>(m->X, n,
+                                                                                                      m->d_sums);
+    double h[2 * NF];
+    st = m->cuda(cudaMemcpyAsync(h, m->d_sums, sizeof(h), cudaMemcpyDeviceToHost, m->stream), "sums");
+    if (st == HCC_OK) st = m->cuda(cudaStreamSynchronize(m->stream), "fit_norm");
+    if (st != HCC_OK) return st;
+    float nrm[2 * NF];
+    for (int t = 0; t < NF; ++t) {
+        const double mean = h[t] / double(n), var = h[NF + t] / double(n) - mean * mean;
+        nrm[t] = float(mean);
+        nrm[NF + t] = var > 1e-12 ? float(1.0 / std::sqrt(var)) : 1.f;
+    }
+    return m->cuda(cudaMemcpy(m->norm, nrm, sizeof(nrm), cudaMemcpyHostToDevice), "normalisation");
+}
+
+namespace {
+hcc_status train_pass(hcc_mlp *m, const float *X, const uint8_t *Y, int64_t nrows, int64_t nbatch, int random,
+                      int update, float *grad, float *loss) {
+    const int ntiles = int((nbatch + 127) / 128);
+    const int grid = std::max(1, std::min(ntiles, m->sms));
+    TrainArgs A{};
+    A.w = m->weights();
+    A.X = X;
+    A.Y = Y;
+    A.nrows = nrows;
+    A.nbatch = nbatch;
+    A.random = random;
+    A.seed = m->cfg.seed;
+    A.iter = uint64_t(m->adam_t);
+    A.inv_batch = 1.f / float(nbatch);
+    A.pos_weight = float(m->cfg.pos_weight);
+    A.part = m->part;
+    A.err = m->d_err;
+    cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, int(TrainSmem::SIZE));
+    k_train<<<grid, 128, TrainSmem::SIZE, m->stream>>>(A, ntiles);
+    float c1 = 1.f, c2 = 1.f;
+    if (update) {
+        m->adam_t += 1;
+        c1 = float(1.0 / (1.0 - std::pow(m->cfg.beta1, double(m->adam_t))));
+        c2 = float(1.0 / (1.0 - std::pow(m->cfg.beta2, double(m->adam_t))));
+    }
+    k_adam<<<(NPARAM + 1 + 255) / 256, 256, 0, m->stream>>>(
+        m->params, m->adam_m, m->adam_v, m->part, grid, update, float(m->cfg.lr), float(m->cfg.beta1),
+        float(m->cfg.beta2), float(m->cfg.adam_eps), c1, c2, m->W1b, m->W2b, grad, loss);
+    return m->cuda(cudaGetLastError(), "training kernels");
+}
+}  // namespace
+
+hcc_status hcc_mlp_train(hcc_mlp *m, int64_t iters, int64_t batch, double holdout, double *loss_out) {
+    if (!m || iters < 0 || batch < 1 || batch > int64_t(128) * 4096 || !(holdout >= 0.0 && holdout < 1.0))
+        return HCC_ERR_INVALID;
+    const int64_t n = int64_t(double(m->rows()) * (1.0 - holdout));
+    if (n < 1) return m->fail(HCC_ERR_STATE, "train: no training rows");
+    hcc_status st = HCC_OK;
+    for (int64_t it = 0; it < iters && st == HCC_OK; ++it)
+        st = train_pass(m, m->X, m->Y, n, batch, 1, 1, nullptr, m->loss);
+    if (st == HCC_OK) st = m->cuda(cudaStreamSynchronize(m->stream), "train");
+    if (st == HCC_OK) st = m->check_err("train");
+    if (st == HCC_OK && loss_out) {
+        float l = 0.f;
+        st = m->cuda(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost), "loss");
+        *loss_out = l;
+    }
+    return st;
+}
+
+hcc_status hcc_mlp_loss_grad(hcc_mlp *m, const float *X, const uint8_t *y, int64_t n, float *grad, double *loss) {
+    if (!m || n < 1 || !X || !y || n > int64_t(128) * 4096) return HCC_ERR_INVALID;
+    hcc_status st = m->scratch(n);
+    if (st == HCC_OK) st = m->cuda(cudaMemcpy(m->sX, X, size_t(n) * NF * sizeof(float), cudaMemcpyHostToDevice), "rows");
+    if (st == HCC_OK) st = m->cuda(cudaMemcpy(m->sY, y, size_t(n), cudaMemcpyHostToDevice), "labels");
+    if (st == HCC_OK) st = train_pass(m, m->sX, m->sY, n, n, 0, 0, m->grad, m->loss);
+    if (st == HCC_OK) st = m->cuda(cudaStreamSynchronize(m->stream), "loss_grad");
+    if (st == HCC_OK) st = m->check_err("loss_grad");
+    if (st == HCC_OK && grad)
+        st = m->cuda(cudaMemcpy(grad, m->grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost), "gradient");
+    if (st == HCC_OK && loss) {
+        float l = 0.f;
+        st = m->cuda(cudaMemcpy(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost), "loss");
+        *loss = l;
+    }
+    return st;
+}
+
+hcc_status hcc_mlp_predict_rows(hcc_mlp *m, const float *X, int64_t n, float *logits) {
+    if (!m || n < 0 || (n > 0 && (!X || !logits))) return HCC_ERR_INVALID;
+    if (n == 0) return HCC_OK;
+    hcc_status st = m->scratch(n);
+    if (st == HCC_OK) st = m->cuda(cudaMemcpy(m->sX, X, size_t(n) * NF * sizeof(float), cudaMemcpyHostToDevice), "rows");
+    if (st != HCC_OK) return st;
+    RowSrc src{m->sX, nullptr, 0, n, m->sL, nullptr, 0.f};
+    launch_infer(src, m->weights(), n, m->sms * 4, m->d_err, m->stream);
+    st = m->cuda(cudaStreamSynchronize(m->stream), "predict_rows");
+    if (st == HCC_OK) st = m->check_err("predict_rows");
+    if (st == HCC_OK) st = m->cuda(cudaMemcpy(logits, m->sL, size_t(n) * sizeof(float), cudaMemcpyDeviceToHost), "logits");
+    return st;
+}
+
+hcc_status hcc_mlp_evaluate(hcc_mlp *m, double thr, double holdout, int64_t *counts) {
+    if (!m || !counts || !(thr > 0.0 && thr < 1.0) || !(holdout > 0.0 && holdout <= 1.0)) return HCC_ERR_INVALID;
+    const int64_t rows = m->rows();
+    const int64_t start = int64_t(double(rows) * (1.0 - holdout));
+    const int64_t n = rows - start;
+    hcc_status st = m->cuda(cudaMemset(m->counters + 2, 0, 4 * sizeof(unsigned long long)), "counts");
+    if (st != HCC_OK) return st;
+    RowSrc src{m->X, m->Y, start, n, nullptr, m->counters + 2, float(std::log(thr / (1.0 - thr)))};
+    launch_infer(src, m->weights(), n, m->sms * 4, m->d_err, m->stream);
+    st = m->cuda(cudaStreamSynchronize(m->stream), "evaluate");
+    if (st == HCC_OK) st = m->check_err("evaluate");
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (st == HCC_OK) st = m->cuda(cudaMemcpy(h, m->counters + 2, sizeof(h), cudaMemcpyDeviceToHost), "counts");
+    for (int q = 0; q < 4; ++q) counts[q] = int64_t(h[q]);
+    return st;
+}
+
+}  // extern "C"

@@ -161,6 +161,7 @@ typedef struct {
     int64_t steps;                     /* steps taken by the context */
     int64_t kernel_launches_total;     /* kernels launched since the context was created */
     int64_t graph_steps;               /* steps taken as one captured CUDA graph (hcc_set_step_graphs) */
+    int64_t predicted;                 /* particles the troubled-point predictor pre-lowered in the last step */
 } hcc_counters;
 
 typedef struct hcc_ctx hcc_ctx;
@@ -291,6 +292,80 @@ hcc_status hcc_get_kernel_times(hcc_ctx *ctx, hcc_kernel_times *out, int reset);
 hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n, int64_t npad, const int32_t *counts,
                                      const int32_t *nidx, const double *dweights, const uint8_t *is_boundary,
                                      const double *U, void *stream, double *dt_out);
+
+/* ------------------------------------------------------------------ learned troubled-point predictor
+   No counterpart in the reference (its MOOD loop computes every particle at full order first, MOOD.jl:375-405).
+   A small MLP (24 -> 64 -> 64 -> 1, GELU, BF16 weights and activations on the tensor cores, FP32 accumulate)
+   reads 24 stencil features of the start-of-step state and pre-lowers the order of the particles it predicts to be
+   troubled (one order, as a MOOD drop), before the step's first reconstruction. Full MOOD still runs on every
+   particle as the judge; the predictor only saves recompute passes. The network is trained on the device (forward
+   and backward kernels, Adam) on (feature, MOOD-flag) pairs the solver itself generates.
+
+   Features, per particle i, from its neighbours j (offsets x_ij) and four quantities q (Euler: density, pressure,
+   momentum magnitude, total energy; other systems: components 0..3, the last repeated), six per quantity, in FP32:
+   range / (|max| + |min|), (2 q_i - max - min) / range, (q_i - mean_j q_j) / range, RMS residual of the
+   least-squares linear fit / range, |gradient| h / range, RMS deviation / range; max/min over {i} + N(i); the last
+   five are 0 where range <= 1e-6 (|max| + |min|); every feature is clamped to [-8, 8] (NaN -> 0). */
+#define HCC_MLP_FEATURES 24
+#define HCC_MLP_HIDDEN 64
+/* Flat FP32 parameter vector: W1[64][24], b1[64], W2[64][64], b2[64], w3[64], b3 (z1 = W1 x + b1, ...). */
+#define HCC_MLP_NPARAMS (64 * 24 + 64 + 64 * 64 + 64 + 64 + 1)
+
+typedef struct hcc_mlp hcc_mlp;
+
+typedef struct {
+    int64_t capacity;        /* training rows held on the device */
+    double neg_keep;         /* fraction of unflagged interior particles kept by hcc_mlp_collect (flagged: all) */
+    uint64_t seed;           /* negative sampling and mini-batch draws */
+    double lr, beta1, beta2, adam_eps;   /* Adam */
+    double pos_weight;       /* weight of the flagged class in the binary cross-entropy */
+    double reserved[4];
+} hcc_mlp_config;
+
+hcc_status hcc_mlp_create(const hcc_mlp_config *cfg, hcc_mlp **out);
+void hcc_mlp_destroy(hcc_mlp *mlp);
+const char *hcc_mlp_last_error(const hcc_mlp *mlp);
+
+/* Parameters (HCC_MLP_NPARAMS FP32, the master copy Adam updates) and the input normalisation
+   (mean[24], inv_std[24]: x' = (x - mean) * inv_std). Setting parameters resets Adam. */
+hcc_status hcc_mlp_get_params(hcc_mlp *mlp, float *params, float *norm);
+hcc_status hcc_mlp_set_params(hcc_mlp *mlp, const float *params, const float *norm);
+
+/* Training set. hcc_mlp_collect appends the features the context computed at the start of its last step (see
+   hcc_set_feature_capture) with that step's MOOD flags as labels; hcc_mlp_add_rows appends host rows
+   (X[n][24], y[n]). hcc_mlp_rows reports the rows held and how many are flagged. hcc_mlp_clear empties it. */
+hcc_status hcc_mlp_collect(hcc_mlp *mlp, hcc_ctx *ctx);
+hcc_status hcc_mlp_add_rows(hcc_mlp *mlp, const float *X, const uint8_t *y, int64_t n);
+hcc_status hcc_mlp_rows(hcc_mlp *mlp, int64_t *rows, int64_t *flagged);
+hcc_status hcc_mlp_clear(hcc_mlp *mlp);
+
+/* Normalisation from the training rows [0, (1 - holdout) rows): mean and 1/std per feature. */
+hcc_status hcc_mlp_fit_norm(hcc_mlp *mlp, double holdout);
+
+/* iters Adam steps on mini-batches of `batch` rows drawn from [0, (1 - holdout) rows); *loss_out = mean loss of the
+   last mini-batch. */
+hcc_status hcc_mlp_train(hcc_mlp *mlp, int64_t iters, int64_t batch, double holdout, double *loss_out);
+
+/* Confusion counts {tp, fp, fn, tn} of the rows [(1 - holdout) rows, rows) at probability threshold thr. */
+hcc_status hcc_mlp_evaluate(hcc_mlp *mlp, double thr, double holdout, int64_t *counts);
+
+/* One forward/backward pass on host rows without an update: the mean loss and its gradient (HCC_MLP_NPARAMS). */
+hcc_status hcc_mlp_loss_grad(hcc_mlp *mlp, const float *X, const uint8_t *y, int64_t n, float *grad, double *loss);
+
+/* Logits of host rows X[n][24] through the inference kernel. */
+hcc_status hcc_mlp_predict_rows(hcc_mlp *mlp, const float *X, int64_t n, float *logits);
+
+/* Attach a predictor to a context (NULL detaches): every hcc_step then pre-lowers the particles whose predicted
+   probability exceeds thr. The predictor must outlive the attachment. */
+hcc_status hcc_set_predictor(hcc_ctx *ctx, hcc_mlp *mlp, double thr);
+
+/* Keep the start-of-step features of every step (for hcc_mlp_collect / hcc_download_features). */
+hcc_status hcc_set_feature_capture(hcc_ctx *ctx, int enable);
+
+/* Features (N x 24) of the current state (the start state of the next step), and the particles the predictor
+   pre-lowered in the last step (N, 0/1). */
+hcc_status hcc_download_features(hcc_ctx *ctx, float *features);
+hcc_status hcc_download_predicted(hcc_ctx *ctx, uint8_t *predicted);
 
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);

@@ -560,6 +560,7 @@ struct Solver {
     Tableau tab;
     double ssp_C = 0.0, ratio = 0.0;
     std::vector<double> rho_n, rho_cand, rho_sub;
+    std::vector<uint8_t> prelowered;   // pre-lowered particles of the next step (empty: none)
     std::vector<std::vector<double>> Y, KE, KI;
     std::vector<uint8_t> triggered, changed, dirty, scratch, trig_step;
     int64_t inadmissible = 0, mood_iters = 0, steps = 0;
@@ -1600,6 +1601,12 @@ struct Solver {
         std::fill(grads.begin(), grads.end(), 0.0);
         rho_n = rhos;
         std::fill(orders.begin(), orders.end(), max_order);
+        if (!prelowered.empty()) {
+            // particles a troubled-point predictor pre-lowered start the step one order lower (interior only)
+            for (int64_t q = 0; q < N; ++q)
+                if (prelowered[q] && !bnd[q]) orders[q] = std::max(1, max_order - 1);
+            prelowered.clear();
+        }
         std::fill(trig_step.begin(), trig_step.end(), 0);
         inadmissible = 0; mood_iters = 0;
         const int s = tab.s;
@@ -1681,6 +1688,117 @@ inline hcc_status fail(Solver *s, hcc_status st) { (void)s; return st; }
 struct orc_ctx {
     Solver s;
 };
+
+namespace {
+
+// Stencil features of the learned troubled-point predictor (no counterpart in the reference; definitions in
+// include/hcc.h): four quantities per particle, six FP32 features each, in the operation order of the GPU kernel.
+void feature_quantities(const Solver &s, const double *u, float gm1, float q[4]) {
+    if (s.cfg.pde == HCC_PDE_EULER) {
+        const float rho = float(u[0]);
+        float msq = 0.f;
+        for (int d = 0; d < s.D; ++d) {
+            const float md = float(u[1 + d]);
+            msq = msq + md * md;
+        }
+        const float E = float(u[s.D + 1]);
+        q[0] = rho;
+        q[1] = gm1 * (E - (0.5f * msq) / rho);
+        q[2] = std::sqrt(msq);
+        q[3] = E;
+    } else {
+        for (int m = 0; m < 4; ++m) q[m] = float(u[m < s.M ? m : s.M - 1]);
+    }
+}
+
+float clamp_feature(float f) {
+    if (!(f == f)) return 0.f;
+    return f > 8.f ? 8.f : (f < -8.f ? -8.f : f);
+}
+
+void point_features(const Solver &s, int64_t i, float h, float gm1, float *f) {
+    const int D = s.D;
+    float qi[4], qmax[4], qmin[4], s1[4] = {0, 0, 0, 0}, s2[4] = {0, 0, 0, 0}, b[4][3] = {}, G[6] = {};
+    feature_quantities(s, &s.rhos[i * s.M], gm1, qi);
+    for (int m = 0; m < 4; ++m) { qmax[m] = qi[m]; qmin[m] = qi[m]; }
+    const int64_t k0 = s.start[i], c = s.start[i + 1] - s.start[i];
+    for (int64_t k = 0; k < c; ++k) {
+        const int64_t slot = k0 + k;
+        const int64_t j = s.nidx[slot];
+        float x[3] = {0, 0, 0};
+        for (int d = 0; d < D; ++d) x[d] = float(s.ndist[slot * D + d]);
+        int e = 0;
+        for (int p = 0; p < D; ++p)
+            for (int q = p; q < D; ++q) G[e++] += x[p] * x[q];
+        float qj[4];
+        feature_quantities(s, &s.rhos[j * s.M], gm1, qj);
+        for (int m = 0; m < 4; ++m) {
+            const float dq = qj[m] - qi[m];
+            s1[m] += dq;
+            s2[m] += dq * dq;
+            for (int d = 0; d < D; ++d) b[m][d] += dq * x[d];
+            qmax[m] = qj[m] > qmax[m] ? qj[m] : qmax[m];
+            qmin[m] = qj[m] < qmin[m] ? qj[m] : qmin[m];
+        }
+    }
+    float Gi[6] = {};
+    float det;
+    if (D == 1) {
+        det = G[0];
+        Gi[0] = 1.f;
+    } else if (D == 2) {
+        det = G[0] * G[2] - G[1] * G[1];
+        Gi[0] = G[2]; Gi[1] = -G[1]; Gi[2] = G[0];
+    } else {
+        Gi[0] = G[3] * G[5] - G[4] * G[4];
+        Gi[1] = G[2] * G[4] - G[1] * G[5];
+        Gi[2] = G[1] * G[4] - G[2] * G[3];
+        Gi[3] = G[0] * G[5] - G[2] * G[2];
+        Gi[4] = G[1] * G[2] - G[0] * G[4];
+        Gi[5] = G[0] * G[3] - G[1] * G[1];
+        det = (G[0] * Gi[0] + G[1] * Gi[1]) + G[2] * Gi[2];
+    }
+    const bool solve = det > 0.f;
+    const float ic = c > 0 ? 1.f / float(c) : 0.f;
+    for (int m = 0; m < 4; ++m) {
+        float g[3] = {0, 0, 0};
+        if (D == 1) {
+            g[0] = solve ? b[m][0] / det : 0.f;
+        } else if (D == 2) {
+            g[0] = solve ? (Gi[0] * b[m][0] + Gi[1] * b[m][1]) / det : 0.f;
+            g[1] = solve ? (Gi[1] * b[m][0] + Gi[2] * b[m][1]) / det : 0.f;
+        } else {
+            g[0] = solve ? ((Gi[0] * b[m][0] + Gi[1] * b[m][1]) + Gi[2] * b[m][2]) / det : 0.f;
+            g[1] = solve ? ((Gi[1] * b[m][0] + Gi[3] * b[m][1]) + Gi[4] * b[m][2]) / det : 0.f;
+            g[2] = solve ? ((Gi[2] * b[m][0] + Gi[4] * b[m][1]) + Gi[5] * b[m][2]) / det : 0.f;
+        }
+        float bgb = 0.f, gg = 0.f;
+        for (int d = 0; d < D; ++d) {
+            bgb += b[m][d] * g[d];
+            gg += g[d] * g[d];
+        }
+        const float r = qmax[m] - qmin[m];
+        const float sc = std::fabs(qmax[m]) + std::fabs(qmin[m]);
+        float *o = f + 6 * m;
+        o[0] = sc > 0.f ? r / sc : 0.f;
+        if (c > 0 && r > 1e-6f * sc) {
+            const float ir = 1.f / r;
+            const float mean = s1[m] * ic;
+            const float res = (s2[m] - bgb) * ic;
+            const float var = s2[m] * ic - mean * mean;
+            o[1] = ((2.f * qi[m] - qmax[m]) - qmin[m]) * ir;
+            o[2] = -(mean * ir);
+            o[3] = (res > 0.f ? std::sqrt(res) : 0.f) * ir;
+            o[4] = (std::sqrt(gg) * h) * ir;
+            o[5] = (var > 0.f ? std::sqrt(var) : 0.f) * ir;
+        } else {
+            o[1] = o[2] = o[3] = o[4] = o[5] = 0.f;
+        }
+        for (int t = 0; t < 6; ++t) o[t] = clamp_feature(o[t]);
+    }
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1796,6 +1914,23 @@ hcc_status orc_compute_rhs_orders(orc_ctx *ctx, const int32_t *orders, double *K
     std::vector<double> Kv(s.N * s.M, 0.0);
     s.compute_rhs(Kv, s.rhos.data(), true);
     std::memcpy(K, Kv.data(), Kv.size() * sizeof(double));
+    return HCC_OK;
+}
+hcc_status orc_features(orc_ctx *ctx, float *out) {
+    if (!ctx || !out) return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    if (!s.have_nb) return HCC_ERR_STATE;
+    double hm = s.cfg.dx[0];
+    for (int d = 1; d < s.D; ++d) hm = std::min(hm, s.cfg.dx[d]);
+    const float h = float(hm), gm1 = float(s.cfg.gamma - 1.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < s.N; ++i) point_features(s, i, h, gm1, out + i * HCC_MLP_FEATURES);
+    return HCC_OK;
+}
+hcc_status orc_set_prelowered(orc_ctx *ctx, const uint8_t *mask) {
+    if (!ctx) return HCC_ERR_INVALID;
+    if (mask) ctx->s.prelowered.assign(mask, mask + ctx->s.N);
+    else ctx->s.prelowered.clear();
     return HCC_OK;
 }
 hcc_status orc_step(orc_ctx *ctx, double t, double dt) {

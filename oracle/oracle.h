@@ -81,6 +81,10 @@ hcc_status orc_interface_orders(orc_ctx *ctx, int64_t i, int64_t j, int32_t *oi,
 /* detect_and_drop! (MOOD.jl:375-405) against explicit prev/cand states; dirty may be NULL (full). */
 hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *cand, int32_t full,
                                const uint8_t *dirty, int32_t with_eq, int32_t *changed_any);
+/* Stencil features of the learned troubled-point predictor of the current state (N x 24, FP32; definitions in
+   include/hcc.h), and the particles the next orc_step pre-lowers by one order (NULL: none). */
+hcc_status orc_features(orc_ctx *ctx, float *out);
+hcc_status orc_set_prelowered(orc_ctx *ctx, const uint8_t *mask);
 /* Grid mover of the context (GridMovers.jl). */
 hcc_status orc_set_mover(orc_ctx *ctx, const hcc_mover *mover);
 /* The MOOD criterion of particle p (MOOD.jl:175-271) for hand-set stage states (N*M), gradients (N*Br*M), orders

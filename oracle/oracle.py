@@ -77,6 +77,8 @@ def load(abi) -> C.CDLL:
         ("orc_apply_bcs", C.c_int, [P, dp]),
         ("orc_criterion_flags", C.c_int, [P, C.c_int64, dp, dp, ip, dp, ip]),
         ("orc_set_mover", C.c_int, [P, C.POINTER(abi.HccMover)]),
+        ("orc_features", C.c_int, [P, C.POINTER(C.c_float)]),
+        ("orc_set_prelowered", C.c_int, [P, up]),
     ]
     for name, res, args in protos:
         fn = getattr(lib, name)
@@ -272,6 +274,20 @@ class OracleContext:
                                                  _p(o, C.c_int32), _p(c, C.c_double), C.byref(f)),
                     "orc_criterion_flags")
         return bool(f.value)
+
+    def features(self):
+        """Stencil features of the learned troubled-point predictor (N x 24, FP32) of the current state."""
+        out = np.zeros((self.n, 24), dtype=np.float32)
+        self._check(self.lib.orc_features(self._h, _p(out, C.c_float)), "orc_features")
+        return out
+
+    def set_prelowered(self, mask):
+        """Particles the next step pre-lowers by one order (None: none)."""
+        if mask is None:
+            self._check(self.lib.orc_set_prelowered(self._h, None), "orc_set_prelowered")
+            return
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        self._check(self.lib.orc_set_prelowered(self._h, _p(m, C.c_uint8)), "orc_set_prelowered")
 
     def apply_bcs(self, buf):
         b = np.ascontiguousarray(buf, dtype=np.float64).copy()
