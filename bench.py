@@ -5,9 +5,10 @@ interior particles plus ghosts; four-quadrant Riemann initial state split at (0.
 boundaries; MUSCL order 2 with the MLS divergence fit of order 2; MOOD (EPD1, MOODu1 with delta = 1e-4 h^2);
 Rusanov flux; SSP-RK3; dt = 0.4 x the CFL step at the initial state. Synthetic, seeded inputs (no dataset).
 
-`value` is the FP32 bulk path (the headline), measured with the state resident in HBM; `e2e` is the same metric
-through the C ABI with host buffers (state uploaded from pinned memory and downloaded every step); `fp64_plain` is
-the plain FP64 path on the same cloud. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's
+`value` is the FP32 bulk path with the learned troubled-point predictor attached (the headline; the plain FP32
+path is `fp32_plain`), measured with the state resident in HBM; `e2e` is the same metric through the C ABI with
+host buffers (state uploaded from pinned memory and downloaded every step); `fp64_plain` is the plain FP64 path on
+the same cloud; `accuracy_vs_finer_fp64` compares the density L1 errors of the three against an FP64 run at h/2. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's
 CPU path) on a bounded sample of the same workload. `--impl reference` runs only that CPU path.
 
 Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under torch.distributed.run (one rank per GPU,
@@ -254,12 +255,30 @@ def time_e2e(hcc, ctx, U_host, dt, steps, world, f32):
     return reduce_max(el, world), host.nbytes, out.nbytes
 
 
-def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_dt=None, acc_steps=0):
+def load_predictor(hcc):
+    """The troubled-point predictor shipped with the package (train_predictor.py recipe), or None."""
+    learned = sys.modules["hcc_gb300.learned"]
+    path = learned.default_weights_path()
+    if not path.exists():
+        return None
+    pred = hcc.TroubledPointPredictor(capacity=16)
+    pred.load(path)
+    return pred
+
+
+PREDICTOR_THRESHOLD = 0.7
+
+
+def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_dt=None, acc_steps=0,
+            predictor=None):
     """One precision on one workload: K device-timed steps (the step graph, no profiling), the same K steps again
     with per-kernel CUDA events (host-driven step) for the roofline, the end-to-end C-ABI leg, and — when asked —
-    `acc_steps` steps from the initial state with a fixed dt whose final density is returned for the L1 check."""
+    `acc_steps` steps from the initial state with a fixed dt whose final density is returned for the L1 check.
+    With a predictor, every step pre-lowers the particles it predicts troubled (MOOD still judges all)."""
     f32 = prec == "fp32"
     ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+    if predictor is not None:
+        ctx.set_predictor(predictor, PREDICTOR_THRESHOLD)
     if HOST_DRIVEN:
         ctx.set_step_graphs(False)
     ctx.upload_cloud(cloud)
@@ -298,6 +317,25 @@ def rel_l1(a, b, sel):
     return float(np.abs(a[sel] - b[sel]).sum() / np.abs(b[sel]).sum())
 
 
+def fine_reference(hcc, cloud, h, dt, steps):
+    """Density of the plain FP64 path on the same problem at spacing h/2 after 2*steps steps of dt/2 (the same
+    final time), sampled at the particles of `cloud` (nearest fine particle): the reference of the L1 errors."""
+    from scipy.spatial import cKDTree
+    D = cloud.pos.shape[1]
+    fine = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h / 2, 2.5 * h / 2, jitter=0.25 * h / 2, seed=42)
+    ctx = hcc.Context(make_cfg(hcc, fine, h / 2, "fp64"))
+    ctx.upload_cloud(fine)
+    ctx.build_neighbours()
+    ctx.prepare_geometry()
+    ctx.upload_state(quadrant_state(fine) if D == 2 else blast_state(fine))
+    for _ in range(2 * steps):
+        ctx.step(0.0, dt / 2)
+    rho = ctx.download_state()[:, 0].copy()
+    ctx.close()
+    _, idx = cKDTree(fine.pos).query(cloud.pos)
+    return rho[idx]
+
+
 def run_3d(hcc, args, world, local):
     """The 3-D Euler blast at 8.0M interior particles (K ~ 67): FP32 bulk and FP64 plain step rates and the FP32
     density's relative L1 distance from the FP64 run after the same steps."""
@@ -312,6 +350,19 @@ def run_3d(hcc, args, world, local):
     inner = cloud.is_boundary == 0
     K = r32["counters"]["total_neighbours"] / max(cloud.n, 1)
     kt = r32["kt"]
+    learned = {}
+    predictor = None if args.no_learned else load_predictor(hcc)
+    if predictor is not None:
+        # the network trained on 2-D runs, applied as-is to the 3-D stencils (MOOD still judges every particle)
+        rl = measure(hcc, cloud, U0, h, "fp32", steps32, 2, world, local, e2e=False, predictor=predictor)
+        rla = measure(hcc, cloud, U0, h, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt, acc_steps=acc,
+                      predictor=predictor)
+        learned = {"fp32_learned": {"value": n_int * STAGES * steps32 * world / (rl["ms"] / 1e3),
+                                    "ms_per_step": rl["ms"] / steps32,
+                                    "mood_iterations_last_step": rl["counters"]["mood_iterations"],
+                                    "predicted_last_step": rl["counters"]["predicted"], "clocks": rl["clocks"]},
+                   "l1_density_learned_vs_fp64": {"value": rel_l1(rla["rho"], r64["rho"], inner), "steps": acc,
+                                                  "dt": dt}}
     return {"workload": name, "description": WORKLOADS[name][2], "n_particles": cloud.n, "n_interior": n_int,
             "mean_neighbours": K,
             "fp32": {"value": n_int * STAGES * steps32 * world / (r32["ms"] / 1e3), "ms_per_step": r32["ms"] / steps32,
@@ -320,7 +371,8 @@ def run_3d(hcc, args, world, local):
                      "mood_iterations_last_step": r32["counters"]["mood_iterations"], "clocks": r32["clocks"]},
             "fp64_plain": {"value": n_int * STAGES * steps64 * world / (r64["ms"] / 1e3),
                            "ms_per_step": r64["ms"] / steps64, "clocks": r64["clocks"]},
-            "l1_density_fp32_vs_fp64": {"value": rel_l1(r32a["rho"], r64["rho"], inner), "steps": acc, "dt": dt}}
+            "l1_density_fp32_vs_fp64": {"value": rel_l1(r32a["rho"], r64["rho"], inner), "steps": acc, "dt": dt},
+            **learned}
 
 
 def run_gpu(args):
@@ -335,14 +387,22 @@ def run_gpu(args):
     n_int = cloud.n_interior
     results = {}
     acc_steps, acc_dt = 10, None
-    for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
-        results[prec] = measure(hcc, cloud, U0, h, prec, args.steps, args.warmup, world, local,
-                                acc_dt=acc_dt, acc_steps=acc_steps if acc_dt else 0)
+    predictor = None if args.no_learned else load_predictor(hcc)
+    arms = ["fp32", "fp64"] if not args.fp32_only else ["fp32"]
+    if predictor is not None:
+        arms = ["fp32_learned"] + arms
+    for arm in arms:
+        prec = "fp64" if arm == "fp64" else "fp32"
+        pr = predictor if arm == "fp32_learned" else None
+        results[arm] = measure(hcc, cloud, U0, h, prec, args.steps, args.warmup, world, local,
+                               acc_dt=acc_dt, acc_steps=acc_steps if acc_dt else 0, predictor=pr)
         if acc_dt is None:
-            acc_dt = results[prec]["dt"]
-            r = measure(hcc, cloud, U0, h, prec, 1, 0, world, local, e2e=False, acc_dt=acc_dt, acc_steps=acc_steps)
-            results[prec]["rho"] = r["rho"]
-    r = results["fp32"]
+            acc_dt = results[arm]["dt"]
+            r = measure(hcc, cloud, U0, h, prec, 1, 0, world, local, e2e=False, acc_dt=acc_dt, acc_steps=acc_steps,
+                        predictor=pr)
+            results[arm]["rho"] = r["rho"]
+    head = "fp32_learned" if predictor is not None else "fp32"
+    r = results[head]
     units = n_int * STAGES * args.steps * world
     value = units / (r["ms"] / 1e3)
     cnt = r["counters"]
@@ -360,7 +420,10 @@ def run_gpu(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
                    "n_particles": cloud.n, "n_interior": n_int, "mean_neighbours": K, "stages_per_step": STAGES,
-                   "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": False,
+                   "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": predictor is not None,
+                   "predictor": ({"weights": "hypercloudcore.jl_gb300/predictor_euler2d.npz (train_predictor.py: "
+                                  "200 seeded Voronoi runs at 250k nodes to t = 0.2)",
+                                  "threshold": PREDICTOR_THRESHOLD} if predictor is not None else None),
                    "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
                    "l2": "inputs larger than L2 (per-slot arrays ~0.5 GB)", "parallelism": f"replicas x{world}",
                    "dt": r["dt"]},
@@ -376,8 +439,15 @@ def run_gpu(args):
                      "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
                      "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps"},
         "clocks": r["clocks"],
-        "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"]},
+        "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],
+                 "predicted_last_step": cnt.get("predicted", 0)},
     }
+    if head != "fp32":
+        r0 = results["fp32"]
+        line["fp32_plain"] = {"value": units / (r0["ms"] / 1e3), "ms_per_step": r0["ms"] / args.steps,
+                              "e2e": units / r0["e2e_s"], "gpu_launches": r0["launches"],
+                              "mood": {"flagged_last_step": r0["counters"]["mood_flagged"],
+                                       "iterations_last_step": r0["counters"]["mood_iterations"]}}
     if "fp64" in results:
         r64 = results["fp64"]
         line["fp64_plain"] = {"value": units / (r64["ms"] / 1e3), "ms_per_step": r64["ms"] / args.steps,
@@ -386,8 +456,22 @@ def run_gpu(args):
                               "e2e": units / r64["e2e_s"], "clocks": r64["clocks"]}
         line["fp32_over_fp64"] = line["value"] / line["fp64_plain"]["value"]
         inner = cloud.is_boundary == 0
-        line["l1_density_fp32_vs_fp64"] = {"value": rel_l1(r["rho"], r64["rho"], inner), "steps": acc_steps,
-                                           "dt": acc_dt, "note": "relative L1 over interior particles, same dt"}
+        line["l1_density_fp32_vs_fp64"] = {"value": rel_l1(results["fp32"]["rho"], r64["rho"], inner),
+                                           "steps": acc_steps, "dt": acc_dt,
+                                           "note": "relative L1 over interior particles, same dt"}
+        if head != "fp32":
+            line["l1_density_learned_vs_fp64"] = {"value": rel_l1(r["rho"], r64["rho"], inner), "steps": acc_steps,
+                                                  "dt": acc_dt}
+        if not args.no_reference_solution and D == 2:
+            ref = fine_reference(hcc, cloud, h, acc_dt, acc_steps)
+            acc = {"reference": "FP64 plain at h/2 (4x the particles), 2x the steps at dt/2, nearest fine particle",
+                   "steps": acc_steps, "l1_fp64": rel_l1(r64["rho"], ref, inner),
+                   "l1_fp32": rel_l1(results["fp32"]["rho"], ref, inner)}
+            if head != "fp32":
+                acc["l1_fp32_learned"] = rel_l1(r["rho"], ref, inner)
+                acc["learned_over_fp64"] = acc["l1_fp32_learned"] / acc["l1_fp64"]
+            acc["fp32_over_fp64"] = acc["l1_fp32"] / acc["l1_fp64"]
+            line["accuracy_vs_finer_fp64"] = acc
     if not args.no_published:
         line["published_case"] = run_published_case(hcc, args.steps)
     if not args.no_3d and D == 2:
@@ -499,6 +583,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="no troubled-point predictor (plain FP32 headline)")
+    ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
     ap.add_argument("--no-published", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--host-driven", action="store_true")

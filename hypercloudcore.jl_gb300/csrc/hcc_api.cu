@@ -212,6 +212,8 @@ struct hcc_ctx {
     int capture_feat = 0;
     float *feat = nullptr;
     uint8_t *pred = nullptr;
+    uint4 *pred_rows = nullptr;       // compact list of the rows that passed the smoothness gate
+    int32_t *pred_idx = nullptr;
     int64_t predicted = 0;
     bool feat_valid = false;
     // moving grid: mover, start-of-step / stage / final positions and the stage grid velocities (SoA FP64)
@@ -318,7 +320,7 @@ struct hcc_ctx {
             for (void **p : {&Y[s], &KE[s], &KI[s]}) { if (*p) cudaFree(*p); *p = nullptr; }
         dfree(orders); dfree(nbmin); dfree(trig_step); dfree(inadm);
         dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
-        dfree(ftiles); dfree(fmask); dfree(forced); dfree(feat); dfree(pred);
+        dfree(ftiles); dfree(fmask); dfree(forced); dfree(feat); dfree(pred); dfree(pred_rows); dfree(pred_idx);
         feat_valid = false;
     }
     void free_slots() {
@@ -643,6 +645,8 @@ hcc_status ensure_learn_buffers(hcc_ctx *c) {
     if (st == HCC_OK && c->mlp && !c->pred) {
         st = c->alloc(c->pred, size_t(c->n), "predicted mask");
         if (st == HCC_OK) st = c->cuda(cudaMemset(c->pred, 0, size_t(c->n)), "predicted mask");
+        if (st == HCC_OK) st = c->alloc(c->pred_rows, size_t(c->n) * 4, "predictor rows");
+        if (st == HCC_OK) st = c->alloc(c->pred_idx, size_t(c->n), "predictor rows");
     }
     return st;
 }
@@ -655,18 +659,24 @@ int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
     int k = 0;
     if (c->capture_feat || c->mlp) {
         const FeatArgs fa = feat_args(c, c->rhos);
-        if (c->capture_feat && launch_features(fa, c->feat, st)) k += 1;
         if (c->mlp) {
-            // the predicted particles start the step one order lower (MOOD still judges every particle)
+            // the predicted particles start the step one order lower (MOOD still judges every particle); the
+            // captured training features come out of the same feature pass
             PredictOut po{};
             po.orders = c->orders;
             po.lowered = int8_t(std::max(1, c->max_order - 1));
             po.pred = c->pred;
             po.count = &c->mood_stats->predicted;
             po.thr_logit = c->thr_logit;
-            if (launch_predict(fa, mlp_weights(c->mlp), po, std::max(1, c->list_blocks / 8) * 4,
-                               &c->mood_stats->tc_error, st))
-                k += 1;
+            po.rows = c->pred_rows;
+            po.row_idx = c->pred_idx;
+            po.nrows = &c->mood_stats->pred_rows;
+            po.cap = c->n;
+            if (launch_predict(fa, mlp_weights(c->mlp), po, c->capture_feat ? c->feat : nullptr,
+                               std::max(1, c->list_blocks / 8) * 2, &c->mood_stats->tc_error, st))
+                k += 2;
+        } else if (launch_features(fa, c->feat, st)) {
+            k += 1;
         }
     }
     c->ops->stage1(args, c->n, st);

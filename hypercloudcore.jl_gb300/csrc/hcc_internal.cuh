@@ -414,6 +414,7 @@ struct MoodStats {
     unsigned long long iterations, flagged, inadmissible, timeout;
     unsigned int iter_in_checkpoint, pad;
     unsigned long long predicted;     // particles the troubled-point predictor pre-lowered
+    unsigned long long pred_rows;     // rows that passed the predictor's smoothness gate
     unsigned int tc_error, pad2;      // a tensor-core wait of the predictor gave up
 };
 
@@ -460,7 +461,8 @@ struct MlpWeights {
     const uint16_t *W1, *W2;
     const float *params, *norm;
 };
-// Outputs of the in-step prediction.
+// Buffers and outputs of the in-step prediction: the compact list of gated rows (normalised BF16 features, four
+// 16-byte segments each, and their particle numbers), the mask of predicted particles and the orders they get.
 struct PredictOut {
     int8_t *orders;
     int8_t lowered;                   // order of a predicted particle (one below the maximum)
@@ -468,10 +470,15 @@ struct PredictOut {
     float *logits;                    // [n] or nullptr
     unsigned long long *count;        // predicted particles (accumulated)
     float thr_logit;
+    uint4 *rows;                      // [cap * 4] (nullptr: features only)
+    int32_t *row_idx;                 // [cap]
+    unsigned long long *nrows;        // rows appended (zeroed before the pass)
+    int64_t cap;
 };
 bool launch_features(const FeatArgs &fa, float *out, cudaStream_t s);
-bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, int grid, unsigned *err,
-                    cudaStream_t s);
+// Pass 1 (features, gate, compaction; raw features into `raw` when not null) and pass 2 (the network).
+bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, float *raw, int grid,
+                    unsigned *err, cudaStream_t s);
 MlpWeights mlp_weights(const hcc_mlp *m);
 hcc_status mlp_append(hcc_mlp *m, const float *feat, const uint8_t *labels, const uint8_t *bnd, int64_t n,
                       cudaStream_t s);

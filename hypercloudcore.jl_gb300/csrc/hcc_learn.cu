@@ -35,19 +35,20 @@ constexpr uint32_t WAIT_LIMIT = 1u << 20;
 
 // --------------------------------------------------------------------------------------------- features
 template <typename T, int D, int M, int PDE>
-__device__ __forceinline__ void quantities(const T *u, float gm1, float q[4]) {
+__device__ __forceinline__ void quantities(const T *u, float q[4]) {
     if constexpr (PDE == HCC_PDE_EULER) {
+        // density, rho * (rho e) = rho p / (gamma - 1), |momentum|^2, total energy: no division, no root
         const float rho = float(u[0]);
         float msq = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             const float md = float(u[1 + d]);
-            msq = msq + md * md;
+            msq = fmaf(md, md, msq);
         }
         const float E = float(u[D + 1]);
         q[0] = rho;
-        q[1] = gm1 * (E - (0.5f * msq) / rho);
-        q[2] = sqrtf(msq);
+        q[1] = fmaf(E, rho, -(0.5f * msq));
+        q[2] = msq;
         q[3] = E;
     } else {
 #pragma unroll
@@ -68,7 +69,7 @@ __device__ void point_features(const FeatArgs &a, int64_t i, float *f) {
     const int64_t np = a.npad;
     constexpr int NG = D * (D + 1) / 2;
     float qi[4], qmax[4], qmin[4], s1[4], s2[4], b[4][D], G[NG];
-    quantities<T, D, M, PDE>(U + i * M, a.gm1, qi);
+    quantities<T, D, M, PDE>(U + i * M, qi);
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
         qmax[m] = qi[m];
@@ -81,27 +82,42 @@ __device__ void point_features(const FeatArgs &a, int64_t i, float *f) {
 #pragma unroll
     for (int e = 0; e < NG; ++e) G[e] = 0.f;
     const int c = a.cnt[i];
-    for (int k = 0; k < c; ++k) {
-        const int32_t j = a.nidx[int64_t(k) * np + i];
-        float x[D];
+    // four slots in flight per thread (independent loads first), accumulated in slot order; slot-major pointers
+    // advance by whole slots
+    constexpr int U4 = 4;
+    const int32_t *pn = a.nidx + i;
+    const T *pd = dist + i;
+    for (int k0 = 0; k0 < c; k0 += U4, pn += U4 * np, pd += U4 * D * np) {
+        int32_t jj[U4];
+        float xx[U4][D], qq[U4][4];
 #pragma unroll
-        for (int d = 0; d < D; ++d) x[d] = float(dist[(int64_t(k) * D + d) * np + i]);
-        int e = 0;
+        for (int u = 0; u < U4; ++u) jj[u] = k0 + u < c ? pn[u * np] : int32_t(i);
 #pragma unroll
-        for (int p = 0; p < D; ++p)
+        for (int u = 0; u < U4; ++u)
 #pragma unroll
-            for (int q = p; q < D; ++q) G[e++] += x[p] * x[q];
-        float qj[4];
-        quantities<T, D, M, PDE>(U + int64_t(j) * M, a.gm1, qj);
+            for (int d = 0; d < D; ++d) xx[u][d] = k0 + u < c ? float(pd[(u * D + d) * np]) : 0.f;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            const float dq = qj[m] - qi[m];
-            s1[m] += dq;
-            s2[m] += dq * dq;
+        for (int u = 0; u < U4; ++u) quantities<T, D, M, PDE>(U + int64_t(jj[u]) * M, qq[u]);
 #pragma unroll
-            for (int d = 0; d < D; ++d) b[m][d] += dq * x[d];
-            qmax[m] = qj[m] > qmax[m] ? qj[m] : qmax[m];
-            qmin[m] = qj[m] < qmin[m] ? qj[m] : qmin[m];
+        for (int u = 0; u < U4; ++u) {
+            if (k0 + u >= c) break;
+            const float *x = xx[u];
+            int e = 0;
+#pragma unroll
+            for (int p = 0; p < D; ++p)
+#pragma unroll
+                for (int q = p; q < D; ++q) { G[e] = fmaf(x[p], x[q], G[e]); ++e; }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const float qj = qq[u][m];
+                const float dq = qj - qi[m];
+                s1[m] += dq;
+                s2[m] = fmaf(dq, dq, s2[m]);
+#pragma unroll
+                for (int d = 0; d < D; ++d) b[m][d] = fmaf(dq, x[d], b[m][d]);
+                qmax[m] = qj > qmax[m] ? qj : qmax[m];
+                qmin[m] = qj < qmin[m] ? qj : qmin[m];
+            }
         }
     }
     // least-squares gradient g = G^-1 b (cofactors; no solve where det <= 0)
@@ -125,26 +141,27 @@ __device__ void point_features(const FeatArgs &a, int64_t i, float *f) {
         det = (G[0] * Gi[0] + G[1] * Gi[1]) + G[2] * Gi[2];
     }
     const bool solve = det > 0.f;
+    const float idet = solve ? 1.f / det : 0.f;
     const float h = a.h;
     const float ic = c > 0 ? 1.f / float(c) : 0.f;
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
         float g[D];
         if constexpr (D == 1) {
-            g[0] = solve ? b[m][0] / det : 0.f;
+            g[0] = b[m][0] * idet;
         } else if constexpr (D == 2) {
-            g[0] = solve ? (Gi[0] * b[m][0] + Gi[1] * b[m][1]) / det : 0.f;
-            g[1] = solve ? (Gi[1] * b[m][0] + Gi[2] * b[m][1]) / det : 0.f;
+            g[0] = fmaf(Gi[0], b[m][0], Gi[1] * b[m][1]) * idet;
+            g[1] = fmaf(Gi[1], b[m][0], Gi[2] * b[m][1]) * idet;
         } else {
-            g[0] = solve ? ((Gi[0] * b[m][0] + Gi[1] * b[m][1]) + Gi[2] * b[m][2]) / det : 0.f;
-            g[1] = solve ? ((Gi[1] * b[m][0] + Gi[3] * b[m][1]) + Gi[4] * b[m][2]) / det : 0.f;
-            g[2] = solve ? ((Gi[2] * b[m][0] + Gi[4] * b[m][1]) + Gi[5] * b[m][2]) / det : 0.f;
+            g[0] = fmaf(Gi[0], b[m][0], fmaf(Gi[1], b[m][1], Gi[2] * b[m][2])) * idet;
+            g[1] = fmaf(Gi[1], b[m][0], fmaf(Gi[3], b[m][1], Gi[4] * b[m][2])) * idet;
+            g[2] = fmaf(Gi[2], b[m][0], fmaf(Gi[4], b[m][1], Gi[5] * b[m][2])) * idet;
         }
         float bgb = 0.f, gg = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            bgb += b[m][d] * g[d];
-            gg += g[d] * g[d];
+            bgb = fmaf(b[m][d], g[d], bgb);
+            gg = fmaf(g[d], g[d], gg);
         }
         const float r = qmax[m] - qmin[m];
         const float sc = fabsf(qmax[m]) + fabsf(qmin[m]);
@@ -179,9 +196,27 @@ __global__ void __launch_bounds__(128) k_features(FeatArgs a, float *out) {
 }
 
 // --------------------------------------------------------------------------------------------- the network
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+// GELU x Phi(x) with the normal CDF Phi replaced by an odd degree-9 polynomial on [-3.2, 3.2] (least-squares fit of
+// Phi - 1/2, |error| <= 1.1e-3; held at its end values outside): FMA-pipe arithmetic only, no special-function unit.
+constexpr float ACT_L = 3.2f, ACT_C1 = 0.397573032f, ACT_C3 = -0.0633290983f, ACT_C5 = 0.00785629494f,
+                ACT_C7 = -0.000559308202f, ACT_C9 = 0.0000167396374f;
+__device__ __forceinline__ float act_phi(float x, float &xc, float &u) {
+    xc = fminf(fmaxf(x, -ACT_L), ACT_L);
+    u = xc * xc;
+    const float P = fmaf(fmaf(fmaf(fmaf(ACT_C9, u, ACT_C7), u, ACT_C5), u, ACT_C3), u, ACT_C1);
+    return fmaf(xc, P, 0.5f);
+}
+__device__ __forceinline__ float gelu(float x) {
+    float xc, u;
+    return x * act_phi(x, xc, u);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
-    return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * (0.39894228040143268f * expf(-0.5f * x * x));
+    float xc, u;
+    const float phi = act_phi(x, xc, u);
+    const float P = fmaf(fmaf(fmaf(fmaf(ACT_C9, u, ACT_C7), u, ACT_C5), u, ACT_C3), u, ACT_C1);
+    const float dP = fmaf(fmaf(fmaf(4.f * ACT_C9, u, 3.f * ACT_C7), u, 2.f * ACT_C5), u, ACT_C3);
+    const float dphi = fabsf(x) < ACT_L ? fmaf(2.f * u, dP, P) : 0.f;
+    return fmaf(x, dphi, phi);
 }
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -224,6 +259,29 @@ __device__ void load_weight_images(const MlpWeights &w, uint8_t *w1, uint8_t *w2
         *reinterpret_cast<__nv_bfloat16 *>(w2 + tc::kmajor_offset(o, h, NH)) = W2[e];
         if (w2n) *reinterpret_cast<__nv_bfloat16 *>(w2n + tc::kmajor_offset(h, o, NH)) = W2[e];
     }
+}
+
+// Normalised features of one row as four 16-byte segments (8 BF16 each; columns 24-31 zero).
+__device__ __forceinline__ void pack_feature_row(const float *f, const float *mean, const float *istd, uint4 *seg) {
+#pragma unroll
+    for (int c8 = 0; c8 < KF / 8; ++c8) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int f0 = c8 * 8 + 2 * q;
+            const float x0 = f0 < NF ? (f[f0] - mean[f0]) * istd[f0] : 0.f;
+            const float x1 = f0 + 1 < NF ? (f[f0 + 1] - mean[f0 + 1]) * istd[f0 + 1] : 0.f;
+            pk[q] = pack_bf16(x0, x1);
+        }
+        seg[c8] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+}
+
+// A row that passes the smoothness gate: some quantity's relative stencil range exceeds GATE (features 0, 6, 12,
+// 18). Rows below it are predicted untroubled without the network (their stencils are flat to FP32 resolution).
+constexpr float GATE = 1e-6f;
+__device__ __forceinline__ bool passes_gate(const float *f) {
+    return fmaxf(fmaxf(f[0], f[6]), fmaxf(f[12], f[18])) > GATE;
 }
 
 // Normalised features of one row into the row's 16-byte core-matrix segments of a K = 32 operand.
@@ -284,11 +342,15 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Src src, MlpWeights w, int nt
     constexpr uint32_t ID = tc::idesc_bf16(128, NH);
     uint32_t phase = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int nt = src.tiles(ntiles);
+    for (int tile = blockIdx.x; tile < nt; tile += gridDim.x) {
         const int64_t i = int64_t(tile) * 128 + r;
-        float f[NF];
-        const bool valid = src.features(i, f);
-        store_feature_row(sm + InferSmem::ACT, r, f, valid, par, nullptr);
+        uint4 seg[KF / 8];
+        const bool valid = src.load_row(i, par, seg);
+#pragma unroll
+        for (int c8 = 0; c8 < KF / 8; ++c8)
+            *reinterpret_cast<uint4 *>(sm + InferSmem::ACT + tc::kmajor_offset(r, c8 * 8, KF)) =
+                valid ? seg[c8] : make_uint4(0u, 0u, 0u, 0u);
         tc::fence_async_smem();
         tc::fence_before_sync();
         __syncthreads();
@@ -349,28 +411,74 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Src src, MlpWeights w, int nt
     }
 }
 
-// Features from the cloud; pre-lowers the predicted interior particles.
-template <typename T, int D, int M, int PDE> struct CloudSrc {
-    FeatArgs a;
+// In-step prediction, pass 1 (one thread per particle, full occupancy): the features of every interior particle;
+// the rows that pass the smoothness gate are normalised to BF16 and appended to a compact list; the mask of
+// predicted particles is cleared; optionally the raw features of every particle are written (training capture).
+template <typename T, int D, int M, int PDE>
+__global__ void __launch_bounds__(128, 7) k_features_gate(FeatArgs a, PredictOut o, const float *norm, float *raw) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool take = false;
+    uint4 seg[KF / 8];
+    if (i < a.n) {
+        if (o.pred) o.pred[i] = 0;
+        if (raw || !a.bnd[i]) {
+            float f[NF];
+            point_features<T, D, M, PDE>(a, i, f);
+            if (raw) {
+#pragma unroll
+                for (int t = 0; t < NF; ++t) raw[i * NF + t] = f[t];
+            }
+            if (o.rows && !a.bnd[i] && passes_gate(f)) {
+                take = true;
+                pack_feature_row(f, norm, norm + NF, seg);
+            }
+        }
+    }
+    if (!o.rows) return;
+    const unsigned bits = __ballot_sync(0xffffffffu, take);
+    if (!bits) return;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == __ffs(bits) - 1) base = atomicAdd(o.nrows, (unsigned long long)__popc(bits));
+    base = __shfl_sync(0xffffffffu, base, __ffs(bits) - 1);
+    if (take) {
+        const int64_t slot = int64_t(base) + __popc(bits & ((1u << lane) - 1u));
+        if (slot < o.cap) {
+#pragma unroll
+            for (int c8 = 0; c8 < KF / 8; ++c8) o.rows[slot * (KF / 8) + c8] = seg[c8];
+            o.row_idx[slot] = int32_t(i);
+        }
+    }
+}
+
+// In-step prediction, pass 2: the network on the compact rows; hits are pre-lowered.
+struct CompactSrc {
     PredictOut o;
-    __device__ bool features(int64_t i, float *f) const {
-        if (i >= a.n || a.bnd[i]) return false;
-        point_features<T, D, M, PDE>(a, i, f);
+    __device__ int tiles(int) const {
+        const long long n = std::min<long long>((long long)*o.nrows, o.cap);
+        return int((n + 127) / 128);
+    }
+    __device__ bool load_row(int64_t i, const float *, uint4 *seg) const {
+        if (i >= std::min<long long>((long long)*o.nrows, o.cap)) return false;
+#pragma unroll
+        for (int c8 = 0; c8 < KF / 8; ++c8) seg[c8] = o.rows[i * (KF / 8) + c8];
         return true;
     }
     __device__ void emit(int64_t i, bool valid, float logit) const {
         const bool hit = valid && logit > o.thr_logit;
-        if (i < a.n) {
-            o.pred[i] = hit ? 1 : 0;
-            if (o.logits) o.logits[i] = valid ? logit : 0.f;
-            if (hit) o.orders[i] = o.lowered;
+        if (hit) {
+            const int32_t p = o.row_idx[i];
+            o.pred[p] = 1;
+            o.orders[p] = o.lowered;
+            if (o.logits) o.logits[p] = logit;
         }
         const unsigned bits = __ballot_sync(0xffffffffu, hit);
         if ((threadIdx.x & 31) == 0 && bits) atomicAdd(o.count, (unsigned long long)__popc(bits));
     }
 };
 
-// Features from rows X[start + i][24]; logits out and/or confusion counts {tp, fp, fn, tn} against labels Y.
+// Features from rows X[start + i][24]; logits out (-inf for rows below the smoothness gate) and/or confusion
+// counts {tp, fp, fn, tn} against labels Y (gated rows count as predicted untroubled).
 struct RowSrc {
     const float *X;
     const uint8_t *Y;
@@ -378,16 +486,28 @@ struct RowSrc {
     float *logits;
     unsigned long long *counts;
     float thr_logit;
-    __device__ bool features(int64_t i, float *f) const {
+    __device__ int tiles(int ntiles) const { return ntiles; }
+    __device__ bool load_row(int64_t i, const float *par, uint4 *seg) const {
         if (i >= n) return false;
+        float f[NF];
 #pragma unroll
         for (int t = 0; t < NF; ++t) f[t] = X[(start + i) * NF + t];
+        pack_feature_row(f, par + P_MEAN, par + P_ISTD, seg);
         return true;
     }
     __device__ void emit(int64_t i, bool valid, float logit) const {
-        if (valid && logits) logits[i] = logit;
+        bool gated = false;
+        if (valid) {
+            float f[NF];
+            f[0] = X[(start + i) * NF + 0];
+            f[6] = X[(start + i) * NF + 6];
+            f[12] = X[(start + i) * NF + 12];
+            f[18] = X[(start + i) * NF + 18];
+            gated = !passes_gate(f);
+        }
+        if (valid && logits) logits[i] = gated ? -INFINITY : logit;
         if (counts) {
-            const bool p = valid && logit > thr_logit, y = valid && Y[start + i] != 0;
+            const bool p = valid && !gated && logit > thr_logit, y = valid && Y[start + i] != 0;
             const unsigned tp = __ballot_sync(0xffffffffu, valid && p && y);
             const unsigned fp = __ballot_sync(0xffffffffu, valid && p && !y);
             const unsigned fn = __ballot_sync(0xffffffffu, valid && !p && y);
@@ -767,12 +887,19 @@ bool launch_features(const FeatArgs &fa, float *out, cudaStream_t s) {
     });
 }
 
-bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, int grid, unsigned *err,
-                    cudaStream_t s) {
+bool launch_predict(const FeatArgs &fa, const MlpWeights &w, const PredictOut &po, float *raw, int grid,
+                    unsigned *err, cudaStream_t s) {
+    if (fa.n == 0) return true;
     return with_physics(fa.f32, fa.D, fa.M, fa.pde, [&](auto t, auto d, auto m, auto p) {
         using T = typename decltype(t)::type;
-        CloudSrc<T, decltype(d)::value, decltype(m)::value, decltype(p)::value> src{fa, po};
-        launch_infer(src, w, fa.n, grid, err, s);
+        k_features_gate<T, decltype(d)::value, decltype(m)::value, decltype(p)::value>
+            <<<unsigned((fa.n + 127) / 128), 128, 0, s>>>(fa, po, w.norm, raw);
+        if (po.rows) {
+            CompactSrc src{po};
+            const int ntiles = int((fa.n + 127) / 128);
+            k_mlp_infer<CompactSrc><<<std::max(1, std::min(grid, ntiles)), 128, InferSmem::SIZE, s>>>(src, w, ntiles,
+                                                                                                       err);
+        }
     });
 }
 

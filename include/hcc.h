@@ -295,14 +295,16 @@ hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n, int64_t n
 
 /* ------------------------------------------------------------------ learned troubled-point predictor
    No counterpart in the reference (its MOOD loop computes every particle at full order first, MOOD.jl:375-405).
-   A small MLP (24 -> 64 -> 64 -> 1, GELU, BF16 weights and activations on the tensor cores, FP32 accumulate)
+   A small MLP (24 -> 64 -> 64 -> 1, GELU with a polynomial normal CDF, BF16 weights and activations on the tensor
+   cores, FP32 accumulate)
    reads 24 stencil features of the start-of-step state and pre-lowers the order of the particles it predicts to be
    troubled (one order, as a MOOD drop), before the step's first reconstruction. Full MOOD still runs on every
    particle as the judge; the predictor only saves recompute passes. The network is trained on the device (forward
    and backward kernels, Adam) on (feature, MOOD-flag) pairs the solver itself generates.
 
-   Features, per particle i, from its neighbours j (offsets x_ij) and four quantities q (Euler: density, pressure,
-   momentum magnitude, total energy; other systems: components 0..3, the last repeated), six per quantity, in FP32:
+   Features, per particle i, from its neighbours j (offsets x_ij) and four quantities q (Euler: density,
+   rho E - |m|^2 / 2 (= rho p / (gamma - 1)), |m|^2, total energy E; other systems: components 0..3, the last
+   repeated), six per quantity, in FP32:
    range / (|max| + |min|), (2 q_i - max - min) / range, (q_i - mean_j q_j) / range, RMS residual of the
    least-squares linear fit / range, |gradient| h / range, RMS deviation / range; max/min over {i} + N(i); the last
    five are 0 where range <= 1e-6 (|max| + |min|); every feature is clamped to [-8, 8] (NaN -> 0). */

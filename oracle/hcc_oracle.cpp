@@ -1693,18 +1693,19 @@ namespace {
 
 // Stencil features of the learned troubled-point predictor (no counterpart in the reference; definitions in
 // include/hcc.h): four quantities per particle, six FP32 features each, in the operation order of the GPU kernel.
-void feature_quantities(const Solver &s, const double *u, float gm1, float q[4]) {
+void feature_quantities(const Solver &s, const double *u, float q[4]) {
     if (s.cfg.pde == HCC_PDE_EULER) {
+        // density, rho * (rho e), |momentum|^2, total energy
         const float rho = float(u[0]);
         float msq = 0.f;
         for (int d = 0; d < s.D; ++d) {
             const float md = float(u[1 + d]);
-            msq = msq + md * md;
+            msq = std::fma(md, md, msq);
         }
         const float E = float(u[s.D + 1]);
         q[0] = rho;
-        q[1] = gm1 * (E - (0.5f * msq) / rho);
-        q[2] = std::sqrt(msq);
+        q[1] = std::fma(E, rho, -(0.5f * msq));
+        q[2] = msq;
         q[3] = E;
     } else {
         for (int m = 0; m < 4; ++m) q[m] = float(u[m < s.M ? m : s.M - 1]);
@@ -1716,10 +1717,10 @@ float clamp_feature(float f) {
     return f > 8.f ? 8.f : (f < -8.f ? -8.f : f);
 }
 
-void point_features(const Solver &s, int64_t i, float h, float gm1, float *f) {
+void point_features(const Solver &s, int64_t i, float h, float *f) {
     const int D = s.D;
     float qi[4], qmax[4], qmin[4], s1[4] = {0, 0, 0, 0}, s2[4] = {0, 0, 0, 0}, b[4][3] = {}, G[6] = {};
-    feature_quantities(s, &s.rhos[i * s.M], gm1, qi);
+    feature_quantities(s, &s.rhos[i * s.M], qi);
     for (int m = 0; m < 4; ++m) { qmax[m] = qi[m]; qmin[m] = qi[m]; }
     const int64_t k0 = s.start[i], c = s.start[i + 1] - s.start[i];
     for (int64_t k = 0; k < c; ++k) {
@@ -1729,14 +1730,14 @@ void point_features(const Solver &s, int64_t i, float h, float gm1, float *f) {
         for (int d = 0; d < D; ++d) x[d] = float(s.ndist[slot * D + d]);
         int e = 0;
         for (int p = 0; p < D; ++p)
-            for (int q = p; q < D; ++q) G[e++] += x[p] * x[q];
+            for (int q = p; q < D; ++q) { G[e] = std::fma(x[p], x[q], G[e]); ++e; }
         float qj[4];
-        feature_quantities(s, &s.rhos[j * s.M], gm1, qj);
+        feature_quantities(s, &s.rhos[j * s.M], qj);
         for (int m = 0; m < 4; ++m) {
             const float dq = qj[m] - qi[m];
             s1[m] += dq;
-            s2[m] += dq * dq;
-            for (int d = 0; d < D; ++d) b[m][d] += dq * x[d];
+            s2[m] = std::fma(dq, dq, s2[m]);
+            for (int d = 0; d < D; ++d) b[m][d] = std::fma(dq, x[d], b[m][d]);
             qmax[m] = qj[m] > qmax[m] ? qj[m] : qmax[m];
             qmin[m] = qj[m] < qmin[m] ? qj[m] : qmin[m];
         }
@@ -1759,23 +1760,24 @@ void point_features(const Solver &s, int64_t i, float h, float gm1, float *f) {
         det = (G[0] * Gi[0] + G[1] * Gi[1]) + G[2] * Gi[2];
     }
     const bool solve = det > 0.f;
+    const float idet = solve ? 1.f / det : 0.f;
     const float ic = c > 0 ? 1.f / float(c) : 0.f;
     for (int m = 0; m < 4; ++m) {
         float g[3] = {0, 0, 0};
         if (D == 1) {
-            g[0] = solve ? b[m][0] / det : 0.f;
+            g[0] = b[m][0] * idet;
         } else if (D == 2) {
-            g[0] = solve ? (Gi[0] * b[m][0] + Gi[1] * b[m][1]) / det : 0.f;
-            g[1] = solve ? (Gi[1] * b[m][0] + Gi[2] * b[m][1]) / det : 0.f;
+            g[0] = std::fma(Gi[0], b[m][0], Gi[1] * b[m][1]) * idet;
+            g[1] = std::fma(Gi[1], b[m][0], Gi[2] * b[m][1]) * idet;
         } else {
-            g[0] = solve ? ((Gi[0] * b[m][0] + Gi[1] * b[m][1]) + Gi[2] * b[m][2]) / det : 0.f;
-            g[1] = solve ? ((Gi[1] * b[m][0] + Gi[3] * b[m][1]) + Gi[4] * b[m][2]) / det : 0.f;
-            g[2] = solve ? ((Gi[2] * b[m][0] + Gi[4] * b[m][1]) + Gi[5] * b[m][2]) / det : 0.f;
+            g[0] = std::fma(Gi[0], b[m][0], std::fma(Gi[1], b[m][1], Gi[2] * b[m][2])) * idet;
+            g[1] = std::fma(Gi[1], b[m][0], std::fma(Gi[3], b[m][1], Gi[4] * b[m][2])) * idet;
+            g[2] = std::fma(Gi[2], b[m][0], std::fma(Gi[4], b[m][1], Gi[5] * b[m][2])) * idet;
         }
         float bgb = 0.f, gg = 0.f;
         for (int d = 0; d < D; ++d) {
-            bgb += b[m][d] * g[d];
-            gg += g[d] * g[d];
+            bgb = std::fma(b[m][d], g[d], bgb);
+            gg = std::fma(g[d], g[d], gg);
         }
         const float r = qmax[m] - qmin[m];
         const float sc = std::fabs(qmax[m]) + std::fabs(qmin[m]);
@@ -1922,9 +1924,9 @@ hcc_status orc_features(orc_ctx *ctx, float *out) {
     if (!s.have_nb) return HCC_ERR_STATE;
     double hm = s.cfg.dx[0];
     for (int d = 1; d < s.D; ++d) hm = std::min(hm, s.cfg.dx[d]);
-    const float h = float(hm), gm1 = float(s.cfg.gamma - 1.0);
+    const float h = float(hm);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < s.N; ++i) point_features(s, i, h, gm1, out + i * HCC_MLP_FEATURES);
+    for (int64_t i = 0; i < s.N; ++i) point_features(s, i, h, out + i * HCC_MLP_FEATURES);
     return HCC_OK;
 }
 hcc_status orc_set_prelowered(orc_ctx *ctx, const uint8_t *mask) {

@@ -30,6 +30,16 @@ except ImportError:  # pragma: no cover
     _erf = np.vectorize(math.erf, otypes=[np.float64])
 
 
+GATE = np.float32(1e-6)
+
+
+def gated(X) -> np.ndarray:
+    """Rows the kernels predict untroubled without the network: every quantity's relative stencil range (features
+    0, 6, 12, 18) is at most GATE."""
+    X = np.asarray(X, dtype=np.float32)
+    return X[:, [0, 6, 12, 18]].max(axis=1) <= GATE
+
+
 def bf16(x) -> np.ndarray:
     """Round FP32 values to BF16 (round to nearest, ties to even), returned as FP32."""
     a = np.ascontiguousarray(x, dtype=np.float32)
@@ -40,12 +50,35 @@ def bf16(x) -> np.ndarray:
     return np.where(np.isnan(a), a, out)
 
 
+# GELU x Phi(x) with Phi replaced by the kernels' odd degree-9 polynomial on [-3.2, 3.2] (held at its end values
+# outside); the coefficients are the FP32 constants of the kernels.
+ACT_L = np.float32(3.2)
+ACT_C = [np.float32(v) for v in (0.397573032, -0.0633290983, 0.00785629494, -0.000559308202, 0.0000167396374)]
+
+
+def _act_poly(x):
+    xc = np.clip(np.asarray(x, dtype=np.float64), -float(ACT_L), float(ACT_L))
+    u = xc * xc
+    c1, c3, c5, c7, c9 = (float(c) for c in ACT_C)
+    P = (((c9 * u + c7) * u + c5) * u + c3) * u + c1
+    dP = ((4 * c9 * u + 3 * c7) * u + 2 * c5) * u + c3
+    return xc, u, P, dP
+
+
 def gelu(x):
-    return 0.5 * x * (1.0 + _erf(x / math.sqrt(2.0)))
+    xc, u, P, _ = _act_poly(x)
+    return np.asarray(x, dtype=np.float64) * (0.5 + xc * P)
 
 
 def gelu_grad(x):
-    return 0.5 * (1.0 + _erf(x / math.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / math.sqrt(2.0 * math.pi)
+    x = np.asarray(x, dtype=np.float64)
+    xc, u, P, dP = _act_poly(x)
+    dphi = np.where(np.abs(x) < float(ACT_L), P + 2.0 * u * dP, 0.0)
+    return (0.5 + xc * P) + x * dphi
+
+
+def normal_cdf(x):
+    return 0.5 * (1.0 + _erf(np.asarray(x, dtype=np.float64) / math.sqrt(2.0)))
 
 
 def softplus(x):
