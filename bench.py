@@ -266,7 +266,7 @@ def load_predictor(hcc):
     return pred
 
 
-PREDICTOR_THRESHOLD = 0.7
+PREDICTOR_THRESHOLD = 0.9
 
 
 def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_dt=None, acc_steps=0,
@@ -437,6 +437,7 @@ def run_gpu(args):
                      "flux_ms_per_launch": flux_ms,
                      "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
                      "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
+                     "predict_ms_per_step": kt["predict_ms"] / max(kt["steps"], 1),
                      "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps"},
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],

@@ -90,7 +90,7 @@ class HccMlpConfig(C.Structure):
 class HccKernelTimes(C.Structure):
     _fields_ = [("gather_ms", C.c_double), ("gather_launches", C.c_int64), ("flux_ms", C.c_double),
                 ("flux_launches", C.c_int64), ("recompute_ms", C.c_double), ("recompute_launches", C.c_int64),
-                ("steps", C.c_int64)]
+                ("steps", C.c_int64), ("predict_ms", C.c_double), ("predict_launches", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -281,6 +281,7 @@ struct hcc_ctx {
             cudaEventElapsedTime(&ms, ev_pool[q], ev_pool[q + 1]);
             if (ev_kind[q / 2] == 0) { times.gather_ms += ms; times.gather_launches += 1; }
             else if (ev_kind[q / 2] == 1) { times.flux_ms += ms; times.flux_launches += 1; }
+            else if (ev_kind[q / 2] == 3) { times.predict_ms += ms; times.predict_launches += 1; }
             else { times.recompute_ms += ms; times.recompute_launches += 1; }
         }
         ev_used = 0;
@@ -672,9 +673,12 @@ int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
             po.row_idx = c->pred_idx;
             po.nrows = &c->mood_stats->pred_rows;
             po.cap = c->n;
+            const bool prof = c->prof && st == c->stream;
+            if (prof) c->prof_begin(3);
             if (launch_predict(fa, mlp_weights(c->mlp), po, c->capture_feat ? c->feat : nullptr,
                                std::max(1, c->list_blocks / 8) * 2, &c->mood_stats->tc_error, st))
                 k += 2;
+            if (prof) c->prof_end();
         } else if (launch_features(fa, c->feat, st)) {
             k += 1;
         }

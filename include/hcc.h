@@ -272,6 +272,8 @@ typedef struct {
     double recompute_ms;         /* MOOD recompute passes (masked gather + flux) */
     int64_t recompute_launches;
     int64_t steps;
+    double predict_ms;           /* troubled-point predictor (feature pass + network), when one is attached */
+    int64_t predict_launches;
 } hcc_kernel_times;
 hcc_status hcc_set_profiling(hcc_ctx *ctx, int enable);
 hcc_status hcc_get_kernel_times(hcc_ctx *ctx, hcc_kernel_times *out, int reset);
