@@ -119,16 +119,38 @@ class MUSCL:
     flux: str = "rusanov"
 
 
-def Upwind(div_order: int = 0, flux: str = "rusanov") -> MUSCL:
-    """UpwindDivergence(T, D, M, 1, :Classic, flux; div_order) (src/Interpolation/Upwind.jl): piecewise-constant
-    states, the numerical flux per pair and the MLS divergence of degree 1 — the first-order MUSCL scheme (the
-    reference's unit test unit_core.jl:937-945 holds the two equal to 1e-12)."""
-    return MUSCL(1, div_order, "none", flux)
+@dataclass
+class UpwindDivergence:
+    """UpwindDivergence(T, D, 1, 1, algorithm, flux; div_order) with algorithm :Tiwari (per axis the upwind-side
+    gradient fit times v_d) or :Praveen (2-D, edge-normal / tangential upwind coefficients), Upwind.jl:158-249."""
+    algorithm: str = "Tiwari"
+    div_order: int = 0
+    order: int = 1
+
+
+def Upwind(div_order: int = 0, flux: str = "rusanov", algorithm: str = "Classic"):
+    """UpwindDivergence(T, D, M, 1, algorithm, flux; div_order) (src/Interpolation/Upwind.jl). :Classic —
+    piecewise-constant states, the numerical flux per pair and the MLS divergence of degree 1 — is the first-order
+    MUSCL scheme (the reference's unit test unit_core.jl:937-945 holds the two equal to 1e-12); :Tiwari and
+    :Praveen are scalar-only schemes of their own."""
+    if algorithm == "Classic":
+        return MUSCL(1, div_order, "none", flux)
+    if algorithm not in _abi.UPWIND_ALGORITHMS:
+        raise ValueError(f"unknown upwind algorithm {algorithm!r}")
+    return UpwindDivergence(algorithm, div_order)
 
 
 @dataclass
 class WENO:
     """WENO(T, D, 1, order; div_order) (src/Interpolation/WENO.jl:43): scalar equations only."""
+    order: int = 2
+    div_order: int = 0
+
+
+@dataclass
+class CentralDivergence:
+    """CentralDivergence(T, D, M, order; div_order) (src/Interpolation/Central.jl:45-88): the divergence of F_j - F_i
+    by the MLS intercept fit of degree = the particle's order (capped by div_order), no reconstruction."""
     order: int = 2
     div_order: int = 0
 
@@ -213,6 +235,11 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
     cfg.div_order = scheme.div_order
     if isinstance(scheme, WENO):
         cfg.scheme = _abi.SCHEME_WENO
+    elif isinstance(scheme, CentralDivergence):
+        cfg.scheme = _abi.SCHEME_CENTRAL
+    elif isinstance(scheme, UpwindDivergence):
+        cfg.scheme = _abi.SCHEME_UPWIND
+        cfg.upwind_algorithm = _abi.UPWIND_ALGORITHMS[scheme.algorithm]
     else:
         cfg.scheme = _abi.SCHEME_MUSCL
         cfg.limiter = _abi.LIMITERS[scheme.limiter]
@@ -486,7 +513,7 @@ from .learned import TroubledPointPredictor  # noqa: E402
 
 __all__ = [
     "TroubledPointPredictor",
-    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "WENO", "mover", "MOOD", "MOODu1", "MOODu2",
+    "HCCError", "load_library", "LinearAdvection", "Euler", "KineticRelaxation", "MUSCL", "Upwind", "UpwindDivergence", "WENO", "CentralDivergence", "mover", "MOOD", "MOODu1", "MOODu2",
     "MOODPAD", "OnlyMOOD", "NoMOOD", "EPD_NONE", "EPD0", "EPD1", "EPD2", "STRICT_EPD0", "make_config", "Context",
     "GB300RKTimeStepper", "Cloud", "rectangular_cloud", "morton_permutation", "splitmix64_uniform", "TABLEAUS",
     "BC_KEEP", "BC_DIRICHLET", "BC_OUTFLOW", "HccConfig",

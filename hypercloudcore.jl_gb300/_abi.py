@@ -29,7 +29,8 @@ TABLEAUS = {
     "IMEX_Euler": 6, "IMEX_ARS233": 7, "IMEX_ARS222": 8, "IMEX_PRSSP3": 9, "IMEX_SSP2332": 10,
 }
 # hcc_scheme / hcc_limiter
-SCHEME_MUSCL, SCHEME_WENO = 0, 1
+SCHEME_MUSCL, SCHEME_WENO, SCHEME_CENTRAL, SCHEME_UPWIND = 0, 1, 2, 3
+UPWIND_ALGORITHMS = {"Tiwari": 1, "Praveen": 2}
 LIMITERS = {"none": 0, "bj_soft": 1, "bj_hard": 2, "vk_soft": 3, "vk_hard": 4}
 # hcc_bc_kind
 BC_KEEP, BC_DIRICHLET, BC_OUTFLOW = 0, 1, 2
@@ -43,7 +44,7 @@ class HccConfig(C.Structure):
         ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
         ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
         ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("flux", C.c_int32),
-        ("reset_orders_per_stage", C.c_int32), ("reserved_i", C.c_int32 * 3),
+        ("reset_orders_per_stage", C.c_int32), ("upwind_algorithm", C.c_int32), ("reserved_i", C.c_int32 * 2),
         ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
         ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),

@@ -173,6 +173,12 @@ struct hcc_ctx {
     int max_order = 2, DO = 0, rdeg = 1, Br = 1, full_div = 2, ddeg = 1, Bd = 2, need_dw1 = 0;
     double invL = 1.0, h = 1.0;
     int weno = 0;
+    int central = 0;                  // CentralDivergence: no reconstruction, per-degree divergence weight sets
+    int upwind = 0;                   // UpwindDivergence :Tiwari / :Praveen (scalar, first order)
+    int qmax = 1;
+    double *dwc64[3] = {}; float *dwc32[3] = {}; uint8_t *okc[3] = {};
+    bool no_recon() const { return weno || central || upwind; }
+
     Tableau tab;
     double ssp_C = 0.0, ratio = 0.0;
     int has_source = 0;
@@ -328,6 +334,7 @@ struct hcc_ctx {
         drop_graphs();
         dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
         dfree(dw1_32); dfree(gw32);
+        for (int q = 0; q < 3; ++q) { dfree(dwc64[q]); dfree(dwc32[q]); dfree(okc[q]); }
     }
     void free_bins() { dfree(binnb); dfree(cell_count); dfree(cell_cursor); dfree(cell_start); }
 };
@@ -380,6 +387,11 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
         g.gw = c->gw32;
     }
     g.ok_r = c->ok_r; g.ok_d = c->ok_d; g.ok_1 = c->ok_1;
+    for (int q = 0; q < 3; ++q) {
+        if constexpr (sizeof(T) == 8) g.dwc[q] = c->dwc64[q];
+        else g.dwc[q] = c->dwc32[q];
+        g.okc[q] = c->okc[q];
+    }
     g.bnd = c->bnd;
     g.invL = T(c->invL);
     g.invL64 = c->invL;
@@ -391,6 +403,7 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.sc.criterion = c->cfg.mood_criterion;
     a.sc.has_source = c->has_source;
     a.sc.limiter = c->cfg.limiter;
+    a.sc.upwind_alg = c->upwind;
     a.sc.aligned = c->cfg.flux == HCC_FLUX_ALIGNED;
     a.orders = c->orders;
     a.nbmin = c->nbmin;
@@ -516,13 +529,19 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
     return a;
 }
 
+// The flux pass of the context's scheme (MUSCL, WENO or CentralDivergence).
+using PassFn = void (*)(const void *, int64_t, cudaStream_t);
+PassFn pass_op(const hcc_ctx *c) {
+    return c->weno ? c->ops->weno : c->central ? c->ops->central : c->upwind ? c->ops->upwind : c->ops->flux;
+}
+
 // Full pass of stage s: reconstruction, (EPD2 neighbourhood orders), flux with its fused epilogue (the failed
 // candidates go to the t list), and — without the MOOD check — the boundary conditions of the new candidate (with
 // the check they are part of the decrement launch). Returns the kernels launched.
 template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
     const int64_t n = c->n;
     int k = 0;
-    if (!c->weno) {
+    if (!c->no_recon()) {
         if (prof) c->prof_begin(0);
         c->ops->gather(&a, n, st);
         if (prof) c->prof_end();
@@ -537,7 +556,7 @@ template <typename T> int enqueue_full(hcc_ctx *c, const StageArgs<T> &a, cudaSt
         ++k;
     }
     if (prof) c->prof_begin(1);
-    (c->weno ? c->ops->weno : c->ops->flux)(&a, n, st);
+    pass_op(c)(&a, n, st);
     if (prof) c->prof_end();
     ++k;
     if (!a.check) {
@@ -579,7 +598,7 @@ int enqueue_drop(hcc_ctx *c, void *Y, cudaStream_t st, const cudaGraphConditiona
 // with the decrement launch that follows. Returns the kernels launched.
 template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
     const int64_t n = c->n;
-    const int hops = c->weno ? 0 : (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
+    const int hops = c->no_recon() ? 0 : (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
     int k = 0;
     if (c->cfg.mood_strategy == HCC_STRICT_EPD0) {
         launch_force(c->ctiles, c->cmask, c->lcounts, c->ctiles, c->orders, c->bnd, c->cnt, c->nidx, c->npad, c->forced,
@@ -615,7 +634,7 @@ template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, c
     fa.wmask = hops > 0 ? c->dmask : c->cmask;
     fa.clear_wmask = 1;
     if (prof) c->prof_begin(2);
-    (c->weno ? c->ops->weno : c->ops->flux)(&fa, n, st);
+    pass_op(c)(&fa, n, st);
     if (prof) c->prof_end();
     return k + 1;
 }
@@ -910,10 +929,10 @@ template <typename T> hcc_status run_rhs(hcc_ctx *c) {
     a.U = static_cast<const T *>(c->rhos);
     a.K = static_cast<T *>(c->KE[0]);
     a.full = 1;
-    if (!c->weno) c->ops->gather(&a, n, c->stream);
+    if (!c->no_recon()) c->ops->gather(&a, n, c->stream);
     if (c->cfg.mood_strategy == HCC_EPD2)
         launch_nbmin(c->orders, c->nbmin, c->cnt, c->nidx, n, c->npad, nullptr, nullptr, nullptr, 0, c->stream);
-    (c->weno ? c->ops->weno : c->ops->flux)(&a, n, c->stream);
+    pass_op(c)(&a, n, c->stream);
     hcc_status st = launch_check(c, "rhs kernels");
     if (st != HCC_OK) return st;
     return c->sync("rhs");
@@ -1006,7 +1025,9 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     if (f.flux < HCC_FLUX_RUSANOV || f.flux > HCC_FLUX_ALIGNED) return c->fail(HCC_ERR_INVALID, "unknown numerical flux");
     if (f.pde == HCC_PDE_BGK && !(f.bgk_epsilon > 0.0)) return c->fail(HCC_ERR_INVALID, "bgk_epsilon must be positive");
     if (f.limiter < HCC_LIMITER_NONE || f.limiter > HCC_LIMITER_VK_HARD) return c->fail(HCC_ERR_INVALID, "unknown limiter");
-    if (f.scheme != HCC_SCHEME_MUSCL && f.scheme != HCC_SCHEME_WENO) return c->fail(HCC_ERR_INVALID, "unknown scheme");
+    if (f.scheme != HCC_SCHEME_MUSCL && f.scheme != HCC_SCHEME_WENO && f.scheme != HCC_SCHEME_CENTRAL &&
+        f.scheme != HCC_SCHEME_UPWIND)
+        return c->fail(HCC_ERR_INVALID, "unknown scheme");
     c->max_order = f.muscl_order;
     c->DO = f.div_order > c->max_order ? c->max_order : f.div_order;
     if (c->DO < 0) return c->fail(HCC_ERR_INVALID, "div_order must be >= 0");
@@ -1023,8 +1044,24 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     c->invL = 1.0 / h;
     c->h = h;
     c->weno = f.scheme == HCC_SCHEME_WENO;
+    c->central = f.scheme == HCC_SCHEME_CENTRAL;
+    c->upwind = f.scheme == HCC_SCHEME_UPWIND ? f.upwind_algorithm : 0;
+    if (f.scheme == HCC_SCHEME_UPWIND) {
+        if (c->M != 1 || f.pde != HCC_PDE_ADVECTION)
+            return c->fail(HCC_ERR_INVALID, "UpwindDivergence :Tiwari / :Praveen are scalar (linear advection, n_vars 1)");
+        if (c->max_order != 1) return c->fail(HCC_ERR_INVALID, "UpwindDivergence is first order (muscl_order 1)");
+        if (c->upwind != HCC_UPWIND_TIWARI && c->upwind != HCC_UPWIND_PRAVEEN)
+            return c->fail(HCC_ERR_INVALID, "unknown upwind algorithm");
+        if (c->upwind == HCC_UPWIND_PRAVEEN && c->D != 2) return c->fail(HCC_ERR_INVALID, "Praveen is two-dimensional");
+        for (int d = 1; d < c->D; ++d)
+            if (f.dx[d] != f.dx[0])
+                return c->fail(HCC_ERR_UNSUPPORTED, "UpwindDivergence with anisotropic spacing");
+    }
+    c->qmax = c->DO == 0 ? c->max_order : c->DO;
     if (c->weno && (c->M != 1 || f.pde != HCC_PDE_ADVECTION))
         return c->fail(HCC_ERR_INVALID, "WENO is a scalar scheme: linear advection with n_vars = 1");
+    if (c->central && f.mood_criterion == HCC_MOOD_U2)
+        return c->fail(HCC_ERR_INVALID, "MOODu2 needs cached reconstruction gradients (MUSCL)");
     c->tab = make_tableau(f.tableau);
     if (c->tab.s == 0) return c->fail(HCC_ERR_INVALID, "unknown tableau");
     c->has_source = f.pde == HCC_PDE_BGK;
@@ -1039,10 +1076,14 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
         }
     }
     c->ratio = (f.mood_substeps && c->ssp_C > 0.0 && f.mood_criterion != HCC_MOOD_NONE) ? 1.0 / c->ssp_C : 0.0;
-    c->ops = find_ops(f, c->rdeg);
+    c->ops = find_ops(f, (c->central || c->upwind) ? 1 : c->rdeg);
     if (!c->ops) return c->fail(HCC_ERR_UNSUPPORTED, "this (dim, n_vars, pde) combination is not instantiated");
     if (c->weno && (!c->ops->weno || c->max_order > 3))
         return c->fail(HCC_ERR_UNSUPPORTED, "WENO of this dimension / order is not instantiated");
+    if (c->upwind && !c->ops->upwind)
+        return c->fail(HCC_ERR_UNSUPPORTED, "UpwindDivergence of this combination is not instantiated");
+    if (c->central && !c->ops->central)
+        return c->fail(HCC_ERR_UNSUPPORTED, "CentralDivergence of this combination is not instantiated");
     hcc_status st = c->cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
     if (st != HCC_OK) return st;
     if ((st = c->alloc(c->d_counters, 8, "counters")) != HCC_OK) return st;
@@ -1289,7 +1330,8 @@ hcc_status hcc_set_mover(hcc_ctx *c, const hcc_mover *mv) {
     const bool fluid = c->cfg.pde == HCC_PDE_EULER || (c->cfg.pde == HCC_PDE_ADVECTION && c->M == 1);
     if ((mv->kind == HCC_MOVER_LAGRANGIAN || mv->kind == HCC_MOVER_SCALED) && !fluid)
         return c->fail(HCC_ERR_UNSUPPORTED, "this system defines no fluid velocity (Lagrangian movers)");
-    if (mv->kind != HCC_MOVER_NONE && c->weno) return c->fail(HCC_ERR_UNSUPPORTED, "moving grids with WENO");
+    if (mv->kind != HCC_MOVER_NONE && c->no_recon())
+        return c->fail(HCC_ERR_UNSUPPORTED, "moving grids with WENO / CentralDivergence / UpwindDivergence");
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->drop_graphs();
     c->mover = *mv;
@@ -1427,7 +1469,18 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
     m.cnt = c->cnt; m.nidx = c->nidx; m.dist = c->dist64; m.w = c->w64; m.invL = c->invL;
     m.inv_r = c->inv_r64; m.ok_r = c->ok_r; m.inv_d = c->inv_d64; m.ok_d = c->ok_d;
     m.dw = c->dw64; m.dw1 = c->dw1_64; m.ok_1 = c->ok_1;
-    m.weno_cfl_degree = c->weno ? std::min(c->max_order, c->D == 3 ? 3 : 4) : 0;
+    // WENO / CentralDivergence: the CFL weights of the assembled Taylor fit of degree = the scheme's order
+    // (_divergence_degree, API.jl:236), and for Central its per-degree divergence weight sets
+    m.weno_cfl_degree = c->no_recon() ? std::min(c->max_order, c->D == 3 ? 3 : 4) : 0;
+    if (c->central) {
+        m.central_qmax = c->qmax;
+        for (int q = 0; q < c->qmax; ++q) {
+            HCC_TRY(c->alloc(c->dwc64[q], slots * D, "central weights"));
+            HCC_TRY(c->alloc(c->okc[q], size_t(c->npad), "central flags"));
+            m.dwc[q] = c->dwc64[q];
+            m.okc[q] = c->okc[q];
+        }
+    }
     if ((st = mls_prepare(m, c->stream, c->err)) != HCC_OK) return st;
     if (c->f32) {
         HCC_TRY(c->alloc(c->dist32, slots * D, "distances f32"));
@@ -1437,7 +1490,7 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
         launch_cast_f64_to_f32(c->w64, c->w32, int64_t(slots), c->stream);
         launch_cast_f64_to_f32(c->dw64, c->dw32, int64_t(slots) * D, c->stream);
         launch_cast_f64_to_f32(c->inv_r64, c->inv_r32, c->npad * c->Br * c->Br, c->stream);
-        if (c->rdeg == 1 && !c->weno) {
+        if (c->rdeg == 1 && !c->no_recon()) {
             HCC_TRY(c->alloc(c->gw32, slots * D, "gradient weights f32"));
             launch_grad_weights(c->n, c->npad, D, std::max(c->kmax, 1), c->cnt, c->dist64, c->w64, c->inv_r64, c->ok_r,
                                 c->invL, c->gw32, c->stream);
@@ -1445,6 +1498,10 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
         if (c->need_dw1) {
             HCC_TRY(c->alloc(c->dw1_32, slots * D, "degree-1 weights f32"));
             launch_cast_f64_to_f32(c->dw1_64, c->dw1_32, int64_t(slots) * D, c->stream);
+        }
+        for (int q = 0; q < (c->central ? c->qmax : 0); ++q) {
+            HCC_TRY(c->alloc(c->dwc32[q], slots * D, "central weights f32"));
+            launch_cast_f64_to_f32(c->dwc64[q], c->dwc32[q], int64_t(slots) * D, c->stream);
         }
     }
     // outflow donor roots, then the boundary list (tag -> condition)

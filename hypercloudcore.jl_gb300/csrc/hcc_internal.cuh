@@ -161,6 +161,7 @@ struct SchemeParams {
     int has_source;                   // BGK relaxation source present
     int limiter;                      // hcc_limiter
     int aligned;                      // AlignedRusanovFlux
+    int upwind_alg;                   // hcc_upwind_algorithm (HCC_SCHEME_UPWIND)
 };
 
 // Device view of the neighbour lists and geometry caches (slot-major, stride = npad).
@@ -177,6 +178,8 @@ template <typename T> struct Geometry {
     const T *gw;                      // FP32, degree-1 reconstruction: gradient weights of the cached fit,
                                       // [(k*D + b) * npad + i] = invL Σ_c inv_r[b][c] w_k x_k[c] (else nullptr)
     const uint8_t *bnd;
+    const T *dwc[3];                  // CentralDivergence: weights of the intercept fit of degree q = 1..3
+    const uint8_t *okc[3];
     T invL;
     double invL64;                    // 1/min(dx) in FP64 (the MLS fits of both paths)
     double h64;                       // min(dx)
@@ -301,6 +304,8 @@ struct StageOps {
     void (*stage1)(const void *args, int64_t n, cudaStream_t s);   // Y_1 (predictor + implicit part)
     void (*cfl)(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s);
     void (*weno)(const void *args, int64_t n, cudaStream_t s);   // WENO flux pass (scalar advection only)
+    void (*central)(const void *args, int64_t n, cudaStream_t s);   // CentralDivergence pass
+    void (*upwind)(const void *args, int64_t n, cudaStream_t s);    // UpwindDivergence :Tiwari / :Praveen pass
 };
 
 const StageOps *stage_ops_f64_r1(int D, int M, int pde);
@@ -349,6 +354,9 @@ struct MlsArgs {
     double *inv_d; uint8_t *ok_d;
     double *dw; double *dw1; uint8_t *ok_1;
     int weno_cfl_degree;              // > 0: per-slot CFL weights of the assembled Taylor fit (WENO), not MUSCL caches
+    int central_qmax;                 // > 0: CentralDivergence weight sets of degree 1..central_qmax
+    double *dwc[3];
+    uint8_t *okc[3];
 };
 hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err);
 

@@ -265,6 +265,40 @@ __global__ void k_mls(MlsArgs a) {
     }
 }
 
+// CentralDivergence weight set of degree q (Central.jl:45-88 with compute_dynamic_divergence,
+// Interpolators.jl:290-334, in the per-slot form of the MUSCL cache): rows 2..D+1 of inv(N) (w p~) invL for the
+// particles with basis_count(D, q) + 1 neighbours (the others never use degree q).
+template <int BM>
+__global__ void k_mls_central(MlsArgs a, int q) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int cnt = a.cnt[i];
+    const int B = c_tabs[a.D][q].B + 1;
+    double *dwq = a.dwc[q - 1];
+    bool ok = false;
+    double inv[BM * BM];
+    if (cnt >= B) ok = inverse_moment<BM>(a, i, cnt, q, true, B, inv);
+    a.okc[q - 1][i] = ok;
+    double x[3], p[BM], v[BM];
+    for (int k = 0; k < cnt; ++k) {
+        const int64_t s = int64_t(k) * a.npad + i;
+        if (!ok) {
+            for (int d = 0; d < a.D; ++d) dwq[(int64_t(k) * a.D + d) * a.npad + i] = 0.0;
+            continue;
+        }
+        for (int d = 0; d < a.D; ++d) x[d] = a.dist[(int64_t(k) * a.D + d) * a.npad + i] * a.invL;
+        gen_basis(a.D, q, true, x, p);
+        const double w = a.w[s];
+        for (int b = 0; b < B; ++b) v[b] = w * p[b];
+        for (int d = 0; d < a.D; ++d) {
+            const double *row = inv + (1 + d) * B;
+            double acc = row[0] * v[0];
+            for (int b = 1; b < B; ++b) acc = acc + row[b] * v[b];
+            dwq[(int64_t(k) * a.D + d) * a.npad + i] = acc * a.invL;
+        }
+    }
+}
+
 // ---- outflow donor map
 __global__ void k_donor_init(DonorArgs a, int tag, int first) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -307,12 +341,18 @@ hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err) {
     std::call_once(g_tabs_once, upload_tables);
     if (g_tabs_err != cudaSuccess) { err = std::string("basis tables: ") + cudaGetErrorString(g_tabs_err); return HCC_ERR_CUDA; }
     if (a.n == 0) return HCC_OK;
-    const int need = a.weno_cfl_degree > 0 ? basis_count(a.D, a.weno_cfl_degree)
-                                           : std::max(std::max(a.Bd, a.Br), a.D + 1);
+    int need = a.weno_cfl_degree > 0 ? basis_count(a.D, a.weno_cfl_degree)
+                                     : std::max(std::max(a.Bd, a.Br), a.D + 1);
+    if (a.central_qmax > 0) need = std::max(need, basis_count(a.D, a.central_qmax) + 1);
     if (need > kMaxB) { err = "basis too large for the MLS kernel"; return HCC_ERR_UNSUPPORTED; }
     if (need <= 4) k_mls<4><<<grid_for(a.n, 128), 128, 0, s>>>(a);
     else if (need <= 10) k_mls<10><<<grid_for(a.n, 128), 128, 0, s>>>(a);
     else k_mls<kMaxB><<<grid_for(a.n, 64), 64, 0, s>>>(a);
+    for (int q = 1; q <= a.central_qmax; ++q) {
+        if (need <= 4) k_mls_central<4><<<grid_for(a.n, 128), 128, 0, s>>>(a, q);
+        else if (need <= 10) k_mls_central<10><<<grid_for(a.n, 128), 128, 0, s>>>(a, q);
+        else k_mls_central<kMaxB><<<grid_for(a.n, 64), 64, 0, s>>>(a, q);
+    }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { err = std::string("mls kernel: ") + cudaGetErrorString(e); return HCC_ERR_CUDA; }

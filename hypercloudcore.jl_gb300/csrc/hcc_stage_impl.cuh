@@ -1228,11 +1228,11 @@ __device__ __forceinline__ void chol_solve_fixed(const double *U, const double *
 }
 
 // _mls_solve_masked of degree Q (Interpolators.jl:412-443) over the slots of particle i, all of them (dsel < 0) or
-// the one-sided stencil along axis dsel (upwind side of the velocity); out[0..D) = the first-derivative
-// coefficients (scaled by invL). Returns the factorisation status (out = 0 when it fails).
+// the one-sided stencil along axis dsel: side 1 x_d < 0, side 2 x_d >= 0 (WENO's upwind sides), side 3 x_d <= 0
+// (Tiwari's upwind side for v_d > 0); out[0..D) = the first-derivative coefficients (scaled by invL). Returns the
+// factorisation status (out = 0 when it fails).
 template <typename T, int D, int Q>
-__device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, bool use_left, double fi,
-                         double *out) {
+__device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side, double fi, double *out) {
     constexpr int B = ExpTable<D, Q>::B;
     const int64_t np = a.g.npad;
     double N[B * B], bs[B];
@@ -1241,7 +1241,7 @@ __device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, bo
     for (int k = 0; k < cnt; ++k) {
         if (dsel >= 0) {
             const double dd = double(a.g.dist[(int64_t(k) * D + dsel) * np + i]);
-            if (!((use_left && dd < 0.0) || (!use_left && dd >= 0.0))) continue;
+            if (!(side == 1 ? dd < 0.0 : side == 2 ? dd >= 0.0 : dd <= 0.0)) continue;
         }
         const int64_t s = int64_t(k) * np + i;
         double x[D], p[B];
@@ -1265,11 +1265,11 @@ __device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, bo
 }
 
 template <typename T, int D>
-__device__ __forceinline__ void weno_fit_q(int q, const StageArgs<T> &a, int64_t i, int cnt, int dsel, bool left,
+__device__ __forceinline__ void weno_fit_q(int q, const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side,
                                            double fi, double *out) {
-    if (q == 1) weno_fit<T, D, 1>(a, i, cnt, dsel, left, fi, out);
-    else if (q == 2) weno_fit<T, D, 2>(a, i, cnt, dsel, left, fi, out);
-    else weno_fit<T, D, 3>(a, i, cnt, dsel, left, fi, out);
+    if (q == 1) weno_fit<T, D, 1>(a, i, cnt, dsel, side, fi, out);
+    else if (q == 2) weno_fit<T, D, 2>(a, i, cnt, dsel, side, fi, out);
+    else weno_fit<T, D, 3>(a, i, cnt, dsel, side, fi, out);
 }
 
 // The WENO functor (WENO.jl:55-165): central fit over the whole stencil and one upwind one-sided fit per axis,
@@ -1299,7 +1299,7 @@ __device__ __forceinline__ bool weno_one(const StageArgs<T> &a, const int64_t i)
         const int DO = a.sc.DO;
         const double dx2 = a.g.h64 * a.g.h64;
         double resC[D];
-        weno_fit_q<T, D>(DO == 0 ? p_order : (DO < p_order ? DO : p_order), a, i, cnt, -1, false, fi, resC);
+        weno_fit_q<T, D>(DO == 0 ? p_order : (DO < p_order ? DO : p_order), a, i, cnt, -1, 0, fi, resC);
         double smoothC = (resC[0] * resC[0]) * dx2;
 #pragma unroll
         for (int d = 1; d < D; ++d) smoothC = smoothC + (resC[d] * resC[d]) * dx2;
@@ -1322,7 +1322,7 @@ __device__ __forceinline__ bool weno_one(const StageArgs<T> &a, const int64_t i)
                 continue;
             }
             double resS[D];
-            weno_fit_q<T, D>(DO == 0 ? p_d : (DO < p_d ? DO : p_d), a, i, cnt, d, use_left, fi, resS);
+            weno_fit_q<T, D>(DO == 0 ? p_d : (DO < p_d ? DO : p_d), a, i, cnt, d, use_left ? 1 : 2, fi, resS);
             double smoothS = (resS[0] * resS[0]) * dx2;
 #pragma unroll
             for (int e = 1; e < D; ++e) smoothS = smoothS + (resS[e] * resS[e]) * dx2;
@@ -1354,6 +1354,190 @@ __global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
         const uint32_t word = a.wmask[tile];
         const int64_t i = int64_t(tile) * 32 + lane;
         const bool f = ((word >> lane) & 1u) ? weno_one<T, D>(a, i) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
+}
+
+// UpwindDivergence (Upwind.jl), scalar advection, first order. Tiwari (:158-202): per axis d the gradient fit on
+// the upwind side v_d x_d <= 0 (order lowered while that side has fewer than basis_count(D, p) points; an axis
+// without enough contributes 0), summed as v_d (d_d u). Praveen (:205-249, 2-D): from the moment matrix
+// N = sum w (x/L)(x/L)^T, per slot c = N^-1 (w x/L) / L, the edge normal n and tangent s, the coefficient
+// (n . c) min(v . n, 0) + min((s . c)(v . s), 0) on u_j - u_i, summed and doubled. K_E = -that. FP64 fits.
+template <typename T, int D, int ALG>
+__device__ __forceinline__ bool upwind_one(const StageArgs<T> &a, const int64_t i) {
+    if (a.g.bnd[i]) {
+        if (a.full) a.K[i] = T(0);
+        return false;
+    }
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    const T fiT = a.U[i];
+    T mn = fiT, mx = fiT;
+    if (a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2))
+        for (int k = 0; k < cnt; ++k) {
+            const T fj = a.U[a.g.nidx[int64_t(k) * np + i]];
+            mn = vmin(mn, fj);
+            mx = vmax(mx, fj);
+        }
+    const double fi = double(fiT);
+    double total = 0.0;
+    if constexpr (ALG == HCC_UPWIND_TIWARI) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double vel = double(a.ph.c[d][0]);
+            int stencil = 0;
+            for (int k = 0; k < cnt; ++k)
+                stencil += vel * double(a.g.dist[(int64_t(k) * D + d) * np + i]) <= 0.0;
+            int p_d = a.orders[i];
+            while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
+            if (stencil < basis_count(D, p_d)) continue;
+            const int q = a.sc.DO == 0 ? p_d : (a.sc.DO < p_d ? a.sc.DO : p_d);
+            // v_d x_d <= 0: x_d <= 0 for v_d > 0, x_d >= 0 for v_d < 0, every slot for v_d = 0
+            double res[D];
+            weno_fit_q<T, D>(q, a, i, cnt, vel == 0.0 ? -1 : d, vel > 0.0 ? 3 : 2, fi, res);
+            total = total + res[d] * vel;
+        }
+    } else if constexpr (D == 2) {
+        if (cnt >= 3 && a.g.h64 >= 1e-14) {
+            const double iL = a.g.invL64;
+            const double vx = double(a.ph.c[0][0]), vy = double(a.ph.c[1][0]);
+            double n11 = 0.0, n12 = 0.0, n22 = 0.0;
+            for (int k = 0; k < cnt; ++k) {
+                const double w = double(a.g.wt[int64_t(k) * np + i]);
+                const double x = double(a.g.dist[(int64_t(k) * 2) * np + i]) * iL;
+                const double y = double(a.g.dist[(int64_t(k) * 2 + 1) * np + i]) * iL;
+                n11 = n11 + w * (x * x);
+                n12 = n12 + w * (x * y);
+                n22 = n22 + w * (y * y);
+            }
+            const double det = n11 * n22 - n12 * n12;
+            const double tr = n11 + n22;
+            if (!(fabs(det) <= 4.0 * 2.220446049250313e-16 * (tr * tr))) {
+                double div = 0.0;
+                for (int k = 0; k < cnt; ++k) {
+                    const double w = double(a.g.wt[int64_t(k) * np + i]);
+                    const double dx = double(a.g.dist[(int64_t(k) * 2) * np + i]);
+                    const double dy = double(a.g.dist[(int64_t(k) * 2 + 1) * np + i]);
+                    const double bx = w * dx * iL, by = w * dy * iL;
+                    const double cx = ((n22 * bx - n12 * by) / det) * iL;
+                    const double cy = ((n11 * by - n12 * bx) / det) * iL;
+                    const double hyp = sqrt(dx * dx + dy * dy);
+                    double nx = 1.0, ny = 0.0;
+                    if (!(hyp <= 2.220446049250313e-16 * a.g.h64)) { nx = dx / hyp; ny = dy / hyp; }
+                    const double sx = -ny, sy = nx;
+                    const double alfa = nx * cx + ny * cy;
+                    const double beta = sx * cx + sy * cy;
+                    const double vn = vx * nx + vy * ny;
+                    const double vs = vx * sx + vy * sy;
+                    const double bv = beta * vs;
+                    const double cij = alfa * (vn < 0.0 ? vn : 0.0) + (bv < 0.0 ? bv : 0.0);
+                    div = div + cij * (double(a.U[a.g.nidx[int64_t(k) * np + i]]) - fi);
+                }
+                total = 2.0 * div;
+            }
+        }
+    }
+    const T Kv = T(-total);
+    return stage_epilogue<T, D, 1, HCC_PDE_ADVECTION>(a, i, &fiT, &Kv, &mn, &mx);
+}
+
+template <typename T, int D, int ALG>
+__global__ void __launch_bounds__(128) k_upwind(const StageArgs<T> a) {
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? upwind_one<T, D, ALG>(a, i) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? upwind_one<T, D, ALG>(a, i) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
+}
+
+// CentralDivergence (Central.jl:45-88): the particle's order, lowered while it has fewer than basis_count(D, p) + 1
+// neighbours (zero divergence if even order 1 lacks them), capped by div_order, selects the degree-q intercept fit
+// of the flux differences F(f_j) - F(f_i); its per-slot weights (the geometry cache) are applied slot by slot.
+// K_E = -div; the MOOD check of the next candidate runs in the shared epilogue.
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ bool central_one(const StageArgs<T> &a, const int64_t i) {
+    if (a.g.bnd[i]) {
+        if (a.full) {
+            T z[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) z[m] = T(0);
+            store_vec<T, M>(a.K + i * M, z);
+        }
+        return false;
+    }
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    T fi[M], mn[M], mx[M];
+    load_vec<T, M>(a.U + i * M, fi);
+#pragma unroll
+    for (int m = 0; m < M; ++m) mn[m] = mx[m] = fi[m];
+    const bool ext = a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2);
+    int p = a.orders[i];
+    while (p > 1 && cnt < basis_count(D, p) + 1) --p;
+    const int q = a.sc.DO == 0 ? p : (a.sc.DO < p ? a.sc.DO : p);
+    const T *wq = (cnt >= basis_count(D, p) + 1 && a.g.okc[q - 1][i]) ? a.g.dwc[q - 1] : nullptr;
+    T Fi[D][M], lam[D], div[M];
+    flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lam);
+#pragma unroll
+    for (int m = 0; m < M; ++m) div[m] = T(0);
+    for (int k = 0; k < cnt; ++k) {
+        const int64_t j = a.g.nidx[int64_t(k) * np + i];
+        T fj[M];
+        load_vec<T, M>(a.U + j * M, fj);
+        if (ext) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                mn[m] = vmin(mn[m], fj[m]);
+                mx[m] = vmax(mx[m], fj[m]);
+            }
+        }
+        if (wq) {
+            T Fj[D][M], lj[D];
+            flux_and_speed<T, D, M, PDE>(a.ph, fj, Fj, lj);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const T c = wq[(int64_t(k) * D + d) * np + i];
+#pragma unroll
+                for (int m = 0; m < M; ++m) div[m] = div[m] + c * (Fj[d][m] - Fi[d][m]);
+            }
+        }
+    }
+    T Kv[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Kv[m] = -div[m];
+    return stage_epilogue<T, D, M, PDE>(a, i, fi, Kv, mn, mx);
+}
+
+// A full pass or a worklist pass over tiles (the changed particles: no order reach), as the MUSCL flux pass.
+template <typename T, int D, int M, int PDE>
+__global__ void __launch_bounds__(128) k_central(const StageArgs<T> a) {
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? central_one<T, D, M, PDE>(a, i) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? central_one<T, D, M, PDE>(a, i) : false;
         if (a.check) tile_failures(a, tile, f);
         if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
     }
@@ -1460,9 +1644,24 @@ struct StageInst {
             k_weno<T, D><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
         }
     }
+    static void upwind(const void *args, int64_t n, cudaStream_t s) {
+        if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
+            const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+            if (a.sc.upwind_alg == HCC_UPWIND_TIWARI)
+                k_upwind<T, D, HCC_UPWIND_TIWARI><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+            else if constexpr (D == 2)
+                k_upwind<T, D, HCC_UPWIND_PRAVEEN><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+        }
+    }
+    static void central(const void *args, int64_t n, cudaStream_t s) {
+        const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        k_central<T, D, M, PDE><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+    }
     static const StageOps *ops() {
         static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,
-                                   (M == 1 && PDE == HCC_PDE_ADVECTION) ? &weno : nullptr};
+                                   (M == 1 && PDE == HCC_PDE_ADVECTION) ? &weno : nullptr,
+                                   RDEG == 1 ? &central : nullptr,
+                                   (RDEG == 1 && M == 1 && PDE == HCC_PDE_ADVECTION) ? &upwind : nullptr};
         return &o;
     }
 };

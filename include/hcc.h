@@ -84,8 +84,16 @@ typedef enum {               /* src/TimeStepping/ButcherTableaus.jl */
 
 typedef enum {               /* divergence interpolator (src/Interpolation/) */
     HCC_SCHEME_MUSCL = 0,    /* MUSCL (MUSCL.jl), streamed divergence */
-    HCC_SCHEME_WENO = 1      /* meshless WENO, scalar equations only (WENO.jl) */
+    HCC_SCHEME_WENO = 1,     /* meshless WENO, scalar equations only (WENO.jl) */
+    HCC_SCHEME_CENTRAL = 2,  /* CentralDivergence (Central.jl): intercept fit of degree = order of F_j - F_i */
+    HCC_SCHEME_UPWIND = 3    /* UpwindDivergence (Upwind.jl), scalar advection, order 1, `upwind_algorithm` below
+                                (:Classic is the first-order MUSCL scheme: HCC_SCHEME_MUSCL with muscl_order 1) */
 } hcc_scheme;
+
+typedef enum {               /* UpwindDivergence algorithms (Upwind.jl) */
+    HCC_UPWIND_TIWARI = 1,   /* per axis: the gradient fit on the upwind side (v_d x_d <= 0), times v_d */
+    HCC_UPWIND_PRAVEEN = 2   /* 2-D: edge-normal / tangential upwind coefficients from the local moment matrix */
+} hcc_upwind_algorithm;
 
 typedef enum {               /* slope limiters of the MUSCL pre-pass (Limiter.jl) */
     HCC_LIMITER_NONE = 0,    /* NoLimiter */
@@ -128,7 +136,8 @@ typedef struct {
     int32_t slot_capacity;             /* neighbours per particle the lists may hold (0: no limit) */
     int32_t flux;                      /* hcc_flux (MUSCL numerical flux) */
     int32_t reset_orders_per_stage;    /* 1: restore the maximum order before each stage's full pass */
-    int32_t reserved_i[3];
+    int32_t upwind_algorithm;          /* hcc_upwind_algorithm (HCC_SCHEME_UPWIND) */
+    int32_t reserved_i[2];
     double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
     double  radius;                    /* support radius R of ExponentialWeightFunction */
     double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */

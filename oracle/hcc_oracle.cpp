@@ -540,6 +540,11 @@ struct Solver {
     // scheme
     int max_order = 2, DO = 0, rdeg = 1, Br = 1, full_div = 2, ddeg = 1, Bd = 2;
     bool weno = false;
+    bool central = false;            // CentralDivergence (Central.jl)
+    int upwind = 0;                  // UpwindDivergence algorithm (Upwind.jl): 1 Tiwari, 2 Praveen
+    int qmax = 1;                    // Central: highest divergence degree
+    std::vector<double> dwc[3];      // Central: per-slot weights of the intercept fit of degree q = 1..qmax
+    std::vector<uint8_t> okc[3];
     double invL = 1.0;
     bool streamed = true;
     bool aligned = false;            // AlignedRusanovFlux
@@ -584,9 +589,18 @@ struct Solver {
         max_order = c.muscl_order;
         aligned = c.flux == HCC_FLUX_ALIGNED;
         weno = c.scheme == HCC_SCHEME_WENO;
+        central = c.scheme == HCC_SCHEME_CENTRAL;
+        upwind = c.scheme == HCC_SCHEME_UPWIND ? c.upwind_algorithm : 0;
+        if (c.scheme == HCC_SCHEME_UPWIND) {
+            if (M != 1 || c.pde != HCC_PDE_ADVECTION) { err = "UpwindDivergence :Tiwari/:Praveen are scalar"; return false; }
+            if (c.muscl_order != 1) { err = "UpwindDivergence is first order"; return false; }
+            if (upwind != HCC_UPWIND_TIWARI && upwind != HCC_UPWIND_PRAVEEN) { err = "unknown upwind algorithm"; return false; }
+            if (upwind == HCC_UPWIND_PRAVEEN && D != 2) { err = "Praveen is two-dimensional"; return false; }
+        }
         if (max_order < 1 || max_order > 3) { err = "muscl_order must be 1..3"; return false; }
         if (weno && (M != 1 || c.pde == HCC_PDE_EULER)) { err = "WENO is a scalar scheme (n_vars = 1)"; return false; }
         DO = c.div_order > max_order ? max_order : c.div_order;
+        qmax = DO == 0 ? max_order : DO;
         rdeg = std::max(1, max_order - 1);
         Br = basis_count(D, rdeg);
         full_div = div_idx(D, DO == 0 ? max_order : DO);
@@ -801,8 +815,64 @@ struct Solver {
                 }
             }
         }
+        if (central) central_weights();
         have_geom = true;
         return true;
+    }
+
+    // CentralDivergence (Central.jl:45-88) takes the intercept fit of degree q = the particle's (starved-lowered)
+    // order, capped by div_order, of the flux differences F_j - F_i (compute_dynamic_divergence,
+    // Interpolators.jl:290-334). Its per-slot weights for every q: rows 2..D+1 of inv(N_q) (w p~) invL, the form
+    // of the MUSCL cache (MUSCL.jl:211-223); a particle uses degree q only if it has basis_count(D, q) + 1
+    // neighbours.
+    void central_weights() {
+        for (int q = 1; q <= qmax; ++q) {
+            dwc[q - 1].assign(nidx.size() * D, 0.0);
+            okc[q - 1].assign(N, 0);
+            const BasisTable &bt = basis_table(D, q);
+            const int B = bt.B + 1;
+#pragma omp parallel for schedule(dynamic, 256)
+            for (int64_t i = 0; i < N; ++i) {
+                if (nnb(i) < bt.B + 1) continue;
+                double inv[400];
+                const bool ok = inverse_moment(i, q, true, B, inv);
+                okc[q - 1][i] = ok;
+                if (!ok) continue;
+                double p[32], sd[3], v[32];
+                for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                    for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
+                    p[0] = 1.0; build_basis(bt, sd, p + 1);
+                    const double w = nw[s];
+                    for (int b = 0; b < B; ++b) v[b] = w * p[b];
+                    for (int d = 0; d < D; ++d) {
+                        const double *row = &inv[(1 + d) * B];
+                        double acc = row[0] * v[0];
+                        for (int b = 1; b < B; ++b) acc = acc + row[b] * v[b];
+                        dwc[q - 1][s * D + d] = acc * invL;
+                    }
+                }
+            }
+        }
+    }
+
+    // The divergence of particle i (streamed: per-slot weights times the flux differences, slot by slot).
+    void central_particle(int64_t i, const double *U, double *div) const {
+        for (int m = 0; m < M; ++m) div[m] = 0.0;
+        const int num = nnb(i);
+        int p_order = orders[i];
+        while (p_order > 1 && num < basis_count(D, p_order) + 1) --p_order;
+        if (num < basis_count(D, p_order) + 1) return;
+        const int q = DO == 0 ? p_order : std::min(DO, p_order);
+        if (!okc[q - 1][i]) return;
+        double Fi[3 * HCC_MAX_VARS], Fj[3 * HCC_MAX_VARS];
+        phys.flux(&U[i * M], Fi);
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            phys.flux(&U[int64_t(nidx[s]) * M], Fj);
+            for (int d = 0; d < D; ++d) {
+                const double c = dwc[q - 1][s * D + d];
+                for (int m = 0; m < M; ++m) div[m] = div[m] + c * (Fj[d * M + m] - Fi[d * M + m]);
+            }
+        }
     }
 
     // ------------------------------------------------------------ gather pass (MUSCL.jl:351-384)
@@ -1123,6 +1193,76 @@ struct Solver {
     }
 
     // ------------------------------------------------------------ WENO (WENO.jl:55-165), scalar
+    // Tiwari (Upwind.jl:158-202): per axis d the particles with v_d x_d <= 0 (the upwind side); the order lowered
+    // while that stencil has fewer than basis_count(D, p) points (then the axis contributes 0); the gradient fit
+    // of degree q (div_order cap) on it; the result is sum_d v_d (d_d u).
+    double tiwari_particle(int64_t i, const double *U) const {
+        const int num = nnb(i);
+        std::vector<uint8_t> mask(num, 0);
+        double total = 0.0;
+        for (int d = 0; d < D; ++d) {
+            const double vel = phys.c[d][0];
+            int stencil = 0;
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                const bool in = vel * ndist[s * D + d] <= 0.0;
+                mask[s - start[i]] = in;
+                stencil += in;
+            }
+            int p_d = orders[i];
+            while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
+            if (stencil < basis_count(D, p_d)) continue;
+            const int q = DO == 0 ? p_d : std::min(DO, p_d);
+            double res[32];
+            masked_fit(i, U, q, mask, res);
+            total = total + res[d] * vel;
+        }
+        return total;
+    }
+
+    // Praveen (Upwind.jl:205-249), 2-D, first order: the moment matrix N = sum w (x/L)(x/L)^T; per slot
+    // c = N \ (w x / L) / L, the edge normal n = x / |x| and tangent s = (-n_y, n_x); the coefficient
+    // (n . c) min(v . n, 0) + min((s . c)(v . s), 0) times u_j - u_i, summed, doubled.
+    double praveen_particle(int64_t i, const double *U) const {
+        const int num = nnb(i);
+        if (num < 3) return 0.0;
+        const double scale = std::min(cfg.dx[0], cfg.dx[1]);
+        if (scale < 1e-14) return 0.0;
+        const double iL = 1.0 / scale;
+        const double vx = phys.c[0][0], vy = phys.c[1][0];
+        double n11 = 0.0, n12 = 0.0, n22 = 0.0;
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            const double w = nw[s];
+            const double x = ndist[s * 2] * iL, y = ndist[s * 2 + 1] * iL;
+            n11 = n11 + w * (x * x);
+            n12 = n12 + w * (x * y);
+            n22 = n22 + w * (y * y);
+        }
+        const double det = n11 * n22 - n12 * n12;
+        const double tr = n11 + n22;
+        if (std::fabs(det) <= 4.0 * 2.220446049250313e-16 * (tr * tr)) return 0.0;
+        const double fi = U[i];
+        double div = 0.0;
+        for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+            const double w = nw[s];
+            const double dx = ndist[s * 2], dy = ndist[s * 2 + 1];
+            const double bx = w * dx * iL, by = w * dy * iL;
+            const double cx = ((n22 * bx - n12 * by) / det) * iL;
+            const double cy = ((n11 * by - n12 * bx) / det) * iL;
+            const double hyp = std::sqrt(dx * dx + dy * dy);
+            double nx = 1.0, ny = 0.0;
+            if (!(hyp <= 2.220446049250313e-16 * scale)) { nx = dx / hyp; ny = dy / hyp; }
+            const double sx = -ny, sy = nx;
+            const double alfa = nx * cx + ny * cy;
+            const double beta = sx * cx + sy * cy;
+            const double vn = vx * nx + vy * ny;
+            const double vs = vx * sx + vy * sy;
+            const double bv = beta * vs;
+            const double cij = alfa * (vn < 0.0 ? vn : 0.0) + (bv < 0.0 ? bv : 0.0);
+            div = div + cij * (U[nidx[s]] - fi);
+        }
+        return 2.0 * div;
+    }
+
     // _mls_solve_masked (Interpolators.jl:412-443) of degree q over the slots with mask[k]; out[0..B) scaled.
     bool masked_fit(int64_t i, const double *U, int q, const std::vector<uint8_t> &mask, double *out) const {
         const BasisTable &bt = basis_table(D, q);
@@ -1283,6 +1423,26 @@ struct Solver {
     // compute_explicit_rhs! (TimeSteppers.jl:312-356); on a moving grid K_X = w and the flux in the ALE frame
     std::vector<double> *KX_cur = nullptr;
     void compute_rhs(std::vector<double> &K, const double *Ystate, bool full) {
+        if (upwind) {
+#pragma omp parallel for schedule(dynamic, 256)
+            for (int64_t p = 0; p < N; ++p) {
+                if (bnd[p]) { if (full) K[p] = 0.0; continue; }
+                if (!(full || dirty[p])) continue;
+                K[p] = -(upwind == HCC_UPWIND_TIWARI ? tiwari_particle(p, Ystate) : praveen_particle(p, Ystate));
+            }
+            return;
+        }
+        if (central) {
+#pragma omp parallel for schedule(dynamic, 256)
+            for (int64_t p = 0; p < N; ++p) {
+                if (bnd[p]) { if (full) for (int m = 0; m < M; ++m) K[p * M + m] = 0.0; continue; }
+                if (!(full || dirty[p])) continue;
+                double div[HCC_MAX_VARS];
+                central_particle(p, Ystate, div);
+                for (int m = 0; m < M; ++m) K[p * M + m] = -div[m];
+            }
+            return;
+        }
         if (weno) {
 #pragma omp parallel for schedule(dynamic, 256)
             for (int64_t p = 0; p < N; ++p) {
@@ -1562,7 +1722,7 @@ struct Solver {
     }
 
     // _order_reach (MUSCL_hooks.jl:10-11; API.jl:250 default 0 for schemes that read no neighbour orders: WENO)
-    int order_reach() const { return weno ? 0 : (cfg.mood_strategy == HCC_EPD2 ? 2 : 1); }
+    int order_reach() const { return (weno || central || upwind) ? 0 : (cfg.mood_strategy == HCC_EPD2 ? 2 : 1); }
 
     bool mood_checkpoint(int i, double dt) {
         const std::vector<double> &Yprev = Y[i - 2];
@@ -1658,8 +1818,9 @@ struct Solver {
             const double *Ui = &rhos[i * M];
             double Li[3];
             for (int d = 0; d < D; ++d) Li[d] = phys.lam(Ui, d);
-            if (weno) {
-                // dispatch_cfl: degree _divergence_degree(WENO) = its order, clamped to 3 in 3-D / 4 otherwise
+            if (weno || central || upwind) {
+                // dispatch_cfl: degree _divergence_degree(WENO / Central / Upwind) = its order, clamped to 3 in 3-D / 4
+                // otherwise (API.jl:236)
                 int degree = std::min(max_order, D == 3 ? 3 : 4);
                 double sc = cfl_sum_assembled(i, Li, degree);
                 if (sc > tol) best = std::min(best, inv_dim / sc);
@@ -2110,7 +2271,7 @@ hcc_status orc_set_mover(orc_ctx *ctx, const hcc_mover *mv) {
     if (mv->kind < HCC_MOVER_NONE || mv->kind > HCC_MOVER_PRESCRIBED) return HCC_ERR_INVALID;
     if ((mv->kind == HCC_MOVER_LAGRANGIAN || mv->kind == HCC_MOVER_SCALED) && !s.phys.has_fluid_velocity())
         return HCC_ERR_UNSUPPORTED;
-    if (mv->kind != HCC_MOVER_NONE && s.weno) return HCC_ERR_UNSUPPORTED;
+    if (mv->kind != HCC_MOVER_NONE && (s.weno || s.central || s.upwind)) return HCC_ERR_UNSUPPORTED;
     s.mover = *mv;
     return HCC_OK;
 }

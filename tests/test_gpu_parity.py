@@ -611,3 +611,93 @@ def test_snapshot_resume(hcc, cuda_lib, tmp_path, moving, precision):
     assert _bits_equal(a.download_state(), b.download_state())
     assert _bits_equal(a.positions(), b.positions())
     np.testing.assert_array_equal(a.mood_flags(), b.mood_flags())
+
+
+@pytest.mark.parametrize("D,order,graphs", [(1, 2, True), (2, 1, True), (2, 2, False), (2, 3, True), (3, 2, True)])
+def test_central_divergence_steps_bit_exact(hcc, oracle, cuda_lib, D, order, graphs):
+    """CentralDivergence (Central.jl:45-88) on scalar advection with MOOD u1: RHS, CFL (assembled fit of degree =
+    order), states, orders and flags; 1-D Central2 RK2 is the reference's backend-parity case
+    (unit_backends.jl:38)."""
+    h = {1: 0.02, 2: 0.04, 3: 0.1}[D]
+    cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=17)
+    vel = tuple(((1.0, 0.5, -0.3)[d],) for d in range(D))
+    cfg = hcc.make_config(hcc.LinearAdvection(vel), cloud, scheme=hcc.CentralDivergence(order),
+                          mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D)),
+                          tableau="RK2_SSP" if D == 1 else "RK3_SSP")
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    g.set_step_graphs(graphs)
+    r2 = ((cloud.pos - 0.5) ** 2).sum(axis=1)
+    U0 = np.where(r2 < 0.04, 1.0, 0.0)[:, None] + 0.1 * np.exp(-r2 / 0.02)[:, None]
+    g.upload_state(U0)
+    o.upload_state(U0)
+    assert _bits_equal(g.compute_rhs(), o.compute_rhs())
+    assert g.time_step() == o.time_step()
+    dt = 0.3 * o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+        assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+        np.testing.assert_array_equal(g.orders(), o.orders())
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+    assert o.mood_flags().sum() > 0
+
+
+def test_central_divergence_euler_bit_exact_and_fp32(hcc, oracle, cuda_lib):
+    """Central2 on the 2-D Euler quadrant problem with MOOD u1 and outflow walls: FP64 bit for bit, FP32 within
+    1e-5 relative L1 of the FP64 oracle after 3 steps."""
+    h = 1 / 48
+    cloud = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    U0 = quadrant_ic(cloud)
+    outs = {}
+    for prec in ("fp64", "fp32"):
+        cfg = hcc.make_config(hcc.Euler(2, 1.4), cloud, scheme=hcc.CentralDivergence(2),
+                              mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), bc_map=OUTFLOW, precision=prec)
+        g, o = _pair(hcc, oracle, cfg, cloud)
+        g.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
+        o.upload_state(U0)
+        dt = 0.3 * o.time_step()
+        for k in range(3):
+            g.step(k * dt, dt)
+            o.step(k * dt, dt)
+        outs[prec] = (g.download_state(), o.download_state(), g.mood_flags(), o.mood_flags())
+    Ug, Uo, fg, fo = outs["fp64"]
+    assert _bits_equal(Ug, Uo)
+    np.testing.assert_array_equal(fg, fo)
+    assert fo.sum() > 0
+    U32, Uo, _, _ = outs["fp32"]
+    inner = cloud.is_boundary == 0
+    l1 = np.abs(U32[inner] - Uo[inner]).sum(axis=0) / np.abs(Uo[inner]).sum(axis=0)
+    assert np.all(l1 < 1e-5), l1
+
+
+@pytest.mark.parametrize("alg,D,graphs", [("Tiwari", 1, True), ("Tiwari", 2, True), ("Tiwari", 3, False),
+                                          ("Praveen", 2, True), ("Praveen", 2, False)])
+def test_upwind_algorithms_bit_exact(hcc, oracle, cuda_lib, alg, D, graphs):
+    """UpwindDivergence :Tiwari / :Praveen (Upwind.jl:158-249) on scalar advection with MOOD u1 (first order: the
+    judge can only unflag): RHS, CFL (assembled degree-1 fit), states and flags bit for bit; FP32 within 1e-5."""
+    h = {1: 0.02, 2: 0.04, 3: 0.1}[D]
+    cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=17)
+    vel = tuple(((1.0, -0.5, 0.3)[d],) for d in range(D))
+    r2 = ((cloud.pos - 0.5) ** 2).sum(axis=1)
+    U0 = np.where(r2 < 0.04, 1.0, 0.0)[:, None] + 0.1 * np.exp(-r2 / 0.02)[:, None]
+    res = {}
+    for prec in ("fp64", "fp32"):
+        cfg = hcc.make_config(hcc.LinearAdvection(vel), cloud, scheme=hcc.Upwind(algorithm=alg),
+                              mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D)), precision=prec)
+        g, o = _pair(hcc, oracle, cfg, cloud)
+        g.set_step_graphs(graphs)
+        g.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
+        o.upload_state(U0)
+        if prec == "fp64":
+            assert _bits_equal(g.compute_rhs(), o.compute_rhs())
+            assert g.time_step() == o.time_step()
+        dt = 0.3 * o.time_step()
+        for k in range(3):
+            g.step(k * dt, dt)
+            o.step(k * dt, dt)
+            if prec == "fp64":
+                assert _bits_equal(g.download_state(), o.download_state()), f"step {k}"
+                np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+        res[prec] = (g.download_state(), o.download_state())
+    U32, Uo = res["fp32"]
+    assert np.abs(U32 - Uo).sum() / np.abs(Uo).sum() < 1e-5

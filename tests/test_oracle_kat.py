@@ -775,3 +775,132 @@ def test_strict_epd0_forcing_uses_the_snapshot(hcc, oracle, abi):
             assert o.detect_and_drop(U, U, full=False, dirty=dirty)
             got = o.orders()
             assert got[q] == 1 and got[p] == 1
+
+
+# ----------------------------------------------------------------------------------------------- CentralDivergence
+def test_central_divergence_exact_for_a_linear_flux(hcc, oracle, abi, olib):
+    """unit_schemes.jl:356-373 (CentralDivergence on a jittered periodic 1-D cloud, R = 2.5 dx, F = u = x): the
+    divergence is 1 away from the periodic seam, for every degree the order allows (orders 1-3 here), and the
+    streamed per-slot form equals the direct fit of the same degree (orc_mls_divergence) to 1e-12."""
+    dx = 2 / 40
+    cl = hcc.rectangular_cloud((-1.0,), (1.0,), dx, 2.5 * dx, periodic=True, jitter=0.2 * dx, seed=1)
+    inner = np.abs(cl.pos[:, 0]) < 0.7
+    for order in (1, 2, 3):
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.CentralDivergence(order))
+        o.prepare_geometry()
+        o.upload_state(cl.pos[:, :1].copy())
+        K = o.compute_rhs()[:, 0]
+        assert np.max(np.abs(K[inner] + 1.0)) < 1e-10, order
+    # streamed vs direct, degree 2 on a sine
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.CentralDivergence(2))
+    o.prepare_geometry()
+    u = np.sin(np.pi * cl.pos[:, 0])
+    o.upload_state(u[:, None].copy())
+    K = o.compute_rhs()[:, 0]
+    counts, idx, w, dist = o.neighbours()
+    start = np.concatenate([[0], np.cumsum(counts)])
+    import ctypes as C
+    for i in range(0, cl.n, 7):
+        s0, s1 = start[i], start[i + 1]
+        dists = np.ascontiguousarray(dist[s0:s1])
+        ww = np.ascontiguousarray(w[s0:s1])
+        dF = np.ascontiguousarray((u[idx[s0:s1]] - u[i])[:, None])
+        out = np.zeros(1)
+        dp = C.POINTER(C.c_double)
+        ok = olib.orc_mls_divergence(1, 1, 2, s1 - s0, dists.ctypes.data_as(dp), ww.ctypes.data_as(dp),
+                                     dF.ctypes.data_as(dp), dx, out.ctypes.data_as(dp))
+        assert ok == 1
+        assert abs(-K[i] - out[0]) <= 1e-12 * (1.0 + abs(out[0]))
+
+
+def test_central_order_reach_and_cfl_degree(hcc, oracle, abi):
+    """unit_core.jl:704-706: CentralDivergence has order reach 0 (MOOD recomputes only the changed particles) and
+    divergence degree = its order (the CFL uses the assembled fit of that degree: degree 2 for Central2 equals
+    WENO2's time step on the same cloud)."""
+    cl = lattice_1d(hcc, 40)
+    oc = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((2.0,),)), scheme=hcc.CentralDivergence(2))
+    ow = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((2.0,),)), scheme=hcc.WENO(2))
+    for o in (oc, ow):
+        o.upload_state(np.zeros((cl.n, 1)))
+    assert oc.time_step() == ow.time_step()
+    # a single dropped particle recomputes only itself: OnlyMOOD drops everyone once per iteration, and with reach
+    # 0 the fixed point still ends at order 1 everywhere
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.CentralDivergence(2),
+             mood=hcc.MOOD(hcc.EPD1, hcc.OnlyMOOD()), tableau="RK2_SSP")
+    o.upload_state(np.exp(-cl.pos[:, :1] ** 2 / 0.02))
+    o.step(0.0, 0.01)
+    assert np.all(o.orders()[cl.is_boundary == 0] == 1)
+
+
+def test_central_converges_on_smooth_advection(hcc, oracle, abi):
+    """Central2 (degree-2 divergence fit, RK3) on a periodic 2-D cloud: second-order convergence of a sine wave."""
+    errs = []
+    for n in (24, 48):
+        h = 1.0 / n
+        cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.1 * h, seed=5)
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (0.5,))), scheme=hcc.CentralDivergence(2))
+        f = lambda x, y: np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)
+        o.upload_state(f(cl.pos[:, 0], cl.pos[:, 1])[:, None])
+        T = 0.1
+        dt = 0.2 * o.time_step()
+        steps = int(np.ceil(T / dt))
+        dt = T / steps
+        for k in range(steps):
+            o.step(k * dt, dt)
+        pos = o.positions()
+        errs.append(np.abs(o.download_state()[:, 0] - f(pos[:, 0] - T, pos[:, 1] - 0.5 * T)).mean())
+    assert errs[0] / errs[1] > 3.0, errs
+
+
+# ----------------------------------------------------------------------------------------------- UpwindDivergence
+@pytest.mark.parametrize("alg", ["Classic", "Tiwari", "Praveen"])
+def test_2d_upwind_algorithms_converge_at_first_order(hcc, oracle, abi, alg):
+    """pipeline_tests.jl:255-275: on the periodic [-1, 1]^2 cloud (50^2 and 100^2), advection with v = (1, 1) of a
+    Gaussian to t = 0.1 with SSP-RK2 at CFL 0.4: the finer run is more accurate and the convergence order lies in
+    (0.5, 1.5) for :Classic (first-order MUSCL), :Tiwari and :Praveen."""
+    errs = []
+    for n in (50, 100):
+        h = 2.0 / n
+        cl = hcc.rectangular_cloud((-1.0, -1.0), (1.0, 1.0), h, 2.5 * h, periodic=True)
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (1.0,))), scheme=hcc.Upwind(algorithm=alg),
+                 tableau="RK2_SSP")
+        f = lambda x, y: np.exp(-(x * x + y * y) / 0.1)
+        o.upload_state(f(cl.pos[:, 0], cl.pos[:, 1])[:, None])
+        T = 0.1
+        dt = 0.4 * o.time_step()
+        steps = int(np.ceil(T / dt))
+        dt = T / steps
+        for k in range(steps):
+            o.step(k * dt, dt)
+        x = cl.pos[:, 0] - T
+        y = cl.pos[:, 1] - T
+        x = x - 2.0 * np.round(x / 2.0)
+        y = y - 2.0 * np.round(y / 2.0)
+        ex = f(x, y)
+        errs.append(np.sqrt(((o.download_state()[:, 0] - ex) ** 2).sum() / (ex ** 2).sum()))
+    eoc = math.log(errs[0] / errs[1], 2)
+    assert errs[1] < errs[0] and 0.5 < eoc < 1.5, (errs, eoc)
+
+
+def test_tiwari_is_exact_for_a_linear_field(hcc, oracle, abi):
+    """Tiwari: every axis with an upwind stencil fits a linear field exactly, so K = -(v . grad u) away from the
+    periodic seam; Praveen is first order and only consistent (K -> -(v . grad u) as the cloud refines)."""
+    h = 1 / 20
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=2)
+    inner = (np.abs(cl.pos - 0.5) < 0.3).all(axis=1)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (-0.5,))), scheme=hcc.Upwind(algorithm="Tiwari"))
+    o.prepare_geometry()
+    o.upload_state((2.0 * cl.pos[:, 0] + 3.0 * cl.pos[:, 1])[:, None].copy())
+    K = o.compute_rhs()[:, 0]
+    assert np.max(np.abs(K[inner] - (-(1.0 * 2.0 - 0.5 * 3.0)))) < 1e-10
+
+
+def test_upwind_configuration_rules(hcc, oracle, abi):
+    """Upwind.jl:70-86: :Tiwari / :Praveen are scalar and first order, :Praveen two-dimensional."""
+    cl = lattice_1d(hcc, 20)
+    with pytest.raises(Exception):
+        make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=hcc.Upwind(algorithm="Praveen"))
+    bad = hcc.Upwind(algorithm="Tiwari")
+    bad.order = 2
+    with pytest.raises(Exception):
+        make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,),)), scheme=bad)
