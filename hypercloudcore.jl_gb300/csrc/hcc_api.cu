@@ -595,7 +595,8 @@ int enqueue_drop(hcc_ctx *c, void *Y, cudaStream_t st, const cudaGraphConditiona
 // One MOOD recompute (mood_checkpoint!, TimeSteppers.jl:471-475) over worklists: reconstruction of the changed
 // particles, which also pushes their reach (one hop; a second for EPD2; expand_mask!, MOOD.jl:343-351; none for
 // WENO, which reads no neighbour orders), then the flux and candidate of the reach. Its boundary conditions come
-// with the decrement launch that follows. Returns the kernels launched.
+// with the decrement launch that follows. Schemes without a reconstruction (WENO, CentralDivergence,
+// UpwindDivergence) read no neighbour orders: no gather and no reach. Returns the kernels launched.
 template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, cudaStream_t st, bool prof) {
     const int64_t n = c->n;
     const int hops = c->no_recon() ? 0 : (c->cfg.mood_strategy == HCC_EPD2) ? 2 : 1;
@@ -605,7 +606,7 @@ template <typename T> int enqueue_recompute(hcc_ctx *c, const StageArgs<T> &a, c
                      c->fmask, c->ftiles, c->list_blocks, st);
         k += 2;
     }
-    if (!c->weno) {
+    if (!c->no_recon()) {
         StageArgs<T> ga = a;
         ga.full = 0;
         ga.wtiles = c->ctiles;
@@ -1539,8 +1540,11 @@ hcc_status hcc_download_geometry(hcc_ctx *c, double *dweights, uint8_t *ok_recon
     if (!c->have_geom) return c->fail(HCC_ERR_STATE, "geometry not prepared");
     hcc_status st;
     const int64_t n = c->n;
+    // CentralDivergence: the weights and flags of its full-degree fit (no MUSCL caches)
+    const uint8_t *okd = c->central ? c->okc[c->qmax - 1] : c->ok_d;
+    const double *dwsrc = c->central ? c->dwc64[c->qmax - 1] : c->dw64;
     if (ok_recon) HCC_TRY(c->cuda(cudaMemcpy(ok_recon, c->ok_r, n, cudaMemcpyDeviceToHost), "ok_r"));
-    if (ok_div) HCC_TRY(c->cuda(cudaMemcpy(ok_div, c->ok_d, n, cudaMemcpyDeviceToHost), "ok_d"));
+    if (ok_div) HCC_TRY(c->cuda(cudaMemcpy(ok_div, okd, n, cudaMemcpyDeviceToHost), "ok_d"));
     if (!dweights) return HCC_OK;
     std::vector<int32_t> cnt(n);
     HCC_TRY(c->cuda(cudaMemcpy(cnt.data(), c->cnt, n * 4, cudaMemcpyDeviceToHost), "counts"));
@@ -1552,7 +1556,7 @@ hcc_status hcc_download_geometry(hcc_ctx *c, double *dweights, uint8_t *ok_recon
     HCC_TRY(c->alloc(d_rs, n, "row starts"));
     HCC_TRY(c->valloc(tmp, size_t(std::max<int64_t>(tot, 1)) * 8 * c->D, "row buffer"));
     cudaMemcpy(d_rs, rs.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice);
-    launch_gather_rows(c->dw64, tmp, c->cnt, d_rs, n, c->npad, c->D, 8, c->stream);
+    launch_gather_rows(dwsrc, tmp, c->cnt, d_rs, n, c->npad, c->D, 8, c->stream);
     st = c->sync("row gather");
     if (st == HCC_OK) st = c->cuda(cudaMemcpy(dweights, tmp, size_t(tot) * c->D * 8, cudaMemcpyDeviceToHost), "dweights");
     cudaFree(d_rs);

@@ -266,8 +266,8 @@ __global__ void k_mls(MlsArgs a) {
 }
 
 // CentralDivergence weight set of degree q (Central.jl:45-88 with compute_dynamic_divergence,
-// Interpolators.jl:290-334, in the per-slot form of the MUSCL cache): rows 2..D+1 of inv(N) (w p~) invL for the
-// particles with basis_count(D, q) + 1 neighbours (the others never use degree q).
+// Interpolators.jl:290-334, per slot as _slot_weight(::DynamicWeights), MUSCL.jl:442-445): C \ (w p~), rows 2..D+1,
+// times invL, for the particles with basis_count(D, q) + 1 neighbours (the others never use degree q).
 template <int BM>
 __global__ void k_mls_central(MlsArgs a, int q) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -275,9 +275,12 @@ __global__ void k_mls_central(MlsArgs a, int q) {
     const int cnt = a.cnt[i];
     const int B = c_tabs[a.D][q].B + 1;
     double *dwq = a.dwc[q - 1];
+    double N[BM * BM], U[BM * BM];
     bool ok = false;
-    double inv[BM * BM];
-    if (cnt >= B) ok = inverse_moment<BM>(a, i, cnt, q, true, B, inv);
+    if (cnt >= B) {
+        assemble<BM>(a, i, cnt, q, true, B, N);
+        ok = cholesky_moment(B, N, U);
+    }
     a.okc[q - 1][i] = ok;
     double x[3], p[BM], v[BM];
     for (int k = 0; k < cnt; ++k) {
@@ -289,13 +292,9 @@ __global__ void k_mls_central(MlsArgs a, int q) {
         for (int d = 0; d < a.D; ++d) x[d] = a.dist[(int64_t(k) * a.D + d) * a.npad + i] * a.invL;
         gen_basis(a.D, q, true, x, p);
         const double w = a.w[s];
-        for (int b = 0; b < B; ++b) v[b] = w * p[b];
-        for (int d = 0; d < a.D; ++d) {
-            const double *row = inv + (1 + d) * B;
-            double acc = row[0] * v[0];
-            for (int b = 1; b < B; ++b) acc = acc + row[b] * v[b];
-            dwq[(int64_t(k) * a.D + d) * a.npad + i] = acc * a.invL;
-        }
+        for (int b = 0; b < B; ++b) p[b] = w * p[b];
+        chol_solve<BM>(B, U, p, v);
+        for (int d = 0; d < a.D; ++d) dwq[(int64_t(k) * a.D + d) * a.npad + i] = v[d + 1] * a.invL;
     }
 }
 

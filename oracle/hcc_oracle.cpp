@@ -822,9 +822,9 @@ struct Solver {
 
     // CentralDivergence (Central.jl:45-88) takes the intercept fit of degree q = the particle's (starved-lowered)
     // order, capped by div_order, of the flux differences F_j - F_i (compute_dynamic_divergence,
-    // Interpolators.jl:290-334). Its per-slot weights for every q: rows 2..D+1 of inv(N_q) (w p~) invL, the form
-    // of the MUSCL cache (MUSCL.jl:211-223); a particle uses degree q only if it has basis_count(D, q) + 1
-    // neighbours.
+    // Interpolators.jl:290-334). Its per-slot weights for every q, as _slot_weight(::DynamicWeights)
+    // (MUSCL.jl:442-445): C \ (w p~), rows 2..D+1, times invL; a particle uses degree q only if it has
+    // basis_count(D, q) + 1 neighbours.
     void central_weights() {
         for (int q = 1; q <= qmax; ++q) {
             dwc[q - 1].assign(nidx.size() * D, 0.0);
@@ -833,23 +833,26 @@ struct Solver {
             const int B = bt.B + 1;
 #pragma omp parallel for schedule(dynamic, 256)
             for (int64_t i = 0; i < N; ++i) {
-                if (nnb(i) < bt.B + 1) continue;
-                double inv[400];
-                const bool ok = inverse_moment(i, q, true, B, inv);
-                okc[q - 1][i] = ok;
-                if (!ok) continue;
-                double p[32], sd[3], v[32];
+                if (nnb(i) < B) continue;
+                double Nm[400], Uc[400], p[32], sd[3], c[32];
+                for (int k = 0; k < B * B; ++k) Nm[k] = 0.0;
                 for (int64_t s = start[i]; s < start[i + 1]; ++s) {
                     for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
                     p[0] = 1.0; build_basis(bt, sd, p + 1);
                     const double w = nw[s];
-                    for (int b = 0; b < B; ++b) v[b] = w * p[b];
-                    for (int d = 0; d < D; ++d) {
-                        const double *row = &inv[(1 + d) * B];
-                        double acc = row[0] * v[0];
-                        for (int b = 1; b < B; ++b) acc = acc + row[b] * v[b];
-                        dwc[q - 1][s * D + d] = acc * invL;
-                    }
+                    for (int r = 0; r < B; ++r)
+                        for (int cc = 0; cc < B; ++cc) Nm[r * B + cc] = Nm[r * B + cc] + w * (p[r] * p[cc]);
+                }
+                const bool ok = cholesky_moment(B, Nm, Uc);
+                okc[q - 1][i] = ok;
+                if (!ok) continue;
+                for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                    for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
+                    p[0] = 1.0; build_basis(bt, sd, p + 1);
+                    const double w = nw[s];
+                    for (int b = 0; b < B; ++b) p[b] = w * p[b];
+                    chol_solve(B, Uc, p, c);
+                    for (int d = 0; d < D; ++d) dwc[q - 1][s * D + d] = c[d + 1] * invL;
                 }
             }
         }
@@ -2032,9 +2035,12 @@ hcc_status orc_prepare_geometry(orc_ctx *ctx) {
 hcc_status orc_download_geometry(orc_ctx *ctx, double *dweights, uint8_t *ok_recon, uint8_t *ok_div) {
     if (!ctx || !ctx->s.have_geom) return HCC_ERR_STATE;
     Solver &s = ctx->s;
-    if (dweights) std::memcpy(dweights, s.dw.data(), s.dw.size() * sizeof(double));
+    // CentralDivergence: the weights and flags of its full-degree fit
+    const std::vector<double> &w = s.central ? s.dwc[s.qmax - 1] : s.dw;
+    const std::vector<uint8_t> &okd = s.central ? s.okc[s.qmax - 1] : s.ok_d;
+    if (dweights) std::memcpy(dweights, w.data(), w.size() * sizeof(double));
     if (ok_recon) std::memcpy(ok_recon, s.ok_r.data(), s.N);
-    if (ok_div) std::memcpy(ok_div, s.ok_d.data(), s.N);
+    if (ok_div) std::memcpy(ok_div, okd.data(), s.N);
     return HCC_OK;
 }
 hcc_status orc_upload_state(orc_ctx *ctx, const double *U) {
