@@ -112,11 +112,13 @@ class KineticRelaxation:
 class MUSCL:
     """MUSCL(T, D, M, order, limiter, flux; div_order) (src/Interpolation/MUSCL.jl:116). `limiter` is one
     of "none", "bj_soft", "bj_hard", "vk_soft", "vk_hard" (BarthJespersen / Venkatakrishnan, :soft / :hard);
-    `flux` is "rusanov" (RusanovFlux) or "aligned" (AlignedRusanovFlux, FluxFunctions.jl:103-111)."""
+    `flux` is "rusanov" (RusanovFlux) or "aligned" (AlignedRusanovFlux, FluxFunctions.jl:103-111);
+    `moment_correction` adds the first-moment-free dissipation of a first-order scheme (MUSCL.jl:57, :224-283)."""
     order: int = 2
     div_order: int = 0
     limiter: str = "none"
     flux: str = "rusanov"
+    moment_correction: bool = False
 
 
 @dataclass
@@ -244,6 +246,7 @@ def make_config(pde, cloud: Cloud, *, scheme: MUSCL = None, mood: MOOD = None, t
         cfg.scheme = _abi.SCHEME_MUSCL
         cfg.limiter = _abi.LIMITERS[scheme.limiter]
         cfg.flux = _abi.FLUXES[scheme.flux]
+        cfg.moment_correction = int(bool(scheme.moment_correction))
     cfg.tableau = TABLEAUS[tableau] if isinstance(tableau, str) else int(tableau)
     cfg.mood_substeps = 1 if mood_substeps else 0
     cfg.max_mood_iterations = max_mood_iterations

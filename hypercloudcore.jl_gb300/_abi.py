@@ -44,7 +44,8 @@ class HccConfig(C.Structure):
         ("mood_substeps", C.c_int32), ("periodic", C.c_int32 * HCC_MAX_DIM),
         ("bc_by_tag", C.c_int32 * HCC_MAX_TAGS), ("max_mood_iterations", C.c_int32),
         ("scheme", C.c_int32), ("limiter", C.c_int32), ("slot_capacity", C.c_int32), ("flux", C.c_int32),
-        ("reset_orders_per_stage", C.c_int32), ("upwind_algorithm", C.c_int32), ("reserved_i", C.c_int32 * 2),
+        ("reset_orders_per_stage", C.c_int32), ("upwind_algorithm", C.c_int32), ("moment_correction", C.c_int32),
+        ("reserved_i", C.c_int32 * 1),
         ("dx", C.c_double * HCC_MAX_DIM), ("radius", C.c_double), ("weight_alpha", C.c_double),
         ("canvas_min", C.c_double * HCC_MAX_DIM), ("canvas_max", C.c_double * HCC_MAX_DIM),
         ("domain_min", C.c_double * HCC_MAX_DIM), ("domain_max", C.c_double * HCC_MAX_DIM),

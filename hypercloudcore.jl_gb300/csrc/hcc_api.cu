@@ -177,6 +177,8 @@ struct hcc_ctx {
     int upwind = 0;                   // UpwindDivergence :Tiwari / :Praveen (scalar, first order)
     int qmax = 1;
     double *dwc64[3] = {}; float *dwc32[3] = {}; uint8_t *okc[3] = {};
+    double *mw64 = nullptr; float *mw32 = nullptr;   // moment-correction weights (first-order MUSCL)
+    bool moment() const { return cfg.moment_correction && max_order == 1 && !weno && !central && !upwind; }
     bool no_recon() const { return weno || central || upwind; }
 
     Tableau tab;
@@ -335,6 +337,7 @@ struct hcc_ctx {
         dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
         dfree(dw1_32); dfree(gw32);
         for (int q = 0; q < 3; ++q) { dfree(dwc64[q]); dfree(dwc32[q]); dfree(okc[q]); }
+        dfree(mw64); dfree(mw32);
     }
     void free_bins() { dfree(binnb); dfree(cell_count); dfree(cell_cursor); dfree(cell_start); }
 };
@@ -387,6 +390,8 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
         g.gw = c->gw32;
     }
     g.ok_r = c->ok_r; g.ok_d = c->ok_d; g.ok_1 = c->ok_1;
+    if constexpr (sizeof(T) == 8) g.mw = c->moment() ? c->mw64 : nullptr;
+    else g.mw = c->moment() ? c->mw32 : nullptr;
     for (int q = 0; q < 3; ++q) {
         if constexpr (sizeof(T) == 8) g.dwc[q] = c->dwc64[q];
         else g.dwc[q] = c->dwc32[q];
@@ -1482,6 +1487,12 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
             m.okc[q] = c->okc[q];
         }
     }
+    if (c->moment()) {
+        HCC_TRY(c->alloc(c->mw64, slots * D, "moment weights"));
+        cudaMemsetAsync(c->mw64, 0, slots * D * sizeof(double), c->stream);
+        m.mw = c->mw64;
+        m.aligned = c->cfg.flux == HCC_FLUX_ALIGNED;
+    }
     if ((st = mls_prepare(m, c->stream, c->err)) != HCC_OK) return st;
     if (c->f32) {
         HCC_TRY(c->alloc(c->dist32, slots * D, "distances f32"));
@@ -1499,6 +1510,10 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
         if (c->need_dw1) {
             HCC_TRY(c->alloc(c->dw1_32, slots * D, "degree-1 weights f32"));
             launch_cast_f64_to_f32(c->dw1_64, c->dw1_32, int64_t(slots) * D, c->stream);
+        }
+        if (c->moment()) {
+            HCC_TRY(c->alloc(c->mw32, slots * D, "moment weights f32"));
+            launch_cast_f64_to_f32(c->mw64, c->mw32, int64_t(slots) * D, c->stream);
         }
         for (int q = 0; q < (c->central ? c->qmax : 0); ++q) {
             HCC_TRY(c->alloc(c->dwc32[q], slots * D, "central weights f32"));

@@ -178,6 +178,7 @@ template <typename T> struct Geometry {
     const T *gw;                      // FP32, degree-1 reconstruction: gradient weights of the cached fit,
                                       // [(k*D + b) * npad + i] = invL Σ_c inv_r[b][c] w_k x_k[c] (else nullptr)
     const uint8_t *bnd;
+    const T *mw;                      // moment-correction weights e^d_ij [(k*D + d) * npad + i] (or nullptr)
     const T *dwc[3];                  // CentralDivergence: weights of the intercept fit of degree q = 1..3
     const uint8_t *okc[3];
     T invL;
@@ -357,6 +358,8 @@ struct MlsArgs {
     int central_qmax;                 // > 0: CentralDivergence weight sets of degree 1..central_qmax
     double *dwc[3];
     uint8_t *okc[3];
+    double *mw;                       // != nullptr: moment-correction weights of a first-order scheme (from dw)
+    int aligned;                      // AlignedRusanovFlux (the dissipation direction of the moment weights)
 };
 hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err);
 

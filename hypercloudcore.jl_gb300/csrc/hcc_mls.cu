@@ -298,6 +298,135 @@ __global__ void k_mls_central(MlsArgs a, int q) {
     }
 }
 
+// _moment_mu (MUSCL.jl:285-330) for particle i: mu with sum_k (x_k . mu)_+ x_k = b over the scaled offsets, by Newton
+// steps on the active slots with Armijo backtracking; zero when b is zero, a Hessian fails the pivot test or 30
+// steps do not converge. The operation order is the oracle's.
+__device__ void moment_hessian(const MlsArgs &a, int64_t i, int cnt, const double *m, const double *b, double *H,
+                               double *g, double *phi, bool all) {
+    const int D = a.D;
+    for (int q = 0; q < D * D; ++q) H[q] = 0.0;
+    if (g) for (int d = 0; d < D; ++d) g[d] = -b[d];
+    if (phi) {
+        double t = b[0] * m[0];
+        for (int d = 1; d < D; ++d) t = t + b[d] * m[d];
+        *phi = -t;
+    }
+    for (int k = 0; k < cnt; ++k) {
+        double x[3];
+        for (int d = 0; d < D; ++d) x[d] = a.dist[(int64_t(k) * D + d) * a.npad + i] * a.invL;
+        double t = 0.0;
+        if (!all) {
+            t = x[0] * m[0];
+            for (int d = 1; d < D; ++d) t = t + x[d] * m[d];
+            if (!(t > 0.0)) continue;
+        }
+        for (int r = 0; r < D; ++r)
+            for (int c = 0; c < D; ++c) H[r * D + c] = H[r * D + c] + x[r] * x[c];
+        if (g) for (int d = 0; d < D; ++d) g[d] = g[d] + t * x[d];
+        if (phi) *phi = *phi + (t * t) / 2.0;
+    }
+}
+__device__ bool moment_pivots_ok(int D, const double *H, double *U) {
+    if (!cholesky_upper(D, H, U)) return false;
+    for (int k = 0; k < D; ++k) {
+        const double u = U[k * D + k];
+        if (!(u * u > 10.0 * 2.220446049250313e-16 * H[k * D + k])) return false;
+    }
+    return true;
+}
+__device__ void moment_mu(const MlsArgs &a, int64_t i, int cnt, const double *b, double *mu) {
+    const int D = a.D;
+    for (int d = 0; d < D; ++d) mu[d] = 0.0;
+    double nb2 = b[0] * b[0];
+    for (int d = 1; d < D; ++d) nb2 = nb2 + b[d] * b[d];
+    if (!(nb2 > 0.0)) return;
+    double H[9], U[9], m[3], g[3], Dl[3], zero[3] = {0.0, 0.0, 0.0};
+    moment_hessian(a, i, cnt, zero, b, H, nullptr, nullptr, true);
+    if (!moment_pivots_ok(D, H, U)) return;
+    chol_solve<3>(D, U, b, m);
+    for (int d = 0; d < D; ++d) m[d] = 2.0 * m[d];
+    const double tol = 1.4901161193847656e-08;    // sqrt(eps)
+    for (int it = 0; it < 30; ++it) {
+        double phi;
+        moment_hessian(a, i, cnt, m, b, H, g, &phi, false);
+        double gg = g[0] * g[0];
+        for (int d = 1; d < D; ++d) gg = gg + g[d] * g[d];
+        if (gg <= (tol * tol) * nb2) {
+            for (int d = 0; d < D; ++d) mu[d] = m[d];
+            return;
+        }
+        if (!moment_pivots_ok(D, H, U)) return;
+        chol_solve<3>(D, U, g, Dl);
+        double gD = g[0] * Dl[0];
+        for (int d = 1; d < D; ++d) gD = gD + g[d] * Dl[d];
+        double lam = 1.0;
+        for (int ls = 0; ls < 40; ++ls) {
+            double mn[3];
+            for (int d = 0; d < D; ++d) mn[d] = m[d] - lam * Dl[d];
+            double t0 = b[0] * mn[0];
+            for (int d = 1; d < D; ++d) t0 = t0 + b[d] * mn[d];
+            double phin = -t0;
+            for (int k = 0; k < cnt; ++k) {
+                double t = (a.dist[(int64_t(k) * D) * a.npad + i] * a.invL) * mn[0];
+                for (int d = 1; d < D; ++d) t = t + (a.dist[(int64_t(k) * D + d) * a.npad + i] * a.invL) * mn[d];
+                if (t > 0.0) phin = phin + (t * t) / 2.0;
+            }
+            if (phin <= phi - (lam * gD) / 4.0) break;
+            lam = lam / 2.0;
+        }
+        for (int d = 0; d < D; ++d) m[d] = m[d] - lam * Dl[d];
+    }
+}
+
+// update_moment_weights! (MUSCL.jl:224-283): per axis d the first moment b = sum_k g^d_k x_k of the dissipation
+// coefficients g^d_k = (dir_d > 0 ? c^d_k : -c^d_k) (dir: the signs of c for AlignedRusanovFlux, the offset
+// otherwise), mu_d = _moment_mu(-b), e^d_k = (x_k . mu_d)_+, scaled down so that sum e <= sum |c| (_MOMENT_CAP 1).
+__global__ void k_mweights(MlsArgs a) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int D = a.D, cnt = a.cnt[i];
+    const int64_t np = a.npad;
+    double mus[3][3];
+    for (int d = 0; d < D; ++d) {
+        double b[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < cnt; ++k) {
+            const double c = a.dw[(int64_t(k) * D + d) * np + i];
+            const double dir = a.aligned ? (c > 0.0 ? 1.0 : (c < 0.0 ? -1.0 : 0.0)) : a.dist[(int64_t(k) * D + d) * np + i];
+            const double gcoef = dir > 0.0 ? c : -c;
+            for (int e = 0; e < D; ++e) b[e] = b[e] + gcoef * (a.dist[(int64_t(k) * D + e) * np + i] * a.invL);
+        }
+        double nb[3];
+        for (int e = 0; e < D; ++e) nb[e] = -b[e];
+        moment_mu(a, i, cnt, nb, mus[d]);
+    }
+    double sum_e = 0.0, sum_g = 0.0;
+    for (int k = 0; k < cnt; ++k) {
+        double x[3];
+        for (int e = 0; e < D; ++e) x[e] = a.dist[(int64_t(k) * D + e) * np + i] * a.invL;
+        double se = 0.0, sg = 0.0;
+        for (int d = 0; d < D; ++d) {
+            double t = x[0] * mus[d][0];
+            for (int e = 1; e < D; ++e) t = t + x[e] * mus[d][e];
+            const double ep = t > 0.0 ? t : 0.0;
+            se = d == 0 ? ep : se + ep;
+            const double ag = fabs(a.dw[(int64_t(k) * D + d) * np + i]);
+            sg = d == 0 ? ag : sg + ag;
+        }
+        sum_e = sum_e + se;
+        sum_g = sum_g + sg;
+    }
+    const double scale = sum_e > sum_g ? sum_g / sum_e : 1.0;
+    for (int k = 0; k < cnt; ++k) {
+        double x[3];
+        for (int e = 0; e < D; ++e) x[e] = a.dist[(int64_t(k) * D + e) * np + i] * a.invL;
+        for (int d = 0; d < D; ++d) {
+            double t = x[0] * mus[d][0];
+            for (int e = 1; e < D; ++e) t = t + x[e] * mus[d][e];
+            a.mw[(int64_t(k) * D + d) * np + i] = scale * (t > 0.0 ? t : 0.0);
+        }
+    }
+}
+
 // ---- outflow donor map
 __global__ void k_donor_init(DonorArgs a, int tag, int first) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -347,6 +476,7 @@ hcc_status mls_prepare(MlsArgs &a, cudaStream_t s, std::string &err) {
     if (need <= 4) k_mls<4><<<grid_for(a.n, 128), 128, 0, s>>>(a);
     else if (need <= 10) k_mls<10><<<grid_for(a.n, 128), 128, 0, s>>>(a);
     else k_mls<kMaxB><<<grid_for(a.n, 64), 64, 0, s>>>(a);
+    if (a.mw) k_mweights<<<grid_for(a.n, 128), 128, 0, s>>>(a);
     for (int q = 1; q <= a.central_qmax; ++q) {
         if (need <= 4) k_mls_central<4><<<grid_for(a.n, 128), 128, 0, s>>>(a, q);
         else if (need <= 10) k_mls_central<10><<<grid_for(a.n, 128), 128, 0, s>>>(a, q);

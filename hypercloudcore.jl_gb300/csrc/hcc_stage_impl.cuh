@@ -1070,6 +1070,18 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
                 }
             }
             acc.add(t);
+            if (a.g.mw) {
+                // moment correction of a first-order scheme (MUSCL.jl:501-505): -1/2 sum_d s_d e^d_ij (f_ji - f_ij),
+                // the speeds s_d = max(λ_d) of the pair (FP32: the doubled form of the scaled Rusanov flux)
+                T se = vmax(lij[0], lji[0]) * a.g.mw[(int64_t(k) * D) * np + i];
+#pragma unroll
+                for (int d = 1; d < D; ++d) se = se + vmax(lij[d], lji[d]) * a.g.mw[(int64_t(k) * D + d) * np + i];
+                const T corr = kFast ? se : T(0.5) * se;
+                T t2[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) t2[m] = -(corr * (fji[m] - fij[m]));
+                acc.add(t2);
+            }
         }
     } else if (need_ext) {
         for (int k = k0; k < cnt; k += KSTEP) {

@@ -137,7 +137,8 @@ typedef struct {
     int32_t flux;                      /* hcc_flux (MUSCL numerical flux) */
     int32_t reset_orders_per_stage;    /* 1: restore the maximum order before each stage's full pass */
     int32_t upwind_algorithm;          /* hcc_upwind_algorithm (HCC_SCHEME_UPWIND) */
-    int32_t reserved_i[2];
+    int32_t moment_correction;         /* MUSCL(...; moment_correction = true): first-order schemes only (MUSCL.jl:57) */
+    int32_t reserved_i[1];
     double  dx[HCC_MAX_DIM];           /* nominal spacing per axis; h = min(dx) scales the MLS basis */
     double  radius;                    /* support radius R of ExponentialWeightFunction */
     double  weight_alpha;              /* alpha of ExponentialWeightFunction (MLSWeightFunctions.jl:79-82) */

@@ -548,6 +548,8 @@ struct Solver {
     double invL = 1.0;
     bool streamed = true;
     bool aligned = false;            // AlignedRusanovFlux
+    bool moment = false;             // MUSCL(...; moment_correction = true) of a first-order scheme
+    std::vector<double> mw;          // its per-slot weights e^d_ij (slots * D)
     // moving grid (GridMovers.jl): mover kind, its parameters, positions as stage variables
     hcc_mover mover{};
     std::vector<double> x_n, x_cand, Xst[5], KX[5];
@@ -588,6 +590,7 @@ struct Solver {
         }
         max_order = c.muscl_order;
         aligned = c.flux == HCC_FLUX_ALIGNED;
+        moment = c.moment_correction != 0 && max_order == 1 && c.scheme == HCC_SCHEME_MUSCL;
         weno = c.scheme == HCC_SCHEME_WENO;
         central = c.scheme == HCC_SCHEME_CENTRAL;
         upwind = c.scheme == HCC_SCHEME_UPWIND ? c.upwind_algorithm : 0;
@@ -816,8 +819,135 @@ struct Solver {
             }
         }
         if (central) central_weights();
+        if (moment) moment_weights();
         have_geom = true;
         return true;
+    }
+
+    // _moment_mu (MUSCL.jl:285-330): mu with sum_k (x_k . mu)_+ x_k = b over the scaled offsets x_k of particle i,
+    // the minimiser of the convex Phi(mu) = 1/2 sum_k (x_k . mu)_+^2 - b . mu by Newton steps on the active slots
+    // with Armijo backtracking; zero when b is zero, a Hessian fails the pivot test, or 30 steps do not converge.
+    void moment_mu(int64_t i, const double *b, double *mu) const {
+        for (int d = 0; d < D; ++d) mu[d] = 0.0;
+        double nb2 = b[0] * b[0];
+        for (int d = 1; d < D; ++d) nb2 = nb2 + b[d] * b[d];
+        if (!(nb2 > 0.0)) return;
+        auto hessian = [&](const double *m, double *H, double *g, double *phi, bool all) {
+            for (int q = 0; q < D * D; ++q) H[q] = 0.0;
+            if (g) for (int d = 0; d < D; ++d) g[d] = -b[d];
+            if (phi) {
+                double t = b[0] * m[0];
+                for (int d = 1; d < D; ++d) t = t + b[d] * m[d];
+                *phi = -t;
+            }
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                double x[3];
+                for (int d = 0; d < D; ++d) x[d] = ndist[s * D + d] * invL;
+                double t = 0.0;
+                if (!all) {
+                    t = x[0] * m[0];
+                    for (int d = 1; d < D; ++d) t = t + x[d] * m[d];
+                    if (!(t > 0.0)) continue;
+                }
+                for (int r = 0; r < D; ++r)
+                    for (int c = 0; c < D; ++c) H[r * D + c] = H[r * D + c] + x[r] * x[c];
+                if (g) for (int d = 0; d < D; ++d) g[d] = g[d] + t * x[d];
+                if (phi) *phi = *phi + (t * t) / 2.0;
+            }
+        };
+        auto pivots_ok = [&](const double *H, double *Uc) {
+            if (!cholesky_upper(D, H, Uc)) return false;
+            for (int k = 0; k < D; ++k) {
+                const double u = Uc[k * D + k];
+                if (!(u * u > 10.0 * kEps * H[k * D + k])) return false;
+            }
+            return true;
+        };
+        double H[9], Uc[9], m[3], g[3], Dl[3], zero[3] = {0.0, 0.0, 0.0};
+        hessian(zero, H, nullptr, nullptr, true);
+        if (!pivots_ok(H, Uc)) return;
+        chol_solve(D, Uc, b, m);
+        for (int d = 0; d < D; ++d) m[d] = 2.0 * m[d];
+        const double tol = std::sqrt(kEps);
+        for (int it = 0; it < 30; ++it) {
+            double phi;
+            hessian(m, H, g, &phi, false);
+            double gg = g[0] * g[0];
+            for (int d = 1; d < D; ++d) gg = gg + g[d] * g[d];
+            if (gg <= (tol * tol) * nb2) {
+                for (int d = 0; d < D; ++d) mu[d] = m[d];
+                return;
+            }
+            if (!pivots_ok(H, Uc)) return;
+            chol_solve(D, Uc, g, Dl);
+            double gD = g[0] * Dl[0];
+            for (int d = 1; d < D; ++d) gD = gD + g[d] * Dl[d];
+            double lam = 1.0;
+            for (int ls = 0; ls < 40; ++ls) {
+                double mn[3];
+                for (int d = 0; d < D; ++d) mn[d] = m[d] - lam * Dl[d];
+                double t0 = b[0] * mn[0];
+                for (int d = 1; d < D; ++d) t0 = t0 + b[d] * mn[d];
+                double phin = -t0;
+                for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                    double t = (ndist[s * D] * invL) * mn[0];
+                    for (int d = 1; d < D; ++d) t = t + (ndist[s * D + d] * invL) * mn[d];
+                    if (t > 0.0) phin = phin + (t * t) / 2.0;
+                }
+                if (phin <= phi - (lam * gD) / 4.0) break;
+                lam = lam / 2.0;
+            }
+            for (int d = 0; d < D; ++d) m[d] = m[d] - lam * Dl[d];
+        }
+    }
+
+    // update_moment_weights! (MUSCL.jl:224-283): per axis d the first moment b = sum_k g^d_k x_k of the dissipation
+    // coefficients g^d_k = (dir_d > 0 ? c^d_k : -c^d_k) (dir: the signs of c for AlignedRusanovFlux, the offset
+    // otherwise), mu_d = _moment_mu(-b), e^d_k = (x_k . mu_d)_+; scaled down so that sum e <= sum |c| (_MOMENT_CAP 1).
+    void moment_weights() {
+        mw.assign(nidx.size() * D, 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < N; ++i) {
+            double mus[3][3] = {};
+            for (int d = 0; d < D; ++d) {
+                double b[3] = {0.0, 0.0, 0.0};
+                for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                    const double c = dw[s * D + d];
+                    const double dir = aligned ? (c > 0.0 ? 1.0 : (c < 0.0 ? -1.0 : 0.0)) : ndist[s * D + d];
+                    const double gcoef = dir > 0.0 ? c : -c;
+                    for (int e = 0; e < D; ++e) b[e] = b[e] + gcoef * (ndist[s * D + e] * invL);
+                }
+                double nb[3];
+                for (int e = 0; e < D; ++e) nb[e] = -b[e];
+                moment_mu(i, nb, mus[d]);
+            }
+            double sum_e = 0.0, sum_g = 0.0;
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                double x[3];
+                for (int e = 0; e < D; ++e) x[e] = ndist[s * D + e] * invL;
+                double se = 0.0, sg = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    double t = x[0] * mus[d][0];
+                    for (int e = 1; e < D; ++e) t = t + x[e] * mus[d][e];
+                    const double ep = t > 0.0 ? t : 0.0;
+                    se = d == 0 ? ep : se + ep;
+                    const double ag = std::fabs(dw[s * D + d]);
+                    sg = d == 0 ? ag : sg + ag;
+                }
+                sum_e = sum_e + se;
+                sum_g = sum_g + sg;
+            }
+            const double scale = sum_e > sum_g ? sum_g / sum_e : 1.0;
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                double x[3];
+                for (int e = 0; e < D; ++e) x[e] = ndist[s * D + e] * invL;
+                for (int d = 0; d < D; ++d) {
+                    double t = x[0] * mus[d][0];
+                    for (int e = 1; e < D; ++e) t = t + x[e] * mus[d][e];
+                    mw[s * D + d] = scale * (t > 0.0 ? t : 0.0);
+                }
+            }
+        }
     }
 
     // CentralDivergence (Central.jl:45-88) takes the intercept fit of degree q = the particle's (starved-lowered)
@@ -1061,6 +1191,8 @@ struct Solver {
 
         double pi_[32], pj_[32], hd[3], fij[HCC_MAX_VARS], fji[HCC_MAX_VARS];
         double Fij[3 * HCC_MAX_VARS], Fji[3 * HCC_MAX_VARS], dF[3 * HCC_MAX_VARS];
+        double sd_axis[3] = {0.0, 0.0, 0.0}, extra[HCC_MAX_VARS];
+        for (int m = 0; m < M; ++m) extra[m] = 0.0;
         for (int64_t s = start[i]; s < start[i + 1]; ++s) {
             const double *dk = &ndist[s * D];
             int64_t j = nidx[s];
@@ -1121,6 +1253,7 @@ struct Solver {
                 const double *FR = pos_ ? &Fji[d * M] : &Fij[d * M];
                 double sdd = ale ? jmax(phys.lam_shift(fL, d, wv[d]), phys.lam_shift(fR, d, wv[d]))
                                  : jmax(phys.lam(fL, d), phys.lam(fR, d));
+                sd_axis[d] = sdd;
                 for (int m = 0; m < M; ++m) {
                     double Fn = 0.5 * ((FL[m] + FR[m]) - sdd * (fR[m] - fL[m]));
                     dF[d * M + m] = Fn - Fi[d * M + m];
@@ -1136,6 +1269,14 @@ struct Solver {
             } else {
                 double *dst = &buf[size_t(s - start[i]) * D * M];
                 for (int q = 0; q < D * M; ++q) dst[q] = dF[q];
+            }
+            if (moment) {
+                // moment correction of a first-order scheme (MUSCL.jl:501-505): -1/2 sum_d s_d e^d_ij (f_ji - f_ij)
+                double se = sd_axis[0] * mw[s * D + 0];
+                for (int d = 1; d < D; ++d) se = se + sd_axis[d] * mw[s * D + d];
+                const double corr = 0.5 * se;
+                double *tgt = per_slot ? div : extra;
+                for (int m = 0; m < M; ++m) tgt[m] = tgt[m] - corr * (fji[m] - fij[m]);
             }
         }
         if (per_slot) return;
@@ -1193,6 +1334,8 @@ struct Solver {
                 div[m] = acc * invL;
             }
         }
+        if (moment)   // fit + extra (MUSCL.jl:420)
+            for (int m = 0; m < M; ++m) div[m] = div[m] + extra[m];
     }
 
     // ------------------------------------------------------------ WENO (WENO.jl:55-165), scalar
