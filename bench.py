@@ -375,6 +375,83 @@ def run_3d(hcc, args, world, local):
             **learned}
 
 
+def run_ensemble(hcc, args, world, local):
+    """Batched ensemble: `args.ensemble_clouds` independent 2-D clouds (default 512) with log-uniform node counts in
+    [4k, 256k] (seeded), one spacing h = 1/256, jittered lattices with transmissive walls. Even clouds: Euler
+    (gamma 1.4) from random Voronoi states (2-6 regions, rho, p ~ U[0.1, 2], u, v ~ U[-1, 1]) with MUSCL2 + MOOD,
+    SSP-RK3. Odd clouds: BGK-type discrete-velocity relaxation, 16 velocities on the unit ring, epsilon 1e-4, one
+    macro moment advected with (1, 0.5), implicit source by IMEX ARS(2,2,2), from smooth random Fourier densities.
+    FP32 bulk. One context per system holds its whole batch (hcc_upload_batch: one cell list, one captured step
+    graph per step), one dt per batch (its minimum CFL step)."""
+    learned = sys.modules["hcc_gb300.learned"]
+    rng = np.random.default_rng(2026)
+    nc = args.ensemble_clouds
+    target = np.exp(rng.uniform(np.log(4000.0), np.log(256000.0), nc))
+    sides = np.maximum(8, np.rint(np.sqrt(target)).astype(int) - 1)
+    h = 1.0 / 256
+    t0 = time.time()
+    groups = {"euler": [], "bgk": []}
+    states = {"euler": [], "bgk": []}
+    for k in range(nc):
+        L = sides[k] * h
+        cl = hcc.rectangular_cloud((0.0, 0.0), (L, L), h, 2.5 * h, jitter=0.25 * h, seed=1000 + k)
+        xl = cl.pos / L
+        if k % 2 == 0:
+            groups["euler"].append(cl)
+            states["euler"].append(learned.voronoi_state(xl, seed=k))
+        else:
+            r = np.random.default_rng(50000 + k)
+            rho = np.ones(cl.n)
+            for _ in range(3):
+                kx, ky = r.integers(1, 4, 2)
+                rho += 0.1 * r.uniform(0.5, 1.0) * np.sin(2 * np.pi * (kx * xl[:, 0] + ky * xl[:, 1]) + r.uniform(0, 6.3))
+            groups["bgk"].append(cl)
+            states["bgk"].append(np.repeat((rho / 16.0)[:, None], 16, axis=1))
+    ring = [(float(np.cos(2 * np.pi * q / 16)), float(np.sin(2 * np.pi * q / 16))) for q in range(16)]
+    out = {"workload": f"ensemble_{nc}_clouds_2d", "clouds": nc, "setup": {}}
+    totals = {}
+    for name in ("euler", "bgk"):
+        cl0 = groups[name][0]
+        mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
+        bc = {t: hcc.BC_OUTFLOW for t in range(1, 5)}
+        if name == "euler":
+            cfg = hcc.make_config(hcc.Euler(2, 1.4), cl0, scheme=hcc.MUSCL(2, 2), mood=mood, tableau="RK3_SSP",
+                                  bc_map=bc, precision="fp32")
+            stages = 3
+        else:
+            pde = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
+            cfg = hcc.make_config(pde, cl0, scheme=hcc.MUSCL(2, 2), mood=mood, tableau="IMEX_ARS222",
+                                  bc_map=bc, precision="fp32")
+            stages = 3          # ARS(2,2,2): three stages (ButcherTableaus.jl:218-229)
+        ctx = hcc.Context(cfg)
+        ts = time.time()
+        union = ctx.upload_batch(groups[name])
+        ctx.build_neighbours()
+        ctx.prepare_geometry()
+        U = np.concatenate(states[name]).astype(np.float32)
+        ctx.upload_state(U)
+        dt = 0.4 * ctx.time_step()
+        for _ in range(2):
+            ctx.step(0.0, dt)
+        ctx.upload_state(U)
+        with ClockSampler(local) as clk:
+            ms, launches = time_device_steps(hcc, ctx, dt, args.ensemble_steps, world)
+        c = ctx.counters()
+        n_int = int((union.is_boundary == 0).sum())
+        totals[name] = (n_int * stages * args.ensemble_steps, ms)
+        out[name] = {"clouds": len(groups[name]), "particles": union.n, "interior": n_int,
+                     "ms_per_step": ms / args.ensemble_steps, "stages": stages, "dt": dt, "gpu_launches": launches,
+                     "mood_iterations_last_step": c["mood_iterations"], "graph_steps": c["graph_steps"],
+                     "setup_s": time.time() - ts, "clocks": clk.summary()}
+        ctx.close()
+    units = sum(u for u, _ in totals.values())
+    ms_total = sum(m for _, m in totals.values())
+    out["value"] = units * world / (ms_total / 1e3)
+    out["unit"] = "point-updates/s per RK stage (both batches, interior particles)"
+    out["generation_s"] = time.time() - t0
+    return out
+
+
 def run_gpu(args):
     world, rank, local = dist_setup()
     hcc = package()
@@ -477,6 +554,8 @@ def run_gpu(args):
         line["published_case"] = run_published_case(hcc, args.steps)
     if not args.no_3d and D == 2:
         line["euler3d_blast_8M"] = run_3d(hcc, args, world, local)
+    if not args.no_ensemble and D == 2:
+        line["ensemble"] = run_ensemble(hcc, args, world, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(hcc, cloud, U0, h, args.cpu_steps)
     if rank == 0:
@@ -585,6 +664,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp32-only", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="no troubled-point predictor (plain FP32 headline)")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched 512-cloud ensemble")
+    ap.add_argument("--ensemble-clouds", type=int, default=512)
+    ap.add_argument("--ensemble-steps", type=int, default=5)
     ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
     ap.add_argument("--no-published", action="store_true")
     ap.add_argument("--no-3d", action="store_true")

@@ -342,6 +342,40 @@ class Context:
                                               _ptr(tags, C.c_int32), _ptr(vol, C.c_double)), "hcc_upload_cloud")
         self.n = pos.shape[0]
 
+    def upload_batch(self, clouds) -> Cloud:
+        """Upload independent clouds as one batch (hcc_upload_batch): the library packs them side by side with
+        gaps wider than the support; returns the union as a Cloud (positions shifted, the union canvas), whose
+        meta holds the per-cloud `offsets` and `shifts`."""
+        D = self.D
+        offsets = np.zeros(len(clouds) + 1, dtype=np.int64)
+        offsets[1:] = np.cumsum([c.n for c in clouds])
+        pos = np.ascontiguousarray(np.concatenate([c.pos for c in clouds]), dtype=np.float64)
+        bnd = np.ascontiguousarray(np.concatenate([c.is_boundary for c in clouds]), dtype=np.uint8)
+        tags = np.ascontiguousarray(np.concatenate([c.tags for c in clouds]), dtype=np.int32)
+        vol = np.ascontiguousarray(np.concatenate([c.volumes for c in clouds]), dtype=np.float64)
+        shifts = np.zeros((len(clouds), D), dtype=np.float64)
+        canvas = np.zeros(2 * D, dtype=np.float64)
+        self._check(self.lib.hcc_upload_batch(self._h, len(clouds), _ptr(offsets, C.c_int64), _ptr(pos, C.c_double),
+                                              _ptr(bnd, C.c_uint8), _ptr(tags, C.c_int32), _ptr(vol, C.c_double),
+                                              _ptr(shifts, C.c_double), _ptr(canvas, C.c_double)),
+                    "hcc_upload_batch")
+        self.n = int(offsets[-1])
+        self._batch_n = len(clouds)
+        shifted = pos + np.repeat(shifts, np.diff(offsets), axis=0)
+        lo, hi = tuple(canvas[:D]), tuple(canvas[D:])
+        c0 = clouds[0]
+        return Cloud(shifted, bnd, tags, vol, c0.dx, c0.radius, lo, hi, lo, hi, (False,) * D,
+                     {"offsets": offsets, "shifts": shifts, "batch": True})
+
+    def batch_total_mass(self) -> np.ndarray:
+        """total_mass per cloud of the last batch: (n_clouds, M)."""
+        n = getattr(self, "_batch_n", None)
+        if n is None:
+            raise HCCError(_abi.HCC_ERR_STATE, "no batch uploaded", "hcc_batch_total_mass")
+        out = np.zeros((n, self.M), dtype=np.float64)
+        self._check(self.lib.hcc_batch_total_mass(self._h, _ptr(out, C.c_double)), "hcc_batch_total_mass")
+        return out
+
     def build_neighbours(self):
         self._check(self.lib.hcc_build_neighbours(self._h), "hcc_build_neighbours")
 

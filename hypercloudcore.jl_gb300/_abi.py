@@ -135,6 +135,8 @@ PROTOTYPES = [
     ("hcc_load_snapshot", C.c_int, [P, C.c_char_p]),
     ("hcc_get_kernel_times", C.c_int, [P, C.POINTER(HccKernelTimes), C.c_int]),
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
+    ("hcc_upload_batch", C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), _dp, _u8p, _i32p, _dp, _dp, _dp]),
+    ("hcc_batch_total_mass", C.c_int, [P, _dp]),
     ("hcc_mlp_create", C.c_int, [C.POINTER(HccMlpConfig), C.POINTER(P)]),
     ("hcc_mlp_destroy", None, [P]),
     ("hcc_mlp_last_error", C.c_char_p, [P]),

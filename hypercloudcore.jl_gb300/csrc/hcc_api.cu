@@ -178,6 +178,7 @@ struct hcc_ctx {
     int qmax = 1;
     double *dwc64[3] = {}; float *dwc32[3] = {}; uint8_t *okc[3] = {};
     double *mw64 = nullptr; float *mw32 = nullptr;   // moment-correction weights (first-order MUSCL)
+    std::vector<int64_t> batch_offsets;              // clouds of the last hcc_upload_batch (empty: one cloud)
     bool moment() const { return cfg.moment_correction && max_order == 1 && !weno && !central && !upwind; }
     bool no_recon() const { return weno || central || upwind; }
 
@@ -1154,6 +1155,7 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
     c->free_particles();
     c->free_slots();
     c->have_cloud = c->have_nb = c->have_geom = c->have_state = false;
+    c->batch_offsets.clear();
     c->n = n;
     c->npad = ((n + 31) / 32) * 32;
     const int D = c->D, M = c->M;
@@ -1723,6 +1725,101 @@ hcc_status hcc_get_kernel_times(hcc_ctx *c, hcc_kernel_times *out, int reset) {
     if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
     *out = c->times;
     if (reset) c->times = hcc_kernel_times{};
+    return HCC_OK;
+}
+
+hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets, const double *pos,
+                            const uint8_t *is_boundary, const int32_t *tags, const double *volumes, double *shifts,
+                            double *canvas) {
+    if (!c) return HCC_ERR_INVALID;
+    if (n_clouds < 1 || !offsets || offsets[0] != 0) return c->fail(HCC_ERR_INVALID, "bad batch offsets");
+    for (int b = 0; b < n_clouds; ++b)
+        if (offsets[b + 1] < offsets[b]) return c->fail(HCC_ERR_INVALID, "batch offsets must not decrease");
+    const int D = c->D;
+    for (int d = 0; d < D; ++d)
+        if (c->cfg.periodic[d]) return c->fail(HCC_ERR_INVALID, "batches of periodic clouds are not supported");
+    const int64_t n = offsets[n_clouds];
+    if (n > 0 && !pos) return c->fail(HCC_ERR_INVALID, "bad cloud arguments");
+    // bounding boxes
+    std::vector<double> lo(size_t(n_clouds) * 3, 0.0), hi(size_t(n_clouds) * 3, 0.0);
+    for (int b = 0; b < n_clouds; ++b) {
+        for (int d = 0; d < D; ++d) { lo[b * 3 + d] = INFINITY; hi[b * 3 + d] = -INFINITY; }
+        for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i)
+            for (int d = 0; d < D; ++d) {
+                const double x = pos[i * D + d];
+                if (!std::isfinite(x)) return c->fail(HCC_ERR_NONFINITE, "non-finite position");
+                lo[b * 3 + d] = std::min(lo[b * 3 + d], x);
+                hi[b * 3 + d] = std::max(hi[b * 3 + d], x);
+            }
+        for (int d = 0; d < D; ++d)
+            if (offsets[b + 1] == offsets[b]) { lo[b * 3 + d] = 0.0; hi[b * 3 + d] = 0.0; }
+    }
+    // shelf packing in the (x, y) plane, tallest first; z (3-D) aligned at 0; 1-D: one row
+    const double gap = 2.0 * c->cfg.radius;
+    std::vector<int> order(n_clouds);
+    for (int b = 0; b < n_clouds; ++b) order[b] = b;
+    auto ext = [&](int b, int d) { return hi[b * 3 + d] - lo[b * 3 + d]; };
+    if (D >= 2)
+        std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return ext(p, 1) > ext(q, 1); });
+    double area = 0.0, widest = 0.0;
+    for (int b = 0; b < n_clouds; ++b) {
+        area += (ext(b, 0) + gap) * (D >= 2 ? ext(b, 1) + gap : 1.0);
+        widest = std::max(widest, ext(b, 0) + gap);
+    }
+    const double row_w = D >= 2 ? std::max(widest, 1.2 * std::sqrt(area)) : INFINITY;
+    std::vector<double> sh(size_t(n_clouds) * 3, 0.0);
+    double x = 0.0, y = 0.0, row_h = 0.0;
+    for (int b : order) {
+        const double w = ext(b, 0) + gap;
+        if (x > 0.0 && x + w > row_w) { x = 0.0; y += row_h; row_h = 0.0; }
+        sh[b * 3 + 0] = x - lo[b * 3 + 0];
+        if (D >= 2) sh[b * 3 + 1] = y - lo[b * 3 + 1];
+        if (D == 3) sh[b * 3 + 2] = -lo[b * 3 + 2];
+        x += w;
+        if (D >= 2) row_h = std::max(row_h, ext(b, 1) + gap);
+    }
+    std::vector<double> up(size_t(n) * D);
+    double cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < n_clouds; ++b)
+        for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i)
+            for (int d = 0; d < D; ++d) {
+                const double v = pos[i * D + d] + sh[b * 3 + d];
+                up[i * D + d] = v;
+                cmin[d] = std::min(cmin[d], v);
+                cmax[d] = std::max(cmax[d], v);
+            }
+    for (int d = 0; d < D; ++d) {
+        if (!(cmax[d] > cmin[d])) { cmin[d] -= gap; cmax[d] += gap; }
+        c->cfg.canvas_min[d] = cmin[d];
+        c->cfg.canvas_max[d] = cmax[d];
+        c->cfg.domain_min[d] = cmin[d];
+        c->cfg.domain_max[d] = cmax[d];
+        if (canvas) { canvas[d] = cmin[d]; canvas[D + d] = cmax[d]; }
+    }
+    if (shifts)
+        for (int b = 0; b < n_clouds; ++b)
+            for (int d = 0; d < D; ++d) shifts[b * D + d] = sh[b * 3 + d];
+    hcc_status st = hcc_upload_cloud(c, n, up.data(), is_boundary, tags, volumes);
+    if (st != HCC_OK) return st;
+    c->batch_offsets.assign(offsets, offsets + n_clouds + 1);
+    return HCC_OK;
+}
+
+hcc_status hcc_batch_total_mass(hcc_ctx *c, double *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    if (c->batch_offsets.size() < 2) return c->fail(HCC_ERR_STATE, "no batch uploaded");
+    hcc_status st;
+    const size_t nb = c->batch_offsets.size() - 1;
+    for (size_t b = 0; b < nb; ++b) {
+        const int64_t o = c->batch_offsets[b], m = c->batch_offsets[b + 1] - o;
+        const void *U = c->f32 ? static_cast<const void *>(static_cast<const float *>(c->rhos) + o * c->M)
+                               : static_cast<const void *>(static_cast<const double *>(c->rhos) + o * c->M);
+        launch_total_mass(U, c->vol + o, m, c->M, c->f32, c->d_mass, c->stream);
+        HCC_TRY(c->sync("batch mass"));
+        HCC_TRY(c->cuda(cudaMemcpy(out + b * c->M, c->d_mass, c->M * sizeof(double), cudaMemcpyDeviceToHost),
+                        "batch mass copy"));
+    }
     return HCC_OK;
 }
 

@@ -288,6 +288,22 @@ typedef struct {
 hcc_status hcc_set_profiling(hcc_ctx *ctx, int enable);
 hcc_status hcc_get_kernel_times(hcc_ctx *ctx, hcc_kernel_times *out, int reset);
 
+/* Batched ensemble: many independent clouds of the same configuration (physics, spacing, radius, scheme) advanced
+   by one context — one cell list, one set of passes, one captured step graph — with no communication between the
+   clouds. No counterpart in the reference (one ParticleGrid per run). The clouds (concatenated; cloud c is
+   [offsets[c], offsets[c+1])) come in their own frames; the library packs their bounding boxes side by side
+   (shelf packing, tallest first) with gaps of two support radii, so that no particle has a neighbour in another
+   cloud, sets the context's canvas to the union and uploads it. shifts[c*dim + d] (may be NULL) receives the
+   translation applied to cloud c, canvas[0..2*dim) (may be NULL) the union box (min then max). Non-periodic
+   configurations only. Afterwards the context behaves as with hcc_upload_cloud on the union (same particle
+   numbering: cloud by cloud); every step uses one dt for all clouds (the minimum CFL step of the union). */
+hcc_status hcc_upload_batch(hcc_ctx *ctx, int32_t n_clouds, const int64_t *offsets, const double *pos,
+                            const uint8_t *is_boundary, const int32_t *tags, const double *volumes, double *shifts,
+                            double *canvas);
+
+/* total_mass per cloud of the last hcc_upload_batch: out[c*M + m] (FP64 accumulation on the device). */
+hcc_status hcc_batch_total_mass(hcc_ctx *ctx, double *out);
+
 /* CFL time step of caller-owned device arrays WITHOUT allocating device memory. No counterpart in the reference.
    For callers that cannot allocate GPU memory when they need a time step: a code that reserves its device memory
    up front and then freezes it, or one that routes all device memory through its own pool and forbids
