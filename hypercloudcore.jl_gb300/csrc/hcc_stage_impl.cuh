@@ -885,7 +885,7 @@ template <typename T, int M> struct FluxPart {
 
 // The flux pass of particle i over its slots k0, k0 + KSTEP, ... With KSTEP = 1 the whole pass and its epilogue;
 // with KSTEP > 1 (FP32) the partial sums and extrema go to `part` for the caller to combine.
-template <typename T, int D, int M, int PDE, int RDEG, bool ALE, int KSTEP = 1>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, int KSTEP = 1, bool MOM = false>
 __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i, const int k0 = 0,
                                          FluxPart<T, M> *part = nullptr) {
     constexpr int BR = RBasis<D, RDEG>::B;
@@ -1070,7 +1070,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
                 }
             }
             acc.add(t);
-            if (a.g.mw) {
+            if constexpr (MOM) {
                 // moment correction of a first-order scheme (MUSCL.jl:501-505): -1/2 sum_d s_d e^d_ij (f_ji - f_ij),
                 // the speeds s_d = max(λ_d) of the pair (FP32: the doubled form of the scaled Rusanov flux)
                 T se = vmax(lij[0], lji[0]) * a.g.mw[(int64_t(k) * D) * np + i];
@@ -1122,12 +1122,12 @@ template <typename T> __device__ __forceinline__ void tile_failures(const StageA
 
 // A full pass (one thread per particle) or a worklist pass over tiles (one warp per tile, the members of its word;
 // the reach marks are cleared once read). Either way each warp reports the failed candidates of its tile.
-template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, bool MOM = false>
 __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_flux(const StageArgs<T> a) {
     const int lane = int(threadIdx.x & 31);
     if (a.full) {
         const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG, ALE>(a, i) : false;
+        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG, ALE, 1, MOM>(a, i) : false;
         if (a.check) tile_failures(a, i >> 5, f);
         return;
     }
@@ -1137,7 +1137,7 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
         const int32_t tile = a.wtiles[q];
         const uint32_t word = a.wmask[tile];
         const int64_t i = int64_t(tile) * 32 + lane;
-        const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG, ALE>(a, i) : false;
+        const bool f = ((word >> lane) & 1u) ? flux_one<T, D, M, PDE, RDEG, ALE, 1, MOM>(a, i) : false;
         if (a.check) tile_failures(a, tile, f);
         if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
     }
@@ -1147,7 +1147,7 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
 // (a quarter of the serial slot chain, the latency that bounds the short worklist passes), warp 0 combines the four
 // compensated partial sums (Kahan over the partials, minus their compensations) and the extrema, and runs the
 // epilogue. One block per tile, block-stride over the list.
-template <typename T, int D, int M, int PDE, int RDEG, bool ALE>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, bool MOM = false>
 __global__ void __launch_bounds__(128) k_flux_tiles(const StageArgs<T> a) {
     __shared__ FluxPart<T, M> parts[4][32];
     const int lane = int(threadIdx.x & 31), w = int(threadIdx.x >> 5);
@@ -1157,7 +1157,7 @@ __global__ void __launch_bounds__(128) k_flux_tiles(const StageArgs<T> a) {
         const uint32_t word = a.wmask[tile];
         const int64_t i = int64_t(tile) * 32 + lane;
         const bool live = ((word >> lane) & 1u) && !a.g.bnd[i];
-        if (live) flux_one<T, D, M, PDE, RDEG, ALE, 4>(a, i, w, &parts[w][lane]);
+        if (live) flux_one<T, D, M, PDE, RDEG, ALE, 4, MOM>(a, i, w, &parts[w][lane]);
         __syncthreads();
         if (w == 0) {
             bool f = false;
@@ -1629,8 +1629,27 @@ struct StageInst {
         }
         k_gather<T, D, M, PDE, RDEG><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
     }
+    template <bool MOM> static void flux_mom(const StageArgs<T> &a, int64_t n, cudaStream_t s) {
+        if constexpr (sizeof(T) == 4) {
+            if (!a.full) {
+                const unsigned g = std::max(1u, unsigned(a.list_blocks));
+                if (a.mover) k_flux_tiles<T, D, M, PDE, RDEG, true, MOM><<<g, 128, 0, s>>>(a);
+                else k_flux_tiles<T, D, M, PDE, RDEG, false, MOM><<<g, 128, 0, s>>>(a);
+                return;
+            }
+        }
+        if (a.mover)
+            k_flux<T, D, M, PDE, RDEG, true, MOM><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+        else
+            k_flux<T, D, M, PDE, RDEG, false, MOM><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+    }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        // first-order MUSCL with the moment correction: its own instantiation (the per-slot correction costs the
+        // plain pass registers)
+        if constexpr (RDEG == 1) {
+            if (a.g.mw) { flux_mom<true>(a, n, s); return; }
+        }
         if constexpr (sizeof(T) == 4) {
             if (!a.full) {   // FP32 worklist pass: split tiles (four warps a tile)
                 const unsigned g = std::max(1u, unsigned(a.list_blocks));
