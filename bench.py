@@ -452,6 +452,38 @@ def run_ensemble(hcc, args, world, local):
     return out
 
 
+def run_profile_case(args):
+    """Fixed workloads for kernel profilers (no timing, no JSON contract): `learned` / `plain` run
+    `--profile-steps` host-driven steps of the bench workload with / without the shipped predictor; `predictor`
+    runs the predictor's kernels on their own (1M random feature rows through the network, one 9728-row
+    forward/backward pass) and then three host-driven steps with the predictor."""
+    hcc = package()
+    import torch
+    torch.cuda.set_device(0)
+    cloud, U0, h = make_workload(hcc, args.workload)
+    pred = load_predictor(hcc)
+    if args.profile == "predictor":
+        rng = np.random.default_rng(0)
+        X = np.abs(rng.normal(0.0, 0.5, (1 << 20, 24))).astype(np.float32)
+        pred.predict_rows(X)
+        n = 128 * 152 * 8 // 16
+        pred.loss_grad(X[:n], (rng.random(n) < 0.4).astype(np.uint8))
+    steps = 3 if args.profile == "predictor" else args.profile_steps
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, "fp32"))
+    ctx.upload_cloud(cloud)
+    ctx.build_neighbours()
+    ctx.prepare_geometry()
+    ctx.upload_state(U0.astype(np.float32))
+    if args.profile != "plain":
+        ctx.set_predictor(pred, PREDICTOR_THRESHOLD)
+    ctx.set_step_graphs(False)
+    dt = 0.4 * ctx.time_step()
+    for _ in range(steps):
+        ctx.step(0.0, dt)
+    ctx.synchronize()
+    print(json.dumps({"profile": args.profile, "steps": steps, "counters": ctx.counters()}), flush=True)
+
+
 def run_gpu(args):
     world, rank, local = dist_setup()
     hcc = package()
@@ -665,6 +697,9 @@ def main():
     ap.add_argument("--fp32-only", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="no troubled-point predictor (plain FP32 headline)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched 512-cloud ensemble")
+    ap.add_argument("--profile", choices=["learned", "plain", "predictor"], default=None,
+                    help="run a fixed workload for a kernel profiler instead of the benchmark")
+    ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--ensemble-clouds", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=5)
     ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
@@ -676,7 +711,9 @@ def main():
         args.warmup = 3
     global HOST_DRIVEN
     HOST_DRIVEN = args.host_driven
-    if args.impl == "reference":
+    if args.profile:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
