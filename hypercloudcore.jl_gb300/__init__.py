@@ -190,12 +190,17 @@ class MOOD:
 
 
 def mover(kind: str = "none", *, alpha: float = 1.0, velocity=(0.0, 0.0, 0.0), omega=(0.0, 0.0, 0.0),
-          center=(0.0, 0.0, 0.0), full_search_per_stage: bool = False) -> "_abi.HccMover":
+          center=(0.0, 0.0, 0.0), full_search_per_stage: bool = False, volume_estimator: str = "shepard",
+          shepard_sweeps: int = 1) -> "_abi.HccMover":
     """Grid mover (src/TimeStepping/GridMovers.jl): "none" (NoGridMover), "lagrangian" (LagrangianMover), "scaled"
-    (ScaledLagrangianMover(alpha)) or "prescribed" (PrescribedMover with w(x) = velocity + omega x (x - center))."""
+    (ScaledLagrangianMover(alpha)) or "prescribed" (PrescribedMover with w(x) = velocity + omega x (x - center)).
+    `volume_estimator` ("shepard": ShepardVolumes(sweeps) after each step, the reference's default; "none": keep
+    the volumes) is GeneralRKTimeStepper's `volume_estimator` (TimeSteppers.jl:145-146)."""
     m = _abi.HccMover()
     m.kind = _abi.MOVERS[kind]
     m.full_search_per_stage = int(bool(full_search_per_stage))
+    m.keep_volumes = 0 if volume_estimator == "shepard" else 1
+    m.shepard_sweeps = int(shepard_sweeps)
     m.alpha = float(alpha)
     for d in range(3):
         m.velocity[d], m.omega[d], m.center[d] = float(velocity[d]), float(omega[d]), float(center[d])
@@ -366,6 +371,15 @@ class Context:
         c0 = clouds[0]
         return Cloud(shifted, bnd, tags, vol, c0.dx, c0.radius, lo, hi, lo, hi, (False,) * D,
                      {"offsets": offsets, "shifts": shifts, "batch": True})
+
+    def update_volumes(self, sweeps: int = 1):
+        """update_volumes!(pg, ShepardVolumes(sweeps)) (Volumes.jl:183-229)."""
+        self._check(self.lib.hcc_update_volumes(self._h, int(sweeps)), "hcc_update_volumes")
+
+    def volumes(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.float64)
+        self._check(self.lib.hcc_download_volumes(self._h, _ptr(out, C.c_double)), "hcc_download_volumes")
+        return out
 
     def batch_total_mass(self) -> np.ndarray:
         """total_mass per cloud of the last batch: (n_clouds, M)."""

@@ -72,7 +72,7 @@ class HccCounters(C.Structure):
 class HccMover(C.Structure):
     _fields_ = [("kind", C.c_int32), ("full_search_per_stage", C.c_int32), ("alpha", C.c_double),
                 ("velocity", C.c_double * HCC_MAX_DIM), ("omega", C.c_double * HCC_MAX_DIM),
-                ("center", C.c_double * HCC_MAX_DIM)]
+                ("center", C.c_double * HCC_MAX_DIM), ("keep_volumes", C.c_int32), ("shepard_sweeps", C.c_int32)]
 
 
 MOVERS = {"none": 0, "lagrangian": 1, "scaled": 2, "prescribed": 3}
@@ -137,6 +137,8 @@ PROTOTYPES = [
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_upload_batch", C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), _dp, _u8p, _i32p, _dp, _dp, _dp]),
     ("hcc_batch_total_mass", C.c_int, [P, _dp]),
+    ("hcc_update_volumes", C.c_int, [P, C.c_int32]),
+    ("hcc_download_volumes", C.c_int, [P, _dp]),
     ("hcc_mlp_create", C.c_int, [C.POINTER(HccMlpConfig), C.POINTER(P)]),
     ("hcc_mlp_destroy", None, [P]),
     ("hcc_mlp_last_error", C.c_char_p, [P]),

@@ -792,8 +792,12 @@ template <typename T> hcc_status run_step_host(hcc_ctx *c, double dt) {
             return st;
     }
     if (mv) {
-        // final positions; full search with periodic re-wrap for the next step (TimeSteppers.jl:571-575)
+        // final positions; full search with periodic re-wrap for the next step (TimeSteppers.jl:571-575), then the
+        // volume estimator (:574)
         if ((st = apply_positions(c, c->x_cand, true)) != HCC_OK) return st;
+        if (!c->mover.keep_volumes &&
+            (st = hcc_update_volumes(c, c->mover.shepard_sweeps > 0 ? c->mover.shepard_sweeps : 1)) != HCC_OK)
+            return st;
     }
     if ((st = read_mood_stats(c, c->stream)) != HCC_OK) return st;
     st = c->sync("step");
@@ -1821,6 +1825,45 @@ hcc_status hcc_batch_total_mass(hcc_ctx *c, double *out) {
                         "batch mass copy"));
     }
     return HCC_OK;
+}
+
+hcc_status hcc_update_volumes(hcc_ctx *c, int32_t sweeps) {
+    if (!c) return HCC_ERR_INVALID;
+    if (sweeps < 0) return c->fail(HCC_ERR_INVALID, "sweeps must be >= 0");
+    if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
+    const int64_t n = c->n;
+    if (n == 0) return HCC_OK;
+    const double w0 = 1.0;     // ExponentialWeightFunction at zero distance: 1 / (1 + 0)
+    double *S = nullptr, *Vt = nullptr, *part = nullptr;
+    const unsigned nb = shepard_blocks(n);
+    hcc_status st = c->alloc(S, size_t(n), "Shepard sums");
+    if (st == HCC_OK) st = c->alloc(Vt, size_t(n), "Shepard sweep");
+    if (st == HCC_OK) st = c->alloc(part, size_t(nb), "Shepard partials");
+    if (st == HCC_OK) {
+        launch_shepard(c->cnt, c->nidx, c->w64, n, c->npad, w0, sweeps, S, c->vol, Vt, part, c->stream);
+        std::vector<double> hp(nb);
+        st = c->cuda(cudaMemcpyAsync(hp.data(), part, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                     "Shepard partials");
+        if (st == HCC_OK) st = c->sync("Shepard volumes");
+        if (st == HCC_OK) {
+            double sum = 0.0;
+            for (double v : hp) sum = sum + v;
+            double box = 1.0;
+            for (int d = 0; d < c->D; ++d) box = box * (c->cfg.domain_max[d] - c->cfg.domain_min[d]);
+            launch_scale(c->vol, n, box / sum, c->stream);
+            st = c->sync("Shepard scale");
+        }
+    }
+    dfree(S);
+    dfree(Vt);
+    dfree(part);
+    return st;
+}
+
+hcc_status hcc_download_volumes(hcc_ctx *c, double *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (!c->have_cloud) return c->fail(HCC_ERR_STATE, "no cloud");
+    return c->cuda(cudaMemcpy(out, c->vol, size_t(c->n) * sizeof(double), cudaMemcpyDeviceToHost), "volumes");
 }
 
 hcc_status hcc_set_predictor(hcc_ctx *c, hcc_mlp *mlp, double thr) {

@@ -418,6 +418,10 @@ void launch_count_inadmissible(const uint8_t *inadm, const uint8_t *bnd, int64_t
 void launch_grad_weights(int64_t n, int64_t npad, int D, int kmax, const int32_t *cnt, const double *dist,
                          const double *w, const double *inv_r, const uint8_t *ok_r, double invL, float *gw,
                          cudaStream_t s);
+void launch_shepard(const int32_t *cnt, const int32_t *nidx, const double *w, int64_t n, int64_t npad, double w0,
+                    int sweeps, double *S, double *V, double *Vt, double *partial, cudaStream_t s);
+void launch_scale(double *V, int64_t n, double f, cudaStream_t s);
+unsigned shepard_blocks(int64_t n);
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out,
                        cudaStream_t s);
 // Statistics of the MOOD fixed points of one step (device; zeroed at the start of the step).

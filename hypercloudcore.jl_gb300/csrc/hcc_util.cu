@@ -357,6 +357,66 @@ void launch_grad_weights(int64_t n, int64_t npad, int D, int kmax, const int32_t
                          cudaStream_t s) {
     if (n > 0) k_grad_weights<<<grid_for(n), HCC_BLOCK, 0, s>>>(n, npad, D, kmax, cnt, dist, w, inv_r, ok_r, invL, gw);
 }
+// ShepardVolumes (Volumes.jl:183-229): kernel sums and the 1/S start, the partition-of-unity sweeps, and the
+// clamped volumes' block partial sums for the renormalisation.
+__global__ void k_shepard_sums(const int32_t *cnt, const double *w, int64_t n, int64_t npad, double w0, double *S,
+                               double *V) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sm = w0;
+    const int c = cnt[i];
+    for (int k = 0; k < c; ++k) sm = sm + w[int64_t(k) * npad + i];
+    S[i] = sm;
+    V[i] = 1.0 / sm;
+}
+__global__ void k_shepard_sweep(const int32_t *cnt, const int32_t *nidx, const double *w, int64_t n, int64_t npad,
+                                double w0, const double *S, const double *V, double *Vt) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = (w0 / S[i]) * V[i];
+    const int c = cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int64_t j = nidx[int64_t(k) * npad + i];
+        acc = acc + (w[int64_t(k) * npad + i] / S[j]) * V[j];
+    }
+    Vt[i] = acc;
+}
+__global__ void k_clamp_partials(double *V, int64_t n, double *partial) {
+    __shared__ double sh[HCC_BLOCK];
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        v = V[i] > 0.0 ? V[i] : 0.0;
+        V[i] = v;
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (int(threadIdx.x) < o) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+__global__ void k_scale(double *V, int64_t n, double f) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) V[i] = V[i] * f;
+}
+
+void launch_shepard(const int32_t *cnt, const int32_t *nidx, const double *w, int64_t n, int64_t npad, double w0,
+                    int sweeps, double *S, double *V, double *Vt, double *partial, cudaStream_t s) {
+    if (n <= 0) return;
+    k_shepard_sums<<<grid_for(n), HCC_BLOCK, 0, s>>>(cnt, w, n, npad, w0, S, V);
+    for (int q = 0; q < sweeps; ++q) {
+        k_shepard_sweep<<<grid_for(n), HCC_BLOCK, 0, s>>>(cnt, nidx, w, n, npad, w0, S, V, Vt);
+        cudaMemcpyAsync(V, Vt, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    }
+    k_clamp_partials<<<grid_for(n), HCC_BLOCK, 0, s>>>(V, n, partial);
+}
+void launch_scale(double *V, int64_t n, double f, cudaStream_t s) {
+    if (n > 0) k_scale<<<grid_for(n), HCC_BLOCK, 0, s>>>(V, n, f);
+}
+unsigned shepard_blocks(int64_t n) { return grid_for(n); }
+
 void launch_total_mass(const void *U, const double *vol, int64_t n, int M, int is_f32, double *out, cudaStream_t s) {
     cudaMemsetAsync(out, 0, sizeof(double) * M, s);
     if (n <= 0) return;

@@ -79,17 +79,20 @@ _criterion(::NoMOOD) = (Int32(0), 0.0)
 struct HccMover
     kind::Int32; full_search_per_stage::Int32; alpha::Float64
     velocity::NTuple{3, Float64}; omega::NTuple{3, Float64}; center::NTuple{3, Float64}
+    keep_volumes::Int32; shepard_sweeps::Int32          # volume_estimator: ShepardVolumes(sweeps) or nothing
 end
 struct RigidMotion
     velocity::NTuple{3, Float64}; omega::NTuple{3, Float64}; center::NTuple{3, Float64}
 end
-function _set_mover(h, mv; full_search_per_stage::Bool = false)
+function _set_mover(h, mv; full_search_per_stage::Bool = false, volume_estimator = ShepardVolumes())
     z = (0.0, 0.0, 0.0)
-    m = mv isa LagrangianMover ? HccMover(1, full_search_per_stage, 1.0, z, z, z) :
-        mv isa ScaledLagrangianMover ? HccMover(2, full_search_per_stage, Float64(mv.alpha), z, z, z) :
+    kv = volume_estimator === nothing ? Int32(1) : Int32(0)
+    sw = volume_estimator === nothing ? Int32(1) : Int32(volume_estimator.sweeps)
+    m = mv isa LagrangianMover ? HccMover(1, full_search_per_stage, 1.0, z, z, z, kv, sw) :
+        mv isa ScaledLagrangianMover ? HccMover(2, full_search_per_stage, Float64(mv.alpha), z, z, z, kv, sw) :
         mv isa PrescribedMover && mv.velocity isa RigidMotion ?
-            HccMover(3, full_search_per_stage, 1.0, mv.velocity.velocity, mv.velocity.omega, mv.velocity.center) :
-        mv isa NoGridMover ? HccMover(0, 0, 1.0, z, z, z) : error("unsupported mover $(typeof(mv))")
+            HccMover(3, full_search_per_stage, 1.0, mv.velocity.velocity, mv.velocity.omega, mv.velocity.center, kv, sw) :
+        mv isa NoGridMover ? HccMover(0, 0, 1.0, z, z, z, kv, sw) : error("unsupported mover $(typeof(mv))")
     _check(ccall((:hcc_set_mover, libhcc), Cint, (Ptr{Cvoid}, Ref{HccMover}), h, m), h, "hcc_set_mover")
 end
 

@@ -238,6 +238,8 @@ typedef struct {
     double velocity[HCC_MAX_DIM];      /* prescribed translation */
     double omega[HCC_MAX_DIM];         /* prescribed angular velocity */
     double center[HCC_MAX_DIM];        /* centre of the prescribed rotation */
+    int32_t keep_volumes;              /* 1: volume_estimator = nothing; 0 (default): ShepardVolumes after each step */
+    int32_t shepard_sweeps;            /* sweeps of ShepardVolumes (0 -> 1, the reference's default) */
 } hcc_mover;
 
 /* Select the grid mover of the context (default HCC_MOVER_NONE); before hcc_step. */
@@ -267,6 +269,13 @@ hcc_status hcc_download_orders(hcc_ctx *ctx, int32_t *orders);
 hcc_status hcc_download_mood_flags(hcc_ctx *ctx, uint8_t *flags);
 
 hcc_status hcc_get_counters(hcc_ctx *ctx, hcc_counters *out);
+
+/* update_volumes!(pg, ShepardVolumes(sweeps)) (Volumes.jl:183-240): S_i = w(0) + sum_j w_ij, V_i = 1 / S_i,
+   `sweeps` partition-of-unity sweeps V_i <- (w(0)/S_i) V_i + sum_j (w_ij / S_j) V_j, negatives clamped to 0 and
+   sum V rescaled to the box volume prod(domain_max - domain_min). Moving grids run it after every step unless the
+   mover keeps the volumes. hcc_download_volumes: the current V (N). */
+hcc_status hcc_update_volumes(hcc_ctx *ctx, int32_t sweeps);
+hcc_status hcc_download_volumes(hcc_ctx *ctx, double *volumes);
 
 /* total_mass(pg) (Volumes.jl:103-107) accumulated in FP64 on the device: out[M]. */
 hcc_status hcc_total_mass(hcc_ctx *ctx, double *out);

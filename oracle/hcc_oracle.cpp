@@ -1946,9 +1946,46 @@ struct Solver {
             // final positions, full search with periodic re-wrap for the next step (TimeSteppers.jl:571-575)
             pos = x_cand;
             if (!build_neighbours() || !prepare_geometry()) return false;
+            // ts.volume_estimator (TimeSteppers.jl:574): ShepardVolumes(sweeps) unless the volumes are kept
+            if (!mover.keep_volumes) update_volumes(mover.shepard_sweeps > 0 ? mover.shepard_sweeps : 1);
         }
         ++steps;
         return true;
+    }
+
+    // update_volumes!(pg, ShepardVolumes(sweeps)) (Volumes.jl:183-229): S_i = w(0) + sum_j w_ij, V_i = 1/S_i, then
+    // sweeps V_i <- (w(0)/S_i) V_i + sum_j (w_ij/S_j) V_j, negatives clamped and sum V rescaled to the box volume.
+    void update_volumes(int sweeps) {
+        if (N == 0) return;
+        const double w0 = weight(0.0);
+        std::vector<double> S(N), Vt(N);
+        vol.assign(N, 0.0);
+        for (int64_t i = 0; i < N; ++i) {
+            double sm = w0;
+            for (int64_t q = start[i]; q < start[i + 1]; ++q) sm = sm + nw[q];
+            S[i] = sm;
+            vol[i] = 1.0 / sm;
+        }
+        for (int it = 0; it < sweeps; ++it) {
+            for (int64_t i = 0; i < N; ++i) {
+                double acc = (w0 / S[i]) * vol[i];
+                for (int64_t q = start[i]; q < start[i + 1]; ++q) {
+                    const int64_t j = nidx[q];
+                    acc = acc + (nw[q] / S[j]) * vol[j];
+                }
+                Vt[i] = acc;
+            }
+            vol = Vt;
+        }
+        double sum = 0.0;
+        for (int64_t i = 0; i < N; ++i) {
+            if (!(vol[i] > 0.0)) vol[i] = 0.0;
+            sum = sum + vol[i];
+        }
+        double box = 1.0;
+        for (int d = 0; d < D; ++d) box = box * (cfg.domain_max[d] - cfg.domain_min[d]);
+        const double f = box / sum;
+        for (int64_t i = 0; i < N; ++i) vol[i] = vol[i] * f;
     }
 
     // get_time_step (ParticleGrids.jl:386-450) with the cached slot weights
@@ -2294,6 +2331,17 @@ hcc_status orc_total_mass(orc_ctx *ctx, double *out) {
     for (int m = 0; m < s.M; ++m) out[m] = 0.0;
     for (int64_t i = 0; i < s.N; ++i)
         for (int m = 0; m < s.M; ++m) out[m] += s.vol[i] * s.rhos[i * s.M + m];
+    return HCC_OK;
+}
+hcc_status orc_update_volumes(orc_ctx *ctx, int32_t sweeps) {
+    if (!ctx || sweeps < 0) return HCC_ERR_INVALID;
+    if (!ctx->s.have_nb) return HCC_ERR_STATE;
+    ctx->s.update_volumes(sweeps);
+    return HCC_OK;
+}
+hcc_status orc_download_volumes(orc_ctx *ctx, double *out) {
+    if (!ctx || !out) return HCC_ERR_INVALID;
+    std::memcpy(out, ctx->s.vol.data(), ctx->s.vol.size() * sizeof(double));
     return HCC_OK;
 }
 hcc_status orc_set_streamed(orc_ctx *ctx, int streamed) {

@@ -85,6 +85,9 @@ hcc_status orc_detect_and_drop(orc_ctx *ctx, const double *prev, const double *c
    include/hcc.h), and the particles the next orc_step pre-lowers by one order (NULL: none). */
 hcc_status orc_features(orc_ctx *ctx, float *out);
 hcc_status orc_set_prelowered(orc_ctx *ctx, const uint8_t *mask);
+/* update_volumes!(pg, ShepardVolumes(sweeps)) (Volumes.jl:183-229) and the current volumes (N). */
+hcc_status orc_update_volumes(orc_ctx *ctx, int32_t sweeps);
+hcc_status orc_download_volumes(orc_ctx *ctx, double *volumes);
 /* Grid mover of the context (GridMovers.jl). */
 hcc_status orc_set_mover(orc_ctx *ctx, const hcc_mover *mover);
 /* The MOOD criterion of particle p (MOOD.jl:175-271) for hand-set stage states (N*M), gradients (N*Br*M), orders

@@ -78,6 +78,8 @@ def load(abi) -> C.CDLL:
         ("orc_criterion_flags", C.c_int, [P, C.c_int64, dp, dp, ip, dp, ip]),
         ("orc_set_mover", C.c_int, [P, C.POINTER(abi.HccMover)]),
         ("orc_features", C.c_int, [P, C.POINTER(C.c_float)]),
+        ("orc_update_volumes", C.c_int, [P, C.c_int32]),
+        ("orc_download_volumes", C.c_int, [P, dp]),
         ("orc_set_prelowered", C.c_int, [P, up]),
     ]
     for name, res, args in protos:
@@ -274,6 +276,14 @@ class OracleContext:
                                                  _p(o, C.c_int32), _p(c, C.c_double), C.byref(f)),
                     "orc_criterion_flags")
         return bool(f.value)
+
+    def update_volumes(self, sweeps=1):
+        self._check(self.lib.orc_update_volumes(self._h, int(sweeps)), "orc_update_volumes")
+
+    def volumes(self):
+        out = np.zeros(self.n, dtype=np.float64)
+        self._check(self.lib.orc_download_volumes(self._h, _p(out, C.c_double)), "orc_download_volumes")
+        return out
 
     def features(self):
         """Stencil features of the learned troubled-point predictor (N x 24, FP32) of the current state."""

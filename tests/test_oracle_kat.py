@@ -959,3 +959,30 @@ def test_moment_correction_is_ignored_above_order_one(hcc, oracle, abi):
         o.upload_state(u.copy())
         out.append(o.compute_rhs())
     assert np.array_equal(out[0], out[1])
+
+
+# ----------------------------------------------------------------------------------------------- ShepardVolumes
+def test_shepard_volumes_exact_on_a_uniform_periodic_lattice(hcc, oracle, abi):
+    """Volumes.jl:36-50: ShepardVolumes is exact (V_i = dx^D) on a uniform periodic lattice, for any sweeps."""
+    for D, n in ((1, 40), (2, 20)):
+        h = 1.0 / n
+        cl = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=True)
+        o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(tuple((1.0,) for _ in range(D))))
+        for sweeps in (0, 1, 3):
+            o.update_volumes(sweeps)
+            np.testing.assert_allclose(o.volumes(), h ** D, rtol=1e-13)
+
+
+def test_shepard_volumes_partition_the_box(hcc, oracle, abi):
+    """On a jittered bounded box: positive volumes summing to the box volume, the same for every sweep count, and
+    close to dx^D inside (the partition-of-unity sweeps smooth the kernel-density estimate)."""
+    h = 1 / 24
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.3 * h, seed=8)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(((1.0,), (1.0,))))
+    inner = (np.abs(cl.pos - 0.5) < 0.35).all(axis=1)
+    for sweeps in (0, 1, 2):
+        o.update_volumes(sweeps)
+        V = o.volumes()
+        assert np.all(V >= 0.0)
+        assert V.sum() == pytest.approx(1.0, rel=1e-13)
+        assert np.abs(V[inner] / h ** 2 - 1.0).max() < 0.5
