@@ -223,6 +223,10 @@ struct hcc_ctx {
     uint8_t *pred = nullptr;
     uint4 *pred_rows = nullptr;       // compact list of the rows that passed the smoothness gate
     int32_t *pred_idx = nullptr;
+    uint32_t *rough = nullptr;        // per tile: particles whose stencil was not flat at the last step's end
+    void reset_rough() {
+        if (rough) cudaMemset(rough, 0xff, size_t(npad / 32) * sizeof(uint32_t));
+    }
     int64_t predicted = 0;
     bool feat_valid = false;
     // moving grid: mover, start-of-step / stage / final positions and the stage grid velocities (SoA FP64)
@@ -331,6 +335,7 @@ struct hcc_ctx {
         dfree(orders); dfree(nbmin); dfree(trig_step); dfree(inadm);
         dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
         dfree(ftiles); dfree(fmask); dfree(forced); dfree(feat); dfree(pred); dfree(pred_rows); dfree(pred_idx);
+        dfree(rough);
         feat_valid = false;
     }
     void free_slots() {
@@ -493,6 +498,8 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
         a.KI[q] = static_cast<const T *>(c->KI[q]);
     }
     const StageCoeffs<T> *coef = static_cast<const StageCoeffs<T> *>(c->coef_dev);
+    // with a predictor, the final stage's full flux pass marks the tiles the next step's feature pass must visit
+    if (c->mlp && s == S - 1 && !c->no_recon()) a.rough_words = c->rough;
     if (c->moving()) {
         a.mover = c->mover.kind;
         a.mv_alpha = T(c->mover.alpha);
@@ -674,6 +681,8 @@ hcc_status ensure_learn_buffers(hcc_ctx *c) {
         if (st == HCC_OK) st = c->cuda(cudaMemset(c->pred, 0, size_t(c->n)), "predicted mask");
         if (st == HCC_OK) st = c->alloc(c->pred_rows, size_t(c->n) * 4, "predictor rows");
         if (st == HCC_OK) st = c->alloc(c->pred_idx, size_t(c->n), "predictor rows");
+        if (st == HCC_OK) st = c->alloc(c->rough, size_t(c->npad / 32), "predictor tiles");
+        if (st == HCC_OK) c->reset_rough();
     }
     return st;
 }
@@ -699,6 +708,7 @@ int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
             po.row_idx = c->pred_idx;
             po.nrows = &c->mood_stats->pred_rows;
             po.cap = c->n;
+            po.rough = c->rough;
             const bool prof = c->prof && st == c->stream;
             if (prof) c->prof_begin(3);
             if (launch_predict(fa, mlp_weights(c->mlp), po, c->capture_feat ? c->feat : nullptr,
@@ -1430,6 +1440,7 @@ hcc_status hcc_load_snapshot(hcc_ctx *c, const char *path) {
     HCC_TRY(c->cuda(cudaMemcpy(c->trig_step, flags.data(), n, cudaMemcpyHostToDevice), "flags"));
     c->steps = h.steps;
     c->have_state = true;
+    c->reset_rough();
     return HCC_OK;
 }
 
@@ -1601,6 +1612,7 @@ static hcc_status upload_state_impl(hcc_ctx *c, const void *U, int src_f32) {
     }
     HCC_TRY(c->sync("upload state"));
     c->have_state = true;
+    c->reset_rough();            // a new state: the predictor visits every tile in the next step
     return HCC_OK;
 }
 
@@ -1873,6 +1885,7 @@ hcc_status hcc_set_predictor(hcc_ctx *c, hcc_mlp *mlp, double thr) {
     c->drop_graphs();
     c->mlp = mlp;
     c->thr_logit = mlp ? float(std::log(thr / (1.0 - thr))) : 0.f;
+    c->reset_rough();
     return HCC_OK;
 }
 

@@ -230,6 +230,8 @@ template <typename T> struct StageArgs {
     T *KInext;
     int implicit_mode;                // 0 none, 1 implicit solve (a_ii != 0), 2 explicit source evaluation
     int check;                        // run the MOOD check of the candidate
+    uint32_t *rough_words;            // last stage with a predictor: per tile, the particles whose stencil range of
+                                      // the stage state is not flat (the next step's feature pass skips the rest)
     int check_substep;                // 1: W = Y_s + h_sub (K + KI_s), 0: the candidate itself
     const T *KIs;                     // K_I[s] for the substep of implicit-source tableaus
     T delta;
@@ -485,6 +487,7 @@ struct PredictOut {
     float *logits;                    // [n] or nullptr
     unsigned long long *count;        // predicted particles (accumulated)
     float thr_logit;
+    const uint32_t *rough;            // [tiles] from the last step's final flux pass (nullptr: every particle)
     uint4 *rows;                      // [cap * 4] (nullptr: features only)
     int32_t *row_idx;                 // [cap]
     unsigned long long *nrows;        // rows appended (zeroed before the pass)

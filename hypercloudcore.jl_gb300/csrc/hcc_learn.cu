@@ -419,9 +419,12 @@ __global__ void __launch_bounds__(128, 7) k_features_gate(FeatArgs a, PredictOut
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     bool take = false;
     uint4 seg[KF / 8];
+    // the last step's final flux pass marked the particles whose stencil was not flat; the others are below the
+    // smoothness gate already (a whole warp skips a flat tile)
+    const bool flat = !raw && o.rough && i < a.n && !((o.rough[i >> 5] >> (i & 31)) & 1u);
     if (i < a.n) {
         if (o.pred) o.pred[i] = 0;
-        if (raw || !a.bnd[i]) {
+        if (!flat && (raw || !a.bnd[i])) {
             float f[NF];
             point_features<T, D, M, PDE>(a, i, f);
             if (raw) {

@@ -887,7 +887,7 @@ template <typename T, int M> struct FluxPart {
 // with KSTEP > 1 (FP32) the partial sums and extrema go to `part` for the caller to combine.
 template <typename T, int D, int M, int PDE, int RDEG, bool ALE, int KSTEP = 1, bool MOM = false>
 __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i, const int k0 = 0,
-                                         FluxPart<T, M> *part = nullptr) {
+                                         FluxPart<T, M> *part = nullptr, bool *rough = nullptr) {
     constexpr int BR = RBasis<D, RDEG>::B;
     if (a.g.bnd[i]) {
         if (a.full) {
@@ -1108,6 +1108,13 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
     T Kv[M];
 #pragma unroll
     for (int m = 0; m < M; ++m) Kv[m] = kFast ? -acc.s[m] : -(T(2) * acc.s[m]);
+    if (rough) {
+        // the stencil of the stage state is not flat in some component (without the extrema: assume not flat)
+        bool r = !need_ext;
+#pragma unroll
+        for (int m = 0; m < M; ++m) r = r || (mx[m] - mn[m]) > T(1e-6) * (fabs(mx[m]) + fabs(mn[m]));
+        *rough = r;
+    }
     return stage_epilogue<T, D, M, PDE, RDEG>(a, i, fi, Kv, mn, mx);
 }
 
@@ -1127,8 +1134,15 @@ __global__ void __launch_bounds__(HCC_FLUX_BLOCK, flux_min_blocks<T, D, M>()) k_
     const int lane = int(threadIdx.x & 31);
     if (a.full) {
         const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG, ALE, 1, MOM>(a, i) : false;
+        bool rough = false;
+        const bool f = (i < a.g.n) ? flux_one<T, D, M, PDE, RDEG, ALE, 1, MOM>(a, i, 0, nullptr,
+                                                                               a.rough_words ? &rough : nullptr)
+                                   : false;
         if (a.check) tile_failures(a, i >> 5, f);
+        if (a.rough_words) {
+            const unsigned b = __ballot_sync(0xffffffffu, rough);
+            if (lane == 0 && (i >> 5) * 32 < a.g.n) a.rough_words[i >> 5] = b;
+        }
         return;
     }
     const unsigned nt = *a.wcount;
