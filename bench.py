@@ -380,8 +380,8 @@ def run_ensemble(hcc, args, world, local):
     [4k, 256k] (seeded), one spacing h = 1/256, jittered lattices with transmissive walls. Even clouds: Euler
     (gamma 1.4) from random Voronoi states (2-6 regions, rho, p ~ U[0.1, 2], u, v ~ U[-1, 1]) with MUSCL2 + MOOD,
     SSP-RK3. Odd clouds: BGK-type discrete-velocity relaxation, 16 velocities on the unit ring, epsilon 1e-4, one
-    macro moment advected with (1, 0.5), implicit source by IMEX ARS(2,2,2), from smooth random Fourier densities.
-    FP32 bulk. One context per system holds its whole batch (hcc_upload_batch: one cell list, one captured step
+    macro moment advected with (1, 0.5), implicit source by IMEX ARS(2,2,2), from the Maxwellian of smooth random
+    Fourier densities (the local relaxation initialisation of test/kinetic_source.jl:110-131). FP32 bulk. One context per system holds its whole batch (hcc_upload_batch: one cell list, one captured step
     graph per step), one dt per batch (its minimum CFL step)."""
     learned = sys.modules["hcc_gb300.learned"]
     rng = np.random.default_rng(2026)
@@ -390,6 +390,8 @@ def run_ensemble(hcc, args, world, local):
     sides = np.maximum(8, np.rint(np.sqrt(target)).astype(int) - 1)
     h = 1.0 / 256
     t0 = time.time()
+    ring = [(float(np.cos(2 * np.pi * q / 16)), float(np.sin(2 * np.pi * q / 16))) for q in range(16)]
+    bgk = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
     groups = {"euler": [], "bgk": []}
     states = {"euler": [], "bgk": []}
     for k in range(nc):
@@ -406,8 +408,7 @@ def run_ensemble(hcc, args, world, local):
                 kx, ky = r.integers(1, 4, 2)
                 rho += 0.1 * r.uniform(0.5, 1.0) * np.sin(2 * np.pi * (kx * xl[:, 0] + ky * xl[:, 1]) + r.uniform(0, 6.3))
             groups["bgk"].append(cl)
-            states["bgk"].append(np.repeat((rho / 16.0)[:, None], 16, axis=1))
-    ring = [(float(np.cos(2 * np.pi * q / 16)), float(np.sin(2 * np.pi * q / 16))) for q in range(16)]
+            states["bgk"].append(bgk.maxwellian(rho))
     out = {"workload": f"ensemble_{nc}_clouds_2d", "clouds": nc, "setup": {}}
     totals = {}
     for name in ("euler", "bgk"):
@@ -419,8 +420,7 @@ def run_ensemble(hcc, args, world, local):
                                   bc_map=bc, precision="fp32")
             stages = 3
         else:
-            pde = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
-            cfg = hcc.make_config(pde, cl0, scheme=hcc.MUSCL(2, 2), mood=mood, tableau="IMEX_ARS222",
+            cfg = hcc.make_config(bgk, cl0, scheme=hcc.MUSCL(2, 2), mood=mood, tableau="IMEX_ARS222",
                                   bc_map=bc, precision="fp32")
             stages = 3          # ARS(2,2,2): three stages (ButcherTableaus.jl:218-229)
         ctx = hcc.Context(cfg)

@@ -107,6 +107,24 @@ class KineticRelaxation:
     def n_vars(self) -> int:
         return len(self.speeds)
 
+    def maxwellian(self, u) -> np.ndarray:
+        """Kinetic state at equilibrium with macro moments `u` (shape (N,)): f_k = coefficient (u + Σ_d a_d u
+        interior_factor / v_k,d), a speed component below 1e-14 contributing nothing — the local relaxation
+        initialisation set_initial_conditions! (test/kinetic_source.jl:110-131). Returns (N, n_vars) float64."""
+        u = np.asarray(u, dtype=np.float64).reshape(-1)
+        D, K = self.dim, self.n_vars
+        coeff = float(self.coefficient if self.coefficient is not None else 1.0 / K)
+        fac = float(self.interior_factor if self.interior_factor is not None else D)
+        f = np.empty((u.size, K))
+        for k in range(K):
+            fd = np.zeros_like(u)
+            for d in range(D):
+                v = float(self.speeds[k][d])
+                if abs(v) > 1e-14:
+                    fd = fd + float(self.macro_velocity[d]) * u * (fac / v)
+            f[:, k] = coeff * (u + fd)
+        return f
+
 
 @dataclass
 class MUSCL:

@@ -11,6 +11,9 @@
 #include "hcc_internal.cuh"
 
 // Launch shape of the flux pass (threads per block, minimum resident blocks per SM for the register budget).
+#ifndef HCC_FLUX_MINB_MANY
+#define HCC_FLUX_MINB_MANY 2     // FP32 flux blocks per SM for systems of 8+ components (16-velocity BGK)
+#endif
 #ifndef HCC_FLUX_BLOCK
 #define HCC_FLUX_BLOCK 128
 #endif
@@ -870,7 +873,7 @@ __device__ __forceinline__ int interface_terms(int o) {
 // (FP32 2-D scalar/Euler: 72 registers; wider states and FP64 need more).
 template <typename T, int D, int M> constexpr int flux_min_blocks() {
     if (sizeof(T) == 8) return M >= 8 ? 1 : (D * M >= 12 ? 2 : HCC_FLUX_MINB64);
-    return M >= 8 ? 2 : (D * M >= 12 ? HCC_FLUX_MINB_WIDE : HCC_FLUX_MINB);
+    return M >= 8 ? HCC_FLUX_MINB_MANY : (D * M >= 12 ? HCC_FLUX_MINB_WIDE : HCC_FLUX_MINB);
 }
 
 // The MUSCL functor (MUSCL.jl:390-508) in its streamed form: per slot, EPD interface reconstruction, physical
@@ -997,6 +1000,40 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
                     if (b >= keep_i) pi[b] = T(0);
                     if (b >= keep_j) pj[b] = T(0);
                 }
+            }
+            if constexpr (kFast && PDE != HCC_PDE_EULER && !ALE) {
+                // FP32, linear fluxes F_d(f)_m = c_dm f_m with constant speeds (advection, BGK), fixed grid: the
+                // doubled Rusanov difference per component on the fly, without flux arrays (registers:
+                // 2 (F_n - F_i)_m = sum_d w_d (c_dm (f_ij + f_ji - 2 f_i) - s_d max(λ_d) (f_ji - f_ij)))
+                T sw[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    sw[d] = (below ? wk[d] : dk[d]) > T(0) ? a.ph.amax[d] : -a.ph.amax[d];
+                T t[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    T si = gi[0][m] * pi[0];
+                    T sj = gj[m] * pj[0];
+#pragma unroll
+                    for (int b = 1; b < BR; ++b) {
+                        si = si + gi[b][m] * pi[b];
+                        sj = sj + gj[b * M + m] * pj[b];
+                    }
+                    const T fij = fi[m] + si, fji = fj[m] + sj;
+                    const T sum = (fij + fji) - T(2) * fi[m], jump = fji - fij;
+                    T tm = wk[0] * (a.ph.c[0][m] * sum - sw[0] * jump);
+#pragma unroll
+                    for (int d = 1; d < D; ++d) tm = tm + wk[d] * (a.ph.c[d][m] * sum - sw[d] * jump);
+                    t[m] = tm;
+                    if constexpr (MOM) {
+                        T se = a.ph.amax[0] * a.g.mw[(int64_t(k) * D) * np + i];
+#pragma unroll
+                        for (int d = 1; d < D; ++d) se = se + a.ph.amax[d] * a.g.mw[(int64_t(k) * D + d) * np + i];
+                        t[m] = t[m] - se * jump;
+                    }
+                }
+                acc.add(t);
+                continue;
             }
             T fij[M], fji[M];
             if constexpr (kFast) {

@@ -488,6 +488,27 @@ def test_steppers_run_and_stay_finite(hcc, oracle, abi, tab, mood):
     assert np.all((o.orders() >= 1) & (o.orders() <= 3))
 
 
+def test_maxwellian_initialisation_is_the_relaxation_fixed_point(hcc, oracle, abi):
+    """set_initial_conditions! (test/kinetic_source.jl:110-131): the kinetic state built from macro moments u
+    carries u as its moment, and a uniform one is left unchanged by an IMEX step of the oracle."""
+    ring = [(math.cos(2 * math.pi * q / 16), math.sin(2 * math.pi * q / 16)) for q in range(16)]
+    pde = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
+    u = np.linspace(0.5, 1.5, 7)
+    f = pde.maxwellian(u)
+    np.testing.assert_allclose(f.sum(axis=1), u, rtol=1e-13)
+    np.testing.assert_allclose(pde.maxwellian(f.sum(axis=1)), f, rtol=1e-12)
+    h = 1 / 16
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=1, periodic=True)
+    o = make(hcc, oracle, abi, cl, pde, scheme=hcc.MUSCL(2, 2),
+             mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), tableau="IMEX_ARS222")
+    o.prepare_geometry()
+    U0 = pde.maxwellian(np.full(cl.n, 0.8))
+    o.upload_state(U0)
+    o.step(0.0, 0.4 * o.time_step())
+    np.testing.assert_allclose(o.download_state(), U0, rtol=0, atol=1e-12)
+    assert o.mood_flags().sum() == 0
+
+
 def test_first_order_muscl_advances(hcc, oracle, abi):
     """unit_core.jl:938-945 (first half): MUSCL order 1 with forward Euler moves the solution."""
     cl = lattice_1d(hcc, 60)
