@@ -34,6 +34,7 @@ PKG = ROOT / "hypercloudcore.jl_gb300"
 METRIC = "point-updates/s per RK stage, FP32+learned vs plain FP64 on 1 GB300 at equal L1"
 STAGES = 3
 HOST_DRIVEN = False     # --host-driven: steps without the step graph (e.g. for kernel profilers)
+AUTOTUNE = True         # --no-autotune: keep the default launch shapes (hcc_autotune picks them otherwise)
 
 
 def _load(name, path, pkg_dir=None):
@@ -101,17 +102,70 @@ def make_cfg(hcc, cloud, h, precision):
 
 # --------------------------------------------------------------------------------------------- helpers
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    """SM clocks and clock-event (throttle) reasons sampled while the timed region runs: NVML through ctypes every
+    millisecond (a timed region of ten 1-ms steps still gets samples), else `nvidia-smi -lms 200`. Reads only."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
-    def __init__(self, gpu_index=0):
+    def __init__(self, gpu_index=0, period_s=0.001):
         self.gpu = gpu_index
+        self.period = period_s
         self.proc = None
         self.lines = []
+        self.samples = []           # (sm_mhz, max_mhz, reason bits) from NVML
+        self.nvml = None
+        self.stop = threading.Event()
+
+    def _open_nvml(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if lib.nvmlInit_v2() != 0:
+            return None
+        dev = C.c_void_p()
+        bus = self._pci_bus_id()
+        if bus is not None and lib.nvmlDeviceGetHandleByPciBusId_v2(C.c_char_p(bus.encode()), C.byref(dev)) == 0:
+            pass
+        elif lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.gpu), C.byref(dev)) != 0:
+            lib.nvmlShutdown()
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, dev, reasons
+
+    def _pci_bus_id(self):
+        """The CUDA device's PCI address in NVML's form (NVML numbers GPUs without CUDA_VISIBLE_DEVICES)."""
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(self.gpu)
+            return f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0"
+        except Exception:
+            return None
+
+    def _poll(self):
+        import ctypes as C
+        lib, dev, reasons = self.nvml
+        cur, mx, bits = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while True:
+            ok = lib.nvmlDeviceGetClockInfo(dev, 1, C.byref(cur)) == 0          # NVML_CLOCK_SM
+            ok = ok and lib.nvmlDeviceGetMaxClockInfo(dev, 1, C.byref(mx)) == 0
+            ok = ok and reasons(dev, C.byref(bits)) == 0
+            if ok:
+                self.samples.append((float(cur.value), float(mx.value), int(bits.value)))
+            if self.stop.wait(self.period):
+                break
 
     def __enter__(self):
+        self.nvml = self._open_nvml()
+        if self.nvml:
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -127,6 +181,10 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=2)
+            self.nvml[0].nvmlShutdown()
         if self.proc:
             self.proc.terminate()
             try:
@@ -137,6 +195,10 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], None, set()
+        for cur, m, bits in self.samples:
+            sm.append(cur)
+            mx = m
+            reasons.update(nm for nm, b in self.BITS.items() if bits & b)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -151,7 +213,7 @@ class ClockSampler:
                 if v.lower() in ("active", "1", "0x1"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvml" if self.samples else "nvidia-smi"}
 
 
 def measured_peaks():
@@ -290,6 +352,7 @@ def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_
     for _ in range(warmup):
         ctx.step(0.0, dt)
     ctx.upload_state(U_in)
+    tune = ctx.autotune(dt, steps=3) if AUTOTUNE else None
     with ClockSampler(local) as clk:
         ms, launches = time_device_steps(hcc, ctx, dt, steps, world)
     cnt = ctx.counters()
@@ -301,7 +364,8 @@ def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_
     ctx.synchronize()
     ctx.set_profiling(False)
     kt = ctx.kernel_times(reset=True)
-    out = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt, "dt": dt}
+    out = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt, "dt": dt,
+           "tuning": tune}
     if e2e:
         out["e2e_s"], out["h2d"], out["d2h"] = time_e2e(hcc, ctx, U0, dt, steps, world, f32)
     if acc_steps:
@@ -434,6 +498,7 @@ def run_ensemble(hcc, args, world, local):
         for _ in range(2):
             ctx.step(0.0, dt)
         ctx.upload_state(U)
+        tune = ctx.autotune(dt, steps=2) if AUTOTUNE else None
         with ClockSampler(local) as clk:
             ms, launches = time_device_steps(hcc, ctx, dt, args.ensemble_steps, world)
         c = ctx.counters()
@@ -442,7 +507,7 @@ def run_ensemble(hcc, args, world, local):
         out[name] = {"clouds": len(groups[name]), "particles": union.n, "interior": n_int,
                      "ms_per_step": ms / args.ensemble_steps, "stages": stages, "dt": dt, "gpu_launches": launches,
                      "mood_iterations_last_step": c["mood_iterations"], "graph_steps": c["graph_steps"],
-                     "setup_s": time.time() - ts, "clocks": clk.summary()}
+                     "setup_s": time.time() - ts, "clocks": clk.summary(), "tuning": tune}
         ctx.close()
     units = sum(u for u, _ in totals.values())
     ms_total = sum(m for _, m in totals.values())
@@ -535,7 +600,7 @@ def run_gpu(args):
                                   "threshold": PREDICTOR_THRESHOLD} if predictor is not None else None),
                    "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
                    "l2": "inputs larger than L2 (per-slot arrays ~0.5 GB)", "parallelism": f"replicas x{world}",
-                   "dt": r["dt"]},
+                   "dt": r["dt"], "launch_shapes": r["tuning"]},
         "gpu_launches": r["launches"],
         "e2e": {"value": units / r["e2e_s"], "unit": "point-updates/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
@@ -706,11 +771,13 @@ def main():
     ap.add_argument("--no-published", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--host-driven", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    global HOST_DRIVEN
+    global HOST_DRIVEN, AUTOTUNE
     HOST_DRIVEN = args.host_driven
+    AUTOTUNE = not args.no_autotune
     if args.profile:
         run_profile_case(args)
     elif args.impl == "reference":

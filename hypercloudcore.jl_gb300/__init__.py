@@ -512,6 +512,25 @@ class Context:
         """Take each step as one captured CUDA graph (default) or drive the MOOD fixed points from the host."""
         self._check(self.lib.hcc_set_step_graphs(self._h, int(bool(enable))), "hcc_set_step_graphs")
 
+    def tuning(self) -> dict:
+        """Launch shapes of the step: flux_block, gather_block, list_blocks_per_sm, drop_blocks_per_sm."""
+        t = _abi.HccTuning()
+        self._check(self.lib.hcc_get_tuning(self._h, C.byref(t)), "hcc_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **shapes):
+        """Set some of the launch shapes (the others stay); results are bit-identical across shapes."""
+        t = _abi.HccTuning(**{**self.tuning(), **shapes})
+        self._check(self.lib.hcc_set_tuning(self._h, C.byref(t)), "hcc_set_tuning")
+
+    def autotune(self, dt: float, steps: int = 5) -> dict:
+        """Time the launch-shape candidates over `steps` steps of size dt from the current state and keep the
+        fastest (hcc_autotune); the state and counters are left as they were. Returns the report."""
+        r = _abi.HccTuneReport()
+        self._check(self.lib.hcc_autotune(self._h, float(dt), int(steps), C.byref(r)), "hcc_autotune")
+        return {"best": r.best.as_dict(), "default_ms": r.default_ms, "best_ms": r.best_ms,
+                "candidates": r.candidates, "steps": r.steps}
+
     def kernel_times(self, reset: bool = False) -> dict:
         t = _abi.HccKernelTimes()
         self._check(self.lib.hcc_get_kernel_times(self._h, C.byref(t), int(bool(reset))), "hcc_get_kernel_times")

@@ -98,6 +98,19 @@ class HccKernelTimes(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class HccTuning(C.Structure):
+    _fields_ = [("flux_block", C.c_int32), ("gather_block", C.c_int32), ("list_blocks_per_sm", C.c_int32),
+                ("drop_blocks_per_sm", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class HccTuneReport(C.Structure):
+    _fields_ = [("best", HccTuning), ("default_ms", C.c_double), ("best_ms", C.c_double),
+                ("candidates", C.c_int32), ("steps", C.c_int32)]
+
+
 P = C.c_void_p
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -139,6 +152,9 @@ PROTOTYPES = [
     ("hcc_batch_total_mass", C.c_int, [P, _dp]),
     ("hcc_update_volumes", C.c_int, [P, C.c_int32]),
     ("hcc_download_volumes", C.c_int, [P, _dp]),
+    ("hcc_get_tuning", C.c_int, [P, C.POINTER(HccTuning)]),
+    ("hcc_set_tuning", C.c_int, [P, C.POINTER(HccTuning)]),
+    ("hcc_autotune", C.c_int, [P, C.c_double, C.c_int32, C.POINTER(HccTuneReport)]),
     ("hcc_mlp_create", C.c_int, [C.POINTER(HccMlpConfig), C.POINTER(P)]),
     ("hcc_mlp_destroy", None, [P]),
     ("hcc_mlp_last_error", C.c_char_p, [P]),

@@ -213,6 +213,12 @@ struct hcc_ctx {
     int32_t *forced = nullptr;                    // StrictEPD0 order offers (0x7f7f7f7f: none)
     ListCounts *lcounts = nullptr, *h_lcounts = nullptr;
     int list_blocks = 1, drop_blocks = 1;
+    int sms = 1;                                 // SM count of the device
+    hcc_tuning tune{128, 128, 8, 2};             // launch shapes of the step (hcc_set_tuning / hcc_autotune)
+    void apply_tuning() {
+        list_blocks = std::max(1, sms) * tune.list_blocks_per_sm;
+        drop_blocks = std::max(1, sms) * tune.drop_blocks_per_sm;
+    }
     unsigned long long *u2_keys = nullptr;       // MOODu2 global range of the stage state (ordered keys)
     // learned troubled-point predictor: the attached network, its threshold (logit), the start-of-step features
     // (captured for training) and the mask of the particles it pre-lowered
@@ -424,6 +430,8 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.tcount = &c->lcounts->t;
     a.inadm = c->inadm;
     a.list_blocks = c->list_blocks;
+    a.flux_block = c->tune.flux_block;
+    a.gather_block = c->tune.gather_block;
     a.delta = T(c->cfg.mood_delta);
     a.u2_plateau = T(c->cfg.u2_plateau);
     a.u2_ratio = T(c->cfg.u2_ratio);
@@ -712,7 +720,7 @@ int enqueue_prologue(hcc_ctx *c, const void *args, cudaStream_t st) {
             const bool prof = c->prof && st == c->stream;
             if (prof) c->prof_begin(3);
             if (launch_predict(fa, mlp_weights(c->mlp), po, c->capture_feat ? c->feat : nullptr,
-                               std::max(1, c->list_blocks / 8) * 2, &c->mood_stats->tc_error, st))
+                               c->sms * 2, &c->mood_stats->tc_error, st))
                 k += 2;
             if (prof) c->prof_end();
         } else if (launch_features(fa, c->feat, st)) {
@@ -1127,8 +1135,8 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
         if ((st = c->cuda(cudaGetDevice(&dev), "device")) != HCC_OK) return st;
         if ((st = c->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) != HCC_OK)
             return st;
-        c->list_blocks = std::max(1, sms) * 8;   // worklist passes: a few resident blocks per SM, grid-stride
-        c->drop_blocks = std::max(1, sms) * 2;
+        c->sms = std::max(1, sms);
+        c->apply_tuning();   // worklist passes: a few resident blocks per SM, grid-stride
     }
     if ((st = c->cuda(cudaMallocHost(reinterpret_cast<void **>(&c->mood_stats_host), sizeof(MoodStats)),
                       "pinned MOOD statistics")) != HCC_OK) return st;
@@ -1669,6 +1677,133 @@ hcc_status hcc_step(hcc_ctx *c, double t, double dt) {
     if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
     if (c->n == 0) return HCC_OK;
     return c->f32 ? run_step<float>(c, dt) : run_step<double>(c, dt);
+}
+
+static bool tuning_ok(const hcc_tuning &t) {
+    auto blk = [](int32_t b) { return b >= 32 && b <= 128 && b % 32 == 0; };
+    return blk(t.flux_block) && blk(t.gather_block) && t.list_blocks_per_sm >= 1 && t.list_blocks_per_sm <= 32 &&
+           t.drop_blocks_per_sm >= 1 && t.drop_blocks_per_sm <= 32;
+}
+
+hcc_status hcc_get_tuning(hcc_ctx *c, hcc_tuning *out) {
+    if (!c || !out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    *out = c->tune;
+    return HCC_OK;
+}
+
+hcc_status hcc_set_tuning(hcc_ctx *c, const hcc_tuning *t) {
+    if (!c || !t) return c ? c->fail(HCC_ERR_INVALID, "null tuning") : HCC_ERR_INVALID;
+    if (!tuning_ok(*t)) return c->fail(HCC_ERR_INVALID, "tuning out of range");
+    c->tune = *t;
+    c->apply_tuning();
+    c->drop_graphs();
+    return HCC_OK;
+}
+
+hcc_status hcc_autotune(hcc_ctx *c, double dt, int32_t steps, hcc_tune_report *report) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!std::isfinite(dt) || !(dt >= 0.0)) return c->fail(HCC_ERR_NONFINITE, "dt must be finite and >= 0");
+    if (steps < 1 || steps > 1000) return c->fail(HCC_ERR_INVALID, "steps must be in [1, 1000]");
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    if (c->moving()) return c->fail(HCC_ERR_STATE, "autotune on a moving grid (its steps move the particles)");
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    hcc_status st;
+    const size_t sbytes = size_t(c->n) * c->M * (c->f32 ? 4 : 8);
+    const size_t rbytes = c->rough ? size_t(c->npad / 32) * sizeof(uint32_t) : 0;
+    // what the tuning steps overwrite: the state, last step's orders / flags, the rough-tile marks, the counters
+    char *save = nullptr;
+    if ((st = c->alloc(save, sbytes + 2 * size_t(c->n) + rbytes, "autotune snapshot")) != HCC_OK) return st;
+    char *s_orders = save + sbytes, *s_flags = s_orders + c->n, *s_rough = s_flags + c->n;
+    const int64_t k_launches = c->launches, k_iters = c->mood_iters, k_flagged = c->flagged,
+                  k_inadm = c->inadmissible, k_steps = c->steps, k_total = c->launches_total,
+                  k_graph = c->graph_steps, k_pred = c->predicted;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto restore = [&]() -> hcc_status {
+        hcc_status r = c->cuda(cudaMemcpyAsync(c->rhos, save, sbytes, cudaMemcpyDeviceToDevice, c->stream), "restore");
+        if (r == HCC_OK && rbytes)
+            r = c->cuda(cudaMemcpyAsync(c->rough, s_rough, rbytes, cudaMemcpyDeviceToDevice, c->stream), "restore");
+        return r;
+    };
+    // ms per step of tuning t: drop the graphs (their launches hold the shapes), one warm-up step (captures the
+    // graph), then `steps` timed steps, each sequence from the saved state
+    auto time_of = [&](const hcc_tuning &t, double *ms) -> hcc_status {
+        c->tune = t;
+        c->apply_tuning();
+        c->drop_graphs();
+        hcc_status r;
+        if ((r = restore()) != HCC_OK) return r;
+        if ((r = hcc_step(c, 0.0, dt)) != HCC_OK) return r;
+        if ((r = restore()) != HCC_OK) return r;
+        if ((r = c->cuda(cudaEventRecord(e0, c->stream), "event")) != HCC_OK) return r;
+        for (int q = 0; q < steps; ++q)
+            if ((r = hcc_step(c, 0.0, dt)) != HCC_OK) return r;
+        if ((r = c->cuda(cudaEventRecord(e1, c->stream), "event")) != HCC_OK) return r;
+        if ((r = c->cuda(cudaEventSynchronize(e1), "event")) != HCC_OK) return r;
+        float el = 0.f;
+        if ((r = c->cuda(cudaEventElapsedTime(&el, e0, e1), "event")) != HCC_OK) return r;
+        *ms = double(el) / steps;
+        return HCC_OK;
+    };
+    const hcc_tuning start = c->tune;
+    hcc_tuning best = start;
+    double best_ms = 0.0, default_ms = 0.0;
+    int cands = 0;
+    st = c->cuda(cudaMemcpyAsync(save, c->rhos, sbytes, cudaMemcpyDeviceToDevice, c->stream), "snapshot");
+    if (st == HCC_OK) st = c->cuda(cudaMemcpyAsync(s_orders, c->orders, c->n, cudaMemcpyDeviceToDevice, c->stream),
+                                   "snapshot");
+    if (st == HCC_OK) st = c->cuda(cudaMemcpyAsync(s_flags, c->trig_step, c->n, cudaMemcpyDeviceToDevice, c->stream),
+                                   "snapshot");
+    if (st == HCC_OK && rbytes)
+        st = c->cuda(cudaMemcpyAsync(s_rough, c->rough, rbytes, cudaMemcpyDeviceToDevice, c->stream), "snapshot");
+    if (st == HCC_OK) st = c->cuda(cudaEventCreate(&e0), "event");
+    if (st == HCC_OK) st = c->cuda(cudaEventCreate(&e1), "event");
+    if (st == HCC_OK) st = time_of(start, &default_ms);
+    if (st == HCC_OK) {
+        best_ms = default_ms;
+        cands = 1;
+        static const int32_t flux_c[] = {128, 96, 64}, gather_c[] = {128, 64}, list_c[] = {8, 4, 16, 2},
+                             drop_c[] = {2, 1, 4};
+        struct Knob { int32_t hcc_tuning::*field; const int32_t *vals; int nv; };
+        const Knob knobs[] = {{&hcc_tuning::flux_block, flux_c, 3}, {&hcc_tuning::gather_block, gather_c, 2},
+                              {&hcc_tuning::list_blocks_per_sm, list_c, 4},
+                              {&hcc_tuning::drop_blocks_per_sm, drop_c, 3}};
+        for (const Knob &kb : knobs) {
+            for (int v = 0; v < kb.nv && st == HCC_OK; ++v) {
+                if (kb.vals[v] == best.*kb.field) continue;
+                hcc_tuning t = best;
+                t.*kb.field = kb.vals[v];
+                double ms = 0.0;
+                st = time_of(t, &ms);
+                ++cands;
+                if (st == HCC_OK && ms < 0.99 * best_ms) { best = t; best_ms = ms; }
+            }
+        }
+    }
+    // put back what the timed steps overwrote, and the winner (or, after an error, the starting shapes)
+    c->tune = (st == HCC_OK) ? best : start;
+    c->apply_tuning();
+    c->drop_graphs();
+    hcc_status rs = restore();
+    if (rs == HCC_OK)
+        rs = c->cuda(cudaMemcpyAsync(c->orders, s_orders, c->n, cudaMemcpyDeviceToDevice, c->stream), "restore");
+    if (rs == HCC_OK)
+        rs = c->cuda(cudaMemcpyAsync(c->trig_step, s_flags, c->n, cudaMemcpyDeviceToDevice, c->stream), "restore");
+    if (rs == HCC_OK) rs = c->sync("autotune");
+    c->launches = k_launches; c->mood_iters = k_iters; c->flagged = k_flagged; c->inadmissible = k_inadm;
+    c->steps = k_steps; c->launches_total = k_total; c->graph_steps = k_graph; c->predicted = k_pred;
+    c->feat_valid = false;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    dfree(save);
+    if (st == HCC_OK) st = rs;
+    if (st == HCC_OK && report) {
+        report->best = best;
+        report->default_ms = default_ms;
+        report->best_ms = best_ms;
+        report->candidates = cands;
+        report->steps = steps;
+    }
+    return st;
 }
 
 hcc_status hcc_download_orders(hcc_ctx *c, int32_t *orders) {

@@ -218,6 +218,7 @@ template <typename T> struct StageArgs {
     int32_t *rtiles;                  // and its neighbours) is marked here, each tile listed once
     unsigned *rcount;
     int list_blocks;                  // grid of a worklist pass (warp-stride over the tiles)
+    int flux_block, gather_block;     // block sizes of the full flux / gather passes (multiples of 32, <= 128)
     // epilogue: next candidate (Y_{s+1} or the final state) and the MOOD check of checkpoint s+1
     int form_next;
     const T *Un;                      // start-of-step state (pg.rhos)

@@ -1670,6 +1670,8 @@ struct StageInst {
         const unsigned g = grid(n, bs);
         return a.full ? g : std::max(1u, std::min(g, unsigned(a.list_blocks)));
     }
+    // block of a full pass of the other flux-like schemes (the tuned flux block); worklist passes keep 128
+    static int fbs(const StageArgs<T> &a) { return a.full ? a.flux_block : 128; }
     static void gather(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
         if constexpr (sizeof(T) == 4 && RDEG == 1) {
@@ -1678,7 +1680,8 @@ struct StageInst {
                 return;
             }
         }
-        k_gather<T, D, M, PDE, RDEG><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+        const int bs = a.full ? a.gather_block : 128;
+        k_gather<T, D, M, PDE, RDEG><<<pass_grid(a, n, bs), bs, 0, s>>>(a);
     }
     template <bool MOM> static void flux_mom(const StageArgs<T> &a, int64_t n, cudaStream_t s) {
         if constexpr (sizeof(T) == 4) {
@@ -1689,10 +1692,11 @@ struct StageInst {
                 return;
             }
         }
+        const int bs = a.full ? a.flux_block : HCC_FLUX_BLOCK;
         if (a.mover)
-            k_flux<T, D, M, PDE, RDEG, true, MOM><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+            k_flux<T, D, M, PDE, RDEG, true, MOM><<<pass_grid(a, n, bs), bs, 0, s>>>(a);
         else
-            k_flux<T, D, M, PDE, RDEG, false, MOM><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+            k_flux<T, D, M, PDE, RDEG, false, MOM><<<pass_grid(a, n, bs), bs, 0, s>>>(a);
     }
     static void flux(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
@@ -1709,10 +1713,11 @@ struct StageInst {
                 return;
             }
         }
+        const int bs = a.full ? a.flux_block : HCC_FLUX_BLOCK;
         if (a.mover)     // moving grid: the ALE-frame instantiation (grid velocities, shifted fluxes and speeds)
-            k_flux<T, D, M, PDE, RDEG, true><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+            k_flux<T, D, M, PDE, RDEG, true><<<pass_grid(a, n, bs), bs, 0, s>>>(a);
         else
-            k_flux<T, D, M, PDE, RDEG, false><<<pass_grid(a, n, HCC_FLUX_BLOCK), HCC_FLUX_BLOCK, 0, s>>>(a);
+            k_flux<T, D, M, PDE, RDEG, false><<<pass_grid(a, n, bs), bs, 0, s>>>(a);
     }
     static void stage1(const void *args, int64_t n, cudaStream_t s) {
         k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
@@ -1723,21 +1728,21 @@ struct StageInst {
     static void weno(const void *args, int64_t n, cudaStream_t s) {
         if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
             const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
-            k_weno<T, D><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+            k_weno<T, D><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         }
     }
     static void upwind(const void *args, int64_t n, cudaStream_t s) {
         if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
             const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
             if (a.sc.upwind_alg == HCC_UPWIND_TIWARI)
-                k_upwind<T, D, HCC_UPWIND_TIWARI><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+                k_upwind<T, D, HCC_UPWIND_TIWARI><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
             else if constexpr (D == 2)
-                k_upwind<T, D, HCC_UPWIND_PRAVEEN><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+                k_upwind<T, D, HCC_UPWIND_PRAVEEN><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         }
     }
     static void central(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
-        k_central<T, D, M, PDE><<<pass_grid(a, n, 128), 128, 0, s>>>(a);
+        k_central<T, D, M, PDE><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
     }
     static const StageOps *ops() {
         static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,

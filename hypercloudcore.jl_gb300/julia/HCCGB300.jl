@@ -176,4 +176,33 @@ function HyperCloudCore.get_time_step(pg::ParticleGrid, eq::HyperbolicPDE, ts::G
     return dt[]
 end
 
+# Launch shapes of the step and the autotuner (hcc_tuning / hcc_autotune): the shapes change no result.
+struct HccTuning
+    flux_block::Int32
+    gather_block::Int32
+    list_blocks_per_sm::Int32
+    drop_blocks_per_sm::Int32
+end
+
+struct HccTuneReport
+    best::HccTuning
+    default_ms::Float64
+    best_ms::Float64
+    candidates::Int32
+    steps::Int32
+end
+
+# Times the candidates over `steps` steps of size dt from the stepper's current state and keeps the fastest.
+function autotune!(ts::GB300RKTimeStepper, dt::Real; steps::Integer = 5)
+    r = Ref{HccTuneReport}()
+    _check(ccall((:hcc_autotune, libhcc), Cint, (Ptr{Cvoid}, Cdouble, Int32, Ref{HccTuneReport}),
+                 ts.handle, dt, steps, r), ts.handle, "hcc_autotune")
+    return r[]
+end
+
+function set_tuning!(ts::GB300RKTimeStepper, t::HccTuning)
+    _check(ccall((:hcc_set_tuning, libhcc), Cint, (Ptr{Cvoid}, Ref{HccTuning}), ts.handle, t), ts.handle, "hcc_set_tuning")
+    return ts
+end
+
 end # module

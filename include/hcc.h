@@ -406,6 +406,38 @@ hcc_status hcc_set_feature_capture(hcc_ctx *ctx, int enable);
 hcc_status hcc_download_features(hcc_ctx *ctx, float *features);
 hcc_status hcc_download_predicted(hcc_ctx *ctx, uint8_t *predicted);
 
+/* Launch shapes of a step. They change no result: every particle is computed by the same code whatever the grid
+   (the results are bit-identical across shapes). No counterpart in the reference (KernelAbstractions picks its
+   workgroup size at launch). */
+typedef struct hcc_tuning {
+    int32_t flux_block;          /* threads per block of the full flux pass (and the other schemes' full passes):
+                                    32, 64, 96 or 128; default 128 */
+    int32_t gather_block;        /* threads per block of the full reconstruction pre-pass: 32..128 step 32; 128 */
+    int32_t list_blocks_per_sm;  /* grid of the MOOD worklist (recompute) passes, blocks per SM: 1..32; 8 */
+    int32_t drop_blocks_per_sm;  /* grid of the MOOD decision pass, blocks per SM: 1..32; 2 */
+} hcc_tuning;
+
+typedef struct hcc_tune_report {
+    hcc_tuning best;             /* the shapes kept (applied to the context) */
+    double default_ms;           /* ms per step with the shapes in place when the tuner started */
+    double best_ms;              /* ms per step with `best` */
+    int32_t candidates;          /* configurations timed */
+    int32_t steps;               /* timed steps per configuration (after one warm-up step) */
+} hcc_tune_report;
+
+hcc_status hcc_get_tuning(hcc_ctx *ctx, hcc_tuning *out);
+/* HCC_ERR_INVALID for a value outside the ranges above. Drops the captured step graphs. */
+hcc_status hcc_set_tuning(hcc_ctx *ctx, const hcc_tuning *tuning);
+
+/* The project's autotuner: coordinate descent over the four shapes (flux block {128, 96, 64}, gather block
+   {128, 64}, worklist blocks per SM {8, 4, 16, 2}, decision blocks per SM {2, 1, 4}), each configuration timed
+   with CUDA events over `steps` steps of size dt (the context's own step path: captured graph or host-driven)
+   from the current state after one warm-up step; a change is kept when it is at least 1 % faster. The state,
+   the step counters and the predictor's rough-tile marks are restored afterwards, so the next hcc_step computes
+   what it would have without tuning. Needs an uploaded state; HCC_ERR_STATE on a moving grid (its steps move the
+   particles). `report` may be NULL. */
+hcc_status hcc_autotune(hcc_ctx *ctx, double dt, int32_t steps, hcc_tune_report *report);
+
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);
 
