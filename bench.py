@@ -268,7 +268,8 @@ def reduce_max(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -303,14 +304,14 @@ def time_e2e(hcc, ctx, U_host, dt, steps, world, f32):
     pinned = torch.empty(U_host.shape, dtype=dtype, pin_memory=True)
     pinned.copy_(torch.from_numpy(U_host.astype(np.float32 if f32 else np.float64)))
     host = pinned.numpy()
-    out = np.empty_like(host)
+    out = torch.empty(U_host.shape, dtype=dtype, pin_memory=True).numpy()
     barrier(world)
     ctx.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         ctx.upload_state(host)
         ctx.step(0.0, dt)
-        out[...] = ctx.download_state(dtype=host.dtype)
+        ctx.download_state(out=out)
     ctx.synchronize()
     el = time.perf_counter() - t0
     barrier(world)

@@ -444,8 +444,16 @@ class Context:
             a = np.ascontiguousarray(U, dtype=np.float64)
             self._check(self.lib.hcc_upload_state(self._h, _ptr(a, C.c_double)), "hcc_upload_state")
 
-    def download_state(self, dtype=np.float64) -> np.ndarray:
-        out = np.zeros((self.n, self.M), dtype=dtype)
+    def download_state(self, dtype=np.float64, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The state (N x M) as float64 or float32; `out` (C-contiguous, that shape and dtype — e.g. a view of
+        pinned host memory) is filled in place instead of a new array."""
+        if out is None:
+            out = np.empty((self.n, self.M), dtype=dtype)
+        else:
+            dtype = out.dtype
+            if out.shape != (self.n, self.M) or dtype not in (np.float32, np.float64) or \
+                    not out.flags["C_CONTIGUOUS"] or not out.flags["WRITEABLE"]:
+                raise ValueError("out must be a writeable C-contiguous (N, M) float32/float64 array")
         if dtype == np.float32:
             self._check(self.lib.hcc_download_state_f32(self._h, _ptr(out, C.c_float)), "hcc_download_state_f32")
         else:

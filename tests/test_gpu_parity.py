@@ -777,3 +777,22 @@ def test_shepard_volumes_and_moving_mass(hcc, oracle, cuda_lib):
         assert _bits_equal(g.download_state(), o.download_state())
         np.testing.assert_allclose(g.volumes(), o.volumes(), rtol=1e-13)
         np.testing.assert_allclose(g.total_mass(), o.total_mass(), rtol=1e-12)
+
+
+def test_download_into_a_caller_buffer(hcc, cuda_lib):
+    h = 1 / 32
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=3)
+    g = hcc.Context(hcc.make_config(hcc.Euler(2, 1.4), cl, scheme=hcc.MUSCL(2, 2), bc_map=OUTFLOW, precision="fp32"))
+    g.upload_cloud(cl)
+    g.build_neighbours()
+    g.prepare_geometry()
+    g.upload_state(quadrant_ic(cl).astype(np.float32))
+    g.step(0.0, 0.3 * g.time_step())
+    for dt in (np.float32, np.float64):
+        buf = np.full((cl.n, 4), np.nan, dtype=dt)
+        assert g.download_state(out=buf) is buf
+        np.testing.assert_array_equal(buf, g.download_state(dtype=dt))
+    with pytest.raises(ValueError):
+        g.download_state(out=np.zeros((cl.n, 3), dtype=np.float32))
+    with pytest.raises(ValueError):
+        g.download_state(out=np.zeros((4, cl.n), dtype=np.float64).T)
