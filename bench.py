@@ -135,7 +135,10 @@ class ClockSampler:
             lib.nvmlShutdown()
             return None
         reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
-            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        if reasons is None:
+            lib.nvmlShutdown()
+            return None
         return lib, dev, reasons
 
     def _pci_bus_id(self):
