@@ -608,18 +608,18 @@ __global__ void __launch_bounds__(128) k_gather_tiles(const StageArgs<T> a) {
         __syncthreads();
         const int gp = path[lane];
         {
-            // warp-uniform slot loop (the reach marks are combined across the warp)
+            // warp-uniform slot loop over every live member (the reach marks, combined across the warp); the
+            // cached-fit members also accumulate their gradients here
             const int myc = (live && gp) ? cnt : 0;
-            const int kw = __reduce_max_sync(0xffffffffu, myc);
+            const int myr = (live && a.rmask) ? cnt : myc;
+            const int kw = __reduce_max_sync(0xffffffffu, myr);
             T fi[M], out[BR * M];
             if (myc > 0) load_vec<T, M>(a.U + i * M, fi);
 #pragma unroll
             for (int b = 0; b < BR * M; ++b) out[b] = T(0);
             for (int k = w; k < kw; k += 4) {
-                const bool on = k < myc;
-                int32_t j = -1;
-                if (on) {
-                    j = a.g.nidx[int64_t(k) * np + i];
+                const int32_t j = k < myr ? a.g.nidx[int64_t(k) * np + i] : -1;
+                if (k < myc) {
                     T gk[D], df[M];
 #pragma unroll
                     for (int d = 0; d < D; ++d) gk[d] = a.g.gw[(int64_t(k) * D + d) * np + i];
@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(128) k_gather_tiles(const StageArgs<T> a) {
                 for (int b = 0; b < BR * M; ++b) parts[w][lane][b] = out[b];
         }
         __syncthreads();
-        if (w == 0 && a.rmask) reach_mark_warp(a.rmask, a.rtiles, a.rcount, (live && gp) ? int32_t(i) : -1);
+        if (w == 0 && a.rmask) reach_mark_warp(a.rmask, a.rtiles, a.rcount, live ? int32_t(i) : -1);
         if (w == 0 && live) {
             if (gp) {
                 T fi[M], out[BR][M];
@@ -653,10 +653,6 @@ __global__ void __launch_bounds__(128) k_gather_tiles(const StageArgs<T> a) {
                 store_vec<T, BR * M>(a.grad + i * (BR * M), &out[0][0]);
             } else {
                 gather_one<T, D, M, PDE, RDEG>(a, i);
-                if (a.rmask) {
-                    reach_mark(a.rmask, a.rtiles, a.rcount, int32_t(i));
-                    for (int k = 0; k < cnt; ++k) reach_mark(a.rmask, a.rtiles, a.rcount, a.g.nidx[int64_t(k) * np + i]);
-                }
             }
         }
         if (threadIdx.x == 0 && a.clear_wmask) a.wmask[tile] = 0u;   // every lane read the word before the barrier
