@@ -89,6 +89,37 @@ def test_batch_union_matches_the_oracle_and_stays_independent(hcc, oracle, cuda_
         assert rel < 1e-9, (b, rel)
 
 
+def test_bgk_batch_matches_the_oracle(hcc, oracle, cuda_lib):
+    """A BGK batch (16 ring velocities, IMEX ARS(2,2,2), clouds started at the Maxwellian of their densities):
+    states and MOOD flags of the union bit for bit against the oracle, FP64."""
+    abi = sys.modules["hcc_gb300._abi"]
+    h = 1 / 48
+    clouds = _clouds(hcc, h, (20, 12))
+    ring = [(float(np.cos(2 * np.pi * q / 16)), float(np.sin(2 * np.pi * q / 16))) for q in range(16)]
+    pde = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
+    kw = dict(scheme=hcc.MUSCL(2, 2), mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), tableau="IMEX_ARS222",
+              bc_map=OUTFLOW)
+    g = hcc.Context(hcc.make_config(pde, clouds[0], **kw))
+    union = g.upload_batch(clouds)
+    g.build_neighbours()
+    g.prepare_geometry()
+    o = oracle.OracleContext(hcc.make_config(pde, union, **kw), abi)
+    o.upload_cloud(union)
+    o.build_neighbours()
+    o.prepare_geometry()
+    rho = 1.0 + 0.2 * np.sin(7.0 * union.pos[:, 0]) * np.cos(5.0 * union.pos[:, 1])
+    U0 = pde.maxwellian(rho)
+    g.upload_state(U0)
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    assert g.time_step() == o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+    assert np.array_equal(g.download_state().view(np.uint64), o.download_state().view(np.uint64))
+    np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+
+
 def test_batch_rejects_periodic_and_bad_offsets(hcc, cuda_lib):
     h = 1 / 32
     per = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True)

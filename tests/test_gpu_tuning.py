@@ -122,3 +122,42 @@ def test_autotune_refuses_a_moving_grid(hcc, cuda_lib):
     g.set_mover(hcc.mover("lagrangian"))
     with pytest.raises(hcc.HCCError):
         g.autotune(1e-4, steps=1)
+
+
+def test_autotune_with_the_predictor_keeps_the_next_steps(hcc, cuda_lib):
+    """With the shipped predictor attached the tuner also puts back the rough-tile marks that steer the next
+    step's feature pass: three steps after tuning equal three steps of an untuned context bit for bit."""
+    import sys
+    L = sys.modules["hcc_gb300.learned"]
+    pred = hcc.TroubledPointPredictor(capacity=16)
+    pred.load(L.default_weights_path())
+    h = 1 / 128
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=42)
+    U0 = L.voronoi_state(cl.pos, 77).astype(np.float32)
+
+    def ctx():
+        cfg = hcc.make_config(hcc.Euler(2, 1.4), cl, scheme=hcc.MUSCL(2, 2),
+                              mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), bc_map=OUTFLOW, precision="fp32")
+        g = hcc.Context(cfg)
+        g.upload_cloud(cl)
+        g.build_neighbours()
+        g.prepare_geometry()
+        g.set_predictor(pred, 0.7)
+        g.upload_state(U0)
+        return g
+
+    g, r = ctx(), ctx()
+    dt = 0.4 * g.time_step()
+    for c in (g, r):
+        c.step(0.0, dt)                  # leaves rough-tile marks behind
+    g.autotune(dt, steps=2)
+    g.set_tuning(**ODD)                  # and other shapes than the reference context's
+    pg = pr = 0
+    for k in range(3):
+        g.step((k + 1) * dt, dt)
+        r.step((k + 1) * dt, dt)
+        pg += g.counters()["predicted"]
+        pr += r.counters()["predicted"]
+    assert pr > 0 and pg == pr
+    assert np.array_equal(_bits(g.download_state()), _bits(r.download_state()))
+    np.testing.assert_array_equal(g.mood_flags(), r.mood_flags())
