@@ -678,13 +678,16 @@ __global__ void __launch_bounds__(128) k_gather(const StageArgs<T> a) {
         const uint32_t word = a.wmask[tile];
         __syncwarp();
         if (a.clear_wmask && lane == 0) a.wmask[tile] = 0u;     // the changed list is consumed here
-        if (!((word >> lane) & 1u)) continue;
+        const bool mem = (word >> lane) & 1u;
         const int32_t i = tile * 32 + lane;
-        gather_one<T, D, M, PDE, RDEG>(a, i);
+        if (mem) gather_one<T, D, M, PDE, RDEG>(a, i);
         if (a.rmask) {
-            reach_mark(a.rmask, a.rtiles, a.rcount, i);
-            const int c = a.g.cnt[i];
-            for (int k = 0; k < c; ++k) reach_mark(a.rmask, a.rtiles, a.rcount, a.g.nidx[int64_t(k) * np + i]);
+            // the reach (members and their neighbours), slot by slot across the warp with combined atomics
+            reach_mark_warp(a.rmask, a.rtiles, a.rcount, mem ? i : -1);
+            const int c = mem ? a.g.cnt[i] : 0;
+            const int kw = __reduce_max_sync(0xffffffffu, c);
+            for (int k = 0; k < kw; ++k)
+                reach_mark_warp(a.rmask, a.rtiles, a.rcount, k < c ? a.g.nidx[int64_t(k) * np + i] : -1);
         }
     }
 }

@@ -176,10 +176,12 @@ __global__ void k_reach_hop2(ListCounts *counts, int32_t *dtiles, uint32_t *dmas
     const int lane = int(threadIdx.x & 31);
     const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
     for (unsigned q = warp; q < n1; q += nwarps) {
-        if (!((words1[q] >> lane) & 1u)) continue;
+        const bool mem = (words1[q] >> lane) & 1u;
         const int64_t i = int64_t(dtiles[q]) * 32 + lane;
-        const int c = cnt[i];
-        for (int k = 0; k < c; ++k) reach_mark(dmask, dtiles, &counts->d, nidx[int64_t(k) * npad + i]);
+        const int c = mem ? cnt[i] : 0;
+        const int kw = __reduce_max_sync(0xffffffffu, c);
+        for (int k = 0; k < kw; ++k)     // slot by slot across the warp, combined atomics
+            reach_mark_warp(dmask, dtiles, &counts->d, k < c ? nidx[int64_t(k) * npad + i] : -1);
     }
 }
 
