@@ -619,6 +619,16 @@ def run_gpu(args):
     flux_ms = kt["flux_ms"] / max(kt["flux_launches"], 1)
     achieved = flux_b * n_int / (flux_ms / 1e3) / 1e9
     traffic = recorded_traffic().get("flux_f32_euler2d_bytes_per_point_stage") if D == 2 else None
+    # the reconstruction pre-pass against the same peak: model bytes, and the DRAM bytes of its ncu capture
+    gather_ms = kt["gather_ms"] / max(kt["gather_launches"], 1)
+    g_traffic = recorded_traffic().get("gather_f32_euler2d_bytes_per_point_stage") if D == 2 else None
+    g_model = gather_b * n_int / (gather_ms / 1e3) / 1e9
+    gather_roof = {"kernel": f"k_gather<float,{D},{M},EULER,1>", "bound": "hbm", "unit": "GB/s", "peak": peak,
+                   "achieved": g_model, "frac": g_model / peak,
+                   "dram_achieved": (g_traffic * n_int / (gather_ms / 1e3) / 1e9) if g_traffic else None,
+                   "dram_frac": (g_traffic * n_int / (gather_ms / 1e3) / 1e9 / peak) if g_traffic else None,
+                   "note": "achieved: model bytes / live launch time; dram_achieved: ncu DRAM bytes per point-stage "
+                           "(profiles/traffic.txt) x N_interior / live launch time"}
     line = {
         "metric": METRIC, "value": value, "unit": "point-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
@@ -643,7 +653,8 @@ def run_gpu(args):
                      "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
                      "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
                      "predict_ms_per_step": kt["predict_ms"] / max(kt["steps"], 1),
-                     "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps"},
+                     "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps",
+                     "gather": gather_roof},
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],
                  "predicted_last_step": cnt.get("predicted", 0)},
