@@ -1718,6 +1718,8 @@ hcc_status hcc_autotune(hcc_ctx *c, double dt, int32_t steps, hcc_tune_report *r
                   k_inadm = c->inadmissible, k_steps = c->steps, k_total = c->launches_total,
                   k_graph = c->graph_steps, k_pred = c->predicted;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int prof0 = c->prof;   // the tuning steps stay out of the kernel timings (and take the graph path)
+    c->prof = 0;
     auto restore = [&]() -> hcc_status {
         hcc_status r = c->cuda(cudaMemcpyAsync(c->rhos, save, sbytes, cudaMemcpyDeviceToDevice, c->stream), "restore");
         if (r == HCC_OK && rbytes)
@@ -1789,6 +1791,7 @@ hcc_status hcc_autotune(hcc_ctx *c, double dt, int32_t steps, hcc_tune_report *r
     if (rs == HCC_OK)
         rs = c->cuda(cudaMemcpyAsync(c->trig_step, s_flags, c->n, cudaMemcpyDeviceToDevice, c->stream), "restore");
     if (rs == HCC_OK) rs = c->sync("autotune");
+    c->prof = prof0;
     c->launches = k_launches; c->mood_iters = k_iters; c->flagged = k_flagged; c->inadmissible = k_inadm;
     c->steps = k_steps; c->launches_total = k_total; c->graph_steps = k_graph; c->predicted = k_pred;
     c->feat_valid = false;
