@@ -8,8 +8,12 @@ Rusanov flux; SSP-RK3; dt = 0.4 x the CFL step at the initial state. Synthetic, 
 `value` is the FP32 bulk path with the learned troubled-point predictor attached (the headline; the plain FP32
 path is `fp32_plain`), measured with the state resident in HBM; `e2e` is the same metric through the C ABI with
 host buffers (state uploaded from pinned memory and downloaded every step); `fp64_plain` is the plain FP64 path on
-the same cloud; `accuracy_vs_finer_fp64` compares the density L1 errors of the three against an FP64 run at h/2. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's
-CPU path) on a bounded sample of the same workload. `--impl reference` runs only that CPU path.
+the same cloud; `accuracy_vs_finer_fp64` compares the density L1 errors of the three against an FP64 run at h/2.
+`roofline` rates the flux pass (and, under `roofline.gather`, the reconstruction pre-pass) against the measured HBM
+copy peak. Every context is tuned by `hcc_autotune` before its timed region (`--no-autotune`: default shapes).
+`euler3d_blast_8M` and `ensemble` add the 3-D blast (with its own equal-L1 study at 1.0M) and the 512-cloud
+batched ensemble. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's CPU path) on a
+bounded sample of the same workload. `--impl reference` runs only that CPU path.
 
 Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under torch.distributed.run (one rank per GPU,
 independent replicas: the path does not shard).
