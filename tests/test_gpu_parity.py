@@ -796,3 +796,62 @@ def test_download_into_a_caller_buffer(hcc, cuda_lib):
         g.download_state(out=np.zeros((cl.n, 3), dtype=np.float32))
     with pytest.raises(ValueError):
         g.download_state(out=np.zeros((4, cl.n), dtype=np.float64).T)
+
+
+def _subset(cloud, keep):
+    c = type(cloud)(cloud.pos[keep], cloud.is_boundary[keep], cloud.tags[keep], cloud.volumes[keep], cloud.dx,
+                    cloud.radius, cloud.domain_min, cloud.domain_max, cloud.canvas_min, cloud.canvas_max,
+                    cloud.periodic)
+    return c
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_starved_and_isolated_particles(hcc, oracle, cuda_lib, precision):
+    """A hole in the cloud with one particle left at its centre (no neighbour at all) and a ragged rim of particles
+    with half-empty supports: lists, orders, flags and states against the oracle — bit for bit in FP64, within
+    1e-5 relative in FP32; the isolated particle keeps its state (no flux, no fit)."""
+    h = 1 / 40
+    full = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, jitter=0.25 * h, seed=21)
+    r = np.linalg.norm(full.pos - 0.5, axis=1)
+    centre = int(np.argmin(r))
+    keep = (r > 0.16) | (np.arange(full.n) == centre) | (full.is_boundary != 0)
+    cloud = _subset(full, keep)
+    ci = int(np.flatnonzero(np.flatnonzero(keep) == centre)[0])
+    mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h))
+    cfg = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=OUTFLOW,
+                          precision=precision)
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    counts, _ = _assert_same_lists(g, o)
+    inner = counts[cloud.is_boundary == 0]
+    assert counts[ci] == 0 and (inner < 0.75 * np.median(inner)).sum() > 10
+    U0 = quadrant_ic(cloud)
+    g.upload_state(U0.astype(np.float32) if precision == "fp32" else U0)
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    for k in range(3):
+        g.step(k * dt, dt)
+        o.step(k * dt, dt)
+    Ug, Uo = g.download_state(), o.download_state()
+    if precision == "fp64":
+        assert _bits_equal(Ug, Uo)
+        np.testing.assert_array_equal(g.orders(), o.orders())
+        np.testing.assert_array_equal(g.mood_flags(), o.mood_flags())
+    else:
+        assert np.abs(Ug - Uo).max() <= 1e-5 * np.abs(Uo).max()
+    np.testing.assert_allclose(Ug[ci], U0[ci], rtol=1e-6)
+    if precision == "fp64":
+        np.testing.assert_array_equal(Ug[ci], U0[ci])
+
+
+def test_empty_cloud_steps(hcc, cuda_lib):
+    """Zero particles: every call succeeds and the step is a no-op."""
+    h = 1 / 16
+    full = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h)
+    cloud = _subset(full, np.zeros(full.n, dtype=bool))
+    g = hcc.Context(hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), bc_map=OUTFLOW))
+    g.upload_cloud(cloud)
+    g.build_neighbours()
+    g.prepare_geometry()
+    g.upload_state(np.zeros((0, 4)))
+    g.step(0.0, 1e-3)
+    assert g.download_state().shape == (0, 4)
