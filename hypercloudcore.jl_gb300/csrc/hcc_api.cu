@@ -1707,6 +1707,10 @@ hcc_status hcc_autotune(hcc_ctx *c, double dt, int32_t steps, hcc_tune_report *r
     if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
     if (c->moving()) return c->fail(HCC_ERR_STATE, "autotune on a moving grid (its steps move the particles)");
     if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (c->n == 0) {                       // nothing to time: the shapes stay
+        if (report) *report = hcc_tune_report{c->tune, 0.0, 0.0, 0, steps};
+        return HCC_OK;
+    }
     hcc_status st;
     const size_t sbytes = size_t(c->n) * c->M * (c->f32 ? 4 : 8);
     const size_t rbytes = c->rough ? size_t(c->npad / 32) * sizeof(uint32_t) : 0;

@@ -855,3 +855,5 @@ def test_empty_cloud_steps(hcc, cuda_lib):
     g.upload_state(np.zeros((0, 4)))
     g.step(0.0, 1e-3)
     assert g.download_state().shape == (0, 4)
+    rep = g.autotune(1e-3, steps=1)
+    assert rep["candidates"] == 0 and rep["best"] == g.tuning()
