@@ -70,3 +70,36 @@ def test_upwind_is_first_order_muscl(hcc):
     a = hcc.make_config(hcc.LinearAdvection(((1.0,), (1.0,))), cl, scheme=hcc.Upwind(2))
     b = hcc.make_config(hcc.LinearAdvection(((1.0,), (1.0,))), cl, scheme=hcc.MUSCL(1, 2))
     assert bytes(a) == bytes(b)
+
+
+def test_struct_layouts_match_the_header(hcc, tmp_path):
+    """Every struct of include/hcc.h has the size and field offsets of its ctypes mirror (compiled with the host C
+    compiler against the header; no GPU)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    import sys
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    abi = sys.modules["hcc_gb300._abi"]
+    pairs = {"hcc_config": abi.HccConfig, "hcc_counters": abi.HccCounters, "hcc_mover": abi.HccMover,
+             "hcc_kernel_times": abi.HccKernelTimes, "hcc_mlp_config": abi.HccMlpConfig,
+             "hcc_tuning": abi.HccTuning, "hcc_tune_report": abi.HccTuneReport}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hcc.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = ROOT / "include"
+    subprocess.run([cc, "-std=c11", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in pairs.items():
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
