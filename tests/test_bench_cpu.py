@@ -1,0 +1,43 @@
+"""Host logic of bench.py (no GPU): the clock-sample summary and its throttle reasons, the byte model of the
+roofline, and the committed DRAM-traffic figures it reads."""
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+sys.path.insert(0, str(ROOT))
+import bench  # noqa: E402
+
+
+def test_clock_summary_from_nvml_samples():
+    s = bench.ClockSampler(0)
+    s.samples = [(2070.0, 2070.0, 0x0), (2055.0, 2070.0, 0x4), (2070.0, 2070.0, 0x0)]
+    out = s.summary()
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0 and out["samples"] == 3
+    assert out["reasons"] == ["sw_power_cap"] and out["source"] == "nvml"
+    s.samples.append((1500.0, 2070.0, 0x8 | 0x40))
+    assert s.summary()["reasons"] == ["hw_slowdown", "hw_thermal_slowdown", "sw_power_cap"]
+
+
+def test_clock_summary_from_nvidia_smi_lines():
+    s = bench.ClockSampler(0)
+    s.lines = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "0, 2040, 2070, 1200.5, 0x4, Not Active, Not Active, Active, Active",
+               "garbage"]
+    out = s.summary()
+    assert out["samples"] == 2 and out["sm_mhz"] == pytest.approx(2055.0)
+    assert out["reasons"] == ["sw_power_cap", "sw_thermal_slowdown"] and out["source"] == "nvidia-smi"
+
+
+def test_algorithmic_bytes_model():
+    # 2-D Euler FP32, MUSCL2 (Br = D) with the degree-1 divergence fit (Bd = D + 1)
+    flux, gather = bench.algorithmic_bytes(19.26, 2, 4, 2, 3, 4)
+    assert flux == pytest.approx(4 * 19.26 + 16 + 72 + 4 * 4 * 7)
+    assert gather == pytest.approx(4 * 19.26 + 16 + 32 + 4 * 4 * 3)
+
+
+def test_recorded_traffic_is_read():
+    t = bench.recorded_traffic()
+    assert t["flux_f32_euler2d_bytes_per_point_stage"] > 277.0
+    assert t["gather_f32_euler2d_bytes_per_point_stage"] > 173.0
