@@ -1679,6 +1679,14 @@ hcc_status hcc_step(hcc_ctx *c, double t, double dt) {
     return c->f32 ? run_step<float>(c, dt) : run_step<double>(c, dt);
 }
 
+#define HCC_STR2(x) #x
+#define HCC_STR(x) HCC_STR2(x)
+const char *hcc_build_info(void) {
+    return "flux_block=" HCC_STR(HCC_FLUX_BLOCK) " flux_minb=" HCC_STR(HCC_FLUX_MINB)
+           " flux_minb_wide=" HCC_STR(HCC_FLUX_MINB_WIDE) " flux_minb64=" HCC_STR(HCC_FLUX_MINB64)
+           " flux_minb_many=" HCC_STR(HCC_FLUX_MINB_MANY);
+}
+
 static bool tuning_ok(const hcc_tuning &t) {
     auto blk = [](int32_t b) { return b >= 32 && b <= 128 && b % 32 == 0; };
     return blk(t.flux_block) && blk(t.gather_block) && t.list_blocks_per_sm >= 1 && t.list_blocks_per_sm <= 32 &&

@@ -8,6 +8,24 @@
 #include <vector>
 #include "../../include/hcc.h"
 
+// Launch bounds of the stage kernels (compile-time; a variant build overrides them with -D, and
+// hcc_build_info reports the values a library was built with).
+#ifndef HCC_FLUX_MINB_MANY
+#define HCC_FLUX_MINB_MANY 2     // FP32 flux blocks per SM for systems of 8+ components (16-velocity BGK)
+#endif
+#ifndef HCC_FLUX_BLOCK
+#define HCC_FLUX_BLOCK 128
+#endif
+#ifndef HCC_FLUX_MINB
+#define HCC_FLUX_MINB 7            // FP32, D*M < 12: caps the flux kernel at 72 registers
+#endif
+#ifndef HCC_FLUX_MINB_WIDE
+#define HCC_FLUX_MINB_WIDE 4       // FP32, D*M >= 12 (3-D Euler): 128 registers
+#endif
+#ifndef HCC_FLUX_MINB64
+#define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
+#endif
+
 #define HCC_MAX_STAGES 5
 #define HCC_BLOCK 256
 

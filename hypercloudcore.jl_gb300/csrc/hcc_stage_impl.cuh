@@ -10,22 +10,8 @@
 
 #include "hcc_internal.cuh"
 
-// Launch shape of the flux pass (threads per block, minimum resident blocks per SM for the register budget).
-#ifndef HCC_FLUX_MINB_MANY
-#define HCC_FLUX_MINB_MANY 2     // FP32 flux blocks per SM for systems of 8+ components (16-velocity BGK)
-#endif
-#ifndef HCC_FLUX_BLOCK
-#define HCC_FLUX_BLOCK 128
-#endif
-#ifndef HCC_FLUX_MINB
-#define HCC_FLUX_MINB 7            // FP32, D*M < 12: caps the flux kernel at 72 registers
-#endif
-#ifndef HCC_FLUX_MINB_WIDE
-#define HCC_FLUX_MINB_WIDE 4       // FP32, D*M >= 12 (3-D Euler): 128 registers
-#endif
-#ifndef HCC_FLUX_MINB64
-#define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
-#endif
+// Launch shape of the flux pass (threads per block, minimum resident blocks per SM for the register budget): the
+// HCC_FLUX_* constants of hcc_internal.cuh.
 
 namespace hcc {
 

@@ -438,6 +438,10 @@ hcc_status hcc_set_tuning(hcc_ctx *ctx, const hcc_tuning *tuning);
    particles). `report` may be NULL. */
 hcc_status hcc_autotune(hcc_ctx *ctx, double dt, int32_t steps, hcc_tune_report *report);
 
+/* The compile-time launch bounds the library was built with, e.g. "flux_block=128 flux_minb=7 flux_minb_wide=4
+   flux_minb64=3 flux_minb_many=2" (static string; no GPU needed). Tells apart variant builds loaded side by side. */
+const char *hcc_build_info(void);
+
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);
 

@@ -103,3 +103,10 @@ def test_struct_layouts_match_the_header(hcc, tmp_path):
         assert got[(cname, "size")] == C.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_build_info_names_the_launch_bounds(cuda_lib):
+    info = cuda_lib.hcc_build_info().decode()
+    keys = dict(kv.split("=") for kv in info.split())
+    assert set(keys) == {"flux_block", "flux_minb", "flux_minb_wide", "flux_minb64", "flux_minb_many"}
+    assert all(v.isdigit() for v in keys.values()) and keys["flux_block"] == "128"
