@@ -110,3 +110,18 @@ def test_build_info_names_the_launch_bounds(cuda_lib):
     keys = dict(kv.split("=") for kv in info.split())
     assert set(keys) == {"flux_block", "flux_minb", "flux_minb_wide", "flux_minb64", "flux_minb_many"}
     assert all(v.isdigit() for v in keys.values()) and keys["flux_block"] == "128"
+
+
+def test_bindings_call_only_declared_entry_points():
+    """The Julia shim's ccalls and the ctypes prototype table name only entry points of include/hcc.h, and the
+    ctypes table covers all of them."""
+    import importlib.util
+    names = set(_declared_symbols())
+    jl = (ROOT / "hypercloudcore.jl_gb300" / "julia" / "HCCGB300.jl").read_text()
+    called = set(re.findall(r"ccall\(\(:(hcc_[a-z0-9_]+),", jl))
+    assert called and called <= names, called - names
+    spec = importlib.util.spec_from_file_location("_abi_only", ROOT / "hypercloudcore.jl_gb300" / "_abi.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    bound = {p[0] for p in mod.PROTOTYPES}
+    assert bound == names, (bound ^ names)
