@@ -1894,18 +1894,15 @@ hcc_status hcc_get_kernel_times(hcc_ctx *c, hcc_kernel_times *out, int reset) {
     return HCC_OK;
 }
 
-hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets, const double *pos,
-                            const uint8_t *is_boundary, const int32_t *tags, const double *volumes, double *shifts,
-                            double *canvas) {
-    if (!c) return HCC_ERR_INVALID;
-    if (n_clouds < 1 || !offsets || offsets[0] != 0) return c->fail(HCC_ERR_INVALID, "bad batch offsets");
+hcc_status hcc_batch_layout(int32_t dim, double radius, int32_t n_clouds, const int64_t *offsets, const double *pos,
+                            double *shifts, double *canvas) {
+    if (dim < 1 || dim > 3 || !(radius > 0.0) || n_clouds < 1 || !offsets || offsets[0] != 0 || !shifts || !canvas)
+        return HCC_ERR_INVALID;
     for (int b = 0; b < n_clouds; ++b)
-        if (offsets[b + 1] < offsets[b]) return c->fail(HCC_ERR_INVALID, "batch offsets must not decrease");
-    const int D = c->D;
-    for (int d = 0; d < D; ++d)
-        if (c->cfg.periodic[d]) return c->fail(HCC_ERR_INVALID, "batches of periodic clouds are not supported");
+        if (offsets[b + 1] < offsets[b]) return HCC_ERR_INVALID;
+    const int D = dim;
     const int64_t n = offsets[n_clouds];
-    if (n > 0 && !pos) return c->fail(HCC_ERR_INVALID, "bad cloud arguments");
+    if (n > 0 && !pos) return HCC_ERR_INVALID;
     // bounding boxes
     std::vector<double> lo(size_t(n_clouds) * 3, 0.0), hi(size_t(n_clouds) * 3, 0.0);
     for (int b = 0; b < n_clouds; ++b) {
@@ -1913,7 +1910,7 @@ hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets
         for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i)
             for (int d = 0; d < D; ++d) {
                 const double x = pos[i * D + d];
-                if (!std::isfinite(x)) return c->fail(HCC_ERR_NONFINITE, "non-finite position");
+                if (!std::isfinite(x)) return HCC_ERR_NONFINITE;
                 lo[b * 3 + d] = std::min(lo[b * 3 + d], x);
                 hi[b * 3 + d] = std::max(hi[b * 3 + d], x);
             }
@@ -1921,7 +1918,7 @@ hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets
             if (offsets[b + 1] == offsets[b]) { lo[b * 3 + d] = 0.0; hi[b * 3 + d] = 0.0; }
     }
     // shelf packing in the (x, y) plane, tallest first; z (3-D) aligned at 0; 1-D: one row
-    const double gap = 2.0 * c->cfg.radius;
+    const double gap = 2.0 * radius;
     std::vector<int> order(n_clouds);
     for (int b = 0; b < n_clouds; ++b) order[b] = b;
     auto ext = [&](int b, int d) { return hi[b * 3 + d] - lo[b * 3 + d]; };
@@ -1944,27 +1941,52 @@ hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets
         x += w;
         if (D >= 2) row_h = std::max(row_h, ext(b, 1) + gap);
     }
-    std::vector<double> up(size_t(n) * D);
     double cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int b = 0; b < n_clouds; ++b)
         for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i)
             for (int d = 0; d < D; ++d) {
                 const double v = pos[i * D + d] + sh[b * 3 + d];
-                up[i * D + d] = v;
                 cmin[d] = std::min(cmin[d], v);
                 cmax[d] = std::max(cmax[d], v);
             }
     for (int d = 0; d < D; ++d) {
         if (!(cmax[d] > cmin[d])) { cmin[d] -= gap; cmax[d] += gap; }
-        c->cfg.canvas_min[d] = cmin[d];
-        c->cfg.canvas_max[d] = cmax[d];
-        c->cfg.domain_min[d] = cmin[d];
-        c->cfg.domain_max[d] = cmax[d];
-        if (canvas) { canvas[d] = cmin[d]; canvas[D + d] = cmax[d]; }
+        canvas[d] = cmin[d];
+        canvas[D + d] = cmax[d];
     }
-    if (shifts)
-        for (int b = 0; b < n_clouds; ++b)
-            for (int d = 0; d < D; ++d) shifts[b * D + d] = sh[b * 3 + d];
+    for (int b = 0; b < n_clouds; ++b)
+        for (int d = 0; d < D; ++d) shifts[b * D + d] = sh[b * 3 + d];
+    return HCC_OK;
+}
+
+hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets, const double *pos,
+                            const uint8_t *is_boundary, const int32_t *tags, const double *volumes, double *shifts,
+                            double *canvas) {
+    if (!c) return HCC_ERR_INVALID;
+    if (n_clouds < 1 || !offsets || offsets[0] != 0) return c->fail(HCC_ERR_INVALID, "bad batch offsets");
+    for (int b = 0; b < n_clouds; ++b)
+        if (offsets[b + 1] < offsets[b]) return c->fail(HCC_ERR_INVALID, "batch offsets must not decrease");
+    const int D = c->D;
+    for (int d = 0; d < D; ++d)
+        if (c->cfg.periodic[d]) return c->fail(HCC_ERR_INVALID, "batches of periodic clouds are not supported");
+    const int64_t n = offsets[n_clouds];
+    if (n > 0 && !pos) return c->fail(HCC_ERR_INVALID, "bad cloud arguments");
+    std::vector<double> sh(size_t(n_clouds) * D), cv(2 * size_t(D));
+    const hcc_status ls = hcc_batch_layout(D, c->cfg.radius, n_clouds, offsets, pos, sh.data(), cv.data());
+    if (ls == HCC_ERR_NONFINITE) return c->fail(ls, "non-finite position");
+    if (ls != HCC_OK) return c->fail(ls, "bad batch layout arguments");
+    std::vector<double> up(size_t(n) * D);
+    for (int b = 0; b < n_clouds; ++b)
+        for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i)
+            for (int d = 0; d < D; ++d) up[i * D + d] = pos[i * D + d] + sh[size_t(b) * D + d];
+    for (int d = 0; d < D; ++d) {
+        c->cfg.canvas_min[d] = cv[d];
+        c->cfg.canvas_max[d] = cv[D + d];
+        c->cfg.domain_min[d] = cv[d];
+        c->cfg.domain_max[d] = cv[D + d];
+        if (canvas) { canvas[d] = cv[d]; canvas[D + d] = cv[D + d]; }
+    }
+    if (shifts) std::copy(sh.begin(), sh.end(), shifts);
     hcc_status st = hcc_upload_cloud(c, n, up.data(), is_boundary, tags, volumes);
     if (st != HCC_OK) return st;
     c->batch_offsets.assign(offsets, offsets + n_clouds + 1);

@@ -310,6 +310,12 @@ hcc_status hcc_upload_batch(hcc_ctx *ctx, int32_t n_clouds, const int64_t *offse
                             const uint8_t *is_boundary, const int32_t *tags, const double *volumes, double *shifts,
                             double *canvas);
 
+/* The packing hcc_upload_batch applies, on the host only (no context, no GPU): shifts[c*dim + d] and the union box
+   canvas[0..2*dim) for clouds of `dim`-D positions with support `radius`. HCC_ERR_INVALID for bad arguments,
+   HCC_ERR_NONFINITE for a non-finite position. */
+hcc_status hcc_batch_layout(int32_t dim, double radius, int32_t n_clouds, const int64_t *offsets, const double *pos,
+                            double *shifts, double *canvas);
+
 /* total_mass per cloud of the last hcc_upload_batch: out[c*M + m] (FP64 accumulation on the device). */
 hcc_status hcc_batch_total_mass(hcc_ctx *ctx, double *out);
 
