@@ -427,6 +427,27 @@ class Context:
                                                      _ptr(dist, C.c_double)), "hcc_download_neighbours")
         return counts, idx, w, dist
 
+    def neighbour_counts(self):
+        """Neighbour count of every particle (no list download)."""
+        counts = np.zeros(self.n, dtype=np.int32)
+        self._check(self.lib.hcc_download_neighbours(self._h, _ptr(counts, C.c_int32), None, None, None),
+                    "hcc_download_neighbours")
+        return counts
+
+    def neighbours_of(self, ids, max_slots: int):
+        """(counts, idx, w, dist) of the selected particles: row q holds the first max_slots slots of ids[q]."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        q = len(ids)
+        counts = np.zeros(q, dtype=np.int32)
+        idx = np.full((q, max_slots), -1, dtype=np.int32)
+        w = np.zeros((q, max_slots), dtype=np.float64)
+        dist = np.zeros((q, max_slots, self.D), dtype=np.float64)
+        self._check(self.lib.hcc_download_neighbours_of(self._h, q, _ptr(ids, C.c_int64), int(max_slots),
+                                                        _ptr(counts, C.c_int32), _ptr(idx, C.c_int32),
+                                                        _ptr(w, C.c_double), _ptr(dist, C.c_double)),
+                    "hcc_download_neighbours_of")
+        return counts, idx, w, dist
+
     def geometry(self, total: int):
         dw = np.zeros((total, self.D), dtype=np.float64)
         okr = np.zeros(self.n, dtype=np.uint8)

@@ -127,6 +127,7 @@ PROTOTYPES = [
     ("hcc_upload_cloud", C.c_int, [P, C.c_int64, _dp, _u8p, _i32p, _dp]),
     ("hcc_build_neighbours", C.c_int, [P]),
     ("hcc_download_neighbours", C.c_int, [P, _i32p, _i32p, _dp, _dp]),
+    ("hcc_download_neighbours_of", C.c_int, [P, C.c_int64, C.POINTER(C.c_int64), C.c_int32, _i32p, _i32p, _dp, _dp]),
     ("hcc_prepare_geometry", C.c_int, [P]),
     ("hcc_download_geometry", C.c_int, [P, _dp, _u8p, _u8p]),
     ("hcc_upload_state", C.c_int, [P, _dp]),

@@ -1256,7 +1256,7 @@ hcc_status hcc_build_neighbours(hcc_ctx *c) {
     const hcc_config &f = c->cfg;
     const int D = c->D;
     hcc_status st;
-    // GlobalBins (NeighborLogic.jl:123-141) and the 3^D window of every bin (:144-177), on the host
+    // GlobalBins (NeighborLogic.jl:22-40) and the 3^D window of every bin (_fill_bin_neighbors!, :43-76), on the host
     c->nbins = 1;
     for (int d = 0; d < 3; ++d) { c->dims[d] = 1; c->csize[d] = 1.0; }
     for (int d = 0; d < D; ++d) {
@@ -1480,6 +1480,44 @@ hcc_status hcc_download_neighbours(hcc_ctx *c, int32_t *counts, int32_t *idx, do
     if (w && st == HCC_OK) st = pull(c->w64, w, 1, 8);
     if (dist && st == HCC_OK) st = pull(c->dist64, dist, c->D, 8);
     cudaFree(d_rs);
+    cudaFree(tmp);
+    return st;
+}
+
+hcc_status hcc_download_neighbours_of(hcc_ctx *c, int64_t n_sel, const int64_t *ids, int32_t max_slots,
+                                      int32_t *counts, int32_t *idx, double *w, double *dist) {
+    if (!c) return HCC_ERR_INVALID;
+    if (!c->have_nb) return c->fail(HCC_ERR_STATE, "neighbour lists missing");
+    if (n_sel < 0 || max_slots < 0 || (n_sel > 0 && !ids)) return c->fail(HCC_ERR_INVALID, "bad selection");
+    if (n_sel == 0) return HCC_OK;
+    for (int64_t q = 0; q < n_sel; ++q)
+        if (ids[q] < 0 || ids[q] >= c->n) return c->fail(HCC_ERR_INVALID, "selected particle out of range");
+    hcc_status st;
+    int64_t *d_ids = nullptr;
+    void *tmp = nullptr;
+    HCC_TRY(c->alloc(d_ids, n_sel, "selection"));
+    const size_t rows = size_t(n_sel) * size_t(std::max(max_slots, 1));
+    st = c->valloc(tmp, rows * 8 * c->D + 8, "selection rows");
+    if (st != HCC_OK) { cudaFree(d_ids); return st; }
+    st = c->cuda(cudaMemcpy(d_ids, ids, size_t(n_sel) * sizeof(int64_t), cudaMemcpyHostToDevice), "selection");
+    if (counts && st == HCC_OK) {
+        // counts of the selected particles (uncapped)
+        std::vector<int32_t> all(c->n);
+        st = c->cuda(cudaMemcpy(all.data(), c->cnt, size_t(c->n) * sizeof(int32_t), cudaMemcpyDeviceToHost), "counts");
+        for (int64_t q = 0; q < n_sel && st == HCC_OK; ++q) counts[q] = all[ids[q]];
+    }
+    auto pull = [&](const void *src, void *dst, int width, int eb) -> hcc_status {
+        launch_gather_rows_of(src, tmp, c->cnt, d_ids, n_sel, c->npad, width, max_slots, eb, c->stream);
+        hcc_status s2 = c->sync("selected rows");
+        if (s2 != HCC_OK) return s2;
+        return c->cuda(cudaMemcpy(dst, tmp, rows * width * eb, cudaMemcpyDeviceToHost), "selected row copy");
+    };
+    if (max_slots > 0) {
+        if (idx && st == HCC_OK) st = pull(c->nidx, idx, 1, 4);
+        if (w && st == HCC_OK) st = pull(c->w64, w, 1, 8);
+        if (dist && st == HCC_OK) st = pull(c->dist64, dist, c->D, 8);
+    }
+    cudaFree(d_ids);
     cudaFree(tmp);
     return st;
 }

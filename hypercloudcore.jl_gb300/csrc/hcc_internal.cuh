@@ -32,7 +32,7 @@
 namespace hcc {
 
 // ----------------------------------------------------------------------------------- float helpers
-// Base.min / Base.max of Julia for IEEE floats: NaN-propagating, -0 below +0 (src/Utils.jl:259-262).
+// Base.min / Base.max of Julia for IEEE floats: NaN-propagating, -0 below +0 (Julia Base `min`/`max` on IEEE floats; the reference calls them in `_local_extrema`, src/Interpolation/Limiter.jl, and in the MOOD extrema, src/TimeStepping/MOOD.jl).
 template <typename T> __host__ __device__ __forceinline__ bool is_nan(T x) { return x != x; }
 template <typename T> __host__ __device__ __forceinline__ T jmin(T x, T y) {
     bool take_y = (y < x) || (signbit(y) && !signbit(x));
@@ -478,6 +478,8 @@ struct DropArgs {
 void launch_drop_decide(const DropArgs &a, int is_f32, int drop_blocks, cudaStream_t s);
 void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
                         int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
+void launch_gather_rows_of(const void *src, void *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel,
+                           int64_t npad, int width, int max_slots, int elem_bytes, cudaStream_t s);
 
 
 // ----------------------------------------------------------------------------------- learned predictor

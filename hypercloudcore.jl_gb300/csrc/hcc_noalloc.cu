@@ -9,8 +9,8 @@
 // partial minimum per thread block — in a file-scope __device__ array of fixed size.
 //
 // Scratch rules:
-//  * g_cfl_scratch holds 65536 partial minima plus one result word (about 512 KiB). Every GPU
-//    that loads this library holds it until the process exits.
+//  * g_cfl_scratch holds 65536 partial minima plus one result word (about 512 KiB of device memory per GPU on
+//    which this file's module is loaded; the module stays loaded until the process exits).
 //  * n above HCC_NOALLOC_MAX_PARTICLES (= max blocks x block size) is rejected with HCC_ERR_CAPACITY.
 //  * Every call shares the array and leaves its contents behind. A call writes every word it reads before reading
 //    it (each block writes its partial, then the final kernel reads exactly those partials and writes the result
@@ -18,7 +18,11 @@
 //    or two host threads on one device) race on the array and must be serialised by the caller.
 //  * Host code never uses g_cfl_scratch's name as an address: the device address comes from
 //    cudaGetSymbolAddress, once per device, with that device current, on the first call made on that device.
-//    That first call therefore performs a CUDA runtime query and should come before any stream capture.
+//  * First call per device: with CUDA's lazy module loading (the default), that call is what loads this file's
+//    module (the scratch array and the kernels), and loading can allocate device memory. A caller that freezes its
+//    device memory must therefore make one call with n > 0 for each physics shape it will use on each device
+//    before it freezes the memory (and before any stream capture); later calls allocate nothing.
+//  * The stream must belong to the current device (checked: HCC_ERR_INVALID otherwise).
 #include "hcc_stage_impl.cuh"
 #include <algorithm>
 #include <cstring>
@@ -170,6 +174,15 @@ extern "C" hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n
     if (cfg->dim < 1 || cfg->dim > 3 || cfg->n_vars < 1 || cfg->n_vars > HCC_MAX_VARS) return HCC_ERR_INVALID;
     if (n > int64_t(HCC_NOALLOC_MAX_PARTICLES)) return HCC_ERR_CAPACITY;   // n beyond the fixed scratch
     if (n == 0) { *dt_out = INFINITY; return HCC_OK; }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // an error left pending by an earlier, unrelated runtime call is consumed here, so that the launch check below
+    // reports this call's own launches only
+    (void)cudaGetLastError();
+    if (s) {
+        int cur = 0, sdev = 0;
+        if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(s, &sdev) != cudaSuccess) return HCC_ERR_CUDA;
+        if (sdev != cur) return HCC_ERR_INVALID;          // the scratch address below is the current device's
+    }
     unsigned long long *scratch = nullptr;
     hcc_status st = scratch_address(&scratch);
     if (st != HCC_OK) return st;
@@ -185,7 +198,6 @@ extern "C" hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n
     a.n = n; a.npad = npad; a.cnt = counts; a.nidx = nidx; a.dw = dweights; a.bnd = is_boundary; a.U = U;
     a.scratch = scratch;
     const int blocks = int((n + kNoallocBlock - 1) / kNoallocBlock);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int pde = cfg->pde == HCC_PDE_BGK ? HCC_PDE_ADVECTION : cfg->pde;
     if (cfg->pde == HCC_PDE_EULER && cfg->n_vars != cfg->dim + 2) return HCC_ERR_INVALID;
     if (!launch_for(cfg->dim, cfg->n_vars, pde, a, blocks, s)) return HCC_ERR_UNSUPPORTED;

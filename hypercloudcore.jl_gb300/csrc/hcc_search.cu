@@ -16,7 +16,7 @@ __device__ __forceinline__ double jmod(double x, double y) {
     return r;
 }
 
-// _wrap_position! (NeighborLogic.jl:380-387) + get_flat_bin_index (:187-203) + _bin_count! (:240-245)
+// _wrap_position! (NeighborLogic.jl:279-286) + get_flat_bin_index (:86-102) + _bin_count! (:139-144)
 __global__ void k_bin(SearchArgs a) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -77,7 +77,7 @@ __global__ void k_scan_bins(const int32_t *count, int64_t *start, int64_t nbins,
     }
 }
 
-// _bin_scatter! (NeighborLogic.jl:247-252)
+// _bin_scatter! (NeighborLogic.jl:146-151)
 __global__ void k_scatter(SearchArgs a) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
@@ -86,7 +86,7 @@ __global__ void k_scatter(SearchArgs a) {
     a.cellp[a.cell_start[b] + k] = int32_t(i);
 }
 
-// _bin_sort! (NeighborLogic.jl:255-268): insertion sort of each bin, descending index.
+// _bin_sort! (NeighborLogic.jl:153-167): insertion sort of each bin, descending index.
 __global__ void k_binsort(SearchArgs a) {
     int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (b >= a.nbins) return;
@@ -115,7 +115,7 @@ __device__ __forceinline__ double pair_distance(const SearchArgs &a, int64_t i, 
     return s;
 }
 
-// _count_neighbours! (NeighborLogic.jl:389-402); stats: [0] max count, [1] total, [2] min interior count
+// _count_neighbours! (NeighborLogic.jl:288-301); stats: [0] max count, [1] total, [2] min interior count
 template <int D>
 __global__ void k_count(SearchArgs a, unsigned long long *stats) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -156,7 +156,7 @@ __device__ __forceinline__ double exp_weight(double d2, double alpha, double inv
     return 1.0 / den;
 }
 
-// _write_neighbours! (NeighborLogic.jl:410-430) into the slot-major layout
+// _write_neighbours! (NeighborLogic.jl:309-329) into the slot-major layout
 template <int D>
 __global__ void k_write(SearchArgs a) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -254,7 +254,7 @@ __device__ __forceinline__ bool admissible(const PhysParams<T> &ph, const T *U) 
     return ok;
 }
 
-// BGK Maxwellian of the single macro moment (test/kinetic_source.jl:194-231).
+// BGK Maxwellian of the single macro moment (evaluate_source / implicit_solve, test/kinetic_source.jl:67-104).
 template <typename T, int D, int M>
 __device__ __forceinline__ void maxwellian(const PhysParams<T> &ph, const T *U, T *Mk) {
     T u = U[0];
@@ -862,7 +862,7 @@ template <typename T, int D, int M> constexpr int flux_min_blocks() {
 }
 
 // The MUSCL functor (MUSCL.jl:390-508) in its streamed form: per slot, EPD interface reconstruction, physical
-// fluxes, Rusanov (FluxFunctions.jl:90-100) with sort_flux (Utils.jl:270-278), the flux difference ΔF and its
+// fluxes, Rusanov (FluxFunctions.jl:66-76) with sort_flux (Utils.jl:95-102), the flux difference ΔF and its
 // contraction with the divergence weights; K_E = -2 Σ c·ΔF (TimeSteppers.jl:354). Fused epilogue: the next
 // candidate (_stage_predictor!, :400-421, and the implicit part), the Euler substep (:511-518) and the MOOD
 // check of the next checkpoint (_mood_flag!, MOOD.jl:289-295; the extrema come from this loop's neighbour reads).

@@ -36,7 +36,7 @@ __global__ void k_bc(T *Y, const T *rhos, const int32_t *blist, const int32_t *b
 // After a flux pass with the MOOD check, one launch: the boundary conditions of the new candidate (blocks below
 // bc_blocks; apply_boundary_conditions!, BoundaryConditions.jl:43-130), _mood_drop! (MOOD.jl:299-309) over the
 // failed candidates — an order above 1 drops by one and the particle joins the changed list — and, in the last
-// block to finish, the loop condition of mood_checkpoint! (TimeSteppers.jl:461-476): no changed order ends the loop;
+// block to finish, the loop condition of mood_checkpoint! (TimeSteppers.jl:454-477): no changed order ends the loop;
 // otherwise the flagged count grows and the loop repeats, unless the checkpoint already ran `cap` recomputes (the
 // timeout flag ends it). The decision publishes the changed list and clears the other lists for the next pass.
 template <typename T>
@@ -297,6 +297,19 @@ __global__ void k_rows(const E *src, E *dst, const int32_t *cnt, const int64_t *
         for (int q = 0; q < width; ++q) dst[(r0 + k) * width + q] = src[(int64_t(k) * width + q) * npad + i];
 }
 
+// slot-major [ (k*width + c) * npad + ids[q] ] -> [ (q*max_slots + k) * width + c ] for the selected particles
+template <typename E>
+__global__ void k_rows_of(const E *src, E *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel, int64_t npad,
+                          int width, int max_slots) {
+    const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= n_sel) return;
+    const int64_t i = ids[q];
+    const int c = cnt[i] < max_slots ? cnt[i] : max_slots;
+    for (int k = 0; k < c; ++k)
+        for (int e = 0; e < width; ++e)
+            dst[(q * max_slots + k) * width + e] = src[(int64_t(k) * width + e) * npad + i];
+}
+
 }  // namespace
 
 void launch_cast_f64_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s) {
@@ -434,6 +447,19 @@ void launch_gather_rows(const void *src, void *dst, const int32_t *cnt, const in
     else if (elem_bytes == 4)
         k_rows<unsigned int><<<grid_for(n), HCC_BLOCK, 0, s>>>(
             static_cast<const unsigned int *>(src), static_cast<unsigned int *>(dst), cnt, rowstart, n, npad, width);
+}
+
+void launch_gather_rows_of(const void *src, void *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel,
+                           int64_t npad, int width, int max_slots, int elem_bytes, cudaStream_t s) {
+    if (n_sel <= 0) return;
+    if (elem_bytes == 8)
+        k_rows_of<unsigned long long><<<grid_for(n_sel), HCC_BLOCK, 0, s>>>(
+            static_cast<const unsigned long long *>(src), static_cast<unsigned long long *>(dst), cnt, ids, n_sel, npad,
+            width, max_slots);
+    else if (elem_bytes == 4)
+        k_rows_of<unsigned int><<<grid_for(n_sel), HCC_BLOCK, 0, s>>>(
+            static_cast<const unsigned int *>(src), static_cast<unsigned int *>(dst), cnt, ids, n_sel, npad, width,
+            max_slots);
 }
 
 }  // namespace hcc

@@ -48,7 +48,7 @@ typedef enum {
     HCC_PDE_ADVECTION = 0,   /* diagonal linear advection: F_d(U)_m = c[d][m] U_m (test/PDEs/linear_advection.jl:24-32) */
     HCC_PDE_EULER = 1,       /* compressible Euler, ideal gas, M = D + 2 (not in the reference; PAD = rho>0, p>0, finite) */
     HCC_PDE_BGK = 2          /* discrete-velocity kinetic relaxation: advection with speeds v_k + implicit
-                                Maxwellian relaxation (test/kinetic_source.jl:194-231) */
+                                Maxwellian relaxation (test/kinetic_source.jl:67-104) */
 } hcc_pde_kind;
 
 typedef enum {
@@ -191,13 +191,20 @@ const char *hcc_status_string(hcc_status s);
 hcc_status hcc_upload_cloud(hcc_ctx *ctx, int64_t n, const double *pos, const uint8_t *is_boundary,
                             const int32_t *tags, const double *volumes);
 
-/* Neighbour search: (nd::NeighborData)(pg) (NeighborLogic.jl:336-375) with the cell list of
-   build_global_bins! (:217-237). Slot-major device layout (:283). */
+/* Neighbour search: (nd::NeighborData)(pg) (NeighborLogic.jl:235-274) with the cell list of
+   build_global_bins! (:116-136). Slot-major device layout (_slot_range, :182). */
 hcc_status hcc_build_neighbours(hcc_ctx *ctx);
 
 /* Neighbour lists in the reference's row-major order (ranges as counts, NeighborLogic.jl:282):
    counts[N]; then idx/w/dist of total_neighbours slots (dist: total*D). Any output may be NULL. */
 hcc_status hcc_download_neighbours(hcc_ctx *ctx, int32_t *counts, int32_t *idx, double *w, double *dist);
+
+/* The lists of n_sel selected particles (the per-particle slot views pg.neighbor.indices[ranges[i]] of
+   NeighbourViews.jl:11-43 / NeighborLogic.jl:182), for inspecting a large cloud without downloading every list:
+   counts[q] = the full count of particle ids[q]; its first min(count, max_slots) slots in idx[q*max_slots + k],
+   w[q*max_slots + k], dist[(q*max_slots + k)*dim + d]. Any output may be NULL. */
+hcc_status hcc_download_neighbours_of(hcc_ctx *ctx, int64_t n_sel, const int64_t *ids, int32_t max_slots,
+                                      int32_t *counts, int32_t *idx, double *w, double *dist);
 
 /* prepare_geometry!(muscl, pg) (MUSCL.jl:172-187): cached inverse moments, ok flags, per-slot
    divergence weights (update_divergence_weights!, MUSCL.jl:197-223) and the outflow donor map. */
@@ -325,12 +332,19 @@ hcc_status hcc_batch_total_mass(hcc_ctx *ctx, double *out);
    cudaMalloc/cudaFree inside its time loop. Same value as hcc_time_step (ParticleGrids.jl:386-450 arithmetic, FP64).
    Inputs are DEVICE pointers in the library's slot-major layout: counts[n], nidx[k*npad + i],
    dweights[(k*dim + d)*npad + i], is_boundary[n], U[i*n_vars + m] (FP64); physics parameters come from cfg
-   (pde, dim, n_vars, velocity, gamma). stream is a cudaStream_t (NULL = default stream); *dt_out is written on
-   return (the call synchronises the stream).
-   Scratch: a fixed file-scope device array (about 512 KiB, held by every GPU that loads the library until exit);
-   n above HCC_NOALLOC_MAX_PARTICLES returns HCC_ERR_CAPACITY. All calls share it: calls that overlap on the GPU
-   race and must be serialised by the caller. The first call on each device looks up the array's device address
-   (a CUDA runtime query) and should come before any stream capture. */
+   (pde, dim, n_vars, velocity, gamma). Supported shapes (pde: dim, n_vars): HCC_PDE_EULER: (1, 3), (2, 4), (3, 5);
+   HCC_PDE_ADVECTION and HCC_PDE_BGK: (1, 1), (2, 1), (3, 1), (2, 2), (2, 16), (1, 2); any other shape returns
+   HCC_ERR_UNSUPPORTED. stream is a cudaStream_t of the CURRENT device (NULL = default stream; a stream of another
+   device returns HCC_ERR_INVALID); *dt_out is written on return (the call synchronises the stream). A runtime error
+   left pending by an earlier, unrelated CUDA call is consumed on entry; HCC_ERR_CUDA reports this call's own
+   launch or copy failure.
+   Scratch: a fixed file-scope device array (about 512 KiB on every GPU where the library's no-allocation module is
+   loaded, held until the process exits); n above HCC_NOALLOC_MAX_PARTICLES returns HCC_ERR_CAPACITY. All calls
+   share it: calls that overlap on the GPU race and must be serialised by the caller.
+   First call: under CUDA's lazy module loading (the default) the first call on a device loads the module that holds
+   the scratch array and the kernels, and that load can allocate device memory; it also looks up the array's device
+   address (a CUDA runtime query). Make one call with n > 0, for each shape used, on each device before the caller's
+   memory is frozen and before any stream capture; calls after that allocate nothing. */
 #define HCC_NOALLOC_MAX_PARTICLES (65536 * 256)
 hcc_status hcc_cfl_time_step_noalloc(const hcc_config *cfg, int64_t n, int64_t npad, const int32_t *counts,
                                      const int32_t *nidx, const double *dweights, const uint8_t *is_boundary,

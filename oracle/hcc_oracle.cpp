@@ -377,7 +377,7 @@ double ssp_coefficient(const Tableau &t) {
 
 // ---------------------------------------------------------------- physics modules
 // LinearAdvection (test/PDEs/linear_advection.jl:24-32), diagonal systems; Euler (new: ideal gas);
-// BGK kinetic relaxation (test/kinetic_source.jl:156-231) = advection of the kinetic variables + source.
+// BGK kinetic relaxation (test/kinetic_source.jl:37-104) = advection of the kinetic variables + source.
 struct Physics {
     int kind = HCC_PDE_ADVECTION;
     int D = 2, M = 1;
@@ -483,7 +483,7 @@ struct Physics {
         return true;
     }
     bool has_implicit_source() const { return kind == HCC_PDE_BGK; }
-    // Maxwellian of the single macro moment (kinetic_source.jl:194-231)
+    // Maxwellian of the single macro moment (kinetic_source.jl:67-104)
     void maxwellian(const double *U, double *Mk) const {
         double u = U[0];
         for (int k = 1; k < M; ++k) u = u + U[k];
@@ -495,13 +495,13 @@ struct Physics {
             Mk[k] = coeff * (u + fd);
         }
     }
-    // evaluate_source (kinetic_source.jl:194-205)
+    // evaluate_source (kinetic_source.jl:67-78)
     void source(const double *U, double *S) const {
         double Mk[HCC_MAX_VARS];
         maxwellian(U, Mk);
         for (int k = 0; k < M; ++k) S[k] = (Mk[k] - U[k]) * inv_eps;
     }
-    // implicit_solve (kinetic_source.jl:207-231)
+    // implicit_solve (kinetic_source.jl:80-104)
     void implicit_solve(const double *Y, double dt_coeff, double *out) const {
         double dto = dt_coeff * inv_eps;
         double denom = 1.0 / (1.0 + dto);
@@ -652,25 +652,29 @@ struct Solver {
     }
 
     // ------------------------------------------------------------ neighbour search (NeighborLogic.jl)
-    bool build_neighbours() {
-        if (N == 0) { err = "no cloud"; return false; }
-        // _wrap_position! (:380-387): periodic axes back into [min, min + L)
+    // cell list of the whole cloud: bins, their 3^D windows, the particles of each bin
+    int NOFF = 1;
+    int64_t nbins = 1;
+    std::vector<int64_t> binnb, bin_of, cstart, cellp;
+
+    void build_bins() {
+        // _wrap_position! (NeighborLogic.jl:279-286): periodic axes back into [min, min + L)
         for (int64_t i = 0; i < N; ++i)
             for (int d = 0; d < D; ++d)
                 if (per[d]) pos[i * D + d] = cmin[d] + jmod(pos[i * D + d] - cmin[d], Lphys[d]);
-        // GlobalBins (:123-141)
+        // GlobalBins (NeighborLogic.jl:22-40)
         int dims[3] = {1, 1, 1};
         double csize[3] = {1, 1, 1};
-        int64_t nbins = 1;
+        nbins = 1;
         for (int d = 0; d < D; ++d) {
             double sz = cmax[d] - cmin[d];
             dims[d] = std::max(1, int(std::floor(sz / R)));
             csize[d] = sz / double(dims[d]);
             nbins *= dims[d];
         }
-        const int NOFF = (D == 1) ? 3 : (D == 2 ? 9 : 27);
-        std::vector<int64_t> binnb(nbins * NOFF);
-        // _fill_bin_neighbors! (:144-177): window in CartesianIndices order (x offset fastest)
+        NOFF = (D == 1) ? 3 : (D == 2 ? 9 : 27);
+        binnb.assign(nbins * NOFF, 0);
+        // _fill_bin_neighbors! (NeighborLogic.jl:43-76): window in CartesianIndices order (x offset fastest)
         for (int64_t b = 0; b < nbins; ++b) {
             int cart[3] = {0, 0, 0};
             int64_t r = b;
@@ -698,8 +702,10 @@ struct Solver {
                 binnb[b * NOFF + w] = rep ? nbins : raw[w];
             }
         }
-        // build_global_bins! (:217-237) with get_flat_bin_index (:187-203)
-        std::vector<int64_t> bin_of(N), count(nbins + 1, 0), cstart(nbins + 2, 0);
+        // build_global_bins! (NeighborLogic.jl:116-136) with get_flat_bin_index (:86-102)
+        bin_of.assign(N, 0);
+        std::vector<int64_t> count(nbins + 1, 0);
+        cstart.assign(nbins + 2, 0);
         for (int64_t i = 0; i < N; ++i) {
             int64_t lin = 0, stride = 1;
             for (int d = 0; d < D; ++d) {
@@ -714,52 +720,64 @@ struct Solver {
         cstart[0] = 0;
         for (int64_t b = 0; b < nbins; ++b) cstart[b + 1] = cstart[b] + count[b];
         cstart[nbins + 1] = N;
-        std::vector<int64_t> cellp(N);
+        cellp.assign(N, 0);
         std::vector<int64_t> cursor(nbins, 0);
         for (int64_t i = 0; i < N; ++i) { int64_t b = bin_of[i]; cellp[cstart[b] + cursor[b]++] = i; }
-        for (int64_t b = 0; b < nbins; ++b)   // _bin_sort!: descending index within a bin
+        for (int64_t b = 0; b < nbins; ++b)   // _bin_sort! (NeighborLogic.jl:153-167): descending index within a bin
             std::sort(cellp.begin() + cstart[b], cellp.begin() + cstart[b + 1], std::greater<int64_t>());
-        // pass 1: counts (:389-402)
-        std::vector<int64_t> cnt(N, 0);
-#pragma omp parallel for schedule(dynamic, 256)
-        for (int64_t i = 0; i < N; ++i) {
-            int64_t c = 0;
-            double dist[3];
-            for (int w = 0; w < NOFF; ++w) {
-                int64_t b = binnb[bin_of[i] * NOFF + w];
-                for (int64_t s = cstart[b]; s < cstart[b + 1]; ++s) {
-                    int64_t j = cellp[s];
-                    if (i != j) { distance(i, j, dist); if (sumsq(dist) <= R_sq) ++c; }
+    }
+
+    // _count_neighbours! (NeighborLogic.jl:288-301) of particle i
+    int64_t count_of(int64_t i) const {
+        int64_t c = 0;
+        double dist[3];
+        for (int w = 0; w < NOFF; ++w) {
+            int64_t b = binnb[bin_of[i] * NOFF + w];
+            for (int64_t s = cstart[b]; s < cstart[b + 1]; ++s) {
+                int64_t j = cellp[s];
+                if (i != j) { distance(i, j, dist); if (sumsq(dist) <= R_sq) ++c; }
+            }
+        }
+        return c;
+    }
+
+    // _write_neighbours! (NeighborLogic.jl:309-329) of particle i into idx/w/dist from slot 0; returns the count
+    int64_t write_of(int64_t i, int32_t *idx, double *w, double *dst) const {
+        int64_t k = 0;
+        double dist[3];
+        for (int wn = 0; wn < NOFF; ++wn) {
+            int64_t b = binnb[bin_of[i] * NOFF + wn];
+            for (int64_t s = cstart[b]; s < cstart[b + 1]; ++s) {
+                int64_t j = cellp[s];
+                if (i == j) continue;
+                distance(i, j, dist);
+                double d2 = sumsq(dist);
+                if (d2 <= R_sq) {
+                    idx[k] = int32_t(j);
+                    w[k] = weight(d2);
+                    for (int d = 0; d < D; ++d) dst[k * D + d] = dist[d];
+                    ++k;
                 }
             }
-            cnt[i] = c;
         }
+        return k;
+    }
+
+    bool build_neighbours() {
+        if (N == 0) { err = "no cloud"; return false; }
+        build_bins();
+        // pass 1: counts
+        std::vector<int64_t> cnt(N, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t i = 0; i < N; ++i) cnt[i] = count_of(i);
         start.assign(N + 1, 0);
         max_nb = 0;
         for (int64_t i = 0; i < N; ++i) { start[i + 1] = start[i] + cnt[i]; max_nb = std::max<int32_t>(max_nb, int32_t(cnt[i])); }
         int64_t total = start[N];
         nidx.assign(total, 0); nw.assign(total, 0.0); ndist.assign(total * D, 0.0);
-        // pass 2: write (:410-430)
+        // pass 2: write
 #pragma omp parallel for schedule(dynamic, 256)
-        for (int64_t i = 0; i < N; ++i) {
-            int64_t k = start[i];
-            double dist[3];
-            for (int w = 0; w < NOFF; ++w) {
-                int64_t b = binnb[bin_of[i] * NOFF + w];
-                for (int64_t s = cstart[b]; s < cstart[b + 1]; ++s) {
-                    int64_t j = cellp[s];
-                    if (i == j) continue;
-                    distance(i, j, dist);
-                    double d2 = sumsq(dist);
-                    if (d2 <= R_sq) {
-                        nidx[k] = int32_t(j);
-                        nw[k] = weight(d2);
-                        for (int d = 0; d < D; ++d) ndist[k * D + d] = dist[d];
-                        ++k;
-                    }
-                }
-            }
-        }
+        for (int64_t i = 0; i < N; ++i) write_of(i, &nidx[start[i]], &nw[start[i]], &ndist[start[i] * D]);
         have_nb = true;
         have_geom = false;
         return true;
@@ -1244,7 +1262,7 @@ struct Solver {
             // full order, or always at order 1, the states are sorted by the signs of c_ij instead of the distance
             const bool below = max_order == 1 || eff < max_order || orders[j] < max_order;
             const double *dir = (aligned && below) ? wk : dk;
-            // sort_flux (Utils.jl:270-278) + RusanovFlux (FluxFunctions.jl:90-100)
+            // sort_flux (Utils.jl:95-102) + RusanovFlux (FluxFunctions.jl:66-76)
             for (int d = 0; d < D; ++d) {
                 bool pos_ = dir[d] > 0.0;
                 const double *fL = pos_ ? fij : fji;
@@ -2202,6 +2220,35 @@ hcc_status orc_download_neighbours(orc_ctx *ctx, int32_t *counts, int32_t *idx, 
     if (w) std::memcpy(w, s.nw.data(), s.nw.size() * sizeof(double));
     if (dist) std::memcpy(dist, s.ndist.data(), s.ndist.size() * sizeof(double));
     return HCC_OK;
+}
+hcc_status orc_neighbour_counts(orc_ctx *ctx, int32_t *counts) {
+    if (!ctx || !counts) return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    if (s.N == 0) return HCC_OK;
+    s.build_bins();
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < s.N; ++i) counts[i] = int32_t(s.count_of(i));
+    return HCC_OK;
+}
+hcc_status orc_neighbours_of(orc_ctx *ctx, int64_t n_sel, const int64_t *ids, int32_t max_slots, int32_t *counts,
+                             int32_t *idx, double *w, double *dist) {
+    if (!ctx || n_sel < 0 || max_slots < 0 || (n_sel > 0 && (!ids || !counts || !idx || !w || !dist)))
+        return HCC_ERR_INVALID;
+    Solver &s = ctx->s;
+    for (int64_t q = 0; q < n_sel; ++q)
+        if (ids[q] < 0 || ids[q] >= s.N) return HCC_ERR_INVALID;
+    if (n_sel == 0) return HCC_OK;
+    s.build_bins();
+    bool over = false;
+#pragma omp parallel for schedule(dynamic, 16) reduction(|| : over)
+    for (int64_t q = 0; q < n_sel; ++q) {
+        const int64_t i = ids[q];
+        const int64_t c = s.count_of(i);
+        counts[q] = int32_t(c);
+        if (c > max_slots) { over = true; continue; }
+        s.write_of(i, idx + q * max_slots, w + q * max_slots, dist + q * max_slots * s.D);
+    }
+    return over ? HCC_ERR_CAPACITY : HCC_OK;
 }
 hcc_status orc_download_positions(orc_ctx *ctx, double *pos) {
     if (!ctx || !pos) return HCC_ERR_INVALID;

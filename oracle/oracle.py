@@ -48,6 +48,8 @@ def load(abi) -> C.CDLL:
         ("orc_neighbour_total", C.c_int, [P, C.POINTER(C.c_int64), ip]),
         ("orc_download_neighbours", C.c_int, [P, ip, ip, dp, dp]),
         ("orc_download_positions", C.c_int, [P, dp]),
+        ("orc_neighbour_counts", C.c_int, [P, ip]),
+        ("orc_neighbours_of", C.c_int, [P, C.c_int64, C.POINTER(C.c_int64), C.c_int32, ip, ip, dp, dp]),
         ("orc_prepare_geometry", C.c_int, [P]),
         ("orc_download_geometry", C.c_int, [P, dp, up, up]),
         ("orc_upload_state", C.c_int, [P, dp]),
@@ -162,6 +164,25 @@ class OracleContext:
         dist = np.zeros((tot.value, self.D), dtype=np.float64)
         self._check(self.lib.orc_download_neighbours(self._h, _p(counts, C.c_int32), _p(idx, C.c_int32),
                                                      _p(w, C.c_double), _p(dist, C.c_double)), "orc_download_neighbours")
+        return counts, idx, w, dist
+
+    def neighbour_counts(self):
+        """Neighbour counts of every particle (the count pass alone)."""
+        counts = np.zeros(self.n, dtype=np.int32)
+        self._check(self.lib.orc_neighbour_counts(self._h, _p(counts, C.c_int32)), "orc_neighbour_counts")
+        return counts
+
+    def neighbours_of(self, ids, max_slots: int):
+        """(counts, idx, w, dist) of the selected particles in the reference's order, rows of max_slots slots."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        q = len(ids)
+        counts = np.zeros(q, dtype=np.int32)
+        idx = np.full((q, max_slots), -1, dtype=np.int32)
+        w = np.zeros((q, max_slots), dtype=np.float64)
+        dist = np.zeros((q, max_slots, self.D), dtype=np.float64)
+        self._check(self.lib.orc_neighbours_of(self._h, q, ids.ctypes.data_as(C.POINTER(C.c_int64)), int(max_slots),
+                                               _p(counts, C.c_int32), _p(idx, C.c_int32), _p(w, C.c_double),
+                                               _p(dist, C.c_double)), "orc_neighbours_of")
         return counts, idx, w, dist
 
     def positions(self):

@@ -125,6 +125,29 @@ def test_neighbour_lists_match_brute_force(hcc, oracle, abi, D, periodic):
                                    1 / (1 + y * (1 + y * (0.5 + y * (1 / 6 + y / 24)))), rtol=1e-14)
 
 
+@pytest.mark.parametrize("D,periodic", [(2, True), (3, False)])
+def test_selected_lists_and_counts_equal_the_full_search(hcc, oracle, abi, D, periodic):
+    """The oracle's per-particle lists (used on clouds too large to list whole) and its count pass equal the rows and
+    counts of the full search (NeighborLogic.jl:288-329)."""
+    h = 0.05 if D == 2 else 0.1
+    cl = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, periodic=periodic, jitter=0.25 * h, seed=4)
+    o = make(hcc, oracle, abi, cl, hcc.LinearAdvection(tuple((1.0,) for _ in range(D))))
+    counts, idx, w, dist = o.neighbours()
+    np.testing.assert_array_equal(o.neighbour_counts(), counts)
+    start = np.concatenate([[0], np.cumsum(counts)])
+    ids = np.random.default_rng(1).choice(cl.n, 50, replace=False)
+    mx = int(counts.max())
+    c2, i2, w2, d2 = o.neighbours_of(ids, mx)
+    for q, i in enumerate(ids):
+        c = counts[i]
+        assert c2[q] == c
+        np.testing.assert_array_equal(i2[q, :c], idx[start[i]:start[i + 1]])
+        assert np.array_equal(w2[q, :c], w[start[i]:start[i + 1]])
+        assert np.array_equal(d2[q, :c], dist[start[i]:start[i + 1]])
+    with pytest.raises(Exception):
+        o.neighbours_of(ids, int(counts[ids].max()) - 1)   # a row shorter than a count is refused
+
+
 def test_morton_numbering_is_z_order(hcc):
     """Reordering.jl:55-102: the permutation sorts by interleaved 16-bit keys (2-D)."""
     cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), 0.05, 0.125, jitter=0.01, seed=4)
