@@ -1,19 +1,23 @@
 """Throughput of the explicit right-hand-side path: point-updates/s per RK stage.
 
-Workload (default): 2-D compressible Euler, gamma 1.4, on [0,1]^2, jittered lattice h = 1e-3 (±0.25h), about 1.0M
-interior particles plus ghosts; four-quadrant Riemann initial state split at (0.5, 0.5); transmissive (outflow)
-boundaries; MUSCL order 2 with the MLS divergence fit of order 2; MOOD (EPD1, MOODu1 with delta = 1e-4 h^2);
+Workload (default, `euler3d_blast_8M`): 3-D compressible Euler, gamma 1.4, on [0,1]^3, jittered lattice h = 1/200
+(±0.25h), 8.0M interior particles plus 0.85M ghosts, about 66 neighbours each within R = 2.5h; spherical blast
+(rho = 1, p = 1 for r < 0.2 about the centre, else rho = 0.125, p = 0.1, zero velocity); transmissive (outflow)
+boundaries; MUSCL order 2 with the MLS divergence fit of order 2; MOOD (EPD1, MOODu1 with delta = 1e-4 h^3);
 Rusanov flux; SSP-RK3; dt = 0.4 x the CFL step at the initial state. Synthetic, seeded inputs (no dataset).
 
 `value` is the FP32 bulk path with the learned troubled-point predictor attached (the headline; the plain FP32
-path is `fp32_plain`), measured with the state resident in HBM; `e2e` is the same metric through the C ABI with
-host buffers (state uploaded from pinned memory and downloaded every step); `fp64_plain` is the plain FP64 path on
-the same cloud; `accuracy_vs_finer_fp64` compares the density L1 errors of the three against an FP64 run at h/2.
-`roofline` rates the flux pass (and, under `roofline.gather`, the reconstruction pre-pass) against the measured HBM
-copy peak. Every context is tuned by `hcc_autotune` before its timed region (`--no-autotune`: default shapes).
-`euler3d_blast_8M` and `ensemble` add the 3-D blast (with its own equal-L1 study at 1.0M) and the 512-cloud
-batched ensemble. `cpu_baseline` times the CPU oracle (the C++ restatement of the reference's CPU path) on a
-bounded sample of the same workload. `--impl reference` runs only that CPU path.
+path is `fp32_plain`), measured over --steps steps after --warmup warm-up steps with the state resident in HBM;
+`e2e` is the same metric through the C ABI with host buffers (state uploaded from pinned memory and downloaded every
+step); `fp64_plain` is the plain FP64 path on the same cloud over the same --steps/--warmup. `roofline` rates the
+flux pass (and, under `roofline.gather`, the reconstruction pre-pass) against the measured HBM copy peak, with the
+DRAM bytes per point-stage of the committed ncu capture (`profiles/traffic.txt`) as `traffic`. Every FP32 context is
+tuned by `hcc_autotune` before its timed region (`--no-autotune`: default shapes). `euler2d_quadrant_1M`,
+`published_case` and `ensemble` add the 2-D quadrant Riemann problem at 1.0M interior particles, the reference's own
+benchmark case and the 512-cloud batched ensemble. `cpu_baseline` times the CPU oracle (the C++ restatement of the
+reference's CPU path) on a bounded sample of the same workload; `--impl reference` runs only that CPU path.
+`--study accuracy` runs the equal-L1 study at the configurations' end times instead (minutes; not part of the
+default run).
 
 Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under torch.distributed.run (one rank per GPU,
 independent replicas: the path does not shard).
@@ -336,54 +340,64 @@ def load_predictor(hcc):
     return pred
 
 
+# One threshold for every workload, chosen on the training run's held-out rows (not on a test metric): the lowest
+# evaluated threshold whose held-out precision reaches 0.97 (0.974 at 0.9; a wrong pre-lowering costs accuracy, a
+# missed one only a MOOD recompute).
 PREDICTOR_THRESHOLD = 0.9
-# the 2-D-trained network on 3-D stencils: a higher threshold keeps the density L1 error within 1.1x of FP64's
-# (1.095x at 0.95 against 1.105x at 0.9 on the 1.0M blast after 10 steps)
-PREDICTOR_THRESHOLD_3D = 0.95
 
 
-def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, e2e=True, acc_dt=None, acc_steps=0,
-            predictor=None, threshold=None):
-    """One precision on one workload: K device-timed steps (the step graph, no profiling), the same K steps again
-    with per-kernel CUDA events (host-driven step) for the roofline, the end-to-end C-ABI leg, and — when asked —
-    `acc_steps` steps from the initial state with a fixed dt whose final density is returned for the L1 check.
-    With a predictor, every step pre-lowers the particles it predicts troubled (MOOD still judges all)."""
+def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, *, e2e_steps=None, profile_steps=None,
+            acc_dt=None, acc_steps=0, predictor=None, autotune=None):
+    """One precision on one workload: `warmup` untimed steps, `steps` device-timed steps (the step graph, no
+    profiling), `profile_steps` steps again with per-kernel CUDA events (host-driven) for the roofline, `e2e_steps`
+    steps of the end-to-end C-ABI leg, and -- when asked -- `acc_steps` steps from the initial state with a fixed dt
+    whose final density is returned for the L1 checks. With a predictor, every step pre-lowers the particles it
+    predicts troubled (MOOD still judges every particle)."""
     f32 = prec == "fp32"
+    e2e_steps = steps if e2e_steps is None else e2e_steps
+    profile_steps = steps if profile_steps is None else profile_steps
+    autotune = (AUTOTUNE and f32) if autotune is None else autotune
     ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
     if predictor is not None:
-        ctx.set_predictor(predictor, PREDICTOR_THRESHOLD if threshold is None else threshold)
+        ctx.set_predictor(predictor, PREDICTOR_THRESHOLD)
     if HOST_DRIVEN:
         ctx.set_step_graphs(False)
+    t0 = time.perf_counter()
     ctx.upload_cloud(cloud)
     ctx.build_neighbours()
     ctx.prepare_geometry()
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t0
     U_in = U0.astype(np.float32) if f32 else U0
     ctx.upload_state(U_in)
     dt = 0.4 * ctx.time_step()
-    for _ in range(warmup):
-        ctx.step(0.0, dt)
-    ctx.upload_state(U_in)
-    tune = ctx.autotune(dt, steps=3) if AUTOTUNE else None
-    with ClockSampler(local) as clk:
-        ms, launches = time_device_steps(hcc, ctx, dt, steps, world)
-    cnt = ctx.counters()
-    ctx.upload_state(U_in)
-    ctx.set_profiling(True)
-    ctx.kernel_times(reset=True)
-    for _ in range(steps):
-        ctx.step(0.0, dt)
-    ctx.synchronize()
-    ctx.set_profiling(False)
-    kt = ctx.kernel_times(reset=True)
-    out = {"ms": ms, "launches": launches, "kt": kt, "clocks": clk.summary(), "counters": cnt, "dt": dt,
-           "tuning": tune}
-    if e2e:
-        out["e2e_s"], out["h2d"], out["d2h"] = time_e2e(hcc, ctx, U0, dt, steps, world, f32)
+    tune = ctx.autotune(dt, steps=3) if autotune and steps > 0 else None
+    out = {"dt": dt, "tuning": tune, "setup_s": setup_s}
+    if steps > 0:
+        ctx.upload_state(U_in)
+        for _ in range(warmup):
+            ctx.step(0.0, dt)
+        with ClockSampler(local) as clk:
+            ms, launches = time_device_steps(hcc, ctx, dt, steps, world)
+        out.update({"ms": ms, "launches": launches, "clocks": clk.summary(), "counters": ctx.counters()})
+    if profile_steps > 0:
+        ctx.upload_state(U_in)
+        ctx.set_profiling(True)
+        ctx.kernel_times(reset=True)
+        for _ in range(profile_steps):
+            ctx.step(0.0, dt)
+        ctx.synchronize()
+        ctx.set_profiling(False)
+        out["kt"] = ctx.kernel_times(reset=True)
+    if e2e_steps > 0:
+        out["e2e_s"], out["h2d"], out["d2h"] = time_e2e(hcc, ctx, U0, dt, e2e_steps, world, f32)
+        out["e2e_steps"] = e2e_steps
     if acc_steps:
         ctx.upload_state(U_in)
         for _ in range(acc_steps):
             ctx.step(0.0, dt if acc_dt is None else acc_dt)
         out["rho"] = ctx.download_state(dtype=np.float64)[:, 0].copy()
+        out["acc_counters"] = ctx.counters()
     ctx.close()
     return out
 
@@ -392,86 +406,69 @@ def rel_l1(a, b, sel):
     return float(np.abs(a[sel] - b[sel]).sum() / np.abs(b[sel]).sum())
 
 
-def fine_reference(hcc, cloud, h, dt, steps):
-    """Density of the plain FP64 path on the same problem at spacing h/2 after 2*steps steps of dt/2 (the same
-    final time), sampled at the particles of `cloud` (nearest fine particle): the reference of the L1 errors."""
-    from scipy.spatial import cKDTree
-    D = cloud.pos.shape[1]
-    fine = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h / 2, 2.5 * h / 2, jitter=0.25 * h / 2, seed=42)
-    ctx = hcc.Context(make_cfg(hcc, fine, h / 2, "fp64"))
-    ctx.upload_cloud(fine)
-    ctx.build_neighbours()
-    ctx.prepare_geometry()
-    ctx.upload_state(quadrant_state(fine) if D == 2 else blast_state(fine))
-    for _ in range(2 * steps):
-        ctx.step(0.0, dt / 2)
-    rho = ctx.download_state()[:, 0].copy()
-    ctx.close()
-    _, idx = cKDTree(fine.pos).query(cloud.pos)
-    return rho[idx]
+def per_launch(kt, name):
+    return kt[f"{name}_ms"] / max(kt[f"{name}_launches"], 1)
 
 
-def run_3d(hcc, args, world, local):
-    """The 3-D Euler blast at 8.0M interior particles (K ~ 67): FP32 bulk and FP64 plain step rates and the FP32
-    density's relative L1 distance from the FP64 run after the same steps; and the density L1 errors of FP64, FP32
-    and FP32 + predictor at 1.0M interior against the FP64 path at h/2."""
-    name = "euler3d_blast_8M"
-    cloud, U0, h = make_workload(hcc, name)
-    n_int = cloud.n_interior
-    steps32, steps64, acc = max(3, min(args.steps, 10)), 2, 5
-    r32 = measure(hcc, cloud, U0, h, "fp32", steps32, 2, world, local, e2e=False)
-    dt = r32["dt"]
-    r32a = measure(hcc, cloud, U0, h, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt, acc_steps=acc)
-    r64 = measure(hcc, cloud, U0, h, "fp64", steps64, 1, world, local, e2e=False, acc_dt=dt, acc_steps=acc)
-    inner = cloud.is_boundary == 0
-    K = r32["counters"]["total_neighbours"] / max(cloud.n, 1)
-    kt = r32["kt"]
-    learned = {}
-    predictor = None if args.no_learned else load_predictor(hcc)
-    if predictor is not None:
-        # the network trained on 2-D runs, applied as-is to the 3-D stencils (MOOD still judges every particle)
-        rl = measure(hcc, cloud, U0, h, "fp32", steps32, 2, world, local, e2e=False, predictor=predictor,
-                     threshold=PREDICTOR_THRESHOLD_3D)
-        rla = measure(hcc, cloud, U0, h, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt, acc_steps=acc,
-                      predictor=predictor, threshold=PREDICTOR_THRESHOLD_3D)
-        learned = {"fp32_learned": {"threshold": PREDICTOR_THRESHOLD_3D,
-                                    "value": n_int * STAGES * steps32 * world / (rl["ms"] / 1e3),
-                                    "ms_per_step": rl["ms"] / steps32,
-                                    "mood_iterations_last_step": rl["counters"]["mood_iterations"],
-                                    "predicted_last_step": rl["counters"]["predicted"], "clocks": rl["clocks"]},
-                   "l1_density_learned_vs_fp64": {"value": rel_l1(rla["rho"], r64["rho"], inner), "steps": acc,
-                                                  "dt": dt}}
-    accuracy = {}
-    if not args.no_reference_solution:
-        # equal-L1 check in 3-D: the blast at h = 1/100 (1.0M interior) in FP64, FP32 and FP32 + predictor against
-        # the FP64 path at h/2 (8.0M interior, twice the steps at dt/2)
-        c1, u1, h1 = make_workload(hcc, "euler3d_blast_1M")
-        steps1 = 10
-        a64 = measure(hcc, c1, u1, h1, "fp64", 1, 0, world, local, e2e=False, acc_steps=steps1)
-        dt1 = a64["dt"]
-        a32 = measure(hcc, c1, u1, h1, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt1, acc_steps=steps1)
-        ref = fine_reference(hcc, c1, h1, dt1, steps1)
-        in1 = c1.is_boundary == 0
-        accuracy = {"reference": "FP64 plain at h/2 (8x the particles), 2x the steps at dt/2, nearest fine particle",
-                    "workload": "euler3d_blast_1M", "steps": steps1, "dt": dt1,
-                    "l1_fp64": rel_l1(a64["rho"], ref, in1), "l1_fp32": rel_l1(a32["rho"], ref, in1)}
-        accuracy["fp32_over_fp64"] = accuracy["l1_fp32"] / accuracy["l1_fp64"]
-        if predictor is not None:
-            al = measure(hcc, c1, u1, h1, "fp32", 1, 0, world, local, e2e=False, acc_dt=dt1, acc_steps=steps1,
-                         predictor=predictor, threshold=PREDICTOR_THRESHOLD_3D)
-            accuracy["l1_fp32_learned"] = rel_l1(al["rho"], ref, in1)
-            accuracy["learned_over_fp64"] = accuracy["l1_fp32_learned"] / accuracy["l1_fp64"]
-        accuracy = {"accuracy_vs_finer_fp64": accuracy}
-    return {"workload": name, "description": WORKLOADS[name][2], "n_particles": cloud.n, "n_interior": n_int,
-            "mean_neighbours": K,
-            "fp32": {"value": n_int * STAGES * steps32 * world / (r32["ms"] / 1e3), "ms_per_step": r32["ms"] / steps32,
-                     "flux_ms_per_launch": kt["flux_ms"] / max(kt["flux_launches"], 1),
-                     "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
-                     "mood_iterations_last_step": r32["counters"]["mood_iterations"], "clocks": r32["clocks"]},
-            "fp64_plain": {"value": n_int * STAGES * steps64 * world / (r64["ms"] / 1e3),
-                           "ms_per_step": r64["ms"] / steps64, "clocks": r64["clocks"]},
-            "l1_density_fp32_vs_fp64": {"value": rel_l1(r32a["rho"], r64["rho"], inner), "steps": acc, "dt": dt},
-            **learned, **accuracy}
+def roofline_of(workload, D, M, K, n_int, kt, peak, peak_kind):
+    """The flux pass (dominant kernel) and the reconstruction pre-pass against the HBM copy peak: algorithmic bytes
+    per point-stage x interior points / CUDA-event launch time; `traffic` = the ncu DRAM bytes per point-stage of
+    profiles/traffic.txt for this workload, scaled to the launch."""
+    flux_b, gather_b = algorithmic_bytes(K, D, M, D, D + 1, 4)
+    rec = recorded_traffic()
+    flux_ms, gather_ms = per_launch(kt, "flux"), per_launch(kt, "gather")
+    achieved = flux_b * n_int / (flux_ms / 1e3) / 1e9
+    traffic = rec.get(f"flux_f32_{workload}_bytes_per_point_stage")
+    g_traffic = rec.get(f"gather_f32_{workload}_bytes_per_point_stage")
+    g_model = gather_b * n_int / (gather_ms / 1e3) / 1e9
+    gather_roof = {"kernel": f"k_gather<float,{D},{M},EULER,1>", "bound": "hbm", "unit": "GB/s", "peak": peak,
+                   "achieved": g_model, "frac": g_model / peak,
+                   "traffic": (g_traffic * n_int) if g_traffic else None,
+                   "dram_achieved": (g_traffic * n_int / (gather_ms / 1e3) / 1e9) if g_traffic else None,
+                   "dram_frac": (g_traffic * n_int / (gather_ms / 1e3) / 1e9 / peak) if g_traffic else None,
+                   "ms_per_launch": gather_ms}
+    return {"bound": "hbm", "kernel": f"k_flux<float,{D},{M},EULER,1>", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+            if peak_kind == "measured" else peak_kind,
+            "traffic": (traffic * n_int) if traffic else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per point-stage (profiles/traffic.txt)"
+                              " x interior points",
+            "algorithmic_bytes_per_point_stage": {"flux": flux_b, "gather": gather_b},
+            "flux_ms_per_launch": flux_ms, "gather_ms_per_launch": gather_ms,
+            "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
+            "predict_ms_per_step": kt["predict_ms"] / max(kt["steps"], 1),
+            "kernel_times": "CUDA events on the context's stream around each launch of a separate host-driven run "
+                            "of the same steps",
+            "gather": gather_roof}
+
+
+def fp64_roofline(D, M, K, n_int, kt, fp64_peak):
+    """The FP64 flux pass against the FP64 pipe: FP64 operations per slot counted from the source (fp64_flops_per_slot)
+    x slots / CUDA-event launch time."""
+    if not kt or not kt.get("flux_launches"):
+        return None
+    flops = fp64_flops_per_slot(D, M)
+    ms = per_launch(kt, "flux")
+    achieved = flops * K * n_int / (ms / 1e3) / 1e12
+    return {"bound": "fp64", "kernel": f"k_flux<double,{D},{M},EULER,1>", "flops_per_slot": flops,
+            "achieved": achieved, "unit": "TFLOP/s", "peak": fp64_peak.get("tflops") if fp64_peak else None,
+            "frac": (achieved / fp64_peak["tflops"]) if fp64_peak and fp64_peak.get("tflops") else None,
+            "peak_source": fp64_peak.get("source") if fp64_peak else None, "flux_ms_per_launch": ms,
+            "gather_ms_per_launch": per_launch(kt, "gather")}
+
+
+def fp64_flops_per_slot(D, M):
+    """FP64 operations (an FMA counts 2, a division or square root 1) of one slot of the FP64 MUSCL2 Euler flux pass
+    (flux_one in hcc_stage_impl.cuh, compiled without contraction): two interface reconstructions (2 M D mul+add),
+    two Euler flux/speed evaluations (each: 1 div, D mul + D-1 fma-pairs for |u|^2, 3 for p, 1 div + 1 sqrt + 2 mul
+    for c, D(D+1) + 2D + D products for F, 2D for lambda), per axis the Rusanov flux (max, M jumps, M x 5) and the
+    weighted accumulation (2 M D), the extrema (2 M)."""
+    recon = 2 * (2 * M * D)
+    euler = 2 * (1 + D + 2 * (D - 1) + 1 + 3 + 4 + D * (D + 1) + 2 * D + D + 2 * D)
+    rusanov = D * (1 + M * 5)
+    accum = 2 * M * D + M
+    extrema = 2 * M
+    return recon + euler + rusanov + accum + extrema
 
 
 def run_ensemble(hcc, args, world, local):
@@ -591,118 +588,296 @@ def run_gpu(args):
         _load("hcc_gb300_build", PKG / "build.py").build()
     import torch
     torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
     cloud, U0, h = make_workload(hcc, args.workload)
+    t_gen = time.perf_counter() - t_gen
     D = cloud.pos.shape[1]
+    M = D + 2
     n_int = cloud.n_interior
-    results = {}
-    acc_steps, acc_dt = 10, None
+    inner = cloud.is_boundary == 0
+    K_steps, W = args.steps, args.warmup
     predictor = None if args.no_learned else load_predictor(hcc)
-    arms = ["fp32", "fp64"] if not args.fp32_only else ["fp32"]
-    if predictor is not None:
-        arms = ["fp32_learned"] + arms
+    fp64_steps = K_steps if args.fp64_steps is None else args.fp64_steps
+    # the headline arm first; each arm also runs `acc` steps from the initial state at one shared dt (the first
+    # arm's) for the density L1 distances between the arms
+    acc, acc_dt = 5, None
+    arms = (["fp32_learned"] if predictor is not None else []) + ["fp32"] + ([] if args.fp32_only else ["fp64"])
+    res = {}
     for arm in arms:
         prec = "fp64" if arm == "fp64" else "fp32"
-        pr = predictor if arm == "fp32_learned" else None
-        results[arm] = measure(hcc, cloud, U0, h, prec, args.steps, args.warmup, world, local,
-                               acc_dt=acc_dt, acc_steps=acc_steps if acc_dt else 0, predictor=pr)
+        kw = {}
+        if prec == "fp64":          # ~1.4 s a step at 8M: no tuning (launch shapes are FP32 choices), short legs
+            kw = {"profile_steps": min(fp64_steps, 2), "e2e_steps": min(fp64_steps, 2)}
+        r = measure(hcc, cloud, U0, h, prec, fp64_steps if prec == "fp64" else K_steps, W if prec == "fp32" else
+                    min(W, 3), world, local, acc_dt=acc_dt, acc_steps=acc,
+                    predictor=predictor if arm == "fp32_learned" else None, **kw)
         if acc_dt is None:
-            acc_dt = results[arm]["dt"]
-            r = measure(hcc, cloud, U0, h, prec, 1, 0, world, local, e2e=False, acc_dt=acc_dt, acc_steps=acc_steps,
-                        predictor=pr)
-            results[arm]["rho"] = r["rho"]
-    head = "fp32_learned" if predictor is not None else "fp32"
-    r = results[head]
-    units = n_int * STAGES * args.steps * world
+            acc_dt = r["dt"]                 # the first arm's acc run used its own dt: the shared one
+        res[arm] = r
+    head = arms[0] if not args.fp32_only or predictor is not None else "fp32"
+    r = res[head]
+    units = n_int * STAGES * K_steps * world
     value = units / (r["ms"] / 1e3)
     cnt = r["counters"]
     K = cnt["total_neighbours"] / max(cloud.n, 1)
-    M = D + 2
-    flux_b, gather_b = algorithmic_bytes(K, D, M, D, D + 1, 4)
     peak, peak_kind = measured_peaks()
-    kt = r["kt"]
-    flux_ms = kt["flux_ms"] / max(kt["flux_launches"], 1)
-    achieved = flux_b * n_int / (flux_ms / 1e3) / 1e9
-    traffic = recorded_traffic().get("flux_f32_euler2d_bytes_per_point_stage") if D == 2 else None
-    # the reconstruction pre-pass against the same peak: model bytes, and the DRAM bytes of its ncu capture
-    gather_ms = kt["gather_ms"] / max(kt["gather_launches"], 1)
-    g_traffic = recorded_traffic().get("gather_f32_euler2d_bytes_per_point_stage") if D == 2 else None
-    g_model = gather_b * n_int / (gather_ms / 1e3) / 1e9
-    gather_roof = {"kernel": f"k_gather<float,{D},{M},EULER,1>", "bound": "hbm", "unit": "GB/s", "peak": peak,
-                   "achieved": g_model, "frac": g_model / peak,
-                   "dram_achieved": (g_traffic * n_int / (gather_ms / 1e3) / 1e9) if g_traffic else None,
-                   "dram_frac": (g_traffic * n_int / (gather_ms / 1e3) / 1e9 / peak) if g_traffic else None,
-                   "note": "achieved: model bytes / live launch time; dram_achieved: ncu DRAM bytes per point-stage "
-                           "(profiles/traffic.txt) x N_interior / live launch time"}
     line = {
-        "metric": METRIC, "value": value, "unit": "point-updates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "point-updates/s", "n_gpus": world, "steps": K_steps,
+        "warmup": W, "ms_per_step": r["ms"] / K_steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
                    "n_particles": cloud.n, "n_interior": n_int, "mean_neighbours": K, "stages_per_step": STAGES,
-                   "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": predictor is not None,
+                   "precision": "FP32 bulk (FP64 MLS assembly/Cholesky)", "learned_mood": head == "fp32_learned",
                    "predictor": ({"weights": "hypercloudcore.jl_gb300/predictor_euler2d.npz (train_predictor.py: "
                                   "200 seeded Voronoi runs at 250k nodes to t = 0.2)",
-                                  "threshold": PREDICTOR_THRESHOLD} if predictor is not None else None),
+                                  "threshold": PREDICTOR_THRESHOLD,
+                                  "threshold_rule": "lowest held-out threshold with precision >= 0.97"}
+                                 if head == "fp32_learned" else None),
                    "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
-                   "l2": "inputs larger than L2 (per-slot arrays ~0.5 GB)", "parallelism": f"replicas x{world}",
-                   "dt": r["dt"], "launch_shapes": r["tuning"]},
+                   "l2": "inputs larger than L2 (per-slot neighbour arrays of several GB)",
+                   "parallelism": f"replicas x{world}", "dt": r["dt"], "launch_shapes": r["tuning"],
+                   "setup_s": r["setup_s"], "cloud_generation_s": t_gen},
         "gpu_launches": r["launches"],
-        "e2e": {"value": units / r["e2e_s"], "unit": "point-updates/s", "h2d_bytes_per_step": r["h2d"],
-                "d2h_bytes_per_step": r["d2h"]},
-        "roofline": {"bound": "hbm", "kernel": f"k_flux<float,{D},{M},EULER,1>", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": (traffic * n_int) if traffic else None,
-                     "algorithmic_bytes_per_point_stage": {"flux": flux_b, "gather": gather_b},
-                     "flux_ms_per_launch": flux_ms,
-                     "gather_ms_per_launch": kt["gather_ms"] / max(kt["gather_launches"], 1),
-                     "recompute_ms_total": kt["recompute_ms"], "recompute_launches": kt["recompute_launches"],
-                     "predict_ms_per_step": kt["predict_ms"] / max(kt["steps"], 1),
-                     "kernel_times": "CUDA events around each launch of a separate host-driven run of the same steps",
-                     "gather": gather_roof},
+        "e2e": {"value": n_int * STAGES * r["e2e_steps"] * world / r["e2e_s"], "unit": "point-updates/s",
+                "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"], "steps": r["e2e_steps"]},
+        "roofline": roofline_of(args.workload, D, M, K, n_int, r["kt"], peak, peak_kind),
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],
                  "predicted_last_step": cnt.get("predicted", 0)},
     }
     if head != "fp32":
-        r0 = results["fp32"]
-        line["fp32_plain"] = {"value": units / (r0["ms"] / 1e3), "ms_per_step": r0["ms"] / args.steps,
-                              "e2e": units / r0["e2e_s"], "gpu_launches": r0["launches"],
+        r0 = res["fp32"]
+        line["fp32_plain"] = {"value": units / (r0["ms"] / 1e3), "ms_per_step": r0["ms"] / K_steps,
+                              "e2e": n_int * STAGES * r0["e2e_steps"] * world / r0["e2e_s"],
+                              "gpu_launches": r0["launches"], "clocks": r0["clocks"],
+                              "flux_ms_per_launch": per_launch(r0["kt"], "flux"),
+                              "gather_ms_per_launch": per_launch(r0["kt"], "gather"),
                               "mood": {"flagged_last_step": r0["counters"]["mood_flagged"],
                                        "iterations_last_step": r0["counters"]["mood_iterations"]}}
-    if "fp64" in results:
-        r64 = results["fp64"]
-        line["fp64_plain"] = {"value": units / (r64["ms"] / 1e3), "ms_per_step": r64["ms"] / args.steps,
-                              "flux_ms_per_launch": r64["kt"]["flux_ms"] / max(r64["kt"]["flux_launches"], 1),
-                              "gather_ms_per_launch": r64["kt"]["gather_ms"] / max(r64["kt"]["gather_launches"], 1),
-                              "e2e": units / r64["e2e_s"], "clocks": r64["clocks"]}
+        line["learned_over_plain"] = line["value"] / line["fp32_plain"]["value"]
+    if "fp64" in res:
+        r64 = res["fp64"]
+        u64 = n_int * STAGES * fp64_steps * world
+        line["fp64_plain"] = {"value": u64 / (r64["ms"] / 1e3), "ms_per_step": r64["ms"] / fp64_steps,
+                              "steps": fp64_steps, "warmup": min(W, 3),
+                              "e2e": n_int * STAGES * r64["e2e_steps"] * world / r64["e2e_s"],
+                              "clocks": r64["clocks"], "setup_s": r64["setup_s"],
+                              "roofline": fp64_roofline(D, M, K, n_int, r64.get("kt"), fp64_peak(hcc))}
         line["fp32_over_fp64"] = line["value"] / line["fp64_plain"]["value"]
-        inner = cloud.is_boundary == 0
-        line["l1_density_fp32_vs_fp64"] = {"value": rel_l1(results["fp32"]["rho"], r64["rho"], inner),
-                                           "steps": acc_steps, "dt": acc_dt,
-                                           "note": "relative L1 over interior particles, same dt"}
-        if head != "fp32":
-            line["l1_density_learned_vs_fp64"] = {"value": rel_l1(r["rho"], r64["rho"], inner), "steps": acc_steps,
-                                                  "dt": acc_dt}
-        if not args.no_reference_solution and D == 2:
-            ref = fine_reference(hcc, cloud, h, acc_dt, acc_steps)
-            acc = {"reference": "FP64 plain at h/2 (4x the particles), 2x the steps at dt/2, nearest fine particle",
-                   "steps": acc_steps, "l1_fp64": rel_l1(r64["rho"], ref, inner),
-                   "l1_fp32": rel_l1(results["fp32"]["rho"], ref, inner)}
-            if head != "fp32":
-                acc["l1_fp32_learned"] = rel_l1(r["rho"], ref, inner)
-                acc["learned_over_fp64"] = acc["l1_fp32_learned"] / acc["l1_fp64"]
-            acc["fp32_over_fp64"] = acc["l1_fp32"] / acc["l1_fp64"]
-            line["accuracy_vs_finer_fp64"] = acc
+        for arm in arms:
+            if arm != "fp64":
+                line[f"l1_density_{arm}_vs_fp64"] = {"value": rel_l1(res[arm]["rho"], r64["rho"], inner),
+                                                     "steps": acc, "dt": acc_dt,
+                                                     "note": "relative L1 over interior particles, same dt"}
+    rec = recorded_accuracy()
+    if rec:
+        line["accuracy_vs_finer_fp64"] = rec
+    if not args.no_2d and D == 3:
+        line["euler2d_quadrant_1M"] = run_secondary(hcc, args, world, local, "euler2d_quadrant_1M", predictor,
+                                                    peak, peak_kind)
     if not args.no_published:
-        line["published_case"] = run_published_case(hcc, args.steps)
-    if not args.no_3d and D == 2:
-        line["euler3d_blast_8M"] = run_3d(hcc, args, world, local)
-    if not args.no_ensemble and D == 2:
+        line["published_case"] = run_published_case(hcc, K_steps)
+    if not args.no_ensemble:
         line["ensemble"] = run_ensemble(hcc, args, world, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(hcc, cloud, U0, h, args.cpu_steps)
+        line["cpu_baseline"] = cpu_baseline(hcc, args.workload, args.cpu_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_secondary(hcc, args, world, local, name, predictor, peak, peak_kind):
+    """Another workload in the same line: FP32 (+ predictor) and FP64 step rates, the flux roofline."""
+    cloud, U0, h = make_workload(hcc, name)
+    D = cloud.pos.shape[1]
+    n_int = cloud.n_interior
+    K_steps = args.steps
+    out = {"workload": name, "description": WORKLOADS[name][2], "n_particles": cloud.n, "n_interior": n_int}
+    for arm in (["fp32_learned"] if predictor is not None else []) + ["fp32", "fp64"]:
+        prec = "fp64" if arm == "fp64" else "fp32"
+        r = measure(hcc, cloud, U0, h, prec, K_steps, args.warmup, world, local, e2e_steps=0,
+                    profile_steps=min(K_steps, 3) if prec == "fp64" else K_steps,
+                    predictor=predictor if arm == "fp32_learned" else None)
+        units = n_int * STAGES * K_steps * world
+        K = r["counters"]["total_neighbours"] / max(cloud.n, 1)
+        out[arm] = {"value": units / (r["ms"] / 1e3), "ms_per_step": r["ms"] / K_steps, "clocks": r["clocks"],
+                    "mood_iterations_last_step": r["counters"]["mood_iterations"]}
+        if prec == "fp32":
+            out[arm]["roofline"] = roofline_of(name, D, D + 2, K, n_int, r["kt"], peak, peak_kind)
+        else:
+            out[arm]["roofline"] = fp64_roofline(D, D + 2, K, n_int, r.get("kt"), fp64_peak(hcc))
+        out["mean_neighbours"] = K
+    return out
+
+
+def recorded_accuracy():
+    """The equal-L1 study's last recorded result (profiles/accuracy_equal_l1.json, written by --study accuracy)."""
+    p = ROOT / "profiles" / "accuracy_equal_l1.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    d["source"] = "recorded by `python bench.py --study accuracy` (profiles/accuracy_equal_l1.json)"
+    return d
+
+
+_FP64_PEAK = {}
+
+
+def fp64_peak(hcc):
+    """The FP64 FMA rate of this GPU, measured once per run (hcc_fp64_fma_rate)."""
+    if "tflops" not in _FP64_PEAK:
+        try:
+            _FP64_PEAK["tflops"] = hcc.fp64_fma_rate()
+            _FP64_PEAK["source"] = "measured: hcc_fp64_fma_rate (FP64 FMA chains on every SM, CUDA events)"
+        except Exception as e:        # noqa: BLE001 - the roofline then has no peak
+            _FP64_PEAK["tflops"] = None
+            _FP64_PEAK["source"] = f"unavailable: {e}"
+    return _FP64_PEAK
+
+
+# --------------------------------------------------------------------------------------------- equal-L1 study
+def radial_blast_reference(t_end, r_query, gamma=1.4, n=10000, r_max=0.9):
+    """Density of the spherical blast (rho = 1, p = 1 for r < 0.2, else 0.125 / 0.1, at rest) at time t_end and radii
+    r_query, from a fine 1-D solve in spherical symmetry (FP64): finite volumes on n cells of [0, r_max] with the
+    geometric pressure source, minmod-limited linear reconstruction, Rusanov fluxes, SSP-RK3 at CFL 0.4, mirror
+    condition at r = 0 and transmissive at r_max. Valid while the outer wave stays inside the unit cube's inscribed
+    ball (t_end well below 0.15)."""
+    dr = r_max / n
+    rf = np.arange(n + 1) * dr
+    rc = 0.5 * (rf[:-1] + rf[1:])
+    A = rf ** 2
+    V = (rf[1:] ** 3 - rf[:-1] ** 3) / 3.0
+    dA = A[1:] - A[:-1]
+    rho = np.where(rc < 0.2, 1.0, 0.125)
+    pr = np.where(rc < 0.2, 1.0, 0.1)
+    U = np.stack([rho, np.zeros(n), pr / (gamma - 1)])
+    mirror = np.array([[1.0], [-1.0], [1.0]])
+
+    def prim(U):
+        r = U[0]
+        u = U[1] / r
+        return r, u, (gamma - 1) * (U[2] - 0.5 * r * u * u)
+
+    def minmod(a, b):
+        return np.where(a * b > 0, np.sign(a) * np.minimum(np.abs(a), np.abs(b)), 0.0)
+
+    def flux(r, u, p):
+        E = p / (gamma - 1) + 0.5 * r * u * u
+        return np.stack([r, r * u, u * r * u + p, u * (E + p)]), np.stack([r * u, r * u * u + p, u * (E + p)])
+
+    def rhs(U):
+        r, u, p = prim(U)
+        W = np.stack([r, u, p])
+        Wg = np.concatenate([W[:, 1::-1] * mirror, W, np.repeat(W[:, -1:], 2, axis=1)], axis=1)
+        d = np.diff(Wg, axis=1)
+        s = minmod(d[:, :-1], d[:, 1:])                  # slopes of columns 1 .. n+2
+        WL = Wg[:, 1:n + 2] + 0.5 * s[:, 0:n + 1]        # faces 0 .. n
+        WR = Wg[:, 2:n + 3] - 0.5 * s[:, 1:n + 2]
+        cL, FL = flux(WL[0], WL[1], WL[2])
+        cR, FR = flux(WR[0], WR[1], WR[2])
+        UL = np.stack([WL[0], WL[0] * WL[1], WL[2] / (gamma - 1) + 0.5 * WL[0] * WL[1] ** 2])
+        UR = np.stack([WR[0], WR[0] * WR[1], WR[2] / (gamma - 1) + 0.5 * WR[0] * WR[1] ** 2])
+        sm = np.maximum(np.abs(WL[1]) + np.sqrt(gamma * WL[2] / WL[0]), np.abs(WR[1]) + np.sqrt(gamma * WR[2] / WR[0]))
+        F = 0.5 * (FL + FR) - 0.5 * sm * (UR - UL)
+        AF = A * F
+        out = -(AF[:, 1:] - AF[:, :-1]) / V
+        out[1] += p * dA / V
+        return out
+
+    t = 0.0
+    while t < t_end:
+        r, u, p = prim(U)
+        dt = min(0.4 * dr / np.max(np.abs(u) + np.sqrt(gamma * p / r)), t_end - t)
+        U1 = U + dt * rhs(U)
+        U2 = 0.75 * U + 0.25 * (U1 + dt * rhs(U1))
+        U = U / 3.0 + 2.0 / 3.0 * (U2 + dt * rhs(U2))
+        t += dt
+    return np.interp(r_query, rc, U[0])
+
+
+def run_cfl_steps(hcc, cloud, U0, h, prec, dts=None, steps=None, t_end=None, predictor=None):
+    """Steps from the initial state: with `dts`, exactly those step sizes; otherwise dt = 0.4 x the CFL step of the
+    current state until `steps` steps or time `t_end`. Returns (density, the dt sequence, MOOD flags summed over the
+    steps, seconds)."""
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+    if predictor is not None:
+        ctx.set_predictor(predictor, PREDICTOR_THRESHOLD)
+    ctx.upload_cloud(cloud)
+    ctx.build_neighbours()
+    ctx.prepare_geometry()
+    ctx.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
+    seq, t, flagged = [], 0.0, 0
+    t0 = time.perf_counter()
+    while True:
+        if dts is not None:
+            if len(seq) == len(dts):
+                break
+            dt = dts[len(seq)]
+        else:
+            if (steps is not None and len(seq) == steps) or (t_end is not None and t >= t_end * (1 - 1e-14)):
+                break
+            dt = 0.4 * ctx.time_step()
+            if t_end is not None:
+                dt = min(dt, t_end - t)
+        ctx.step(t, dt)
+        seq.append(dt)
+        t += dt
+        flagged += ctx.counters()["mood_flagged"]
+    ctx.synchronize()
+    el = time.perf_counter() - t0
+    rho = ctx.download_state(dtype=np.float64)[:, 0].copy()
+    ctx.close()
+    return rho, seq, flagged, el
+
+
+def run_accuracy_study(args):
+    """Density L1 errors of FP64 plain, FP32 bulk and FP32 + predictor at the configurations' end times:
+    the 3-D blast at 8.0M interior particles after 200 steps (dt = 0.4 x the FP64 path's CFL step each step, the
+    same sequence replayed by the FP32 arms) against the fine 1-D radial solve at the same time; the 2-D quadrant
+    problem at 1.0M interior particles at t = 0.25 against the FP64 path at h/2 (nearest fine particle)."""
+    from scipy.spatial import cKDTree
+    hcc = package()
+    import torch
+    torch.cuda.set_device(0)
+    predictor = load_predictor(hcc)
+    out = {"threshold": PREDICTOR_THRESHOLD}
+    for name in args.study_workloads.split(","):
+        cloud, U0, h = make_workload(hcc, name)
+        D = cloud.pos.shape[1]
+        inner = cloud.is_boundary == 0
+        rec = {"workload": name}
+        rho64, dts, f64, s64 = run_cfl_steps(hcc, cloud, U0, h, "fp64",
+                                             steps=200 if D == 3 else None, t_end=None if D == 3 else 0.25)
+        t_end = float(np.sum(dts))
+        rec.update({"steps": len(dts), "t_end": t_end, "dt_first": dts[0], "dt_last": dts[-1]})
+        if D == 3:
+            r = np.sqrt(((cloud.pos - 0.5) ** 2).sum(axis=1))
+            ref = radial_blast_reference(t_end, r)
+            rec["reference"] = "1-D spherical FP64 solve (10,000 cells on [0, 0.9], Rusanov + minmod, SSP-RK3)"
+        else:
+            fine = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h / 2, 2.5 * h / 2, jitter=0.25 * h / 2, seed=42)
+            Uf = quadrant_state(fine)
+            rf, fdts, _, sf = run_cfl_steps(hcc, fine, Uf, h / 2, "fp64", t_end=t_end)
+            _, idx = cKDTree(fine.pos).query(cloud.pos)
+            ref = rf[idx]
+            rec["reference"] = (f"FP64 plain at h/2 ({fine.n} particles), its own CFL steps ({len(fdts)}) to the same "
+                                f"time, nearest fine particle")
+            rec["reference_seconds"] = sf
+        rec["l1_fp64"] = rel_l1(rho64, ref, inner)
+        rec["fp64_seconds"] = s64
+        rec["fp64_flagged_total"] = f64
+        rho32, _, f32, s32 = run_cfl_steps(hcc, cloud, U0, h, "fp32", dts=dts)
+        rec.update({"l1_fp32": rel_l1(rho32, ref, inner), "fp32_seconds": s32, "fp32_flagged_total": f32})
+        rec["fp32_over_fp64"] = rec["l1_fp32"] / rec["l1_fp64"]
+        if predictor is not None:
+            rhol, _, fl, sl = run_cfl_steps(hcc, cloud, U0, h, "fp32", dts=dts, predictor=predictor)
+            rec.update({"l1_fp32_learned": rel_l1(rhol, ref, inner), "fp32_learned_seconds": sl,
+                        "fp32_learned_flagged_total": fl})
+            rec["learned_over_fp64"] = rec["l1_fp32_learned"] / rec["l1_fp64"]
+        out[name] = rec
+        print(json.dumps({name: rec}), flush=True)
+    print(json.dumps({"accuracy_study": out}), flush=True)
+    if args.study_out:
+        Path(args.study_out).write_text(json.dumps(out, indent=1) + "\n")
 
 
 # --------------------------------------------------------------------------------------------- published case
@@ -750,14 +925,30 @@ def run_published_case(hcc, steps, n_side=1000):
 
 
 # --------------------------------------------------------------------------------------------- CPU (reference) arm
-def cpu_baseline(hcc, cloud, U0, h, steps, warmup=1):
-    """The oracle (C++ restatement of the reference CPU path, OpenMP on all host cores) on a bounded sample:
-    `steps` steps of the same cloud after `warmup` warm-up steps."""
+def reference_sample(hcc, workload):
+    """The bounded sample of a workload that the CPU path is timed on. 2-D: the whole cloud. The 3-D blast at 8.0M:
+    the sub-box [0.25, 0.75]^3 at the same spacing and support radius (1.03M interior particles, the same ~66
+    neighbours each, the same physics and scheme), which contains the whole initial blast sphere; the metric is per
+    point-update, so the sample measures the same per-point cost at a size the CPU finishes in seconds per step."""
+    D, h, _ = WORKLOADS[workload]
+    if D == 2:
+        cloud, U0, h = make_workload(hcc, workload)
+        return cloud, U0, h, f"the full {cloud.n}-particle cloud"
+    lo, hi = 0.25, 0.75
+    cloud = hcc.rectangular_cloud((lo,) * D, (hi,) * D, h, 2.5 * h, jitter=0.25 * h, seed=42)
+    return cloud, blast_state(cloud), h, (f"the sub-box [{lo}, {hi}]^3 of the workload at the same spacing "
+                                          f"({cloud.n} particles, {cloud.n_interior} interior)")
+
+
+def cpu_baseline(hcc, workload, steps, warmup=1):
+    """The oracle (C++ restatement of the reference CPU path, OpenMP on all host cores, FP64) on a bounded sample of
+    the workload: `steps` steps after `warmup` warm-up steps."""
     orc = _load("hcc_oracle_py", ROOT / "oracle" / "oracle.py")
     abi = sys.modules["hcc_gb300._abi"]
     cores = os.cpu_count() or 1
     orc.load(abi)
     orc.OracleContext.set_threads(cores)
+    cloud, U0, h, what = reference_sample(hcc, workload)
     o = orc.OracleContext(make_cfg(hcc, cloud, h, "fp64"), abi)
     o.upload_cloud(cloud)
     o.build_neighbours()
@@ -773,8 +964,7 @@ def cpu_baseline(hcc, cloud, U0, h, steps, warmup=1):
     v = cloud.n_interior * STAGES * steps / el
     o.close()
     return {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} SSP-RK3 step(s) of the full {cloud.n}-particle cloud after {warmup} warm-up "
-                      f"step(s), FP64"}
+            "sample": f"{steps} SSP-RK3 step(s) after {warmup} warm-up step(s) of {what}, FP64"}
 
 
 def run_reference(args):
@@ -783,19 +973,19 @@ def run_reference(args):
     if rank != 0:
         return
     hcc = package()
-    cloud, U0, h = make_workload(hcc, args.workload)
-    # K timed and W warm-up steps of the whole cloud (about 0.6 s each on 16 Arm cores)
+    D, h, desc = WORKLOADS[args.workload]
+    # K timed and W warm-up steps of the bounded sample (about 1-3 s a step on 16 Arm cores)
     steps, warmup = max(1, args.steps), max(0, args.warmup)
-    base = cpu_baseline(hcc, cloud, U0, h, steps, warmup)
+    base = cpu_baseline(hcc, args.workload, steps, warmup)
     line = {"metric": METRIC, "value": base["value"], "unit": "point-updates/s", "n_gpus": world, "steps": steps,
-            "warmup": warmup, "ms_per_step": cloud.n_interior * STAGES / base["value"] * 1e3, "higher_is_better": True,
+            "warmup": warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice)",
-            "config": {"workload": args.workload, "description": WORKLOADS[args.workload][2],
-                       "n_particles": cloud.n, "n_interior": cloud.n_interior},
+            "config": {"workload": args.workload, "description": desc},
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "point-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "Julia is not available on this box; the reference CPU path is its C++ restatement (oracle/)"}
+            "note": "Julia is not available on this box; the reference CPU path is its C++ restatement (oracle/), "
+                    "timed on a bounded sample of the workload (cpu_baseline.sample)"}
     print(json.dumps(line), flush=True)
 
 
@@ -805,7 +995,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="euler2d_quadrant_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="euler3d_blast_8M", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp32-only", action="store_true")
@@ -818,7 +1008,12 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=5)
     ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
     ap.add_argument("--no-published", action="store_true")
-    ap.add_argument("--no-3d", action="store_true")
+    ap.add_argument("--no-2d", action="store_true", help="skip the 2-D quadrant workload of a 3-D run")
+    ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: --steps)")
+    ap.add_argument("--study", choices=["accuracy"], default=None,
+                    help="run the equal-L1 study at the configurations' end times instead of the benchmark")
+    ap.add_argument("--study-workloads", default="euler3d_blast_8M,euler2d_quadrant_1M")
+    ap.add_argument("--study-out", default=None, help="also write the study's JSON here")
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
     args = ap.parse_args()
@@ -827,7 +1022,9 @@ def main():
     global HOST_DRIVEN, AUTOTUNE
     HOST_DRIVEN = args.host_driven
     AUTOTUNE = not args.no_autotune
-    if args.profile:
+    if args.study == "accuracy":
+        run_accuracy_study(args)
+    elif args.profile:
         run_profile_case(args)
     elif args.impl == "reference":
         run_reference(args)

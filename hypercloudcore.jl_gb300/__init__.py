@@ -60,6 +60,16 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     return lib
 
 
+def fp64_fma_rate() -> float:
+    """FP64 FMA rate of the current GPU in TFLOP/s (hcc_fp64_fma_rate): the FP64 path's roofline denominator."""
+    lib = load_library()
+    out = C.c_double(0.0)
+    st = lib.hcc_fp64_fma_rate(C.byref(out))
+    if st != 0:
+        raise HCCError(st, "FP64 FMA-rate kernel failed", "hcc_fp64_fma_rate")
+    return out.value
+
+
 # ------------------------------------------------------------------------------------------ descriptors
 @dataclass
 class LinearAdvection:

@@ -1725,6 +1725,19 @@ const char *hcc_build_info(void) {
            " flux_minb_many=" HCC_STR(HCC_FLUX_MINB_MANY);
 }
 
+hcc_status hcc_fp64_fma_rate(double *tflops_out) {
+    if (!tflops_out) return HCC_ERR_INVALID;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return HCC_ERR_CUDA;
+    cudaError_t e = cudaSuccess;
+    const double r = hcc::fp64_fma_rate_tflops(sms, nullptr, &e);
+    if (e != cudaSuccess) return HCC_ERR_CUDA;
+    *tflops_out = r;
+    return HCC_OK;
+}
+
 static bool tuning_ok(const hcc_tuning &t) {
     auto blk = [](int32_t b) { return b >= 32 && b <= 128 && b % 32 == 0; };
     return blk(t.flux_block) && blk(t.gather_block) && t.list_blocks_per_sm >= 1 && t.list_blocks_per_sm <= 32 &&

@@ -478,6 +478,8 @@ struct DropArgs {
 void launch_drop_decide(const DropArgs &a, int is_f32, int drop_blocks, cudaStream_t s);
 void launch_gather_rows(const void *slotmajor, void *rowmajor, const int32_t *cnt, const int64_t *rowstart,
                         int64_t n, int64_t npad, int width, int elem_bytes, cudaStream_t s);
+// FP64 FMA rate of the current device in TFLOP/s (2 FLOP per FMA), from a timed kernel on every SM.
+double fp64_fma_rate_tflops(int sms, cudaStream_t st, cudaError_t *err);
 void launch_gather_rows_of(const void *src, void *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel,
                            int64_t npad, int width, int max_slots, int elem_bytes, cudaStream_t s);
 

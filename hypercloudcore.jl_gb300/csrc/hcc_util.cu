@@ -297,7 +297,8 @@ __global__ void k_rows(const E *src, E *dst, const int32_t *cnt, const int64_t *
         for (int q = 0; q < width; ++q) dst[(r0 + k) * width + q] = src[(int64_t(k) * width + q) * npad + i];
 }
 
-// slot-major [ (k*width + c) * npad + ids[q] ] -> [ (q*max_slots + k) * width + c ] for the selected particles
+// slot-major [ (k*width + c) * npad + ids[q] ] -> [ (q*max_slots + k) * width + c ] for the selected particles;
+// the slots of a row past the particle's count are zero
 template <typename E>
 __global__ void k_rows_of(const E *src, E *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel, int64_t npad,
                           int width, int max_slots) {
@@ -305,12 +306,53 @@ __global__ void k_rows_of(const E *src, E *dst, const int32_t *cnt, const int64_
     if (q >= n_sel) return;
     const int64_t i = ids[q];
     const int c = cnt[i] < max_slots ? cnt[i] : max_slots;
-    for (int k = 0; k < c; ++k)
+    for (int k = 0; k < max_slots; ++k)
         for (int e = 0; e < width; ++e)
-            dst[(q * max_slots + k) * width + e] = src[(int64_t(k) * width + e) * npad + i];
+            dst[(q * max_slots + k) * width + e] = k < c ? src[(int64_t(k) * width + e) * npad + i] : E(0);
+}
+
+// Eight independent chains of dependent FP64 FMAs per thread (x <- x a + b, bounded: converges to b / (1 - a)); the
+// sum is written only when it equals an impossible value, so the chains stay live without a store per thread.
+__global__ void __launch_bounds__(256) k_fp64_fma(double *sink, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = double(threadIdx.x) * 1e-9 + q;
+    for (int it = 0; it < iters; ++it)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s = s + x[q];
+    if (s == -1.0) sink[0] = s;
 }
 
 }  // namespace
+
+double fp64_fma_rate_tflops(int sms, cudaStream_t st, cudaError_t *err) {
+    double *sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.0f;
+    const int iters = 1 << 14, blocks = sms * 8, threads = 256;
+    cudaError_t e = cudaMalloc(&sink, sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) {
+        k_fp64_fma<<<blocks, threads, 0, st>>>(sink, iters / 16, 0.999999, 1e-6);   // warm-up
+        cudaEventRecord(e0, st);
+        k_fp64_fma<<<blocks, threads, 0, st>>>(sink, iters, 0.999999, 1e-6);
+        cudaEventRecord(e1, st);
+        e = cudaEventSynchronize(e1);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (sink) cudaFree(sink);
+    *err = e;
+    if (e != cudaSuccess || ms <= 0.0f) return 0.0;
+    const double flops = 2.0 * 8.0 * double(iters) * double(blocks) * double(threads);
+    return flops / (double(ms) * 1e-3) / 1e12;
+}
 
 void launch_cast_f64_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s) {
     if (n > 0) k_cast_f64_f32<<<grid_for(n), HCC_BLOCK, 0, s>>>(src, dst, n);

@@ -202,7 +202,8 @@ hcc_status hcc_download_neighbours(hcc_ctx *ctx, int32_t *counts, int32_t *idx, 
 /* The lists of n_sel selected particles (the per-particle slot views pg.neighbor.indices[ranges[i]] of
    NeighbourViews.jl:11-43 / NeighborLogic.jl:182), for inspecting a large cloud without downloading every list:
    counts[q] = the full count of particle ids[q]; its first min(count, max_slots) slots in idx[q*max_slots + k],
-   w[q*max_slots + k], dist[(q*max_slots + k)*dim + d]. Any output may be NULL. */
+   w[q*max_slots + k], dist[(q*max_slots + k)*dim + d]; the slots of a row past the count are zero. Any output
+   may be NULL. */
 hcc_status hcc_download_neighbours_of(hcc_ctx *ctx, int64_t n_sel, const int64_t *ids, int32_t max_slots,
                                       int32_t *counts, int32_t *idx, double *w, double *dist);
 
@@ -461,6 +462,11 @@ hcc_status hcc_autotune(hcc_ctx *ctx, double dt, int32_t steps, hcc_tune_report 
 /* The compile-time launch bounds the library was built with, e.g. "flux_block=128 flux_minb=7 flux_minb_wide=4
    flux_minb64=3 flux_minb_many=2" (static string; no GPU needed). Tells apart variant builds loaded side by side. */
 const char *hcc_build_info(void);
+
+/* Calibration, no counterpart in the reference: the FP64 FMA rate of the current GPU in TFLOP/s (an FMA counts 2),
+   from chains of dependent FMAs on every SM timed with CUDA events on the default stream (allocates 8 bytes). The
+   denominator of the FP64 path's roofline (the GPU's FP64 units are a small fraction of its FP32 ones). */
+hcc_status hcc_fp64_fma_rate(double *tflops_out);
 
 /* Waits for the context's stream. */
 hcc_status hcc_synchronize(hcc_ctx *ctx);

@@ -2246,6 +2246,11 @@ hcc_status orc_neighbours_of(orc_ctx *ctx, int64_t n_sel, const int64_t *ids, in
         const int64_t c = s.count_of(i);
         counts[q] = int32_t(c);
         if (c > max_slots) { over = true; continue; }
+        for (int64_t k = 0; k < max_slots; ++k) {            // slots past the count are zero
+            idx[q * max_slots + k] = 0;
+            w[q * max_slots + k] = 0.0;
+            for (int d = 0; d < s.D; ++d) dist[(q * max_slots + k) * s.D + d] = 0.0;
+        }
         s.write_of(i, idx + q * max_slots, w + q * max_slots, dist + q * max_slots * s.D);
     }
     return over ? HCC_ERR_CAPACITY : HCC_OK;

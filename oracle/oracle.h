@@ -36,8 +36,8 @@ hcc_status orc_download_positions(orc_ctx *ctx, double *pos);
 /* Neighbour counts of every particle (pass 1 of the search only, no lists kept). */
 hcc_status orc_neighbour_counts(orc_ctx *ctx, int32_t *counts);
 /* The lists of n_sel selected particles in the reference's order: row q holds particle ids[q]'s slots
-   idx[q*max_slots + k], w[q*max_slots + k], dist[(q*max_slots + k)*D + d]; counts[q]. HCC_ERR_CAPACITY when a
-   count exceeds max_slots. The cell list covers the whole cloud; no other list is kept. */
+   idx[q*max_slots + k], w[q*max_slots + k], dist[(q*max_slots + k)*D + d] (zero past the count); counts[q].
+   HCC_ERR_CAPACITY when a count exceeds max_slots. The cell list covers the whole cloud; no other list is kept. */
 hcc_status orc_neighbours_of(orc_ctx *ctx, int64_t n_sel, const int64_t *ids, int32_t max_slots, int32_t *counts,
                              int32_t *idx, double *w, double *dist);
 hcc_status orc_prepare_geometry(orc_ctx *ctx);

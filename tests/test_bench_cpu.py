@@ -39,5 +39,20 @@ def test_algorithmic_bytes_model():
 
 def test_recorded_traffic_is_read():
     t = bench.recorded_traffic()
-    assert t["flux_f32_euler2d_bytes_per_point_stage"] > 277.0
-    assert t["gather_f32_euler2d_bytes_per_point_stage"] > 173.0
+    for w in ("euler2d_quadrant_1M", "euler3d_blast_8M"):
+        assert t[f"flux_f32_{w}_bytes_per_point_stage"] > 0.0
+        assert t[f"gather_f32_{w}_bytes_per_point_stage"] > 0.0
+
+
+def test_radial_blast_reference_conserves_mass_and_converges():
+    """The 1-D spherical reference of the equal-L1 study: mass is conserved while the waves stay inside, and halving
+    the cell size moves the solution by much less than the 3-D errors it judges (~1e-2)."""
+    import numpy as np
+    r = np.linspace(0.0, 0.6, 2401)
+    w = r ** 2
+    coarse = bench.radial_blast_reference(0.02, r, n=600)
+    fine = bench.radial_blast_reference(0.02, r, n=1200)
+    assert np.sum(np.abs(coarse - fine) * w) / np.sum(fine * w) < 5e-3
+    m0 = np.sum(np.where(r < 0.2, 1.0, 0.125) * w)
+    assert abs(np.sum(fine * w) - m0) / m0 < 2e-3           # trapezoid-free sum on a fine radius grid
+    assert fine[0] == 1.0 and fine[-1] == 0.125
