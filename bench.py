@@ -43,6 +43,7 @@ METRIC = "point-updates/s per RK stage, FP32+learned vs plain FP64 on 1 GB300 at
 STAGES = 3
 HOST_DRIVEN = False     # --host-driven: steps without the step graph (e.g. for kernel profilers)
 AUTOTUNE = True         # --no-autotune: keep the default launch shapes (hcc_autotune picks them otherwise)
+TILE_STAGING = True     # --no-tile-staging: stream-fed FP32 full passes instead of the tile-staged ones
 
 
 def _load(name, path, pkg_dir=None):
@@ -368,11 +369,13 @@ def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, *, e2e_steps=N
     ctx.prepare_geometry()
     ctx.synchronize()
     setup_s = time.perf_counter() - t0
+    if not TILE_STAGING:
+        ctx.set_tile_staging(False)
     U_in = U0.astype(np.float32) if f32 else U0
     ctx.upload_state(U_in)
     dt = 0.4 * ctx.time_step()
     tune = ctx.autotune(dt, steps=3) if autotune and steps > 0 else None
-    out = {"dt": dt, "tuning": tune, "setup_s": setup_s}
+    out = {"dt": dt, "tuning": tune, "setup_s": setup_s, "tile_staging": ctx.tile_staging()}
     if steps > 0:
         ctx.upload_state(U_in)
         for _ in range(warmup):
@@ -636,7 +639,7 @@ def run_gpu(args):
                    "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
                    "l2": "inputs larger than L2 (per-slot neighbour arrays of several GB)",
                    "parallelism": f"replicas x{world}", "dt": r["dt"], "launch_shapes": r["tuning"],
-                   "setup_s": r["setup_s"], "cloud_generation_s": t_gen},
+                   "setup_s": r["setup_s"], "cloud_generation_s": t_gen, "tile_staging": r["tile_staging"]},
         "gpu_launches": r["launches"],
         "e2e": {"value": n_int * STAGES * r["e2e_steps"] * world / r["e2e_s"], "unit": "point-updates/s",
                 "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"], "steps": r["e2e_steps"]},
@@ -1016,12 +1019,14 @@ def main():
     ap.add_argument("--study-out", default=None, help="also write the study's JSON here")
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
+    ap.add_argument("--no-tile-staging", action="store_true", help="stream-fed FP32 full passes (A/B)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    global HOST_DRIVEN, AUTOTUNE
+    global HOST_DRIVEN, AUTOTUNE, TILE_STAGING
     HOST_DRIVEN = args.host_driven
     AUTOTUNE = not args.no_autotune
+    TILE_STAGING = not args.no_tile_staging
     if args.study == "accuracy":
         run_accuracy_study(args)
     elif args.profile:

@@ -547,6 +547,17 @@ class Context:
         """Resume from a snapshot of a context with the same configuration and particle count."""
         self._check(self.lib.hcc_load_snapshot(self._h, str(path).encode()), "hcc_load_snapshot")
 
+    def set_tile_staging(self, enable: bool = True):
+        """Tile-staged FP32 full passes (default on where the context qualifies) or the stream-fed ones."""
+        self._check(self.lib.hcc_set_tile_staging(self._h, int(bool(enable))), "hcc_set_tile_staging")
+
+    def tile_staging(self) -> dict:
+        """{"active": next step's full passes are tile-staged, "union_entries", "largest_union"}."""
+        act, tot, mx = C.c_int32(), C.c_int64(), C.c_int32()
+        self._check(self.lib.hcc_get_tile_staging(self._h, C.byref(act), C.byref(tot), C.byref(mx)),
+                    "hcc_get_tile_staging")
+        return {"active": bool(act.value), "union_entries": tot.value, "largest_union": mx.value}
+
     def set_step_graphs(self, enable: bool = True):
         """Take each step as one captured CUDA graph (default) or drive the MOOD fixed points from the host."""
         self._check(self.lib.hcc_set_step_graphs(self._h, int(bool(enable))), "hcc_set_step_graphs")

@@ -156,6 +156,8 @@ PROTOTYPES = [
     ("hcc_download_volumes", C.c_int, [P, _dp]),
     ("hcc_build_info", C.c_char_p, []),
     ("hcc_fp64_fma_rate", C.c_int, [_dp]),
+    ("hcc_set_tile_staging", C.c_int, [P, C.c_int32]),
+    ("hcc_get_tile_staging", C.c_int, [P, _i32p, C.POINTER(C.c_int64), _i32p]),
     ("hcc_get_tuning", C.c_int, [P, C.POINTER(HccTuning)]),
     ("hcc_set_tuning", C.c_int, [P, C.POINTER(HccTuning)]),
     ("hcc_autotune", C.c_int, [P, C.c_double, C.c_int32, C.POINTER(HccTuneReport)]),

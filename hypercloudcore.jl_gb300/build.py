@@ -30,6 +30,7 @@ UNITS = {
     "hcc_stage_f32_r1.cu": ["-ftz=true"],
     "hcc_stage_f32_r2.cu": ["-ftz=true"],
     "hcc_noalloc.cu": ["-fmad=false"],
+    "hcc_tiles.cu": [],
     "hcc_learn.cu": ["-fmad=false"],
 }
 

@@ -215,6 +215,8 @@ struct hcc_ctx {
     int list_blocks = 1, drop_blocks = 1;
     int sms = 1;                                 // SM count of the device
     hcc_tuning tune{128, 128, 8, 2};             // launch shapes of the step (hcc_set_tuning / hcc_autotune)
+    TileTables tiles;                            // tile staging of the FP32 full passes (hcc_tiles.cu)
+    int tile_enabled = 1;
     void apply_tuning() {
         list_blocks = std::max(1, sms) * tune.list_blocks_per_sm;
         drop_blocks = std::max(1, sms) * tune.drop_blocks_per_sm;
@@ -331,6 +333,7 @@ struct hcc_ctx {
 
     void free_particles() {
         drop_graphs();
+        tiles.release();
         free_mover_buffers();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
@@ -346,6 +349,7 @@ struct hcc_ctx {
     }
     void free_slots() {
         drop_graphs();
+        tiles.release();
         dfree(nidx); dfree(w64); dfree(dist64); dfree(dw64); dfree(dw1_64); dfree(dist32); dfree(w32); dfree(dw32);
         dfree(dw1_32); dfree(gw32);
         for (int q = 0; q < 3; ++q) { dfree(dwc64[q]); dfree(dwc32[q]); dfree(okc[q]); }
@@ -437,6 +441,15 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     a.u2_ratio = T(c->cfg.u2_ratio);
     a.u2_h = T(c->h);
     a.u2_range = c->u2_plateau_on() ? c->u2_keys : nullptr;
+    if constexpr (sizeof(T) == 4) {
+        if (c->tiles.ok && c->tile_enabled && !c->moving()) {
+            a.tile = 1;
+            TileView &v = a.tv;
+            v.ntiles = c->tiles.ntiles; v.ustart = c->tiles.ustart; v.uid = c->tiles.uid; v.upos = c->tiles.upos;
+            v.quantum = c->tiles.quantum; v.lidx = c->tiles.lidx; v.lself = c->tiles.lself; v.coef = c->tiles.coef;
+            v.cw = c->tiles.cw; v.umax = c->tiles.umax; v.wscale = c->tiles.wscale;
+        }
+    }
     return a;
 }
 
@@ -1364,6 +1377,7 @@ hcc_status hcc_set_mover(hcc_ctx *c, const hcc_mover *mv) {
         return c->fail(HCC_ERR_UNSUPPORTED, "moving grids with WENO / CentralDivergence / UpwindDivergence");
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->drop_graphs();
+    if (mv->kind != HCC_MOVER_NONE) c->tiles.release();   // moving positions: the full passes read the slot streams
     c->mover = *mv;
     c->free_mover_buffers();
     return HCC_OK;
@@ -1522,6 +1536,52 @@ hcc_status hcc_download_neighbours_of(hcc_ctx *c, int64_t n_sel, const int64_t *
     return st;
 }
 
+// Tile tables of an FP32 context whose full passes can be staged (MUSCL of order <= 2 with the degree-1 divergence
+// fit, no moment correction, EPD0/EPD1/StrictEPD0 interface orders): every full gather and flux pass then reads
+// its neighbours from shared memory and recomputes the slot offsets and weights. Contexts or clouds that do not
+// qualify keep the stream-fed passes (tiles.ok = 0).
+hcc_status build_tiles(hcc_ctx *c) {
+    c->tiles.release();
+    const int pde = c->cfg.pde;
+    const bool eligible = c->f32 && c->rdeg == 1 && c->max_order <= 2 && c->ddeg == 1 && !c->no_recon() &&
+                          !c->moment() && !c->moving() && c->cfg.mood_strategy != HCC_EPD2 &&
+                          (pde == HCC_PDE_EULER || pde == HCC_PDE_ADVECTION || pde == HCC_PDE_BGK);
+    if (!eligible || c->n == 0) return HCC_OK;
+    const int D = c->D, M = c->M;
+    const int W = (4 + M + D * M + 3) / 4 * 4;                 // shared-memory row of the flux pass (floats)
+    const long budget = 200L * 1024 - long(HCC_TILE) * 4 * M * long(sizeof(float));
+    TileBuild b{};
+    b.n = c->n; b.npad = c->npad; b.D = D; b.kmax = std::max(c->kmax, 1);
+    b.cnt = c->cnt; b.nidx = c->nidx; b.pos = c->pos;
+    for (int d = 0; d < D; ++d) {
+        b.periodic[d] = c->cfg.periodic[d];
+        const double L = c->cfg.domain_max[d] - c->cfg.domain_min[d];
+        b.Lwrap[d] = b.periodic[d] ? L : 0.0;
+        b.invLwrap[d] = b.periodic[d] ? 1.0 / L : 0.0;
+    }
+    b.R = c->cfg.radius;
+    b.inv_r = c->inv_r64; b.inv_d = c->inv_d64; b.ok_r = c->ok_r; b.ok_d = c->ok_d;
+    b.invL = c->invL;
+    b.wscale = c->cfg.weight_alpha / (c->cfg.radius * c->cfg.radius);
+    b.max_union = int(std::max(0L, budget / (4L * W)));
+    return build_tile_tables(b, c->tiles, c->stream, c->err);
+}
+
+hcc_status hcc_set_tile_staging(hcc_ctx *c, int32_t enable) {
+    if (!c) return HCC_ERR_INVALID;
+    c->drop_graphs();
+    c->tile_enabled = enable != 0;
+    return HCC_OK;
+}
+
+hcc_status hcc_get_tile_staging(hcc_ctx *c, int32_t *active, int64_t *union_entries, int32_t *largest_union) {
+    if (!c) return HCC_ERR_INVALID;
+    if (active) *active = (c->tiles.ok && c->tile_enabled && !c->moving()) ? 1 : 0;
+    if (union_entries) *union_entries = c->tiles.utotal;
+    if (largest_union) *largest_union = c->tiles.umax;
+    return HCC_OK;
+}
+
 hcc_status hcc_prepare_geometry(hcc_ctx *c) {
     if (c) c->drop_graphs();
     if (!c) return HCC_ERR_INVALID;
@@ -1582,6 +1642,7 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
             HCC_TRY(c->alloc(c->dwc32[q], slots * D, "central weights f32"));
             launch_cast_f64_to_f32(c->dwc64[q], c->dwc32[q], int64_t(slots) * D, c->stream);
         }
+        if ((st = build_tiles(c)) != HCC_OK) return st;
     }
     // outflow donor roots, then the boundary list (tag -> condition)
     DonorArgs da{};
@@ -2176,6 +2237,7 @@ namespace {
 // geometry caches (MLS inverses, divergence and gradient weights, donor map) at the new positions.
 hcc_status apply_positions(hcc_ctx *c, const double *src, bool full_search) {
     hcc_status st;
+    c->tiles.release();                           // the tile tables describe the positions being replaced
     HCC_TRY(c->cuda(cudaMemcpyAsync(c->pos, src, size_t(c->npad) * c->D * sizeof(double), cudaMemcpyDeviceToDevice,
                                     c->stream), "stage positions"));
     if (full_search) {

@@ -204,6 +204,32 @@ template <typename T> struct Geometry {
     double h64;                       // min(dx)
 };
 
+// Tile staging of the FP32 full passes (MUSCL of order <= 2 with the degree-1 divergence fit, fixed grids): the
+// particles in tiles of HCC_TILE consecutive (Morton-numbered) particles; per tile the sorted union of its particles
+// and of all their neighbours, which one thread block stages in shared memory; per slot the neighbour's place in its
+// particle's tile union (16 bits); per union entry the position relative to the tile's first particle as int32
+// multiples of the tile's power-of-two quantum (so x_j - x_i is an exact integer difference, rounded once when
+// converted to FP32); per particle the FP32 rows of its cached fits: A_d and B_de of the divergence weights
+// dw_k[d] = w_k (A_d + sum_e B_de x_e) and G_bc of the gradient weights gw_k[b] = w_k sum_c G_bc x_c, with
+// w_k = w(|x_k|^2) the weight function. The slot streams of distances, weights and divergence weights are then
+// never read by the full passes: they recompute them from positions that come from shared memory.
+#ifndef HCC_TILE
+#define HCC_TILE 128
+#endif
+struct TileView {
+    int64_t ntiles;
+    const int64_t *ustart;            // [ntiles + 1] union offsets
+    const int32_t *uid;               // [utotal] particle numbers, ascending within a tile
+    const int4 *upos;                 // [utotal] quantised offsets from the tile's first particle (x, y, z, 0)
+    const float *quantum;             // [ntiles] length of one unit of upos (a power of two)
+    const uint16_t *lidx;             // [kmax * npad] slot k of particle i: place of its neighbour in the union
+    const uint16_t *lself;            // [n] place of the particle itself in its tile's union
+    const float *coef;                // [n * cw] A (D), B (D*D), G (D*D), zero-padded to cw floats
+    int cw;                           // a multiple of 4
+    int umax;                         // largest union of any tile
+    float wscale;                     // alpha / R^2 of the weight function
+};
+
 // dt-dependent coefficients of one candidate, read by the kernels from device memory so that one captured step
 // graph serves every dt: hE[j] = dt a_t (0 = skipped), hI[j] = dt a (0 = skipped), h_sub = dt / C of the Euler
 // substep, dt_ii = dt a_ii and its inverse for the implicit part.
@@ -267,6 +293,8 @@ template <typename T> struct StageArgs {
     const double *x_n;
     const double *KX[HCC_MAX_STAGES];
     double *Xnext;
+    int tile;                         // 1: full passes of this FP32 context are tile-staged (tv is valid)
+    TileView tv;
     uint32_t *tmask;                  // MOOD check: failed candidates (a ballot word per tile) ...
     int32_t *ttiles;                  // ... the tiles with a failure ...
     unsigned *tcount;                 // ... and their count
@@ -483,6 +511,36 @@ double fp64_fma_rate_tflops(int sms, cudaStream_t st, cudaError_t *err);
 void launch_gather_rows_of(const void *src, void *dst, const int32_t *cnt, const int64_t *ids, int64_t n_sel,
                            int64_t npad, int width, int max_slots, int elem_bytes, cudaStream_t s);
 
+
+// Tile tables of a context (hcc_tiles.cu): built from the FP64 geometry after the MLS caches; `ok` = 0 when the
+// cloud does not qualify (a union above 65535 entries or beyond the shared-memory budget, a periodic axis shorter than
+// 2 (tile extent) + R), in which case the full passes keep the slot streams.
+struct TileBuild {
+    int64_t n, npad;
+    int D, kmax;
+    const int32_t *cnt, *nidx;
+    const double *pos;                // SoA [d * npad + i]
+    int periodic[3];
+    double Lwrap[3], invLwrap[3], R;
+    const double *inv_r, *inv_d;      // FP64 inverse moments: D x D (reconstruction), (D+1) x (D+1) (divergence)
+    const uint8_t *ok_r, *ok_d;
+    double invL, wscale;
+    int max_union;                    // refuse unions above this many entries
+};
+struct TileTables {
+    int64_t ntiles = 0, utotal = 0;
+    int64_t *ustart = nullptr;
+    int32_t *uid = nullptr;
+    int4 *upos = nullptr;
+    float *quantum = nullptr;
+    uint16_t *lidx = nullptr, *lself = nullptr;
+    float *coef = nullptr;
+    int cw = 0, umax = 0;
+    float wscale = 0.f;
+    int ok = 0;
+    void release();
+};
+hcc_status build_tile_tables(const TileBuild &b, TileTables &t, cudaStream_t s, std::string &err);
 
 // ----------------------------------------------------------------------------------- learned predictor
 // Inputs of the stencil features (state in the context's precision, slot-major neighbour lists and offsets).

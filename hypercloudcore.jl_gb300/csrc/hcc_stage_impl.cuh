@@ -871,6 +871,162 @@ template <typename T, int M> struct FluxPart {
     T s[M], c[M], mn[M], mx[M];
 };
 
+// One slot k of the flux pass of particle i (the MUSCL functor's slot body, MUSCL.jl:463-508): interface orders oi,
+// oj and the sort orientation `below` are the caller's; the interface reconstructions, the physical fluxes, the
+// Rusanov flux of the pair sorted by the signs of the axis offsets (sort_flux, Utils.jl:95-102; FluxFunctions.jl:66-76)
+// and its flux difference contracted with the slot's divergence weights wk go into acc.
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, bool MOM>
+__device__ __forceinline__ void flux_slot(const StageArgs<T> &a, const T *fi, const T (*gi)[M], const T (*Fi)[M],
+                                          const T *wp, const T *fj, const T *gj, const int oi, const int oj,
+                                          const bool below, const T *dk, const T *wk, AccumV<T, M> &acc,
+                                          const int64_t i, const int k) {
+    constexpr int BR = RBasis<D, RDEG>::B;
+    constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form
+    const int64_t np = a.g.npad;
+    (void)np; (void)i; (void)k; (void)wp;
+    T pi[BR], pj[BR];
+    if constexpr (kFast && RDEG == 1) {
+        // degree 1: an interface of order 2 keeps the linear terms, order 1 none (the midpoint offsets
+        // ±dk/2 scaled by 0 or ±1/2)
+        const T si = oi >= 2 ? T(0.5) : T(0), sj = oj >= 2 ? T(-0.5) : T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) { pi[d] = si * dk[d]; pj[d] = sj * dk[d]; }
+    } else {
+        const int keep_i = interface_terms<D, RDEG>(oi);
+        const int keep_j = interface_terms<D, RDEG>(oj);
+        T hx[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
+        recon_basis<D, RDEG, T>(hx, pi);
+#pragma unroll
+        for (int d = 0; d < D; ++d) hx[d] = T(-0.5) * dk[d];
+        recon_basis<D, RDEG, T>(hx, pj);
+#pragma unroll
+        for (int b = 0; b < BR; ++b) {
+            if (b >= keep_i) pi[b] = T(0);
+            if (b >= keep_j) pj[b] = T(0);
+        }
+    }
+    if constexpr (kFast && PDE != HCC_PDE_EULER && !ALE) {
+        // FP32, linear fluxes F_d(f)_m = c_dm f_m with constant speeds (advection, BGK), fixed grid: the
+        // doubled Rusanov difference per component on the fly, without flux arrays (registers:
+        // 2 (F_n - F_i)_m = sum_d w_d (c_dm (f_ij + f_ji - 2 f_i) - s_d max(λ_d) (f_ji - f_ij)))
+        T sw[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            sw[d] = (below ? wk[d] : dk[d]) > T(0) ? a.ph.amax[d] : -a.ph.amax[d];
+        T t[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            T si = gi[0][m] * pi[0];
+            T sj = gj[m] * pj[0];
+#pragma unroll
+            for (int b = 1; b < BR; ++b) {
+                si = si + gi[b][m] * pi[b];
+                sj = sj + gj[b * M + m] * pj[b];
+            }
+            const T fij = fi[m] + si, fji = fj[m] + sj;
+            const T sum = (fij + fji) - T(2) * fi[m], jump = fji - fij;
+            T tm = wk[0] * (a.ph.c[0][m] * sum - sw[0] * jump);
+#pragma unroll
+            for (int d = 1; d < D; ++d) tm = tm + wk[d] * (a.ph.c[d][m] * sum - sw[d] * jump);
+            t[m] = tm;
+            if constexpr (MOM) {
+                T se = a.ph.amax[0] * a.g.mw[(int64_t(k) * D) * np + i];
+#pragma unroll
+                for (int d = 1; d < D; ++d) se = se + a.ph.amax[d] * a.g.mw[(int64_t(k) * D + d) * np + i];
+                t[m] = t[m] - se * jump;
+            }
+        }
+        acc.add(t);
+        return;
+    }
+    T fij[M], fji[M];
+    if constexpr (kFast) {
+#pragma unroll
+        for (int q = 0; q < M / 2; ++q) {
+            float2 si = p_mul(p_ld(gi[0], q), p_bc(pi[0]));
+            float2 sj = p_mul(p_ld(gj, q), p_bc(pj[0]));
+#pragma unroll
+            for (int b = 1; b < BR; ++b) {
+                si = p_fma(p_ld(gi[b], q), p_bc(pi[b]), si);
+                sj = p_fma(p_ld(gj + b * M, q), p_bc(pj[b]), sj);
+            }
+            p_st(fij, q, p_add(p_ld(fi, q), si));
+            p_st(fji, q, p_add(p_ld(fj, q), sj));
+        }
+    }
+#pragma unroll
+    for (int m = kFast ? (M / 2) * 2 : 0; m < M; ++m) {
+        T si = gi[0][m] * pi[0];
+        T sj = gj[m] * pj[0];
+#pragma unroll
+        for (int b = 1; b < BR; ++b) {
+            si = si + gi[b][m] * pi[b];
+            sj = sj + gj[b * M + m] * pj[b];
+        }
+        fij[m] = fi[m] + si;
+        fji[m] = fj[m] + sj;
+    }
+    T Fij[D][M], Fji[D][M], lij[D], lji[D];
+    flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij, wp);
+    flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji, wp);
+    T t[M];
+    if constexpr (kFast) {
+        // FP32: 2 (F_n - F_i) = (F_ij + F_ji) - s_d max(λ) (f_ji - f_ij) - 2 F_i with s_d = sign of the
+        // axis component (the sort_flux orientation folded into the speed); the factor 2 leaves K = -Σ.
+        // (pairs of components with the packed instructions, a scalar tail for odd M)
+        T jump[M];
+#pragma unroll
+        for (int q = 0; q < M / 2; ++q) p_st(jump, q, p_sub(p_ld(fji, q), p_ld(fij, q)));
+        if constexpr (M & 1) jump[M - 1] = fji[M - 1] - fij[M - 1];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const T ssd = (below ? wk[d] : dk[d]) > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
+            const float2 nssd = p_bc(-ssd), w2 = p_bc(wk[d]);
+#pragma unroll
+            for (int q = 0; q < M / 2; ++q) {
+                const float2 Fs = p_add(p_ld(Fij[d], q), p_ld(Fji[d], q));
+                const float2 dF2 = p_sub(p_fma(nssd, p_ld(jump, q), Fs), p_ld(Fi[d], q));
+                p_st(t, q, (d == 0) ? p_mul(w2, dF2) : p_fma(w2, dF2, p_ld(t, q)));
+            }
+            if constexpr (M & 1) {
+                const T dF2 = ((Fij[d][M - 1] + Fji[d][M - 1]) - ssd * jump[M - 1]) - Fi[d][M - 1];
+                t[M - 1] = (d == 0) ? wk[0] * dF2 : t[M - 1] + wk[d] * dF2;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const bool pos = (below ? wk[d] : dk[d]) > T(0);
+            // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
+            // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its
+            // orientation
+            const T sdd = vmax(lij[d], lji[d]);
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const T jump = pos ? (fji[m] - fij[m]) : (fij[m] - fji[m]);
+                const T Fn = T(0.5) * ((Fij[d][m] + Fji[d][m]) - sdd * jump);
+                const T dF = Fn - Fi[d][m];
+                t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
+            }
+        }
+    }
+    acc.add(t);
+    if constexpr (MOM) {
+        // moment correction of a first-order scheme (MUSCL.jl:501-505): -1/2 sum_d s_d e^d_ij (f_ji - f_ij),
+        // the speeds s_d = max(λ_d) of the pair (FP32: the doubled form of the scaled Rusanov flux)
+        T se = vmax(lij[0], lji[0]) * a.g.mw[(int64_t(k) * D) * np + i];
+#pragma unroll
+        for (int d = 1; d < D; ++d) se = se + vmax(lij[d], lji[d]) * a.g.mw[(int64_t(k) * D + d) * np + i];
+        const T corr = kFast ? se : T(0.5) * se;
+        T t2[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) t2[m] = -(corr * (fji[m] - fij[m]));
+        acc.add(t2);
+    }
+}
+
 // The flux pass of particle i over its slots k0, k0 + KSTEP, ... With KSTEP = 1 the whole pass and its epilogue;
 // with KSTEP > 1 (FP32) the partial sums and extrema go to `part` for the caller to combine.
 template <typename T, int D, int M, int PDE, int RDEG, bool ALE, int KSTEP = 1, bool MOM = false>
@@ -963,147 +1119,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
             // order 1) the states are sorted by the signs of the slot's divergence weights instead of the distance
             const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
                                                 oj_own < a.sc.max_order);
-            T pi[BR], pj[BR];
-            if constexpr (kFast && RDEG == 1) {
-                // degree 1: an interface of order 2 keeps the linear terms, order 1 none (the midpoint offsets
-                // ±dk/2 scaled by 0 or ±1/2)
-                const T si = oi >= 2 ? T(0.5) : T(0), sj = oj >= 2 ? T(-0.5) : T(0);
-#pragma unroll
-                for (int d = 0; d < D; ++d) { pi[d] = si * dk[d]; pj[d] = sj * dk[d]; }
-            } else {
-                const int keep_i = interface_terms<D, RDEG>(oi);
-                const int keep_j = interface_terms<D, RDEG>(oj);
-                T hx[D];
-#pragma unroll
-                for (int d = 0; d < D; ++d) hx[d] = T(0.5) * dk[d];
-                recon_basis<D, RDEG, T>(hx, pi);
-#pragma unroll
-                for (int d = 0; d < D; ++d) hx[d] = T(-0.5) * dk[d];
-                recon_basis<D, RDEG, T>(hx, pj);
-#pragma unroll
-                for (int b = 0; b < BR; ++b) {
-                    if (b >= keep_i) pi[b] = T(0);
-                    if (b >= keep_j) pj[b] = T(0);
-                }
-            }
-            if constexpr (kFast && PDE != HCC_PDE_EULER && !ALE) {
-                // FP32, linear fluxes F_d(f)_m = c_dm f_m with constant speeds (advection, BGK), fixed grid: the
-                // doubled Rusanov difference per component on the fly, without flux arrays (registers:
-                // 2 (F_n - F_i)_m = sum_d w_d (c_dm (f_ij + f_ji - 2 f_i) - s_d max(λ_d) (f_ji - f_ij)))
-                T sw[D];
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    sw[d] = (below ? wk[d] : dk[d]) > T(0) ? a.ph.amax[d] : -a.ph.amax[d];
-                T t[M];
-#pragma unroll
-                for (int m = 0; m < M; ++m) {
-                    T si = gi[0][m] * pi[0];
-                    T sj = gj[m] * pj[0];
-#pragma unroll
-                    for (int b = 1; b < BR; ++b) {
-                        si = si + gi[b][m] * pi[b];
-                        sj = sj + gj[b * M + m] * pj[b];
-                    }
-                    const T fij = fi[m] + si, fji = fj[m] + sj;
-                    const T sum = (fij + fji) - T(2) * fi[m], jump = fji - fij;
-                    T tm = wk[0] * (a.ph.c[0][m] * sum - sw[0] * jump);
-#pragma unroll
-                    for (int d = 1; d < D; ++d) tm = tm + wk[d] * (a.ph.c[d][m] * sum - sw[d] * jump);
-                    t[m] = tm;
-                    if constexpr (MOM) {
-                        T se = a.ph.amax[0] * a.g.mw[(int64_t(k) * D) * np + i];
-#pragma unroll
-                        for (int d = 1; d < D; ++d) se = se + a.ph.amax[d] * a.g.mw[(int64_t(k) * D + d) * np + i];
-                        t[m] = t[m] - se * jump;
-                    }
-                }
-                acc.add(t);
-                continue;
-            }
-            T fij[M], fji[M];
-            if constexpr (kFast) {
-#pragma unroll
-                for (int q = 0; q < M / 2; ++q) {
-                    float2 si = p_mul(p_ld(gi[0], q), p_bc(pi[0]));
-                    float2 sj = p_mul(p_ld(gj, q), p_bc(pj[0]));
-#pragma unroll
-                    for (int b = 1; b < BR; ++b) {
-                        si = p_fma(p_ld(gi[b], q), p_bc(pi[b]), si);
-                        sj = p_fma(p_ld(gj + b * M, q), p_bc(pj[b]), sj);
-                    }
-                    p_st(fij, q, p_add(p_ld(fi, q), si));
-                    p_st(fji, q, p_add(p_ld(fj, q), sj));
-                }
-            }
-#pragma unroll
-            for (int m = kFast ? (M / 2) * 2 : 0; m < M; ++m) {
-                T si = gi[0][m] * pi[0];
-                T sj = gj[m] * pj[0];
-#pragma unroll
-                for (int b = 1; b < BR; ++b) {
-                    si = si + gi[b][m] * pi[b];
-                    sj = sj + gj[b * M + m] * pj[b];
-                }
-                fij[m] = fi[m] + si;
-                fji[m] = fj[m] + sj;
-            }
-            T Fij[D][M], Fji[D][M], lij[D], lji[D];
-            flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij, wp);
-            flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji, wp);
-            T t[M];
-            if constexpr (kFast) {
-                // FP32: 2 (F_n - F_i) = (F_ij + F_ji) - s_d max(λ) (f_ji - f_ij) - 2 F_i with s_d = sign of the
-                // axis component (the sort_flux orientation folded into the speed); the factor 2 leaves K = -Σ.
-                // (pairs of components with the packed instructions, a scalar tail for odd M)
-                T jump[M];
-#pragma unroll
-                for (int q = 0; q < M / 2; ++q) p_st(jump, q, p_sub(p_ld(fji, q), p_ld(fij, q)));
-                if constexpr (M & 1) jump[M - 1] = fji[M - 1] - fij[M - 1];
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    const T ssd = (below ? wk[d] : dk[d]) > T(0) ? vmax(lij[d], lji[d]) : -vmax(lij[d], lji[d]);
-                    const float2 nssd = p_bc(-ssd), w2 = p_bc(wk[d]);
-#pragma unroll
-                    for (int q = 0; q < M / 2; ++q) {
-                        const float2 Fs = p_add(p_ld(Fij[d], q), p_ld(Fji[d], q));
-                        const float2 dF2 = p_sub(p_fma(nssd, p_ld(jump, q), Fs), p_ld(Fi[d], q));
-                        p_st(t, q, (d == 0) ? p_mul(w2, dF2) : p_fma(w2, dF2, p_ld(t, q)));
-                    }
-                    if constexpr (M & 1) {
-                        const T dF2 = ((Fij[d][M - 1] + Fji[d][M - 1]) - ssd * jump[M - 1]) - Fi[d][M - 1];
-                        t[M - 1] = (d == 0) ? wk[0] * dF2 : t[M - 1] + wk[d] * dF2;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    const bool pos = (below ? wk[d] : dk[d]) > T(0);
-                    // sort_flux + Rusanov without per-component selects: F_L + F_R is Fij + Fji in either order
-                    // (IEEE addition commutes) and max(λ_L, λ_R) is symmetric; only f_R - f_L keeps its
-                    // orientation
-                    const T sdd = vmax(lij[d], lji[d]);
-#pragma unroll
-                    for (int m = 0; m < M; ++m) {
-                        const T jump = pos ? (fji[m] - fij[m]) : (fij[m] - fji[m]);
-                        const T Fn = T(0.5) * ((Fij[d][m] + Fji[d][m]) - sdd * jump);
-                        const T dF = Fn - Fi[d][m];
-                        t[m] = (d == 0) ? wk[0] * dF : t[m] + wk[d] * dF;
-                    }
-                }
-            }
-            acc.add(t);
-            if constexpr (MOM) {
-                // moment correction of a first-order scheme (MUSCL.jl:501-505): -1/2 sum_d s_d e^d_ij (f_ji - f_ij),
-                // the speeds s_d = max(λ_d) of the pair (FP32: the doubled form of the scaled Rusanov flux)
-                T se = vmax(lij[0], lji[0]) * a.g.mw[(int64_t(k) * D) * np + i];
-#pragma unroll
-                for (int d = 1; d < D; ++d) se = se + vmax(lij[d], lji[d]) * a.g.mw[(int64_t(k) * D + d) * np + i];
-                const T corr = kFast ? se : T(0.5) * se;
-                T t2[M];
-#pragma unroll
-                for (int m = 0; m < M; ++m) t2[m] = -(corr * (fji[m] - fij[m]));
-                acc.add(t2);
-            }
+            flux_slot<T, D, M, PDE, RDEG, ALE, MOM>(a, fi, gi, Fi, wp, fj, gj, oi, oj, below, dk, wk, acc, i, k);
         }
     } else if (need_ext) {
         for (int k = k0; k < cnt; k += KSTEP) {
@@ -1224,6 +1240,280 @@ __global__ void __launch_bounds__(128) k_flux_tiles(const StageArgs<T> a) {
         }
         __syncthreads();
     }
+}
+
+// ----------------------------------------------------------------------------------- tile-staged full passes (FP32)
+// Full gather and flux passes of an FP32 context with tile tables (TileView): one block per tile of HCC_TILE
+// consecutive particles first copies the tile's neighbour union into shared memory -- positions (and orders), states,
+// and for the flux pass the gradients -- with loads that follow the ascending union ids (consecutive ids: contiguous,
+// coalesced words), then every slot reads its neighbour from shared memory. Offsets x_j - x_i are exact differences
+// of the quantised union positions, rounded once to FP32; the weight w(|x|^2) and the slot's gradient and divergence
+// weights follow from the particle's FP32 fit rows. The arithmetic after that is flux_slot / the cached gather of the
+// stream-fed passes.
+
+// Shared-memory row of one union entry: int4 position (the order in .w for the flux pass), then the state, then (flux
+// pass) the gradient; a multiple of 4 words so rows start on 16 bytes.
+template <int D, int M, bool GRAD> constexpr int tile_row_words() { return (4 + M + (GRAD ? D * M : 0) + 3) / 4 * 4; }
+
+// Exponential weight of a squared distance (MLSWeightFunctions.jl:68-82: 1 / the degree-4 Taylor sum of e^y,
+// y = alpha r^2 / R^2), FP32.
+__device__ __forceinline__ float tile_weight(float r2, float wscale) {
+    const float y = r2 * wscale;
+    return recip<float>(1.0f + y * (1.0f + y * (0.5f + y * (0.16666667f + y * 0.041666668f))));
+}
+
+template <int D>
+__device__ __forceinline__ void tile_offset(const int4 qj, const int4 qi, float qt, float *x) {
+    x[0] = float(qj.x - qi.x) * qt;
+    if constexpr (D > 1) x[1] = float(qj.y - qi.y) * qt;
+    if constexpr (D > 2) x[2] = float(qj.z - qi.z) * qt;
+}
+
+// Stage the union of tile t: rows of W words; the state (and gradient) words of each entry from global memory.
+template <int D, int M, bool GRAD>
+__device__ __forceinline__ int tile_stage(const StageArgs<float> &a, int64_t t, float *sm) {
+    constexpr int W = tile_row_words<D, M, GRAD>();
+    const int64_t u0 = a.tv.ustart[t];
+    const int nu = int(a.tv.ustart[t + 1] - u0);
+    const int32_t *uid = a.tv.uid + u0;
+    for (int e = threadIdx.x; e < nu; e += blockDim.x) {
+        int4 q = a.tv.upos[u0 + e];
+        if constexpr (GRAD) q.w = a.orders[uid[e]];
+        *reinterpret_cast<int4 *>(sm + e * W) = q;
+    }
+    for (int f = threadIdx.x; f < nu * M; f += blockDim.x) {
+        const int e = f / M, m = f - e * M;
+        sm[e * W + 4 + m] = a.U[int64_t(uid[e]) * M + m];
+    }
+    if constexpr (GRAD) {
+        constexpr int G = D * M;
+        for (int f = threadIdx.x; f < nu * G; f += blockDim.x) {
+            const int e = f / G, q = f - e * G;
+            sm[e * W + 4 + M + q] = a.grad[int64_t(uid[e]) * G + q];
+        }
+    }
+    return nu;
+}
+
+// Reconstruction pre-pass, one thread per particle of the tile: the cached degree-1 fit of gather_one with the
+// gradient weights recomputed per slot; every other case (boundary, starved or lowered order, failed fit, limiter)
+// goes through gather_one itself.
+template <int D, int M, int PDE>
+__global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float> a) {
+    extern __shared__ __align__(16) float sm[];
+    constexpr int W = tile_row_words<D, M, false>();
+    const int64_t t = blockIdx.x;
+    tile_stage<D, M, false>(a, t, sm);
+    __syncthreads();
+    const int64_t i = t * HCC_TILE + threadIdx.x;
+    if (i >= a.g.n || a.g.bnd[i]) return;
+    const int cnt = a.g.cnt[i];
+    int p = a.orders[i];
+    {
+        int q = p;
+        while (q > 1 && cnt < basis_count(D, q - 1)) --q;
+        if (!(q == a.sc.max_order && q > 1 && a.g.ok_r[i] && a.sc.limiter == HCC_LIMITER_NONE)) {
+            gather_one<float, D, M, PDE, 1>(a, i);
+            return;
+        }
+        p = q;
+    }
+    const int64_t np = a.g.npad;
+    const float *own = sm + int(a.tv.lself[i]) * W;
+    const int4 qi = *reinterpret_cast<const int4 *>(own);
+    float fi[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) fi[m] = own[4 + m];
+    float G[D][D];
+    const float *cf = a.tv.coef + i * a.tv.cw + D + D * D;
+#pragma unroll
+    for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int c = 0; c < D; ++c) G[b][c] = cf[b * D + c];
+    const float qt = a.tv.quantum[t], ws = a.tv.wscale;
+    float out[D][M];
+#pragma unroll
+    for (int b = 0; b < D; ++b)
+#pragma unroll
+        for (int m = 0; m < M; ++m) out[b][m] = 0.0f;
+#pragma unroll 2
+    for (int k = 0; k < cnt; ++k) {
+        const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
+        float x[D];
+        tile_offset<D>(*reinterpret_cast<const int4 *>(row), qi, qt, x);
+        float r2 = x[0] * x[0];
+#pragma unroll
+        for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
+        const float w = tile_weight(r2, ws);
+        float gk[D];
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+            float v = G[b][0] * x[0];
+#pragma unroll
+            for (int c = 1; c < D; ++c) v = v + G[b][c] * x[c];
+            gk[b] = w * v;
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const float dm = row[4 + m] - fi[m];
+#pragma unroll
+            for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
+        }
+    }
+    store_vec<float, D * M>(a.grad + i * (D * M), &out[0][0]);
+}
+
+// Flux pass, two threads per particle of the tile (slots k = h, h + 2, ... for h = 0, 1); the second writes its
+// compensated partial sums and extrema to shared memory, the first combines them and runs the epilogue.
+template <int D, int M> constexpr int tile_flux_min_blocks() { return M >= 8 ? 1 : 2; }
+
+template <int D, int M, int PDE>
+__global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_flux_tile(const StageArgs<float> a) {
+    extern __shared__ __align__(16) float sm[];
+    constexpr int W = tile_row_words<D, M, true>();
+    const int64_t t = blockIdx.x;
+    const int nu = tile_stage<D, M, true>(a, t, sm);
+    FluxPart<float, M> *parts = reinterpret_cast<FluxPart<float, M> *>(sm + nu * W);
+    __syncthreads();
+    const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
+    const int64_t i = t * HCC_TILE + pl;
+    const bool live = i < a.g.n && !a.g.bnd[i];
+    const int64_t np = a.g.npad;
+    const bool need_ext = a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2);
+    AccumV<float, M> acc;
+    float mn[M], mx[M], fi[M];
+    float gi[D][M], Fi[D][M];
+    int cnt = 0;
+    if (live) {
+        cnt = a.g.cnt[i];
+        const float *own = sm + int(a.tv.lself[i]) * W;
+        const int4 qi = *reinterpret_cast<const int4 *>(own);
+        const int oi_own = qi.w;
+#pragma unroll
+        for (int m = 0; m < M; ++m) { fi[m] = own[4 + m]; mn[m] = fi[m]; mx[m] = fi[m]; }
+#pragma unroll
+        for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int m = 0; m < M; ++m) gi[b][m] = own[4 + M + b * M + m];
+        float lami[D];
+        flux_and_speed<float, D, M, PDE>(a.ph, fi, Fi, lami, nullptr);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int m = 0; m < M; ++m) Fi[d][m] = 2.0f * Fi[d][m];
+        const bool wok = cnt > 0 && a.g.ok_d[i];
+        if (wok) {
+            const float *cf = a.tv.coef + i * a.tv.cw;
+            float A[D], B[D][D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                A[d] = cf[d];
+#pragma unroll
+                for (int e = 0; e < D; ++e) B[d][e] = cf[D + d * D + e];
+            }
+            const float qt = a.tv.quantum[t], ws = a.tv.wscale;
+            for (int k = h; k < cnt; k += 2) {
+                const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
+                const int4 qj = *reinterpret_cast<const int4 *>(row);
+                float dk[D], wk[D];
+                tile_offset<D>(qj, qi, qt, dk);
+                float r2 = dk[0] * dk[0];
+#pragma unroll
+                for (int d = 1; d < D; ++d) r2 = r2 + dk[d] * dk[d];
+                const float w = tile_weight(r2, ws);
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    float v = A[d];
+#pragma unroll
+                    for (int e = 0; e < D; ++e) v = v + B[d][e] * dk[e];
+                    wk[d] = w * v;
+                }
+                float fj[M], gj[D * M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) fj[m] = row[4 + m];
+#pragma unroll
+                for (int q = 0; q < D * M; ++q) gj[q] = row[4 + M + q];
+                if (need_ext) {
+#pragma unroll
+                    for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], fj[m]); mx[m] = vmax(mx[m], fj[m]); }
+                }
+                const int oj_own = qj.w;
+                int oi, oj;
+                if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
+                else { oi = oi_own; oj = oj_own; }
+                const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
+                                                    oj_own < a.sc.max_order);
+                flux_slot<float, D, M, PDE, 1, false, false>(a, fi, gi, Fi, nullptr, fj, gj, oi, oj, below, dk, wk,
+                                                             acc, i, k);
+            }
+        } else if (need_ext) {
+            for (int k = h; k < cnt; k += 2) {
+                const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
+#pragma unroll
+                for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], row[4 + m]); mx[m] = vmax(mx[m], row[4 + m]); }
+            }
+        }
+        if (h == 1) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                parts[pl].s[m] = acc.s[m];
+                parts[pl].c[m] = acc.c[m];
+                parts[pl].mn[m] = mn[m];
+                parts[pl].mx[m] = mx[m];
+            }
+        }
+    }
+    __syncthreads();
+    if (h == 1) return;
+    bool f = false, rough = false;
+    if (i < a.g.n) {
+        if (a.g.bnd[i]) {
+            float z[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) z[m] = 0.0f;
+            store_vec<float, M>(a.K + i * M, z);
+        } else {
+            // the two compensated partials: their sum, minus both compensations and the rounding error of that sum
+            float Kv[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const float s1 = parts[pl].s[m];
+                const float u = acc.s[m] + s1;
+                const float cm = (u - acc.s[m]) - s1;
+                Kv[m] = -(u - ((acc.c[m] + parts[pl].c[m]) + cm));
+                mn[m] = vmin(mn[m], parts[pl].mn[m]);
+                mx[m] = vmax(mx[m], parts[pl].mx[m]);
+            }
+            if (a.rough_words) {
+                bool r = !need_ext;
+#pragma unroll
+                for (int m = 0; m < M; ++m) r = r || (mx[m] - mn[m]) > 1e-6f * (fabsf(mx[m]) + fabsf(mn[m]));
+                rough = r;
+            }
+            f = stage_epilogue<float, D, M, PDE, 1>(a, i, fi, Kv, mn, mx);
+        }
+    }
+    if (a.check) tile_failures(a, i >> 5, f);
+    if (a.rough_words) {
+        const unsigned b = __ballot_sync(0xffffffffu, rough);
+        if ((threadIdx.x & 31) == 0 && (i >> 5) * 32 < a.g.n) a.rough_words[i >> 5] = b;
+    }
+}
+
+// The opt-in shared-memory limit of a block on the current device (the tile passes' dynamic allocation may go up
+// to it).
+inline int tile_smem_optin() {
+    int dev = 0, v = 48 * 1024;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+// Dynamic shared memory of the tile passes for the largest union.
+template <int D, int M> inline size_t tile_gather_smem(int umax) {
+    return size_t(umax) * tile_row_words<D, M, false>() * sizeof(float);
+}
+template <int D, int M> inline size_t tile_flux_smem(int umax) {
+    return size_t(umax) * tile_row_words<D, M, true>() * sizeof(float) + size_t(HCC_TILE) * sizeof(FluxPart<float, M>);
 }
 
 // ----------------------------------------------------------------------------------- WENO (scalar)
@@ -1660,6 +1950,16 @@ struct StageInst {
     static void gather(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
         if constexpr (sizeof(T) == 4 && RDEG == 1) {
+            if (a.full && a.tile) {   // FP32 full pass with tile tables: neighbours staged in shared memory
+                static bool attr = false;
+                if (!attr) {
+                    cudaFuncSetAttribute(k_gather_tile<D, M, PDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tile_smem_optin());
+                    attr = true;
+                }
+                k_gather_tile<D, M, PDE><<<unsigned(a.tv.ntiles), HCC_TILE, tile_gather_smem<D, M>(a.tv.umax), s>>>(a);
+                return;
+            }
             if (!a.full) {   // FP32 degree-1 worklist pass: split tiles (four warps a tile)
                 k_gather_tiles<T, D, M, PDE, RDEG><<<std::max(1u, unsigned(a.list_blocks)), 128, 0, s>>>(a);
                 return;
@@ -1691,6 +1991,18 @@ struct StageInst {
             if (a.g.mw) { flux_mom<true>(a, n, s); return; }
         }
         if constexpr (sizeof(T) == 4) {
+            if constexpr (RDEG == 1) {
+                if (a.full && a.tile) {   // full pass with tile tables: neighbours staged in shared memory
+                    static bool attr = false;
+                    if (!attr) {
+                        cudaFuncSetAttribute(k_flux_tile<D, M, PDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tile_smem_optin());
+                        attr = true;
+                    }
+                    k_flux_tile<D, M, PDE><<<unsigned(a.tv.ntiles), 2 * HCC_TILE, tile_flux_smem<D, M>(a.tv.umax), s>>>(a);
+                    return;
+                }
+            }
             if (!a.full) {   // FP32 worklist pass: split tiles (four warps a tile)
                 const unsigned g = std::max(1u, unsigned(a.list_blocks));
                 if (a.mover) k_flux_tiles<T, D, M, PDE, RDEG, true><<<g, 128, 0, s>>>(a);

@@ -463,6 +463,19 @@ hcc_status hcc_autotune(hcc_ctx *ctx, double dt, int32_t steps, hcc_tune_report 
    flux_minb64=3 flux_minb_many=2" (static string; no GPU needed). Tells apart variant builds loaded side by side. */
 const char *hcc_build_info(void);
 
+/* Tile staging of the FP32 full passes (no counterpart in the reference; the reference's gather and flux loops read
+   neighbours through the slot views, NeighbourViews.jl:11-43). For an FP32 context with MUSCL of order <= 2, the
+   degree-1 divergence fit, EPD0/EPD1/StrictEPD0 interface orders and a fixed grid, hcc_prepare_geometry also builds
+   tile tables: per tile of 128 consecutive particles the union of their neighbours, which one thread block stages in
+   shared memory, and per slot the neighbour's place in it; the full passes then recompute the slot offsets, weights
+   and divergence / gradient weights from quantised positions and per-particle FP32 fit rows instead of reading the
+   per-slot streams. Results agree with the stream-fed passes to FP32 rounding (both round the same FP64 geometry).
+   Enabled by default where the cloud qualifies; enable = 0 keeps the stream-fed passes. */
+hcc_status hcc_set_tile_staging(hcc_ctx *ctx, int32_t enable);
+/* Whether the full passes of the next step are tile-staged, the union entries over all tiles and the largest union
+   (any output may be NULL). */
+hcc_status hcc_get_tile_staging(hcc_ctx *ctx, int32_t *active, int64_t *union_entries, int32_t *largest_union);
+
 /* Calibration, no counterpart in the reference: the FP64 FMA rate of the current GPU in TFLOP/s (an FMA counts 2),
    from chains of dependent FMAs on every SM timed with CUDA events on the default stream (allocates 8 bytes). The
    denominator of the FP64 path's roofline (the GPU's FP64 units are a small fraction of its FP32 ones). */

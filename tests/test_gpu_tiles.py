@@ -1,0 +1,133 @@
+"""Tile-staged FP32 full passes (neighbours staged in shared memory per 128-particle tile, slot offsets and weights
+recomputed from quantised positions and per-particle FP32 fit rows) against the stream-fed FP32 passes and the FP64
+oracle.
+
+Both FP32 forms round the same FP64 geometry to FP32, so their right-hand sides agree to FP32 rounding (1e-5 relative
+L1 per component stated); after steps the states agree to the same bound, and both stay within the FP32 path's stated
+tolerance of the FP64 oracle. The tile path is taken only where the context and the cloud qualify.
+"""
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import blast_ic, quadrant_ic
+
+pytestmark = pytest.mark.gpu
+
+OUTFLOW = {t: 2 for t in range(1, 7)}
+
+
+def _rel_l1(a, b, sel):
+    out = []
+    for m in range(a.shape[1]):
+        den = np.abs(b[sel, m]).sum() + np.abs(b[sel, 0]).sum() * 1e-3
+        out.append(np.abs(a[sel, m] - b[sel, m]).sum() / den)
+    return max(out)
+
+
+def _system(hcc, kind, h, seed=3, periodic=False):
+    D = 3 if kind == "euler3d" else 2
+    cloud = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h, 2.5 * h, jitter=0.25 * h, seed=seed, periodic=periodic)
+    mood = hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D))
+    bc = {} if periodic else OUTFLOW
+    if kind == "euler2d":
+        cfg = lambda prec: hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=bc,
+                                           precision=prec)
+        U = quadrant_ic(cloud)
+    elif kind == "euler3d":
+        cfg = lambda prec: hcc.make_config(hcc.Euler(3), cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=bc,
+                                           precision=prec)
+        U = blast_ic(cloud)
+    elif kind == "advection":
+        pde = hcc.LinearAdvection(((1.0,), (0.5,)))
+        cfg = lambda prec: hcc.make_config(pde, cloud, scheme=hcc.MUSCL(2, 2), mood=mood, bc_map=bc, precision=prec)
+        U = np.exp(-((cloud.pos - 0.4) ** 2).sum(axis=1) / 0.01)[:, None].copy()
+    else:
+        ring = tuple((float(np.cos(2 * np.pi * q / 16)), float(np.sin(2 * np.pi * q / 16))) for q in range(16))
+        pde = hcc.KineticRelaxation(ring, epsilon=1e-4, macro_velocity=(1.0, 0.5))
+        cfg = lambda prec: hcc.make_config(pde, cloud, scheme=hcc.MUSCL(2, 2), mood=mood, tableau="IMEX_ARS222",
+                                           bc_map=bc, precision=prec)
+        x = cloud.pos
+        U = pde.maxwellian(1.0 + 0.2 * np.sin(2 * np.pi * x[:, 0]) * np.cos(2 * np.pi * x[:, 1]))
+    return cloud, cfg, np.ascontiguousarray(U, dtype=np.float64)
+
+
+def _ctx(hcc, cfg, cloud, U, tiles=True):
+    g = hcc.Context(cfg)
+    g.upload_cloud(cloud)
+    g.build_neighbours()
+    g.prepare_geometry()
+    g.set_tile_staging(tiles)
+    g.upload_state(U)
+    return g
+
+
+@pytest.mark.parametrize("kind,h", [("euler2d", 0.01), ("euler3d", 1.0 / 24), ("advection", 0.01), ("bgk", 0.02)])
+def test_tile_passes_match_stream_passes_and_oracle(hcc, oracle, cuda_lib, kind, h):
+    abi = sys.modules["hcc_gb300._abi"]
+    cloud, cfg, U0 = _system(hcc, kind, h)
+    t = _ctx(hcc, cfg("fp32"), cloud, U0, tiles=True)
+    s = _ctx(hcc, cfg("fp32"), cloud, U0, tiles=False)
+    info = t.tile_staging()
+    assert info["active"] and info["largest_union"] > 0
+    assert not s.tile_staging()["active"]
+    inner = cloud.is_boundary == 0
+    assert _rel_l1(t.compute_rhs(), s.compute_rhs(), inner) < 1e-5
+    o = oracle.OracleContext(cfg("fp64"), abi)
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    o.prepare_geometry()
+    o.upload_state(U0)
+    dt = 0.4 * o.time_step()
+    for k in range(3):
+        for c in (t, s, o):
+            c.step(k * dt, dt)
+    ut, us, uo = t.download_state(), s.download_state(), o.download_state()
+    assert np.all(np.isfinite(ut))
+    assert _rel_l1(ut, us, inner) < 1e-5
+    assert _rel_l1(ut, uo, inner) < 1e-5
+    for c in (t, s, o):
+        c.close()
+
+
+def test_tile_step_graph_matches_host_driven_tile_step(hcc, cuda_lib):
+    """The captured step graph and the host-driven step run the same tile kernels: bit-identical results."""
+    cloud, cfg, U0 = _system(hcc, "euler2d", 0.01)
+    a = _ctx(hcc, cfg("fp32"), cloud, U0)
+    b = _ctx(hcc, cfg("fp32"), cloud, U0)
+    b.set_step_graphs(False)
+    dt = 0.4 * a.time_step()
+    for k in range(3):
+        a.step(k * dt, dt)
+        b.step(k * dt, dt)
+    assert np.array_equal(a.download_state(dtype=np.float32), b.download_state(dtype=np.float32))
+    np.testing.assert_array_equal(a.mood_flags(), b.mood_flags())
+
+
+def test_tile_staging_only_where_it_applies(hcc, cuda_lib):
+    cloud, cfg, U0 = _system(hcc, "euler2d", 0.02)
+    g = _ctx(hcc, cfg("fp64"), cloud, U0)
+    assert not g.tile_staging()["active"]                     # FP64 keeps the stream-fed (bit-exact) passes
+    h = 0.02
+    c3 = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(3, 0), precision="fp32", bc_map=OUTFLOW)
+    g3 = _ctx(hcc, c3, cloud, U0)
+    assert not g3.tile_staging()["active"]                    # MUSCL3: degree-2 reconstruction
+    ce = hcc.make_config(hcc.Euler(2), cloud, scheme=hcc.MUSCL(2, 2), precision="fp32", bc_map=OUTFLOW,
+                         mood=hcc.MOOD(hcc.EPD2, hcc.MOODu1(1e-4 * h * h)))
+    assert not _ctx(hcc, ce, cloud, U0).tile_staging()["active"]
+    # a small periodic box: a tile's union spans too much of the period for consistent minimum-image offsets
+    small, cfgs, Us = _system(hcc, "advection", 0.05, periodic=True)
+    assert not _ctx(hcc, cfgs("fp32"), small, Us).tile_staging()["active"]
+    big, cfgb, Ub = _system(hcc, "advection", 0.005, periodic=True)
+    gb = _ctx(hcc, cfgb("fp32"), big, Ub)
+    assert gb.tile_staging()["active"]
+    gs = _ctx(hcc, cfgb("fp32"), big, Ub, tiles=False)
+    inner = big.is_boundary == 0
+    assert _rel_l1(gb.compute_rhs(), gs.compute_rhs(), inner) < 1e-5
+    # a moving grid reads the slot streams
+    cl, cfgm, Um = _system(hcc, "euler2d", 0.02)
+    gm = _ctx(hcc, cfgm("fp32"), cl, Um)
+    assert gm.tile_staging()["active"]
+    gm.set_mover(hcc.mover("lagrangian"))
+    assert not gm.tile_staging()["active"]
