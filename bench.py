@@ -68,6 +68,7 @@ WORKLOADS = {
     "euler2d_quadrant_250k": (2, 2e-3, "2-D Euler quadrant Riemann, h=2e-3 (250k interior), MUSCL2+MOOD, SSP-RK3"),
     "euler3d_blast_8M": (3, 1 / 200, "3-D Euler spherical blast, h=1/200 (8.0M interior), MUSCL2+MOOD, SSP-RK3"),
     "euler3d_blast_1M": (3, 1 / 100, "3-D Euler spherical blast, h=1/100 (1.0M interior), MUSCL2+MOOD, SSP-RK3"),
+    "euler3d_blast_262k": (3, 1 / 64, "3-D Euler spherical blast, h=1/64 (262k interior), MUSCL2+MOOD, SSP-RK3"),
 }
 
 
@@ -574,6 +575,8 @@ def run_profile_case(args):
     ctx.build_neighbours()
     ctx.prepare_geometry()
     ctx.upload_state(U0.astype(np.float32))
+    if not TILE_STAGING:
+        ctx.set_tile_staging(False)
     if args.profile != "plain":
         ctx.set_predictor(pred, PREDICTOR_THRESHOLD)
     ctx.set_step_graphs(False)
