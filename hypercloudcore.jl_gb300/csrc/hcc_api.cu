@@ -1548,7 +1548,10 @@ hcc_status build_tiles(hcc_ctx *c) {
                           (pde == HCC_PDE_EULER || pde == HCC_PDE_ADVECTION || pde == HCC_PDE_BGK);
     if (!eligible || c->n == 0) return HCC_OK;
     const int D = c->D, M = c->M;
-    const int W = (4 + M + D * M + 3) / 4 * 4;                 // shared-memory row of the flux pass (floats)
+    // shared memory of the flux pass per union entry (floats): the int4 position and the state + gradient row in an
+    // odd number of 16-byte groups (tile_flux_row in hcc_stage_impl.cuh)
+    const int groups = (M + D * M + 3) / 4;
+    const int W = 4 + 4 * (groups % 2 == 1 ? groups : groups + 1);
     const long budget = 200L * 1024 - long(HCC_TILE) * 4 * M * long(sizeof(float));
     TileBuild b{};
     b.n = c->n; b.npad = c->npad; b.D = D; b.kmax = std::max(c->kmax, 1);

@@ -1245,15 +1245,22 @@ __global__ void __launch_bounds__(128) k_flux_tiles(const StageArgs<T> a) {
 // ----------------------------------------------------------------------------------- tile-staged full passes (FP32)
 // Full gather and flux passes of an FP32 context with tile tables (TileView): one block per tile of HCC_TILE
 // consecutive particles first copies the tile's neighbour union into shared memory -- positions (and orders), states,
-// and for the flux pass the gradients -- with loads that follow the ascending union ids (consecutive ids: contiguous,
-// coalesced words), then every slot reads its neighbour from shared memory. Offsets x_j - x_i are exact differences
-// of the quantised union positions, rounded once to FP32; the weight w(|x|^2) and the slot's gradient and divergence
-// weights follow from the particle's FP32 fit rows. The arithmetic after that is flux_slot / the cached gather of the
-// stream-fed passes.
+// and for the flux pass the gradients; a thread copies whole entries, and the ascending union ids make a warp's loads
+// cover contiguous runs -- then every slot reads its neighbour from shared memory with 16-byte loads. Offsets
+// x_j - x_i are exact differences of the quantised union positions, rounded once to FP32; the weight w(|x|^2) and the
+// slot's gradient and divergence weights follow from the particle's FP32 fit rows. The arithmetic after that is
+// flux_slot / the cached gather of the stream-fed passes. Each thread loads the union place of its next slot while
+// it computes the current one.
 
-// Shared-memory row of one union entry: int4 position (the order in .w for the flux pass), then the state, then (flux
-// pass) the gradient; a multiple of 4 words so rows start on 16 bytes.
-template <int D, int M, bool GRAD> constexpr int tile_row_words() { return (4 + M + (GRAD ? D * M : 0) + 3) / 4 * 4; }
+// Shared-memory layout. Gather pass: one row per union entry, the position (D ints) then the state. Flux pass: an
+// int4 array of positions (the order in .w), then one row per entry of the state and the gradient. Rows are whole
+// 16-byte groups, an odd number of them, so the rows that the lanes of a warp read spread over the banks.
+constexpr int tile_odd_groups(int words) {
+    const int g = (words + 3) / 4;
+    return (g % 2 == 1) ? g : g + 1;
+}
+template <int D, int M> constexpr int tile_gather_row() { return 4 * tile_odd_groups(D + M); }
+template <int D, int M> constexpr int tile_flux_row() { return 4 * tile_odd_groups(M + D * M); }
 
 // Exponential weight of a squared distance (MLSWeightFunctions.jl:68-82: 1 / the degree-4 Taylor sum of e^y,
 // y = alpha r^2 / R^2), FP32.
@@ -1263,36 +1270,35 @@ __device__ __forceinline__ float tile_weight(float r2, float wscale) {
 }
 
 template <int D>
-__device__ __forceinline__ void tile_offset(const int4 qj, const int4 qi, float qt, float *x) {
-    x[0] = float(qj.x - qi.x) * qt;
-    if constexpr (D > 1) x[1] = float(qj.y - qi.y) * qt;
-    if constexpr (D > 2) x[2] = float(qj.z - qi.z) * qt;
+__device__ __forceinline__ void tile_offset(const int *qj, const int *qi, float qt, float *x) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[d] = float(qj[d] - qi[d]) * qt;
 }
 
-// Stage the union of tile t: rows of W words; the state (and gradient) words of each entry from global memory.
-template <int D, int M, bool GRAD>
-__device__ __forceinline__ int tile_stage(const StageArgs<float> &a, int64_t t, float *sm) {
-    constexpr int W = tile_row_words<D, M, GRAD>();
-    const int64_t u0 = a.tv.ustart[t];
-    const int nu = int(a.tv.ustart[t + 1] - u0);
-    const int32_t *uid = a.tv.uid + u0;
-    for (int e = threadIdx.x; e < nu; e += blockDim.x) {
-        int4 q = a.tv.upos[u0 + e];
-        if constexpr (GRAD) q.w = a.orders[uid[e]];
-        *reinterpret_cast<int4 *>(sm + e * W) = q;
+// N words of a 16-byte-aligned shared-memory row as whole 16-byte loads.
+template <int N>
+__device__ __forceinline__ void lds_words(const float *row, float *out) {
+    constexpr int G = (N + 3) / 4;
+    const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        const float4 v = r4[g];
+        if (4 * g + 0 < N) out[4 * g + 0] = v.x;
+        if (4 * g + 1 < N) out[4 * g + 1] = v.y;
+        if (4 * g + 2 < N) out[4 * g + 2] = v.z;
+        if (4 * g + 3 < N) out[4 * g + 3] = v.w;
     }
-    for (int f = threadIdx.x; f < nu * M; f += blockDim.x) {
-        const int e = f / M, m = f - e * M;
-        sm[e * W + 4 + m] = a.U[int64_t(uid[e]) * M + m];
-    }
-    if constexpr (GRAD) {
-        constexpr int G = D * M;
-        for (int f = threadIdx.x; f < nu * G; f += blockDim.x) {
-            const int e = f / G, q = f - e * G;
-            sm[e * W + 4 + M + q] = a.grad[int64_t(uid[e]) * G + q];
-        }
-    }
-    return nu;
+}
+
+// N words into a 16-byte-aligned shared-memory row (the padding of the last group is written as zero).
+template <int N>
+__device__ __forceinline__ void sts_words(float *row, const float *in) {
+    constexpr int G = (N + 3) / 4;
+    float4 *r4 = reinterpret_cast<float4 *>(row);
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+        r4[g] = make_float4(in[4 * g], 4 * g + 1 < N ? in[4 * g + 1] : 0.0f, 4 * g + 2 < N ? in[4 * g + 2] : 0.0f,
+                            4 * g + 3 < N ? in[4 * g + 3] : 0.0f);
 }
 
 // Reconstruction pre-pass, one thread per particle of the tile: the cached degree-1 fit of gather_one with the
@@ -1301,29 +1307,41 @@ __device__ __forceinline__ int tile_stage(const StageArgs<float> &a, int64_t t, 
 template <int D, int M, int PDE>
 __global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float> a) {
     extern __shared__ __align__(16) float sm[];
-    constexpr int W = tile_row_words<D, M, false>();
+    constexpr int W = tile_gather_row<D, M>();
     const int64_t t = blockIdx.x;
-    tile_stage<D, M, false>(a, t, sm);
+    {
+        const int64_t u0 = a.tv.ustart[t];
+        const int nu = int(a.tv.ustart[t + 1] - u0);
+        for (int e = threadIdx.x; e < nu; e += blockDim.x) {
+            const int32_t j = a.tv.uid[u0 + e];
+            const int4 q = a.tv.upos[u0 + e];
+            float v[D + M];
+            v[0] = __int_as_float(q.x);
+            if constexpr (D > 1) v[1] = __int_as_float(q.y);
+            if constexpr (D > 2) v[2] = __int_as_float(q.z);
+#pragma unroll
+            for (int m = 0; m < M; ++m) v[D + m] = a.U[int64_t(j) * M + m];
+            sts_words<D + M>(sm + e * W, v);
+        }
+    }
     __syncthreads();
     const int64_t i = t * HCC_TILE + threadIdx.x;
     if (i >= a.g.n || a.g.bnd[i]) return;
     const int cnt = a.g.cnt[i];
-    int p = a.orders[i];
     {
-        int q = p;
+        int q = a.orders[i];
         while (q > 1 && cnt < basis_count(D, q - 1)) --q;
         if (!(q == a.sc.max_order && q > 1 && a.g.ok_r[i] && a.sc.limiter == HCC_LIMITER_NONE)) {
             gather_one<float, D, M, PDE, 1>(a, i);
             return;
         }
-        p = q;
     }
     const int64_t np = a.g.npad;
-    const float *own = sm + int(a.tv.lself[i]) * W;
-    const int4 qi = *reinterpret_cast<const int4 *>(own);
-    float fi[M];
+    float own[D + M];
+    lds_words<D + M>(sm + int(a.tv.lself[i]) * W, own);
+    int qi[D];
 #pragma unroll
-    for (int m = 0; m < M; ++m) fi[m] = own[4 + m];
+    for (int d = 0; d < D; ++d) qi[d] = __float_as_int(own[d]);
     float G[D][D];
     const float *cf = a.tv.coef + i * a.tv.cw + D + D * D;
 #pragma unroll
@@ -1336,11 +1354,19 @@ __global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float>
     for (int b = 0; b < D; ++b)
 #pragma unroll
         for (int m = 0; m < M; ++m) out[b][m] = 0.0f;
-#pragma unroll 2
+    const uint16_t *lp = a.tv.lidx + i;
+    int ln = cnt > 0 ? int(*lp) : 0;
     for (int k = 0; k < cnt; ++k) {
-        const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
+        const int l = ln;
+        lp += np;
+        if (k + 1 < cnt) ln = int(*lp);
+        float r[D + M];
+        lds_words<D + M>(sm + l * W, r);
+        int qj[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) qj[d] = __float_as_int(r[d]);
         float x[D];
-        tile_offset<D>(*reinterpret_cast<const int4 *>(row), qi, qt, x);
+        tile_offset<D>(qj, qi, qt, x);
         float r2 = x[0] * x[0];
 #pragma unroll
         for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
@@ -1355,7 +1381,7 @@ __global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float>
         }
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            const float dm = row[4 + m] - fi[m];
+            const float dm = r[D + m] - own[D + m];
 #pragma unroll
             for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
         }
@@ -1370,10 +1396,26 @@ template <int D, int M> constexpr int tile_flux_min_blocks() { return M >= 8 ? 1
 template <int D, int M, int PDE>
 __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_flux_tile(const StageArgs<float> a) {
     extern __shared__ __align__(16) float sm[];
-    constexpr int W = tile_row_words<D, M, true>();
+    constexpr int W = tile_flux_row<D, M>();
+    constexpr int RW = M + D * M;                 // used words of a row: the state, then the gradient
     const int64_t t = blockIdx.x;
-    const int nu = tile_stage<D, M, true>(a, t, sm);
-    FluxPart<float, M> *parts = reinterpret_cast<FluxPart<float, M> *>(sm + nu * W);
+    const int64_t u0 = a.tv.ustart[t];
+    const int nu = int(a.tv.ustart[t + 1] - u0);
+    int4 *spos = reinterpret_cast<int4 *>(sm);
+    float *srow = sm + 4 * a.tv.umax;
+    FluxPart<float, M> *parts = reinterpret_cast<FluxPart<float, M> *>(srow + a.tv.umax * W);
+    for (int e = threadIdx.x; e < nu; e += blockDim.x) {
+        const int32_t j = a.tv.uid[u0 + e];
+        int4 q = a.tv.upos[u0 + e];
+        q.w = a.orders[j];
+        spos[e] = q;
+        float v[RW];
+#pragma unroll
+        for (int m = 0; m < M; ++m) v[m] = a.U[int64_t(j) * M + m];
+#pragma unroll
+        for (int c = 0; c < D * M; ++c) v[M + c] = a.grad[int64_t(j) * (D * M) + c];
+        sts_words<RW>(srow + e * W, v);
+    }
     __syncthreads();
     const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
     const int64_t i = t * HCC_TILE + pl;
@@ -1383,18 +1425,22 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
     AccumV<float, M> acc;
     float mn[M], mx[M], fi[M];
     float gi[D][M], Fi[D][M];
-    int cnt = 0;
     if (live) {
-        cnt = a.g.cnt[i];
-        const float *own = sm + int(a.tv.lself[i]) * W;
-        const int4 qi = *reinterpret_cast<const int4 *>(own);
-        const int oi_own = qi.w;
+        const int cnt = a.g.cnt[i];
+        const int li = int(a.tv.lself[i]);
+        const int4 q4 = spos[li];
+        const int qi[3] = {q4.x, q4.y, q4.z};
+        const int oi_own = q4.w;
+        {
+            float own[RW];
+            lds_words<RW>(srow + li * W, own);
 #pragma unroll
-        for (int m = 0; m < M; ++m) { fi[m] = own[4 + m]; mn[m] = fi[m]; mx[m] = fi[m]; }
+            for (int m = 0; m < M; ++m) { fi[m] = own[m]; mn[m] = fi[m]; mx[m] = fi[m]; }
 #pragma unroll
-        for (int b = 0; b < D; ++b)
+            for (int b = 0; b < D; ++b)
 #pragma unroll
-            for (int m = 0; m < M; ++m) gi[b][m] = own[4 + M + b * M + m];
+                for (int m = 0; m < M; ++m) gi[b][m] = own[M + b * M + m];
+        }
         float lami[D];
         flux_and_speed<float, D, M, PDE>(a.ph, fi, Fi, lami, nullptr);
 #pragma unroll
@@ -1402,6 +1448,9 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
 #pragma unroll
             for (int m = 0; m < M; ++m) Fi[d][m] = 2.0f * Fi[d][m];
         const bool wok = cnt > 0 && a.g.ok_d[i];
+        const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+        const int64_t lstep = 2 * np;
+        int ln = h < cnt ? int(*lp) : 0;
         if (wok) {
             const float *cf = a.tv.coef + i * a.tv.cw;
             float A[D], B[D][D];
@@ -1413,8 +1462,11 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
             }
             const float qt = a.tv.quantum[t], ws = a.tv.wscale;
             for (int k = h; k < cnt; k += 2) {
-                const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
-                const int4 qj = *reinterpret_cast<const int4 *>(row);
+                const int l = ln;
+                lp += lstep;
+                if (k + 2 < cnt) ln = int(*lp);
+                const int4 qj4 = spos[l];
+                const int qj[3] = {qj4.x, qj4.y, qj4.z};
                 float dk[D], wk[D];
                 tile_offset<D>(qj, qi, qt, dk);
                 float r2 = dk[0] * dk[0];
@@ -1428,29 +1480,30 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                     for (int e = 0; e < D; ++e) v = v + B[d][e] * dk[e];
                     wk[d] = w * v;
                 }
-                float fj[M], gj[D * M];
-#pragma unroll
-                for (int m = 0; m < M; ++m) fj[m] = row[4 + m];
-#pragma unroll
-                for (int q = 0; q < D * M; ++q) gj[q] = row[4 + M + q];
+                float r[RW];
+                lds_words<RW>(srow + l * W, r);
                 if (need_ext) {
 #pragma unroll
-                    for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], fj[m]); mx[m] = vmax(mx[m], fj[m]); }
+                    for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], r[m]); mx[m] = vmax(mx[m], r[m]); }
                 }
-                const int oj_own = qj.w;
+                const int oj_own = qj4.w;
                 int oi, oj;
                 if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
                 else { oi = oi_own; oj = oj_own; }
                 const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
                                                     oj_own < a.sc.max_order);
-                flux_slot<float, D, M, PDE, 1, false, false>(a, fi, gi, Fi, nullptr, fj, gj, oi, oj, below, dk, wk,
-                                                             acc, i, k);
+                flux_slot<float, D, M, PDE, 1, false, false>(a, fi, gi, Fi, nullptr, r, r + M, oi, oj, below, dk,
+                                                             wk, acc, i, k);
             }
         } else if (need_ext) {
             for (int k = h; k < cnt; k += 2) {
-                const float *row = sm + int(a.tv.lidx[int64_t(k) * np + i]) * W;
+                const int l = ln;
+                lp += lstep;
+                if (k + 2 < cnt) ln = int(*lp);
+                float r[M];
+                lds_words<M>(srow + l * W, r);
 #pragma unroll
-                for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], row[4 + m]); mx[m] = vmax(mx[m], row[4 + m]); }
+                for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], r[m]); mx[m] = vmax(mx[m], r[m]); }
             }
         }
         if (h == 1) {
@@ -1510,10 +1563,10 @@ inline int tile_smem_optin() {
 
 // Dynamic shared memory of the tile passes for the largest union.
 template <int D, int M> inline size_t tile_gather_smem(int umax) {
-    return size_t(umax) * tile_row_words<D, M, false>() * sizeof(float);
+    return size_t(umax) * tile_gather_row<D, M>() * sizeof(float);
 }
 template <int D, int M> inline size_t tile_flux_smem(int umax) {
-    return size_t(umax) * tile_row_words<D, M, true>() * sizeof(float) + size_t(HCC_TILE) * sizeof(FluxPart<float, M>);
+    return size_t(umax) * (4 + tile_flux_row<D, M>()) * sizeof(float) + size_t(HCC_TILE) * sizeof(FluxPart<float, M>);
 }
 
 // ----------------------------------------------------------------------------------- WENO (scalar)
