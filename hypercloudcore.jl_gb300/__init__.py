@@ -31,7 +31,7 @@ from ._abi import (HccConfig, HccCounters, FP32, FP64, PDE_ADVECTION, PDE_BGK, P
 from .cloud import Cloud, rectangular_cloud, morton_permutation, splitmix64_uniform
 
 PKG_DIR = Path(__file__).resolve().parent
-LIB_PATH = PKG_DIR / "libhcc_gb300.so"
+LIB_PATH = Path(os.environ["HCC_GB300_LIB"]) if os.environ.get("HCC_GB300_LIB") else PKG_DIR / "libhcc_gb300.so"
 
 
 class HCCError(RuntimeError):

@@ -1786,7 +1786,7 @@ hcc_status hcc_step(hcc_ctx *c, double t, double dt) {
 const char *hcc_build_info(void) {
     return "flux_block=" HCC_STR(HCC_FLUX_BLOCK) " flux_minb=" HCC_STR(HCC_FLUX_MINB)
            " flux_minb_wide=" HCC_STR(HCC_FLUX_MINB_WIDE) " flux_minb64=" HCC_STR(HCC_FLUX_MINB64)
-           " flux_minb_many=" HCC_STR(HCC_FLUX_MINB_MANY);
+           " flux_minb_many=" HCC_STR(HCC_FLUX_MINB_MANY) " fp32_packed=" HCC_STR(HCC_FP32_PACKED);
 }
 
 hcc_status hcc_fp64_fma_rate(double *tflops_out) {

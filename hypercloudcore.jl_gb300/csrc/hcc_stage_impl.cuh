@@ -34,11 +34,21 @@ template <> struct Accum<float> {
 };
 
 // FP32 component vectors in pairs: the packed FP32x2 instructions of sm_100+ (per component identical to the scalar
-// operations; a - b as fma(b, -1, a) is the same rounding of the same exact value).
+// operations; a - b as fma(b, -1, a) is the same rounding of the same exact value). HCC_FP32_PACKED=0 builds the
+// same arithmetic from scalar instructions (identical results; a launch-shape choice measured per build).
+#if HCC_FP32_PACKED
 __device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+#else
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) {
+    return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+#endif
 __device__ __forceinline__ float2 p_bc(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 p_ld(const float *x, int q) { return make_float2(x[2 * q], x[2 * q + 1]); }
 __device__ __forceinline__ void p_st(float *x, int q, float2 v) { x[2 * q] = v.x; x[2 * q + 1] = v.y; }
@@ -1354,37 +1364,47 @@ __global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float>
     for (int b = 0; b < D; ++b)
 #pragma unroll
         for (int m = 0; m < M; ++m) out[b][m] = 0.0f;
+    // union places of the slots in groups of PF, the next group's loads in flight while this group is summed
+    constexpr int PF = 8;
     const uint16_t *lp = a.tv.lidx + i;
-    int ln = cnt > 0 ? int(*lp) : 0;
-    for (int k = 0; k < cnt; ++k) {
-        const int l = ln;
-        lp += np;
-        if (k + 1 < cnt) ln = int(*lp);
-        float r[D + M];
-        lds_words<D + M>(sm + l * W, r);
-        int qj[D];
+    int lbuf[PF];
 #pragma unroll
-        for (int d = 0; d < D; ++d) qj[d] = __float_as_int(r[d]);
-        float x[D];
-        tile_offset<D>(qj, qi, qt, x);
-        float r2 = x[0] * x[0];
+    for (int q = 0; q < PF; ++q) lbuf[q] = q < cnt ? int(lp[int64_t(q) * np]) : 0;
+    for (int k0 = 0; k0 < cnt; k0 += PF) {
+        int lnext[PF];
 #pragma unroll
-        for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
-        const float w = tile_weight(r2, ws);
-        float gk[D];
+        for (int q = 0; q < PF; ++q) lnext[q] = k0 + PF + q < cnt ? int(lp[int64_t(k0 + PF + q) * np]) : 0;
 #pragma unroll
-        for (int b = 0; b < D; ++b) {
-            float v = G[b][0] * x[0];
+        for (int q = 0; q < PF; ++q) {
+            if (k0 + q >= cnt) break;
+            float r[D + M];
+            lds_words<D + M>(sm + lbuf[q] * W, r);
+            int qj[D];
 #pragma unroll
-            for (int c = 1; c < D; ++c) v = v + G[b][c] * x[c];
-            gk[b] = w * v;
+            for (int d = 0; d < D; ++d) qj[d] = __float_as_int(r[d]);
+            float x[D];
+            tile_offset<D>(qj, qi, qt, x);
+            float r2 = x[0] * x[0];
+#pragma unroll
+            for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
+            const float w = tile_weight(r2, ws);
+            float gk[D];
+#pragma unroll
+            for (int b = 0; b < D; ++b) {
+                float v = G[b][0] * x[0];
+#pragma unroll
+                for (int c = 1; c < D; ++c) v = v + G[b][c] * x[c];
+                gk[b] = w * v;
+            }
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const float dm = r[D + m] - own[D + m];
+#pragma unroll
+                for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
+            }
         }
 #pragma unroll
-        for (int m = 0; m < M; ++m) {
-            const float dm = r[D + m] - own[D + m];
-#pragma unroll
-            for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
-        }
+        for (int q = 0; q < PF; ++q) lbuf[q] = lnext[q];
     }
     store_vec<float, D * M>(a.grad + i * (D * M), &out[0][0]);
 }
