@@ -35,7 +35,7 @@ template <> struct Accum<float> {
 
 // FP32 component vectors in pairs: the packed FP32x2 instructions of sm_100+ (per component identical to the scalar
 // operations; a - b as fma(b, -1, a) is the same rounding of the same exact value). HCC_FP32_PACKED=0 builds the
-// same arithmetic from scalar instructions (identical results; a launch-shape choice measured per build).
+// same arithmetic from scalar instructions (identical results; which form runs faster is measured).
 #if HCC_FP32_PACKED
 __device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
