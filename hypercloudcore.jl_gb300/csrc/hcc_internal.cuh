@@ -23,7 +23,8 @@
 #define HCC_FLUX_MINB_WIDE 4       // FP32, D*M >= 12 (3-D Euler): 128 registers
 #endif
 #ifndef HCC_FP32_PACKED
-#define HCC_FP32_PACKED 1          // FP32 stage kernels: packed FP32x2 instructions for component pairs
+#define HCC_FP32_PACKED 0          // FP32 stage kernels: 1 = packed FP32x2 instructions for component pairs (measured
+                                   // slower than scalar instructions in the tile-staged 3-D flux pass)
 #endif
 #ifndef HCC_FLUX_MINB64
 #define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
