@@ -548,7 +548,7 @@ class Context:
         self._check(self.lib.hcc_load_snapshot(self._h, str(path).encode()), "hcc_load_snapshot")
 
     def set_tile_staging(self, enable: bool = True):
-        """Tile-staged FP32 full passes (default on where the context qualifies) or the stream-fed ones."""
+        """Tile-staged FP32 full passes (the default for 3-D contexts that qualify) or the stream-fed ones."""
         self._check(self.lib.hcc_set_tile_staging(self._h, int(bool(enable))), "hcc_set_tile_staging")
 
     def tile_staging(self) -> dict:

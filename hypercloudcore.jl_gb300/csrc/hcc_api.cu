@@ -1053,6 +1053,9 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
     const hcc_config &f = c->cfg;
     if (f.abi_version != HCC_ABI_VERSION) return c->fail(HCC_ERR_INVALID, "abi_version mismatch");
     c->D = f.dim;
+    // tile staging by default where it measured faster: the 3-D stencils (K ~ 66; flux 7.05 vs 10.4 ms at 8.0M
+    // points); 2-D stencils (K ~ 19) ran faster stream-fed (flux 0.21 vs 0.30 ms at 1.0M)
+    c->tile_enabled = f.dim == 3 ? 1 : 0;
     c->M = f.n_vars;
     c->f32 = f.precision == HCC_FP32;
     c->capacity = capacity;

@@ -471,7 +471,8 @@ const char *hcc_build_info(void);
    shared memory, and per slot the neighbour's place in it; the full passes then recompute the slot offsets, weights
    and divergence / gradient weights from quantised positions and per-particle FP32 fit rows instead of reading the
    per-slot streams. Results agree with the stream-fed passes to FP32 rounding (both round the same FP64 geometry).
-   Enabled by default where the cloud qualifies; enable = 0 keeps the stream-fed passes. */
+   Enabled by default for 3-D contexts (about 66 neighbours a particle: faster than the stream-fed passes), off by
+   default for 1-D and 2-D ones (about 19 neighbours: slower); enable = 1 / 0 chooses either way. */
 hcc_status hcc_set_tile_staging(hcc_ctx *ctx, int32_t enable);
 /* Whether the full passes of the next step are tile-staged, the union entries over all tiles and the largest union
    (any output may be NULL). */
