@@ -6,13 +6,17 @@
 #   using HyperCloudCore, HCCGB300
 #   ts = GB300RKTimeStepper(eq, pg, MUSCL(Float64, 2, 4, 2, NoLimiter(), RusanovFlux(); div_order = 2),
 #                           MOOD(EPD1(), MOODu1(1e-4 * prod(pg.meta.dx))), RK3_SSP_Tableau(Float64);
-#                           bc_map = Dict(1 => HCCGB300.OUTFLOW, 2 => HCCGB300.OUTFLOW, 3 => HCCGB300.OUTFLOW,
-#                                         4 => HCCGB300.OUTFLOW), precision = :fp64)
+#                           precision = :fp64)
 #   while t < tmax
 #       dt = min(0.4 * get_time_step(pg, eq, ts), tmax - t)
 #       ts(eq, pg, t, dt)
 #       t += dt
 #   end
+#
+# The boundary conditions come from the grid's own map, pg.geometry.bc_map (FixedDirichlet / OutflowBC per tag,
+# BoundaryConditions.jl:43-130); the tableau is the tableau object itself (any built-in one of
+# ButcherTableaus.jl:125-263); the scheme may be MUSCL (with its div_order, moment_correction and streamed
+# settings), WENO, CentralDivergence or UpwindDivergence.
 #
 # The grid's positions, tags and states are uploaded at construction; `ts(eq, pg, t, dt)` runs the step on the
 # GPU and writes `pg.rhos` and `pg.core.particle_orders` back, so every host-side consumer of the reference
@@ -26,7 +30,27 @@ export GB300RKTimeStepper, hcc_pde_kind
 
 const libhcc = get(ENV, "HCC_GB300_LIB", joinpath(@__DIR__, "..", "libhcc_gb300.so"))
 
-const KEEP, DIRICHLET, OUTFLOW = Int32(0), Int32(1), Int32(2)
+# The enums of include/hcc.h, value for value.
+const HCC_BC_KEEP, HCC_BC_DIRICHLET, HCC_BC_OUTFLOW = Int32(0), Int32(1), Int32(2)
+const KEEP, DIRICHLET, OUTFLOW = HCC_BC_KEEP, HCC_BC_DIRICHLET, HCC_BC_OUTFLOW
+const HCC_TAB_RK1_EULER = Int32(0)
+const HCC_TAB_RK2_SSP = Int32(1)
+const HCC_TAB_RK2_RALSTON = Int32(2)
+const HCC_TAB_RK3_SSP = Int32(3)
+const HCC_TAB_RK4_CLASSICAL = Int32(4)
+const HCC_TAB_RK4_SSP = Int32(5)
+const HCC_TAB_IMEX_EULER = Int32(6)
+const HCC_TAB_IMEX_ARS233 = Int32(7)
+const HCC_TAB_IMEX_ARS222 = Int32(8)
+const HCC_TAB_IMEX_PRSSP3 = Int32(9)
+const HCC_TAB_IMEX_SSP2332 = Int32(10)
+const HCC_MOOD_NONE, HCC_MOOD_U1, HCC_MOOD_PAD, HCC_MOOD_ONLY, HCC_MOOD_U2 = Int32(0), Int32(1), Int32(2), Int32(3), Int32(4)
+const HCC_EPD_NONE, HCC_EPD0, HCC_EPD1, HCC_EPD2, HCC_STRICT_EPD0 = Int32(0), Int32(1), Int32(2), Int32(3), Int32(4)
+const HCC_SCHEME_MUSCL, HCC_SCHEME_WENO, HCC_SCHEME_CENTRAL, HCC_SCHEME_UPWIND = Int32(0), Int32(1), Int32(2), Int32(3)
+const HCC_UPWIND_TIWARI, HCC_UPWIND_PRAVEEN = Int32(1), Int32(2)
+const HCC_LIMITER_NONE, HCC_LIMITER_BJ_SOFT, HCC_LIMITER_BJ_HARD = Int32(0), Int32(1), Int32(2)
+const HCC_LIMITER_VK_SOFT, HCC_LIMITER_VK_HARD = Int32(3), Int32(4)
+const HCC_FLUX_RUSANOV, HCC_FLUX_ALIGNED = Int32(0), Int32(1)
 
 # hcc_config (include/hcc.h), field for field
 mutable struct HccConfig
@@ -34,7 +58,7 @@ mutable struct HccConfig
     div_order::Int32; mood_criterion::Int32; mood_strategy::Int32; tableau::Int32; mood_substeps::Int32
     periodic::NTuple{3, Int32}; bc_by_tag::NTuple{16, Int32}; max_mood_iterations::Int32
     scheme::Int32; limiter::Int32; slot_capacity::Int32; flux::Int32; reset_orders_per_stage::Int32
-    reserved_i::NTuple{3, Int32}
+    upwind_algorithm::Int32; moment_correction::Int32; reserved_i::NTuple{1, Int32}
     dx::NTuple{3, Float64}; radius::Float64; weight_alpha::Float64
     canvas_min::NTuple{3, Float64}; canvas_max::NTuple{3, Float64}
     domain_min::NTuple{3, Float64}; domain_max::NTuple{3, Float64}
@@ -58,22 +82,100 @@ mutable struct GB300RKTimeStepper{D, M} <: TimeStepper
     N::Int
 end
 
-_tableau_id(bt) = error("unknown tableau")
-_strategy_id(::EPD0) = Int32(1); _strategy_id(::EPD1) = Int32(2); _strategy_id(::EPD2) = Int32(3)
-_strategy_id(::StrictEPD0) = Int32(4)
-_strategy_id(::MOODStrategy) = Int32(0)
-_flux_id(::RusanovFlux) = Int32(0)
-_flux_id(::AlignedRusanovFlux) = Int32(1)
-_limiter_id(::NoLimiter) = Int32(0)
-_limiter_id(::BarthJespersenLimiter{:soft}) = Int32(1)
-_limiter_id(::BarthJespersenLimiter{:hard}) = Int32(2)
-_limiter_id(::VenkatakrishnanLimiter{:soft}) = Int32(3)
-_limiter_id(::VenkatakrishnanLimiter{:hard}) = Int32(4)
-_criterion(c::MOODu1) = (Int32(1), Float64(c.d))
-_criterion(c::MOODu2) = (Int32(4), Float64(c.d))
-_criterion(::MOODPAD) = (Int32(2), 0.0)
-_criterion(::OnlyMOOD) = (Int32(3), 0.0)
-_criterion(::NoMOOD) = (Int32(0), 0.0)
+# The tableau object (ButcherTableaus.jl:125-263 build IMEXButcherTableau values, not types): matched coefficient
+# for coefficient against the built-in tableaus of its element type; an Integer is taken as the hcc_tableau id.
+const _BUILTIN_TABLEAUS = ((HyperCloudCore.RK1_Euler_Tableau, HCC_TAB_RK1_EULER),
+                           (HyperCloudCore.RK2_SSP_Tableau, HCC_TAB_RK2_SSP),
+                           (HyperCloudCore.RK2_Ralston_Tableau, HCC_TAB_RK2_RALSTON),
+                           (HyperCloudCore.RK3_SSP_Tableau, HCC_TAB_RK3_SSP),
+                           (HyperCloudCore.RK4_Classical_Tableau, HCC_TAB_RK4_CLASSICAL),
+                           (HyperCloudCore.RK4_SSP_Tableau, HCC_TAB_RK4_SSP),
+                           (HyperCloudCore.IMEX_Euler_Tableau, HCC_TAB_IMEX_EULER),
+                           (HyperCloudCore.IMEX_ARS233_Tableau, HCC_TAB_IMEX_ARS233),
+                           (HyperCloudCore.IMEX_ARS222_Tableau, HCC_TAB_IMEX_ARS222),
+                           (HyperCloudCore.IMEX_PRSSP3_Tableau, HCC_TAB_IMEX_PRSSP3),
+                           (HyperCloudCore.IMEX_SSP2332_Tableau, HCC_TAB_IMEX_SSP2332))
+_same_tableau(x, y) = all(isapprox(getfield(x, f), getfield(y, f); rtol = 0, atol = 64 * eps(Float64))
+                          for f in (:a, :a_t, :c, :c_t, :b, :b_t))
+function _tableau_id(bt::HyperCloudCore.IMEXButcherTableau{T}) where {T}
+    for (make, id) in _BUILTIN_TABLEAUS
+        ref = make(T)
+        size(ref.a) == size(bt.a) && _same_tableau(bt, ref) && return id
+    end
+    error("GB300 stepper: the tableau is none of the built-in tableaus (ButcherTableaus.jl:125-263)")
+end
+_tableau_id(id::Integer) = Int32(id)
+
+_strategy_id(::EPD0) = HCC_EPD0
+_strategy_id(::EPD1) = HCC_EPD1
+_strategy_id(::EPD2) = HCC_EPD2
+_strategy_id(::StrictEPD0) = HCC_STRICT_EPD0
+_strategy_id(::MOODStrategy) = HCC_EPD_NONE
+_flux_id(::RusanovFlux) = HCC_FLUX_RUSANOV
+_flux_id(::AlignedRusanovFlux) = HCC_FLUX_ALIGNED
+_flux_id(f) = error("GB300 stepper: unsupported numerical flux $(typeof(f))")
+_limiter_id(::NoLimiter) = HCC_LIMITER_NONE
+_limiter_id(::BarthJespersenLimiter{:soft}) = HCC_LIMITER_BJ_SOFT
+_limiter_id(::BarthJespersenLimiter{:hard}) = HCC_LIMITER_BJ_HARD
+_limiter_id(::VenkatakrishnanLimiter{:soft}) = HCC_LIMITER_VK_SOFT
+_limiter_id(::VenkatakrishnanLimiter{:hard}) = HCC_LIMITER_VK_HARD
+_limiter_id(l) = error("GB300 stepper: unsupported limiter $(typeof(l))")
+_criterion(c::MOODu1) = (HCC_MOOD_U1, Float64(c.d))
+_criterion(c::MOODu2) = (HCC_MOOD_U2, Float64(c.d))
+_criterion(::MOODPAD) = (HCC_MOOD_PAD, 0.0)
+_criterion(::OnlyMOOD) = (HCC_MOOD_ONLY, 0.0)
+_criterion(::NoMOOD) = (HCC_MOOD_NONE, 0.0)
+
+# pg.geometry.bc_map (tag => condition functor, Domains.jl:27; applied by apply_boundary_conditions!,
+# BoundaryConditions.jl:43-48) -> bc_by_tag. The library implements the two conditions the package ships.
+_bc_kind(::FixedDirichlet) = HCC_BC_DIRICHLET
+_bc_kind(::OutflowBC) = HCC_BC_OUTFLOW
+_bc_kind(bc) = error("GB300 stepper: no device implementation of the boundary condition $(typeof(bc))")
+function _bc_by_tag(bc_map)
+    kinds = fill(HCC_BC_KEEP, 16)
+    for (tag, bc) in bc_map
+        1 <= tag <= 16 || error("GB300 stepper: boundary tag $tag outside 1..16")
+        kinds[tag] = bc isa Integer ? Int32(bc) : _bc_kind(bc)
+    end
+    return ntuple(t -> kinds[t], 16)
+end
+
+# The divergence interpolator -> (scheme, order, div_order, limiter, flux, upwind algorithm, moment correction).
+# MUSCL's `streamed` setting selects between two evaluations of the same divergence (MUSCL.jl:426-458); the library
+# always streams, so either value is accepted.
+function _scheme!(cfg, interp::MUSCL{D, M, T, B_LEN, MAX_ORDER, DIV_ORDER}) where {D, M, T, B_LEN, MAX_ORDER, DIV_ORDER}
+    cfg.scheme = HCC_SCHEME_MUSCL
+    cfg.muscl_order = MAX_ORDER
+    cfg.div_order = DIV_ORDER
+    cfg.limiter = _limiter_id(interp.limiter)
+    cfg.flux = _flux_id(interp.flux)
+    cfg.moment_correction = Int32(interp.moment isa Val{true})
+    return cfg
+end
+function _scheme!(cfg, ::WENO{D, M, T, MAX_ORDER, DIV_ORDER}) where {D, M, T, MAX_ORDER, DIV_ORDER}
+    cfg.scheme, cfg.muscl_order, cfg.div_order = HCC_SCHEME_WENO, MAX_ORDER, DIV_ORDER
+    return cfg
+end
+function _scheme!(cfg, ::CentralDivergence{D, M, T, MAX_ORDER, DIV_ORDER}) where {D, M, T, MAX_ORDER, DIV_ORDER}
+    cfg.scheme, cfg.muscl_order, cfg.div_order = HCC_SCHEME_CENTRAL, MAX_ORDER, DIV_ORDER
+    return cfg
+end
+_upwind_alg(::Type{<:TiwariAlgorithm}) = HCC_UPWIND_TIWARI
+_upwind_alg(::Type{<:PraveenAlgorithm}) = HCC_UPWIND_PRAVEEN
+_upwind_alg(A) = error("GB300 stepper: unsupported upwind algorithm $A")
+function _scheme!(cfg, u::UpwindDivergence{D, M, T, MAX_ORDER, DIV_ORDER, B_LEN, INTERPS, ALG}) where
+        {D, M, T, MAX_ORDER, DIV_ORDER, B_LEN, INTERPS, ALG}
+    cfg.muscl_order, cfg.div_order = MAX_ORDER, DIV_ORDER
+    cfg.flux = _flux_id(u.flux)
+    if ALG <: ClassicAlgorithm             # UpwindDivergence(:Classic) is the first-order MUSCL scheme
+        cfg.scheme = HCC_SCHEME_MUSCL
+    else
+        cfg.scheme = HCC_SCHEME_UPWIND
+        cfg.upwind_algorithm = _upwind_alg(ALG)
+    end
+    return cfg
+end
+_scheme!(cfg, interp) = error("GB300 stepper: unsupported divergence interpolator $(typeof(interp))")
 
 # pg.mover (GridMovers.jl:28-63) -> hcc_set_mover; PrescribedMover takes a rigid motion (velocity, omega, center)
 struct HccMover
@@ -96,16 +198,14 @@ function _set_mover(h, mv; full_search_per_stage::Bool = false, volume_estimator
     _check(ccall((:hcc_set_mover, libhcc), Cint, (Ptr{Cvoid}, Ref{HccMover}), h, m), h, "hcc_set_mover")
 end
 
-function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T}, interp::MUSCL, mood::MOOD,
-                            tableau_id::Integer; bc_map = Dict{Int, Int32}(), precision::Symbol = :fp64,
+function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T}, interp, mood::MOOD,
+                            tableau; bc_map = nothing, precision::Symbol = :fp64,
                             reset_orders_per_stage::Bool = false, mood_substeps::Bool = true) where {D, M, T}
     cfg = HccConfig()
     cfg.dim, cfg.n_vars, cfg.pde = D, M, hcc_pde_kind(eq)
     cfg.precision = precision === :fp32 ? 1 : 0
-    cfg.muscl_order = HyperCloudCore._extract_order(interp)
-    cfg.limiter = _limiter_id(interp.limiter)
-    cfg.flux = _flux_id(interp.flux)
-    cfg.tableau = tableau_id
+    _scheme!(cfg, interp)
+    cfg.tableau = _tableau_id(tableau)
     cfg.reset_orders_per_stage = Int32(reset_orders_per_stage)
     cfg.mood_substeps = Int32(mood_substeps)
     cfg.mood_strategy = _strategy_id(mood.strategy)
@@ -119,7 +219,8 @@ function GB300RKTimeStepper(eq::HyperbolicPDE{D, M, T}, pg::ParticleGrid{D, M, T
     cfg.canvas_min = pad3(pg.domain.canvas_mins, 0.0); cfg.canvas_max = pad3(pg.domain.canvas_maxs, 1.0)
     cfg.domain_min = pad3(pg.geometry.mins, 0.0); cfg.domain_max = pad3(pg.geometry.maxs, 1.0)
     cfg.periodic = ntuple(d -> d <= D ? Int32(pg.domain.is_periodic[d]) : Int32(0), 3)
-    cfg.bc_by_tag = ntuple(t -> Int32(get(bc_map, t, KEEP)), 16)
+    # the grid's own conditions; an explicit bc_map (tag => FixedDirichlet() / OutflowBC() or an hcc_bc_kind) replaces them
+    cfg.bc_by_tag = _bc_by_tag(bc_map === nothing ? pg.geometry.bc_map : bc_map)
     cfg.gamma = hcc_gamma(eq)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     st = ccall((:hcc_create, libhcc), Cint, (Ref{HccConfig}, Int64, Ref{Ptr{Cvoid}}), cfg, 0, h)
@@ -139,11 +240,11 @@ end
 
 # build_timestepper(context; time_conf) (Builders/timestepper.jl:15-35) for the GB300 stepper: the same context keys
 # (:Equation, :Scheme, :MOOD, :Tableau, :Grid) and Time options (reset_orders_per_stage, full_search_per_stage,
-# mood_substeps), plus :Precision (:fp64 / :fp32) and :BCMap (tag => HCC_BC_* kind).
+# mood_substeps), plus :Precision (:fp64 / :fp32) and, to override the grid's own map, :BCMap.
 function build_gb300_timestepper(context::Dict; time_conf::Dict = Dict{Symbol, Any}())
     pg = context[:Grid]::ParticleGrid
-    ts = GB300RKTimeStepper(context[:Equation], pg, context[:Scheme], context[:MOOD], _tableau_id(context[:Tableau]);
-                            bc_map = get(context, :BCMap, Dict{Int, Int32}()),
+    ts = GB300RKTimeStepper(context[:Equation], pg, context[:Scheme], context[:MOOD], context[:Tableau];
+                            bc_map = get(context, :BCMap, nothing),
                             precision = get(context, :Precision, :fp64),
                             reset_orders_per_stage = get(time_conf, :reset_orders_per_stage, false)::Bool,
                             mood_substeps = get(time_conf, :mood_substeps, true)::Bool)
