@@ -1103,8 +1103,8 @@ hcc_status hcc_create(const hcc_config *cfg, int64_t capacity, hcc_ctx **out) {
                 return c->fail(HCC_ERR_UNSUPPORTED, "UpwindDivergence with anisotropic spacing");
     }
     c->qmax = c->DO == 0 ? c->max_order : c->DO;
-    if (c->weno && (c->M != 1 || f.pde != HCC_PDE_ADVECTION))
-        return c->fail(HCC_ERR_INVALID, "WENO is a scalar scheme: linear advection with n_vars = 1");
+    if (c->weno && c->max_order > 2 && c->M > 1)
+        return c->fail(HCC_ERR_UNSUPPORTED, "WENO for systems: orders 1 and 2 (degree-1 fits)");
     if (c->central && f.mood_criterion == HCC_MOOD_U2)
         return c->fail(HCC_ERR_INVALID, "MOODu2 needs cached reconstruction gradients (MUSCL)");
     c->tab = make_tableau(f.tableau);

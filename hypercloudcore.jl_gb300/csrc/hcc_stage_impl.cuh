@@ -1640,10 +1640,11 @@ __device__ __forceinline__ void chol_solve_fixed(const double *U, const double *
 
 // _mls_solve_masked of degree Q (Interpolators.jl:412-443) over the slots of particle i, all of them (dsel < 0) or
 // the one-sided stencil along axis dsel: side 1 x_d < 0, side 2 x_d >= 0 (WENO's upwind sides), side 3 x_d <= 0
-// (Tiwari's upwind side for v_d > 0); out[0..D) = the first-derivative coefficients (scaled by invL). Returns the
-// factorisation status (out = 0 when it fails).
-template <typename T, int D, int Q>
-__device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side, double fi, double *out) {
+// (Tiwari's upwind side for v_d > 0), of the per-particle field g (fi = its value at i); out[0..D) = the
+// first-derivative coefficients (scaled by invL). Returns the factorisation status (out = 0 when it fails).
+template <typename T, int D, int Q, typename Field>
+__device__ bool weno_fit_f(const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side, double fi, Field g,
+                           double *out) {
     constexpr int B = ExpTable<D, Q>::B;
     const int64_t np = a.g.npad;
     double N[B * B], bs[B];
@@ -1660,7 +1661,7 @@ __device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, in
         for (int d = 0; d < D; ++d) x[d] = double(a.g.dist[(int64_t(k) * D + d) * np + i]) * a.g.invL64;
         table_basis<D, Q, double>(x, p);
         const double w = double(a.g.wt[s]);
-        const double df = double(a.U[a.g.nidx[s]]) - fi;
+        const double df = g(int64_t(a.g.nidx[s])) - fi;
         for (int r = 0; r < B; ++r)
             for (int c = 0; c < B; ++c) N[r * B + c] = N[r * B + c] + w * (p[r] * p[c]);
         for (int r = 0; r < B; ++r) bs[r] = bs[r] + w * (p[r] * df);
@@ -1673,6 +1674,11 @@ __device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, in
 #pragma unroll
     for (int d = 0; d < D; ++d) out[d] = xs[d] * a.g.invL64;   // degree-1 scale factors
     return true;
+}
+
+template <typename T, int D, int Q>
+__device__ bool weno_fit(const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side, double fi, double *out) {
+    return weno_fit_f<T, D, Q>(a, i, cnt, dsel, side, fi, [&a](int64_t j) { return double(a.U[j]); }, out);
 }
 
 template <typename T, int D>
@@ -1765,6 +1771,200 @@ __global__ void __launch_bounds__(128) k_weno(const StageArgs<T> a) {
         const uint32_t word = a.wmask[tile];
         const int64_t i = int64_t(tile) * 32 + lane;
         const bool f = ((word >> lane) & 1u) ? weno_one<T, D>(a, i) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
+}
+
+template <typename T, int D, typename Field>
+__device__ __forceinline__ void weno_fit_qf(int q, const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side,
+                                            double fi, Field g, double *out) {
+    if (q == 1) weno_fit_f<T, D, 1>(a, i, cnt, dsel, side, fi, g, out);
+    else weno_fit_f<T, D, 2>(a, i, cnt, dsel, side, fi, g, out);
+}
+
+// Component-wise meshless WENO of a system (an extension of the scalar functor WENO.jl:55-165, which the reference
+// defines for M = 1 only), orders 1 and 2: the central and one-sided fits, smoothness indicators and weights of the
+// scalar scheme applied to one field at a time. Linear fluxes F_d(U)_m = c_dm U_m (advection, the kinetic model):
+// field U_m, upwind side by the sign of c_dm, divergence sum_d c_dm d_d U_m. Euler: local Lax-Friedrichs splitting
+// F_d^+- = (F_d(U) +- alpha_d U) / 2 with alpha_d the largest lambda_d over {i} u N(i); d_d F_d^+ from the
+// left-biased one-sided fit (x_d < 0), d_d F_d^- from the right-biased one (x_d >= 0). Fits in FP64 in both paths.
+template <typename T, int D, int M, int PDE>
+__device__ __forceinline__ bool weno_sys_one(const StageArgs<T> &a, const int64_t i) {
+    if (a.g.bnd[i]) {
+        if (a.full) {
+            T z[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) z[m] = T(0);
+            store_vec<T, M>(a.K + i * M, z);
+        }
+        return false;
+    }
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    T fiT[M], mn[M], mx[M];
+    load_vec<T, M>(a.U + i * M, fiT);
+#pragma unroll
+    for (int m = 0; m < M; ++m) mn[m] = mx[m] = fiT[m];
+    if (a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2))
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t j = a.g.nidx[int64_t(k) * np + i];
+#pragma unroll
+            for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], a.U[j * M + m]); mx[m] = vmax(mx[m], a.U[j * M + m]); }
+        }
+    double div[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) div[m] = 0.0;
+    int p_order = a.orders[i];
+    while (p_order > 1 && cnt < basis_count(D, p_order)) --p_order;
+    if (cnt >= basis_count(D, p_order)) {
+        const int DO = a.sc.DO;
+        const double dx2 = a.g.h64 * a.g.h64;
+        const int qC = DO == 0 ? p_order : (DO < p_order ? DO : p_order);
+        // fit degree of the one-sided stencil of axis d (side 1: x_d < 0, side 2: x_d >= 0), 0 when too small
+        auto one_sided = [&](int d, int side) {
+            int stencil = 0;
+            for (int k = 0; k < cnt; ++k) {
+                const double dd = double(a.g.dist[(int64_t(k) * D + d) * np + i]);
+                stencil += side == 1 ? (dd < 0.0) : (dd >= 0.0);
+            }
+            int p_d = p_order;
+            while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
+            if (stencil < basis_count(D, p_d)) return 0;
+            return DO == 0 ? p_d : (DO < p_d ? DO : p_d);
+        };
+        auto smooth = [&](const double *r) {
+            double sm = (r[0] * r[0]) * dx2;
+#pragma unroll
+            for (int d = 1; d < D; ++d) sm = sm + (r[d] * r[d]) * dx2;
+            return sm;
+        };
+        if constexpr (PDE != HCC_PDE_EULER) {
+            for (int m = 0; m < M; ++m) {
+                auto g = [&a, m](int64_t j) { return double(a.U[j * M + m]); };
+                const double fi = double(fiT[m]);
+                double resC[D];
+                weno_fit_qf<T, D>(qC, a, i, cnt, -1, 0, fi, g, resC);
+                const double smoothC = smooth(resC);
+                double s2 = jmax(fi * fi, smoothC);
+                s2 = s2 > 0.0 ? s2 : 1.0;
+                const double aC = smoothC / s2 + 1e-12;
+                double div_total = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double vel = double(a.ph.c[d][m]);
+                    const int side = vel > 0.0 ? 1 : 2;
+                    const int qS = one_sided(d, side);
+                    if (qS == 0) {
+                        div_total = div_total + resC[d] * vel;
+                        continue;
+                    }
+                    double resS[D];
+                    weno_fit_qf<T, D>(qS, a, i, cnt, d, side, fi, g, resS);
+                    const double smoothS = smooth(resS);
+                    const double q = (smoothS / s2 + 1e-12) / aC;
+                    const double wS = 1.0 / (1.0 + q * q);
+                    const double wC = 1.0 - wS;
+                    const double div_d = wS * resS[d] + wC * resC[d];
+                    div_total = div_total + div_d * vel;
+                }
+                div[m] = div_total;
+            }
+        } else {
+            const double gamma = double(a.ph.gamma), gm1 = double(a.ph.gm1);
+            // Euler primitives and lambda_d of a state in FP64 (euler_prim and speeds, operation for operation)
+            auto prim = [gm1](const double *Uj, double &inv_rho, double *u, double &p) {
+                const double rho = Uj[0];
+                inv_rho = 1.0 / rho;
+                double q2 = 0.0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    u[d] = Uj[1 + d] * inv_rho;
+                    q2 = (d == 0) ? u[d] * u[d] : q2 + u[d] * u[d];
+                }
+                p = gm1 * (Uj[D + 1] - 0.5 * (rho * q2));
+            };
+            auto lam = [&](const double *Uj, int d) {
+                double inv_rho, u[D], p;
+                prim(Uj, inv_rho, u, p);
+                return fabs(u[d]) + sqrt(gamma * p * inv_rho);
+            };
+            double Ui[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) Ui[m] = double(fiT[m]);
+            double alpha[D];
+            for (int d = 0; d < D; ++d) {
+                alpha[d] = lam(Ui, d);
+                for (int k = 0; k < cnt; ++k) {
+                    const int64_t j = a.g.nidx[int64_t(k) * np + i];
+                    double Uj[M];
+#pragma unroll
+                    for (int m = 0; m < M; ++m) Uj[m] = double(a.U[j * M + m]);
+                    alpha[d] = jmax(alpha[d], lam(Uj, d));
+                }
+            }
+            for (int d = 0; d < D; ++d)
+                for (int sg = 0; sg < 2; ++sg) {
+                    const int side = sg == 0 ? 1 : 2;
+                    const int qS = one_sided(d, side);
+                    for (int m = 0; m < M; ++m) {
+                        // F_d^+-(U_j)_m, the physical flux component as flux_and_speed forms it
+                        auto g = [&a, &prim, &alpha, d, m, sg](int64_t j) {
+                            double Uj[M];
+#pragma unroll
+                            for (int c = 0; c < M; ++c) Uj[c] = double(a.U[j * M + c]);
+                            double inv_rho, u[D], p;
+                            prim(Uj, inv_rho, u, p);
+                            double F;
+                            if (m == 0) F = Uj[1 + d];
+                            else if (m <= D) F = (m - 1 == d) ? Uj[m] * u[d] + p : Uj[m] * u[d];
+                            else F = (Uj[D + 1] + p) * u[d];
+                            const double aU = alpha[d] * Uj[m];
+                            return sg == 0 ? 0.5 * (F + aU) : 0.5 * (F - aU);
+                        };
+                        const double fi = g(i);
+                        double resC[D];
+                        weno_fit_qf<T, D>(qC, a, i, cnt, -1, 0, fi, g, resC);
+                        double deriv = resC[d];
+                        if (qS > 0) {
+                            const double smoothC = smooth(resC);
+                            double s2 = jmax(fi * fi, smoothC);
+                            s2 = s2 > 0.0 ? s2 : 1.0;
+                            const double aC = smoothC / s2 + 1e-12;
+                            double resS[D];
+                            weno_fit_qf<T, D>(qS, a, i, cnt, d, side, fi, g, resS);
+                            const double smoothS = smooth(resS);
+                            const double q = (smoothS / s2 + 1e-12) / aC;
+                            const double wS = 1.0 / (1.0 + q * q);
+                            const double wC = 1.0 - wS;
+                            deriv = wS * resS[d] + wC * resC[d];
+                        }
+                        div[m] = div[m] + deriv;
+                    }
+                }
+        }
+    }
+    T Kv[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Kv[m] = T(-div[m]);
+    return stage_epilogue<T, D, M, PDE>(a, i, fiT, Kv, mn, mx);
+}
+
+template <typename T, int D, int M, int PDE>
+__global__ void __launch_bounds__(128) k_weno_sys(const StageArgs<T> a) {
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? weno_sys_one<T, D, M, PDE>(a, i) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? weno_sys_one<T, D, M, PDE>(a, i) : false;
         if (a.check) tile_failures(a, tile, f);
         if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
     }
@@ -2096,9 +2296,11 @@ struct StageInst {
         k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args), dt_bits);
     }
     static void weno(const void *args, int64_t n, cudaStream_t s) {
+        const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
         if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
-            const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
             k_weno<T, D><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
+        } else if constexpr (RDEG == 1) {       // systems (one instantiation: WENO has no reconstruction degree)
+            k_weno_sys<T, D, M, PDE><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         }
     }
     static void upwind(const void *args, int64_t n, cudaStream_t s) {
@@ -2116,7 +2318,7 @@ struct StageInst {
     }
     static const StageOps *ops() {
         static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,
-                                   (M == 1 && PDE == HCC_PDE_ADVECTION) ? &weno : nullptr,
+                                   ((M == 1 && PDE == HCC_PDE_ADVECTION) || RDEG == 1) ? &weno : nullptr,
                                    RDEG == 1 ? &central : nullptr,
                                    (RDEG == 1 && M == 1 && PDE == HCC_PDE_ADVECTION) ? &upwind : nullptr};
         return &o;

@@ -601,7 +601,6 @@ struct Solver {
             if (upwind == HCC_UPWIND_PRAVEEN && D != 2) { err = "Praveen is two-dimensional"; return false; }
         }
         if (max_order < 1 || max_order > 3) { err = "muscl_order must be 1..3"; return false; }
-        if (weno && (M != 1 || c.pde == HCC_PDE_EULER)) { err = "WENO is a scalar scheme (n_vars = 1)"; return false; }
         DO = c.div_order > max_order ? max_order : c.div_order;
         qmax = DO == 0 ? max_order : DO;
         rdeg = std::max(1, max_order - 1);
@@ -1427,20 +1426,21 @@ struct Solver {
         return 2.0 * div;
     }
 
-    // _mls_solve_masked (Interpolators.jl:412-443) of degree q over the slots with mask[k]; out[0..B) scaled.
-    bool masked_fit(int64_t i, const double *U, int q, const std::vector<uint8_t> &mask, double *out) const {
+    // _mls_solve_masked (Interpolators.jl:412-443) of degree q over the slots with mask[k] of a per-particle field
+    // g(j) (fi = g(i)); out[0..B) scaled.
+    template <typename G>
+    bool masked_fit_field(int64_t i, G g, double fi, int q, const std::vector<uint8_t> &mask, double *out) const {
         const BasisTable &bt = basis_table(D, q);
         const int B = bt.B;
         double Nm[400], bs[32], p[32], sd[3];
         for (int k = 0; k < B * B; ++k) Nm[k] = 0.0;
         for (int b = 0; b < B; ++b) bs[b] = 0.0;
-        const double fi = U[i];
         for (int64_t s = start[i]; s < start[i + 1]; ++s) {
             if (!mask[s - start[i]]) continue;
             for (int d = 0; d < D; ++d) sd[d] = ndist[s * D + d] * invL;
             build_basis(bt, sd, p);
             double w = nw[s];
-            double df = U[nidx[s]] - fi;
+            double df = g(int64_t(nidx[s])) - fi;
             for (int r = 0; r < B; ++r)
                 for (int c = 0; c < B; ++c) Nm[r * B + c] = Nm[r * B + c] + w * (p[r] * p[c]);
             for (int b = 0; b < B; ++b) bs[b] = bs[b] + w * (p[b] * df);
@@ -1452,6 +1452,122 @@ struct Solver {
         build_scales(bt, invL, sc);
         for (int b = 0; b < B; ++b) out[b] = x[b] * sc[b];
         return true;
+    }
+    bool masked_fit(int64_t i, const double *U, int q, const std::vector<uint8_t> &mask, double *out) const {
+        return masked_fit_field(i, [U](int64_t j) { return U[j]; }, U[i], q, mask, out);
+    }
+
+    // Component-wise meshless WENO of a system (an extension of the scalar functor WENO.jl:55-165, which the reference
+    // defines for M = 1 only): the central and one-sided fits, smoothness indicators and weights of the scalar scheme
+    // applied to one field at a time.
+    //  * linear fluxes F_d(U)_m = c_dm U_m (advection, the kinetic model): field U_m, upwind side by the sign of c_dm,
+    //    the divergence sum_d c_dm d_d U_m -- for M = 1 the scalar scheme, operation for operation;
+    //  * Euler: local Lax-Friedrichs splitting F_d = F_d^+ + F_d^-, F_d^+- = (F_d(U) +- alpha_d U) / 2 with alpha_d the
+    //    largest lambda_d over {i} u N(i); d_d F_d^+ from the left-biased one-sided fit (x_d < 0), d_d F_d^- from the
+    //    right-biased one (x_d >= 0), each blended with the central fit of the same field.
+    void weno_system(int64_t i, const double *U, double *div) const {
+        for (int m = 0; m < M; ++m) div[m] = 0.0;
+        const int num = nnb(i);
+        int p_order = orders[i];
+        while (p_order > 1) {
+            if (num >= basis_count(D, p_order)) break;
+            p_order -= 1;
+        }
+        if (num < basis_count(D, p_order)) return;
+        double hmin = cfg.dx[0];
+        for (int d = 1; d < D; ++d) hmin = std::min(hmin, cfg.dx[d]);
+        const double dx2 = hmin * hmin;
+        const int qC = DO == 0 ? p_order : std::min(DO, p_order);
+        std::vector<uint8_t> all(num, 1), side(num, 0);
+        // one-sided stencil of axis d: x_d < 0 (left) or x_d >= 0; returns the fit degree, or 0 when too small
+        auto one_sided = [&](int d, bool left) {
+            int stencil = 0;
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) {
+                const double dk = ndist[s * D + d];
+                const bool in = left ? dk < 0.0 : dk >= 0.0;
+                side[s - start[i]] = in;
+                stencil += in;
+            }
+            int p_d = p_order;
+            while (p_d > 1) {
+                if (stencil >= basis_count(D, p_d)) break;
+                p_d -= 1;
+            }
+            if (stencil < basis_count(D, p_d)) return 0;
+            return DO == 0 ? p_d : std::min(DO, p_d);
+        };
+        auto smooth = [&](const double *res) {
+            double sm = (res[0] * res[0]) * dx2;
+            for (int k = 1; k < D; ++k) sm = sm + (res[k] * res[k]) * dx2;
+            return sm;
+        };
+        if (cfg.pde != HCC_PDE_EULER) {
+            for (int m = 0; m < M; ++m) {
+                auto g = [U, m, this](int64_t j) { return U[j * M + m]; };
+                const double fi = U[i * M + m];
+                double resC[32];
+                masked_fit_field(i, g, fi, qC, all, resC);
+                const double smoothC = smooth(resC);
+                double s2 = jmax(fi * fi, smoothC);
+                s2 = s2 > 0.0 ? s2 : 1.0;
+                const double aC = smoothC / s2 + 1e-12;
+                double div_total = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double vel = phys.c[d][m];
+                    const int qS = one_sided(d, vel > 0.0);
+                    if (qS == 0) {
+                        div_total = div_total + resC[d] * vel;
+                        continue;
+                    }
+                    double resS[32];
+                    masked_fit_field(i, g, fi, qS, side, resS);
+                    const double smoothS = smooth(resS);
+                    const double q = (smoothS / s2 + 1e-12) / aC;
+                    const double wS = 1.0 / (1.0 + q * q);
+                    const double wC = 1.0 - wS;
+                    const double div_d = wS * resS[d] + wC * resC[d];
+                    div_total = div_total + div_d * vel;
+                }
+                div[m] = div_total;
+            }
+            return;
+        }
+        double alpha[3];
+        for (int d = 0; d < D; ++d) {
+            alpha[d] = phys.lam(&U[i * M], d);
+            for (int64_t s = start[i]; s < start[i + 1]; ++s) alpha[d] = jmax(alpha[d], phys.lam(&U[int64_t(nidx[s]) * M], d));
+        }
+        for (int d = 0; d < D; ++d)
+            for (int sg = 0; sg < 2; ++sg) {
+                const bool plus = sg == 0;
+                const int qS = one_sided(d, plus);
+                for (int m = 0; m < M; ++m) {
+                    auto g = [&, d, m, plus](int64_t j) {
+                        double F[3 * HCC_MAX_VARS];
+                        phys.flux(&U[j * M], F);
+                        const double aU = alpha[d] * U[j * M + m];
+                        return plus ? 0.5 * (F[d * M + m] + aU) : 0.5 * (F[d * M + m] - aU);
+                    };
+                    const double fi = g(i);
+                    double resC[32];
+                    masked_fit_field(i, g, fi, qC, all, resC);
+                    double deriv = resC[d];
+                    if (qS > 0) {
+                        const double smoothC = smooth(resC);
+                        double s2 = jmax(fi * fi, smoothC);
+                        s2 = s2 > 0.0 ? s2 : 1.0;
+                        const double aC = smoothC / s2 + 1e-12;
+                        double resS[32];
+                        masked_fit_field(i, g, fi, qS, side, resS);
+                        const double smoothS = smooth(resS);
+                        const double q = (smoothS / s2 + 1e-12) / aC;
+                        const double wS = 1.0 / (1.0 + q * q);
+                        const double wC = 1.0 - wS;
+                        deriv = wS * resS[d] + wC * resC[d];
+                    }
+                    div[m] = div[m] + deriv;
+                }
+            }
     }
 
     double weno_particle(int64_t i, const double *U) const {
@@ -1610,9 +1726,15 @@ struct Solver {
         if (weno) {
 #pragma omp parallel for schedule(dynamic, 256)
             for (int64_t p = 0; p < N; ++p) {
-                if (bnd[p]) { if (full) K[p] = 0.0; continue; }
+                if (bnd[p]) { if (full) for (int m = 0; m < M; ++m) K[p * M + m] = 0.0; continue; }
                 if (!(full || dirty[p])) continue;
-                K[p] = -weno_particle(p, Ystate);
+                if (M == 1 && cfg.pde != HCC_PDE_EULER) {
+                    K[p] = -weno_particle(p, Ystate);
+                } else {
+                    double div[HCC_MAX_VARS];
+                    weno_system(p, Ystate, div);
+                    for (int m = 0; m < M; ++m) K[p * M + m] = -div[m];
+                }
             }
             return;
         }

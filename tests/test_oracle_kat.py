@@ -1030,3 +1030,55 @@ def test_shepard_volumes_partition_the_box(hcc, oracle, abi):
         assert np.all(V >= 0.0)
         assert V.sum() == pytest.approx(1.0, rel=1e-13)
         assert np.abs(V[inner] / h ** 2 - 1.0).max() < 0.5
+
+
+# ----------------------------------------------------------------------------------------------- WENO for systems
+def _weno_oracle(hcc, oracle, abi, cloud, pde, order=2, **kw):
+    o = oracle.OracleContext(hcc.make_config(pde, cloud, scheme=hcc.WENO(order), **kw), abi)
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    o.prepare_geometry()
+    return o
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_weno_system_reduces_to_the_scalar_scheme(hcc, oracle, abi, order):
+    """Component-wise WENO of a two-component advection system: each component's right-hand side equals the scalar
+    WENO scheme's (WENO.jl:55-165) for that component and its velocity, bit for bit."""
+    h = 0.05
+    cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.2 * h, seed=3)
+    x, y = cl.pos[:, 0], cl.pos[:, 1]
+    u0 = np.where((x - 0.5) ** 2 + (y - 0.5) ** 2 < 0.05, 1.0, 0.1) + 0.05 * np.sin(2 * np.pi * x)
+    u1 = np.exp(-((x - 0.3) ** 2 + (y - 0.6) ** 2) / 0.02)
+    vel = ((1.0, -0.4), (0.5, 0.7))                    # c[d][m]
+    sys_ = _weno_oracle(hcc, oracle, abi, cl, hcc.LinearAdvection(vel), order)
+    sys_.upload_state(np.stack([u0, u1], axis=1))
+    K = sys_.compute_rhs()
+    for m, u in enumerate((u0, u1)):
+        sc = _weno_oracle(hcc, oracle, abi, cl, hcc.LinearAdvection(((vel[0][m],), (vel[1][m],))), order)
+        sc.upload_state(u[:, None].copy())
+        assert np.array_equal(K[:, m].view(np.uint64), sc.compute_rhs()[:, 0].view(np.uint64)), m
+
+
+def test_weno_euler_converges_on_a_smooth_wave(hcc, oracle, abi):
+    """Euler WENO (local Lax-Friedrichs splitting, component-wise fits): a density wave carried by a uniform flow at
+    uniform pressure converges to the exact solution at second order (errors ratio >= 2.8 for halved spacing; measured
+    1.06e-2 -> 2.26e-3 mean absolute density error at h = 1/16 -> 1/32)."""
+    errs = []
+    for h in (1.0 / 16, 1.0 / 32):
+        cl = hcc.rectangular_cloud((0.0, 0.0), (1.0, 1.0), h, 2.5 * h, periodic=True, jitter=0.1 * h, seed=5)
+        x, y = cl.pos[:, 0], cl.pos[:, 1]
+        u, v, p = 1.0, 0.5, 1.0
+        rho = 1.0 + 0.2 * np.sin(2 * np.pi * (x + y))
+        U0 = np.stack([rho, rho * u, rho * v, p / 0.4 + 0.5 * rho * (u * u + v * v)], axis=1)
+        o = _weno_oracle(hcc, oracle, abi, cl, hcc.Euler(2), 2, mood=hcc.MOOD(hcc.EPD1, hcc.MOODPAD()))
+        o.upload_state(U0)
+        t_end = 0.1
+        n = int(np.ceil(t_end / (0.3 * o.time_step())))
+        dt = t_end / n
+        for k in range(n):
+            o.step(k * dt, dt)
+        exact = 1.0 + 0.2 * np.sin(2 * np.pi * ((x - u * t_end) + (y - v * t_end)))
+        errs.append(np.abs(o.download_state()[:, 0] - exact).mean())
+        o.close()
+    assert errs[1] < errs[0] / 2.8, errs
