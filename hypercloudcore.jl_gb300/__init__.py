@@ -418,6 +418,23 @@ class Context:
         self._check(self.lib.hcc_batch_total_mass(self._h, _ptr(out, C.c_double)), "hcc_batch_total_mass")
         return out
 
+    def batch_time_steps(self) -> np.ndarray:
+        """The CFL step of every cloud of the last batch (hcc_batch_time_steps)."""
+        n = getattr(self, "_batch_n", None)
+        if n is None:
+            raise HCCError(_abi.HCC_ERR_STATE, "no batch uploaded", "hcc_batch_time_steps")
+        out = np.zeros(n, dtype=np.float64)
+        self._check(self.lib.hcc_batch_time_steps(self._h, _ptr(out, C.c_double)), "hcc_batch_time_steps")
+        return out
+
+    def step_batch(self, t: float, dts):
+        """One step of every cloud of the last batch with its own dt (hcc_batch_step)."""
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        n = getattr(self, "_batch_n", None)
+        if n is None or d.shape != (n,):
+            raise HCCError(_abi.HCC_ERR_INVALID, "one dt per cloud of the batch", "hcc_batch_step")
+        self._check(self.lib.hcc_batch_step(self._h, float(t), _ptr(d, C.c_double)), "hcc_batch_step")
+
     def build_neighbours(self):
         self._check(self.lib.hcc_build_neighbours(self._h), "hcc_build_neighbours")
 

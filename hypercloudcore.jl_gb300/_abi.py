@@ -151,6 +151,8 @@ PROTOTYPES = [
     ("hcc_cfl_time_step_noalloc", C.c_int, [C.POINTER(HccConfig), C.c_int64, C.c_int64, P, P, P, P, P, P, _dp]),
     ("hcc_upload_batch", C.c_int, [P, C.c_int32, C.POINTER(C.c_int64), _dp, _u8p, _i32p, _dp, _dp, _dp]),
     ("hcc_batch_total_mass", C.c_int, [P, _dp]),
+    ("hcc_batch_time_steps", C.c_int, [P, _dp]),
+    ("hcc_batch_step", C.c_int, [P, C.c_double, _dp]),
     ("hcc_batch_layout", C.c_int, [C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_int64), _dp, _dp, _dp]),
     ("hcc_update_volumes", C.c_int, [P, C.c_int32]),
     ("hcc_download_volumes", C.c_int, [P, _dp]),

@@ -179,6 +179,12 @@ struct hcc_ctx {
     double *dwc64[3] = {}; float *dwc32[3] = {}; uint8_t *okc[3] = {};
     double *mw64 = nullptr; float *mw32 = nullptr;   // moment-correction weights (first-order MUSCL)
     std::vector<int64_t> batch_offsets;              // clouds of the last hcc_upload_batch (empty: one cloud)
+    int32_t *cloud_id = nullptr;                     // device: particle -> cloud of the batch
+    unsigned long long *cloud_dt = nullptr;          // device: per-cloud CFL minima (ordered bits)
+    bool per_cloud = false;                          // the step being enqueued uses one dt per cloud (step_dts)
+    std::vector<double> step_dts;
+    int coef_sets = 1;                               // coefficient sets the stage-coefficient buffers hold
+    int graph_per_cloud = -1;                        // the per_cloud mode the step graphs were captured with
     bool moment() const { return cfg.moment_correction && max_order == 1 && !weno && !central && !upwind; }
     bool no_recon() const { return weno || central || upwind; }
 
@@ -345,6 +351,8 @@ struct hcc_ctx {
         dfree(ttiles); dfree(ctiles); dfree(dtiles); dfree(tmask); dfree(cmask); dfree(dmask); dfree(words1);
         dfree(ftiles); dfree(fmask); dfree(forced); dfree(feat); dfree(pred); dfree(pred_rows); dfree(pred_idx);
         dfree(rough);
+        dfree(cloud_id); dfree(cloud_dt);
+        per_cloud = false;
         feat_valid = false;
     }
     void free_slots() {
@@ -483,8 +491,7 @@ template <typename T> void apply_bcs(hcc_ctx *c, void *Y) {
 
 // Coefficients of every candidate of the step (entry 0: stage 1; entry s+1: the candidate the flux pass of stage s
 // forms), from dt and the tableau, into the pinned mirror and then to the device on the context stream.
-template <typename T> hcc_status upload_coeffs(hcc_ctx *c, double dt) {
-    StageCoeffs<T> *h = static_cast<StageCoeffs<T> *>(c->coef_host);
+template <typename T> void fill_coeffs(const hcc_ctx *c, double dt, StageCoeffs<T> *h) {
     const int S = c->tab.s;
     std::memset(h, 0, sizeof(StageCoeffs<T>) * (S + 1));
     h[0].dt_ii = T(dt * c->tab.a[0][0]);
@@ -505,8 +512,18 @@ template <typename T> hcc_status upload_coeffs(hcc_ctx *c, double dt) {
         }
         e.h_sub = T(c->ratio * dt);
     }
-    return c->cuda(cudaMemcpyAsync(c->coef_dev, h, sizeof(StageCoeffs<T>) * (S + 1), cudaMemcpyHostToDevice, c->stream),
-                   "coefficient upload");
+}
+
+// Coefficients of every candidate of the step (entry 0: stage 1; entry s+1: the candidate the flux pass of stage s
+// forms), from dt and the tableau (one set, or one set per cloud of a batch stepped with per-cloud dts), into the
+// pinned mirror and then to the device on the context stream.
+template <typename T> hcc_status upload_coeffs(hcc_ctx *c, double dt) {
+    StageCoeffs<T> *h = static_cast<StageCoeffs<T> *>(c->coef_host);
+    const int S = c->tab.s;
+    const int sets = c->per_cloud ? int(c->step_dts.size()) : 1;
+    for (int b = 0; b < sets; ++b) fill_coeffs<T>(c, c->per_cloud ? c->step_dts[b] : dt, h + size_t(b) * (S + 1));
+    return c->cuda(cudaMemcpyAsync(c->coef_dev, h, sizeof(StageCoeffs<T>) * (S + 1) * sets, cudaMemcpyHostToDevice,
+                                   c->stream), "coefficient upload");
 }
 
 // Kernel arguments of stage s (s = -1: the stage-1 candidate) for the current buffer assignment.
@@ -519,6 +536,10 @@ template <typename T> StageArgs<T> stage_args(hcc_ctx *c, int s) {
         a.KI[q] = static_cast<const T *>(c->KI[q]);
     }
     const StageCoeffs<T> *coef = static_cast<const StageCoeffs<T> *>(c->coef_dev);
+    if (c->per_cloud) {
+        a.cloud_id = c->cloud_id;
+        a.coef_stride = S + 1;
+    }
     // with a predictor, the final stage's full flux pass marks the tiles the next step's feature pass must visit
     if (c->mlp && s == S - 1 && !c->no_recon()) a.rough_words = c->rough;
     if (c->moving()) {
@@ -951,6 +972,10 @@ template <typename T> hcc_status run_step_graph(hcc_ctx *c, double dt) {
 
 template <typename T> hcc_status run_step(hcc_ctx *c, double dt) {
     c->feat_valid = false;
+    if (c->graph_per_cloud != int(c->per_cloud)) {   // graphs hold the coefficient addressing of their mode
+        c->drop_graphs();
+        c->graph_per_cloud = int(c->per_cloud);
+    }
     hcc_status lst = ensure_learn_buffers(c);
     if (lst != HCC_OK) return lst;
     if (c->use_graphs && !c->prof && !c->moving()) {
@@ -1781,7 +1806,69 @@ hcc_status hcc_step(hcc_ctx *c, double t, double dt) {
     if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
     if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
     if (c->n == 0) return HCC_OK;
+    c->per_cloud = false;
     return c->f32 ? run_step<float>(c, dt) : run_step<double>(c, dt);
+}
+
+hcc_status hcc_batch_step(hcc_ctx *c, double t, const double *dts) {
+    (void)t;
+    if (!c) return HCC_ERR_INVALID;
+    if (c->batch_offsets.size() < 2 || !c->cloud_id) return c->fail(HCC_ERR_STATE, "no batch uploaded");
+    if (!dts) return c->fail(HCC_ERR_INVALID, "null time steps");
+    const int nb = int(c->batch_offsets.size()) - 1;
+    for (int b = 0; b < nb; ++b)
+        if (!std::isfinite(dts[b]) || !(dts[b] >= 0.0)) return c->fail(HCC_ERR_NONFINITE, "dt must be finite and >= 0");
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    if (c->n == 0) return HCC_OK;
+    if (nb > c->coef_sets) {                      // room for one coefficient set per cloud
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        c->drop_graphs();
+        const size_t bytes = sizeof(StageCoeffs<double>) * (HCC_MAX_STAGES + 1) * size_t(nb);
+        if (c->coef_host) cudaFreeHost(c->coef_host);
+        c->coef_host = nullptr;
+        hcc_status st = c->valloc(c->coef_dev, bytes, "stage coefficients");
+        if (st == HCC_OK) st = c->cuda(cudaMallocHost(&c->coef_host, bytes), "pinned stage coefficients");
+        if (st != HCC_OK) return st;
+        c->coef_sets = nb;
+    }
+    c->per_cloud = true;
+    c->step_dts.assign(dts, dts + nb);
+    const hcc_status st = c->f32 ? run_step<float>(c, 0.0) : run_step<double>(c, 0.0);
+    c->per_cloud = false;
+    return st;
+}
+
+hcc_status hcc_batch_time_steps(hcc_ctx *c, double *dt_out) {
+    if (!c || !dt_out) return c ? c->fail(HCC_ERR_INVALID, "null output") : HCC_ERR_INVALID;
+    if (c->batch_offsets.size() < 2 || !c->cloud_id) return c->fail(HCC_ERR_STATE, "no batch uploaded");
+    if (!c->have_geom) { hcc_status st = hcc_prepare_geometry(c); if (st != HCC_OK) return st; }
+    if (!c->have_state) return c->fail(HCC_ERR_STATE, "no state");
+    const int nb = int(c->batch_offsets.size()) - 1;
+    hcc_status st;
+    if (!c->cloud_dt) HCC_TRY(c->alloc(c->cloud_dt, size_t(nb), "per-cloud steps"));
+    std::vector<unsigned long long> bits(nb, 0x7ff0000000000000ull);
+    HCC_TRY(c->cuda(cudaMemcpyAsync(c->cloud_dt, bits.data(), size_t(nb) * sizeof(unsigned long long),
+                                    cudaMemcpyHostToDevice, c->stream), "dt init"));
+    if (c->f32) {
+        StageArgs<float> a = base_args<float>(c);
+        a.U = static_cast<const float *>(c->rhos);
+        a.cloud_id = c->cloud_id;
+        c->ops->cfl(&a, c->n, c->cloud_dt, c->stream);
+    } else {
+        StageArgs<double> a = base_args<double>(c);
+        a.U = static_cast<const double *>(c->rhos);
+        a.cloud_id = c->cloud_id;
+        c->ops->cfl(&a, c->n, c->cloud_dt, c->stream);
+    }
+    c->launches = 1;
+    c->launches_total += 1;
+    HCC_TRY(launch_check(c, "cfl kernel"));
+    HCC_TRY(c->cuda(cudaMemcpyAsync(bits.data(), c->cloud_dt, size_t(nb) * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, c->stream), "dt copy"));
+    HCC_TRY(c->sync("cfl"));
+    for (int b = 0; b < nb; ++b) std::memcpy(&dt_out[b], &bits[b], sizeof(double));
+    return HCC_OK;
 }
 
 #define HCC_STR2(x) #x
@@ -2108,6 +2195,13 @@ hcc_status hcc_upload_batch(hcc_ctx *c, int32_t n_clouds, const int64_t *offsets
     hcc_status st = hcc_upload_cloud(c, n, up.data(), is_boundary, tags, volumes);
     if (st != HCC_OK) return st;
     c->batch_offsets.assign(offsets, offsets + n_clouds + 1);
+    std::vector<int32_t> ids(size_t(std::max<int64_t>(n, 1)), 0);
+    for (int b = 0; b < n_clouds; ++b)
+        for (int64_t i = offsets[b]; i < offsets[b + 1]; ++i) ids[i] = b;
+    HCC_TRY(c->alloc(c->cloud_id, size_t(std::max<int64_t>(n, 1)), "cloud ids"));
+    HCC_TRY(c->cuda(cudaMemcpy(c->cloud_id, ids.data(), size_t(std::max<int64_t>(n, 1)) * sizeof(int32_t),
+                               cudaMemcpyHostToDevice), "cloud ids"));
+    dfree(c->cloud_dt);
     return HCC_OK;
 }
 

@@ -272,7 +272,9 @@ template <typename T> struct StageArgs {
     const T *Un;                      // start-of-step state (pg.rhos)
     const T *KE[HCC_MAX_STAGES];
     const T *KI[HCC_MAX_STAGES];
-    const StageCoeffs<T> *coef;       // device: the dt-dependent coefficients of this candidate
+    const StageCoeffs<T> *coef;       // device: the dt-dependent coefficients of this candidate (of cloud 0)
+    const int32_t *cloud_id;          // batches stepped with one dt per cloud: particle -> cloud (else nullptr) ...
+    int coef_stride;                  // ... and the coefficient entries per cloud
     int n_prev;                       // stages entering the candidate (K_E[s] is this kernel's own)
     int self_slot;                    // index of K_E[s] among KE (its value comes from registers)
     T *Ynext;
@@ -304,6 +306,12 @@ template <typename T> struct StageArgs {
     unsigned *tcount;                 // ... and their count
     uint8_t *inadm;
 };
+
+// The coefficients of particle i's candidate: its cloud's set when the batch is stepped with one dt per cloud.
+template <typename T>
+__device__ __forceinline__ const StageCoeffs<T> *coef_of(const StageArgs<T> &a, int64_t i) {
+    return a.cloud_id ? a.coef + int64_t(a.cloud_id[i]) * a.coef_stride : a.coef;
+}
 
 // Device-side tile worklists of the MOOD fixed point: t = tiles with failed candidates, c = tiles with a dropped
 // order (cn: the list being filled by the current decrement, published as c by the decision), d = the reach of the

@@ -285,14 +285,15 @@ __device__ __forceinline__ void maxwellian(const PhysParams<T> &ph, const T *U, 
 // Implicit part of a stage (TimeSteppers.jl:427-444): mode 1 solves U_out - dt a_ii S(U_out) = U_in and sets
 // K_I = (U_out - U_in) / (dt a_ii); mode 2 evaluates K_I = S(Y) explicitly.
 template <typename T, int D, int M, int PDE>
-__device__ __forceinline__ void implicit_part(const StageArgs<T> &a, T *Y, T *KIout) {
+__device__ __forceinline__ void implicit_part(const StageArgs<T> &a, int64_t i, T *Y, T *KIout) {
     if constexpr (PDE == HCC_PDE_BGK) {
         T Mk[M];
         maxwellian<T, D, M>(a.ph, Y, Mk);
         if (a.implicit_mode == 1) {
-            T dto = a.coef->dt_ii * a.ph.inv_eps;
+            const StageCoeffs<T> *cf = coef_of(a, i);
+            T dto = cf->dt_ii * a.ph.inv_eps;
             T denom = T(1) / (T(1) + dto);
-            const T inv_dt_ii = a.coef->inv_dt_ii;
+            const T inv_dt_ii = cf->inv_dt_ii;
 #pragma unroll
             for (int k = 0; k < M; ++k) {
                 T out = (Y[k] + dto * Mk[k]) * denom;
@@ -746,7 +747,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i,
     // _stage_predictor! for the next candidate
     T Y[M];
     load_vec<T, M>(a.Un + i * M, Y);
-    const StageCoeffs<T> *cf = a.coef;
+    const StageCoeffs<T> *cf = coef_of(a, i);
     for (int j = 0; j < a.n_prev; ++j) {
         const T hE = cf->hE[j], hI = cf->hI[j];
         if (hE != T(0)) {
@@ -771,7 +772,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs<T> &a, int64_t i,
     }
     if (a.implicit_mode) {
         T KIo[M];
-        implicit_part<T, D, M, PDE>(a, Y, KIo);
+        implicit_part<T, D, M, PDE>(a, i, Y, KIo);
         store_vec<T, M>(a.KInext + i * M, KIo);
     }
     store_vec<T, M>(a.Ynext + i * M, Y);
@@ -2165,7 +2166,7 @@ __global__ void k_stage1(const StageArgs<T> a) {
     for (int m = 0; m < M; ++m) Y[m] = a.Un[i * M + m];
     if (!a.g.bnd[i] && a.implicit_mode) {
         T KIo[M];
-        implicit_part<T, D, M, PDE>(a, Y, KIo);
+        implicit_part<T, D, M, PDE>(a, i, Y, KIo);
 #pragma unroll
         for (int m = 0; m < M; ++m) a.KInext[i * M + m] = KIo[m];
     }
@@ -2202,12 +2203,22 @@ __global__ void k_cfl(const StageArgs<T> a, unsigned long long *dt_bits) {
     }
     // positive doubles order like their bit patterns
     unsigned long long b = __double_as_longlong(dti);
+    int cl = 0;
+    bool whole_warp = true;
+    if (a.cloud_id) {   // one minimum per cloud of a batch (a warp straddling two clouds: one atomic per lane)
+        cl = i < a.g.n ? a.cloud_id[i] : -1;
+        whole_warp = __match_any_sync(0xffffffffu, cl) == 0xffffffffu;
+        if (!whole_warp) {
+            if (cl >= 0) atomicMin(dt_bits + cl, b);
+            return;
+        }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long ob = __shfl_down_sync(0xffffffffu, b, o);
         b = ob < b ? ob : b;
     }
-    if ((threadIdx.x & 31) == 0) atomicMin(dt_bits, b);
+    if ((threadIdx.x & 31) == 0 && cl >= 0) atomicMin(dt_bits + cl, b);
 }
 
 // ----------------------------------------------------------------------------------- launchers / registry

@@ -324,6 +324,15 @@ hcc_status hcc_upload_batch(hcc_ctx *ctx, int32_t n_clouds, const int64_t *offse
 hcc_status hcc_batch_layout(int32_t dim, double radius, int32_t n_clouds, const int64_t *offsets, const double *pos,
                             double *shifts, double *canvas);
 
+/* Per-cloud time steps of a batch (the reference advances every ParticleGrid with its own get_time_step,
+   ParticleGrids.jl:386-415): dt_out[c] = the CFL step of cloud c (hcc_time_step restricted to its particles; the
+   minimum over the batch is what hcc_time_step returns). */
+hcc_status hcc_batch_time_steps(hcc_ctx *ctx, double *dt_out);
+
+/* One step of every cloud of a batch, cloud c with its own dts[c] (the candidates, implicit parts and substeps of
+   each particle use its cloud's coefficients); otherwise as hcc_step. */
+hcc_status hcc_batch_step(hcc_ctx *ctx, double t, const double *dts);
+
 /* total_mass per cloud of the last hcc_upload_batch: out[c*M + m] (FP64 accumulation on the device). */
 hcc_status hcc_batch_total_mass(hcc_ctx *ctx, double *out);
 

@@ -126,3 +126,61 @@ def test_batch_rejects_periodic_and_bad_offsets(hcc, cuda_lib):
     g = hcc.Context(hcc.make_config(hcc.LinearAdvection(((1.0,), (1.0,))), per))
     with pytest.raises(hcc.HCCError):
         g.upload_batch([per, per])
+
+
+def _scaled_quadrant(c, L, s):
+    """The local quadrant state with every velocity scaled by sqrt(s) and the pressure by s: all wave speeds scale
+    by sqrt(s), so the clouds of a batch get different CFL steps."""
+    U = _local_quadrant(c, L)
+    q = np.sqrt(s)
+    return np.column_stack([U[:, 0], U[:, 1] * q, U[:, 2] * q, U[:, 3] * s])
+
+
+def test_batch_steps_each_cloud_with_its_own_dt(hcc, cuda_lib):
+    """One dt per cloud (the reference steps every ParticleGrid with its own get_time_step, ParticleGrids.jl:386-415):
+    the per-cloud CFL steps equal each cloud's stand-alone step and their minimum the batch's; a batch step with
+    those dts equals every cloud's stand-alone run at its own dt up to summation order; the step graph and the
+    host-driven step agree bit for bit."""
+    h = 1 / 64
+    sizes = (24, 40, 16)
+    scales = (1.0, 4.0, 9.0)
+    clouds = _clouds(hcc, h, sizes)
+    kw = dict(scheme=hcc.MUSCL(2, 2), mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h * h)), bc_map=OUTFLOW)
+    ctxs = []
+    for graphs in (True, False):
+        g = hcc.Context(hcc.make_config(hcc.Euler(2, 1.4), clouds[0], **kw))
+        union = g.upload_batch(clouds)
+        g.build_neighbours()
+        g.prepare_geometry()
+        g.set_step_graphs(graphs)
+        g.upload_state(np.concatenate([_scaled_quadrant(c, n * h, s) for c, n, s in zip(clouds, sizes, scales)]))
+        ctxs.append(g)
+    g = ctxs[0]
+    offs = union.meta["offsets"]
+    dts = g.batch_time_steps()
+    assert len(set(dts.tolist())) == 3 and dts.min() == g.time_step()
+    assert dts[0] > dts[1] > dts[2]
+    steps = 0.3 * dts
+    for k in range(3):
+        for c in ctxs:
+            c.step_batch(k * 0.0, steps)
+    Ug = ctxs[0].download_state()
+    assert np.array_equal(Ug.view(np.uint64), ctxs[1].download_state().view(np.uint64))
+    np.testing.assert_array_equal(ctxs[0].mood_flags(), ctxs[1].mood_flags())
+    for b, (c, n, s) in enumerate(zip(clouds, sizes, scales)):
+        g1 = hcc.Context(hcc.make_config(hcc.Euler(2, 1.4), c, **kw))
+        g1.upload_cloud(c)
+        g1.build_neighbours()
+        g1.prepare_geometry()
+        g1.upload_state(_scaled_quadrant(c, n * h, s))
+        assert abs(g1.time_step() - dts[b]) <= 1e-12 * dts[b]
+        for k in range(3):
+            g1.step(0.0, steps[b])
+        U1 = g1.download_state()
+        sl = slice(offs[b], offs[b + 1])
+        inner = c.is_boundary == 0
+        rel = np.abs(U1[inner] - Ug[sl][inner]).sum() / np.abs(U1[inner]).sum()
+        assert rel < 1e-9, (b, rel)
+    # a single-dt step afterwards still works (the graphs switch back)
+    g.step(0.0, float(steps.min()))
+    assert np.all(np.isfinite(g.download_state()))
