@@ -577,14 +577,15 @@ def run_profile_case(args):
         n = 128 * 152 * 8 // 16
         pred.loss_grad(X[:n], (rng.random(n) < 0.4).astype(np.uint8))
     steps = 3 if args.profile == "predictor" else args.profile_steps
-    ctx = hcc.Context(make_cfg(hcc, cloud, h, "fp32"))
+    prec = args.profile_precision
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
     ctx.upload_cloud(cloud)
     ctx.build_neighbours()
     ctx.prepare_geometry()
-    ctx.upload_state(U0.astype(np.float32))
+    ctx.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
     if not TILE_STAGING:
         ctx.set_tile_staging(False)
-    if args.profile != "plain":
+    if args.profile != "plain" and prec == "fp32":
         ctx.set_predictor(pred, PREDICTOR_THRESHOLD)
     ctx.set_step_graphs(False)
     dt = 0.4 * ctx.time_step()
@@ -1017,6 +1018,7 @@ def main():
     ap.add_argument("--profile", choices=["learned", "plain", "predictor"], default=None,
                     help="run a fixed workload for a kernel profiler instead of the benchmark")
     ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--profile-precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--ensemble-clouds", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=5)
     ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
