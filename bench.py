@@ -346,10 +346,21 @@ def load_predictor(hcc):
     return pred
 
 
-# One threshold for every workload, chosen on the training run's held-out rows (not on a test metric): the lowest
-# evaluated threshold whose held-out precision reaches 0.97 (0.974 at 0.9; a wrong pre-lowering costs accuracy, a
-# missed one only a MOOD recompute).
-PREDICTOR_THRESHOLD = 0.9
+def _predictor_threshold():
+    """One threshold for every workload, chosen on held-out training states, never on a test metric: the table of
+    `train_predictor.py --holdout-eval` (held-out seeds, every row kept) when it is present -- the lowest threshold
+    with precision >= 0.9 -- else 0.9, the lowest threshold whose precision on the training run's held-out rows
+    (unflagged rows subsampled) reaches 0.97. A wrong pre-lowering costs accuracy, a missed one only a recompute."""
+    p = PKG / "predictor_euler2d_holdout.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if d.get("threshold"):
+            return float(d["threshold"]), ("lowest held-out threshold with precision >= %g (held-out seeds, every row "
+                                           "kept; predictor_euler2d_holdout.json)" % d["min_precision"])
+    return 0.9, "lowest threshold with precision >= 0.97 on the training run's held-out rows (unflagged rows subsampled)"
+
+
+PREDICTOR_THRESHOLD, PREDICTOR_THRESHOLD_RULE = _predictor_threshold()
 
 
 def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, *, e2e_steps=None, profile_steps=None,
@@ -645,7 +656,7 @@ def run_gpu(args):
                    "predictor": ({"weights": "hypercloudcore.jl_gb300/predictor_euler2d.npz (train_predictor.py: "
                                   "200 seeded Voronoi runs at 250k nodes to t = 0.2)",
                                   "threshold": PREDICTOR_THRESHOLD,
-                                  "threshold_rule": "lowest held-out threshold with precision >= 0.97"}
+                                  "threshold_rule": PREDICTOR_THRESHOLD_RULE}
                                  if head == "fp32_learned" else None),
                    "step_form": "one CUDA graph per step (MOOD fixed points as conditional WHILE nodes)",
                    "l2": "inputs larger than L2 (per-slot neighbour arrays of several GB)",
@@ -853,6 +864,8 @@ def run_accuracy_study(args):
     import torch
     torch.cuda.set_device(0)
     predictor = load_predictor(hcc)
+    if args.study_learned_only:
+        return run_learned_study(args, hcc, predictor, cKDTree)
     out = {"threshold": PREDICTOR_THRESHOLD}
     for name in args.study_workloads.split(","):
         cloud, U0, h = make_workload(hcc, name)
@@ -890,6 +903,44 @@ def run_accuracy_study(args):
         out[name] = rec
         print(json.dumps({name: rec}), flush=True)
     print(json.dumps({"accuracy_study": out}), flush=True)
+    if args.study_out:
+        Path(args.study_out).write_text(json.dumps(out, indent=1) + "\n")
+
+
+def run_learned_study(args, hcc, predictor, cKDTree):
+    """The FP32 + predictor arm of the equal-L1 study again, for the thresholds of --study-thresholds (default: the
+    held-out one), against the references of the recorded study (profiles/accuracy_equal_l1.json: its end times and
+    FP64 errors; the references recomputed -- the radial solve, or the FP64 run at h/2, which is deterministic). Each
+    run takes its own CFL steps (0.4) to the recorded end time."""
+    global PREDICTOR_THRESHOLD
+    rec = json.loads((ROOT / "profiles" / "accuracy_equal_l1.json").read_text())
+    thresholds = [float(x) for x in args.study_thresholds.split(",")] if args.study_thresholds else \
+        [PREDICTOR_THRESHOLD]
+    keep = PREDICTOR_THRESHOLD
+    out = {"held_out_threshold": keep, "rule": PREDICTOR_THRESHOLD_RULE}
+    for name in args.study_workloads.split(","):
+        r0 = rec[name]
+        cloud, U0, h = make_workload(hcc, name)
+        D = cloud.pos.shape[1]
+        inner = cloud.is_boundary == 0
+        t_end = r0["t_end"]
+        if D == 3:
+            ref = radial_blast_reference(t_end, np.sqrt(((cloud.pos - 0.5) ** 2).sum(axis=1)))
+        else:
+            fine = hcc.rectangular_cloud((0.0,) * D, (1.0,) * D, h / 2, 2.5 * h / 2, jitter=0.25 * h / 2, seed=42)
+            rf, _, _, _ = run_cfl_steps(hcc, fine, quadrant_state(fine), h / 2, "fp64", t_end=t_end)
+            ref = rf[cKDTree(fine.pos).query(cloud.pos)[1]]
+        res = {"t_end": t_end, "l1_fp64": r0["l1_fp64"], "learned": {}}
+        for thr in thresholds:
+            PREDICTOR_THRESHOLD = thr
+            rho, dts, flagged, sec = run_cfl_steps(hcc, cloud, U0, h, "fp32", t_end=t_end, predictor=predictor)
+            l1 = rel_l1(rho, ref, inner)
+            res["learned"][f"{thr:g}"] = {"l1": l1, "over_fp64": l1 / r0["l1_fp64"], "steps": len(dts),
+                                         "flagged_total": flagged, "seconds": sec}
+        PREDICTOR_THRESHOLD = keep
+        out[name] = res
+        print(json.dumps({name: res}), flush=True)
+    print(json.dumps({"learned_study": out}), flush=True)
     if args.study_out:
         Path(args.study_out).write_text(json.dumps(out, indent=1) + "\n")
 
@@ -1029,6 +1080,9 @@ def main():
                     help="run the equal-L1 study at the configurations' end times instead of the benchmark")
     ap.add_argument("--study-workloads", default="euler3d_blast_8M,euler2d_quadrant_1M")
     ap.add_argument("--study-out", default=None, help="also write the study's JSON here")
+    ap.add_argument("--study-learned-only", action="store_true",
+                    help="only the FP32 + predictor arm, against the recorded study's references and end times")
+    ap.add_argument("--study-thresholds", default=None, help="comma-separated predictor thresholds (learned-only)")
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
     ap.add_argument("--no-tile-staging", action="store_true", help="stream-fed FP32 full passes (A/B)")

@@ -1312,11 +1312,14 @@ __device__ __forceinline__ void sts_words(float *row, const float *in) {
                             4 * g + 3 < N ? in[4 * g + 3] : 0.0f);
 }
 
-// Reconstruction pre-pass, one thread per particle of the tile: the cached degree-1 fit of gather_one with the
-// gradient weights recomputed per slot; every other case (boundary, starved or lowered order, failed fit, limiter)
-// goes through gather_one itself.
+// Reconstruction pre-pass, two threads per particle of the tile (slots k = h, h + 2, ... for h = 0, 1): the cached
+// degree-1 fit of gather_one with the gradient weights recomputed per slot, the second thread's partial sums added by
+// the first through shared memory; every other case (boundary, starved or lowered order, failed fit, limiter) goes
+// through gather_one itself.
+template <int D, int M> constexpr int tile_gather_min_blocks() { return M >= 8 ? 1 : 3; }
+
 template <int D, int M, int PDE>
-__global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float> a) {
+__global__ void __launch_bounds__(2 * HCC_TILE, tile_gather_min_blocks<D, M>()) k_gather_tile(const StageArgs<float> a) {
     extern __shared__ __align__(16) float sm[];
     constexpr int W = tile_gather_row<D, M>();
     const int64_t t = blockIdx.x;
@@ -1335,79 +1338,99 @@ __global__ void __launch_bounds__(HCC_TILE) k_gather_tile(const StageArgs<float>
             sts_words<D + M>(sm + e * W, v);
         }
     }
+    float *parts = sm + a.tv.umax * W;           // [HCC_TILE][D * M] partial gradients of the second threads
     __syncthreads();
-    const int64_t i = t * HCC_TILE + threadIdx.x;
-    if (i >= a.g.n || a.g.bnd[i]) return;
-    const int cnt = a.g.cnt[i];
-    {
+    const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
+    const int64_t i = t * HCC_TILE + pl;
+    int mode = 0;                                 // 1: the cached fit here, 2: gather_one (first thread)
+    int cnt = 0;
+    if (i < a.g.n && !a.g.bnd[i]) {
+        cnt = a.g.cnt[i];
         int q = a.orders[i];
         while (q > 1 && cnt < basis_count(D, q - 1)) --q;
-        if (!(q == a.sc.max_order && q > 1 && a.g.ok_r[i] && a.sc.limiter == HCC_LIMITER_NONE)) {
-            gather_one<float, D, M, PDE, 1>(a, i);
-            return;
-        }
+        mode = (q == a.sc.max_order && q > 1 && a.g.ok_r[i] && a.sc.limiter == HCC_LIMITER_NONE) ? 1 : 2;
     }
-    const int64_t np = a.g.npad;
-    float own[D + M];
-    lds_words<D + M>(sm + int(a.tv.lself[i]) * W, own);
-    int qi[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) qi[d] = __float_as_int(own[d]);
-    float G[D][D];
-    const float *cf = a.tv.coef + i * a.tv.cw + D + D * D;
-#pragma unroll
-    for (int b = 0; b < D; ++b)
-#pragma unroll
-        for (int c = 0; c < D; ++c) G[b][c] = cf[b * D + c];
-    const float qt = a.tv.quantum[t], ws = a.tv.wscale;
     float out[D][M];
 #pragma unroll
     for (int b = 0; b < D; ++b)
 #pragma unroll
         for (int m = 0; m < M; ++m) out[b][m] = 0.0f;
-    // union places of the slots in groups of PF, the next group's loads in flight while this group is summed
-    constexpr int PF = 8;
-    const uint16_t *lp = a.tv.lidx + i;
-    int lbuf[PF];
+    if (mode == 1) {
+        const int64_t np = a.g.npad;
+        float own[D + M];
+        lds_words<D + M>(sm + int(a.tv.lself[i]) * W, own);
+        int qi[D];
 #pragma unroll
-    for (int q = 0; q < PF; ++q) lbuf[q] = q < cnt ? int(lp[int64_t(q) * np]) : 0;
-    for (int k0 = 0; k0 < cnt; k0 += PF) {
-        int lnext[PF];
+        for (int d = 0; d < D; ++d) qi[d] = __float_as_int(own[d]);
+        float G[D][D];
+        const float *cf = a.tv.coef + i * a.tv.cw + D + D * D;
 #pragma unroll
-        for (int q = 0; q < PF; ++q) lnext[q] = k0 + PF + q < cnt ? int(lp[int64_t(k0 + PF + q) * np]) : 0;
+        for (int b = 0; b < D; ++b)
 #pragma unroll
-        for (int q = 0; q < PF; ++q) {
-            if (k0 + q >= cnt) break;
-            float r[D + M];
-            lds_words<D + M>(sm + lbuf[q] * W, r);
-            int qj[D];
+            for (int c = 0; c < D; ++c) G[b][c] = cf[b * D + c];
+        const float qt = a.tv.quantum[t], ws = a.tv.wscale;
+        // this thread's slots h, h + 2, ...: their union places in groups of PF, the next group's loads in flight
+        // while this group is summed
+        constexpr int PF = 8;
+        const int mine = cnt > h ? (cnt - h + 1) / 2 : 0;
+        const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+        const int64_t step = 2 * np;
+        int lbuf[PF];
 #pragma unroll
-            for (int d = 0; d < D; ++d) qj[d] = __float_as_int(r[d]);
-            float x[D];
-            tile_offset<D>(qj, qi, qt, x);
-            float r2 = x[0] * x[0];
+        for (int q = 0; q < PF; ++q) lbuf[q] = q < mine ? int(lp[int64_t(q) * step]) : 0;
+        for (int k0 = 0; k0 < mine; k0 += PF) {
+            int lnext[PF];
 #pragma unroll
-            for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
-            const float w = tile_weight(r2, ws);
-            float gk[D];
+            for (int q = 0; q < PF; ++q) lnext[q] = k0 + PF + q < mine ? int(lp[int64_t(k0 + PF + q) * step]) : 0;
 #pragma unroll
-            for (int b = 0; b < D; ++b) {
-                float v = G[b][0] * x[0];
+            for (int q = 0; q < PF; ++q) {
+                if (k0 + q >= mine) break;
+                float r[D + M];
+                lds_words<D + M>(sm + lbuf[q] * W, r);
+                int qj[D];
 #pragma unroll
-                for (int c = 1; c < D; ++c) v = v + G[b][c] * x[c];
-                gk[b] = w * v;
+                for (int d = 0; d < D; ++d) qj[d] = __float_as_int(r[d]);
+                float x[D];
+                tile_offset<D>(qj, qi, qt, x);
+                float r2 = x[0] * x[0];
+#pragma unroll
+                for (int d = 1; d < D; ++d) r2 = r2 + x[d] * x[d];
+                const float w = tile_weight(r2, ws);
+                float gk[D];
+#pragma unroll
+                for (int b = 0; b < D; ++b) {
+                    float v = G[b][0] * x[0];
+#pragma unroll
+                    for (int c = 1; c < D; ++c) v = v + G[b][c] * x[c];
+                    gk[b] = w * v;
+                }
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float dm = r[D + m] - own[D + m];
+#pragma unroll
+                    for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
+                }
             }
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const float dm = r[D + m] - own[D + m];
-#pragma unroll
-                for (int b = 0; b < D; ++b) out[b][m] = out[b][m] + gk[b] * dm;
-            }
+            for (int q = 0; q < PF; ++q) lbuf[q] = lnext[q];
         }
+        if (h == 1)
 #pragma unroll
-        for (int q = 0; q < PF; ++q) lbuf[q] = lnext[q];
+            for (int b = 0; b < D; ++b)
+#pragma unroll
+                for (int m = 0; m < M; ++m) parts[pl * (D * M) + b * M + m] = out[b][m];
     }
-    store_vec<float, D * M>(a.grad + i * (D * M), &out[0][0]);
+    __syncthreads();
+    if (h == 1) return;
+    if (mode == 2) {
+        gather_one<float, D, M, PDE, 1>(a, i);
+    } else if (mode == 1) {
+#pragma unroll
+        for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int m = 0; m < M; ++m) out[b][m] = out[b][m] + parts[pl * (D * M) + b * M + m];
+        store_vec<float, D * M>(a.grad + i * (D * M), &out[0][0]);
+    }
 }
 
 // Flux pass, two threads per particle of the tile (slots k = h, h + 2, ... for h = 0, 1); the second writes its
@@ -1584,7 +1607,7 @@ inline int tile_smem_optin() {
 
 // Dynamic shared memory of the tile passes for the largest union.
 template <int D, int M> inline size_t tile_gather_smem(int umax) {
-    return size_t(umax) * tile_gather_row<D, M>() * sizeof(float);
+    return (size_t(umax) * tile_gather_row<D, M>() + size_t(HCC_TILE) * D * M) * sizeof(float);
 }
 template <int D, int M> inline size_t tile_flux_smem(int umax) {
     return size_t(umax) * (4 + tile_flux_row<D, M>()) * sizeof(float) + size_t(HCC_TILE) * sizeof(FluxPart<float, M>);
@@ -2241,7 +2264,7 @@ struct StageInst {
                                          tile_smem_optin());
                     attr = true;
                 }
-                k_gather_tile<D, M, PDE><<<unsigned(a.tv.ntiles), HCC_TILE, tile_gather_smem<D, M>(a.tv.umax), s>>>(a);
+                k_gather_tile<D, M, PDE><<<unsigned(a.tv.ntiles), 2 * HCC_TILE, tile_gather_smem<D, M>(a.tv.umax), s>>>(a);
                 return;
             }
             if (!a.full) {   // FP32 degree-1 worklist pass: split tiles (four warps a tile)

@@ -204,3 +204,27 @@ def generate_training_set(hcc, predictor: TroubledPointPredictor, runs: int, h: 
 
 def default_weights_path() -> Path:
     return Path(__file__).resolve().parent / "predictor_euler2d.npz"
+
+
+def holdout_path() -> Path:
+    return Path(__file__).resolve().parent / "predictor_euler2d_holdout.json"
+
+
+def holdout_thresholds(hcc, weights, thresholds, runs: int = 8, h: float = 2e-3, t_end: float = 0.2,
+                       every: int = 100, seed0: int = 900000, min_precision: float = 0.9, log=None) -> dict:
+    """Precision and recall of a trained network on held-out runs: the training recipe's seeded 2-D Euler runs with
+    seeds outside the training range, EVERY row kept (the training set keeps only a small share of the unflagged
+    rows, so its held-out precision overstates the precision a step sees). The chosen threshold is the lowest one
+    whose held-out precision reaches `min_precision`: a pre-lowered particle that MOOD would not have flagged costs
+    accuracy, a missed one only a recompute."""
+    pred = TroubledPointPredictor(capacity=1 << 26, neg_keep=1.0, seed=seed0)
+    pred.load(weights)
+    gen = generate_training_set(hcc, pred, runs, h, t_end, seed0=seed0, every=every, log=log)
+    table = {}
+    for thr in thresholds:
+        table[f"{thr:g}"] = pred.evaluate(float(thr), holdout=1.0)
+    chosen = next((thr for thr in sorted(thresholds) if table[f"{thr:g}"]["precision"] >= min_precision), None)
+    pred.close()
+    return {"runs": runs, "seeds": [seed0, seed0 + runs - 1], "rows": gen["rows"], "flagged": gen["flagged"],
+            "every": every, "h": h, "t_end": t_end, "min_precision": min_precision, "table": table,
+            "threshold": chosen}

@@ -7,6 +7,7 @@ its start state and its MOOD flags are appended to the training rows on the devi
 unflagged ones with probability neg_keep). Then Adam on the GPU's tensor-core training kernels.
 
     python hypercloudcore.jl_gb300/train_predictor.py [--runs 200] [--out path]
+    python hypercloudcore.jl_gb300/train_predictor.py --holdout-eval     # threshold table on held-out runs
 """
 from __future__ import annotations
 
@@ -47,9 +48,21 @@ def main(argv=None):
     ap.add_argument("--holdout", type=float, default=0.05)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", type=str, default=str(PKG / "predictor_euler2d.npz"))
+    ap.add_argument("--holdout-eval", action="store_true",
+                    help="only evaluate the weights in --out on held-out runs (every row kept) and write the "
+                         "threshold table next to them")
+    ap.add_argument("--holdout-runs", type=int, default=8)
     a = ap.parse_args(argv)
     hcc = package()
     learned = sys.modules["hcc_gb300.learned"]
+    if a.holdout_eval:
+        res = learned.holdout_thresholds(hcc, a.out, (0.9, 0.95, 0.97, 0.98, 0.99, 0.995, 0.998, 0.999),
+                                         runs=a.holdout_runs, h=a.h, t_end=a.t_end, every=a.every,
+                                         log=lambda m: print(m, flush=True))
+        out = Path(a.out).with_name(Path(a.out).stem + "_holdout.json")
+        out.write_text(json.dumps(res, indent=1) + "\n")
+        print(json.dumps(res), flush=True)
+        return res
     pred = hcc.TroubledPointPredictor(capacity=a.capacity, neg_keep=a.neg_keep, seed=a.seed, lr=a.lr)
     t0 = time.time()
     gen = learned.generate_training_set(hcc, pred, a.runs, a.h, a.t_end, seed0=a.seed * 100000, every=a.every,
