@@ -56,3 +56,45 @@ def test_radial_blast_reference_conserves_mass_and_converges():
     m0 = np.sum(np.where(r < 0.2, 1.0, 0.125) * w)
     assert abs(np.sum(fine * w) - m0) / m0 < 2e-3           # trapezoid-free sum on a fine radius grid
     assert fine[0] == 1.0 and fine[-1] == 0.125
+
+
+def test_predictor_threshold_rule(tmp_path, monkeypatch):
+    import json
+    table = {"0.9": {"precision": 0.85, "recall": 0.7}, "0.95": {"precision": 0.92, "recall": 0.5},
+             "0.99": {"precision": 0.97, "recall": 0.2}}
+    monkeypatch.setattr(bench, "PKG", tmp_path)
+    (tmp_path / "predictor_euler2d_holdout.json").write_text(
+        json.dumps({"min_precision": 0.9, "table": table, "threshold": 0.95}))
+    thr, rule, ok = bench._predictor_threshold()
+    assert thr == 0.95 and ok and "held-out" in rule
+    (tmp_path / "predictor_euler2d_holdout.json").write_text(
+        json.dumps({"min_precision": 0.99, "table": table, "threshold": None}))
+    thr, rule, ok = bench._predictor_threshold()
+    assert thr == 0.9 and not ok and "0.97 at 0.99" in rule
+    (tmp_path / "predictor_euler2d_holdout.json").unlink()
+    assert bench._predictor_threshold()[2] is False
+
+
+def test_recorded_learned_ratio(tmp_path, monkeypatch):
+    import json
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    (tmp_path / "profiles").mkdir()
+    assert bench.learned_l1_ratio("euler3d_blast_8M", 0.9)[0] is None
+    (tmp_path / "profiles" / "accuracy_equal_l1.json").write_text(
+        json.dumps({"threshold": 0.9, "euler3d_blast_8M": {"learned_over_fp64": 1.5}}))
+    assert bench.learned_l1_ratio("euler3d_blast_8M", 0.9)[0] == 1.5
+    assert bench.learned_l1_ratio("euler3d_blast_8M", 0.99)[0] is None
+    (tmp_path / "profiles" / "accuracy_learned.json").write_text(
+        json.dumps({"euler3d_blast_8M": {"learned": {"0.99": {"over_fp64": 1.05}}}}))
+    assert bench.learned_l1_ratio("euler3d_blast_8M", 0.99) == (1.05, "profiles/accuracy_learned.json")
+    assert bench.learned_l1_ratio("euler3d_blast_8M", 0.9)[0] == 1.5
+
+
+def test_committed_holdout_table_is_consistent():
+    import json
+    d = json.loads((ROOT / "hypercloudcore.jl_gb300" / "predictor_euler2d_holdout.json").read_text())
+    q = [float(k) for k, v in d["table"].items() if v["precision"] >= d["min_precision"]]
+    assert d["threshold"] == (min(q) if q else None)
+    for v in d["table"].values():
+        assert v["precision"] == pytest.approx(v["tp"] / (v["tp"] + v["fp"]))
+        assert v["recall"] == pytest.approx(v["tp"] / (v["tp"] + v["fn"]))
