@@ -434,10 +434,10 @@ def per_launch(kt, name):
     return kt[f"{name}_ms"] / max(kt[f"{name}_launches"], 1)
 
 
-def roofline_of(workload, D, M, K, n_int, kt, peak, peak_kind):
+def roofline_of(workload, D, M, K, n_int, kt, peak, peak_kind, tiled=False):
     """The flux pass (dominant kernel) and the reconstruction pre-pass against the HBM copy peak: algorithmic bytes
     per point-stage x interior points / CUDA-event launch time; `traffic` = the ncu DRAM bytes per point-stage of
-    profiles/traffic.txt for this workload, scaled to the launch."""
+    profiles/traffic.txt for this workload, scaled to the launch. `tiled`: the tile-staged passes ran."""
     flux_b, gather_b = algorithmic_bytes(K, D, M, D, D + 1, 4)
     rec = recorded_traffic()
     flux_ms, gather_ms = per_launch(kt, "flux"), per_launch(kt, "gather")
@@ -445,13 +445,15 @@ def roofline_of(workload, D, M, K, n_int, kt, peak, peak_kind):
     traffic = rec.get(f"flux_f32_{workload}_bytes_per_point_stage")
     g_traffic = rec.get(f"gather_f32_{workload}_bytes_per_point_stage")
     g_model = gather_b * n_int / (gather_ms / 1e3) / 1e9
-    gather_roof = {"kernel": f"k_gather<float,{D},{M},EULER,1>", "bound": "hbm", "unit": "GB/s", "peak": peak,
+    gname = f"k_gather_tile<{D},{M},EULER>" if tiled else f"k_gather<float,{D},{M},EULER,1>"
+    fname = f"k_flux_tile<{D},{M},EULER>" if tiled else f"k_flux<float,{D},{M},EULER,1>"
+    gather_roof = {"kernel": gname, "bound": "hbm", "unit": "GB/s", "peak": peak,
                    "achieved": g_model, "frac": g_model / peak,
                    "traffic": (g_traffic * n_int) if g_traffic else None,
                    "dram_achieved": (g_traffic * n_int / (gather_ms / 1e3) / 1e9) if g_traffic else None,
                    "dram_frac": (g_traffic * n_int / (gather_ms / 1e3) / 1e9 / peak) if g_traffic else None,
                    "ms_per_launch": gather_ms}
-    return {"bound": "hbm", "kernel": f"k_flux<float,{D},{M},EULER,1>", "achieved": achieved, "peak": peak,
+    return {"bound": "hbm", "kernel": fname, "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
             if peak_kind == "measured" else peak_kind,
             "traffic": (traffic * n_int) if traffic else None,
@@ -677,7 +679,8 @@ def run_gpu(args):
         "gpu_launches": r["launches"],
         "e2e": {"value": n_int * STAGES * r["e2e_steps"] * world / r["e2e_s"], "unit": "point-updates/s",
                 "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"], "steps": r["e2e_steps"]},
-        "roofline": roofline_of(args.workload, D, M, K, n_int, r["kt"], peak, peak_kind),
+        "roofline": roofline_of(args.workload, D, M, K, n_int, r["kt"], peak, peak_kind,
+                                tiled=bool(r["tile_staging"] and r["tile_staging"].get("active"))),
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],
                  "predicted_last_step": cnt.get("predicted", 0)},
@@ -749,7 +752,8 @@ def run_secondary(hcc, args, world, local, name, predictor, peak, peak_kind):
         out[arm] = {"value": units / (r["ms"] / 1e3), "ms_per_step": r["ms"] / K_steps, "clocks": r["clocks"],
                     "mood_iterations_last_step": r["counters"]["mood_iterations"]}
         if prec == "fp32":
-            out[arm]["roofline"] = roofline_of(name, D, D + 2, K, n_int, r["kt"], peak, peak_kind)
+            out[arm]["roofline"] = roofline_of(name, D, D + 2, K, n_int, r["kt"], peak, peak_kind,
+                                               tiled=bool(r["tile_staging"] and r["tile_staging"].get("active")))
         else:
             out[arm]["roofline"] = fp64_roofline(D, D + 2, K, n_int, r.get("kt"), fp64_peak(hcc))
         out["mean_neighbours"] = K

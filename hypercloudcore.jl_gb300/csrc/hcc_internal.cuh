@@ -26,6 +26,12 @@
 #define HCC_FP32_PACKED 0          // FP32 stage kernels: 1 = packed FP32x2 instructions for component pairs (measured
                                    // slower than scalar instructions in the tile-staged 3-D flux pass)
 #endif
+#ifndef HCC_TILE_FLUX_PF
+#define HCC_TILE_FLUX_PF 8         // tile-staged flux pass: union places of a thread's slots fetched this many slots ahead
+#endif
+#ifndef HCC_TILE_STAGE_UNROLL
+#define HCC_TILE_STAGE_UNROLL 4    // tile passes: union entries a thread stages per round (halved for wide rows)
+#endif
 #ifndef HCC_FLUX_MINB64
 #define HCC_FLUX_MINB64 3          // FP64: its Euler flux needs ~140 registers without spilling
 #endif

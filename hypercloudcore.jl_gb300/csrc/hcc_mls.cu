@@ -154,7 +154,10 @@ __device__ void chol_solve(int B, const double *U, const double *b, double *x) {
     }
 }
 
-// Moment matrix of particle i for a fit of degree q (optionally with intercept): N = Σ w (p p').
+// Moment matrix of particle i for a fit of degree q (optionally with intercept): N = Σ w (p p'). The upper
+// triangle is summed and mirrored: p_r p_c and p_c p_r are the same IEEE product, so every entry equals the full
+// matrix's sum of the same terms in the same order, bit for bit, with 37-45 % fewer FP64 instructions (the
+// pass is bound by the FP64 unit).
 template <int BM>
 __device__ void assemble(const MlsArgs &a, int64_t i, int cnt, int q, bool intercept, int B, double *N) {
     for (int k = 0; k < B * B; ++k) N[k] = 0.0;
@@ -165,8 +168,10 @@ __device__ void assemble(const MlsArgs &a, int64_t i, int cnt, int q, bool inter
         gen_basis(a.D, q, intercept, x, p);
         double w = a.w[s];
         for (int r = 0; r < B; ++r)
-            for (int c = 0; c < B; ++c) N[r * B + c] = N[r * B + c] + w * (p[r] * p[c]);
+            for (int c = r; c < B; ++c) N[r * B + c] = N[r * B + c] + w * (p[r] * p[c]);
     }
+    for (int r = 1; r < B; ++r)
+        for (int c = 0; c < r; ++c) N[r * B + c] = N[c * B + r];
 }
 
 // Inverse moment matrix (C \ e_j per column), padded into a Bpad×Bpad block.

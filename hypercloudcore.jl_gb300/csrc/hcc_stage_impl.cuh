@@ -207,6 +207,55 @@ __device__ __forceinline__ void flux_and_speed(const PhysParams<T> &ph, const T 
     }
 }
 
+// FP32 Euler on a fixed grid, the flux contracted with a weight vector w: Fw(U) = sum_d w_d F_d(U) =
+// (m.w, (u.w) m + p w, (E + p)(u.w)), and the axis speeds |u_d| + c of flux_and_speed. One contracted flux
+// replaces the D axis fluxes and their contraction in the flux pass (the Rusanov flux is linear in the F_d).
+template <int D>
+__device__ __forceinline__ void euler_projected(const PhysParams<float> &ph, const float *U, const float *w,
+                                                float *Fn, float *lam) {
+    float inv_rho, u[D], p;
+    euler_prim<float, D>(ph, U, inv_rho, u, p);
+    const float c = root(ph.gamma * p * inv_rho);
+    float un = u[0] * w[0], mw = U[1] * w[0];
+#pragma unroll
+    for (int d = 1; d < D; ++d) { un = un + u[d] * w[d]; mw = mw + U[1 + d] * w[d]; }
+    Fn[0] = mw;
+#pragma unroll
+    for (int e = 0; e < D; ++e) Fn[1 + e] = un * U[1 + e] + p * w[e];
+    Fn[D + 1] = (U[D + 1] + p) * un;
+#pragma unroll
+    for (int d = 0; d < D; ++d) lam[d] = fabsf(u[d]) + c;
+}
+
+// Whether the flux pass takes the contracted Euler form (FP32, fixed grid, no moment correction).
+template <typename T, int PDE, bool ALE, bool MOM> constexpr bool projected_flux() {
+    return sizeof(T) == 4 && PDE == HCC_PDE_EULER && !ALE && !MOM;
+}
+
+// The own flux a flux pass keeps for particle i: F(f_i) per axis (FP64), doubled (FP32, the scaled Rusanov form),
+// or for the contracted Euler form the constants 2 Fw(f_i) is formed from in every slot, in the first row:
+// (2u, 2p, E + p).
+template <typename T, int D, int M, int PDE, bool ALE, bool MOM>
+__device__ __forceinline__ void own_flux(const PhysParams<T> &ph, const T *fi, T (*Fi)[M], const T *wp) {
+    if constexpr (projected_flux<T, PDE, ALE, MOM>()) {
+        T inv_rho, u[D], p;
+        euler_prim<T, D>(ph, fi, inv_rho, u, p);
+#pragma unroll
+        for (int d = 0; d < D; ++d) Fi[0][d] = T(2) * u[d];
+        Fi[0][D] = T(2) * p;
+        Fi[0][D + 1] = fi[D + 1] + p;
+    } else {
+        T lam[D];
+        flux_and_speed<T, D, M, PDE>(ph, fi, Fi, lam, wp);
+        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+#pragma unroll
+                for (int m = 0; m < M; ++m) Fi[d][m] = T(2) * Fi[d][m];
+        }
+    }
+}
+
 // grid_velocity (GridMovers.jl:60-63) of particle i: fluid velocity (Euler m_d / rho, scalar advection c_d), scaled,
 // or the prescribed field velocity + omega x (x - center) at its current position
 template <typename T, int D, int M, int PDE>
@@ -979,6 +1028,33 @@ __device__ __forceinline__ void flux_slot(const StageArgs<T> &a, const T *fi, co
         fij[m] = fi[m] + si;
         fji[m] = fj[m] + sj;
     }
+    if constexpr (projected_flux<T, PDE, ALE, MOM>()) {
+        // FP32 Euler, fixed grid: the doubled Rusanov difference contracted with the slot's divergence weights,
+        //   sum_d w_d [(F_d(f_ij) + F_d(f_ji)) - s_d max(λ_d) (f_ji - f_ij) - 2 F_d(f_i)]
+        //     = Fw(f_ij) + Fw(f_ji) - S (f_ji - f_ij) - 2 Fw(f_i),   S = sum_d w_d s_d max(λ_d)
+        // with Fw(U) = sum_d w_d F_d(U) (euler_projected) and 2 Fw(f_i) = (rho (2u.w), (2u.w) m + 2p w,
+        // (E + p)(2u.w)) from the own constants of own_flux.
+        T Fa[M], Fb[M], la[D], lb[D];
+        euler_projected<D>(a.ph, fij, wk, Fa, la);
+        euler_projected<D>(a.ph, fji, wk, Fb, lb);
+        T S = T(0), un2 = T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const T sd = vmax(la[d], lb[d]);
+            const T ssd = (below ? wk[d] : dk[d]) > T(0) ? sd : -sd;
+            S = (d == 0) ? wk[0] * ssd : S + wk[d] * ssd;
+            un2 = (d == 0) ? wk[0] * Fi[0][0] : un2 + wk[d] * Fi[0][d];
+        }
+        T t[M], own[M];
+        own[0] = fi[0] * un2;
+#pragma unroll
+        for (int e = 0; e < D; ++e) own[1 + e] = un2 * fi[1 + e] + Fi[0][D] * wk[e];
+        own[D + 1] = Fi[0][D + 1] * un2;
+#pragma unroll
+        for (int m = 0; m < M; ++m) t[m] = ((Fa[m] + Fb[m]) - S * (fji[m] - fij[m])) - own[m];
+        acc.add(t);
+        return;
+    }
     T Fij[D][M], Fji[D][M], lij[D], lji[D];
     flux_and_speed<T, D, M, PDE>(a.ph, fij, Fij, lij, wp);
     flux_and_speed<T, D, M, PDE>(a.ph, fji, Fji, lji, wp);
@@ -1058,7 +1134,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
     const int64_t np = a.g.npad;
     const T invL = a.g.invL;
     (void)invL;
-    T fi[M], gi[BR][M], Fi[D][M], lami[D];
+    T fi[M], gi[BR][M], Fi[D][M];
     load_vec<T, M>(a.U + i * M, fi);
     load_vec<T, BR * M>(a.grad + i * (BR * M), &gi[0][0]);
     // moving grid: this particle's grid velocity (K_X of the stage) and every flux in its frame
@@ -1071,14 +1147,8 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
 #pragma unroll
             for (int d = 0; d < D; ++d) a.KXout[int64_t(d) * a.g.npad + i] = double(wv[d]);
     }
-    flux_and_speed<T, D, M, PDE>(a.ph, fi, Fi, lami, wp);
-    constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form (below)
-    if constexpr (kFast) {
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-#pragma unroll
-            for (int m = 0; m < M; ++m) Fi[d][m] = T(2) * Fi[d][m];
-    }
+    own_flux<T, D, M, PDE, ALE, MOM>(a.ph, fi, Fi, wp);
+    constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form (flux_slot)
     const int oi_own = a.orders[i];
     const int didx = divergence_index(a.sc.DO, D, oi_own, cnt);
     const bool cached = a.g.ok_d[i] && didx == divergence_index(a.sc.DO, D, a.sc.max_order, cnt);
@@ -1316,6 +1386,12 @@ __device__ __forceinline__ void sts_words(float *row, const float *in) {
 // degree-1 fit of gather_one with the gradient weights recomputed per slot, the second thread's partial sums added by
 // the first through shared memory; every other case (boundary, starved or lowered order, failed fit, limiter) goes
 // through gather_one itself.
+// Union entries a thread stages per round in the tile passes (all their loads in flight before the first store):
+// HCC_TILE_STAGE_UNROLL for rows of up to 12 words, half as many for wider rows (registers).
+template <int RW> constexpr int tile_stage_unroll() {
+    return RW <= 12 ? HCC_TILE_STAGE_UNROLL : (HCC_TILE_STAGE_UNROLL + 1) / 2;
+}
+
 template <int D, int M> constexpr int tile_gather_min_blocks() { return M >= 8 ? 1 : 3; }
 
 template <int D, int M, int PDE>
@@ -1326,16 +1402,29 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_gather_min_blocks<D, M>()) 
     {
         const int64_t u0 = a.tv.ustart[t];
         const int nu = int(a.tv.ustart[t + 1] - u0);
-        for (int e = threadIdx.x; e < nu; e += blockDim.x) {
-            const int32_t j = a.tv.uid[u0 + e];
-            const int4 q = a.tv.upos[u0 + e];
-            float v[D + M];
-            v[0] = __int_as_float(q.x);
-            if constexpr (D > 1) v[1] = __int_as_float(q.y);
-            if constexpr (D > 2) v[2] = __int_as_float(q.z);
+        // SU entries per thread and round: their ids first, then every load of the round in flight, then the stores
+        constexpr int SU = tile_stage_unroll<D + M>();
+        const int nt = int(blockDim.x);
+        for (int e0 = threadIdx.x; e0 < nu; e0 += SU * nt) {
+            int32_t jj[SU];
 #pragma unroll
-            for (int m = 0; m < M; ++m) v[D + m] = a.U[int64_t(j) * M + m];
-            sts_words<D + M>(sm + e * W, v);
+            for (int u = 0; u < SU; ++u) jj[u] = e0 + u * nt < nu ? a.tv.uid[u0 + e0 + u * nt] : 0;
+            float v[SU][D + M];
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                const int4 q = a.tv.upos[u0 + e0 + u * nt];
+                v[u][0] = __int_as_float(q.x);
+                if constexpr (D > 1) v[u][1] = __int_as_float(q.y);
+                if constexpr (D > 2) v[u][2] = __int_as_float(q.z);
+#pragma unroll
+                for (int m = 0; m < M; ++m) v[u][D + m] = a.U[int64_t(jj[u]) * M + m];
+            }
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                sts_words<D + M>(sm + (e0 + u * nt) * W, v[u]);
+            }
         }
     }
     float *parts = sm + a.tv.umax * W;           // [HCC_TILE][D * M] partial gradients of the second threads
@@ -1448,17 +1537,34 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
     int4 *spos = reinterpret_cast<int4 *>(sm);
     float *srow = sm + 4 * a.tv.umax;
     FluxPart<float, M> *parts = reinterpret_cast<FluxPart<float, M> *>(srow + a.tv.umax * W);
-    for (int e = threadIdx.x; e < nu; e += blockDim.x) {
-        const int32_t j = a.tv.uid[u0 + e];
-        int4 q = a.tv.upos[u0 + e];
-        q.w = a.orders[j];
-        spos[e] = q;
-        float v[RW];
+    {
+        // SU entries per thread and round: their ids first, then every load of the round in flight, then the stores
+        constexpr int SU = tile_stage_unroll<RW>();
+        const int nt = int(blockDim.x);
+        for (int e0 = threadIdx.x; e0 < nu; e0 += SU * nt) {
+            int32_t jj[SU];
 #pragma unroll
-        for (int m = 0; m < M; ++m) v[m] = a.U[int64_t(j) * M + m];
+            for (int u = 0; u < SU; ++u) jj[u] = e0 + u * nt < nu ? a.tv.uid[u0 + e0 + u * nt] : 0;
+            int4 qq[SU];
+            float v[SU][RW];
 #pragma unroll
-        for (int c = 0; c < D * M; ++c) v[M + c] = a.grad[int64_t(j) * (D * M) + c];
-        sts_words<RW>(srow + e * W, v);
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                const int64_t j = jj[u];
+                qq[u] = a.tv.upos[u0 + e0 + u * nt];
+                qq[u].w = a.orders[j];
+#pragma unroll
+                for (int m = 0; m < M; ++m) v[u][m] = a.U[j * M + m];
+#pragma unroll
+                for (int c = 0; c < D * M; ++c) v[u][M + c] = a.grad[j * (D * M) + c];
+            }
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                spos[e0 + u * nt] = qq[u];
+                sts_words<RW>(srow + (e0 + u * nt) * W, v[u]);
+            }
+        }
     }
     __syncthreads();
     const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
@@ -1485,16 +1591,17 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
 #pragma unroll
                 for (int m = 0; m < M; ++m) gi[b][m] = own[M + b * M + m];
         }
-        float lami[D];
-        flux_and_speed<float, D, M, PDE>(a.ph, fi, Fi, lami, nullptr);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-#pragma unroll
-            for (int m = 0; m < M; ++m) Fi[d][m] = 2.0f * Fi[d][m];
+        own_flux<float, D, M, PDE, false, false>(a.ph, fi, Fi, nullptr);
         const bool wok = cnt > 0 && a.g.ok_d[i];
-        const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+        // this thread's slots h, h + 2, ...: their union places fetched PF slots ahead (a rotating window)
+        constexpr int PF = HCC_TILE_FLUX_PF;
+        const int mine = cnt > h ? (cnt - h + 1) / 2 : 0;
         const int64_t lstep = 2 * np;
-        int ln = h < cnt ? int(*lp) : 0;
+        const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+        int lb[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) lb[q] = q < mine ? int(lp[int64_t(q) * lstep]) : 0;
+        lp += int64_t(PF) * lstep;
         if (wok) {
             const float *cf = a.tv.coef + i * a.tv.cw;
             float A[D], B[D][D];
@@ -1505,10 +1612,13 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                 for (int e = 0; e < D; ++e) B[d][e] = cf[D + d * D + e];
             }
             const float qt = a.tv.quantum[t], ws = a.tv.wscale;
-            for (int k = h; k < cnt; k += 2) {
-                const int l = ln;
+            for (int s = 0; s < mine; ++s) {
+                const int k = h + 2 * s;
+                const int l = lb[0];
+#pragma unroll
+                for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
+                lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
                 lp += lstep;
-                if (k + 2 < cnt) ln = int(*lp);
                 const int4 qj4 = spos[l];
                 const int qj[3] = {qj4.x, qj4.y, qj4.z};
                 float dk[D], wk[D];
@@ -1540,10 +1650,12 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                                                              wk, acc, i, k);
             }
         } else if (need_ext) {
-            for (int k = h; k < cnt; k += 2) {
-                const int l = ln;
+            for (int s = 0; s < mine; ++s) {
+                const int l = lb[0];
+#pragma unroll
+                for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
+                lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
                 lp += lstep;
-                if (k + 2 < cnt) ln = int(*lp);
                 float r[M];
                 lds_words<M>(srow + l * W, r);
 #pragma unroll

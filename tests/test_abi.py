@@ -108,7 +108,8 @@ def test_struct_layouts_match_the_header(hcc, tmp_path):
 def test_build_info_names_the_launch_bounds(cuda_lib):
     info = cuda_lib.hcc_build_info().decode()
     keys = dict(kv.split("=") for kv in info.split())
-    assert set(keys) == {"flux_block", "flux_minb", "flux_minb_wide", "flux_minb64", "flux_minb_many", "fp32_packed"}
+    assert set(keys) == {"flux_block", "flux_minb", "flux_minb_wide", "flux_minb64", "flux_minb_many", "fp32_packed",
+                         "tile_flux_pf", "tile_stage_unroll"}
     assert all(v.isdigit() for v in keys.values()) and keys["flux_block"] == "128"
 
 
