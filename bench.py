@@ -395,8 +395,12 @@ def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, *, e2e_steps=N
     U_in = U0.astype(np.float32) if f32 else U0
     ctx.upload_state(U_in)
     dt = 0.4 * ctx.time_step()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        ctx.time_step()
+    cfl_ms = (time.perf_counter() - t0) / 5 * 1e3
     tune = ctx.autotune(dt, steps=3) if autotune and steps > 0 else None
-    out = {"dt": dt, "tuning": tune, "setup_s": setup_s, "tile_staging": ctx.tile_staging()}
+    out = {"dt": dt, "tuning": tune, "setup_s": setup_s, "tile_staging": ctx.tile_staging(), "cfl_ms": cfl_ms}
     if steps > 0:
         ctx.upload_state(U_in)
         for _ in range(warmup):
@@ -684,6 +688,7 @@ def run_gpu(args):
         "clocks": r["clocks"],
         "mood": {"flagged_last_step": cnt["mood_flagged"], "iterations_last_step": cnt["mood_iterations"],
                  "predicted_last_step": cnt.get("predicted", 0)},
+        "cfl_ms_per_call": r["cfl_ms"],
     }
     other = "fp32" if head == "fp32_learned" else ("fp32_learned" if "fp32_learned" in res else None)
     if other:

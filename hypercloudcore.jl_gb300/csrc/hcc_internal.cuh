@@ -29,6 +29,9 @@
 #ifndef HCC_TILE_FLUX_PF
 #define HCC_TILE_FLUX_PF 8         // tile-staged flux pass: union places of a thread's slots fetched this many slots ahead
 #endif
+#ifndef HCC_FLUX_KAHAN_BLOCK
+#define HCC_FLUX_KAHAN_BLOCK 4     // tile-staged flux pass: slot terms summed plainly per block, blocks compensated
+#endif
 #ifndef HCC_TILE_STAGE_UNROLL
 #define HCC_TILE_STAGE_UNROLL 4    // tile passes: union entries a thread stages per round (halved for wide rows)
 #endif

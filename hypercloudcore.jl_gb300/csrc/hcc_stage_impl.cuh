@@ -88,6 +88,38 @@ template <int M> struct AccumV<float, M> {
     }
 };
 
+// Compensated sums of the tile-staged flux pass in blocks: NB slot terms summed plainly, then the block's sum added
+// with compensation (NB = 1: every term compensated, as AccumV). `flush` adds a partial block; `sum` then holds
+// the compensated sums.
+template <int M, int NB> struct BlockAccum {
+    AccumV<float, M> sum;
+    float p[M];
+    int n;
+    __device__ __forceinline__ BlockAccum() : n(0) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) p[m] = 0.0f;
+    }
+    __device__ __forceinline__ void add(const float *t) {
+        if constexpr (NB == 1) {
+            sum.add(t);
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) p[m] = p[m] + t[m];
+            if (++n == NB) flush();
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        if constexpr (NB > 1) {
+            if (n > 0) {
+                sum.add(p);
+#pragma unroll
+                for (int m = 0; m < M; ++m) p[m] = 0.0f;
+                n = 0;
+            }
+        }
+    }
+};
+
 template <typename T> __device__ __forceinline__ T floatmin_of();
 template <> __device__ __forceinline__ double floatmin_of<double>() { return 2.2250738585072014e-308; }
 template <> __device__ __forceinline__ float floatmin_of<float>() { return 1.17549435e-38f; }
@@ -935,10 +967,10 @@ template <typename T, int M> struct FluxPart {
 // oj and the sort orientation `below` are the caller's; the interface reconstructions, the physical fluxes, the
 // Rusanov flux of the pair sorted by the signs of the axis offsets (sort_flux, Utils.jl:95-102; FluxFunctions.jl:66-76)
 // and its flux difference contracted with the slot's divergence weights wk go into acc.
-template <typename T, int D, int M, int PDE, int RDEG, bool ALE, bool MOM>
+template <typename T, int D, int M, int PDE, int RDEG, bool ALE, bool MOM, class Acc>
 __device__ __forceinline__ void flux_slot(const StageArgs<T> &a, const T *fi, const T (*gi)[M], const T (*Fi)[M],
                                           const T *wp, const T *fj, const T *gj, const int oi, const int oj,
-                                          const bool below, const T *dk, const T *wk, AccumV<T, M> &acc,
+                                          const bool below, const T *dk, const T *wk, Acc &acc,
                                           const int64_t i, const int k) {
     constexpr int BR = RBasis<D, RDEG>::B;
     constexpr bool kFast = sizeof(T) == 4;   // FP32: scaled Rusanov form
@@ -1537,6 +1569,35 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
     int4 *spos = reinterpret_cast<int4 *>(sm);
     float *srow = sm + 4 * a.tv.umax;
     FluxPart<float, M> *parts = reinterpret_cast<FluxPart<float, M> *>(srow + a.tv.umax * W);
+    // the particle's own global loads (count, union place, fit rows, the first union places of its slots) are issued
+    // before the staging so that their latency overlaps it; none of them reads shared memory
+    const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
+    const int64_t i = t * HCC_TILE + pl;
+    const bool live = i < a.g.n && !a.g.bnd[i];
+    const int64_t np = a.g.npad;
+    constexpr int PF = HCC_TILE_FLUX_PF;       // this thread's slots h, h + 2, ...: union places PF slots ahead
+    const int64_t lstep = 2 * np;
+    const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+    int cnt = 0, li = 0, mine = 0;
+    bool wok = false;
+    int lb[PF];
+    float A[D], B[D][D];
+    if (live) {
+        cnt = a.g.cnt[i];
+        li = int(a.tv.lself[i]);
+        wok = cnt > 0 && a.g.ok_d[i];
+        const float *cf = a.tv.coef + i * a.tv.cw;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            A[d] = cf[d];
+#pragma unroll
+            for (int e = 0; e < D; ++e) B[d][e] = cf[D + d * D + e];
+        }
+        mine = cnt > h ? (cnt - h + 1) / 2 : 0;
+#pragma unroll
+        for (int q = 0; q < PF; ++q) lb[q] = q < mine ? int(lp[int64_t(q) * lstep]) : 0;
+        lp += int64_t(PF) * lstep;
+    }
     {
         // SU entries per thread and round: their ids first, then every load of the round in flight, then the stores
         constexpr int SU = tile_stage_unroll<RW>();
@@ -1567,17 +1628,12 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
         }
     }
     __syncthreads();
-    const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
-    const int64_t i = t * HCC_TILE + pl;
-    const bool live = i < a.g.n && !a.g.bnd[i];
-    const int64_t np = a.g.npad;
     const bool need_ext = a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2);
-    AccumV<float, M> acc;
+    BlockAccum<M, HCC_FLUX_KAHAN_BLOCK> blk;
+    AccumV<float, M> &acc = blk.sum;
     float mn[M], mx[M], fi[M];
     float gi[D][M], Fi[D][M];
     if (live) {
-        const int cnt = a.g.cnt[i];
-        const int li = int(a.tv.lself[i]);
         const int4 q4 = spos[li];
         const int qi[3] = {q4.x, q4.y, q4.z};
         const int oi_own = q4.w;
@@ -1592,25 +1648,7 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                 for (int m = 0; m < M; ++m) gi[b][m] = own[M + b * M + m];
         }
         own_flux<float, D, M, PDE, false, false>(a.ph, fi, Fi, nullptr);
-        const bool wok = cnt > 0 && a.g.ok_d[i];
-        // this thread's slots h, h + 2, ...: their union places fetched PF slots ahead (a rotating window)
-        constexpr int PF = HCC_TILE_FLUX_PF;
-        const int mine = cnt > h ? (cnt - h + 1) / 2 : 0;
-        const int64_t lstep = 2 * np;
-        const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
-        int lb[PF];
-#pragma unroll
-        for (int q = 0; q < PF; ++q) lb[q] = q < mine ? int(lp[int64_t(q) * lstep]) : 0;
-        lp += int64_t(PF) * lstep;
         if (wok) {
-            const float *cf = a.tv.coef + i * a.tv.cw;
-            float A[D], B[D][D];
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                A[d] = cf[d];
-#pragma unroll
-                for (int e = 0; e < D; ++e) B[d][e] = cf[D + d * D + e];
-            }
             const float qt = a.tv.quantum[t], ws = a.tv.wscale;
             for (int s = 0; s < mine; ++s) {
                 const int k = h + 2 * s;
@@ -1647,8 +1685,9 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                 const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
                                                     oj_own < a.sc.max_order);
                 flux_slot<float, D, M, PDE, 1, false, false>(a, fi, gi, Fi, nullptr, r, r + M, oi, oj, below, dk,
-                                                             wk, acc, i, k);
+                                                             wk, blk, i, k);
             }
+            blk.flush();
         } else if (need_ext) {
             for (int s = 0; s < mine; ++s) {
                 const int l = lb[0];
@@ -2356,6 +2395,129 @@ __global__ void k_cfl(const StageArgs<T> a, unsigned long long *dt_bits) {
     if ((threadIdx.x & 31) == 0 && cl >= 0) atomicMin(dt_bits + cl, b);
 }
 
+// The CFL step of an FP32 context with tile tables (the same formula as k_cfl): per tile of HCC_TILE particles the
+// union's quantised positions and the axis speeds of its states are staged in shared memory, one speed evaluation per
+// union entry instead of one per slot, and each slot reads only its neighbour's union place; the slot offsets and
+// divergence weights are recomputed from the positions and the particle's fit rows as in the tile flux pass. Two
+// threads per particle (alternate slots, the second's partial sum through shared memory), the per-particle loads
+// issued before the staging, every staging load of a thread in flight at once, union places eight slots ahead. One
+// minimum for the whole cloud (batches with a minimum per cloud take k_cfl).
+template <int D, int M, int PDE>
+__global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float> a, unsigned long long *dt_bits) {
+    extern __shared__ __align__(16) float sm[];
+    int4 *spos = reinterpret_cast<int4 *>(sm);
+    float4 *sspd = reinterpret_cast<float4 *>(sm + 4 * a.tv.umax);
+    float *parts = sm + 8 * a.tv.umax;           // [HCC_TILE] partial sums of the second threads
+    const int64_t t = blockIdx.x;
+    const int64_t u0 = a.tv.ustart[t];
+    const int nu = int(a.tv.ustart[t + 1] - u0);
+    const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
+    const int64_t i = t * HCC_TILE + pl;
+    const int64_t np = a.g.npad;
+    constexpr int PF = 8;
+    const int64_t lstep = 2 * np;
+    const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
+    int li = 0, mine = 0;
+    int lb[PF];
+    float A[D], B[D][D];
+    if (i < a.g.n && !a.g.bnd[i]) {
+        const int cnt = a.g.cnt[i];
+        if (cnt > 0 && a.g.ok_d[i]) {
+            li = int(a.tv.lself[i]);
+            const float *cf = a.tv.coef + i * a.tv.cw;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                A[d] = cf[d];
+#pragma unroll
+                for (int e = 0; e < D; ++e) B[d][e] = cf[D + d * D + e];
+            }
+            mine = cnt > h ? (cnt - h + 1) / 2 : 0;
+#pragma unroll
+            for (int q = 0; q < PF; ++q) lb[q] = q < mine ? int(lp[int64_t(q) * lstep]) : 0;
+            lp += int64_t(PF) * lstep;
+        }
+    }
+    {
+        constexpr int SU = 4;
+        const int nt = int(blockDim.x);
+        for (int e0 = threadIdx.x; e0 < nu; e0 += SU * nt) {
+            int32_t jj[SU];
+#pragma unroll
+            for (int u = 0; u < SU; ++u) jj[u] = e0 + u * nt < nu ? a.tv.uid[u0 + e0 + u * nt] : 0;
+            int4 qq[SU];
+            float U[SU][M];
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                qq[u] = a.tv.upos[u0 + e0 + u * nt];
+#pragma unroll
+                for (int m = 0; m < M; ++m) U[u][m] = a.U[int64_t(jj[u]) * M + m];
+            }
+#pragma unroll
+            for (int u = 0; u < SU; ++u) {
+                if (e0 + u * nt >= nu) break;
+                float L[D];
+                speeds<float, D, M, PDE>(a.ph, U[u], L);
+                spos[e0 + u * nt] = qq[u];
+                sspd[e0 + u * nt] = make_float4(L[0], D > 1 ? L[D > 1 ? 1 : 0] : 0.0f,
+                                                D > 2 ? L[D > 2 ? 2 : 0] : 0.0f, 0.0f);
+            }
+        }
+    }
+    __syncthreads();
+    float sum_c = 0.0f;
+    if (mine > 0) {
+        const int4 q4 = spos[li];
+        const int qi[3] = {q4.x, q4.y, q4.z};
+        const float4 l4 = sspd[li];
+        const float Li[3] = {l4.x, l4.y, l4.z};
+        const float qt = a.tv.quantum[t], ws = a.tv.wscale;
+        for (int s = 0; s < mine; ++s) {
+            const int l = lb[0];
+#pragma unroll
+            for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
+            lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
+            lp += lstep;
+            const int4 qj4 = spos[l];
+            const int qj[3] = {qj4.x, qj4.y, qj4.z};
+            const float4 lj4 = sspd[l];
+            const float Lj[3] = {lj4.x, lj4.y, lj4.z};
+            float dk[D];
+            tile_offset<D>(qj, qi, qt, dk);
+            float r2 = dk[0] * dk[0];
+#pragma unroll
+            for (int d = 1; d < D; ++d) r2 = r2 + dk[d] * dk[d];
+            const float w = tile_weight(r2, ws);
+            float dot = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                float v = A[d];
+#pragma unroll
+                for (int e = 0; e < D; ++e) v = v + B[d][e] * dk[e];
+                const float pr = fabsf(w * v) * jmax(Li[d], Lj[d]);
+                dot = (d == 0) ? pr : dot + pr;
+            }
+            sum_c = sum_c + dot;
+        }
+    }
+    if (h == 1) parts[pl] = sum_c;
+    __syncthreads();
+    if (h == 1) return;
+    double dti = INFINITY;
+    if (i < a.g.n && !a.g.bnd[i]) {
+        sum_c = sum_c + parts[pl];
+        if (sum_c > floatmin_of<float>()) dti = double((1.0f / float(D)) / sum_c);
+    }
+    // positive doubles order like their bit patterns
+    unsigned long long b = __double_as_longlong(dti);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_down_sync(0xffffffffu, b, o);
+        b = ob < b ? ob : b;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMin(dt_bits, b);
+}
+
 // ----------------------------------------------------------------------------------- launchers / registry
 template <typename T, int D, int M, int PDE, int RDEG>
 struct StageInst {
@@ -2439,7 +2601,21 @@ struct StageInst {
         k_stage1<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args));
     }
     static void cfl(const void *args, int64_t n, unsigned long long *dt_bits, cudaStream_t s) {
-        k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(*static_cast<const StageArgs<T> *>(args), dt_bits);
+        const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        if constexpr (sizeof(T) == 4 && RDEG == 1) {
+            if (a.tile && !a.cloud_id) {   // FP32 with tile tables: the union's speeds staged in shared memory
+                const size_t smem = (size_t(a.tv.umax) * 8 + HCC_TILE) * sizeof(float);
+                static bool attr = false;
+                if (!attr) {
+                    cudaFuncSetAttribute(k_cfl_tile<D, M, PDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tile_smem_optin());
+                    attr = true;
+                }
+                k_cfl_tile<D, M, PDE><<<unsigned(a.tv.ntiles), 2 * HCC_TILE, smem, s>>>(a, dt_bits);
+                return;
+            }
+        }
+        k_cfl<T, D, M, PDE, RDEG><<<grid(n, 256), 256, 0, s>>>(a, dt_bits);
     }
     static void weno(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);

@@ -161,3 +161,31 @@ def test_tile_staging_only_where_it_applies(hcc, cuda_lib):
     assert gm.tile_staging()["active"]
     gm.set_mover(hcc.mover("lagrangian"))
     assert not gm.tile_staging()["active"]
+
+
+@pytest.mark.parametrize("kind,h", [("euler2d", 0.01), ("euler3d", 1.0 / 24), ("bgk", 0.02)])
+def test_tile_cfl_matches_stream_cfl_and_oracle(hcc, oracle, cuda_lib, kind, h):
+    """The tile-staged CFL step (speeds per union entry, weights from the fit rows) against the stream-fed FP32 one
+    and the FP64 oracle's: the same formula on FP32 weights rounded by two routes, within 1e-5 relative."""
+    abi = sys.modules["hcc_gb300._abi"]
+    cloud, cfg, U0 = _system(hcc, kind, h)
+    t = _ctx(hcc, cfg("fp32"), cloud, U0, tiles=True)
+    s = _ctx(hcc, cfg("fp32"), cloud, U0, tiles=False)
+    assert t.tile_staging()["active"]
+    o = oracle.OracleContext(cfg("fp64"), abi)
+    o.upload_cloud(cloud)
+    o.build_neighbours()
+    o.prepare_geometry()
+    o.upload_state(U0)
+    dt_t, dt_s, dt_o = t.time_step(), s.time_step(), o.time_step()
+    assert np.isfinite(dt_t) and dt_t > 0
+    assert abs(dt_t - dt_s) <= 1e-5 * dt_s, (dt_t, dt_s)
+    assert abs(dt_t - dt_o) <= 1e-5 * dt_o, (dt_t, dt_o)
+    dt = 0.4 * dt_o                                           # after steps (new states, lowered orders)
+    for k in range(2):
+        for c in (t, s, o):
+            c.step(k * dt, dt)
+    dt_t, dt_s, dt_o = t.time_step(), s.time_step(), o.time_step()
+    assert abs(dt_t - dt_s) <= 1e-5 * dt_s and abs(dt_t - dt_o) <= 1e-5 * dt_o, (dt_t, dt_s, dt_o)
+    for c in (t, s, o):
+        c.close()
