@@ -631,7 +631,10 @@ int enqueue_drop(hcc_ctx *c, void *Y, cudaStream_t st, const cudaGraphConditiona
     d.bsrc = c->bsrc;
     d.nb = c->nbnd;
     d.M = c->M;
-    d.bc_blocks = c->nbnd > 0 ? int(std::min<int64_t>((c->nbnd + HCC_BLOCK - 1) / HCC_BLOCK, 64)) : 0;
+    // boundary conditions of the candidate: up to eight blocks per SM (a few boundary particles a thread; every
+    // copy is a dependent load chain, so the pass is latency-bound and wants the whole GPU)
+    d.bc_blocks = c->nbnd > 0 ? int(std::min<int64_t>((c->nbnd + HCC_BLOCK - 1) / HCC_BLOCK,
+                                                      int64_t(8) * std::max(1, c->sms))) : 0;
     d.orders = c->orders;
     d.trig_step = c->trig_step;
     d.ttiles = c->ttiles;
