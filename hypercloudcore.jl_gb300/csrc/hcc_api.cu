@@ -193,6 +193,7 @@ struct hcc_ctx {
     int has_source = 0;
     // cloud
     double *pos = nullptr; uint8_t *bnd = nullptr; int32_t *tags = nullptr; double *vol = nullptr;
+    float *pos32 = nullptr; unsigned int *pmax32 = nullptr;   // FP32 positions of the search prefilter
     std::vector<uint8_t> h_bnd; std::vector<int32_t> h_tags;
     // cell list
     int dims[3] = {1, 1, 1}; double csize[3] = {1, 1, 1};
@@ -342,6 +343,7 @@ struct hcc_ctx {
         tiles.release();
         free_mover_buffers();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
+        dfree(pos32); dfree(pmax32);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
         for (void **p : {&rhos, &cand, &grad, &xfer}) { if (*p) cudaFree(*p); *p = nullptr; }
@@ -1240,6 +1242,8 @@ hcc_status hcc_upload_cloud(hcc_ctx *c, int64_t n, const double *pos, const uint
     hcc_status st;
 #define HCC_TRY(x) do { if ((st = (x)) != HCC_OK) return st; } while (0)
     HCC_TRY(c->alloc(c->pos, size_t(D) * np, "positions"));
+    HCC_TRY(c->alloc(c->pos32, size_t(D) * np, "FP32 positions"));
+    HCC_TRY(c->alloc(c->pmax32, 1, "largest coordinate"));
     HCC_TRY(c->alloc(c->bnd, np, "is_boundary"));
     HCC_TRY(c->alloc(c->tags, np, "tags"));
     HCC_TRY(c->alloc(c->vol, np, "volumes"));
@@ -1367,6 +1371,14 @@ hcc_status hcc_build_neighbours(hcc_ctx *c) {
     a.R_sq = R * R;
     a.alpha = f.weight_alpha;
     a.invR2 = 1.0 / (R * R);
+    a.pos32 = c->pos32;
+    a.pmax = c->pmax32;
+    a.Lmax = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        a.L32[d] = float(a.Lwrap[d]);
+        a.invL32[d] = float(a.invLwrap[d]);
+        a.Lmax = std::max(a.Lmax, a.Lwrap[d]);
+    }
     if ((st = search_bins(a, c->stream, c->err)) != HCC_OK) return st;
     if ((st = search_count(a, c->stream, c->d_counters + 3, c->err)) != HCC_OK) return st;
     HCC_TRY(c->cuda(cudaMemcpyAsync(c->h_counters + 3, c->d_counters + 3, 2 * sizeof(unsigned long long),

@@ -402,6 +402,12 @@ struct SearchArgs {
     int32_t *cellp;                   // [n]
     int32_t *cnt;                     // [n]
     double R_sq, alpha, invR2;
+    // exact FP32 prefilter of the r^2 test (nullptr: FP64 only): an FP32 copy of the positions, the largest
+    // |coordinate| (float bits, written by the bin pass), the wrap lengths in FP32 and the largest wrap length
+    float *pos32;
+    unsigned int *pmax;
+    float L32[3], invL32[3];
+    double Lmax;
     // output (slot-major)
     int32_t *nidx;
     double *w;

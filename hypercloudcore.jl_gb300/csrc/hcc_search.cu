@@ -115,6 +115,66 @@ __device__ __forceinline__ double pair_distance(const SearchArgs &a, int64_t i, 
     return s;
 }
 
+// FP32 copy of the positions and the largest |coordinate| over the cloud (non-negative floats order like their
+// bits), for the prefilter of the count and write passes.
+__global__ void k_prep32(SearchArgs a) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    float m = 0.0f;
+    if (i < a.n) {
+        for (int d = 0; d < a.D; ++d) {
+            const float f = float(a.pos[d * a.npad + i]);
+            a.pos32[d * a.npad + i] = f;
+            m = fmaxf(m, fabsf(f));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(a.pmax, __float_as_uint(m));
+}
+
+// Exact FP32 prefilter of the test r^2 <= R^2. With u = 2^-24, P the largest |coordinate| and L the largest wrap
+// length, each FP32 axis offset (positions rounded to FP32, the same wrap integer as the FP64 path) lies within
+// Delta = 16 u (P + L) of the FP64 one, and the FP32 sum of squares s within rho s (s >= R^2) or rho R^2 (s < R^2) of
+// the FP64 r^2, rho = 2 (2 sqrt(D) Delta / R + 3 D Delta^2 / R^2 + D u) (a factor 2 of margin). So s < R^2 (1 - rho)
+// proves the pair inside and s > R^2 / (1 - rho) outside; the band between, a wrap quotient within 0.01 of a half
+// integer (where the FP32 and FP64 wrap integers may differ), a NaN or rho >= 0.05 leave the decision to FP64.
+// The lists, their order, weights and distances are therefore those of the FP64 test, bit for bit.
+template <int D> struct Prefilter {
+    bool on;
+    float lo, hi, pi[3];
+    __device__ __forceinline__ Prefilter(const SearchArgs &a, int64_t i) : on(false), lo(0.0f), hi(0.0f) {
+        pi[0] = pi[1] = pi[2] = 0.0f;
+        if (!a.pos32) return;
+        const double u = 5.9604644775390625e-08;
+        const double P = double(__uint_as_float(*a.pmax));
+        const double delta = 16.0 * u * (P + a.Lmax);
+        const double R = sqrt(a.R_sq);
+        const double rho = 2.0 * (2.0 * sqrt(double(D)) * delta / R + 3.0 * D * delta * delta / a.R_sq + D * u);
+        if (!(rho < 0.05)) return;
+        on = true;
+        lo = __double2float_rd(a.R_sq * (1.0 - rho));
+        hi = __double2float_ru(a.R_sq / (1.0 - rho));
+#pragma unroll
+        for (int d = 0; d < D; ++d) pi[d] = a.pos32[d * a.npad + i];
+    }
+    // +1: inside, -1: outside, 0: undecided (the FP64 test decides)
+    __device__ __forceinline__ int decide(const SearchArgs &a, int64_t j) const {
+        float s = 0.0f;
+        bool amb = false;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const float dx = __fsub_rn(a.pos32[d * a.npad + j], pi[d]);
+            const float q = __fmul_rn(dx, a.invL32[d]);
+            const float r = rintf(q);
+            amb = amb || fabsf(__fsub_rn(fabsf(__fsub_rn(q, r)), 0.5f)) < 0.01f;
+            const float dd = __fsub_rn(dx, __fmul_rn(a.L32[d], r));
+            s = (d == 0) ? __fmul_rn(dd, dd) : __fadd_rn(s, __fmul_rn(dd, dd));
+        }
+        if (amb) return 0;
+        return s < lo ? 1 : (s > hi ? -1 : 0);
+    }
+};
+
 // _count_neighbours! (NeighborLogic.jl:288-301); stats: [0] max count, [1] total, [2] min interior count
 template <int D>
 __global__ void k_count(SearchArgs a, unsigned long long *stats) {
@@ -122,12 +182,15 @@ __global__ void k_count(SearchArgs a, unsigned long long *stats) {
     int32_t c = 0;
     if (i < a.n) {
         const int64_t *win = a.binnb + int64_t(a.bin_of[i]) * a.noff;
+        const Prefilter<D> pf(a, i);
         double dist[3];
         for (int w = 0; w < a.noff; ++w) {
             int64_t b = win[w];
             for (int64_t s = a.cell_start[b]; s < a.cell_start[b + 1]; ++s) {
                 int32_t j = a.cellp[s];
-                if (j != i && pair_distance<D>(a, i, j, dist) <= a.R_sq) ++c;
+                if (j == i) continue;
+                const int dec = pf.on ? pf.decide(a, j) : 0;
+                if (dec > 0 || (dec == 0 && pair_distance<D>(a, i, j, dist) <= a.R_sq)) ++c;
             }
         }
         a.cnt[i] = c;
@@ -156,14 +219,42 @@ __device__ __forceinline__ double exp_weight(double d2, double alpha, double inv
     return 1.0 / den;
 }
 
-// _write_neighbours! (NeighborLogic.jl:309-329) into the slot-major layout
+// _write_neighbours! (NeighborLogic.jl:309-329) into the slot-major layout. With the FP32 prefilter in two phases:
+// the candidates in window order, decided in FP32 (FP64 only in the undecided band), give the slot indices; then
+// every lane computes the FP64 distances and weights of its own slots with the warp converged (a warp instruction
+// costs the FP64 unit the same with one lane or 32, and about one candidate in six is accepted). The values and
+// their order are those of the one-phase FP64 loop.
 template <int D>
 __global__ void k_write(SearchArgs a) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const int64_t *win = a.binnb + int64_t(a.bin_of[i]) * a.noff;
+    const Prefilter<D> pf(a, i);
     double dist[3];
     int k = 0;
+    if (pf.on) {
+        for (int w = 0; w < a.noff; ++w) {
+            int64_t b = win[w];
+            for (int64_t s = a.cell_start[b]; s < a.cell_start[b + 1]; ++s) {
+                int32_t j = a.cellp[s];
+                if (j == i) continue;
+                const int dec = pf.decide(a, j);
+                if (dec > 0 || (dec == 0 && pair_distance<D>(a, i, j, dist) <= a.R_sq)) {
+                    if (k < a.kmax) a.nidx[int64_t(k) * a.npad + i] = j;
+                    ++k;
+                }
+            }
+        }
+        const int nk = k < a.kmax ? k : a.kmax;
+        for (int q = 0; q < nk; ++q) {
+            const int64_t slot = int64_t(q) * a.npad + i;
+            const double d2 = pair_distance<D>(a, i, a.nidx[slot], dist);
+            a.w[slot] = exp_weight(d2, a.alpha, a.invR2);
+#pragma unroll
+            for (int d = 0; d < D; ++d) a.dist[(int64_t(q) * D + d) * a.npad + i] = dist[d];
+        }
+        return;
+    }
     for (int w = 0; w < a.noff; ++w) {
         int64_t b = win[w];
         for (int64_t s = a.cell_start[b]; s < a.cell_start[b + 1]; ++s) {
@@ -219,6 +310,10 @@ hcc_status search_bins(SearchArgs &a, cudaStream_t s, std::string &err) {
     cudaMemsetAsync(a.cell_count, 0, sizeof(int32_t) * (a.nbins + 1), s);
     cudaMemsetAsync(a.cell_cursor, 0, sizeof(int32_t) * a.nbins, s);
     k_bin<<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a);
+    if (a.pos32) {
+        cudaMemsetAsync(a.pmax, 0, sizeof(unsigned int), s);
+        k_prep32<<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a);
+    }
     k_scan_bins<<<1, 1024, 0, s>>>(a.cell_count, a.cell_start, a.nbins, a.n);
     k_scatter<<<grid_for(a.n), HCC_BLOCK, 0, s>>>(a);
     k_binsort<<<grid_for(a.nbins), HCC_BLOCK, 0, s>>>(a);
