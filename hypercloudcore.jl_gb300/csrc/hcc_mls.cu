@@ -174,12 +174,10 @@ __device__ void assemble(const MlsArgs &a, int64_t i, int cnt, int q, bool inter
         for (int c = 0; c < r; ++c) N[r * B + c] = N[c * B + r];
 }
 
-// Inverse moment matrix (C \ e_j per column), padded into a Bpad×Bpad block.
+// Inverse (C \ e_j per column) of an assembled B×B moment matrix N (overwritten), padded into a Bpad×Bpad block.
 template <int BM>
-__device__ bool inverse_moment(const MlsArgs &a, int64_t i, int cnt, int q, bool intercept, int Bpad, double *out) {
-    const int B = c_tabs[a.D][q].B + (intercept ? 1 : 0);
-    double N[BM * BM], U[BM * BM];
-    assemble<BM>(a, i, cnt, q, intercept, B, N);
+__device__ bool invert_assembled(int B, double *N, int Bpad, double *out) {
+    double U[BM * BM];
     for (int k = 0; k < Bpad * Bpad; ++k) out[k] = 0.0;
     if (!cholesky_moment(B, N, U)) return false;
     double e[BM], x[BM];
@@ -189,6 +187,15 @@ __device__ bool inverse_moment(const MlsArgs &a, int64_t i, int cnt, int q, bool
         for (int r = 0; r < B; ++r) out[r * Bpad + j] = x[r];
     }
     return true;
+}
+
+// Inverse moment matrix of the fit of degree q, padded into a Bpad×Bpad block.
+template <int BM>
+__device__ bool inverse_moment(const MlsArgs &a, int64_t i, int cnt, int q, bool intercept, int Bpad, double *out) {
+    const int B = c_tabs[a.D][q].B + (intercept ? 1 : 0);
+    double N[BM * BM];
+    assemble<BM>(a, i, cnt, q, intercept, B, N);
+    return invert_assembled<BM>(B, N, Bpad, out);
 }
 
 // One instantiation per basis capacity BM (4: degree-1 fits in 3-D; 10: degree 3 in 2-D; 20: degree 3 in 3-D),
@@ -221,13 +228,27 @@ __global__ void k_mls(MlsArgs a) {
         }
         return;
     }
-    // reconstruction fit (every particle, MLSWeights without intercept)
-    bool okr = inverse_moment<BM>(a, i, cnt, a.rdeg, false, a.Br, inv);
-    for (int k = 0; k < a.Br * a.Br; ++k) a.inv_r[i * a.Br * a.Br + k] = inv[k];
+    // reconstruction fit (every particle, MLSWeights without intercept) and the divergence fit of the degree the
+    // stencil carries at full order (padded to Bd). Where the two degrees agree, the reconstruction moments are the
+    // divergence moments without the intercept row and column -- the same products w (p_r p_c) summed in the same
+    // order, bit for bit -- so one assembly serves both.
+    const int q = divergence_index(a.DO, a.D, a.max_order, cnt) - 1;
+    bool okr, okd;
+    if (q == a.rdeg) {
+        const int Bq = c_tabs[a.D][q].B, B1 = Bq + 1;
+        double Nd[BM * BM], Nr[BM * BM];
+        assemble<BM>(a, i, cnt, q, true, B1, Nd);
+        for (int r = 0; r < Bq; ++r)
+            for (int c = 0; c < Bq; ++c) Nr[r * Bq + c] = Nd[(r + 1) * B1 + (c + 1)];
+        okr = invert_assembled<BM>(Bq, Nr, a.Br, inv);
+        for (int k = 0; k < a.Br * a.Br; ++k) a.inv_r[i * a.Br * a.Br + k] = inv[k];
+        okd = invert_assembled<BM>(B1, Nd, a.Bd, inv);
+    } else {
+        okr = inverse_moment<BM>(a, i, cnt, a.rdeg, false, a.Br, inv);
+        for (int k = 0; k < a.Br * a.Br; ++k) a.inv_r[i * a.Br * a.Br + k] = inv[k];
+        okd = inverse_moment<BM>(a, i, cnt, q, true, a.Bd, inv);
+    }
     a.ok_r[i] = okr;
-    // divergence fit of the degree the stencil carries at full order, padded to Bd
-    int q = divergence_index(a.DO, a.D, a.max_order, cnt) - 1;
-    bool okd = inverse_moment<BM>(a, i, cnt, q, true, a.Bd, inv);
     for (int k = 0; k < a.Bd * a.Bd; ++k) a.inv_d[i * a.Bd * a.Bd + k] = inv[k];
     a.ok_d[i] = okd;
     double x[3], p[BM], v[BM];
