@@ -57,6 +57,19 @@ def test_neighbour_lists_bit_exact(hcc, oracle, cuda_lib, D, periodic):
     assert _bits_equal(dwg, dwo)
 
 
+@pytest.mark.parametrize("D,box", [(3, 1.0), (2, 0.12), (3, 0.3)])
+def test_periodic_neighbour_lists_bit_exact(hcc, oracle, cuda_lib, D, box):
+    """Periodic clouds through the search's FP32 prefilter: a 3-D unit box, and boxes only a few support radii wide
+    (pairs about half a period apart, where the FP32 wrap quotient is near a half integer and FP64 decides)."""
+    h = 0.05 if D == 3 and box == 1.0 else 0.02
+    cloud = hcc.rectangular_cloud((0.0,) * D, (box,) * D, h, 2.5 * h, periodic=True, jitter=0.25 * h, seed=11)
+    pde = hcc.LinearAdvection(tuple((1.0,) for _ in range(D)))
+    cfg = hcc.make_config(pde, cloud, scheme=hcc.MUSCL(2, 2))
+    g, o = _pair(hcc, oracle, cfg, cloud)
+    counts, idx = _assert_same_lists(g, o)
+    assert counts.sum() > 0 and idx.min() >= 0
+
+
 def test_advection_rhs_and_steps_bit_exact(hcc, oracle, cuda_lib):
     cloud = c1_cloud(hcc)
     pde = hcc.LinearAdvection(((1.0,), (1.0,)))
