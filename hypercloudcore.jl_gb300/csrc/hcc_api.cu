@@ -1893,7 +1893,8 @@ const char *hcc_build_info(void) {
            " flux_minb_wide=" HCC_STR(HCC_FLUX_MINB_WIDE) " flux_minb64=" HCC_STR(HCC_FLUX_MINB64)
            " flux_minb_many=" HCC_STR(HCC_FLUX_MINB_MANY) " fp32_packed=" HCC_STR(HCC_FP32_PACKED)
            " tile_flux_pf=" HCC_STR(HCC_TILE_FLUX_PF) " tile_stage_unroll=" HCC_STR(HCC_TILE_STAGE_UNROLL)
-           " flux_kahan_block=" HCC_STR(HCC_FLUX_KAHAN_BLOCK);
+           " flux_kahan_block=" HCC_STR(HCC_FLUX_KAHAN_BLOCK)
+           " tile_flux_group=" HCC_STR(HCC_TILE_FLUX_GROUP) " tile_gather_group=" HCC_STR(HCC_TILE_GATHER_GROUP);
 }
 
 hcc_status hcc_fp64_fma_rate(double *tflops_out) {

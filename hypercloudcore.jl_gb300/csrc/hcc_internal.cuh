@@ -29,6 +29,13 @@
 #ifndef HCC_TILE_FLUX_PF
 #define HCC_TILE_FLUX_PF 8         // tile-staged flux pass: union places of a thread's slots fetched this many slots ahead
 #endif
+#ifndef HCC_TILE_FLUX_GROUP
+#define HCC_TILE_FLUX_GROUP 2      // tile-staged flux pass: union places in groups of this size, the slot body unrolled
+                                   // over a group (0: a rotating window of HCC_TILE_FLUX_PF places)
+#endif
+#ifndef HCC_TILE_GATHER_GROUP
+#define HCC_TILE_GATHER_GROUP 8    // tile-staged gather pass: union places in groups of this size, the slot body unrolled
+#endif
 #ifndef HCC_FLUX_KAHAN_BLOCK
 #define HCC_FLUX_KAHAN_BLOCK 4     // tile-staged flux pass: slot terms summed plainly per block, blocks compensated
 #endif

@@ -1492,7 +1492,7 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_gather_min_blocks<D, M>()) 
         const float qt = a.tv.quantum[t], ws = a.tv.wscale;
         // this thread's slots h, h + 2, ...: their union places in groups of PF, the next group's loads in flight
         // while this group is summed
-        constexpr int PF = 8;
+        constexpr int PF = HCC_TILE_GATHER_GROUP;
         const int mine = cnt > h ? (cnt - h + 1) / 2 : 0;
         const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
         const int64_t step = 2 * np;
@@ -1575,7 +1575,11 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
     const int64_t i = t * HCC_TILE + pl;
     const bool live = i < a.g.n && !a.g.bnd[i];
     const int64_t np = a.g.npad;
-    constexpr int PF = HCC_TILE_FLUX_PF;       // this thread's slots h, h + 2, ...: union places PF slots ahead
+    // this thread's slots h, h + 2, ...: union places PF slots ahead (a rotating window), or in groups of PF with the
+    // next group in flight (HCC_TILE_FLUX_GROUP > 0: the slot body unrolled over the group)
+    // (wide states, M >= 8, keep the window: the unrolled group spills their registers)
+    constexpr int GROUP = M >= 8 ? 0 : HCC_TILE_FLUX_GROUP;
+    constexpr int PF = GROUP > 0 ? GROUP : HCC_TILE_FLUX_PF;
     const int64_t lstep = 2 * np;
     const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
     int cnt = 0, li = 0, mine = 0;
@@ -1650,13 +1654,7 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
         own_flux<float, D, M, PDE, false, false>(a.ph, fi, Fi, nullptr);
         if (wok) {
             const float qt = a.tv.quantum[t], ws = a.tv.wscale;
-            for (int s = 0; s < mine; ++s) {
-                const int k = h + 2 * s;
-                const int l = lb[0];
-#pragma unroll
-                for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
-                lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
-                lp += lstep;
+            auto slot = [&](const int l, const int k) {
                 const int4 qj4 = spos[l];
                 const int qj[3] = {qj4.x, qj4.y, qj4.z};
                 float dk[D], wk[D];
@@ -1686,6 +1684,30 @@ __global__ void __launch_bounds__(2 * HCC_TILE, tile_flux_min_blocks<D, M>()) k_
                                                     oj_own < a.sc.max_order);
                 flux_slot<float, D, M, PDE, 1, false, false>(a, fi, gi, Fi, nullptr, r, r + M, oi, oj, below, dk,
                                                              wk, blk, i, k);
+            };
+            if constexpr (GROUP > 0) {
+                for (int s0 = 0; s0 < mine; s0 += PF) {
+                    int ln[PF];
+#pragma unroll
+                    for (int q = 0; q < PF; ++q) ln[q] = s0 + PF + q < mine ? int(lp[int64_t(q) * lstep]) : 0;
+                    lp += int64_t(PF) * lstep;
+#pragma unroll
+                    for (int q = 0; q < PF; ++q) {
+                        if (s0 + q >= mine) break;
+                        slot(lb[q], h + 2 * (s0 + q));
+                    }
+#pragma unroll
+                    for (int q = 0; q < PF; ++q) lb[q] = ln[q];
+                }
+            } else {
+                for (int s = 0; s < mine; ++s) {
+                    const int l = lb[0];
+#pragma unroll
+                    for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
+                    lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
+                    lp += lstep;
+                    slot(l, h + 2 * s);
+                }
             }
             blk.flush();
         } else if (need_ext) {

@@ -470,7 +470,7 @@ hcc_status hcc_autotune(hcc_ctx *ctx, double dt, int32_t steps, hcc_tune_report 
 
 /* The compile-time launch bounds and variant switches the library was built with, e.g. "flux_block=128
    flux_minb=7 flux_minb_wide=4 flux_minb64=3 flux_minb_many=2 fp32_packed=0 tile_flux_pf=8 tile_stage_unroll=4
-   flux_kahan_block=4" (static string; no GPU
+   flux_kahan_block=4 tile_flux_group=2 tile_gather_group=8" (static string; no GPU
    needed). Tells apart variant builds loaded side by side. */
 const char *hcc_build_info(void);
 

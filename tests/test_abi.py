@@ -109,7 +109,8 @@ def test_build_info_names_the_launch_bounds(cuda_lib):
     info = cuda_lib.hcc_build_info().decode()
     keys = dict(kv.split("=") for kv in info.split())
     assert set(keys) == {"flux_block", "flux_minb", "flux_minb_wide", "flux_minb64", "flux_minb_many", "fp32_packed",
-                         "tile_flux_pf", "tile_stage_unroll", "flux_kahan_block"}
+                         "tile_flux_pf", "tile_stage_unroll", "flux_kahan_block",
+                         "tile_flux_group", "tile_gather_group"}
     assert all(v.isdigit() for v in keys.values()) and keys["flux_block"] == "128"
 
 
