@@ -2422,7 +2422,7 @@ __global__ void k_cfl(const StageArgs<T> a, unsigned long long *dt_bits) {
 // union entry instead of one per slot, and each slot reads only its neighbour's union place; the slot offsets and
 // divergence weights are recomputed from the positions and the particle's fit rows as in the tile flux pass. Two
 // threads per particle (alternate slots, the second's partial sum through shared memory), the per-particle loads
-// issued before the staging, every staging load of a thread in flight at once, union places eight slots ahead. One
+// issued before the staging, every staging load of a thread in flight at once, union places in groups of four. One
 // minimum for the whole cloud (batches with a minimum per cloud take k_cfl).
 template <int D, int M, int PDE>
 __global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float> a, unsigned long long *dt_bits) {
@@ -2436,7 +2436,7 @@ __global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float
     const int pl = int(threadIdx.x) % HCC_TILE, h = int(threadIdx.x) / HCC_TILE;
     const int64_t i = t * HCC_TILE + pl;
     const int64_t np = a.g.npad;
-    constexpr int PF = 8;
+    constexpr int PF = 4;
     const int64_t lstep = 2 * np;
     const uint16_t *lp = a.tv.lidx + int64_t(h) * np + i;
     int li = 0, mine = 0;
@@ -2494,12 +2494,7 @@ __global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float
         const float4 l4 = sspd[li];
         const float Li[3] = {l4.x, l4.y, l4.z};
         const float qt = a.tv.quantum[t], ws = a.tv.wscale;
-        for (int s = 0; s < mine; ++s) {
-            const int l = lb[0];
-#pragma unroll
-            for (int q = 0; q + 1 < PF; ++q) lb[q] = lb[q + 1];
-            lb[PF - 1] = s + PF < mine ? int(*lp) : 0;
-            lp += lstep;
+        auto slot = [&](const int l) {
             const int4 qj4 = spos[l];
             const int qj[3] = {qj4.x, qj4.y, qj4.z};
             const float4 lj4 = sspd[l];
@@ -2520,6 +2515,20 @@ __global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float
                 dot = (d == 0) ? pr : dot + pr;
             }
             sum_c = sum_c + dot;
+        };
+        // groups of PF union places, the next group in flight while this one is summed (the slot body unrolled)
+        for (int s0 = 0; s0 < mine; s0 += PF) {
+            int ln[PF];
+#pragma unroll
+            for (int q = 0; q < PF; ++q) ln[q] = s0 + PF + q < mine ? int(lp[int64_t(q) * lstep]) : 0;
+            lp += int64_t(PF) * lstep;
+#pragma unroll
+            for (int q = 0; q < PF; ++q) {
+                if (s0 + q >= mine) break;
+                slot(lb[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < PF; ++q) lb[q] = ln[q];
         }
     }
     if (h == 1) parts[pl] = sum_c;
