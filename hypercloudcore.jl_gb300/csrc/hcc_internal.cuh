@@ -33,6 +33,9 @@
 #define HCC_TILE_FLUX_GROUP 2      // tile-staged flux pass: union places in groups of this size, the slot body unrolled
                                    // over a group (0: a rotating window of HCC_TILE_FLUX_PF places)
 #endif
+#ifndef HCC_FLUX_STREAM_GROUP
+#define HCC_FLUX_STREAM_GROUP 1    // stream-fed FP32 full flux pass: slots in groups of this size, the body unrolled
+#endif
 #ifndef HCC_TILE_GATHER_GROUP
 #define HCC_TILE_GATHER_GROUP 8    // tile-staged gather pass: union places in groups of this size, the slot body unrolled
 #endif

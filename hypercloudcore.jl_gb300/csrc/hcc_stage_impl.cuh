@@ -1193,7 +1193,69 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
 #pragma unroll
     for (int m = 0; m < M; ++m) { mn[m] = fi[m]; mx[m] = fi[m]; }
 
-    if (wok && k0 < cnt) {
+    // one slot: its neighbour's state, gradient and order, the interface orders, the flux
+    auto slot = [&](const int32_t j, const T *dk, const T *wk, const int k) {
+        T fj[M];
+        load_vec<T, M>(a.U + int64_t(j) * M, fj);
+        T gj[BR * M];
+        load_vec<T, BR * M>(a.grad + int64_t(j) * (BR * M), gj);
+        if (need_ext) {
+#pragma unroll
+            for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], fj[m]); mx[m] = vmax(mx[m], fj[m]); }
+        }
+        const int oj_own = a.orders[j];
+        int oi, oj;
+        if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
+        else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
+        else { oi = oi_own; oj = oj_own; }
+        // AlignedRusanovFlux (MUSCL.jl:331-338): where either particle is below the full order (every pair at
+        // order 1) the states are sorted by the signs of the slot's divergence weights instead of the distance
+        const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
+                                            oj_own < a.sc.max_order);
+        flux_slot<T, D, M, PDE, RDEG, ALE, MOM>(a, fi, gi, Fi, wp, fj, gj, oi, oj, below, dk, wk, acc, i, k);
+    };
+    // FP32 full passes: the slots in groups of UF, the next group's slot data in flight while this group is
+    // computed (the slot body unrolled over the group); otherwise a one-deep software pipeline
+    constexpr int UF = (kFast && KSTEP == 1) ? HCC_FLUX_STREAM_GROUP : 1;
+    if (UF > 1 && wok && k0 < cnt) {
+        int32_t jb[UF];
+        T dkb[UF][D], wkb[UF][D];
+#pragma unroll
+        for (int u = 0; u < UF; ++u) {
+            const int ku = k0 + u;
+            jb[u] = ku < cnt ? a.g.nidx[int64_t(ku) * np + i] : 0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                dkb[u][d] = ku < cnt ? a.g.dist[(int64_t(ku) * D + d) * np + i] : T(0);
+                wkb[u][d] = ku < cnt ? wsl[(int64_t(ku) * D + d) * np + i] : T(0);
+            }
+        }
+        for (int k = k0; k < cnt; k += UF) {
+            int32_t jn[UF];
+            T dkn[UF][D], wkn[UF][D];
+#pragma unroll
+            for (int u = 0; u < UF; ++u) {
+                const int kn = k + UF + u;
+                jn[u] = kn < cnt ? a.g.nidx[int64_t(kn) * np + i] : 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    dkn[u][d] = kn < cnt ? a.g.dist[(int64_t(kn) * D + d) * np + i] : T(0);
+                    wkn[u][d] = kn < cnt ? wsl[(int64_t(kn) * D + d) * np + i] : T(0);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < UF; ++u) {
+                if (k + u >= cnt) break;
+                slot(jb[u], dkb[u], wkb[u], k + u);
+            }
+#pragma unroll
+            for (int u = 0; u < UF; ++u) {
+                jb[u] = jn[u];
+#pragma unroll
+                for (int d = 0; d < D; ++d) { dkb[u][d] = dkn[u][d]; wkb[u][d] = wkn[u][d]; }
+            }
+        }
+    } else if (wok && k0 < cnt) {
         // slot data of the next slot are loaded while this one is computed (one-deep software pipeline)
         int32_t jn = a.g.nidx[int64_t(k0) * np + i];
         T dkn[D], wkn[D];
@@ -1215,24 +1277,7 @@ __device__ __forceinline__ bool flux_one(const StageArgs<T> &a, const int64_t i,
                     wkn[d] = wsl[(int64_t(k + KSTEP) * D + d) * np + i];
                 }
             }
-            T fj[M];
-            load_vec<T, M>(a.U + int64_t(j) * M, fj);
-            T gj[BR * M];
-            load_vec<T, BR * M>(a.grad + int64_t(j) * (BR * M), gj);
-            if (need_ext) {
-#pragma unroll
-                for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], fj[m]); mx[m] = vmax(mx[m], fj[m]); }
-            }
-            const int oj_own = a.orders[j];
-            int oi, oj;
-            if (a.sc.strategy == HCC_EPD1) { oi = oj = (oi_own < oj_own ? oi_own : oj_own); }
-            else if (a.sc.strategy == HCC_EPD2) { int nj = a.nbmin[j]; oi = oj = (nbmin_i < nj ? nbmin_i : nj); }
-            else { oi = oi_own; oj = oj_own; }
-            // AlignedRusanovFlux (MUSCL.jl:331-338): where either particle is below the full order (every pair at
-            // order 1) the states are sorted by the signs of the slot's divergence weights instead of the distance
-            const bool below = a.sc.aligned && (a.sc.max_order == 1 || oi_own < a.sc.max_order ||
-                                                oj_own < a.sc.max_order);
-            flux_slot<T, D, M, PDE, RDEG, ALE, MOM>(a, fi, gi, Fi, wp, fj, gj, oi, oj, below, dk, wk, acc, i, k);
+            slot(j, dk, wk, k);
         }
     } else if (need_ext) {
         for (int k = k0; k < cnt; k += KSTEP) {
