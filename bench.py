@@ -44,6 +44,7 @@ STAGES = 3
 HOST_DRIVEN = False     # --host-driven: steps without the step graph (e.g. for kernel profilers)
 AUTOTUNE = True         # --no-autotune: keep the default launch shapes (hcc_autotune picks them otherwise)
 TILE_STAGING = True     # --no-tile-staging: stream-fed FP32 full passes instead of the tile-staged ones
+FORCE_TILES = False     # --tile-staging: tile-staged passes also where the library's default is stream-fed (2-D)
 
 
 def _load(name, path, pkg_dir=None):
@@ -390,8 +391,8 @@ def measure(hcc, cloud, U0, h, prec, steps, warmup, world, local, *, e2e_steps=N
     ctx.prepare_geometry()
     ctx.synchronize()
     setup_s = time.perf_counter() - t0
-    if not TILE_STAGING:
-        ctx.set_tile_staging(False)
+    if not TILE_STAGING or FORCE_TILES:
+        ctx.set_tile_staging(TILE_STAGING and FORCE_TILES)
     U_in = U0.astype(np.float32) if f32 else U0
     ctx.upload_state(U_in)
     dt = 0.4 * ctx.time_step()
@@ -608,8 +609,8 @@ def run_profile_case(args):
     ctx.build_neighbours()
     ctx.prepare_geometry()
     ctx.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
-    if not TILE_STAGING:
-        ctx.set_tile_staging(False)
+    if not TILE_STAGING or FORCE_TILES:
+        ctx.set_tile_staging(TILE_STAGING and FORCE_TILES)
     if args.profile != "plain" and prec == "fp32":
         ctx.set_predictor(pred, PREDICTOR_THRESHOLD)
     ctx.set_step_graphs(False)
@@ -1137,13 +1138,16 @@ def main():
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
     ap.add_argument("--no-tile-staging", action="store_true", help="stream-fed FP32 full passes (A/B)")
+    ap.add_argument("--tile-staging", action="store_true",
+                    help="tile-staged FP32 passes also where the default is stream-fed (2-D; A/B)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    global HOST_DRIVEN, AUTOTUNE, TILE_STAGING
+    global HOST_DRIVEN, AUTOTUNE, TILE_STAGING, FORCE_TILES
     HOST_DRIVEN = args.host_driven
     AUTOTUNE = not args.no_autotune
     TILE_STAGING = not args.no_tile_staging
+    FORCE_TILES = args.tile_staging
     if args.study == "accuracy":
         run_accuracy_study(args)
     elif args.profile:
