@@ -966,8 +966,8 @@ def run_learned_study(args, hcc, predictor, cKDTree):
     run takes its own CFL steps (0.4) to the recorded end time."""
     global PREDICTOR_THRESHOLD
     rec = json.loads((ROOT / "profiles" / "accuracy_equal_l1.json").read_text())
-    thresholds = [float(x) for x in args.study_thresholds.split(",")] if args.study_thresholds else \
-        [PREDICTOR_THRESHOLD]
+    thresholds = [(x if x == "plain" else float(x)) for x in args.study_thresholds.split(",")] \
+        if args.study_thresholds else [PREDICTOR_THRESHOLD]
     keep = PREDICTOR_THRESHOLD
     out = {"held_out_threshold": keep, "rule": PREDICTOR_THRESHOLD_RULE}
     for name in args.study_workloads.split(","):
@@ -984,6 +984,12 @@ def run_learned_study(args, hcc, predictor, cKDTree):
             ref = rf[cKDTree(fine.pos).query(cloud.pos)[1]]
         res = {"t_end": t_end, "l1_fp64": r0["l1_fp64"], "learned": {}}
         for thr in thresholds:
+            if thr == "plain":                  # the FP32 arm without the predictor, for comparison
+                rho, dts, flagged, sec = run_cfl_steps(hcc, cloud, U0, h, "fp32", t_end=t_end)
+                l1 = rel_l1(rho, ref, inner)
+                res["fp32_plain"] = {"l1": l1, "over_fp64": l1 / r0["l1_fp64"], "steps": len(dts),
+                                     "flagged_total": flagged, "seconds": sec}
+                continue
             PREDICTOR_THRESHOLD = thr
             rho, dts, flagged, sec = run_cfl_steps(hcc, cloud, U0, h, "fp32", t_end=t_end, predictor=predictor)
             l1 = rel_l1(rho, ref, inner)
@@ -1134,7 +1140,8 @@ def main():
     ap.add_argument("--study-out", default=None, help="also write the study's JSON here")
     ap.add_argument("--study-learned-only", action="store_true",
                     help="only the FP32 + predictor arm, against the recorded study's references and end times")
-    ap.add_argument("--study-thresholds", default=None, help="comma-separated predictor thresholds (learned-only)")
+    ap.add_argument("--study-thresholds", default=None,
+                    help="comma-separated predictor thresholds (learned-only); 'plain' adds the FP32 arm without it")
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
     ap.add_argument("--no-tile-staging", action="store_true", help="stream-fed FP32 full passes (A/B)")
