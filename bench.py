@@ -793,6 +793,12 @@ def recorded_accuracy():
         return None
     d = json.loads(p.read_text())
     d["source"] = "recorded by `python bench.py --study accuracy` (profiles/accuracy_equal_l1.json)"
+    q = ROOT / "profiles" / "accuracy_learned.json"
+    if q.exists():                       # the later sweep's plain FP32 arm (same references and end times)
+        for name, r in json.loads(q.read_text()).items():
+            if isinstance(r, dict) and "fp32_plain" in r and name in d:
+                d[name]["fp32_over_fp64_recheck"] = r["fp32_plain"]["over_fp64"]
+                d[name]["recheck_source"] = "profiles/accuracy_learned.json"
     return d
 
 
