@@ -102,11 +102,11 @@ def make_workload(hcc, name):
     return cloud, U0, h
 
 
-def make_cfg(hcc, cloud, h, precision):
-    """MUSCL order 2 with the divergence fit of order 2, MOOD (EPD1, MOODu1(1e-4 h^D)), Rusanov, SSP-RK3,
-    transmissive boundaries on every wall."""
+def make_cfg(hcc, cloud, h, precision, scheme=None):
+    """MUSCL order 2 with the divergence fit of order 2 (or `scheme`), MOOD (EPD1, MOODu1(1e-4 h^D)), Rusanov,
+    SSP-RK3, transmissive boundaries on every wall."""
     D = cloud.pos.shape[1]
-    return hcc.make_config(hcc.Euler(D, 1.4), cloud, scheme=hcc.MUSCL(2, 2),
+    return hcc.make_config(hcc.Euler(D, 1.4), cloud, scheme=scheme if scheme is not None else hcc.MUSCL(2, 2),
                            mood=hcc.MOOD(hcc.EPD1, hcc.MOODu1(1e-4 * h ** D)), tableau="RK3_SSP",
                            bc_map={t: hcc.BC_OUTFLOW for t in range(1, 2 * D + 1)}, precision=precision)
 
@@ -731,6 +731,8 @@ def run_gpu(args):
     rec = recorded_accuracy()
     if rec:
         line["accuracy_vs_finer_fp64"] = rec
+    if not args.no_weno and D == 3:
+        line["weno_variant"] = run_weno_variant(hcc, cloud, U0, h, K_steps, world, local)
     if not args.no_2d and D == 3:
         line["euler2d_quadrant_1M"] = run_secondary(hcc, args, world, local, "euler2d_quadrant_1M", predictor,
                                                     peak, peak_kind)
@@ -784,6 +786,32 @@ def learned_l1_ratio(workload, thr):
         if abs(float(d.get("threshold", -1)) - thr) < 1e-12 and workload in d and "learned_over_fp64" in d[workload]:
             return d[workload]["learned_over_fp64"], "profiles/accuracy_equal_l1.json"
     return None, "no recorded study at this threshold"
+
+
+def run_weno_variant(hcc, cloud, U0, h, steps, world, local):
+    """The configuration's meshless-WENO variant of the same workload: component-wise WENO of order 2 for the Euler
+    system (local Lax-Friedrichs splitting) with the same MOOD, SSP-RK3 and boundaries, FP32 and FP64 from the same
+    state (the step graph, CUDA events; fewer steps for FP64)."""
+    out = {"scheme": "meshless WENO order 2, component-wise (local Lax-Friedrichs splitting), MOOD EPD1/MOODu1",
+           "note": "stream-fed passes (the tile-staged form serves MUSCL)"}
+    n_int = cloud.n_interior
+    for prec, K in (("fp32", min(steps, 10)), ("fp64", 2)):
+        ctx = hcc.Context(make_cfg(hcc, cloud, h, prec, scheme=hcc.WENO(2)))
+        ctx.upload_cloud(cloud)
+        ctx.build_neighbours()
+        ctx.prepare_geometry()
+        ctx.upload_state(U0.astype(np.float32) if prec == "fp32" else U0)
+        dt = 0.4 * ctx.time_step()
+        for _ in range(2):
+            ctx.step(0.0, dt)
+        with ClockSampler(local) as clk:
+            ms, launches = time_device_steps(hcc, ctx, dt, K, world)
+        out[prec] = {"ms_per_step": ms / K, "value": n_int * STAGES * K * world / (ms / 1e3), "steps": K,
+                     "warmup": 2, "gpu_launches": launches, "clocks": clk.summary(),
+                     "mood_iterations_last_step": ctx.counters()["mood_iterations"]}
+        ctx.close()
+    out["fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    return out
 
 
 def recorded_accuracy():
@@ -1139,6 +1167,7 @@ def main():
     ap.add_argument("--no-reference-solution", action="store_true", help="skip the h/2 FP64 reference run")
     ap.add_argument("--no-published", action="store_true")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2-D quadrant workload of a 3-D run")
+    ap.add_argument("--no-weno", action="store_true", help="skip the meshless-WENO variant of a 3-D run")
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: --steps)")
     ap.add_argument("--study", choices=["accuracy"], default=None,
                     help="run the equal-L1 study at the configurations' end times instead of the benchmark")

@@ -172,7 +172,8 @@ def Upwind(div_order: int = 0, flux: str = "rusanov", algorithm: str = "Classic"
 
 @dataclass
 class WENO:
-    """WENO(T, D, 1, order; div_order) (src/Interpolation/WENO.jl:43): scalar equations only."""
+    """WENO(T, D, M, order; div_order) (src/Interpolation/WENO.jl:43, scalar there): systems component-wise, linear
+    fluxes per component with their own velocity, Euler by local Lax-Friedrichs splitting (order <= 2 for M > 1)."""
     order: int = 2
     div_order: int = 0
 
