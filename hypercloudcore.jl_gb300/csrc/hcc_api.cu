@@ -194,6 +194,7 @@ struct hcc_ctx {
     // cloud
     double *pos = nullptr; uint8_t *bnd = nullptr; int32_t *tags = nullptr; double *vol = nullptr;
     float *pos32 = nullptr; unsigned int *pmax32 = nullptr;   // FP32 positions of the search prefilter
+    float *wops = nullptr; int32_t *wcnt = nullptr;             // FP32 Euler WENO operators, stencil sizes
     std::vector<uint8_t> h_bnd; std::vector<int32_t> h_tags;
     // cell list
     int dims[3] = {1, 1, 1}; double csize[3] = {1, 1, 1};
@@ -343,7 +344,7 @@ struct hcc_ctx {
         tiles.release();
         free_mover_buffers();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
-        dfree(pos32); dfree(pmax32);
+        dfree(pos32); dfree(pmax32); dfree(wops); dfree(wcnt);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
         for (void **p : {&rhos, &cand, &grad, &xfer}) { if (*p) cudaFree(*p); *p = nullptr; }
@@ -427,6 +428,10 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     g.invL = T(c->invL);
     g.invL64 = c->invL;
     g.h64 = c->h;
+    if constexpr (sizeof(T) == 4) {
+        g.wops = c->wops;
+        g.wcnt = c->wcnt;
+    }
     a.ph = phys_params<T>(c);
     a.sc.max_order = c->max_order;
     a.sc.DO = c->DO;
@@ -1689,6 +1694,17 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
             launch_cast_f64_to_f32(c->dwc64[q], c->dwc32[q], int64_t(slots) * D, c->stream);
         }
         if ((st = build_tiles(c)) != HCC_OK) return st;
+        if (c->weno && c->ops->weno_geom) {   // FP32 Euler WENO: the fit operators of every stencil, once
+            dfree(c->wops);
+            dfree(c->wcnt);
+            HCC_TRY(c->alloc(c->wops, size_t(c->npad) * weno_ops_floats(D), "WENO operators"));
+            HCC_TRY(c->alloc(c->wcnt, size_t(c->npad) * 2 * D, "WENO stencil sizes"));
+            WenoGeomArgs wg{};
+            wg.n = c->n; wg.npad = c->npad; wg.cnt = c->cnt; wg.dist = c->dist64; wg.w = c->w64; wg.bnd = c->bnd;
+            wg.invL64 = c->invL; wg.ops = c->wops; wg.wcnt = c->wcnt;
+            c->ops->weno_geom(wg, c->stream);
+            HCC_TRY(launch_check(c, "WENO operators"));
+        }
     }
     // outflow donor roots, then the boundary list (tag -> condition)
     DonorArgs da{};

@@ -225,6 +225,11 @@ template <typename T> struct Geometry {
     T invL;
     double invL64;                    // 1/min(dx) in FP64 (the MLS fits of both paths)
     double h64;                       // min(dx)
+    // FP32 meshless WENO of Euler: per particle the first-derivative rows of the inverse moment matrices of its
+    // central and one-sided stencils, degrees 1 and 2 ([i][degree - 1][stencil][d][b], FP32, nullptr when absent),
+    // and the sizes of its one-sided stencils ([i][2 d + side - 1])
+    const float *wops;
+    const int32_t *wcnt;
 };
 
 // Tile staging of the FP32 full passes (MUSCL of order <= 2 with the degree-1 divergence fit, fixed grids): the
@@ -378,6 +383,19 @@ __device__ __forceinline__ void reach_mark_warp(uint32_t *mask, int32_t *tiles, 
 }
 
 // Launchers of one (precision, D, M, pde, reconstruction degree) instantiation.
+// Arguments of the geometry pass of the FP32 meshless WENO of Euler (FP64 slot streams in, FP32 operators out).
+struct WenoGeomArgs {
+    int64_t n, npad;
+    const int32_t *cnt;
+    const double *dist, *w;
+    const uint8_t *bnd;
+    double invL64;
+    float *ops;
+    int32_t *wcnt;
+};
+// floats of the WENO operators of one particle: 2 degrees x (2D + 1) stencils x D rows x the degree-2 basis
+inline int weno_ops_floats(int D) { return 2 * (2 * D + 1) * D * cbasis_count(D, 2); }
+
 struct StageOps {
     int D, M, pde, rdeg, Br;
     void (*gather)(const void *args, int64_t n, cudaStream_t s);
@@ -387,6 +405,7 @@ struct StageOps {
     void (*weno)(const void *args, int64_t n, cudaStream_t s);   // WENO flux pass (scalar advection only)
     void (*central)(const void *args, int64_t n, cudaStream_t s);   // CentralDivergence pass
     void (*upwind)(const void *args, int64_t n, cudaStream_t s);    // UpwindDivergence :Tiwari / :Praveen pass
+    void (*weno_geom)(const WenoGeomArgs &g, cudaStream_t s);      // FP32 Euler WENO operators (or nullptr)
 };
 
 const StageOps *stage_ops_f64_r1(int D, int M, int pde);

@@ -2594,6 +2594,267 @@ __global__ void __launch_bounds__(2 * HCC_TILE) k_cfl_tile(const StageArgs<float
     if ((threadIdx.x & 31) == 0) atomicMin(dt_bits, b);
 }
 
+// ----------------------------------------------------------------------------------- FP32 meshless WENO of Euler
+// The fits of the component-wise WENO (weno_sys_one) are linear in the fitted field: out_s = sum_k c_{s,k} df_k with
+// c_{s,k} = invL R_s (w_k p_k), R_s the first D rows of the inverse moment matrix of stencil s (the central stencil
+// and, per axis, the slots with x_d < 0 and with x_d >= 0). The moment matrices depend on the geometry only: this
+// pass assembles and factorises them once in FP64 (degree 2; the degree-1 matrix is its leading block, the same
+// products), and stores R_s for both degrees in FP32, with the one-sided stencil sizes. A failed factorisation
+// stores zeros (the fit returns zero, as in weno_fit_f).
+template <int D>
+__global__ void k_weno_geom(const WenoGeomArgs g) {
+    constexpr int B1 = cbasis_count(D, 1), B2 = cbasis_count(D, 2), NS = 2 * D + 1;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    float *out = g.ops + i * int64_t(2 * NS * D * B2);
+    for (int q = 0; q < 2 * NS * D * B2; ++q) out[q] = 0.0f;
+    if (g.bnd[i]) return;
+    const int cnt = g.cnt[i];
+    const int64_t np = g.npad;
+    for (int st = 0; st < NS; ++st) {
+        const int dsel = st == 0 ? -1 : (st - 1) / 2, side = st == 0 ? 0 : 1 + (st - 1) % 2;
+        double N[B2 * B2];
+        for (int q = 0; q < B2 * B2; ++q) N[q] = 0.0;
+        int members = 0;
+        for (int k = 0; k < cnt; ++k) {
+            if (dsel >= 0) {
+                const double dd = g.dist[(int64_t(k) * D + dsel) * np + i];
+                if (!(side == 1 ? dd < 0.0 : dd >= 0.0)) continue;
+            }
+            ++members;
+            double x[D], p[B2];
+#pragma unroll
+            for (int d = 0; d < D; ++d) x[d] = g.dist[(int64_t(k) * D + d) * np + i] * g.invL64;
+            table_basis<D, 2, double>(x, p);
+            const double w = g.w[int64_t(k) * np + i];
+            for (int r = 0; r < B2; ++r)
+                for (int c = r; c < B2; ++c) N[r * B2 + c] = N[r * B2 + c] + w * (p[r] * p[c]);
+        }
+        for (int r = 1; r < B2; ++r)
+            for (int c = 0; c < r; ++c) N[r * B2 + c] = N[c * B2 + r];
+        if (st > 0) g.wcnt[i * (2 * D) + (st - 1)] = members;
+        {   // degree 1: the leading block
+            double N1[B1 * B1], U1[B1 * B1];
+            for (int r = 0; r < B1; ++r)
+                for (int c = 0; c < B1; ++c) N1[r * B1 + c] = N[r * B2 + c];
+            if (chol_moment_fixed<B1>(N1, U1)) {
+                float *o = out + (0 * NS + st) * D * B2;
+                for (int b = 0; b < B1; ++b) {
+                    double e[B1], xs[B1];
+                    for (int r = 0; r < B1; ++r) e[r] = r == b ? 1.0 : 0.0;
+                    chol_solve_fixed<B1>(U1, e, xs);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) o[d * B2 + b] = float(xs[d] * g.invL64);
+                }
+            }
+        }
+        {   // degree 2
+            double U2[B2 * B2];
+            if (chol_moment_fixed<B2>(N, U2)) {
+                float *o = out + (1 * NS + st) * D * B2;
+                for (int b = 0; b < B2; ++b) {
+                    double e[B2], xs[B2];
+                    for (int r = 0; r < B2; ++r) e[r] = r == b ? 1.0 : 0.0;
+                    chol_solve_fixed<B2>(U2, e, xs);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) o[d * B2 + b] = float(xs[d] * g.invL64);
+                }
+            }
+        }
+    }
+}
+
+// The component-wise WENO of weno_sys_one for Euler in FP32 with the cached operators. Per axis d one pass over the
+// slots accumulates, with the central operator and the operator of the slot's side, the gradients of the
+// differences F_d(U_j)_m - F_d(U_i)_m and U_j,m - U_i,m and the largest lambda_d of the stencil (alpha_d); the split
+// fields F_d^+- = (F_d +- alpha_d U) / 2 are linear in those, so their central and one-sided gradients, smoothness
+// indicators and WENO weights follow without another pass. Same degree and stencil rules as weno_sys_one.
+template <int D>
+__device__ __forceinline__ bool weno_euler_f32_one(const StageArgs<float> &a, const int64_t i, float *sop) {
+    constexpr int M = D + 2, B2 = cbasis_count(D, 2), NS = 2 * D + 1, R = D * B2;
+    if (a.g.bnd[i]) {
+        if (a.full) {
+            float z[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) z[m] = 0.0f;
+            store_vec<float, M>(a.K + i * M, z);
+        }
+        return false;
+    }
+    const int cnt = a.g.cnt[i];
+    const int64_t np = a.g.npad;
+    float Ui[M], mn[M], mx[M];
+    load_vec<float, M>(a.U + i * M, Ui);
+#pragma unroll
+    for (int m = 0; m < M; ++m) mn[m] = mx[m] = Ui[m];
+    const bool need_ext = a.check && (a.sc.criterion == HCC_MOOD_U1 || a.sc.criterion == HCC_MOOD_U2);
+    float div[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) div[m] = 0.0f;
+    int p_order = a.orders[i];
+    while (p_order > 1 && cnt < basis_count(D, p_order)) --p_order;
+    if (cnt >= basis_count(D, p_order)) {
+        const int DO = a.sc.DO;
+        const float dx2 = float(a.g.h64 * a.g.h64);
+        const int qC = DO == 0 ? p_order : (DO < p_order ? DO : p_order);
+        auto one_sided = [&](int d, int side) {
+            const int stencil = a.g.wcnt[i * (2 * D) + 2 * d + side - 1];
+            int p_d = p_order;
+            while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
+            if (stencil < basis_count(D, p_d)) return 0;
+            return DO == 0 ? p_d : (DO < p_d ? DO : p_d);
+        };
+        float inv_rho_i, u_i[D], p_i;
+        euler_prim<float, D>(a.ph, Ui, inv_rho_i, u_i, p_i);
+        const float c_i = root(a.ph.gamma * p_i * inv_rho_i);
+        const float *ops = a.g.wops + i * int64_t(2 * NS * R);
+        for (int d = 0; d < D; ++d) {
+            const int q1 = one_sided(d, 1), q2 = one_sided(d, 2);
+            // this axis's operators (central, side 1, side 2) into this thread's shared-memory row
+            const float *oC = ops + ((qC - 1) * NS + 0) * R;
+            const float *o1 = ops + ((q1 > 0 ? q1 - 1 : 0) * NS + 1 + 2 * d) * R;
+            const float *o2 = ops + ((q2 > 0 ? q2 - 1 : 0) * NS + 2 + 2 * d) * R;
+            for (int q = 0; q < R; ++q) { sop[q] = oC[q]; sop[R + q] = o1[q]; sop[2 * R + q] = o2[q]; }
+            // F_d of the own state (flux_and_speed's components)
+            float Fi[M];
+            Fi[0] = Ui[1 + d];
+#pragma unroll
+            for (int e = 0; e < D; ++e) Fi[1 + e] = (e == d) ? Ui[1 + e] * u_i[d] + p_i : Ui[1 + e] * u_i[d];
+            Fi[D + 1] = (Ui[D + 1] + p_i) * u_i[d];
+            float alpha = fabsf(u_i[d]) + c_i;
+            float gCF[M][D], gCU[M][D], gSF[2][M][D], gSU[2][M][D];
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+#pragma unroll
+                for (int e = 0; e < D; ++e) {
+                    gCF[m][e] = gCU[m][e] = 0.0f;
+                    gSF[0][m][e] = gSU[0][m][e] = gSF[1][m][e] = gSU[1][m][e] = 0.0f;
+                }
+            for (int k = 0; k < cnt; ++k) {
+                const int64_t j = a.g.nidx[int64_t(k) * np + i];
+                float x[D];
+#pragma unroll
+                for (int e = 0; e < D; ++e) x[e] = a.g.dist[(int64_t(k) * D + e) * np + i] * a.g.invL;
+                const int sd = x[d] < 0.0f ? 0 : 1;
+                float pb[B2];
+                table_basis<D, 2, float>(x, pb);
+                const float w = a.g.wt[int64_t(k) * np + i];
+#pragma unroll
+                for (int b = 0; b < B2; ++b) pb[b] = w * pb[b];
+                float cC[D], cS[D];
+                const float *oS = sop + (1 + sd) * R;
+#pragma unroll
+                for (int e = 0; e < D; ++e) {
+                    float vc = 0.0f, vs = 0.0f;
+#pragma unroll
+                    for (int b = 0; b < B2; ++b) { vc = vc + sop[e * B2 + b] * pb[b]; vs = vs + oS[e * B2 + b] * pb[b]; }
+                    cC[e] = vc;
+                    cS[e] = vs;
+                }
+                float Uj[M];
+                load_vec<float, M>(a.U + j * M, Uj);
+                if (d == 0 && need_ext) {
+#pragma unroll
+                    for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], Uj[m]); mx[m] = vmax(mx[m], Uj[m]); }
+                }
+                float inv_rho, u[D], pj;
+                euler_prim<float, D>(a.ph, Uj, inv_rho, u, pj);
+                alpha = vmax(alpha, fabsf(u[d]) + root(a.ph.gamma * pj * inv_rho));
+                float Fj[M];
+                Fj[0] = Uj[1 + d];
+#pragma unroll
+                for (int e = 0; e < D; ++e) Fj[1 + e] = (e == d) ? Uj[1 + e] * u[d] + pj : Uj[1 + e] * u[d];
+                Fj[D + 1] = (Uj[D + 1] + pj) * u[d];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float dU = Uj[m] - Ui[m], dF = Fj[m] - Fi[m];
+#pragma unroll
+                    for (int e = 0; e < D; ++e) {
+                        gCU[m][e] = gCU[m][e] + cC[e] * dU;
+                        gCF[m][e] = gCF[m][e] + cC[e] * dF;
+                        if (sd == 0) {
+                            gSU[0][m][e] = gSU[0][m][e] + cS[e] * dU;
+                            gSF[0][m][e] = gSF[0][m][e] + cS[e] * dF;
+                        } else {
+                            gSU[1][m][e] = gSU[1][m][e] + cS[e] * dU;
+                            gSF[1][m][e] = gSF[1][m][e] + cS[e] * dF;
+                        }
+                    }
+                }
+            }
+            // the split fields F_d^+ (side 1: x_d < 0) and F_d^- (side 2)
+#pragma unroll
+            for (int sg = 0; sg < 2; ++sg) {
+                const float sgn = sg == 0 ? 1.0f : -1.0f;
+                const int qS = sg == 0 ? q1 : q2;
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float fi = 0.5f * (Fi[m] + sgn * alpha * Ui[m]);
+                    float gC[D];
+#pragma unroll
+                    for (int e = 0; e < D; ++e) gC[e] = 0.5f * (gCF[m][e] + sgn * alpha * gCU[m][e]);
+                    float deriv = gC[d];
+                    if (qS > 0) {
+                        float smoothC = (gC[0] * gC[0]) * dx2;
+#pragma unroll
+                        for (int e = 1; e < D; ++e) smoothC = smoothC + (gC[e] * gC[e]) * dx2;
+                        float s2 = vmax(fi * fi, smoothC);
+                        s2 = s2 > 0.0f ? s2 : 1.0f;
+                        const float aC = smoothC / s2 + 1e-12f;
+                        float gS[D];
+#pragma unroll
+                        for (int e = 0; e < D; ++e) gS[e] = 0.5f * (gSF[sg][m][e] + sgn * alpha * gSU[sg][m][e]);
+                        float smoothS = (gS[0] * gS[0]) * dx2;
+#pragma unroll
+                        for (int e = 1; e < D; ++e) smoothS = smoothS + (gS[e] * gS[e]) * dx2;
+                        const float qq = (smoothS / s2 + 1e-12f) / aC;
+                        const float wS = 1.0f / (1.0f + qq * qq);
+                        deriv = wS * gS[d] + (1.0f - wS) * gC[d];
+                    }
+                    div[m] = div[m] + deriv;
+                }
+            }
+        }
+    } else if (need_ext) {
+        for (int k = 0; k < cnt; ++k) {
+            const int64_t j = a.g.nidx[int64_t(k) * np + i];
+#pragma unroll
+            for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], a.U[j * M + m]); mx[m] = vmax(mx[m], a.U[j * M + m]); }
+        }
+    }
+    float Kv[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Kv[m] = -div[m];
+    return stage_epilogue<float, D, M, HCC_PDE_EULER>(a, i, Ui, Kv, mn, mx);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_weno_euler_f32(const StageArgs<float> a) {
+    constexpr int RS = (3 * D * cbasis_count(D, 2)) | 1;   // odd row stride: conflict-free per-thread rows
+    extern __shared__ float wsm[];
+    float *sop = wsm + int(threadIdx.x) * RS;
+    const int lane = int(threadIdx.x & 31);
+    if (a.full) {
+        const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool f = (i < a.g.n) ? weno_euler_f32_one<D>(a, i, sop) : false;
+        if (a.check) tile_failures(a, i >> 5, f);
+        return;
+    }
+    const unsigned nt = *a.wcount;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = warp; q < nt; q += nwarps) {
+        const int32_t tile = a.wtiles[q];
+        const uint32_t word = a.wmask[tile];
+        const int64_t i = int64_t(tile) * 32 + lane;
+        const bool f = ((word >> lane) & 1u) ? weno_euler_f32_one<D>(a, i, sop) : false;
+        if (a.check) tile_failures(a, tile, f);
+        if (lane == 0 && a.clear_wmask) a.wmask[tile] = 0u;
+    }
+}
+template <int D> inline size_t weno_euler_smem() {
+    return size_t(128) * ((3 * D * cbasis_count(D, 2)) | 1) * sizeof(float);
+}
+
 // ----------------------------------------------------------------------------------- launchers / registry
 template <typename T, int D, int M, int PDE, int RDEG>
 struct StageInst {
@@ -2695,6 +2956,18 @@ struct StageInst {
     }
     static void weno(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
+        if constexpr (sizeof(T) == 4 && PDE == HCC_PDE_EULER && RDEG == 1) {
+            if (a.g.wops) {   // FP32 Euler with the cached operators
+                static bool attr = false;
+                if (!attr) {
+                    cudaFuncSetAttribute(k_weno_euler_f32<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(weno_euler_smem<D>()));
+                    attr = true;
+                }
+                k_weno_euler_f32<D><<<pass_grid(a, n, 128), 128, weno_euler_smem<D>(), s>>>(a);
+                return;
+            }
+        }
         if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
             k_weno<T, D><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         } else if constexpr (RDEG == 1) {       // systems (one instantiation: WENO has no reconstruction degree)
@@ -2710,6 +2983,10 @@ struct StageInst {
                 k_upwind<T, D, HCC_UPWIND_PRAVEEN><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         }
     }
+    static void weno_geom(const WenoGeomArgs &g, cudaStream_t s) {
+        if constexpr (sizeof(T) == 4 && PDE == HCC_PDE_EULER && RDEG == 1)
+            if (g.n > 0) k_weno_geom<D><<<unsigned((g.n + 127) / 128), 128, 0, s>>>(g);
+    }
     static void central(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
         k_central<T, D, M, PDE><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
@@ -2718,7 +2995,8 @@ struct StageInst {
         static const StageOps o = {D, M, PDE, RDEG, RBasis<D, RDEG>::B, &gather, &flux, &stage1, &cfl,
                                    ((M == 1 && PDE == HCC_PDE_ADVECTION) || RDEG == 1) ? &weno : nullptr,
                                    RDEG == 1 ? &central : nullptr,
-                                   (RDEG == 1 && M == 1 && PDE == HCC_PDE_ADVECTION) ? &upwind : nullptr};
+                                   (RDEG == 1 && M == 1 && PDE == HCC_PDE_ADVECTION) ? &upwind : nullptr,
+                                   (sizeof(T) == 4 && PDE == HCC_PDE_EULER && RDEG == 1) ? &weno_geom : nullptr};
         return &o;
     }
 };
