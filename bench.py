@@ -906,11 +906,11 @@ def radial_blast_reference(t_end, r_query, gamma=1.4, n=10000, r_max=0.9):
     return np.interp(r_query, rc, U[0])
 
 
-def run_cfl_steps(hcc, cloud, U0, h, prec, dts=None, steps=None, t_end=None, predictor=None):
+def run_cfl_steps(hcc, cloud, U0, h, prec, dts=None, steps=None, t_end=None, predictor=None, scheme=None):
     """Steps from the initial state: with `dts`, exactly those step sizes; otherwise dt = 0.4 x the CFL step of the
     current state until `steps` steps or time `t_end`. Returns (density, the dt sequence, MOOD flags summed over the
     steps, seconds)."""
-    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec, scheme=scheme))
     if predictor is not None:
         ctx.set_predictor(predictor, PREDICTOR_THRESHOLD)
     ctx.upload_cloud(cloud)
@@ -990,6 +990,33 @@ def run_accuracy_study(args):
         out[name] = rec
         print(json.dumps({name: rec}), flush=True)
     print(json.dumps({"accuracy_study": out}), flush=True)
+    if args.study_out:
+        Path(args.study_out).write_text(json.dumps(out, indent=1) + "\n")
+
+
+def run_weno_study(args):
+    """Density L1 errors of the configuration's two schemes (MUSCL2 + MOOD, meshless WENO of order 2 + MOOD) in FP64
+    and FP32 on the 3-D blast at the size where the FP64 WENO path, whose fits run in FP64 at every stage, is
+    affordable (262k interior), at the recorded study's end time, against the 1-D radial FP64 solve."""
+    hcc = package()
+    import torch
+    torch.cuda.set_device(0)
+    rec = json.loads((ROOT / "profiles" / "accuracy_equal_l1.json").read_text())
+    t_end = rec["euler3d_blast_8M"]["t_end"]
+    name = "euler3d_blast_262k"
+    cloud, U0, h = make_workload(hcc, name)
+    inner = cloud.is_boundary == 0
+    ref = radial_blast_reference(t_end, np.sqrt(((cloud.pos - 0.5) ** 2).sum(axis=1)))
+    out = {"workload": name, "n_interior": int(cloud.n_interior), "t_end": t_end,
+           "reference": "1-D spherical FP64 solve (radial_blast_reference)"}
+    for label, scheme in (("muscl", hcc.MUSCL(2, 2)), ("weno", hcc.WENO(2))):
+        for prec in ("fp64", "fp32"):
+            rho, dts, flagged, sec = run_cfl_steps(hcc, cloud, U0, h, prec, t_end=t_end, scheme=scheme)
+            out[f"{label}_{prec}"] = {"l1": rel_l1(rho, ref, inner), "steps": len(dts), "seconds": sec,
+                                      "flagged_total": flagged}
+            print(json.dumps({f"{label}_{prec}": out[f"{label}_{prec}"]}), flush=True)
+        out[f"{label}_fp32_over_fp64"] = out[f"{label}_fp32"]["l1"] / out[f"{label}_fp64"]["l1"]
+    print(json.dumps({"weno_study": out}), flush=True)
     if args.study_out:
         Path(args.study_out).write_text(json.dumps(out, indent=1) + "\n")
 
@@ -1170,8 +1197,9 @@ def main():
     ap.add_argument("--no-2d", action="store_true", help="skip the 2-D quadrant workload of a 3-D run")
     ap.add_argument("--no-weno", action="store_true", help="skip the meshless-WENO variant of a 3-D run")
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: --steps)")
-    ap.add_argument("--study", choices=["accuracy"], default=None,
-                    help="run the equal-L1 study at the configurations' end times instead of the benchmark")
+    ap.add_argument("--study", choices=["accuracy", "weno"], default=None,
+                    help="run the equal-L1 study at the configurations' end times (accuracy), or the MUSCL / WENO "
+                         "comparison on the 262k blast (weno), instead of the benchmark")
     ap.add_argument("--study-workloads", default="euler3d_blast_8M,euler2d_quadrant_1M")
     ap.add_argument("--study-out", default=None, help="also write the study's JSON here")
     ap.add_argument("--study-learned-only", action="store_true",
@@ -1193,6 +1221,8 @@ def main():
     FORCE_TILES = args.tile_staging
     if args.study == "accuracy":
         run_accuracy_study(args)
+    elif args.study == "weno":
+        run_weno_study(args)
     elif args.profile:
         run_profile_case(args)
     elif args.impl == "reference":
