@@ -2730,15 +2730,28 @@ __device__ __forceinline__ bool weno_euler_f32_one(const StageArgs<float> &a, co
                     gCF[m][e] = gCU[m][e] = 0.0f;
                     gSF[0][m][e] = gSU[0][m][e] = gSF[1][m][e] = gSU[1][m][e] = 0.0f;
                 }
-            for (int k = 0; k < cnt; ++k) {
-                const int64_t j = a.g.nidx[int64_t(k) * np + i];
-                float x[D];
+            // the next slot's index, offsets, weight and state are loaded while this one is computed
+            int64_t jn = 0;
+            float xn[D], wn = 0.0f, Un[M];
+            auto load_slot = [&](int k) {
+                jn = a.g.nidx[int64_t(k) * np + i];
 #pragma unroll
-                for (int e = 0; e < D; ++e) x[e] = a.g.dist[(int64_t(k) * D + e) * np + i] * a.g.invL;
+                for (int e = 0; e < D; ++e) xn[e] = a.g.dist[(int64_t(k) * D + e) * np + i];
+                wn = a.g.wt[int64_t(k) * np + i];
+                load_vec<float, M>(a.U + jn * M, Un);
+            };
+            if (cnt > 0) load_slot(0);
+            for (int k = 0; k < cnt; ++k) {
+                float x[D], Uj[M];
+#pragma unroll
+                for (int e = 0; e < D; ++e) x[e] = xn[e] * a.g.invL;
+                const float w = wn;
+#pragma unroll
+                for (int m = 0; m < M; ++m) Uj[m] = Un[m];
+                if (k + 1 < cnt) load_slot(k + 1);
                 const int sd = x[d] < 0.0f ? 0 : 1;
                 float pb[B2];
                 table_basis<D, 2, float>(x, pb);
-                const float w = a.g.wt[int64_t(k) * np + i];
 #pragma unroll
                 for (int b = 0; b < B2; ++b) pb[b] = w * pb[b];
                 float cC[D], cS[D];
@@ -2751,8 +2764,6 @@ __device__ __forceinline__ bool weno_euler_f32_one(const StageArgs<float> &a, co
                     cC[e] = vc;
                     cS[e] = vs;
                 }
-                float Uj[M];
-                load_vec<float, M>(a.U + j * M, Uj);
                 if (d == 0 && need_ext) {
 #pragma unroll
                     for (int m = 0; m < M; ++m) { mn[m] = vmin(mn[m], Uj[m]); mx[m] = vmax(mx[m], Uj[m]); }
