@@ -195,6 +195,8 @@ struct hcc_ctx {
     double *pos = nullptr; uint8_t *bnd = nullptr; int32_t *tags = nullptr; double *vol = nullptr;
     float *pos32 = nullptr; unsigned int *pmax32 = nullptr;   // FP32 positions of the search prefilter
     float *wops = nullptr; int32_t *wcnt = nullptr;             // FP32 Euler WENO operators, stencil sizes
+    double *wchol = nullptr; uint8_t *wok = nullptr;             // FP64 Euler WENO: packed factors and flags
+    double *wflux64 = nullptr;                                    // FP64 Euler WENO: the stage's flux table
     std::vector<uint8_t> h_bnd; std::vector<int32_t> h_tags;
     // cell list
     int dims[3] = {1, 1, 1}; double csize[3] = {1, 1, 1};
@@ -344,7 +346,7 @@ struct hcc_ctx {
         tiles.release();
         free_mover_buffers();
         dfree(pos); dfree(bnd); dfree(tags); dfree(vol); dfree(bin_of); dfree(cellp); dfree(cnt);
-        dfree(pos32); dfree(pmax32); dfree(wops); dfree(wcnt);
+        dfree(pos32); dfree(pmax32); dfree(wops); dfree(wcnt); dfree(wchol); dfree(wok); dfree(wflux64);
         dfree(ok_r); dfree(ok_d); dfree(ok_1); dfree(inv_r64); dfree(inv_d64); dfree(inv_r32);
         dfree(status); dfree(status2); dfree(root); dfree(blist); dfree(bsrc);
         for (void **p : {&rhos, &cand, &grad, &xfer}) { if (*p) cudaFree(*p); *p = nullptr; }
@@ -431,6 +433,10 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
     if constexpr (sizeof(T) == 4) {
         g.wops = c->wops;
         g.wcnt = c->wcnt;
+    } else {
+        g.wchol = c->wchol;
+        g.wok = c->wok;
+        g.wcnt = c->wcnt;
     }
     a.ph = phys_params<T>(c);
     a.sc.max_order = c->max_order;
@@ -464,6 +470,8 @@ template <typename T> StageArgs<T> base_args(hcc_ctx *c) {
             v.quantum = c->tiles.quantum; v.lidx = c->tiles.lidx; v.lself = c->tiles.lself; v.coef = c->tiles.coef;
             v.cw = c->tiles.cw; v.umax = c->tiles.umax; v.wscale = c->tiles.wscale;
         }
+    } else {
+        a.wflux64 = c->wflux64;
     }
     return a;
 }
@@ -1705,6 +1713,20 @@ hcc_status hcc_prepare_geometry(hcc_ctx *c) {
             c->ops->weno_geom(wg, c->stream);
             HCC_TRY(launch_check(c, "WENO operators"));
         }
+    } else if (c->weno && c->ops->weno_geom) {   // FP64 Euler WENO: the factors of every stencil, once
+        dfree(c->wchol);
+        dfree(c->wok);
+        dfree(c->wcnt);
+        dfree(c->wflux64);
+        HCC_TRY(c->alloc(c->wchol, size_t(c->npad) * weno_chol_doubles(D), "WENO factors"));
+        HCC_TRY(c->alloc(c->wok, size_t(c->npad) * 2 * (2 * D + 1), "WENO factor flags"));
+        HCC_TRY(c->alloc(c->wcnt, size_t(c->npad) * 2 * D, "WENO stencil sizes"));
+        HCC_TRY(c->alloc(c->wflux64, size_t(c->npad) * D * (c->M + 1), "WENO flux table"));
+        WenoGeomArgs wg{};
+        wg.n = c->n; wg.npad = c->npad; wg.cnt = c->cnt; wg.dist = c->dist64; wg.w = c->w64; wg.bnd = c->bnd;
+        wg.invL64 = c->invL; wg.chol = c->wchol; wg.ok = c->wok; wg.wcnt = c->wcnt;
+        c->ops->weno_geom(wg, c->stream);
+        HCC_TRY(launch_check(c, "WENO factors"));
     }
     // outflow donor roots, then the boundary list (tag -> condition)
     DonorArgs da{};

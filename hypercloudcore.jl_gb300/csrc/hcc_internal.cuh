@@ -230,6 +230,10 @@ template <typename T> struct Geometry {
     // and the sizes of its one-sided stencils ([i][2 d + side - 1])
     const float *wops;
     const int32_t *wcnt;
+    // FP64 meshless WENO of Euler: the Cholesky factors of the same moment matrices (packed upper triangles,
+    // [i][degree - 1][stencil][B2 (B2 + 1) / 2]) and their flags ([i][degree - 1][stencil]), nullptr when absent
+    const double *wchol;
+    const uint8_t *wok;
 };
 
 // Tile staging of the FP32 full passes (MUSCL of order <= 2 with the degree-1 divergence fit, fixed grids): the
@@ -278,6 +282,7 @@ template <typename T> struct StageArgs {
     const int8_t *nbmin;              // EPD2: neighbourhood minimum of the orders
     T *grad;                          // [i * Br * M]
     const T *U;                       // stage state Y_s
+    double *wflux64;                  // FP64 Euler WENO: per particle F_d(U)_m and lambda_d of the stage state
     T *K;                             // K_E[s]
     int full;                         // 1: every particle; 0: the members of a tile worklist
     // Worklist pass: tiles of 32 consecutive particles (one warp each, coalesced slot-major loads), the tiles to
@@ -390,9 +395,13 @@ struct WenoGeomArgs {
     const double *dist, *w;
     const uint8_t *bnd;
     double invL64;
-    float *ops;
+    float *ops;                       // FP32 contexts: the operators
     int32_t *wcnt;
+    double *chol;                     // FP64 contexts: the packed Cholesky factors and their flags
+    uint8_t *ok;
 };
+// doubles of the packed WENO Cholesky factors of one particle: 2 degrees x (2D + 1) stencils x B2 (B2 + 1) / 2
+inline int weno_chol_doubles(int D) { return 2 * (2 * D + 1) * cbasis_count(D, 2) * (cbasis_count(D, 2) + 1) / 2; }
 // floats of the WENO operators of one particle: 2 degrees x (2D + 1) stencils x D rows x the degree-2 basis
 inline int weno_ops_floats(int D) { return 2 * (2 * D + 1) * D * cbasis_count(D, 2); }
 

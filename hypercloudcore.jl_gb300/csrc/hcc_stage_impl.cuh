@@ -1931,6 +1931,58 @@ __device__ __forceinline__ void weno_fit_q(int q, const StageArgs<T> &a, int64_t
     else weno_fit<T, D, 3>(a, i, cnt, dsel, side, fi, out);
 }
 
+// Position of the upper-triangle entry (r, c), r <= c, of a B x B matrix stored packed by rows.
+template <int B> __host__ __device__ constexpr int packed_upper(int r, int c) { return r * B - r * (r - 1) / 2 + (c - r); }
+// chol_solve_fixed with the factor packed: the same entries, the same operations in the same order.
+template <int B>
+__device__ __forceinline__ void chol_solve_packed(const double *U, const double *b, double *x) {
+    double y[B];
+    for (int r = 0; r < B; ++r) {
+        double t = b[r];
+        for (int q = 0; q < r; ++q) t = t - U[packed_upper<B>(q, r)] * y[q];
+        y[r] = t / U[packed_upper<B>(r, r)];
+    }
+    for (int r = B - 1; r >= 0; --r) {
+        double t = y[r];
+        for (int q = r + 1; q < B; ++q) t = t - U[packed_upper<B>(r, q)] * x[q];
+        x[r] = t / U[packed_upper<B>(r, r)];
+    }
+}
+
+// weno_fit_f with the moment matrix's Cholesky factor taken from the geometry pass (k_weno_geom64: the same matrix,
+// the same factorisation): only the right-hand side is summed here, in the same order, so the fit is bit for bit
+// that of weno_fit_f.
+template <typename T, int D, int Q, typename Field>
+__device__ bool weno_fit_cached(const StageArgs<T> &a, int64_t i, int cnt, int dsel, int side, double fi, Field g,
+                                const double *Up, bool ok, double *out) {
+    constexpr int B = ExpTable<D, Q>::B;
+    const int64_t np = a.g.npad;
+    double bs[B];
+    for (int q = 0; q < B; ++q) bs[q] = 0.0;
+    for (int k = 0; k < cnt; ++k) {
+        if (dsel >= 0) {
+            const double dd = double(a.g.dist[(int64_t(k) * D + dsel) * np + i]);
+            if (!(side == 1 ? dd < 0.0 : side == 2 ? dd >= 0.0 : dd <= 0.0)) continue;
+        }
+        const int64_t s = int64_t(k) * np + i;
+        double x[D], p[B];
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] = double(a.g.dist[(int64_t(k) * D + d) * np + i]) * a.g.invL64;
+        table_basis<D, Q, double>(x, p);
+        const double w = double(a.g.wt[s]);
+        const double df = g(int64_t(a.g.nidx[s])) - fi;
+        for (int r = 0; r < B; ++r) bs[r] = bs[r] + w * (p[r] * df);
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) out[d] = 0.0;
+    if (!ok) return false;
+    double xs[B];
+    chol_solve_packed<B>(Up, bs, xs);
+#pragma unroll
+    for (int d = 0; d < D; ++d) out[d] = xs[d] * a.g.invL64;
+    return true;
+}
+
 // The WENO functor (WENO.jl:55-165): central fit over the whole stencil and one upwind one-sided fit per axis,
 // blended with w_S = 1 / (1 + (a_S / a_C)^2) on smoothness indicators IS = Σ_d (∂_d u)^2 h^2 normalised by
 // max(u_i^2, IS_C); the result is Σ_d v_d ∂_d u and K_E = -that. Fits in FP64 in both paths.
@@ -2066,9 +2118,13 @@ __device__ __forceinline__ bool weno_sys_one(const StageArgs<T> &a, const int64_
         // fit degree of the one-sided stencil of axis d (side 1: x_d < 0, side 2: x_d >= 0), 0 when too small
         auto one_sided = [&](int d, int side) {
             int stencil = 0;
-            for (int k = 0; k < cnt; ++k) {
-                const double dd = double(a.g.dist[(int64_t(k) * D + d) * np + i]);
-                stencil += side == 1 ? (dd < 0.0) : (dd >= 0.0);
+            if (a.g.wcnt) {
+                stencil = a.g.wcnt[i * (2 * D) + 2 * d + side - 1];
+            } else {
+                for (int k = 0; k < cnt; ++k) {
+                    const double dd = double(a.g.dist[(int64_t(k) * D + d) * np + i]);
+                    stencil += side == 1 ? (dd < 0.0) : (dd >= 0.0);
+                }
             }
             int p_d = p_order;
             while (p_d > 1 && stencil < basis_count(D, p_d)) --p_d;
@@ -2133,39 +2189,64 @@ __device__ __forceinline__ bool weno_sys_one(const StageArgs<T> &a, const int64_
             double Ui[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) Ui[m] = double(fiT[m]);
+            // with the geometry pass's factors and this stage's flux table (k_weno_prep64): the same values, each
+            // computed once instead of once per fit
+            const bool cached = a.g.wchol != nullptr && a.wflux64 != nullptr;
+            constexpr int FW = D * (M + 1);                 // flux table row: F_d(U)_m then lambda_d, per axis
             double alpha[D];
             for (int d = 0; d < D; ++d) {
-                alpha[d] = lam(Ui, d);
+                alpha[d] = cached ? a.wflux64[i * FW + d * (M + 1) + M] : lam(Ui, d);
                 for (int k = 0; k < cnt; ++k) {
                     const int64_t j = a.g.nidx[int64_t(k) * np + i];
+                    if (cached) {
+                        alpha[d] = jmax(alpha[d], a.wflux64[j * FW + d * (M + 1) + M]);
+                        continue;
+                    }
                     double Uj[M];
 #pragma unroll
                     for (int m = 0; m < M; ++m) Uj[m] = double(a.U[j * M + m]);
                     alpha[d] = jmax(alpha[d], lam(Uj, d));
                 }
             }
+            constexpr int B2 = cbasis_count(D, 2), PK = B2 * (B2 + 1) / 2, NS = 2 * D + 1;
+            auto fit = [&](int q, int dsel, int side, double fi, auto g, double *res) {
+                if (!cached) {
+                    weno_fit_qf<T, D>(q, a, i, cnt, dsel, side, fi, g, res);
+                    return;
+                }
+                const int st = dsel < 0 ? 0 : 1 + 2 * dsel + side - 1;
+                const int64_t slot = (i * 2 + (q - 1)) * NS + st;
+                if (q == 1) weno_fit_cached<T, D, 1>(a, i, cnt, dsel, side, fi, g, a.g.wchol + slot * PK, a.g.wok[slot], res);
+                else weno_fit_cached<T, D, 2>(a, i, cnt, dsel, side, fi, g, a.g.wchol + slot * PK, a.g.wok[slot], res);
+            };
             for (int d = 0; d < D; ++d)
                 for (int sg = 0; sg < 2; ++sg) {
                     const int side = sg == 0 ? 1 : 2;
                     const int qS = one_sided(d, side);
                     for (int m = 0; m < M; ++m) {
                         // F_d^+-(U_j)_m, the physical flux component as flux_and_speed forms it
-                        auto g = [&a, &prim, &alpha, d, m, sg](int64_t j) {
-                            double Uj[M];
+                        auto g = [&a, &prim, &alpha, d, m, sg, cached](int64_t j) {
+                            double F, Ujm;
+                            if (cached) {
+                                F = a.wflux64[j * FW + d * (M + 1) + m];
+                                Ujm = double(a.U[j * M + m]);
+                            } else {
+                                double Uj[M];
 #pragma unroll
-                            for (int c = 0; c < M; ++c) Uj[c] = double(a.U[j * M + c]);
-                            double inv_rho, u[D], p;
-                            prim(Uj, inv_rho, u, p);
-                            double F;
-                            if (m == 0) F = Uj[1 + d];
-                            else if (m <= D) F = (m - 1 == d) ? Uj[m] * u[d] + p : Uj[m] * u[d];
-                            else F = (Uj[D + 1] + p) * u[d];
-                            const double aU = alpha[d] * Uj[m];
+                                for (int c = 0; c < M; ++c) Uj[c] = double(a.U[j * M + c]);
+                                double inv_rho, u[D], p;
+                                prim(Uj, inv_rho, u, p);
+                                if (m == 0) F = Uj[1 + d];
+                                else if (m <= D) F = (m - 1 == d) ? Uj[m] * u[d] + p : Uj[m] * u[d];
+                                else F = (Uj[D + 1] + p) * u[d];
+                                Ujm = Uj[m];
+                            }
+                            const double aU = alpha[d] * Ujm;
                             return sg == 0 ? 0.5 * (F + aU) : 0.5 * (F - aU);
                         };
                         const double fi = g(i);
                         double resC[D];
-                        weno_fit_qf<T, D>(qC, a, i, cnt, -1, 0, fi, g, resC);
+                        fit(qC, -1, 0, fi, g, resC);
                         double deriv = resC[d];
                         if (qS > 0) {
                             const double smoothC = smooth(resC);
@@ -2173,7 +2254,7 @@ __device__ __forceinline__ bool weno_sys_one(const StageArgs<T> &a, const int64_
                             s2 = s2 > 0.0 ? s2 : 1.0;
                             const double aC = smoothC / s2 + 1e-12;
                             double resS[D];
-                            weno_fit_qf<T, D>(qS, a, i, cnt, d, side, fi, g, resS);
+                            fit(qS, d, side, fi, g, resS);
                             const double smoothS = smooth(resS);
                             const double q = (smoothS / s2 + 1e-12) / aC;
                             const double wS = 1.0 / (1.0 + q * q);
@@ -2664,6 +2745,98 @@ __global__ void k_weno_geom(const WenoGeomArgs g) {
     }
 }
 
+// The FP64 path's counterpart of k_weno_geom: the same masked moment matrices (upper triangles, the same products
+// in the same order), factorised by chol_moment_fixed as weno_fit_f does at every stage, stored packed with their
+// flags; and the one-sided stencil sizes. weno_sys_one then sums only the right-hand sides.
+template <int D>
+__global__ void k_weno_geom64(const WenoGeomArgs g) {
+    constexpr int B1 = cbasis_count(D, 1), B2 = cbasis_count(D, 2), NS = 2 * D + 1;
+    constexpr int PK = B2 * (B2 + 1) / 2;
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    double *out = g.chol + i * int64_t(2 * NS * PK);
+    uint8_t *okf = g.ok + i * int64_t(2 * NS);
+    for (int q = 0; q < 2 * NS * PK; ++q) out[q] = 0.0;
+    for (int q = 0; q < 2 * NS; ++q) okf[q] = 0;
+    if (g.bnd[i]) return;
+    const int cnt = g.cnt[i];
+    const int64_t np = g.npad;
+    for (int st = 0; st < NS; ++st) {
+        const int dsel = st == 0 ? -1 : (st - 1) / 2, side = st == 0 ? 0 : 1 + (st - 1) % 2;
+        double N[B2 * B2];
+        for (int q = 0; q < B2 * B2; ++q) N[q] = 0.0;
+        int members = 0;
+        for (int k = 0; k < cnt; ++k) {
+            if (dsel >= 0) {
+                const double dd = g.dist[(int64_t(k) * D + dsel) * np + i];
+                if (!(side == 1 ? dd < 0.0 : dd >= 0.0)) continue;
+            }
+            ++members;
+            double x[D], p[B2];
+#pragma unroll
+            for (int d = 0; d < D; ++d) x[d] = g.dist[(int64_t(k) * D + d) * np + i] * g.invL64;
+            table_basis<D, 2, double>(x, p);
+            const double w = g.w[int64_t(k) * np + i];
+            for (int r = 0; r < B2; ++r)
+                for (int c = r; c < B2; ++c) N[r * B2 + c] = N[r * B2 + c] + w * (p[r] * p[c]);
+        }
+        if (st > 0) g.wcnt[i * (2 * D) + (st - 1)] = members;
+        {   // degree 1: the leading block (the degree-1 basis is the degree-2 basis's first B1 terms)
+            double N1[B1 * B1], U1[B1 * B1];
+            for (int r = 0; r < B1; ++r)
+                for (int c = 0; c < B1; ++c) N1[r * B1 + c] = N[r * B2 + c];
+            const bool ok = chol_moment_fixed<B1>(N1, U1);
+            okf[0 * NS + st] = ok;
+            double *o = out + (0 * NS + st) * PK;
+            for (int r = 0; r < B1; ++r)
+                for (int c = r; c < B1; ++c) o[packed_upper<B1>(r, c)] = U1[r * B1 + c];
+        }
+        {   // degree 2
+            double U2[B2 * B2];
+            const bool ok = chol_moment_fixed<B2>(N, U2);
+            okf[1 * NS + st] = ok;
+            double *o = out + (1 * NS + st) * PK;
+            for (int r = 0; r < B2; ++r)
+                for (int c = r; c < B2; ++c) o[packed_upper<B2>(r, c)] = U2[r * B2 + c];
+        }
+    }
+}
+
+// The FP64 flux table of one stage for weno_sys_one: per particle F_d(U)_m and lambda_d, each by the same
+// operations as the fits' field functions compute them.
+template <int D>
+__global__ void k_weno_prep64(const StageArgs<double> a) {
+    constexpr int M = D + 2, FW = D * (M + 1);
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= a.g.n) return;
+    const double gamma = double(a.ph.gamma), gm1 = double(a.ph.gm1);
+    double Uj[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) Uj[m] = double(a.U[j * M + m]);
+    const double rho = Uj[0];
+    const double inv_rho = 1.0 / rho;
+    double u[D], q2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        u[d] = Uj[1 + d] * inv_rho;
+        q2 = (d == 0) ? u[d] * u[d] : q2 + u[d] * u[d];
+    }
+    const double p = gm1 * (Uj[D + 1] - 0.5 * (rho * q2));
+    double *row = a.wflux64 + j * FW;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            double F;
+            if (m == 0) F = Uj[1 + d];
+            else if (m <= D) F = (m - 1 == d) ? Uj[m] * u[d] + p : Uj[m] * u[d];
+            else F = (Uj[D + 1] + p) * u[d];
+            row[d * (M + 1) + m] = F;
+        }
+        row[d * (M + 1) + M] = fabs(u[d]) + sqrt(gamma * p * inv_rho);
+    }
+}
+
 // The component-wise WENO of weno_sys_one for Euler in FP32 with the cached operators. Per axis d one pass over the
 // slots accumulates, with the central operator and the operator of the slot's side, the gradients of the
 // differences F_d(U_j)_m - F_d(U_i)_m and U_j,m - U_i,m and the largest lambda_d of the stencil (alpha_d); the split
@@ -2979,6 +3152,10 @@ struct StageInst {
                 return;
             }
         }
+        if constexpr (sizeof(T) == 8 && PDE == HCC_PDE_EULER && RDEG == 1) {
+            // the stage's flux table, once per stage state (the MOOD worklist passes reuse it)
+            if (a.full && a.wflux64) k_weno_prep64<D><<<grid(n, 256), 256, 0, s>>>(a);
+        }
         if constexpr (M == 1 && PDE == HCC_PDE_ADVECTION) {
             k_weno<T, D><<<pass_grid(a, n, fbs(a)), fbs(a), 0, s>>>(a);
         } else if constexpr (RDEG == 1) {       // systems (one instantiation: WENO has no reconstruction degree)
@@ -2995,8 +3172,11 @@ struct StageInst {
         }
     }
     static void weno_geom(const WenoGeomArgs &g, cudaStream_t s) {
-        if constexpr (sizeof(T) == 4 && PDE == HCC_PDE_EULER && RDEG == 1)
-            if (g.n > 0) k_weno_geom<D><<<unsigned((g.n + 127) / 128), 128, 0, s>>>(g);
+        if constexpr (PDE == HCC_PDE_EULER && RDEG == 1) {
+            if (g.n <= 0) return;
+            if constexpr (sizeof(T) == 4) k_weno_geom<D><<<unsigned((g.n + 127) / 128), 128, 0, s>>>(g);
+            else k_weno_geom64<D><<<unsigned((g.n + 127) / 128), 128, 0, s>>>(g);
+        }
     }
     static void central(const void *args, int64_t n, cudaStream_t s) {
         const StageArgs<T> &a = *static_cast<const StageArgs<T> *>(args);
@@ -3007,7 +3187,7 @@ struct StageInst {
                                    ((M == 1 && PDE == HCC_PDE_ADVECTION) || RDEG == 1) ? &weno : nullptr,
                                    RDEG == 1 ? &central : nullptr,
                                    (RDEG == 1 && M == 1 && PDE == HCC_PDE_ADVECTION) ? &upwind : nullptr,
-                                   (sizeof(T) == 4 && PDE == HCC_PDE_EULER && RDEG == 1) ? &weno_geom : nullptr};
+                                   (PDE == HCC_PDE_EULER && RDEG == 1) ? &weno_geom : nullptr};
         return &o;
     }
 };
