@@ -465,7 +465,7 @@ def roofline_of(workload, D, M, K, n_int, kt, peak, peak_kind, tiled=False):
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per point-stage (profiles/traffic.txt)"
                               " x interior points",
             "algorithmic_bytes_per_point_stage": {"flux": flux_b, "gather": gather_b},
-            "limiter": ("FP32 instruction issue, not HBM: 64 % issue-active, FMA pipe 46 %, DRAM traffic 1.1x the model "
+            "limiter": ("FP32 instruction issue, not HBM: 68 % issue-active, FMA pipe 47 %, DRAM traffic 1.1x the model "
                         "bytes (ncu, profiles/stage_f32_euler3d_blast_262k_tile.md)") if tiled else
                        ("issue / latency (ncu, profiles/stage_f32_euler2d_quadrant_1M.md)"),
             "flux_ms_per_launch": flux_ms, "gather_ms_per_launch": gather_ms,
