@@ -604,7 +604,8 @@ def run_profile_case(args):
         pred.loss_grad(X[:n], (rng.random(n) < 0.4).astype(np.uint8))
     steps = 3 if args.profile == "predictor" else args.profile_steps
     prec = args.profile_precision
-    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec))
+    scheme = hcc.WENO(2) if args.profile_scheme == "weno" else None
+    ctx = hcc.Context(make_cfg(hcc, cloud, h, prec, scheme=scheme))
     ctx.upload_cloud(cloud)
     ctx.build_neighbours()
     ctx.prepare_geometry()
@@ -1208,6 +1209,8 @@ def main():
                     help="comma-separated predictor thresholds (learned-only); 'plain' adds the FP32 arm without it")
     ap.add_argument("--host-driven", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of hcc_autotune's")
+    ap.add_argument("--profile-scheme", choices=["muscl", "weno"], default="muscl",
+                    help="scheme of the profile runs (--profile plain)")
     ap.add_argument("--no-tile-staging", action="store_true", help="stream-fed FP32 full passes (A/B)")
     ap.add_argument("--tile-staging", action="store_true",
                     help="tile-staged FP32 passes also where the default is stream-fed (2-D; A/B)")
